@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""H.Psi tree sweeps per second on one GB300 (QuTree ML-MCTDH hot path).
+
+Workload: the 64-mode tree (physical dim 32, bonds 32 at the bottom growing to
+64 below the top, 127 nodes, Psi 67 MB complex128) with the coupled-oscillator
+SOP of 64 kinetic, 64 quartic on-site and 256 random pair terms.  One step =
+one sweep = Derivative() (density matrices, regularised inverses, represent,
+mean fields, LayerDerivative at every node) plus Expectation.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours      : the library's grouped complex128 plan; `value` with Psi resident in
+            HBM; `e2e` through the C ABI with pinned host buffers (upload Psi,
+            sweep, download dPsi and the energy every step).
+reference : the reference algorithm (CPU restatement, zgemm through OpenBLAS on
+            all host cores), one sweep per step.
+Multi-GPU (torchrun): one independent replica per rank ("replicas only").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "H·Ψ tree sweeps/sec: batched+mixed vs plain complex128 on 1 GB300 at |ΔE|≤1e-8"
+WORKLOAD = "cfg1: 64-mode balanced binary tree, p=32, bonds 32..64, 384-term coupled-oscillator SOP"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, v):
+    if ws <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    rows.append((float(parts[1]), float(parts[2]), parts[5:9], float(parts[3])))
+                except ValueError:
+                    continue
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows), "power_w_max": max(r[3] for r in rows)}
+
+
+def cpu_baseline_sweep(tree, sop, psi, budget_s=45.0):
+    """The reference algorithm on the host cores: the oracle restatement with
+    QuTree's TensorBLAS path (zgemm from OpenBLAS, all cores).  One full sweep
+    is the sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    blas = oracle.attach_openblas(fast=True)
+    flat = psi.flat()
+    t0 = time.perf_counter()
+    r = oracle.derivative(tree, sop, flat, backend=oracle.BLAS, fast=True, want_mats=False)
+    dt = time.perf_counter() - t0
+    return dt, r.energy, blas
+
+
+def run_reference(args, ws, rank):
+    from qutree_gb300.model import config_problem
+    if rank != 0:
+        return
+    tree, sop, psi = config_problem(args.config)
+    cores = os.cpu_count()
+    times, energy, blas = [], None, None
+    warm = min(args.warmup, 1)
+    for i in range(warm + args.steps):
+        dt, energy, blas = cpu_baseline_sweep(tree, sop, psi)
+        if i >= warm:
+            times.append(dt)
+    tot = sum(times)
+    v = len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "sweeps/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": warm, "ms_per_step": 1e3 * tot / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "threads": cores, "blas": blas or "naive loops"},
+        "energy": energy,
+        "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                         "sample": "one full cfg1 sweep per step (reference call sequence, "
+                                   "zgemm via OpenBLAS)"},
+        "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    if args.warmup > warm:
+        line["note"] = f"warm-up capped at {warm} CPU sweep(s) to keep the run within minutes"
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+
+    from qutree_gb300 import qtgpu
+    from qutree_gb300.model import config_problem
+
+    torch.cuda.set_device(local)
+    tree, sop, psi = config_problem(args.config)
+    flat = psi.flat()
+    nbytes = flat.nbytes
+
+    def timed_sweeps(flavour, steps, warmup):
+        hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, device=local)
+        stream = torch.cuda.ExternalStream(hrep.stream())
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+        hrep.upload(flat)
+        for _ in range(warmup):
+            hrep.derivative()
+        hrep.sync()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        barrier(ws)
+        torch.cuda.synchronize()
+        n0 = hrep.ctx.launch_count()
+        with Clocks(local) as clk:
+            for i in range(steps):
+                with torch.cuda.stream(stream):
+                    flush.fill_(i & 0xFF)  # L2 (129 MB) flushed between sweeps, not timed
+                ev[i][0].record(stream)
+                hrep.derivative()
+                ev[i][1].record(stream)
+            hrep.sync()
+            torch.cuda.synchronize()
+        launches = hrep.ctx.launch_count() - n0
+        barrier(ws)
+        times = [a.elapsed_time(b) for a, b in ev]
+        return hrep, times, clk.summary(), launches
+
+    # grouped plan: the headline
+    hrep, times, clocks, launches = timed_sweeps(qtgpu.QT_PLAN_GROUPED, args.steps, args.warmup)
+    tot_ms = max_over_ranks(ws, sum(times))
+    energy = hrep.energy()
+    stats = hrep.stats()
+    value = ws * args.steps / (tot_ms * 1e-3)
+
+    # roofline: every stage launched alone, bracketed by events on the library stream
+    stream = torch.cuda.ExternalStream(hrep.stream())
+    stages = hrep.stages()
+    per_kind = {}
+    reps = 2
+    for _ in range(reps):
+        evs = []
+        for i in range(len(stages)):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            hrep.launch_stage(i)
+            b.record(stream)
+            evs.append((a, b))
+        hrep.sync()
+        for i, (a, b) in enumerate(evs):
+            k = stages[i][0]
+            d = per_kind.setdefault(k, {"ms": 0.0, "flops": 0.0, "bytes": 0.0, "launches": 0})
+            d["ms"] += a.elapsed_time(b) / reps
+            d["flops"] += stages[i][2] / reps
+            d["bytes"] += stages[i][3] / reps
+            d["launches"] += 1 / reps
+    fp64_peak = hrep.ctx.fp64_peak()
+    names = {0: "k_mp (mode products)", 1: "k_hp (hole products)", 2: "k_acc (last-mode accumulate)",
+             3: "k_lin (mean-field sums)", 4: "k_eig (density inverses)", 5: "k_proj (projectors)"}
+    dom = max(per_kind, key=lambda k: per_kind[k]["ms"])
+    d = per_kind[dom]
+    achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+    total_stage_ms = sum(v["ms"] for v in per_kind.values())
+    kernels = {names[k]: {"ms": round(v["ms"], 3), "share": round(v["ms"] / total_stage_ms, 4),
+                          "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4),
+                          "launches_per_sweep": int(round(v["launches"]))}
+               for k, v in sorted(per_kind.items())}
+    hrep.close()
+
+    # plain (reference call sequence) complex128 plan for comparison
+    plain_steps = max(2, min(args.steps, 4))
+    hp, ptimes, _, _ = timed_sweeps(qtgpu.QT_PLAN_REFERENCE, plain_steps, 1)
+    plain_value = plain_steps / (sum(ptimes) * 1e-3)
+    plain_energy = hp.energy()
+    hp.close()
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_GROUPED, device=local)
+        pin_in = torch.empty(flat.size * 2, dtype=torch.float64, pin_memory=True)
+        pin_out = torch.empty(flat.size * 2, dtype=torch.float64, pin_memory=True)
+        pin_in.numpy()[:] = flat.view(np.float64)
+        in_np = pin_in.numpy().view(np.complex128)
+        out_np = pin_out.numpy().view(np.complex128)
+        for _ in range(max(1, args.warmup)):
+            h.upload(in_np)
+            h.derivative()
+            h.dpsi_into(out_np)
+            h.energy()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            h.upload(in_np)
+            h.derivative()
+            h.dpsi_into(out_np)
+            h.energy()
+        t1 = time.perf_counter()
+        e2e_s = max_over_ranks(ws, t1 - t0)
+        e2e = {"value": ws * args.steps / e2e_s, "unit": "sweeps/s", "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes + 32}
+        h.close()
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded N(0,1) node tensors, QR-orthonormalised)",
+        "config": {"workload": WORKLOAD, "plan": "grouped complex128", "parallelism": f"replicas x{ws}",
+                   "l2": "flushed between timed sweeps (256 MB fill, outside the events)"},
+        "energy": energy,
+        "plain_complex128": {"value": plain_value, "unit": "sweeps/s", "steps": plain_steps,
+                             "energy": plain_energy, "plan": "reference call sequence"},
+        "flops_per_sweep": {"reference_algorithm": stats["ref_flops"], "executed": stats["exec_flops"]},
+        "roofline": {"bound": "fp64", "kernel": names[dom], "achieved": achieved,
+                     "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                     "peak_source": "FP64 FMA-loop probe measured in this run (qt_probe_fp64_peak); "
+                                    "MEASURED_PEAKS.json lists HBM copy and bf16 GEMM only",
+                     "traffic": None, "kernels": kernels},
+        "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_cpu_baseline and args.config == 1:
+        dt, cpu_e, blas = cpu_baseline_sweep(tree, sop, psi)
+        line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count(),
+                                "kind": "port",
+                                "sample": "one full cfg1 sweep, reference call sequence, zgemm via "
+                                          f"{'OpenBLAS' if blas else 'naive loops'}",
+                                "energy_diff": abs(cpu_e - energy)}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+    else:
+        run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,193 @@
+/*
+ * qtgpu.h -- C ABI of the GB300 tree-tensor-network H.Psi sweep library
+ * (libqtgpu.so).
+ *
+ * The library replaces, on one GPU, the hot path of QuTree's ML-MCTDH
+ * derivative: the mode-k products, hole / dot-product contractions, the
+ * bottom-up SparseMatrixTree represent sweep, the top-down mean-field sweep,
+ * the density-matrix tree with its regularised inverse, and the per-node
+ * sum-of-products H.Psi application (Apply / LayerDerivative / Derivative).
+ *
+ * Conventions (identical to QuTree's):
+ *  - complex numbers are interleaved (re, im) doubles;
+ *  - a node tensor of shape (d_0, ..., d_{k-1}, d_up) is column-major, the
+ *    first index fastest (include/Core/Tensor_Implementation.h:154-165 of the
+ *    reference); matrices are column-major, M(i,j) = m[i + j*dim1];
+ *  - nodes are numbered in QuTree's bottom-up address order
+ *    (src/TreeShape/Tree.cpp:92-114): children before parents, the top last;
+ *  - "packed" wavefunction layout: node tensors back to back in address
+ *    order, no padding.
+ *
+ * Every call returns a status (QT_OK on success).  The library never exits
+ * the process; qt_last_error() describes the last failure of a context.
+ * Calls on one context are ordered on that context's CUDA stream; a context
+ * must not be used from two host threads at once.
+ */
+#ifndef QTGPU_H
+#define QTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QT_OK 0
+#define QT_ERR_ARG 1     /* null pointer, bad enum, call out of order        */
+#define QT_ERR_SHAPE 2   /* inconsistent tree / operator / tensor geometry   */
+#define QT_ERR_ALLOC 3   /* device or host allocation failed                 */
+#define QT_ERR_CUDA 4    /* a CUDA runtime call failed                       */
+#define QT_ERR_STATE 5   /* call needs an earlier step (upload, prepare, ...) */
+#define QT_ERR_NUMERIC 6 /* non-finite input or result                       */
+
+/* Leaf operator kinds of the operator table. */
+#define QT_OP_DENSE 0 /* p x p complex matrix, column-major                  */
+#define QT_OP_DIAG 1  /* p complex numbers (operator diagonal in the DVR)    */
+
+/* Plan flavours for qt_prepare. */
+#define QT_PLAN_REFERENCE 0 /* one represent / mean-field / apply chain per SOP
+                               term and node, the reference's call sequence   */
+#define QT_PLAN_GROUPED 1   /* terms with identical restrictions share their
+                               matrices and chains; Apply sums the mean fields
+                               of terms with the same inside part first       */
+
+/* Matrix sets for qt_matrices_download. */
+#define QT_MAT_RHO 0     /* density matrices, per node, d_up x d_up          */
+#define QT_MAT_RHOINV 1  /* regularised inverse density matrices             */
+#define QT_MAT_HMAT 2    /* represent matrices, sparse layout                */
+#define QT_MAT_HCON 3    /* mean-field (hole) matrices, sparse layout         */
+
+typedef struct qt_ctx qt_ctx;
+
+/* ---- context -------------------------------------------------------------
+ * One context = one CUDA device, one stream, and the device arena of one
+ * tree, one SOP operator and one wavefunction.  Replaces the reference's
+ * per-call allocations and WorkMemory scratch
+ * (include/TreeClasses/WorkMemory.h:9-60). */
+int qt_ctx_create(qt_ctx** ctx, int device);
+void qt_ctx_destroy(qt_ctx* ctx);
+const char* qt_last_error(const qt_ctx* ctx);
+int qt_sync(qt_ctx* ctx);
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work with the library's. */
+int qt_get_stream(qt_ctx* ctx, void** stream);
+
+/* ---- inputs --------------------------------------------------------------
+ * Tree topology (replaces Tree / Node / TensorShape,
+ * include/TreeShape/Tree.h, include/Core/TensorShape.h:5-67).
+ *   order[n]     number of indices of node n (children + 1; 2 for bottom)
+ *   dims[]       the node shapes back to back, last index = d_up
+ *   parent[n]    parent address, -1 for the top
+ *   child_idx[n] position of n among its parent's children (-1 for top)
+ *   leaf_mode[n] physical mode of a bottom node, -1 for upper nodes */
+int qt_tree_upload(qt_ctx* ctx, int n_nodes, const int* order, const int* dims,
+                   const int* parent, const int* child_idx, const int* leaf_mode);
+
+/* SOP operator (replaces SOPcd / MLOcd / LeafMatrix / LeafFunction,
+ * include/TreeOperators/SumOfProductsOperator.h:5-135,
+ * include/TreeOperators/MultiLeafOperator.h:11-196).
+ *   op_kind/op_dim/op_off  leaf operator table; op_off in complex elements
+ *                          into op_data
+ *   coeff[2*n_terms]       complex coefficient of each term
+ *   term_ptr[n_terms+1]    CSR pointer into term_mode / term_op
+ *   term_mode, term_op     factor (leaf mode, operator) list of each term;
+ *                          factors on the same leaf are applied in list
+ *                          order (MultiLeafOperator::apply,
+ *                          src/TreeOperators/MultiLeafOperator.cpp:11-37) */
+int qt_sop_upload(qt_ctx* ctx, int n_ops, const int* op_kind, const int* op_dim,
+                  const int64_t* op_off, const double* op_data, int n_terms,
+                  const double* coeff, const int* term_ptr, const int* term_mode,
+                  const int* term_op);
+
+/* Regularisation epsilon of the inverse density matrices,
+ * lambda -> 1/(lambda + eps*exp(-lambda/eps)); default 1e-10 as
+ * HamiltonianRepresentation::build uses
+ * (include/TreeClasses/HamiltonianRepresentation.h:72). */
+int qt_set_regularization(qt_ctx* ctx, double eps);
+
+/* Builds the sweep plan, allocates the device arena and captures the sweep
+ * as a CUDA graph.  Needs tree and SOP.  No allocation happens afterwards. */
+int qt_prepare(qt_ctx* ctx, int plan_flavour);
+
+/* Wavefunction, packed layout (TensorTree<cd>,
+ * include/TreeClasses/TensorTree.h:17-132). */
+int qt_psi_upload(qt_ctx* ctx, const double* psi_host);
+int qt_psi_upload_device(qt_ctx* ctx, const void* psi_dev);
+int qt_psi_download(qt_ctx* ctx, double* psi_host);
+int64_t qt_psi_size(const qt_ctx* ctx); /* complex elements, packed */
+
+/* ---- sweep ---------------------------------------------------------------
+ * One H.Psi sweep = Derivative(dPsi, hRep, t, Psi, H, tree, phase)
+ * (src/TreeClasses/HamiltonianRepresentation.cpp:74-81): build (density
+ * matrices, regularised inverses, represent, mean fields), LayerDerivative at
+ * every node, and Expectation at the top
+ * (src/TreeClasses/HamiltonianRepresentation.cpp:45-51).  Asynchronous on
+ * the context stream. */
+int qt_derivative(qt_ctx* ctx, double phase_re, double phase_im);
+int qt_dpsi_download(qt_ctx* ctx, double* dpsi_host);
+int qt_dpsi_device(qt_ctx* ctx, const void** dpsi_dev);
+/* out[4] = { Re h00, Im h00, Re S00, Im S00 }, h00 = <Phi_top|H Phi_top>,
+ * S00 = <Phi_top|Phi_top>; E = Re h00 / Re S00. Synchronises. */
+int qt_energy(qt_ctx* ctx, double* out4);
+
+/* Matrices of the last sweep.  Sparse layout (QT_MAT_HMAT / QT_MAT_HCON):
+ * for each term, for each node on its leaf-to-root paths (SparseTree with
+ * tail, src/TreeClasses/SparseTree.cpp:33-89) in address order, a d_up x d_up
+ * matrix.  Dense layout (QT_MAT_RHO / QT_MAT_RHOINV): per node in address
+ * order.  The top node's represent matrix is zero, as in the reference. */
+int64_t qt_matrices_size(const qt_ctx* ctx, int which);
+int qt_matrices_download(qt_ctx* ctx, int which, double* host);
+
+/* Plan statistics: out[0] reference-algorithm flops per sweep, out[1]
+ * executed flops per sweep, out[2] kernel launches per sweep, out[3] device
+ * arena bytes, out[4] scratch bytes, out[5] represent chains, out[6]
+ * mean-field chains, out[7] apply chains. */
+int qt_plan_stats(const qt_ctx* ctx, double* out8);
+
+/* ---- profiling ------------------------------------------------------------
+ * The prepared sweep is a fixed sequence of batched kernel launches
+ * ("stages").  These calls expose it for per-kernel timing: a caller can
+ * launch stage i alone on the context stream (outside the graph, with the
+ * same arguments the graph uses) and bracket it with its own CUDA events.
+ * kind: 0 mode products, 1 hole products, 2 last-mode accumulations,
+ * 3 mean-field sums, 4 density inverses, 5 projectors. */
+int qt_stage_count(const qt_ctx* ctx);
+int qt_stage_info(const qt_ctx* ctx, int stage, int* kind, int64_t* tiles, double* flops,
+                  double* bytes);
+int qt_stage_launch(qt_ctx* ctx, int stage);
+/* Peak FP64 FMA throughput of the device (TFLOP/s), measured with a dependent-
+ * free FMA loop of the library's own; the roofline denominator of the
+ * complex128 kernels. */
+int qt_probe_fp64_peak(qt_ctx* ctx, double* tflops);
+
+/* ---- primitives on device pointers ---------------------------------------
+ * Mode-k product, the reference's matvec_ / matrixTensor
+ * (include/Core/Tensor_Implementation.h:450-461,553-577; src/Core/LA_lib.f:34-81):
+ *   C[b, a', c] (+)= sum_a h(a', a) B[b, a, c],
+ *   h is activeC x activeB, column-major; add != 0 accumulates. */
+int qt_mode_product(qt_ctx* ctx, void* C, const void* h, const void* B, int64_t before,
+                    int64_t activeB, int64_t activeC, int64_t after, int add);
+/* Hole product, the reference's rhomat_ / contraction
+ * (include/Core/Tensor_Implementation.h:481-531; src/Core/LA_lib.f:718-762):
+ *   S(a, a') = sum_{b,c} conj(A[b, a, c]) B[b, a', c]. */
+int qt_hole_product(qt_ctx* ctx, void* S, const void* A, const void* B, int64_t before,
+                    int64_t activeA, int64_t activeB, int64_t after);
+/* Last-mode product multStateAB (include/Core/Tensor_Implementation.h:732-760):
+ *   C[i, m] (+)= sum_n A(m, n) B[i, n], B is (lastBefore x active). */
+int qt_last_mode_product(qt_ctx* ctx, void* C, const void* A, const void* B,
+                         int64_t last_before, int64_t active, int add);
+
+/* Device memory helpers for callers without their own allocator. */
+int qt_dev_alloc(qt_ctx* ctx, int64_t bytes, void** ptr);
+int qt_dev_free(qt_ctx* ctx, void* ptr);
+int qt_memcpy_h2d(qt_ctx* ctx, void* dst, const void* src, int64_t bytes);
+int qt_memcpy_d2h(qt_ctx* ctx, void* dst, const void* src, int64_t bytes);
+
+/* Number of the library's own kernel launches enqueued since the context was
+ * created (graph launches count their kernels). */
+int64_t qt_launch_count(const qt_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QTGPU_H */

@@ -1,0 +1,670 @@
+// qt_api.cu -- the extern "C" entry points of libqtgpu (include/qtgpu.h).
+//
+// A context owns one CUDA stream and one device arena: the wavefunction, its
+// H.Psi and derivative (packed TensorTree layout), all d x d matrices of the
+// sweep (density, inverse density, represent, mean-field, grouped mean-field
+// and projector matrices), the leaf operator table, the chain scratch and the
+// task tables of the plan.  qt_prepare allocates all of it once and captures
+// the whole sweep as one CUDA graph; qt_derivative only launches that graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/qtgpu.h"
+#include "qt_internal.h"
+
+using qt::Plan;
+using qt::Ref;
+
+struct qt_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  bool have_tree = false, have_sop = false, prepared = false, have_psi = false, swept = false;
+  std::vector<qt::NodeGeo> nodes;
+  qt::OpTable ops;
+  qt::SopDesc sop;
+  double eps = 1e-10;
+  Plan plan;
+  double2* buf[qt::B_NBUF] = {nullptr};
+  int64_t buf_elems[qt::B_NBUF] = {0};
+  void* tables_mem = nullptr;
+  qt::DevTables tables;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches = 0;
+};
+
+namespace {
+
+thread_local std::string g_noctx_err;
+
+int fail(qt_ctx* c, int code, const std::string& msg) {
+  if (c)
+    c->err = msg;
+  else
+    g_noctx_err = msg;
+  return code;
+}
+
+int cuda_fail(qt_ctx* c, cudaError_t e, const char* where) {
+  return fail(c, QT_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define QT_CUDA(c, call)                                  \
+  do {                                                    \
+    cudaError_t e_ = (call);                              \
+    if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+  } while (0)
+
+void release_arena(qt_ctx* c) {
+  if (c->exec) cudaGraphExecDestroy(c->exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->exec = nullptr;
+  c->graph = nullptr;
+  for (int i = 0; i < qt::B_NBUF; ++i) {
+    if (c->buf[i]) cudaFree(c->buf[i]);
+    c->buf[i] = nullptr;
+    c->buf_elems[i] = 0;
+  }
+  if (c->tables_mem) cudaFree(c->tables_mem);
+  c->tables_mem = nullptr;
+  c->tables = qt::DevTables();
+  c->prepared = false;
+  c->have_psi = false;
+  c->swept = false;
+}
+
+const double2* ptr_of(const qt_ctx* c, const Ref& r) {
+  if (r.buf < 0) return nullptr;
+  return c->buf[r.buf] + r.off;
+}
+double2* mptr_of(const qt_ctx* c, const Ref& r) {
+  if (r.buf < 0) return nullptr;
+  return c->buf[r.buf] + r.off;
+}
+
+template <typename T>
+void put(std::vector<char>& blob, std::vector<int64_t>& offs, const std::vector<T>& v) {
+  size_t o = (blob.size() + 255) / 256 * 256;
+  blob.resize(o + v.size() * sizeof(T));
+  if (!v.empty()) std::memcpy(blob.data() + o, v.data(), v.size() * sizeof(T));
+  offs.push_back((int64_t)o);
+}
+
+bool finite_all(const double* p, int64_t n) {
+  for (int64_t i = 0; i < n; ++i)
+    if (!std::isfinite(p[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+int qt_ctx_create(qt_ctx** out, int device) {
+  if (!out) return fail(nullptr, QT_ERR_ARG, "qt_ctx_create: null output pointer");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return fail(nullptr, QT_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+  if (device < 0 || device >= n) return fail(nullptr, QT_ERR_ARG, "qt_ctx_create: no such device");
+  qt_ctx* c = new (std::nothrow) qt_ctx();
+  if (!c) return fail(nullptr, QT_ERR_ALLOC, "qt_ctx_create: out of host memory");
+  c->device = device;
+  e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete c;
+    return fail(nullptr, QT_ERR_CUDA, std::string("qt_ctx_create: ") + cudaGetErrorString(e));
+  }
+  *out = c;
+  return QT_OK;
+}
+
+void qt_ctx_destroy(qt_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  release_arena(c);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* qt_last_error(const qt_ctx* c) { return c ? c->err.c_str() : g_noctx_err.c_str(); }
+
+int qt_sync(qt_ctx* c) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+int qt_get_stream(qt_ctx* c, void** s) {
+  if (!c || !s) return fail(c, QT_ERR_ARG, "null argument");
+  *s = (void*)c->stream;
+  return QT_OK;
+}
+
+int qt_tree_upload(qt_ctx* c, int n_nodes, const int* order, const int* dims, const int* parent,
+                   const int* child_idx, const int* leaf_mode) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (n_nodes <= 0 || !order || !dims || !parent || !child_idx || !leaf_mode)
+    return fail(c, QT_ERR_ARG, "qt_tree_upload: null or empty descriptor");
+  release_arena(c);
+  std::vector<qt::NodeGeo> nodes(n_nodes);
+  int p = 0;
+  for (int i = 0; i < n_nodes; ++i) {
+    if (order[i] < 2 || order[i] > 8) return fail(c, QT_ERR_SHAPE, "qt_tree_upload: node order must be 2..8");
+    for (int k = 0; k < order[i]; ++k) nodes[i].shape.push_back(dims[p + k]);
+    p += order[i];
+    nodes[i].parent = parent[i];
+    nodes[i].child_idx = child_idx[i];
+    nodes[i].leaf_mode = leaf_mode[i];
+    if (parent[i] >= n_nodes || (parent[i] >= 0 && child_idx[i] < 0))
+      return fail(c, QT_ERR_SHAPE, "qt_tree_upload: bad parent / child index");
+  }
+  c->nodes = nodes;
+  c->have_tree = true;
+  return QT_OK;
+}
+
+int qt_sop_upload(qt_ctx* c, int n_ops, const int* op_kind, const int* op_dim, const int64_t* op_off,
+                  const double* op_data, int n_terms, const double* coeff, const int* term_ptr,
+                  const int* term_mode, const int* term_op) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (n_ops <= 0 || n_terms <= 0 || !op_kind || !op_dim || !op_off || !op_data || !coeff ||
+      !term_ptr || !term_mode || !term_op)
+    return fail(c, QT_ERR_ARG, "qt_sop_upload: null or empty descriptor");
+  release_arena(c);
+  qt::OpTable ops;
+  int64_t total = 0;
+  for (int i = 0; i < n_ops; ++i) {
+    if (op_kind[i] != QT_OP_DENSE && op_kind[i] != QT_OP_DIAG)
+      return fail(c, QT_ERR_ARG, "qt_sop_upload: unknown operator kind");
+    if (op_dim[i] <= 0 || op_off[i] < 0) return fail(c, QT_ERR_SHAPE, "qt_sop_upload: bad operator dim/offset");
+    int64_t n = op_kind[i] == QT_OP_DENSE ? (int64_t)op_dim[i] * op_dim[i] : op_dim[i];
+    total = std::max(total, op_off[i] + n);
+  }
+  // repack each operator contiguously (16-element aligned) in the device table
+  int64_t cur = 0;
+  for (int i = 0; i < n_ops; ++i) {
+    int64_t n = op_kind[i] == QT_OP_DENSE ? (int64_t)op_dim[i] * op_dim[i] : op_dim[i];
+    ops.kind.push_back(op_kind[i]);
+    ops.dim.push_back(op_dim[i]);
+    ops.off.push_back(cur);
+    ops.data.resize(2 * (cur + n), 0.0);
+    std::memcpy(ops.data.data() + 2 * cur, op_data + 2 * op_off[i], sizeof(double) * 2 * n);
+    cur = (cur + n + 15) / 16 * 16;
+  }
+  ops.data.resize(2 * std::max<int64_t>(cur, 16), 0.0);
+  if (!finite_all(ops.data.data(), (int64_t)ops.data.size()))
+    return fail(c, QT_ERR_NUMERIC, "qt_sop_upload: non-finite operator entry");
+  qt::SopDesc s;
+  s.n_terms = n_terms;
+  for (int l = 0; l < n_terms; ++l) {
+    if (!std::isfinite(coeff[2 * l]) || !std::isfinite(coeff[2 * l + 1]))
+      return fail(c, QT_ERR_NUMERIC, "qt_sop_upload: non-finite coefficient");
+    s.coeff.push_back(make_double2(coeff[2 * l], coeff[2 * l + 1]));
+  }
+  s.ptr.assign(term_ptr, term_ptr + n_terms + 1);
+  if (s.ptr[0] != 0) return fail(c, QT_ERR_ARG, "qt_sop_upload: term_ptr[0] must be 0");
+  for (int l = 0; l < n_terms; ++l)
+    if (s.ptr[l + 1] < s.ptr[l]) return fail(c, QT_ERR_ARG, "qt_sop_upload: term_ptr not monotone");
+  s.mode.assign(term_mode, term_mode + s.ptr[n_terms]);
+  s.op.assign(term_op, term_op + s.ptr[n_terms]);
+  c->ops = ops;
+  c->sop = s;
+  c->have_sop = true;
+  return QT_OK;
+}
+
+int qt_set_regularization(qt_ctx* c, double eps) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!(eps > 0) || !std::isfinite(eps)) return fail(c, QT_ERR_ARG, "eps must be positive and finite");
+  if (c->prepared) return fail(c, QT_ERR_STATE, "set the regularisation before qt_prepare");
+  c->eps = eps;
+  return QT_OK;
+}
+
+int qt_prepare(qt_ctx* c, int flavour) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->have_tree || !c->have_sop) return fail(c, QT_ERR_STATE, "qt_prepare needs tree and SOP");
+  if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED)
+    return fail(c, QT_ERR_ARG, "unknown plan flavour");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  release_arena(c);
+  int64_t budget = (int64_t)1 << 28;  // scratch elements (4 GiB)
+  if (const char* s = std::getenv("QT_SCRATCH_MIB")) {
+    long v = std::atol(s);
+    if (v > 0) budget = (int64_t)v * (1 << 20) / 16;
+  }
+  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour, budget);
+  if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
+  Plan& P = c->plan;
+  c->buf_elems[qt::B_PSI] = P.psi_arena;
+  c->buf_elems[qt::B_HPHI] = P.psi_arena;
+  c->buf_elems[qt::B_DPSI] = P.psi_arena;
+  c->buf_elems[qt::B_MATS] = P.mats_size;
+  c->buf_elems[qt::B_OPS] = (int64_t)c->ops.data.size() / 2;
+  c->buf_elems[qt::B_SCR] = std::max<int64_t>(P.scratch_size, 16);
+  c->buf_elems[qt::B_PARAM] = 16;
+  int64_t arena = 0;
+  for (int i = 0; i < qt::B_NBUF; ++i) {
+    int64_t n = std::max<int64_t>(c->buf_elems[i], 16);
+    cudaError_t e = cudaMalloc((void**)&c->buf[i], n * sizeof(double2));
+    if (e != cudaSuccess) {
+      release_arena(c);
+      return fail(c, QT_ERR_ALLOC, std::string("qt_prepare: device allocation failed: ") + cudaGetErrorString(e));
+    }
+    arena += n * 16;
+  }
+  QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_MATS], 0, c->buf_elems[qt::B_MATS] * 16, c->stream));
+  QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_HPHI], 0, c->buf_elems[qt::B_HPHI] * 16, c->stream));
+  QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_DPSI], 0, c->buf_elems[qt::B_DPSI] * 16, c->stream));
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_OPS], c->ops.data.data(), c->ops.data.size() * sizeof(double),
+                             cudaMemcpyHostToDevice, c->stream));
+  // bind the symbolic tables to device pointers
+  std::vector<qt::MPTask> mp;
+  for (auto& s : P.mp) {
+    qt::MPTask t;
+    t.in = ptr_of(c, s.in);
+    t.out = mptr_of(c, s.out);
+    t.h = ptr_of(c, s.h);
+    t.alpha = s.alpha;
+    t.before = s.before;
+    t.a_in = s.a_in;
+    t.a_out = s.a_out;
+    t.after = s.after;
+    t.diag = s.diag;
+    t.add = 0;
+    mp.push_back(t);
+  }
+  std::vector<qt::HPTask> hp;
+  for (auto& s : P.hp) {
+    qt::HPTask t;
+    t.A = ptr_of(c, s.A);
+    t.B = ptr_of(c, s.B);
+    t.S = mptr_of(c, s.S);
+    t.before = s.before;
+    t.a = s.a;
+    t.after = s.after;
+    t.aB = 0;
+    hp.push_back(t);
+  }
+  std::vector<qt::AccTask> acc;
+  for (auto& s : P.acc) {
+    qt::AccTask t;
+    t.out = mptr_of(c, s.out);
+    t.alpha_ptr = s.alpha_param ? c->buf[qt::B_PARAM] : nullptr;
+    t.alpha = s.alpha;
+    t.rows = s.rows;
+    t.d = s.d;
+    t.first = s.first;
+    t.count = s.count;
+    t.add = s.add;
+    t.pad = 0;
+    acc.push_back(t);
+  }
+  std::vector<qt::AccTerm> acc_terms;
+  for (auto& s : P.acc_terms) acc_terms.push_back(qt::AccTerm{ptr_of(c, s.H), ptr_of(c, s.X)});
+  std::vector<qt::LinTask> lin;
+  for (auto& s : P.lin) {
+    qt::LinTask t;
+    t.out = mptr_of(c, s.out);
+    t.d = s.d;
+    t.first = s.first;
+    t.count = s.count;
+    t.pad = 0;
+    lin.push_back(t);
+  }
+  std::vector<qt::LinTerm> lin_terms;
+  for (auto& s : P.lin_terms) lin_terms.push_back(qt::LinTerm{s.c, ptr_of(c, s.M)});
+  std::vector<qt::EigTask> eig;
+  for (auto& s : P.eig) {
+    qt::EigTask t;
+    t.rho = ptr_of(c, s.rho);
+    t.rhoinv = mptr_of(c, s.rhoinv);
+    t.U = mptr_of(c, s.U);
+    t.d = s.d;
+    t.pad = 0;
+    eig.push_back(t);
+  }
+  std::vector<qt::ProjTask> proj;
+  for (auto& s : P.proj) {
+    qt::ProjTask t;
+    t.S = mptr_of(c, s.S);
+    t.D = ptr_of(c, s.D);
+    t.rhoinv = ptr_of(c, s.rhoinv);
+    t.Sinv = mptr_of(c, s.Sinv);
+    t.P = mptr_of(c, s.P);
+    t.M2 = mptr_of(c, s.M2);
+    t.d = s.d;
+    t.pad = 0;
+    proj.push_back(t);
+  }
+  std::vector<char> blob;
+  std::vector<int64_t> offs;
+  put(blob, offs, mp);
+  put(blob, offs, hp);
+  put(blob, offs, acc);
+  put(blob, offs, acc_terms);
+  put(blob, offs, lin);
+  put(blob, offs, lin_terms);
+  put(blob, offs, eig);
+  put(blob, offs, proj);
+  put(blob, offs, P.mp_tiles);
+  put(blob, offs, P.hp_tiles);
+  put(blob, offs, P.acc_tiles);
+  {
+    cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
+    if (e != cudaSuccess) {
+      release_arena(c);
+      return fail(c, QT_ERR_ALLOC, std::string("qt_prepare: task table allocation failed: ") + cudaGetErrorString(e));
+    }
+    arena += (int64_t)blob.size();
+  }
+  QT_CUDA(c, cudaMemcpyAsync(c->tables_mem, blob.data(), blob.size(), cudaMemcpyHostToDevice, c->stream));
+  char* base = (char*)c->tables_mem;
+  c->tables.mp = (qt::MPTask*)(base + offs[0]);
+  c->tables.hp = (qt::HPTask*)(base + offs[1]);
+  c->tables.acc = (qt::AccTask*)(base + offs[2]);
+  c->tables.acc_terms = (qt::AccTerm*)(base + offs[3]);
+  c->tables.lin = (qt::LinTask*)(base + offs[4]);
+  c->tables.lin_terms = (qt::LinTerm*)(base + offs[5]);
+  c->tables.eig = (qt::EigTask*)(base + offs[6]);
+  c->tables.proj = (qt::ProjTask*)(base + offs[7]);
+  c->tables.mp_tiles = (int2*)(base + offs[8]);
+  c->tables.hp_tiles = (int4*)(base + offs[9]);
+  c->tables.acc_tiles = (int4*)(base + offs[10]);
+  for (auto& id : P.identities) {
+    cudaError_t e = qt::launch_set_identity(c->buf[qt::B_MATS] + id.first, id.second, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "set identity");
+    c->launches += 1;
+  }
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  // capture the sweep
+  QT_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  for (const auto& st : P.stages) {
+    cudaError_t e = qt::launch_stage(st, c->tables, c->eps, P.max_eig_d, c->stream);
+    if (e != cudaSuccess) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(c->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      release_arena(c);
+      return cuda_fail(c, e, (std::string("capture stage ") + st.name).c_str());
+    }
+  }
+  QT_CUDA(c, cudaStreamEndCapture(c->stream, &c->graph));
+  QT_CUDA(c, cudaGraphInstantiate(&c->exec, c->graph, 0));
+  P.stats.arena_bytes = arena;
+  P.stats.scratch_bytes = c->buf_elems[qt::B_SCR] * 16;
+  c->prepared = true;
+  return QT_OK;
+}
+
+int64_t qt_psi_size(const qt_ctx* c) { return (c && c->prepared) ? c->plan.psi_packed : -1; }
+
+int qt_psi_upload(qt_ctx* c, const double* psi) {
+  if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_upload before qt_prepare");
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI], psi, c->plan.psi_packed * 16, cudaMemcpyHostToDevice,
+                             c->stream));
+  c->have_psi = true;
+  c->swept = false;
+  return QT_OK;
+}
+
+int qt_psi_upload_device(qt_ctx* c, const void* psi) {
+  if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_upload_device before qt_prepare");
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI], psi, c->plan.psi_packed * 16, cudaMemcpyDeviceToDevice,
+                             c->stream));
+  c->have_psi = true;
+  c->swept = false;
+  return QT_OK;
+}
+
+int qt_psi_download(qt_ctx* c, double* psi) {
+  if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->have_psi) return fail(c, QT_ERR_STATE, "no wavefunction uploaded");
+  QT_CUDA(c, cudaMemcpyAsync(psi, c->buf[qt::B_PSI], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
+                             c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_derivative needs qt_prepare and a wavefunction");
+  // alpha = -i * phase
+  double2 alpha = make_double2(phase_im, -phase_re);
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  QT_CUDA(c, cudaGraphLaunch(c->exec, c->stream));
+  c->launches += (int64_t)c->plan.stages.size();
+  c->swept = true;
+  return QT_OK;
+}
+
+int qt_dpsi_download(qt_ctx* c, double* out) {
+  if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
+  QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_DPSI], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
+                             c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+int qt_dpsi_device(qt_ctx* c, const void** p) {
+  if (!c || !p) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_dpsi_device before qt_prepare");
+  *p = c->buf[qt::B_DPSI];
+  return QT_OK;
+}
+
+int qt_energy(qt_ctx* c, double* out4) {
+  if (!c || !out4) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
+  double2 v[2];
+  QT_CUDA(c, cudaMemcpyAsync(&v[0], c->buf[qt::B_MATS] + c->plan.energy_off, 16, cudaMemcpyDeviceToHost, c->stream));
+  QT_CUDA(c, cudaMemcpyAsync(&v[1], c->buf[qt::B_MATS] + c->plan.stop_off, 16, cudaMemcpyDeviceToHost, c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  out4[0] = v[0].x;
+  out4[1] = v[0].y;
+  out4[2] = v[1].x;
+  out4[3] = v[1].y;
+  if (!finite_all(out4, 4)) return fail(c, QT_ERR_NUMERIC, "non-finite energy");
+  return QT_OK;
+}
+
+int64_t qt_matrices_size(const qt_ctx* c, int which) {
+  if (!c || !c->prepared) return -1;
+  const Plan& P = c->plan;
+  int64_t s = 0;
+  int n = (int)P.nodes.size();
+  if (which == QT_MAT_RHO || which == QT_MAT_RHOINV) {
+    for (int a = 0; a < n; ++a) s += (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
+    return s;
+  }
+  if (which == QT_MAT_HMAT || which == QT_MAT_HCON) {
+    for (size_t l = 0; l < P.hslot.size(); ++l)
+      for (int a = 0; a < n; ++a)
+        if (P.hslot[l][a] != -1) s += (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
+    return s;
+  }
+  return -1;
+}
+
+int qt_matrices_download(qt_ctx* c, int which, double* out) {
+  if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
+  const Plan& P = c->plan;
+  std::vector<double2> mats(P.mats_size);
+  QT_CUDA(c, cudaMemcpyAsync(mats.data(), c->buf[qt::B_MATS], P.mats_size * 16, cudaMemcpyDeviceToHost, c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  double2* o = (double2*)out;
+  int n = (int)P.nodes.size();
+  int64_t cur = 0;
+  if (which == QT_MAT_RHO || which == QT_MAT_RHOINV) {
+    const auto& off = which == QT_MAT_RHO ? P.rho_off : P.rhoinv_off;
+    for (int a = 0; a < n; ++a) {
+      int64_t dd = (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
+      std::memcpy(o + cur, mats.data() + off[a], dd * 16);
+      cur += dd;
+    }
+    return QT_OK;
+  }
+  if (which == QT_MAT_HMAT || which == QT_MAT_HCON) {
+    const auto& slot = which == QT_MAT_HMAT ? P.hslot : P.cslot;
+    for (size_t l = 0; l < P.hslot.size(); ++l)
+      for (int a = 0; a < n; ++a) {
+        if (P.hslot[l][a] == -1) continue;
+        int64_t dd = (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
+        if (slot[l][a] >= 0)
+          std::memcpy(o + cur, mats.data() + slot[l][a], dd * 16);
+        else
+          std::memset((void*)(o + cur), 0, dd * 16);
+        cur += dd;
+      }
+    return QT_OK;
+  }
+  return fail(c, QT_ERR_ARG, "unknown matrix set");
+}
+
+int qt_plan_stats(const qt_ctx* c, double* out) {
+  if (!c || !out) return QT_ERR_ARG;
+  if (!c->prepared) return QT_ERR_STATE;
+  const auto& s = c->plan.stats;
+  out[0] = s.ref_flops;
+  out[1] = s.exec_flops;
+  out[2] = (double)c->plan.stages.size();
+  out[3] = (double)s.arena_bytes;
+  out[4] = (double)s.scratch_bytes;
+  out[5] = (double)s.rep_chains;
+  out[6] = (double)s.mf_chains;
+  out[7] = (double)s.app_chains;
+  return QT_OK;
+}
+
+int qt_mode_product(qt_ctx* c, void* C, const void* h, const void* B, int64_t before, int64_t activeB,
+                    int64_t activeC, int64_t after, int add) {
+  if (!c || !C || !h || !B) return fail(c, QT_ERR_ARG, "qt_mode_product: null argument");
+  if (before < 1 || activeB < 1 || activeC < 1 || after < 1 || before * activeB * after > ((int64_t)1 << 31) ||
+      before * activeC * after > ((int64_t)1 << 31))
+    return fail(c, QT_ERR_SHAPE, "qt_mode_product: bad geometry");
+  if (C == B) return fail(c, QT_ERR_ARG, "qt_mode_product: C must not alias B");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  qt::MPTask t;
+  t.in = (const double2*)B;
+  t.out = (double2*)C;
+  t.h = (const double2*)h;
+  t.alpha = make_double2(1.0, 0.0);
+  t.before = (int)before;
+  t.a_in = (int)activeB;
+  t.a_out = (int)activeC;
+  t.after = (int)after;
+  t.diag = 0;
+  t.add = add ? 1 : 0;
+  cudaError_t e = qt::launch_single_mp(t, c->stream, nullptr);
+  if (e != cudaSuccess) return cuda_fail(c, e, "qt_mode_product");
+  c->launches += 1;
+  return QT_OK;
+}
+
+int qt_hole_product(qt_ctx* c, void* S, const void* A, const void* B, int64_t before, int64_t activeA,
+                    int64_t activeB, int64_t after) {
+  if (!c || !S || !A || !B) return fail(c, QT_ERR_ARG, "qt_hole_product: null argument");
+  if (before < 1 || activeA < 1 || activeB < 1 || after < 1 || before * activeA * after > ((int64_t)1 << 31) ||
+      before * activeB * after > ((int64_t)1 << 31) || activeA > 65535 * 32 || activeB > 65535 * 32)
+    return fail(c, QT_ERR_SHAPE, "qt_hole_product: bad geometry");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  qt::HPTask t;
+  t.A = (const double2*)A;
+  t.B = (const double2*)B;
+  t.S = (double2*)S;
+  t.before = (int)before;
+  t.a = (int)activeA;
+  t.after = (int)after;
+  t.aB = (int)activeB;
+  cudaError_t e = qt::launch_single_hp(t, c->stream, nullptr);
+  if (e != cudaSuccess) return cuda_fail(c, e, "qt_hole_product");
+  c->launches += 1;
+  return QT_OK;
+}
+
+int qt_last_mode_product(qt_ctx* c, void* C, const void* A, const void* B, int64_t last_before,
+                         int64_t active, int add) {
+  return qt_mode_product(c, C, A, B, last_before, active, active, 1, add);
+}
+
+int qt_dev_alloc(qt_ctx* c, int64_t bytes, void** p) {
+  if (!c || !p || bytes <= 0) return fail(c, QT_ERR_ARG, "qt_dev_alloc: bad argument");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  cudaError_t e = cudaMalloc(p, (size_t)bytes);
+  if (e != cudaSuccess) return fail(c, QT_ERR_ALLOC, std::string("qt_dev_alloc: ") + cudaGetErrorString(e));
+  return QT_OK;
+}
+
+int qt_dev_free(qt_ctx* c, void* p) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  QT_CUDA(c, cudaFree(p));
+  return QT_OK;
+}
+
+int qt_memcpy_h2d(qt_ctx* c, void* dst, const void* src, int64_t bytes) {
+  if (!c || !dst || !src || bytes < 0) return fail(c, QT_ERR_ARG, "qt_memcpy_h2d: bad argument");
+  QT_CUDA(c, cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+int qt_memcpy_d2h(qt_ctx* c, void* dst, const void* src, int64_t bytes) {
+  if (!c || !dst || !src || bytes < 0) return fail(c, QT_ERR_ARG, "qt_memcpy_d2h: bad argument");
+  QT_CUDA(c, cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+int64_t qt_launch_count(const qt_ctx* c) { return c ? c->launches : -1; }
+
+int qt_stage_count(const qt_ctx* c) { return (c && c->prepared) ? (int)c->plan.stages.size() : -1; }
+
+int qt_stage_info(const qt_ctx* c, int i, int* kind, int64_t* tiles, double* flops, double* bytes) {
+  if (!c || !c->prepared || i < 0 || i >= (int)c->plan.stages.size()) return QT_ERR_ARG;
+  const auto& st = c->plan.stages[i];
+  if (kind) *kind = st.kind;
+  if (tiles) *tiles = st.kind == qt::ST_MP || st.kind == qt::ST_HP || st.kind == qt::ST_ACC ? st.n_tiles : st.n_tasks;
+  if (flops) *flops = st.flops;
+  if (bytes) *bytes = st.bytes;
+  return QT_OK;
+}
+
+int qt_stage_launch(qt_ctx* c, int i) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_stage_launch needs a prepared context and a wavefunction");
+  if (i < 0 || i >= (int)c->plan.stages.size()) return fail(c, QT_ERR_ARG, "no such stage");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "qt_stage_launch");
+  c->launches += 1;
+  return QT_OK;
+}
+
+int qt_probe_fp64_peak(qt_ctx* c, double* tflops) {
+  if (!c || !tflops) return fail(c, QT_ERR_ARG, "null argument");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  double v = 0;
+  cudaError_t e = qt::probe_fp64_peak(c->stream, &v);
+  if (e != cudaSuccess) return cuda_fail(c, e, "qt_probe_fp64_peak");
+  c->launches += 2;
+  *tflops = v;
+  return QT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,243 @@
+// qt_internal.h -- types shared by the planner (qt_plan.cpp), the kernels
+// (qt_kernels.cu) and the C ABI (qt_api.cu) of libqtgpu.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+namespace qt {
+
+// ---------------------------------------------------------------------------
+// Device task records.  One record describes one tensor operation; a launch
+// ("stage") runs a contiguous range of records, split into tiles.
+// ---------------------------------------------------------------------------
+
+// Mode-k product: out[b, j, c] = alpha * sum_a h(j, a) in[b, a, c]
+// (h is a_out x a_in, column-major).  diag != 0: h is the diagonal of a
+// leaf operator (length a_in == a_out) and out[b, j, c] = alpha*h[j]*in[b,j,c].
+// out must not alias in.
+struct MPTask {
+  const double2* in;
+  double2* out;
+  const double2* h;
+  double2 alpha;
+  int before, a_in, a_out, after;
+  int diag;
+  int add;  // 1: out += result
+};
+
+// Hole product: S(i, j) = sum_{b, c} conj(A[b, i, c]) * B[b, j, c].
+struct HPTask {
+  const double2* A;
+  const double2* B;
+  double2* S;
+  int before, a, after;
+  int aB;  // columns of S (activeB); 0 means aB == a
+};
+
+// out[r, j] (+)= alpha * sum_t sum_j' H_t(j, j') X_t[r, j'] over the terms
+// [first, first+count) of the AccTerm table; H == nullptr means identity.
+struct AccTerm {
+  const double2* H;
+  const double2* X;
+};
+struct AccTask {
+  double2* out;
+  const double2* alpha_ptr;  // if non-null, alpha is read from device memory
+  double2 alpha;
+  int rows, d;
+  int first, count;
+  int add, pad;
+};
+
+// out = sum_t c_t * M_t for d x d matrices (grouped mean fields).
+struct LinTerm {
+  double2 c;
+  const double2* M;
+};
+struct LinTask {
+  double2* out;
+  int d, first, count, pad;
+};
+
+// Regularised inverse of a Hermitian d x d matrix via Jacobi eigensolver.
+struct EigTask {
+  const double2* rho;
+  double2* rhoinv;
+  double2* U;  // d x d scratch
+  int d, pad;
+};
+
+// Per non-top node: Sinv = S^-1, P = Sinv * D, M2 = -(rhoinv * P^T).
+struct ProjTask {
+  double2* S;  // overwritten (Gauss-Jordan work)
+  const double2* D;
+  const double2* rhoinv;
+  double2* Sinv;
+  double2* P;
+  double2* M2;
+  int d, pad;
+};
+
+enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ };
+
+struct Stage {
+  int kind;
+  int64_t first_task, n_tasks;
+  int64_t first_tile, n_tiles;
+  const char* name;
+  double flops = 0;  // executed flops of the stage
+  double bytes = 0;  // algorithmic bytes: operands read once, results written once
+};
+
+// ---------------------------------------------------------------------------
+// Host-side plan (symbolic; pointers are bound after the arena exists)
+// ---------------------------------------------------------------------------
+enum Buf { B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_NBUF };
+
+struct Ref {
+  int buf = -1;
+  int64_t off = 0;  // in complex (double2) elements
+};
+
+struct NodeGeo {
+  std::vector<int> shape;
+  int parent = -1, child_idx = -1, leaf_mode = -1;
+  std::vector<int> children;
+  int64_t N = 0, off = 0;  // elements; packed offset of the node tensor
+  int64_t aoff = 0;        // aligned arena offset
+  int depth = 0, height = 0;
+  int dup() const { return shape.back(); }
+  int last() const { return (int)shape.size() - 1; }
+  bool top() const { return parent < 0; }
+  bool bottom() const { return leaf_mode >= 0; }
+  int64_t before(int k) const {
+    int64_t b = 1;
+    for (int i = 0; i < k; ++i) b *= shape[i];
+    return b;
+  }
+  int64_t after(int k) const {
+    int64_t a = 1;
+    for (size_t i = k + 1; i < shape.size(); ++i) a *= shape[i];
+    return a;
+  }
+};
+
+struct PlanStats {
+  double ref_flops = 0, exec_flops = 0;
+  int64_t launches = 0, arena_bytes = 0, scratch_bytes = 0;
+  int64_t rep_chains = 0, mf_chains = 0, app_chains = 0;
+};
+
+struct Plan {
+  // geometry
+  std::vector<NodeGeo> nodes;
+  int64_t psi_packed = 0, psi_arena = 0;
+  // matrices arena layout
+  std::vector<int64_t> rho_off, rhoinv_off, u_off, s_off, sinv_off, d_off, p_off, m2_off;
+  int64_t energy_off = 0, stop_off = 0;
+  // sparse (term, node) -> slot offset of hmat / hcon; -1 if inactive
+  std::vector<std::vector<int64_t>> hslot, cslot;
+  int64_t mats_size = 0;
+  int64_t scratch_size = 0;
+  int64_t ops_size = 0;
+  // symbolic task lists (buffer-relative); bound to pointers by bind()
+  struct SMP {
+    Ref in, out, h;
+    double2 alpha;
+    int before, a_in, a_out, after, diag;
+  };
+  struct SHP {
+    Ref A, B, S;
+    int before, a, after;
+  };
+  struct SAccTerm {
+    Ref H;  // buf == -1: identity
+    Ref X;
+  };
+  struct SAcc {
+    Ref out;
+    bool alpha_param;
+    double2 alpha;
+    int rows, d, first, count, add;
+  };
+  struct SLinTerm {
+    double2 c;
+    Ref M;
+  };
+  struct SLin {
+    Ref out;
+    int d, first, count;
+  };
+  struct SEig {
+    Ref rho, rhoinv, U;
+    int d;
+  };
+  struct SProj {
+    Ref S, D, rhoinv, Sinv, P, M2;
+    int d;
+  };
+  std::vector<SMP> mp;
+  std::vector<SHP> hp;
+  std::vector<SAcc> acc;
+  std::vector<SAccTerm> acc_terms;
+  std::vector<SLin> lin;
+  std::vector<SLinTerm> lin_terms;
+  std::vector<SEig> eig;
+  std::vector<SProj> proj;
+  std::vector<Stage> stages;
+  // tiles (bound with task indices only)
+  std::vector<int2> mp_tiles;
+  std::vector<int4> hp_tiles;
+  std::vector<int4> acc_tiles;
+  // constant matrices written once at prepare: (offset, d) identity
+  std::vector<std::pair<int64_t, int>> identities;
+  PlanStats stats;
+  int max_eig_d = 0;
+};
+
+struct OpTable {
+  std::vector<int> kind, dim;
+  std::vector<int64_t> off;
+  std::vector<double> data;  // interleaved
+};
+
+struct SopDesc {
+  int n_terms = 0;
+  std::vector<double2> coeff;
+  std::vector<int> ptr, mode, op;
+};
+
+// planner entry point; returns "" on success or an error message
+std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
+                       const SopDesc& sop, int flavour, int64_t scratch_budget_elems);
+
+// kernel launches (qt_kernels.cu)
+struct DevTables {
+  MPTask* mp = nullptr;
+  HPTask* hp = nullptr;
+  AccTask* acc = nullptr;
+  AccTerm* acc_terms = nullptr;
+  LinTask* lin = nullptr;
+  LinTerm* lin_terms = nullptr;
+  EigTask* eig = nullptr;
+  ProjTask* proj = nullptr;
+  int2* mp_tiles = nullptr;
+  int4* hp_tiles = nullptr;
+  int4* acc_tiles = nullptr;
+};
+cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d,
+                         cudaStream_t s);
+cudaError_t launch_set_identity(double2* m, int d, cudaStream_t s);
+// single-op launches for the primitive C ABI calls
+cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void* scratch);
+cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void* scratch);
+int mp_outputs_per_tile();
+// FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
+cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
+
+}  // namespace qt

@@ -1,0 +1,620 @@
+// qt_kernels.cu -- complex128 kernels of the H.Psi sweep for sm_103a.
+//
+// GB300 executes FP64 at ~1.2 TFLOP/s (1/61 of its FP32 rate), so every
+// complex128 contraction here is bound by the FP64 pipe, not by HBM: a
+// complex multiply-add needs 4 DFMA but at most 32 bytes of operands, which
+// L1/L2 deliver far faster than the DFMA units consume them.  The kernels are
+// therefore plain SIMT loops with coalesced 16-byte complex loads, shared
+// memory staging where an operand is reused by a whole tile, several
+// independent accumulators per thread for instruction-level parallelism, and
+// fixed summation orders (no atomics: results are bit-identical run to run).
+//
+// Batched launches: each kernel reads a task table and a tile table; block b
+// processes tile b.  The planner (qt_plan.cpp) builds both once per tree.
+#include <cmath>
+
+#include "qt_internal.h"
+
+namespace qt {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kMpPerThread = 4;
+constexpr int kMpTile = kThreads * kMpPerThread;  // 1024, as in the planner
+constexpr int kHpTile = 32;
+constexpr int kHpK = 16;
+constexpr int kAccRows = 64, kAccCols = 16;
+
+__device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+// acc += a * b
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+__device__ __forceinline__ void cfmac(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
+  return make_double2(a.x + b.x, a.y + b.y);
+}
+
+// ---------------------------------------------------------------------------
+// Mode-k product (matvec / matrixTensor): one thread per 4 outputs, each a
+// length-a_in dot product of a row of h with a fiber of the input.  Along
+// mode 0 consecutive threads read consecutive rows of h (coalesced) and share
+// the input fiber; along higher modes they read consecutive input elements
+// (coalesced) and share h.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mp_tile(const MPTask& t, int64_t start) {
+  const int64_t total = (int64_t)t.before * t.a_out * t.after;
+  const int64_t slice_in = (int64_t)t.before * t.a_in;
+  int64_t o[kMpPerThread];
+  const double2* hp[kMpPerThread];
+  const double2* ip[kMpPerThread];
+#pragma unroll
+  for (int q = 0; q < kMpPerThread; ++q) {
+    o[q] = start + threadIdx.x + (int64_t)q * kThreads;
+    int64_t oo = o[q] < total ? o[q] : 0;
+    int64_t b = oo % t.before;
+    int64_t r = oo / t.before;
+    int j = (int)(r % t.a_out);
+    int64_t c = r / t.a_out;
+    hp[q] = t.h + j;
+    ip[q] = t.in + b + slice_in * c;
+    if (t.diag) ip[q] += (int64_t)j * t.before;
+  }
+  double2 acc[kMpPerThread];
+  if (t.diag) {
+#pragma unroll
+    for (int q = 0; q < kMpPerThread; ++q) acc[q] = cmul(__ldg(hp[q]), __ldg(ip[q]));
+  } else {
+#pragma unroll
+    for (int q = 0; q < kMpPerThread; ++q) acc[q] = cz();
+    const int64_t hs = t.a_out, is = t.before;
+    int a = 0;
+    for (; a + 1 < t.a_in; a += 2) {
+      double2 h0[kMpPerThread], x0[kMpPerThread], h1[kMpPerThread], x1[kMpPerThread];
+#pragma unroll
+      for (int q = 0; q < kMpPerThread; ++q) {
+        h0[q] = __ldg(hp[q] + a * hs);
+        x0[q] = __ldg(ip[q] + a * is);
+        h1[q] = __ldg(hp[q] + (a + 1) * hs);
+        x1[q] = __ldg(ip[q] + (a + 1) * is);
+      }
+#pragma unroll
+      for (int q = 0; q < kMpPerThread; ++q) {
+        cfma(acc[q], h0[q], x0[q]);
+        cfma(acc[q], h1[q], x1[q]);
+      }
+    }
+    for (; a < t.a_in; ++a) {
+#pragma unroll
+      for (int q = 0; q < kMpPerThread; ++q) cfma(acc[q], __ldg(hp[q] + a * hs), __ldg(ip[q] + a * is));
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kMpPerThread; ++q)
+    if (o[q] < total) {
+      const double2 v = cmul(t.alpha, acc[q]);
+      t.out[o[q]] = t.add ? cadd(t.out[o[q]], v) : v;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) k_mp(const MPTask* __restrict__ tasks,
+                                                 const int2* __restrict__ tiles, int64_t tile0) {
+  const int2 tl = tiles[tile0 + blockIdx.x];
+  const MPTask t = tasks[tl.x];
+  mp_tile(t, tl.y);
+}
+
+__global__ void __launch_bounds__(kThreads) k_mp_single(MPTask t) {
+  mp_tile(t, (int64_t)blockIdx.x * kMpTile);
+}
+
+// ---------------------------------------------------------------------------
+// Hole product (rhomat / contraction): S(i, j) = sum_k conj(A[k; i]) B[k; j]
+// with k = (b, c).  A 32 x 32 output tile per block, 2 x 2 outputs per
+// thread; A and B are staged through shared memory 16 k-rows at a time with
+// coalesced loads (along b when before > 1, along i when before == 1).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void hp_tile(const HPTask& t, int i0, int j0) {
+  __shared__ double2 sA[kHpK][kHpTile + 1];
+  __shared__ double2 sB[kHpK][kHpTile + 1];
+  const int before = t.before;
+  const int aA = t.a, aB = t.aB > 0 ? t.aB : t.a;
+  const int64_t K = (int64_t)before * t.after;
+  const int64_t sliceA = (int64_t)before * aA, sliceB = (int64_t)before * aB;
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double2 acc00 = cz(), acc01 = cz(), acc10 = cz(), acc11 = cz();
+  for (int64_t k0 = 0; k0 < K; k0 += kHpK) {
+    for (int e = threadIdx.x; e < kHpK * kHpTile; e += kThreads) {
+      int kk, ii;
+      if (before == 1) {
+        ii = e % kHpTile;
+        kk = e / kHpTile;
+      } else {
+        kk = e % kHpK;
+        ii = e / kHpK;
+      }
+      const int64_t k = k0 + kk;
+      double2 va = cz(), vb = cz();
+      if (k < K) {
+        const int64_t b = k % before, c = k / before;
+        const int i = i0 + ii, j = j0 + ii;
+        if (i < aA) va = __ldg(t.A + b + (int64_t)before * i + sliceA * c);
+        if (j < aB) vb = __ldg(t.B + b + (int64_t)before * j + sliceB * c);
+      }
+      sA[kk][ii] = va;
+      sB[kk][ii] = vb;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kHpK; ++kk) {
+      const double2 a0 = sA[kk][tx * 2], a1 = sA[kk][tx * 2 + 1];
+      const double2 b0 = sB[kk][ty * 2], b1 = sB[kk][ty * 2 + 1];
+      cfmac(acc00, a0, b0);
+      cfmac(acc10, a1, b0);
+      cfmac(acc01, a0, b1);
+      cfmac(acc11, a1, b1);
+    }
+    __syncthreads();
+  }
+  const int i = i0 + tx * 2, j = j0 + ty * 2;
+  if (i < aA && j < aB) t.S[i + (int64_t)aA * j] = acc00;
+  if (i + 1 < aA && j < aB) t.S[i + 1 + (int64_t)aA * j] = acc10;
+  if (i < aA && j + 1 < aB) t.S[i + (int64_t)aA * (j + 1)] = acc01;
+  if (i + 1 < aA && j + 1 < aB) t.S[i + 1 + (int64_t)aA * (j + 1)] = acc11;
+}
+
+__global__ void __launch_bounds__(kThreads) k_hp(const HPTask* __restrict__ tasks,
+                                                 const int4* __restrict__ tiles, int64_t tile0) {
+  const int4 tl = tiles[tile0 + blockIdx.x];
+  const HPTask t = tasks[tl.x];
+  hp_tile(t, tl.y, tl.z);
+}
+
+__global__ void __launch_bounds__(kThreads) k_hp_single(HPTask t) {
+  hp_tile(t, blockIdx.x * kHpTile, blockIdx.y * kHpTile);
+}
+
+// ---------------------------------------------------------------------------
+// Last-mode accumulation (multStateAB summed over terms):
+//   out[r, j] (+)= alpha * sum_t sum_j' H_t(j, j') X_t[r, j'].
+// 64 rows x 16 columns per block; a warp covers 32 consecutive rows (coalesced
+// X loads) of 4 columns (H loads broadcast across the warp).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_acc(const AccTask* __restrict__ tasks,
+                                                  const AccTerm* __restrict__ terms,
+                                                  const int4* __restrict__ tiles, int64_t tile0) {
+  const int4 tl = tiles[tile0 + blockIdx.x];
+  const AccTask t = tasks[tl.x];
+  const int r = tl.y + threadIdx.x % kAccRows;
+  const int jb = tl.z + (threadIdx.x / kAccRows) * 4;
+  const bool rv = r < t.rows;
+  const int d = t.d;
+  const int64_t rows = t.rows;
+  double2 acc[4] = {cz(), cz(), cz(), cz()};
+  for (int s = 0; s < t.count; ++s) {
+    const AccTerm T = terms[t.first + s];
+    if (T.H == nullptr) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = jb + q;
+        if (rv && j < d) acc[q] = cadd(acc[q], __ldg(T.X + r + rows * j));
+      }
+    } else {
+      const double2* hrow[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) hrow[q] = T.H + (jb + q < d ? jb + q : 0);
+      for (int jp = 0; jp < d; ++jp) {
+        const double2 x = rv ? __ldg(T.X + r + rows * jp) : cz();
+#pragma unroll
+        for (int q = 0; q < 4; ++q) cfma(acc[q], __ldg(hrow[q] + (int64_t)d * jp), x);
+      }
+    }
+  }
+  const double2 alpha = t.alpha_ptr ? *t.alpha_ptr : t.alpha;
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int j = jb + q;
+    if (rv && j < d) {
+      const double2 v = cmul(alpha, acc[q]);
+      double2* p = t.out + r + rows * j;
+      *p = t.add ? cadd(*p, v) : v;
+    }
+  }
+}
+
+// out = sum_t c_t M_t (d x d), one block per output matrix.
+__global__ void __launch_bounds__(kThreads) k_lin(const LinTask* __restrict__ tasks,
+                                                  const LinTerm* __restrict__ terms, int64_t task0) {
+  const LinTask t = tasks[task0 + blockIdx.x];
+  const int dd = t.d * t.d;
+  for (int e = threadIdx.x; e < dd; e += kThreads) {
+    double2 acc = cz();
+    for (int s = 0; s < t.count; ++s) {
+      const LinTerm T = terms[t.first + s];
+      cfma(acc, T.c, __ldg(T.M + e));
+    }
+    t.out[e] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Regularised inverse of a Hermitian matrix (SpectralDecompositionTree::
+// calculate + invert): parallel cyclic Jacobi with a round-robin pairing
+// (every round rotates d/2 disjoint index pairs at once), then
+//   rhoinv = U diag(1 / (w + eps*exp(-w/eps))) U^dagger.
+// One block per matrix; A lives in shared memory, U in global scratch.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void rr_pair(int m, int r, int i, int& p, int& q) {
+  // circle method over m (even) indices, round r in [0, m-1), pair i in [0, m/2)
+  if (i == 0) {
+    p = r;
+    q = m - 1;
+  } else {
+    p = (r + i) % (m - 1);
+    q = (r - i + (m - 1)) % (m - 1);
+  }
+  if (p > q) {
+    int x = p;
+    p = q;
+    q = x;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) k_eig(const EigTask* __restrict__ tasks, int64_t task0,
+                                                  double eps) {
+  extern __shared__ double2 smem[];
+  const EigTask t = tasks[task0 + blockIdx.x];
+  const int d = t.d;
+  const int m = d + (d & 1);
+  const int np = m / 2;
+  double2* A = smem;                      // d*d
+  double2* rot = A + (int64_t)d * d;      // np entries: (c, s)
+  double2* ph = rot + np;                 // np entries: e
+  double2* fw = ph + np;                  // m entries: f(eigenvalue) in .x
+  int* pq = (int*)(fw + m);               // 2*np
+  __shared__ double red_off[kThreads], red_diag[kThreads];
+  double2* U = t.U;
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int i = e % d, j = e / d;
+    const double2 aij = t.rho[i + (int64_t)d * j], aji = t.rho[j + (int64_t)d * i];
+    // Hermitian part
+    A[e] = (i == j) ? make_double2(aij.x, 0.0)
+                    : make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
+    U[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    double off = 0.0, dg = 0.0;
+    for (int e = threadIdx.x; e < d * d; e += kThreads) {
+      const double v = A[e].x * A[e].x + A[e].y * A[e].y;
+      if (e % d == e / d)
+        dg += v;
+      else
+        off += v;
+    }
+    red_off[threadIdx.x] = off;
+    red_diag[threadIdx.x] = dg;
+    __syncthreads();
+    for (int s = kThreads / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        red_off[threadIdx.x] += red_off[threadIdx.x + s];
+        red_diag[threadIdx.x] += red_diag[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    const double toff = red_off[0], tdiag = red_diag[0];
+    __syncthreads();
+    if (!(toff > 1e-30 * tdiag) || toff == 0.0) break;
+    for (int r = 0; r < m - 1; ++r) {
+      for (int i = threadIdx.x; i < np; i += kThreads) {
+        int p, q;
+        rr_pair(m, r, i, p, q);
+        double c = 1.0, s = 0.0;
+        double2 e = make_double2(1.0, 0.0);
+        if (q < d) {
+          const double2 apq = A[p + d * q];
+          const double ab = hypot(apq.x, apq.y);
+          if (ab > 0.0) {
+            e = make_double2(apq.x / ab, apq.y / ab);
+            const double theta = 0.5 * atan2(2.0 * ab, A[q + d * q].x - A[p + d * p].x);
+            c = cos(theta);
+            s = sin(theta);
+          }
+        }
+        rot[i] = make_double2(c, s);
+        ph[i] = e;
+        pq[2 * i] = p;
+        pq[2 * i + 1] = q;
+      }
+      __syncthreads();
+      // columns: A <- A G, U <- U G
+      for (int idx = threadIdx.x; idx < np * d; idx += kThreads) {
+        const int i = idx / d, k = idx % d;
+        const int p = pq[2 * i], q = pq[2 * i + 1];
+        if (q >= d || rot[i].y == 0.0) continue;
+        const double c = rot[i].x, s = rot[i].y;
+        const double2 e = ph[i];
+        const double2 se = make_double2(s * e.x, s * e.y);    // s*e
+        const double2 sce = make_double2(s * e.x, -s * e.y);  // s*conj(e)
+        double2 akp = A[k + d * p], akq = A[k + d * q];
+        double2 np_ = make_double2(c * akp.x, c * akp.y);
+        double2 t2 = cmul(sce, akq);
+        np_.x -= t2.x;
+        np_.y -= t2.y;
+        double2 nq = cmul(se, akp);
+        nq.x += c * akq.x;
+        nq.y += c * akq.y;
+        A[k + d * p] = np_;
+        A[k + d * q] = nq;
+        double2 ukp = U[k + (int64_t)d * p], ukq = U[k + (int64_t)d * q];
+        np_ = make_double2(c * ukp.x, c * ukp.y);
+        t2 = cmul(sce, ukq);
+        np_.x -= t2.x;
+        np_.y -= t2.y;
+        nq = cmul(se, ukp);
+        nq.x += c * ukq.x;
+        nq.y += c * ukq.y;
+        U[k + (int64_t)d * p] = np_;
+        U[k + (int64_t)d * q] = nq;
+      }
+      __syncthreads();
+      // rows: A <- G^dagger A
+      for (int idx = threadIdx.x; idx < np * d; idx += kThreads) {
+        const int i = idx / d, k = idx % d;
+        const int p = pq[2 * i], q = pq[2 * i + 1];
+        if (q >= d || rot[i].y == 0.0) continue;
+        const double c = rot[i].x, s = rot[i].y;
+        const double2 e = ph[i];
+        const double2 se = make_double2(s * e.x, s * e.y);
+        const double2 sce = make_double2(s * e.x, -s * e.y);
+        const double2 apk = A[p + d * k], aqk = A[q + d * k];
+        double2 np_ = make_double2(c * apk.x, c * apk.y);
+        double2 t2 = cmul(se, aqk);
+        np_.x -= t2.x;
+        np_.y -= t2.y;
+        double2 nq = cmul(sce, apk);
+        nq.x += c * aqk.x;
+        nq.y += c * aqk.y;
+        A[p + d * k] = np_;
+        A[q + d * k] = nq;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < np; i += kThreads) {
+        const int p = pq[2 * i], q = pq[2 * i + 1];
+        if (q < d && rot[i].y != 0.0) {
+          A[p + d * q] = cz();
+          A[q + d * p] = cz();
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int i = threadIdx.x; i < d; i += kThreads) {
+    const double w = A[i + d * i].x;
+    fw[i].x = 1.0 / (w + eps * exp(-w / eps));
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int i = e % d, j = e / d;
+    double2 acc = cz();
+    for (int k = 0; k < d; ++k) {
+      const double2 uik = U[i + (int64_t)d * k];
+      const double2 ujk = U[j + (int64_t)d * k];
+      const double f = fw[k].x;
+      // acc += uik * f * conj(ujk)
+      cfma(acc, make_double2(uik.x * f, uik.y * f), make_double2(ujk.x, -ujk.y));
+    }
+    t.rhoinv[e] = acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Projector pieces of LayerDerivative (projectOut + rho^-1), per node:
+//   Sinv = S^-1 (Gauss-Jordan, partial pivoting; S is overwritten)
+//   P    = Sinv D
+//   M2   = -(rhoinv P^T)
+// so that the derivative is dPsi = alpha ((H Phi) rhoinv^T + Phi M2^T).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads) k_proj(const ProjTask* __restrict__ tasks,
+                                                   int64_t task0) {
+  const ProjTask t = tasks[task0 + blockIdx.x];
+  const int d = t.d;
+  double2* S = t.S;
+  double2* X = t.Sinv;
+  __shared__ double2 fcol[128];
+  __shared__ int piv;
+  __shared__ double2 pinv;
+  for (int e = threadIdx.x; e < d * d; e += kThreads)
+    X[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
+  __syncthreads();
+  for (int col = 0; col < d; ++col) {
+    if (threadIdx.x == 0) {
+      int best = col;
+      double bv = -1.0;
+      for (int r = col; r < d; ++r) {
+        const double2 v = S[r + d * col];
+        const double a = v.x * v.x + v.y * v.y;
+        if (a > bv) bv = a, best = r;
+      }
+      piv = best;
+    }
+    __syncthreads();
+    const int pr = piv;
+    if (pr != col) {
+      for (int j = threadIdx.x; j < d; j += kThreads) {
+        double2 x = S[col + d * j];
+        S[col + d * j] = S[pr + d * j];
+        S[pr + d * j] = x;
+        x = X[col + d * j];
+        X[col + d * j] = X[pr + d * j];
+        X[pr + d * j] = x;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double2 v = S[col + d * col];
+      const double den = v.x * v.x + v.y * v.y;
+      pinv = make_double2(v.x / den, -v.y / den);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < d; j += kThreads) {
+      S[col + d * j] = cmul(S[col + d * j], pinv);
+      X[col + d * j] = cmul(X[col + d * j], pinv);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < d; r += kThreads) fcol[r] = S[r + d * col];
+    __syncthreads();
+    for (int e = threadIdx.x; e < d * d; e += kThreads) {
+      const int r = e % d, j = e / d;
+      if (r == col) continue;
+      const double2 f = fcol[r];
+      const double2 sc = S[col + d * j], xc = X[col + d * j];
+      double2 s = S[e], x = X[e];
+      cfma(s, make_double2(-f.x, -f.y), sc);
+      cfma(x, make_double2(-f.x, -f.y), xc);
+      S[e] = s;
+      X[e] = x;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int i = e % d, j = e / d;
+    double2 acc = cz();
+    for (int k = 0; k < d; ++k) cfma(acc, X[i + d * k], t.D[k + d * j]);
+    t.P[e] = acc;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int j = e % d, m = e / d;
+    double2 acc = cz();
+    for (int n = 0; n < d; ++n) cfma(acc, t.rhoinv[j + d * n], t.P[m + d * n]);
+    t.M2[e] = make_double2(-acc.x, -acc.y);
+  }
+}
+
+__global__ void k_identity(double2* m, int d) {
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x)
+    m[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
+}
+
+// Eight independent FMA chains per thread; one store per thread keeps the
+// chains live.  Every store index is < gridDim.x * blockDim.x.
+__global__ void __launch_bounds__(kThreads) k_fp64_fma(double* out, int iters, double a, double b) {
+  double acc[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc[i] = threadIdx.x + i;
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) acc[i] = fma(acc[i], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) s += acc[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+inline int64_t eig_smem_bytes(int d) {
+  const int m = d + (d & 1);
+  const int np = m / 2;
+  return 16 * ((int64_t)d * d + 2 * np + m) + 8 * (int64_t)np + 16;
+}
+
+}  // namespace
+
+int mp_outputs_per_tile() { return kMpTile; }
+
+cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int blocks = sms * 8, iters = 4096;
+  double* buf = nullptr;
+  e = cudaMallocAsync((void**)&buf, sizeof(double) * blocks * kThreads, s);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  k_fp64_fma<<<blocks, kThreads, 0, s>>>(buf, iters, 0.999, 0.001);  // warm-up
+  cudaEventRecord(e0, s);
+  k_fp64_fma<<<blocks, kThreads, 0, s>>>(buf, iters, 0.999, 0.001);
+  cudaEventRecord(e1, s);
+  e = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(buf, s);
+  cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * kThreads / (ms * 1e-3) / 1e12;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d,
+                         cudaStream_t s) {
+  switch (st.kind) {
+    case ST_MP:
+      k_mp<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
+      break;
+    case ST_HP:
+      k_hp<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.hp, t.hp_tiles, st.first_tile);
+      break;
+    case ST_ACC:
+      k_acc<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.acc, t.acc_terms, t.acc_tiles,
+                                                      st.first_tile);
+      break;
+    case ST_LIN:
+      k_lin<<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.lin, t.lin_terms, st.first_task);
+      break;
+    case ST_EIG: {
+      const int64_t sm = eig_smem_bytes(max_eig_d);
+      cudaError_t e = cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)sm);
+      if (e != cudaSuccess) return e;
+      k_eig<<<(unsigned)st.n_tasks, kThreads, sm, s>>>(t.eig, st.first_task, eps);
+      break;
+    }
+    case ST_PROJ:
+      k_proj<<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.proj, st.first_task);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_identity(double2* m, int d, cudaStream_t s) {
+  k_identity<<<1, kThreads, 0, s>>>(m, d);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void*) {
+  const int64_t total = (int64_t)task.before * task.a_out * task.after;
+  const int64_t blocks = (total + kMpTile - 1) / kMpTile;
+  if (blocks == 0) return cudaSuccess;
+  k_mp_single<<<(unsigned)blocks, kThreads, 0, s>>>(task);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void*) {
+  const int aB = task.aB > 0 ? task.aB : task.a;
+  dim3 grid((task.a + kHpTile - 1) / kHpTile, (aB + kHpTile - 1) / kHpTile);
+  if (grid.x == 0 || grid.y == 0) return cudaSuccess;
+  k_hp_single<<<grid, kThreads, 0, s>>>(task);
+  return cudaGetLastError();
+}
+
+}  // namespace qt

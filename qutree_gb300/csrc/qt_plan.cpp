@@ -1,0 +1,734 @@
+// qt_plan.cpp -- host planner of the H.Psi sweep.
+//
+// Turns (tree, SOP) into a fixed list of batched GPU stages, executed in
+// order for every sweep (and captured once as a CUDA graph):
+//
+//   1. density matrices, top-down by depth
+//      (TreeFunctions::contraction(Rho, Psi, tree, true),
+//       include/TreeClasses/MatrixTreeFunctions_Implementation.h:59-127)
+//   2. regularised inverses of all density matrices
+//      (SpectralDecompositionTree::calculate / invert,
+//       src/TreeClasses/SpectralDecompositionTree.cpp:30-48)
+//   3. represent, bottom-up by height
+//      (TreeFunctions::represent,
+//       include/TreeClasses/SparseMatrixTreeFunctions_Implementation.h:17-78)
+//   4. mean fields, top-down by depth
+//      (TreeFunctions::contraction / contractionLayer, same file :144-203)
+//   5. Apply at every node (src/TreeClasses/HamiltonianRepresentation.cpp:6-43)
+//   6. projector, inverse density and -i*phase (LayerDerivative, :53-72) and
+//      the top-node expectation (Expectation, :45-51).
+//
+// Every represent / mean-field / apply step of the reference is a "chain":
+// an input node tensor, up to a few mode products (or diagonal leaf
+// operators), and a final hole product or last-mode accumulation.  All
+// chains of one tree level run in the same launches: the chains' k-th mode
+// products form one stage, their final contractions the next.
+//
+// Flavour QT_PLAN_REFERENCE keeps one chain per (SOP term, node), exactly the
+// reference's call sequence.  Flavour QT_PLAN_GROUPED gives terms whose
+// restriction to a node's subtree (represent, Apply) or to its complement
+// (mean field) coincide one shared matrix and one chain: the reference
+// computes the same matrix once per term; here it is computed once.  In
+// Apply, terms with the same inside part share the chain and their mean
+// fields are summed first (sum_l c_l H_l) x_last X, which is linear algebra
+// on the same products.
+#include <algorithm>
+#include <map>
+#include <set>
+#include <stdexcept>
+
+#include "qt_internal.h"
+
+namespace qt {
+namespace {
+
+constexpr int kMpTile = 1024;  // outputs per mode-product tile (256 threads x 4)
+constexpr int kHpTile = 32;    // hole-product output tile edge
+constexpr int kAccRows = 64, kAccCols = 16;
+constexpr int64_t kAlign = 16;  // elements (256 bytes)
+
+int64_t align_up(int64_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+double2 c2(double r, double i) {
+  double2 v;
+  v.x = r;
+  v.y = i;
+  return v;
+}
+
+struct COp {
+  int kind;  // 0 mode product, 1 diagonal leaf operator
+  int mode;
+  Ref mat;
+  double2 alpha;
+};
+
+struct Item {
+  int node;  // geometry of the chain's tensors
+  Ref in;
+  std::vector<COp> ops;
+  int fin;  // 0: hole product into S over hp_mode; 1: accumulate into hphi
+  Ref S;
+  int hp_mode = 0;
+  int acc_node = -1;
+  Ref accH;  // buf -1: identity
+};
+
+class Builder {
+ public:
+  Builder(Plan& P, const std::vector<NodeGeo>& nodes, const OpTable& ops, const SopDesc& sop,
+          int flavour, int64_t budget)
+      : P(P), nd(P.nodes), ops(ops), sop(sop), grouped(flavour == 1), budget(budget) {
+    P.nodes = nodes;
+  }
+
+  void run() {
+    geometry();
+    activity();
+    layout();
+    stage_density();
+    stage_inverse();
+    stage_represent();
+    stage_meanfield();
+    stage_apply();
+    stage_final();
+    count_reference_flops();
+    P.stats.launches = (int64_t)P.stages.size();
+  }
+
+ private:
+  Plan& P;
+  std::vector<NodeGeo>& nd;
+  const OpTable& ops;
+  const SopDesc& sop;
+  bool grouped;
+  int64_t budget;
+  int n = 0, L = 0, top = -1;
+  std::vector<std::vector<char>> act;  // [term][node]
+  std::vector<std::vector<char>> inside;  // [node][mode]
+  std::vector<std::vector<int>> gkey;  // apply group of (term) per node, filled per node
+  int64_t mats_cursor = 0;
+  double stage_flops_mark = 0;
+  std::map<std::vector<int>, int64_t> hslot_of_key, cslot_of_key;
+
+  double stage_bytes(int kind, int64_t t0, int64_t t1) const {
+    double b = 0;
+    for (int64_t t = t0; t < t1; ++t) {
+      if (kind == ST_MP) {
+        const auto& m = P.mp[t];
+        double n_in = (double)m.before * m.a_in * m.after, n_out = (double)m.before * m.a_out * m.after;
+        b += 16.0 * (n_in + n_out + (m.diag ? m.a_in : (double)m.a_in * m.a_out));
+      } else if (kind == ST_HP) {
+        const auto& h = P.hp[t];
+        b += 16.0 * (2.0 * h.before * h.a * h.after + (double)h.a * h.a);
+      } else if (kind == ST_ACC) {
+        const auto& a = P.acc[t];
+        double n = (double)a.rows * a.d;
+        b += 16.0 * (n * (a.count + (a.add ? 2 : 1)) + (double)a.count * a.d * a.d);
+      } else if (kind == ST_LIN) {
+        const auto& l = P.lin[t];
+        b += 16.0 * (double)l.d * l.d * (l.count + 1);
+      } else if (kind == ST_EIG) {
+        b += 16.0 * 2 * (double)P.eig[t].d * P.eig[t].d;
+      } else if (kind == ST_PROJ) {
+        b += 16.0 * 6 * (double)P.proj[t].d * P.proj[t].d;
+      }
+    }
+    return b;
+  }
+
+  Ref psi(int node) const { return Ref{B_PSI, nd[node].aoff}; }
+  Ref hphi(int node) const { return Ref{B_HPHI, nd[node].aoff}; }
+  Ref dpsi(int node) const { return Ref{B_DPSI, nd[node].aoff}; }
+  Ref mat(int64_t off) const { return Ref{B_MATS, off}; }
+  Ref opref(int op) const { return Ref{B_OPS, ops.off[op]}; }
+
+  int64_t alloc_mat(int d) {
+    int64_t o = mats_cursor;
+    mats_cursor += align_up((int64_t)d * d);
+    return o;
+  }
+
+  void geometry() {
+    n = (int)nd.size();
+    L = sop.n_terms;
+    top = n - 1;
+    if (n == 0 || !nd[top].top()) throw std::runtime_error("the last node must be the top node");
+    int64_t off = 0, aoff = 0;
+    for (int i = 0; i < n; ++i) {
+      NodeGeo& g = nd[i];
+      g.N = 1;
+      for (int d : g.shape) g.N *= d;
+      // node tensors stay packed in the arena (QuTree's TensorTree layout):
+      // every kernel load is a naturally aligned 16-byte complex
+      g.off = off;
+      g.aoff = aoff;
+      off += g.N;
+      aoff += g.N;
+      g.children.clear();
+      if (g.shape.empty() || g.shape.back() < 1) throw std::runtime_error("empty node shape");
+      if (g.shape.back() > 112) throw std::runtime_error("bond dimension above 112 is not supported");
+      for (int d : g.shape)
+        if (d < 1) throw std::runtime_error("non-positive dimension");
+      if (g.N > (int64_t)1 << 30) throw std::runtime_error("node tensor too large");
+    }
+    P.psi_packed = off;
+    P.psi_arena = aoff;
+    for (int i = 0; i < n; ++i) {
+      if (nd[i].parent >= 0) {
+        if (nd[i].parent <= i) throw std::runtime_error("parents must follow their children");
+        auto& ch = nd[nd[i].parent].children;
+        if ((int)ch.size() <= nd[i].child_idx) ch.resize(nd[i].child_idx + 1, -1);
+        ch[nd[i].child_idx] = i;
+      } else if (i != top) {
+        throw std::runtime_error("only the last node may have no parent");
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      NodeGeo& g = nd[i];
+      if (g.bottom()) {
+        if (g.shape.size() != 2) throw std::runtime_error("bottom nodes must have order 2");
+        g.height = 0;
+      } else {
+        if ((int)g.children.size() + 1 != (int)g.shape.size())
+          throw std::runtime_error("upper node order must be children + 1");
+        int h = 0;
+        for (size_t k = 0; k < g.children.size(); ++k) {
+          int c = g.children[k];
+          if (c < 0) throw std::runtime_error("missing child");
+          if (nd[c].dup() != g.shape[k]) throw std::runtime_error("child bond mismatch");
+          h = std::max(h, nd[c].height + 1);
+        }
+        g.height = h;
+      }
+    }
+    for (int i = n - 1; i >= 0; --i) nd[i].depth = nd[i].top() ? 0 : nd[nd[i].parent].depth + 1;
+  }
+
+  void activity() {
+    int max_mode = -1;
+    std::map<int, int> leaf_node;
+    for (int i = 0; i < n; ++i)
+      if (nd[i].bottom()) {
+        if (leaf_node.count(nd[i].leaf_mode)) throw std::runtime_error("duplicate leaf mode");
+        leaf_node[nd[i].leaf_mode] = i;
+        max_mode = std::max(max_mode, nd[i].leaf_mode);
+      }
+    inside.assign(n, std::vector<char>(max_mode + 1, 0));
+    for (int i = 0; i < n; ++i) {
+      if (nd[i].bottom()) inside[i][nd[i].leaf_mode] = 1;
+      for (int c : nd[i].children)
+        for (int m = 0; m <= max_mode; ++m) inside[i][m] |= inside[c][m];
+    }
+    act.assign(L, std::vector<char>(n, 0));
+    for (int l = 0; l < L; ++l) {
+      if (sop.ptr[l + 1] <= sop.ptr[l]) throw std::runtime_error("empty SOP term");
+      for (int f = sop.ptr[l]; f < sop.ptr[l + 1]; ++f) {
+        auto it = leaf_node.find(sop.mode[f]);
+        if (it == leaf_node.end()) throw std::runtime_error("SOP factor on unknown mode");
+        int op = sop.op[f];
+        if (op < 0 || op >= (int)ops.kind.size()) throw std::runtime_error("bad operator id");
+        if (ops.dim[op] != nd[it->second].shape[0])
+          throw std::runtime_error("operator dim != leaf dim");
+        for (int a = it->second; a >= 0; a = nd[a].parent) act[l][a] = 1;
+      }
+    }
+  }
+
+  // restriction of term l to the modes inside (in=true) or outside node a
+  std::vector<int> key(int l, int a, bool in) const {
+    std::vector<std::pair<int, int>> f;
+    for (int x = sop.ptr[l]; x < sop.ptr[l + 1]; ++x) {
+      int m = sop.mode[x];
+      if ((inside[a][m] != 0) == in) f.push_back({m, sop.op[x]});
+    }
+    std::stable_sort(f.begin(), f.end(),
+                     [](const std::pair<int, int>& u, const std::pair<int, int>& v) {
+                       return u.first < v.first;
+                     });
+    std::vector<int> k;
+    k.push_back(a);
+    k.push_back(in ? 1 : 0);
+    for (auto& p : f) k.push_back(p.first), k.push_back(p.second);
+    return k;
+  }
+
+  void layout() {
+    mats_cursor = 0;
+    P.rho_off.assign(n, 0);
+    P.rhoinv_off.assign(n, 0);
+    P.u_off.assign(n, 0);
+    P.s_off.assign(n, -1);
+    P.sinv_off.assign(n, -1);
+    P.d_off.assign(n, -1);
+    P.p_off.assign(n, -1);
+    P.m2_off.assign(n, -1);
+    for (int i = 0; i < n; ++i) {
+      int d = nd[i].dup();
+      P.rho_off[i] = alloc_mat(d);
+      P.rhoinv_off[i] = alloc_mat(d);
+      P.u_off[i] = alloc_mat(d);
+      P.max_eig_d = std::max(P.max_eig_d, d);
+      if (i != top) {
+        P.s_off[i] = alloc_mat(d);
+        P.sinv_off[i] = alloc_mat(d);
+        P.d_off[i] = alloc_mat(d);
+        P.p_off[i] = alloc_mat(d);
+        P.m2_off[i] = alloc_mat(d);
+      }
+    }
+    int dt = nd[top].dup();
+    P.energy_off = alloc_mat(dt);
+    P.stop_off = alloc_mat(dt);
+    int64_t ident_top = alloc_mat(dt);
+    P.identities.push_back({ident_top, dt});
+    P.identities.push_back({P.rho_off[top], dt});
+    // represent / mean-field slots
+    P.hslot.assign(L, std::vector<int64_t>(n, -1));
+    P.cslot.assign(L, std::vector<int64_t>(n, -1));
+    for (int l = 0; l < L; ++l)
+      for (int a = 0; a < n; ++a) {
+        if (!act[l][a]) continue;
+        if (a == top) {
+          P.hslot[l][a] = -2;  // the reference leaves the top's represent matrix at zero
+          P.cslot[l][a] = ident_top;
+          continue;
+        }
+        std::vector<int> kin = grouped ? key(l, a, true) : std::vector<int>{a, 1, l};
+        auto it = hslot_of_key.find(kin);
+        if (it == hslot_of_key.end()) {
+          int64_t o = alloc_mat(nd[a].dup());
+          hslot_of_key[kin] = o;
+          P.hslot[l][a] = o;
+        } else {
+          P.hslot[l][a] = it->second;
+        }
+        std::vector<int> kout = grouped ? key(l, a, false) : std::vector<int>{a, 0, l};
+        auto jt = cslot_of_key.find(kout);
+        if (jt == cslot_of_key.end()) {
+          int64_t o = alloc_mat(nd[a].dup());
+          cslot_of_key[kout] = o;
+          P.cslot[l][a] = o;
+        } else {
+          P.cslot[l][a] = jt->second;
+        }
+      }
+  }
+
+  // ---- stage emission ------------------------------------------------------
+  void emit_stage(int kind, int64_t t0, int64_t t1, int64_t tile0, int64_t tile1,
+                  const char* name) {
+    if (t1 <= t0) return;
+    const double f1 = P.stats.exec_flops;
+    Stage s;
+    s.flops = f1 - stage_flops_mark;
+    s.bytes = stage_bytes(kind, t0, t1);
+    stage_flops_mark = f1;
+    s.kind = kind;
+    s.first_task = t0;
+    s.n_tasks = t1 - t0;
+    s.first_tile = tile0;
+    s.n_tiles = tile1 - tile0;
+    s.name = name;
+    P.stages.push_back(s);
+  }
+
+  void add_mp(Ref in, Ref out, Ref h, double2 alpha, int node, int mode, bool diag) {
+    const NodeGeo& g = nd[node];
+    Plan::SMP t;
+    t.in = in;
+    t.out = out;
+    t.h = h;
+    t.alpha = alpha;
+    t.before = (int)g.before(mode);
+    t.a_in = g.shape[mode];
+    t.a_out = g.shape[mode];
+    t.after = (int)g.after(mode);
+    t.diag = diag ? 1 : 0;
+    int task = (int)P.mp.size();
+    P.mp.push_back(t);
+    int64_t outs = g.N;
+    for (int64_t s = 0; s < outs; s += kMpTile) P.mp_tiles.push_back(make_int2(task, (int)s));
+    P.stats.exec_flops += diag ? 6.0 * g.N : 8.0 * g.N * g.shape[mode];
+  }
+
+  void add_hp(Ref A, Ref B, Ref S, int node, int mode) {
+    const NodeGeo& g = nd[node];
+    Plan::SHP t;
+    t.A = A;
+    t.B = B;
+    t.S = S;
+    t.before = (int)g.before(mode);
+    t.a = g.shape[mode];
+    t.after = (int)g.after(mode);
+    int task = (int)P.hp.size();
+    P.hp.push_back(t);
+    for (int i0 = 0; i0 < t.a; i0 += kHpTile)
+      for (int j0 = 0; j0 < t.a; j0 += kHpTile) P.hp_tiles.push_back(make_int4(task, i0, j0, 0));
+    P.stats.exec_flops += 8.0 * g.N * g.shape[mode];
+  }
+
+  void add_acc(Ref out, bool alpha_param, double2 alpha, int node,
+               const std::vector<Plan::SAccTerm>& terms, bool add) {
+    const NodeGeo& g = nd[node];
+    Plan::SAcc t;
+    t.out = out;
+    t.alpha_param = alpha_param;
+    t.alpha = alpha;
+    t.d = g.dup();
+    t.rows = (int)(g.N / t.d);
+    t.first = (int)P.acc_terms.size();
+    t.count = (int)terms.size();
+    t.add = add ? 1 : 0;
+    for (auto& x : terms) P.acc_terms.push_back(x);
+    int task = (int)P.acc.size();
+    P.acc.push_back(t);
+    for (int r0 = 0; r0 < t.rows; r0 += kAccRows)
+      for (int j0 = 0; j0 < t.d; j0 += kAccCols) P.acc_tiles.push_back(make_int4(task, r0, j0, 0));
+    for (auto& x : terms) P.stats.exec_flops += (x.H.buf < 0 ? 2.0 : 8.0 * t.d) * g.N;
+  }
+
+  // Run a list of chains as one group (split into chunks by the scratch budget).
+  void run_items(std::vector<Item>& items, const char* name, std::vector<char>* acc_started) {
+    size_t i = 0;
+    while (i < items.size()) {
+      // chunk [i, j)
+      int64_t cursor = 0;
+      size_t j = i;
+      std::vector<std::pair<int64_t, int64_t>> bufs;  // per item buf0, buf1 offsets
+      while (j < items.size()) {
+        const Item& it = items[j];
+        int64_t need = 0;
+        int nb = (int)std::min<size_t>(2, it.ops.size());
+        need = nb * align_up(nd[it.node].N);
+        if (j > i && cursor + need > budget) break;
+        bufs.push_back({nb > 0 ? cursor : -1, nb > 1 ? cursor + align_up(nd[it.node].N) : -1});
+        cursor += need;
+        ++j;
+      }
+      P.scratch_size = std::max(P.scratch_size, cursor);
+      size_t maxops = 0;
+      for (size_t k = i; k < j; ++k) maxops = std::max(maxops, items[k].ops.size());
+      for (size_t pos = 0; pos < maxops; ++pos) {
+        int64_t t0 = (int64_t)P.mp.size(), tile0 = (int64_t)P.mp_tiles.size();
+        for (size_t k = i; k < j; ++k) {
+          const Item& it = items[k];
+          if (pos >= it.ops.size()) continue;
+          const auto& b = bufs[k - i];
+          Ref in = pos == 0 ? it.in : Ref{B_SCR, (pos - 1) % 2 == 0 ? b.first : b.second};
+          Ref out{B_SCR, pos % 2 == 0 ? b.first : b.second};
+          const COp& op = it.ops[pos];
+          add_mp(in, out, op.mat, op.alpha, it.node, op.mode, op.kind == 1);
+        }
+        emit_stage(ST_MP, t0, (int64_t)P.mp.size(), tile0, (int64_t)P.mp_tiles.size(), name);
+      }
+      // finals: hole products
+      {
+        int64_t t0 = (int64_t)P.hp.size(), tile0 = (int64_t)P.hp_tiles.size();
+        for (size_t k = i; k < j; ++k) {
+          const Item& it = items[k];
+          if (it.fin != 0) continue;
+          const auto& b = bufs[k - i];
+          size_t no = it.ops.size();
+          Ref x = no == 0 ? it.in : Ref{B_SCR, (no - 1) % 2 == 0 ? b.first : b.second};
+          add_hp(psi(it.node), x, it.S, it.node, it.hp_mode);
+        }
+        emit_stage(ST_HP, t0, (int64_t)P.hp.size(), tile0, (int64_t)P.hp_tiles.size(), name);
+      }
+      // finals: accumulation per node
+      {
+        int64_t t0 = (int64_t)P.acc.size(), tile0 = (int64_t)P.acc_tiles.size();
+        std::map<int, std::vector<Plan::SAccTerm>> per_node;
+        for (size_t k = i; k < j; ++k) {
+          const Item& it = items[k];
+          if (it.fin != 1) continue;
+          const auto& b = bufs[k - i];
+          size_t no = it.ops.size();
+          Ref x = no == 0 ? it.in : Ref{B_SCR, (no - 1) % 2 == 0 ? b.first : b.second};
+          per_node[it.acc_node].push_back(Plan::SAccTerm{it.accH, x});
+        }
+        for (auto& kv : per_node) {
+          bool add = (*acc_started)[kv.first] != 0;
+          add_acc(hphi(kv.first), false, c2(1.0, 0.0), kv.first, kv.second, add);
+          (*acc_started)[kv.first] = 1;
+        }
+        emit_stage(ST_ACC, t0, (int64_t)P.acc.size(), tile0, (int64_t)P.acc_tiles.size(), name);
+      }
+      i = j;
+    }
+  }
+
+  void stage_density() {
+    int maxdepth = 0;
+    for (auto& g : nd) maxdepth = std::max(maxdepth, g.depth);
+    for (int d = 1; d <= maxdepth; ++d) {
+      std::vector<Item> items;
+      for (int a = 0; a < n; ++a) {
+        if (nd[a].depth != d) continue;
+        int p = nd[a].parent;
+        Item it;
+        it.node = p;
+        it.in = psi(p);
+        if (!nd[p].top())
+          it.ops.push_back(COp{0, nd[p].last(), mat(P.rho_off[p]), c2(1, 0)});
+        it.fin = 0;
+        it.S = mat(P.rho_off[a]);
+        it.hp_mode = nd[a].child_idx;
+        items.push_back(it);
+      }
+      run_items(items, "density", nullptr);
+    }
+  }
+
+  void stage_inverse() {
+    int64_t t0 = (int64_t)P.eig.size();
+    for (int a = 0; a < n; ++a) {
+      Plan::SEig e;
+      e.rho = mat(P.rho_off[a]);
+      e.rhoinv = mat(P.rhoinv_off[a]);
+      e.U = mat(P.u_off[a]);
+      e.d = nd[a].dup();
+      P.eig.push_back(e);
+    }
+    emit_stage(ST_EIG, t0, (int64_t)P.eig.size(), t0, (int64_t)P.eig.size(), "inverse");
+  }
+
+  // operators of term l at node a (represent / apply chain body)
+  std::vector<COp> body(int l, int a, double2 alpha) const {
+    std::vector<COp> o;
+    const NodeGeo& g = nd[a];
+    if (g.bottom()) {
+      for (int f = sop.ptr[l]; f < sop.ptr[l + 1]; ++f) {
+        if (sop.mode[f] != g.leaf_mode) continue;
+        int op = sop.op[f];
+        o.push_back(COp{ops.kind[op] == 0 ? 0 : 1, 0, opref(op), c2(1, 0)});
+      }
+    } else {
+      for (size_t k = 0; k < g.children.size(); ++k) {
+        int c = g.children[k];
+        if (!act[l][c]) continue;
+        o.push_back(COp{0, (int)k, mat(P.hslot[l][c]), c2(1, 0)});
+      }
+    }
+    if (!o.empty()) o[0].alpha = alpha;
+    return o;
+  }
+
+  void stage_represent() {
+    int maxh = nd[top].height;
+    for (int h = 0; h < maxh; ++h) {
+      std::vector<Item> items;
+      std::set<int64_t> done;
+      for (int a = 0; a < n; ++a) {
+        if (nd[a].height != h || a == top) continue;
+        for (int l = 0; l < L; ++l) {
+          if (!act[l][a]) continue;
+          int64_t slot = P.hslot[l][a];
+          if (!done.insert(slot).second) continue;
+          Item it;
+          it.node = a;
+          it.in = psi(a);
+          it.ops = body(l, a, c2(1, 0));
+          it.fin = 0;
+          it.S = mat(slot);
+          it.hp_mode = nd[a].last();
+          items.push_back(it);
+        }
+      }
+      P.stats.rep_chains += (int64_t)items.size();
+      run_items(items, "represent", nullptr);
+    }
+  }
+
+  void stage_meanfield() {
+    int maxdepth = 0;
+    for (auto& g : nd) maxdepth = std::max(maxdepth, g.depth);
+    for (int d = 1; d <= maxdepth; ++d) {
+      std::vector<Item> items;
+      std::set<int64_t> done;
+      for (int a = 0; a < n; ++a) {
+        if (nd[a].depth != d) continue;
+        int p = nd[a].parent;
+        for (int l = 0; l < L; ++l) {
+          if (!act[l][a]) continue;
+          int64_t slot = P.cslot[l][a];
+          if (!done.insert(slot).second) continue;
+          Item it;
+          it.node = p;
+          it.in = psi(p);
+          const NodeGeo& gp = nd[p];
+          for (size_t k = 0; k < gp.children.size(); ++k) {
+            int c = gp.children[k];
+            if ((int)k == nd[a].child_idx || !act[l][c]) continue;
+            it.ops.push_back(COp{0, (int)k, mat(P.hslot[l][c]), c2(1, 0)});
+          }
+          if (!gp.top()) it.ops.push_back(COp{0, gp.last(), mat(P.cslot[l][p]), c2(1, 0)});
+          it.fin = 0;
+          it.S = mat(slot);
+          it.hp_mode = nd[a].child_idx;
+          items.push_back(it);
+        }
+      }
+      P.stats.mf_chains += (int64_t)items.size();
+      run_items(items, "meanfield", nullptr);
+    }
+  }
+
+  void stage_apply() {
+    // group terms per node by their inside restriction; G_g = sum_l c_l H_l
+    std::vector<Item> items;
+    int64_t lin0 = (int64_t)P.lin.size();
+    for (int a = 0; a < n; ++a) {
+      std::map<std::vector<int>, std::vector<int>> groups;
+      std::vector<std::vector<int>> order;
+      for (int l = 0; l < L; ++l) {
+        if (!act[l][a]) continue;
+        std::vector<int> k = grouped ? key(l, a, true) : std::vector<int>{a, 1, l};
+        auto it = groups.find(k);
+        if (it == groups.end()) {
+          groups[k] = {l};
+          order.push_back(k);
+        } else {
+          it->second.push_back(l);
+        }
+      }
+      int d = nd[a].dup();
+      for (auto& k : order) {
+        const auto& terms = groups[k];
+        int64_t g = alloc_mat(d);
+        Plan::SLin lt;
+        lt.out = mat(g);
+        lt.d = d;
+        lt.first = (int)P.lin_terms.size();
+        lt.count = (int)terms.size();
+        for (int l : terms) P.lin_terms.push_back(Plan::SLinTerm{sop.coeff[l], mat(P.cslot[l][a])});
+        P.lin.push_back(lt);
+        Item it;
+        it.node = a;
+        it.in = psi(a);
+        it.ops = body(terms[0], a, c2(1, 0));
+        it.fin = 1;
+        it.acc_node = a;
+        it.accH = mat(g);
+        items.push_back(it);
+      }
+    }
+    emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "apply-sum");
+    P.stats.app_chains += (int64_t)items.size();
+    std::vector<char> started(n, 0);
+    run_items(items, "apply", &started);
+    for (int a = 0; a < n; ++a)
+      if (!started[a]) throw std::runtime_error("a node has no active SOP term");
+  }
+
+  void stage_final() {
+    // overlaps S = Phi^dag Phi and D = Phi^dag (H Phi) of every node
+    int64_t t0 = (int64_t)P.hp.size(), tile0 = (int64_t)P.hp_tiles.size();
+    for (int a = 0; a < n; ++a) {
+      if (a == top) {
+        add_hp(psi(a), hphi(a), mat(P.energy_off), a, nd[a].last());
+        add_hp(psi(a), psi(a), mat(P.stop_off), a, nd[a].last());
+      } else {
+        add_hp(psi(a), psi(a), mat(P.s_off[a]), a, nd[a].last());
+        add_hp(psi(a), hphi(a), mat(P.d_off[a]), a, nd[a].last());
+      }
+    }
+    emit_stage(ST_HP, t0, (int64_t)P.hp.size(), tile0, (int64_t)P.hp_tiles.size(), "overlaps");
+    int64_t p0 = (int64_t)P.proj.size();
+    for (int a = 0; a < n; ++a) {
+      if (a == top) continue;
+      Plan::SProj pj;
+      pj.S = mat(P.s_off[a]);
+      pj.D = mat(P.d_off[a]);
+      pj.rhoinv = mat(P.rhoinv_off[a]);
+      pj.Sinv = mat(P.sinv_off[a]);
+      pj.P = mat(P.p_off[a]);
+      pj.M2 = mat(P.m2_off[a]);
+      pj.d = nd[a].dup();
+      P.proj.push_back(pj);
+      P.stats.exec_flops += 3 * 8.0 * pj.d * pj.d * pj.d;
+    }
+    emit_stage(ST_PROJ, p0, (int64_t)P.proj.size(), p0, (int64_t)P.proj.size(), "projector");
+    // dPsi = -i*phase * (H Phi - Phi P) rhoinv^T  (non-top);  -i*phase * H Phi (top)
+    int64_t a0 = (int64_t)P.acc.size(), atile0 = (int64_t)P.acc_tiles.size();
+    for (int a = 0; a < n; ++a) {
+      std::vector<Plan::SAccTerm> terms;
+      if (a == top) {
+        terms.push_back(Plan::SAccTerm{Ref{-1, 0}, hphi(a)});
+      } else {
+        terms.push_back(Plan::SAccTerm{mat(P.rhoinv_off[a]), hphi(a)});
+        terms.push_back(Plan::SAccTerm{mat(P.m2_off[a]), psi(a)});
+      }
+      add_acc(dpsi(a), true, c2(0, 0), a, terms, false);
+    }
+    emit_stage(ST_ACC, a0, (int64_t)P.acc.size(), atile0, (int64_t)P.acc_tiles.size(), "derivative");
+    P.mats_size = mats_cursor;
+  }
+
+  // Flops of the reference call sequence (independent of this plan):
+  // mode product 8*N*a, hole product 8*N*a, diagonal leaf op 6*N, complex
+  // scale 6*N, accumulate 2*N, projector 24*N*d + 2*N, rho^-1 8*N*d.
+  void count_reference_flops() {
+    double F = 0;
+    for (int a = 0; a < n; ++a) {
+      if (a == top) continue;
+      const NodeGeo& p = nd[nd[a].parent];
+      F += 8.0 * p.N * p.dup() + 8.0 * p.N * nd[a].dup();
+    }
+    auto body_flops = [&](int l, int a) {
+      const NodeGeo& g = nd[a];
+      double f = 0;
+      if (g.bottom()) {
+        for (int x = sop.ptr[l]; x < sop.ptr[l + 1]; ++x)
+          if (sop.mode[x] == g.leaf_mode) f += ops.kind[sop.op[x]] == 0 ? 8.0 * g.N * g.shape[0] : 6.0 * g.N;
+      } else {
+        for (size_t k = 0; k < g.children.size(); ++k)
+          if (act[l][g.children[k]]) f += 8.0 * g.N * g.shape[k];
+      }
+      return f;
+    };
+    for (int l = 0; l < L; ++l)
+      for (int a = 0; a < n; ++a) {
+        if (!act[l][a]) continue;
+        const NodeGeo& g = nd[a];
+        double app = 6.0 * g.N + body_flops(l, a) + (a == top ? 2.0 * g.N : 8.0 * g.N * g.dup() + 2.0 * g.N);
+        F += app;
+        if (a == top) {
+          F += app;  // Expectation repeats Apply at the top
+          continue;
+        }
+        F += body_flops(l, a) + 8.0 * g.N * g.dup();  // represent
+        const NodeGeo& p = nd[g.parent];
+        for (size_t k = 0; k < p.children.size(); ++k)
+          if ((int)k != g.child_idx && act[l][p.children[k]]) F += 8.0 * p.N * p.shape[k];
+        if (!p.top()) F += 8.0 * p.N * p.dup();
+        F += 8.0 * p.N * g.dup();  // mean field
+      }
+    for (int a = 0; a < n; ++a) {
+      const NodeGeo& g = nd[a];
+      if (a == top) {
+        F += 6.0 * g.N + 8.0 * g.N * g.dup();
+      } else {
+        F += 24.0 * g.N * g.dup() + 2.0 * g.N + 8.0 * g.N * g.dup() + 6.0 * g.N;
+      }
+    }
+    P.stats.ref_flops = F;
+  }
+};
+
+}  // namespace
+
+std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
+                       const SopDesc& sop, int flavour, int64_t scratch_budget_elems) {
+  plan = Plan();
+  try {
+    Builder b(plan, nodes, ops, sop, flavour, scratch_budget_elems);
+    b.run();
+  } catch (const std::exception& e) {
+    return e.what();
+  }
+  plan.ops_size = (int64_t)ops.data.size() / 2;
+  return "";
+}
+
+}  // namespace qt

@@ -1,0 +1,222 @@
+// qt_plan_export.cpp -- host-only view of the sweep plan (no CUDA calls).
+//
+// Builds the same plan qt_prepare builds and hands its symbolic task tables
+// (buffer id + element offset instead of device pointers) to the caller.
+// The CPU test suite interprets these tables with numpy to check the
+// planner's schedule on machines without a GPU.  Compiled with g++ into
+// libqtplan.so, separate from the CUDA library.
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "qt_internal.h"
+
+namespace {
+struct Handle {
+  qt::Plan plan;
+};
+
+void put_ref(std::vector<int64_t>& v, const qt::Ref& r) {
+  v.push_back(r.buf);
+  v.push_back(r.off);
+}
+}  // namespace
+
+extern "C" {
+
+void* qtp_build(int n_nodes, const int* order, const int* dims, const int* parent, const int* child_idx,
+                const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
+                const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
+                const int* term_ptr, const int* term_mode, const int* term_op, int flavour,
+                int64_t budget, char* err, int errlen) {
+  std::vector<qt::NodeGeo> nodes(n_nodes);
+  int p = 0;
+  for (int i = 0; i < n_nodes; ++i) {
+    for (int k = 0; k < order[i]; ++k) nodes[i].shape.push_back(dims[p + k]);
+    p += order[i];
+    nodes[i].parent = parent[i];
+    nodes[i].child_idx = child_idx[i];
+    nodes[i].leaf_mode = leaf_mode[i];
+  }
+  // same operator repacking as qt_sop_upload
+  qt::OpTable ops;
+  int64_t cur = 0;
+  for (int i = 0; i < n_ops; ++i) {
+    int64_t n = op_kind[i] == 0 ? (int64_t)op_dim[i] * op_dim[i] : op_dim[i];
+    ops.kind.push_back(op_kind[i]);
+    ops.dim.push_back(op_dim[i]);
+    ops.off.push_back(cur);
+    ops.data.resize(2 * (cur + n), 0.0);
+    std::memcpy(ops.data.data() + 2 * cur, op_data + 2 * op_off[i], sizeof(double) * 2 * n);
+    cur = (cur + n + 15) / 16 * 16;
+  }
+  ops.data.resize(2 * (cur > 16 ? cur : 16), 0.0);
+  qt::SopDesc s;
+  s.n_terms = n_terms;
+  for (int l = 0; l < n_terms; ++l) s.coeff.push_back(make_double2(coeff[2 * l], coeff[2 * l + 1]));
+  s.ptr.assign(term_ptr, term_ptr + n_terms + 1);
+  s.mode.assign(term_mode, term_mode + s.ptr[n_terms]);
+  s.op.assign(term_op, term_op + s.ptr[n_terms]);
+  Handle* h = new Handle();
+  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, budget);
+  if (!msg.empty()) {
+    if (err && errlen > 0) {
+      std::strncpy(err, msg.c_str(), errlen - 1);
+      err[errlen - 1] = 0;
+    }
+    delete h;
+    return nullptr;
+  }
+  h->plan.ops_size = (int64_t)ops.data.size() / 2;
+  return h;
+}
+
+void qtp_free(void* h) { delete (Handle*)h; }
+
+// Table ids: 0 stages, 1 mp, 2 hp, 3 acc, 4 acc_terms, 5 lin, 6 lin_terms,
+// 7 eig, 8 proj, 9 sizes, 10 identities, 11 rho_off, 12 rhoinv_off,
+// 13 hslot, 14 cslot, 15 mp alphas, 16 lin coeffs, 17 stats (doubles).
+// qtp_size returns the element count, qtp_get copies.
+static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vector<double>& dv) {
+  v.clear();
+  dv.clear();
+  switch (what) {
+    case 0:
+      for (auto& s : P.stages) {
+        v.push_back(s.kind);
+        v.push_back(s.first_task);
+        v.push_back(s.n_tasks);
+        v.push_back(s.first_tile);
+        v.push_back(s.n_tiles);
+      }
+      break;
+    case 1:
+      for (auto& t : P.mp) {
+        put_ref(v, t.in);
+        put_ref(v, t.out);
+        put_ref(v, t.h);
+        v.push_back(t.before);
+        v.push_back(t.a_in);
+        v.push_back(t.a_out);
+        v.push_back(t.after);
+        v.push_back(t.diag);
+      }
+      break;
+    case 2:
+      for (auto& t : P.hp) {
+        put_ref(v, t.A);
+        put_ref(v, t.B);
+        put_ref(v, t.S);
+        v.push_back(t.before);
+        v.push_back(t.a);
+        v.push_back(t.after);
+      }
+      break;
+    case 3:
+      for (auto& t : P.acc) {
+        put_ref(v, t.out);
+        v.push_back(t.alpha_param ? 1 : 0);
+        v.push_back(t.rows);
+        v.push_back(t.d);
+        v.push_back(t.first);
+        v.push_back(t.count);
+        v.push_back(t.add);
+      }
+      break;
+    case 4:
+      for (auto& t : P.acc_terms) {
+        put_ref(v, t.H);
+        put_ref(v, t.X);
+      }
+      break;
+    case 5:
+      for (auto& t : P.lin) {
+        put_ref(v, t.out);
+        v.push_back(t.d);
+        v.push_back(t.first);
+        v.push_back(t.count);
+      }
+      break;
+    case 6:
+      for (auto& t : P.lin_terms) put_ref(v, t.M);
+      break;
+    case 7:
+      for (auto& t : P.eig) {
+        put_ref(v, t.rho);
+        put_ref(v, t.rhoinv);
+        put_ref(v, t.U);
+        v.push_back(t.d);
+      }
+      break;
+    case 8:
+      for (auto& t : P.proj) {
+        put_ref(v, t.S);
+        put_ref(v, t.D);
+        put_ref(v, t.rhoinv);
+        put_ref(v, t.Sinv);
+        put_ref(v, t.P);
+        put_ref(v, t.M2);
+        v.push_back(t.d);
+      }
+      break;
+    case 9:
+      v = {P.psi_arena, P.mats_size, P.scratch_size, P.ops_size, P.energy_off, P.stop_off};
+      break;
+    case 10:
+      for (auto& id : P.identities) {
+        v.push_back(id.first);
+        v.push_back(id.second);
+      }
+      break;
+    case 11:
+      v = P.rho_off;
+      break;
+    case 12:
+      v = P.rhoinv_off;
+      break;
+    case 13:
+    case 14: {
+      const auto& sl = what == 13 ? P.hslot : P.cslot;
+      for (auto& row : sl)
+        for (auto x : row) v.push_back(x);
+      break;
+    }
+    case 15:
+      for (auto& t : P.mp) {
+        dv.push_back(t.alpha.x);
+        dv.push_back(t.alpha.y);
+      }
+      break;
+    case 16:
+      for (auto& t : P.lin_terms) {
+        dv.push_back(t.c.x);
+        dv.push_back(t.c.y);
+      }
+      break;
+    case 17:
+      dv = {P.stats.ref_flops, P.stats.exec_flops, (double)P.stages.size(),
+            (double)P.stats.rep_chains, (double)P.stats.mf_chains, (double)P.stats.app_chains};
+      break;
+    default:
+      break;
+  }
+}
+
+int64_t qtp_size(void* h, int what) {
+  std::vector<int64_t> v;
+  std::vector<double> dv;
+  table(((Handle*)h)->plan, what, v, dv);
+  return what >= 15 ? (int64_t)dv.size() : (int64_t)v.size();
+}
+
+void qtp_get(void* h, int what, void* out) {
+  std::vector<int64_t> v;
+  std::vector<double> dv;
+  table(((Handle*)h)->plan, what, v, dv);
+  if (what >= 15)
+    std::memcpy(out, dv.data(), dv.size() * sizeof(double));
+  else
+    std::memcpy(out, v.data(), v.size() * sizeof(int64_t));
+}
+
+}  // extern "C"

@@ -1,0 +1,40 @@
+"""Shared comparison helpers of the test suite."""
+import numpy as np
+
+
+def rel_err(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    s = np.abs(b).max()
+    return float(np.abs(a - b).max() / (s if s > 0 else 1.0))
+
+
+def rho_weighted(tree, dpsi, rho):
+    """dPsi of every non-top node multiplied back by its density matrix
+    (C[r, m] = sum_n rho(m, n) dPsi[r, n]), undoing the regularised inverse
+    whose conditioning amplifies rounding noise; the top node unchanged.
+    Returns the concatenation in node order."""
+    off = tree.offsets()
+    ro = 0
+    out = []
+    for n in tree.nodes:
+        d = n.d_up
+        R = rho[ro:ro + d * d].reshape((d, d), order="F")
+        ro += d * d
+        x = dpsi[off[n.address]:off[n.address + 1]].reshape((-1, d), order="F")
+        out.append((x if n.is_top else x @ R.T).ravel(order="F"))
+    return np.concatenate(out)
+
+
+def rho_condition(tree, rho):
+    ro = 0
+    worst = 1.0
+    for n in tree.nodes:
+        d = n.d_up
+        R = rho[ro:ro + d * d].reshape((d, d), order="F")
+        ro += d * d
+        if n.is_top:
+            continue
+        w = np.linalg.eigvalsh(0.5 * (R + R.conj().T))
+        worst = max(worst, w.max() / max(w.min(), 1e-300))
+    return worst

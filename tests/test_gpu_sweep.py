@@ -1,0 +1,130 @@
+"""Full H.Psi sweeps on the GPU through the C ABI against the oracle.
+
+Tolerances: every contraction result (density matrices, represent and
+mean-field matrices, energy) within 1e-12 relative; the derivative compared
+after multiplying each non-top node back by its density matrix (undoing the
+regularised inverse, whose condition number amplifies rounding noise),
+within 1e-12 relative; the raw derivative within 1e-13 x cond(rho)."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import rel_err, rho_condition, rho_weighted
+from qutree_gb300 import qtgpu
+from qutree_gb300.model import (MLO, OP_DENSE, SOP, HOBasis, OperatorTable, balanced_tree,
+                                config_problem, coupled_oscillators, hartree_wavefunction,
+                                random_wavefunction)
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+
+def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
+    flat = psi.flat()
+    r = O.derivative(tree, sop, flat, eps=eps, phase=phase)
+    hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, eps=eps)
+    try:
+        dpsi = qtgpu.Derivative(hrep, flat, phase)
+        e = hrep.energy()
+        assert abs(e - r.energy) <= TOL * max(1.0, abs(r.energy))
+        rho = hrep.matrices(qtgpu.QT_MAT_RHO)
+        assert rel_err(rho, r.rho) <= TOL
+        assert rel_err(hrep.matrices(qtgpu.QT_MAT_HMAT), r.hmat) <= TOL
+        assert rel_err(hrep.matrices(qtgpu.QT_MAT_HCON), r.hcon) <= TOL
+        rw = rel_err(rho_weighted(tree, dpsi, r.rho), rho_weighted(tree, r.dpsi, r.rho))
+        assert rw <= TOL
+        cond = rho_condition(tree, r.rho)
+        assert rel_err(dpsi, r.dpsi) <= 1e-13 * max(cond, 10.0)
+        ri = hrep.matrices(qtgpu.QT_MAT_RHOINV)
+        assert rel_err(ri, r.rhoinv) <= 1e-13 * max(cond, 10.0)
+        # second call on the same graph reproduces bit for bit
+        hrep.derivative(phase)
+        assert np.array_equal(hrep.dpsi(), dpsi)
+        return hrep.stats()
+    finally:
+        hrep.close()
+
+
+@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED])
+def test_sweep_cfg0(flavour):
+    tree, sop, psi = config_problem(0)
+    _compare(tree, sop, psi, flavour)
+
+
+@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED])
+def test_sweep_cfg4(flavour):
+    tree, sop, psi = config_problem(4)
+    _compare(tree, sop, psi, flavour)
+
+
+@pytest.mark.parametrize("leaves,p,b,seed", [(5, 4, 3, 1), (7, 5, 4, 2), (12, 3, 2, 3), (16, 16, 12, 4),
+                                             (3, 8, 8, 5), (2, 6, 6, 6)])
+def test_sweep_random_trees(leaves, p, b, seed):
+    tree = balanced_tree(leaves, p, b)
+    rng = np.random.default_rng(seed)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
+    psi = random_wavefunction(tree, seed)
+    for fl in (0, 1):
+        _compare(tree, sop, psi, fl, phase=np.exp(0.3j))
+
+
+def test_sweep_known_answer_half_identity():
+    # tests/test_SparseMatrixTree.cpp:54-87 on the GPU: represent = 0.5 I / 0.25 I,
+    # mean field = diag(0.5, 0) / diag(1, 0) / 1 for the Hartree-product state.
+    tree = balanced_tree(8, 2, 2)
+    basis = HOBasis(2, omega=1.0, r0=0.0, wfr0=1.0, wfomega=0.0)
+    psi = hartree_wavefunction(tree, 1993, lambda m: basis)
+    ops = OperatorTable()
+    x = ops.add("x", OP_DENSE, 0.5 * np.eye(2))
+    sop = SOP(ops)
+    sop.push_back(MLO([(0, x), (3, x)]), 1.0)
+    hrep = qtgpu.HamiltonianRepresentation(sop, tree)
+    try:
+        qtgpu.Derivative(hrep, psi.flat())
+        hm = hrep.matrices(qtgpu.QT_MAT_HMAT).reshape(-1, 4)
+        hc = hrep.matrices(qtgpu.QT_MAT_HCON)
+        half = (0.5 * np.eye(2)).ravel(order="F")
+        for k in range(4):
+            assert np.abs(hm[k] - half).max() < 1e-12
+        assert np.abs(hm[4] - 0.5 * half).max() < 1e-12
+        assert np.abs(hm[5][:1]).max() == 0.0
+        x1 = np.array([0.5, 0, 0, 0])
+        for k in range(4):
+            assert np.abs(hc[4 * k:4 * k + 4] - x1).max() < 1e-12
+        assert np.abs(hc[16:20] - 2 * x1).max() < 1e-12
+        assert abs(hc[20] - 1.0) < 1e-12
+    finally:
+        hrep.close()
+
+
+def test_multi_factor_terms():
+    tree = balanced_tree(6, 4, 3)
+    ops = OperatorTable()
+    b = HOBasis(4, omega=1.0)
+    kin = ops.add("k", OP_DENSE, b.kin)
+    x = ops.add("x", 1, b.x.astype(complex))
+    rng = np.random.default_rng(5)
+    m = ops.add("m", OP_DENSE, rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    sop = SOP(ops)
+    sop.push_back(MLO([(0, kin), (0, x)]), 0.7)
+    sop.push_back(MLO([(0, x), (0, kin)]), 0.3 - 0.2j)
+    sop.push_back(MLO([(1, m), (3, x), (5, kin)]), 0.11)
+    sop.push_back(MLO([(2, m), (2, m)]), 0.5)
+    for k in range(6):
+        sop.push_back(MLO([(k, kin)]), 1.0)
+    psi = random_wavefunction(tree, 9)
+    for fl in (0, 1):
+        _compare(tree, sop, psi, fl)
+
+
+def test_errors_are_reported_not_fatal():
+    tree, sop, psi = config_problem(0)
+    hrep = qtgpu.HamiltonianRepresentation(sop, tree)
+    try:
+        with pytest.raises(qtgpu.QtError, match="QT_ERR_STATE"):
+            hrep.dpsi()  # no sweep yet
+        hrep.upload(psi)
+        hrep.derivative()
+        assert np.isfinite(hrep.energy())
+    finally:
+        hrep.close()

@@ -1,0 +1,92 @@
+"""The sweep planner on the CPU: the plan libqtgpu executes, interpreted with
+numpy (tests/plan_emulator.py) and compared with the oracle."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import rel_err, rho_weighted
+from plan_emulator import PlanView
+from qutree_gb300.model import (MLO, OP_DENSE, SOP, HOBasis, OperatorTable, balanced_tree,
+                                config_problem, config_tree_sop, coupled_oscillators,
+                                random_wavefunction)
+
+
+def _check(tree, sop, psi, flavour, budget=1 << 28, tol=1e-12):
+    flat = psi.flat()
+    r = O.derivative(tree, sop, flat)
+    pv = PlanView(tree, sop, flavour, budget)
+    pv.run(flat)
+    h00, s00 = pv.energy_parts()
+    assert abs(h00.real / s00.real - r.energy) < tol * max(1, abs(r.energy))
+    assert rel_err(pv.sparse(0), r.hmat) < tol
+    assert rel_err(pv.sparse(1), r.hcon) < tol
+    assert rel_err(rho_weighted(tree, pv.dpsi(), r.rho), rho_weighted(tree, r.dpsi, r.rho)) < tol
+    return pv
+
+
+@pytest.mark.parametrize("flavour", [0, 1])
+def test_plan_cfg0(flavour):
+    tree, sop, psi = config_problem(0)
+    pv = _check(tree, sop, psi, flavour)
+    if flavour == 1:
+        assert pv.stats["exec_flops"] < pv.stats["ref_flops"]
+
+
+@pytest.mark.parametrize("flavour", [0, 1])
+def test_plan_small_budget_chunks(flavour):
+    # a tiny scratch budget forces every level into many chunks
+    tree, sop, psi = config_problem(0)
+    _check(tree, sop, psi, flavour, budget=200)
+
+
+@pytest.mark.parametrize("leaves,p,b,seed", [(5, 4, 3, 1), (7, 5, 4, 2), (12, 3, 2, 3), (9, 6, 5, 4)])
+@pytest.mark.parametrize("flavour", [0, 1])
+def test_plan_random_trees(leaves, p, b, seed, flavour):
+    tree = balanced_tree(leaves, p, b)
+    rng = np.random.default_rng(seed)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
+    psi = random_wavefunction(tree, seed)
+    _check(tree, sop, psi, flavour)
+
+
+def test_plan_multi_factor_terms():
+    # several factors on the same leaf (applied in list order) and 3-body terms
+    tree = balanced_tree(6, 4, 3)
+    ops = OperatorTable()
+    b = HOBasis(4, omega=1.0)
+    kin = ops.add("k", OP_DENSE, b.kin)
+    x = ops.add("x", 1, b.x.astype(complex))
+    rng = np.random.default_rng(5)
+    m = ops.add("m", OP_DENSE, rng.standard_normal((4, 4)) + 1j * rng.standard_normal((4, 4)))
+    sop = SOP(ops)
+    sop.push_back(MLO([(0, kin), (0, x)]), 0.7)
+    sop.push_back(MLO([(0, x), (0, kin)]), 0.3 - 0.2j)
+    sop.push_back(MLO([(1, m), (3, x), (5, kin)]), 0.11)
+    sop.push_back(MLO([(2, m), (2, m)]), 0.5)
+    for k in range(6):
+        sop.push_back(MLO([(k, kin)]), 1.0)
+    psi = random_wavefunction(tree, 9)
+    for fl in (0, 1):
+        _check(tree, sop, psi, fl)
+
+
+def test_plan_reference_flops_cfg1():
+    # the reference call sequence of one cfg1 sweep (represent, mean fields,
+    # Apply, projector, Expectation): ~0.89 TFLOP
+    tree, sop = config_tree_sop(1)
+    pv = PlanView(tree, sop, 0)
+    assert 0.85e12 < pv.stats["ref_flops"] < 0.95e12
+    pv1 = PlanView(tree, sop, 1)
+    assert pv1.stats["exec_flops"] < 0.6 * pv.stats["exec_flops"]
+    assert pv1.stats["ref_flops"] == pv.stats["ref_flops"]
+
+
+def test_plan_rejects_bad_input():
+    tree, sop = config_tree_sop(0)
+    # operator dimension that does not match the leaf
+    ops = OperatorTable()
+    bad = ops.add("bad", OP_DENSE, np.eye(3))
+    s = SOP(ops)
+    s.push_back(MLO([(0, bad)]), 1.0)
+    with pytest.raises(ValueError, match="operator dim"):
+        PlanView(tree, s, 0)
