@@ -617,8 +617,11 @@ class Builder {
     P.stats.app_chains += (int64_t)items.size();
     std::vector<char> started(n, 0);
     run_items(items, "apply", &started);
+    // nodes no SOP term reaches: H Phi = 0 there (Apply's empty sum)
+    int64_t t0 = (int64_t)P.acc.size(), tile0 = (int64_t)P.acc_tiles.size();
     for (int a = 0; a < n; ++a)
-      if (!started[a]) throw std::runtime_error("a node has no active SOP term");
+      if (!started[a]) add_acc(hphi(a), false, c2(1.0, 0.0), a, {}, false);
+    emit_stage(ST_ACC, t0, (int64_t)P.acc.size(), tile0, (int64_t)P.acc_tiles.size(), "apply-zero");
   }
 
   void stage_final() {

@@ -81,13 +81,15 @@ def test_sweep_known_answer_half_identity():
     hrep = qtgpu.HamiltonianRepresentation(sop, tree)
     try:
         qtgpu.Derivative(hrep, psi.flat())
-        hm = hrep.matrices(qtgpu.QT_MAT_HMAT).reshape(-1, 4)
+        hmat = hrep.matrices(qtgpu.QT_MAT_HMAT)
         hc = hrep.matrices(qtgpu.QT_MAT_HCON)
+        assert hmat.size == 5 * 4 + 1  # five 2x2 matrices and the top's 1x1
+        hm = hmat[:20].reshape(5, 4)
         half = (0.5 * np.eye(2)).ravel(order="F")
         for k in range(4):
             assert np.abs(hm[k] - half).max() < 1e-12
         assert np.abs(hm[4] - 0.5 * half).max() < 1e-12
-        assert np.abs(hm[5][:1]).max() == 0.0
+        assert hmat[20] == 0.0  # the top is not represented
         x1 = np.array([0.5, 0, 0, 0])
         for k in range(4):
             assert np.abs(hc[4 * k:4 * k + 4] - x1).max() < 1e-12
@@ -113,6 +115,20 @@ def test_multi_factor_terms():
     for k in range(6):
         sop.push_back(MLO([(k, kin)]), 1.0)
     psi = random_wavefunction(tree, 9)
+    for fl in (0, 1):
+        _compare(tree, sop, psi, fl)
+
+
+def test_nodes_without_terms():
+    tree = balanced_tree(8, 4, 3)
+    ops = OperatorTable()
+    b = HOBasis(4, omega=1.0)
+    kin = ops.add("k", OP_DENSE, b.kin)
+    x = ops.add("x", 1, b.x.astype(complex))
+    sop = SOP(ops)
+    sop.push_back(MLO([(0, kin)]), 1.0)
+    sop.push_back(MLO([(1, x), (2, x)]), 0.3)
+    psi = random_wavefunction(tree, 21)
     for fl in (0, 1):
         _compare(tree, sop, psi, fl)
 

@@ -70,6 +70,21 @@ def test_plan_multi_factor_terms():
         _check(tree, sop, psi, fl)
 
 
+@pytest.mark.parametrize("flavour", [0, 1])
+def test_plan_nodes_without_terms(flavour):
+    # an SOP acting on a few leaves only: the other nodes get H Phi = 0
+    tree = balanced_tree(8, 4, 3)
+    ops = OperatorTable()
+    b = HOBasis(4, omega=1.0)
+    kin = ops.add("k", OP_DENSE, b.kin)
+    x = ops.add("x", 1, b.x.astype(complex))
+    sop = SOP(ops)
+    sop.push_back(MLO([(0, kin)]), 1.0)
+    sop.push_back(MLO([(1, x), (2, x)]), 0.3)
+    psi = random_wavefunction(tree, 21)
+    _check(tree, sop, psi, flavour)
+
+
 def test_plan_reference_flops_cfg1():
     # the reference call sequence of one cfg1 sweep (represent, mean fields,
     # Apply, projector, Expectation): ~0.89 TFLOP
