@@ -177,6 +177,30 @@ int qt_hole_product(qt_ctx* ctx, void* S, const void* A, const void* B, int64_t 
 int qt_last_mode_product(qt_ctx* ctx, void* C, const void* A, const void* B,
                          int64_t last_before, int64_t active, int add);
 
+/* Regularised inverses rhoinv[b] = U diag(1/(w + eps*exp(-w/eps))) U^dagger
+ * of n_mats Hermitian d x d matrices rho[b] (column-major, back to back) that
+ * already live on the device, without any device allocation.
+ *
+ * This entry point has no counterpart in the reference.  It exists for
+ * callers that cannot call cudaMalloc: code that runs while a CUDA stream is
+ * being captured into a graph (allocation calls are not allowed there),
+ * latency-critical loops that cannot afford the device-wide synchronisation
+ * of cudaFree, and hosts whose device memory belongs to a pooling allocator
+ * that forbids side allocations.  The caller passes inputs and outputs; the
+ * Jacobi workspace is a static device array of 8 MiB owned by the library,
+ * held on every GPU that loads it until the process exits.
+ *   - n_mats * d * d must be <= 524288 (complex elements) and d <= 112;
+ *     larger requests fail with QT_ERR_SHAPE and launch nothing.
+ *   - The first call on a device looks up the array's device address
+ *     (cudaGetSymbolAddress); make that first call before any stream
+ *     capture starts.
+ *   - All calls share the workspace: calls that overlap on the GPU (other
+ *     streams, contexts or threads) race and must be serialised by the
+ *     caller.  The workspace needs no clearing between calls.
+ * Asynchronous on the context stream. */
+int qt_rho_inverse_noalloc(qt_ctx* ctx, void* rhoinv, const void* rho, int n_mats, int d,
+                           double eps);
+
 /* Device memory helpers for callers without their own allocator. */
 int qt_dev_alloc(qt_ctx* ctx, int64_t bytes, void** ptr);
 int qt_dev_free(qt_ctx* ctx, void* ptr);

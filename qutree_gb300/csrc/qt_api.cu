@@ -656,6 +656,26 @@ int qt_stage_launch(qt_ctx* c, int i) {
   return QT_OK;
 }
 
+int qt_rho_inverse_noalloc(qt_ctx* c, void* rhoinv, const void* rho, int n_mats, int d, double eps) {
+  if (!c || !rhoinv || !rho) return fail(c, QT_ERR_ARG, "qt_rho_inverse_noalloc: null argument");
+  if (n_mats < 1 || d < 1 || d > 112)
+    return fail(c, QT_ERR_SHAPE, "qt_rho_inverse_noalloc: need n_mats >= 1 and 1 <= d <= 112");
+  if (!(eps > 0) || !std::isfinite(eps)) return fail(c, QT_ERR_ARG, "qt_rho_inverse_noalloc: eps must be positive");
+  const int64_t need = (int64_t)n_mats * d * d;
+  if (need > qt::static_eig_capacity())
+    return fail(c, QT_ERR_SHAPE,
+                "qt_rho_inverse_noalloc: n_mats*d*d = " + std::to_string(need) +
+                    " exceeds the static scratch of " + std::to_string(qt::static_eig_capacity()) +
+                    " complex elements (8 MiB)");
+  if (rho == rhoinv) return fail(c, QT_ERR_ARG, "qt_rho_inverse_noalloc: rhoinv must not alias rho");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  cudaError_t e = qt::launch_rho_inverse_static((const double2*)rho, (double2*)rhoinv, n_mats, d, eps,
+                                                c->stream);
+  if (e != cudaSuccess) return cuda_fail(c, e, "qt_rho_inverse_noalloc");
+  c->launches += 1;
+  return QT_OK;
+}
+
 int qt_probe_fp64_peak(qt_ctx* c, double* tflops) {
   if (!c || !tflops) return fail(c, QT_ERR_ARG, "null argument");
   QT_CUDA(c, cudaSetDevice(c->device));

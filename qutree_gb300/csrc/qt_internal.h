@@ -237,6 +237,10 @@ cudaError_t launch_set_identity(double2* m, int d, cudaStream_t s);
 cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void* scratch);
 cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void* scratch);
 int mp_outputs_per_tile();
+// allocation-free density inverse (scratch in a static device array)
+int64_t static_eig_capacity();
+cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n_mats, int d,
+                                      double eps, cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
 

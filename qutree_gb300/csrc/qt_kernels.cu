@@ -12,6 +12,7 @@
 // Batched launches: each kernel reads a task table and a tile table; block b
 // processes tile b.  The planner (qt_plan.cpp) builds both once per tree.
 #include <cmath>
+#include <mutex>
 
 #include "qt_internal.h"
 
@@ -272,10 +273,8 @@ __device__ __forceinline__ void rr_pair(int m, int r, int i, int& p, int& q) {
   }
 }
 
-__global__ void __launch_bounds__(kThreads) k_eig(const EigTask* __restrict__ tasks, int64_t task0,
-                                                  double eps) {
+__device__ __forceinline__ void eig_body(const EigTask& t, double eps) {
   extern __shared__ double2 smem[];
-  const EigTask t = tasks[task0 + blockIdx.x];
   const int d = t.d;
   const int m = d + (d & 1);
   const int np = m / 2;
@@ -418,6 +417,12 @@ __global__ void __launch_bounds__(kThreads) k_eig(const EigTask* __restrict__ ta
     }
     t.rhoinv[e] = acc;
   }
+}
+
+__global__ void __launch_bounds__(kThreads) k_eig(const EigTask* __restrict__ tasks, int64_t task0,
+                                                  double eps) {
+  const EigTask t = tasks[task0 + blockIdx.x];
+  eig_body(t, eps);
 }
 
 // ---------------------------------------------------------------------------
@@ -614,6 +619,83 @@ cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void*) {
   dim3 grid((task.a + kHpTile - 1) / kHpTile, (aB + kHpTile - 1) / kHpTile);
   if (grid.x == 0 || grid.y == 0) return cudaSuccess;
   k_hp_single<<<grid, kThreads, 0, s>>>(task);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free density inverse.
+//
+// Callers that may not allocate device memory themselves (code running while
+// a CUDA stream is being captured, where cudaMalloc/cudaFree are not
+// allowed; latency-critical loops that cannot afford the implicit device
+// synchronisation of cudaFree; hosts whose device memory is owned by a pool
+// allocator that forbids side allocations) get the regularised inverses of
+// density matrices they already hold on the device without handing the
+// library any workspace.  The Jacobi eigenvector matrices live in the
+// file-scope array below instead of a cudaMalloc'd arena:
+//   - capacity kStaticEigElems complex elements (8 MiB): n_mats * d * d
+//     must not exceed 524288, e.g. 128 matrices of 64 x 64;
+//   - every GPU that loads the library holds these 8 MiB until the process
+//     exits;
+//   - all calls share the one array and it keeps the last call's contents.
+//     The kernel writes every scratch element before reading it (U starts as
+//     the identity), so nothing needs clearing between calls; two calls that
+//     overlap on the GPU (different streams, contexts or host threads) race
+//     on the array and must be ordered by the caller.
+// Host code cannot use the array's name as a device address, so the address
+// is looked up once per device with cudaGetSymbolAddress (with that device
+// current) on the first call that device sees.  That first call should
+// therefore happen before any stream capture begins.
+// ---------------------------------------------------------------------------
+constexpr int64_t kStaticEigElems = (int64_t)(8 << 20) / 16;
+static __device__ __align__(256) double2 g_eig_scratch[kStaticEigElems];
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+double2* g_eig_scratch_addr[kMaxDevices] = {nullptr};
+std::mutex g_eig_scratch_mutex;
+
+// U[b] = g_eig_scratch + b*d*d; matrix b of the batch is one block
+__global__ void __launch_bounds__(kThreads) k_eig_strided(const double2* __restrict__ rho,
+                                                          double2* __restrict__ rhoinv, double2* U,
+                                                          int d, double eps) {
+  const int64_t o = (int64_t)blockIdx.x * d * d;
+  EigTask t;
+  t.rho = rho + o;
+  t.rhoinv = rhoinv + o;
+  t.U = U + o;
+  t.d = d;
+  t.pad = 0;
+  eig_body(t, eps);
+}
+
+}  // namespace
+
+int64_t static_eig_capacity() { return kStaticEigElems; }
+
+cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n_mats, int d,
+                                      double eps, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  double2* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_eig_scratch_mutex);
+    if (!g_eig_scratch_addr[dev]) {
+      // set-up once per device, with that device current
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_eig_scratch);
+      if (e != cudaSuccess) return e;
+      g_eig_scratch_addr[dev] = (double2*)p;
+    }
+    scratch = g_eig_scratch_addr[dev];
+  }
+  const int64_t sm = eig_smem_bytes(d);
+  e = cudaFuncSetAttribute(k_eig_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_eig_strided<<<(unsigned)n_mats, kThreads, sm, s>>>(rho, rhoinv, scratch, d, eps);
   return cudaGetLastError();
 }
 

@@ -94,6 +94,8 @@ def load(build_if_missing: bool = True):
                            ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_stage_launch": ([_vp, ctypes.c_int], ctypes.c_int),
         "qt_probe_fp64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "qt_rho_inverse_noalloc": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double],
+                                   ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -113,7 +115,7 @@ def exported_symbols():
         "qt_matrices_size", "qt_matrices_download", "qt_plan_stats", "qt_mode_product",
         "qt_hole_product", "qt_last_mode_product", "qt_dev_alloc", "qt_dev_free",
         "qt_memcpy_h2d", "qt_memcpy_d2h", "qt_launch_count", "qt_stage_count",
-        "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak",
+        "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
     ]
 
 
@@ -179,6 +181,11 @@ class Context:
         return v.value
 
     # -- primitives (device pointers) ------------------------------------
+    def rho_inverse_noalloc(self, rhoinv, rho, n_mats, d, eps=1e-10):
+        """Regularised inverses of n_mats Hermitian d x d device matrices; the
+        library allocates nothing (its workspace is a static device array)."""
+        self.check(self.L.qt_rho_inverse_noalloc(self.h, _vp(rhoinv), _vp(rho), n_mats, d, eps))
+
     def mode_product(self, C, h, B, before, activeB, activeC, after, add=False):
         self.check(self.L.qt_mode_product(self.h, _vp(C), _vp(h), _vp(B), before, activeB, activeC,
                                           after, int(add)))
