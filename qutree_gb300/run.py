@@ -1,0 +1,41 @@
+"""Run H.Psi sweeps of a benchmark configuration from the command line.
+
+  python -m qutree_gb300.run --config 1 --sweeps 2 [--flavour grouped|reference]
+
+Prints one line per sweep (energy, milliseconds).  Used to profile the
+library (ncu) with a fixed, small launch sequence: qt_prepare, then
+``--sweeps`` graph launches of the sweep.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+from . import qtgpu
+from .model import config_problem
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--sweeps", type=int, default=2)
+    ap.add_argument("--flavour", default="grouped", choices=["grouped", "reference"])
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    tree, sop, psi = config_problem(a.config)
+    flavour = qtgpu.QT_PLAN_GROUPED if a.flavour == "grouped" else qtgpu.QT_PLAN_REFERENCE
+    hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, device=a.device)
+    hrep.upload(psi)
+    for i in range(a.sweeps):
+        t0 = time.perf_counter()
+        hrep.derivative()
+        e = hrep.energy()  # synchronises
+        print(f"sweep {i}: E = {e:.15f}  {1e3 * (time.perf_counter() - t0):.2f} ms", flush=True)
+    st = hrep.stats()
+    print(f"launches/sweep {int(st['launches'])}  executed GFLOP {st['exec_flops'] / 1e9:.2f}  "
+          f"reference GFLOP {st['ref_flops'] / 1e9:.2f}  scratch MiB {st['scratch_bytes'] / 2**20:.0f}")
+    hrep.close()
+
+
+if __name__ == "__main__":
+    main()
