@@ -51,6 +51,16 @@ extern "C" {
                                matrices and chains; Apply sums the mean fields
                                of terms with the same inside part first       */
 
+/* Arithmetic of the sweep, OR-ed into the plan flavour of qt_prepare.
+ * QT_PREC_F64: complex128 on the FP64 pipe.
+ * QT_PREC_DF64: every real number carried as an unevaluated sum of two
+ * floats (hi + lo, ~48-bit significand) and computed on the FP32 pipe, which
+ * GB300 runs 61x faster than FP64; the density-matrix inverses and
+ * projector solves stay complex128.  Inputs and outputs of the C ABI are
+ * complex128 in both cases. */
+#define QT_PREC_F64 0x000
+#define QT_PREC_DF64 0x100
+
 /* Matrix sets for qt_matrices_download. */
 #define QT_MAT_RHO 0     /* density matrices, per node, d_up x d_up          */
 #define QT_MAT_RHOINV 1  /* regularised inverse density matrices             */
@@ -106,7 +116,8 @@ int qt_sop_upload(qt_ctx* ctx, int n_ops, const int* op_kind, const int* op_dim,
 int qt_set_regularization(qt_ctx* ctx, double eps);
 
 /* Builds the sweep plan, allocates the device arena and captures the sweep
- * as a CUDA graph.  Needs tree and SOP.  No allocation happens afterwards. */
+ * as a CUDA graph.  plan_flavour = QT_PLAN_* | QT_PREC_*.  Needs tree and
+ * SOP.  No allocation happens afterwards. */
 int qt_prepare(qt_ctx* ctx, int plan_flavour);
 
 /* Wavefunction, packed layout (TensorTree<cd>,

@@ -39,6 +39,8 @@ struct qt_ctx {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t launches = 0;
+  int prec = 0;
+  std::vector<double> ops_df;  // double-float operator table staging (prec 1)
 };
 
 namespace {
@@ -68,6 +70,9 @@ void release_arena(qt_ctx* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   c->exec = nullptr;
   c->graph = nullptr;
+  // B_PSI64 / B_DPSI64 alias B_PSI / B_DPSI in complex128 plans: free once
+  if (c->buf[qt::B_PSI64] == c->buf[qt::B_PSI]) c->buf[qt::B_PSI64] = nullptr;
+  if (c->buf[qt::B_DPSI64] == c->buf[qt::B_DPSI]) c->buf[qt::B_DPSI64] = nullptr;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if (c->buf[i]) cudaFree(c->buf[i]);
     c->buf[i] = nullptr;
@@ -235,8 +240,10 @@ int qt_set_regularization(qt_ctx* c, double eps) {
 int qt_prepare(qt_ctx* c, int flavour) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->have_tree || !c->have_sop) return fail(c, QT_ERR_STATE, "qt_prepare needs tree and SOP");
-  if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED)
+  const int prec = (flavour & QT_PREC_DF64) ? 1 : 0;
+  if ((flavour & ~QT_PREC_DF64) != QT_PLAN_REFERENCE && (flavour & ~QT_PREC_DF64) != QT_PLAN_GROUPED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
+  flavour &= ~QT_PREC_DF64;
   QT_CUDA(c, cudaSetDevice(c->device));
   release_arena(c);
   int64_t budget = (int64_t)1 << 28;  // scratch elements (4 GiB)
@@ -244,7 +251,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     long v = std::atol(s);
     if (v > 0) budget = (int64_t)v * (1 << 20) / 16;
   }
-  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour, budget);
+  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour, prec, budget);
   if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
   Plan& P = c->plan;
   c->buf_elems[qt::B_PSI] = P.psi_arena;
@@ -254,8 +261,11 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_OPS] = (int64_t)c->ops.data.size() / 2;
   c->buf_elems[qt::B_SCR] = std::max<int64_t>(P.scratch_size, 16);
   c->buf_elems[qt::B_PARAM] = 16;
+  c->buf_elems[qt::B_PSI64] = prec == 1 ? P.psi_arena : 0;
+  c->buf_elems[qt::B_DPSI64] = prec == 1 ? P.psi_arena : 0;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
+    if ((i == qt::B_PSI64 || i == qt::B_DPSI64) && prec == 0) continue;  // aliases, set below
     int64_t n = std::max<int64_t>(c->buf_elems[i], 16);
     cudaError_t e = cudaMalloc((void**)&c->buf[i], n * sizeof(double2));
     if (e != cudaSuccess) {
@@ -264,11 +274,30 @@ int qt_prepare(qt_ctx* c, int flavour) {
     }
     arena += n * 16;
   }
+  if (prec == 0) {
+    c->buf[qt::B_PSI64] = c->buf[qt::B_PSI];
+    c->buf[qt::B_DPSI64] = c->buf[qt::B_DPSI];
+  }
+  c->prec = prec;
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_MATS], 0, c->buf_elems[qt::B_MATS] * 16, c->stream));
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_HPHI], 0, c->buf_elems[qt::B_HPHI] * 16, c->stream));
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_DPSI], 0, c->buf_elems[qt::B_DPSI] * 16, c->stream));
-  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_OPS], c->ops.data.data(), c->ops.data.size() * sizeof(double),
-                             cudaMemcpyHostToDevice, c->stream));
+  if (prec == 1) {
+    // operator table as double-float pairs (hi, lo) per real number
+    c->ops_df.resize(c->ops.data.size());
+    float* f = (float*)c->ops_df.data();
+    for (size_t i = 0; i < c->ops.data.size(); ++i) {
+      const double x = c->ops.data[i];
+      const float h = (float)x;
+      f[2 * i] = h;
+      f[2 * i + 1] = (float)(x - (double)h);
+    }
+    QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_OPS], c->ops_df.data(), c->ops_df.size() * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+  } else {
+    QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_OPS], c->ops.data.data(), c->ops.data.size() * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+  }
   // bind the symbolic tables to device pointers
   std::vector<qt::MPTask> mp;
   for (auto& s : P.mp) {
@@ -348,6 +377,16 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.pad = 0;
     proj.push_back(t);
   }
+  std::vector<qt::CvtTask> cvt;
+  for (auto& s : P.cvt) {
+    qt::CvtTask t;
+    t.src = ptr_of(c, s.src);
+    t.dst = mptr_of(c, s.dst);
+    t.n = s.n;
+    t.dir = s.dir;
+    t.pad = 0;
+    cvt.push_back(t);
+  }
   std::vector<char> blob;
   std::vector<int64_t> offs;
   put(blob, offs, mp);
@@ -361,6 +400,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, P.mp_tiles);
   put(blob, offs, P.hp_tiles);
   put(blob, offs, P.acc_tiles);
+  put(blob, offs, cvt);
+  put(blob, offs, P.cvt_tiles);
   {
     cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -382,8 +423,10 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.mp_tiles = (int2*)(base + offs[8]);
   c->tables.hp_tiles = (int4*)(base + offs[9]);
   c->tables.acc_tiles = (int4*)(base + offs[10]);
+  c->tables.cvt = (qt::CvtTask*)(base + offs[11]);
+  c->tables.cvt_tiles = (int2*)(base + offs[12]);
   for (auto& id : P.identities) {
-    cudaError_t e = qt::launch_set_identity(c->buf[qt::B_MATS] + id.first, id.second, c->stream);
+    cudaError_t e = qt::launch_set_identity(c->buf[qt::B_MATS] + id.first, id.second, prec, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "set identity");
     c->launches += 1;
   }
@@ -391,7 +434,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   // capture the sweep
   QT_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   for (const auto& st : P.stages) {
-    cudaError_t e = qt::launch_stage(st, c->tables, c->eps, P.max_eig_d, c->stream);
+    cudaError_t e = qt::launch_stage(st, c->tables, c->eps, P.max_eig_d, prec, c->stream);
     if (e != cudaSuccess) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(c->stream, &g);
@@ -413,7 +456,7 @@ int64_t qt_psi_size(const qt_ctx* c) { return (c && c->prepared) ? c->plan.psi_p
 int qt_psi_upload(qt_ctx* c, const double* psi) {
   if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_upload before qt_prepare");
-  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI], psi, c->plan.psi_packed * 16, cudaMemcpyHostToDevice,
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI64], psi, c->plan.psi_packed * 16, cudaMemcpyHostToDevice,
                              c->stream));
   c->have_psi = true;
   c->swept = false;
@@ -423,7 +466,7 @@ int qt_psi_upload(qt_ctx* c, const double* psi) {
 int qt_psi_upload_device(qt_ctx* c, const void* psi) {
   if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_upload_device before qt_prepare");
-  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI], psi, c->plan.psi_packed * 16, cudaMemcpyDeviceToDevice,
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI64], psi, c->plan.psi_packed * 16, cudaMemcpyDeviceToDevice,
                              c->stream));
   c->have_psi = true;
   c->swept = false;
@@ -433,7 +476,7 @@ int qt_psi_upload_device(qt_ctx* c, const void* psi) {
 int qt_psi_download(qt_ctx* c, double* psi) {
   if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->have_psi) return fail(c, QT_ERR_STATE, "no wavefunction uploaded");
-  QT_CUDA(c, cudaMemcpyAsync(psi, c->buf[qt::B_PSI], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
+  QT_CUDA(c, cudaMemcpyAsync(psi, c->buf[qt::B_PSI64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
                              c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   return QT_OK;
@@ -454,7 +497,7 @@ int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
 int qt_dpsi_download(qt_ctx* c, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
-  QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_DPSI], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
+  QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_DPSI64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
                              c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   return QT_OK;
@@ -463,7 +506,7 @@ int qt_dpsi_download(qt_ctx* c, double* out) {
 int qt_dpsi_device(qt_ctx* c, const void** p) {
   if (!c || !p) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_dpsi_device before qt_prepare");
-  *p = c->buf[qt::B_DPSI];
+  *p = c->buf[qt::B_DPSI64];
   return QT_OK;
 }
 
@@ -510,8 +553,16 @@ int qt_matrices_download(qt_ctx* c, int which, double* out) {
   double2* o = (double2*)out;
   int n = (int)P.nodes.size();
   int64_t cur = 0;
+  if (c->prec == 1 && (which == QT_MAT_HMAT || which == QT_MAT_HCON)) {
+    // double-float slots -> complex128
+    for (auto& v : mats) {
+      float4 f;
+      std::memcpy(&f, &v, 16);
+      v = make_double2((double)f.x + (double)f.y, (double)f.z + (double)f.w);
+    }
+  }
   if (which == QT_MAT_RHO || which == QT_MAT_RHOINV) {
-    const auto& off = which == QT_MAT_RHO ? P.rho_off : P.rhoinv_off;
+    const auto& off = which == QT_MAT_RHO ? P.rho64_off : P.rhoinv64_off;
     for (int a = 0; a < n; ++a) {
       int64_t dd = (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
       std::memcpy(o + cur, mats.data() + off[a], dd * 16);
@@ -580,7 +631,7 @@ int qt_hole_product(qt_ctx* c, void* S, const void* A, const void* B, int64_t be
                     int64_t activeB, int64_t after) {
   if (!c || !S || !A || !B) return fail(c, QT_ERR_ARG, "qt_hole_product: null argument");
   if (before < 1 || activeA < 1 || activeB < 1 || after < 1 || before * activeA * after > ((int64_t)1 << 31) ||
-      before * activeB * after > ((int64_t)1 << 31) || activeA > 65535 * 32 || activeB > 65535 * 32)
+      before * activeB * after > ((int64_t)1 << 31) || activeA + activeB > 800)
     return fail(c, QT_ERR_SHAPE, "qt_hole_product: bad geometry");
   QT_CUDA(c, cudaSetDevice(c->device));
   qt::HPTask t;
@@ -650,7 +701,8 @@ int qt_stage_launch(qt_ctx* c, int i) {
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_stage_launch needs a prepared context and a wavefunction");
   if (i < 0 || i >= (int)c->plan.stages.size()) return fail(c, QT_ERR_ARG, "no such stage");
   QT_CUDA(c, cudaSetDevice(c->device));
-  cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->stream);
+  cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->prec,
+                                   c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_stage_launch");
   c->launches += 1;
   return QT_OK;

@@ -83,7 +83,16 @@ struct ProjTask {
   int d, pad;
 };
 
-enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ };
+// Elementwise precision conversion of n complex numbers: dir 0 complex128 ->
+// double-float (float4 hi/lo pairs), dir 1 double-float -> complex128.
+struct CvtTask {
+  const void* src;
+  void* dst;
+  int64_t n;
+  int dir, pad;
+};
+
+enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT };
 
 struct Stage {
   int kind;
@@ -97,7 +106,11 @@ struct Stage {
 // ---------------------------------------------------------------------------
 // Host-side plan (symbolic; pointers are bound after the arena exists)
 // ---------------------------------------------------------------------------
-enum Buf { B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_NBUF };
+// B_PSI64 / B_DPSI64: the caller-facing complex128 wavefunction and derivative.
+// With complex128 arithmetic they alias B_PSI / B_DPSI; with double-float
+// arithmetic B_PSI / B_HPHI / B_DPSI hold double-float numbers and conversion
+// stages move data across.
+enum Buf { B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_NBUF };
 
 struct Ref {
   int buf = -1;
@@ -138,8 +151,12 @@ struct Plan {
   std::vector<NodeGeo> nodes;
   int64_t psi_packed = 0, psi_arena = 0;
   // matrices arena layout
+  // complex128 copies (rho64 ... m2_64) alias the plain offsets when prec == 0
   std::vector<int64_t> rho_off, rhoinv_off, u_off, s_off, sinv_off, d_off, p_off, m2_off;
-  int64_t energy_off = 0, stop_off = 0;
+  std::vector<int64_t> rho64_off, rhoinv64_off, s64_off, d64_off, m2_64_off;
+  int64_t energy_off = 0, stop_off = 0;      // complex128 results read by qt_energy
+  int64_t energy_dev_off = 0, stop_dev_off = 0;  // written by the hole products
+  int prec = 0;
   // sparse (term, node) -> slot offset of hmat / hcon; -1 if inactive
   std::vector<std::vector<int64_t>> hslot, cslot;
   int64_t mats_size = 0;
@@ -181,6 +198,11 @@ struct Plan {
     Ref S, D, rhoinv, Sinv, P, M2;
     int d;
   };
+  struct SCvt {
+    Ref src, dst;
+    int64_t n;
+    int dir;
+  };
   std::vector<SMP> mp;
   std::vector<SHP> hp;
   std::vector<SAcc> acc;
@@ -189,11 +211,13 @@ struct Plan {
   std::vector<SLinTerm> lin_terms;
   std::vector<SEig> eig;
   std::vector<SProj> proj;
+  std::vector<SCvt> cvt;
   std::vector<Stage> stages;
   // tiles (bound with task indices only)
   std::vector<int2> mp_tiles;
   std::vector<int4> hp_tiles;
   std::vector<int4> acc_tiles;
+  std::vector<int2> cvt_tiles;
   // constant matrices written once at prepare: (offset, d) identity
   std::vector<std::pair<int64_t, int>> identities;
   PlanStats stats;
@@ -213,8 +237,9 @@ struct SopDesc {
 };
 
 // planner entry point; returns "" on success or an error message
+// flavour: 0 reference call sequence, 1 grouped; prec: 0 complex128, 1 double-float
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
-                       const SopDesc& sop, int flavour, int64_t scratch_budget_elems);
+                       const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems);
 
 // kernel launches (qt_kernels.cu)
 struct DevTables {
@@ -229,10 +254,13 @@ struct DevTables {
   int2* mp_tiles = nullptr;
   int4* hp_tiles = nullptr;
   int4* acc_tiles = nullptr;
+  CvtTask* cvt = nullptr;
+  int2* cvt_tiles = nullptr;
 };
-cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d,
+// prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe
+cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d, int prec,
                          cudaStream_t s);
-cudaError_t launch_set_identity(double2* m, int d, cudaStream_t s);
+cudaError_t launch_set_identity(double2* m, int d, int prec, cudaStream_t s);
 // single-op launches for the primitive C ABI calls
 cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void* scratch);
 cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void* scratch);

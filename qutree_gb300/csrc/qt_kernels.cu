@@ -14,6 +14,7 @@
 #include <cmath>
 #include <mutex>
 
+#include "qt_arith.cuh"
 #include "qt_internal.h"
 
 namespace qt {
@@ -22,31 +23,16 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kMpPerThread = 4;
 constexpr int kMpTile = kThreads * kMpPerThread;  // 1024, as in the planner
-constexpr int kHpTile = 32;
+constexpr int kHpMaxDim = 112;  // largest bond the planner admits
 constexpr int kHpK = 16;
-constexpr int kAccRows = 64, kAccCols = 16;
+constexpr int kAccRows = 64;
+constexpr int kCvtPerThread = 8;  // 2048 elements per tile, as in the planner
 
-__device__ __forceinline__ double2 cz() { return make_double2(0.0, 0.0); }
-__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
-  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
-}
-// acc += a * b
-__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) {
-  acc.x = fma(a.x, b.x, acc.x);
-  acc.x = fma(-a.y, b.y, acc.x);
-  acc.y = fma(a.x, b.y, acc.y);
-  acc.y = fma(a.y, b.x, acc.y);
-}
-// acc += conj(a) * b
-__device__ __forceinline__ void cfmac(double2& acc, double2 a, double2 b) {
-  acc.x = fma(a.x, b.x, acc.x);
-  acc.x = fma(a.y, b.y, acc.x);
-  acc.y = fma(a.x, b.y, acc.y);
-  acc.y = fma(-a.y, b.x, acc.y);
-}
-__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
-  return make_double2(a.x + b.x, a.y + b.y);
-}
+__device__ __forceinline__ double2 cz() { return cz64(); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) { return cmul64(a, b); }
+__device__ __forceinline__ void cfma(double2& acc, double2 a, double2 b) { cfma64(acc, a, b); }
+__device__ __forceinline__ void cfmac(double2& acc, double2 a, double2 b) { cfmac64(acc, a, b); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return cadd64(a, b); }
 
 // ---------------------------------------------------------------------------
 // Mode-k product (matvec / matrixTensor): one thread per 4 outputs, each a
@@ -55,12 +41,18 @@ __device__ __forceinline__ double2 cadd(double2 a, double2 b) {
 // the input fiber; along higher modes they read consecutive input elements
 // (coalesced) and share h.
 // ---------------------------------------------------------------------------
+template <class P>
 __device__ __forceinline__ void mp_tile(const MPTask& t, int64_t start) {
+  typedef typename P::S S;
+  typedef typename P::A A;
+  const S* __restrict__ in = reinterpret_cast<const S*>(t.in);
+  const S* __restrict__ h = reinterpret_cast<const S*>(t.h);
+  S* out = reinterpret_cast<S*>(t.out);
   const int64_t total = (int64_t)t.before * t.a_out * t.after;
   const int64_t slice_in = (int64_t)t.before * t.a_in;
   int64_t o[kMpPerThread];
-  const double2* hp[kMpPerThread];
-  const double2* ip[kMpPerThread];
+  const S* hp[kMpPerThread];
+  const S* ip[kMpPerThread];
 #pragma unroll
   for (int q = 0; q < kMpPerThread; ++q) {
     o[q] = start + threadIdx.x + (int64_t)q * kThreads;
@@ -69,56 +61,63 @@ __device__ __forceinline__ void mp_tile(const MPTask& t, int64_t start) {
     int64_t r = oo / t.before;
     int j = (int)(r % t.a_out);
     int64_t c = r / t.a_out;
-    hp[q] = t.h + j;
-    ip[q] = t.in + b + slice_in * c;
+    hp[q] = h + j;
+    ip[q] = in + b + slice_in * c;
     if (t.diag) ip[q] += (int64_t)j * t.before;
   }
-  double2 acc[kMpPerThread];
+  const bool unit = t.alpha.x == 1.0 && t.alpha.y == 0.0;
+  const typename P::C alpha = P::coef(t.alpha);
+  S res[kMpPerThread];
   if (t.diag) {
 #pragma unroll
-    for (int q = 0; q < kMpPerThread; ++q) acc[q] = cmul(__ldg(hp[q]), __ldg(ip[q]));
+    for (int q = 0; q < kMpPerThread; ++q) res[q] = P::mul(P::ld(hp[q]), P::ld(ip[q]));
   } else {
+    A acc[kMpPerThread];
 #pragma unroll
-    for (int q = 0; q < kMpPerThread; ++q) acc[q] = cz();
+    for (int q = 0; q < kMpPerThread; ++q) acc[q] = P::zero();
     const int64_t hs = t.a_out, is = t.before;
     int a = 0;
     for (; a + 1 < t.a_in; a += 2) {
-      double2 h0[kMpPerThread], x0[kMpPerThread], h1[kMpPerThread], x1[kMpPerThread];
+      S h0[kMpPerThread], x0[kMpPerThread], h1[kMpPerThread], x1[kMpPerThread];
 #pragma unroll
       for (int q = 0; q < kMpPerThread; ++q) {
-        h0[q] = __ldg(hp[q] + a * hs);
-        x0[q] = __ldg(ip[q] + a * is);
-        h1[q] = __ldg(hp[q] + (a + 1) * hs);
-        x1[q] = __ldg(ip[q] + (a + 1) * is);
+        h0[q] = P::ld(hp[q] + a * hs);
+        x0[q] = P::ld(ip[q] + a * is);
+        h1[q] = P::ld(hp[q] + (a + 1) * hs);
+        x1[q] = P::ld(ip[q] + (a + 1) * is);
       }
 #pragma unroll
       for (int q = 0; q < kMpPerThread; ++q) {
-        cfma(acc[q], h0[q], x0[q]);
-        cfma(acc[q], h1[q], x1[q]);
+        P::mac(acc[q], h0[q], x0[q]);
+        P::mac(acc[q], h1[q], x1[q]);
+        P::norm(acc[q]);
       }
     }
     for (; a < t.a_in; ++a) {
 #pragma unroll
-      for (int q = 0; q < kMpPerThread; ++q) cfma(acc[q], __ldg(hp[q] + a * hs), __ldg(ip[q] + a * is));
+      for (int q = 0; q < kMpPerThread; ++q) P::mac(acc[q], P::ld(hp[q] + a * hs), P::ld(ip[q] + a * is));
     }
+#pragma unroll
+    for (int q = 0; q < kMpPerThread; ++q) res[q] = P::fin(acc[q]);
   }
 #pragma unroll
   for (int q = 0; q < kMpPerThread; ++q)
     if (o[q] < total) {
-      const double2 v = cmul(t.alpha, acc[q]);
-      t.out[o[q]] = t.add ? cadd(t.out[o[q]], v) : v;
+      const S v = unit ? res[q] : P::scale(alpha, res[q]);
+      out[o[q]] = t.add ? P::plus(out[o[q]], v) : v;
     }
 }
 
+template <class P>
 __global__ void __launch_bounds__(kThreads) k_mp(const MPTask* __restrict__ tasks,
                                                  const int2* __restrict__ tiles, int64_t tile0) {
   const int2 tl = tiles[tile0 + blockIdx.x];
   const MPTask t = tasks[tl.x];
-  mp_tile(t, tl.y);
+  mp_tile<P>(t, tl.y);
 }
 
 __global__ void __launch_bounds__(kThreads) k_mp_single(MPTask t) {
-  mp_tile(t, (int64_t)blockIdx.x * kMpTile);
+  mp_tile<F64>(t, (int64_t)blockIdx.x * kMpTile);
 }
 
 // ---------------------------------------------------------------------------
@@ -127,65 +126,94 @@ __global__ void __launch_bounds__(kThreads) k_mp_single(MPTask t) {
 // thread; A and B are staged through shared memory 16 k-rows at a time with
 // coalesced loads (along b when before > 1, along i when before == 1).
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void hp_tile(const HPTask& t, int i0, int j0) {
-  __shared__ double2 sA[kHpK][kHpTile + 1];
-  __shared__ double2 sB[kHpK][kHpTile + 1];
+template <class P>
+__device__ __forceinline__ void hp_tile(const HPTask& t, int mt0) {
+  // Output S is split into 2 x 2 micro-tiles, numbered column-major over the
+  // (ceil(aA/2) x ceil(aB/2)) micro-tile grid; thread x of the block owns
+  // micro-tile mt0 + x.  Threads past the last micro-tile form whole idle
+  // warps (they only help stage operands), so no lanes idle inside a warp.
+  typedef typename P::S S;
+  typedef typename P::A A;
+  extern __shared__ __align__(16) unsigned char hp_smem[];
+  const S* __restrict__ Ap = reinterpret_cast<const S*>(t.A);
+  const S* __restrict__ Bp = reinterpret_cast<const S*>(t.B);
+  S* Sp = reinterpret_cast<S*>(t.S);
   const int before = t.before;
   const int aA = t.a, aB = t.aB > 0 ? t.aB : t.a;
+  S* sA = reinterpret_cast<S*>(hp_smem);   // [kHpK][aA]
+  S* sB = sA + kHpK * aA;                  // [kHpK][aB]
   const int64_t K = (int64_t)before * t.after;
   const int64_t sliceA = (int64_t)before * aA, sliceB = (int64_t)before * aB;
-  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-  double2 acc00 = cz(), acc01 = cz(), acc10 = cz(), acc11 = cz();
+  const int mi = (aA + 1) / 2, mj = (aB + 1) / 2;
+  const int mt = mt0 + threadIdx.x;
+  const bool active = mt < mi * mj;
+  const int i = active ? 2 * (mt % mi) : 0;
+  const int j = active ? 2 * (mt / mi) : 0;
+  const int i1 = i + 1 < aA ? i + 1 : i, j1 = j + 1 < aB ? j + 1 : j;
+  A acc00 = P::zero(), acc01 = P::zero(), acc10 = P::zero(), acc11 = P::zero();
+  const int nA = kHpK * aA, nAB = kHpK * (aA + aB);
   for (int64_t k0 = 0; k0 < K; k0 += kHpK) {
-    for (int e = threadIdx.x; e < kHpK * kHpTile; e += kThreads) {
+    for (int e = threadIdx.x; e < nAB; e += kThreads) {
+      const bool isA = e < nA;
+      const int ee = isA ? e : e - nA;
+      const int ncol = isA ? aA : aB;
       int kk, ii;
       if (before == 1) {
-        ii = e % kHpTile;
-        kk = e / kHpTile;
+        ii = ee % ncol;
+        kk = ee / ncol;
       } else {
-        kk = e % kHpK;
-        ii = e / kHpK;
+        kk = ee % kHpK;
+        ii = ee / kHpK;
       }
       const int64_t k = k0 + kk;
-      double2 va = cz(), vb = cz();
+      S v = P::zero();
       if (k < K) {
         const int64_t b = k % before, c = k / before;
-        const int i = i0 + ii, j = j0 + ii;
-        if (i < aA) va = __ldg(t.A + b + (int64_t)before * i + sliceA * c);
-        if (j < aB) vb = __ldg(t.B + b + (int64_t)before * j + sliceB * c);
+        v = isA ? P::ld(Ap + b + (int64_t)before * ii + sliceA * c)
+                : P::ld(Bp + b + (int64_t)before * ii + sliceB * c);
       }
-      sA[kk][ii] = va;
-      sB[kk][ii] = vb;
+      (isA ? sA : sB)[kk * ncol + ii] = v;
     }
     __syncthreads();
-#pragma unroll
-    for (int kk = 0; kk < kHpK; ++kk) {
-      const double2 a0 = sA[kk][tx * 2], a1 = sA[kk][tx * 2 + 1];
-      const double2 b0 = sB[kk][ty * 2], b1 = sB[kk][ty * 2 + 1];
-      cfmac(acc00, a0, b0);
-      cfmac(acc10, a1, b0);
-      cfmac(acc01, a0, b1);
-      cfmac(acc11, a1, b1);
+    if (active) {
+#pragma unroll 4
+      for (int kk = 0; kk < kHpK; ++kk) {
+        const S a0 = sA[kk * aA + i], a1 = sA[kk * aA + i1];
+        const S b0 = sB[kk * aB + j], b1 = sB[kk * aB + j1];
+        P::macc(acc00, a0, b0);
+        P::macc(acc10, a1, b0);
+        P::macc(acc01, a0, b1);
+        P::macc(acc11, a1, b1);
+        if (kk & 1) {
+          P::norm(acc00);
+          P::norm(acc10);
+          P::norm(acc01);
+          P::norm(acc11);
+        }
+      }
     }
     __syncthreads();
   }
-  const int i = i0 + tx * 2, j = j0 + ty * 2;
-  if (i < aA && j < aB) t.S[i + (int64_t)aA * j] = acc00;
-  if (i + 1 < aA && j < aB) t.S[i + 1 + (int64_t)aA * j] = acc10;
-  if (i < aA && j + 1 < aB) t.S[i + (int64_t)aA * (j + 1)] = acc01;
-  if (i + 1 < aA && j + 1 < aB) t.S[i + 1 + (int64_t)aA * (j + 1)] = acc11;
+  if (!active) return;
+  Sp[i + (int64_t)aA * j] = P::fin(acc00);
+  if (i + 1 < aA) Sp[i + 1 + (int64_t)aA * j] = P::fin(acc10);
+  if (j + 1 < aB) Sp[i + (int64_t)aA * (j + 1)] = P::fin(acc01);
+  if (i + 1 < aA && j + 1 < aB) Sp[i + 1 + (int64_t)aA * (j + 1)] = P::fin(acc11);
 }
 
+template <class P>
 __global__ void __launch_bounds__(kThreads) k_hp(const HPTask* __restrict__ tasks,
                                                  const int4* __restrict__ tiles, int64_t tile0) {
   const int4 tl = tiles[tile0 + blockIdx.x];
   const HPTask t = tasks[tl.x];
-  hp_tile(t, tl.y, tl.z);
+  hp_tile<P>(t, tl.y);
 }
 
 __global__ void __launch_bounds__(kThreads) k_hp_single(HPTask t) {
-  hp_tile(t, blockIdx.x * kHpTile, blockIdx.y * kHpTile);
+  hp_tile<F64>(t, blockIdx.x * kThreads);
 }
+
+inline int hp_smem_bytes(int aA, int aB) { return kHpK * (aA + aB) * 16; }
 
 // ---------------------------------------------------------------------------
 // Last-mode accumulation (multStateAB summed over terms):
@@ -193,60 +221,110 @@ __global__ void __launch_bounds__(kThreads) k_hp_single(HPTask t) {
 // 64 rows x 16 columns per block; a warp covers 32 consecutive rows (coalesced
 // X loads) of 4 columns (H loads broadcast across the warp).
 // ---------------------------------------------------------------------------
+template <class P>
 __global__ void __launch_bounds__(kThreads) k_acc(const AccTask* __restrict__ tasks,
                                                   const AccTerm* __restrict__ terms,
                                                   const int4* __restrict__ tiles, int64_t tile0) {
+  typedef typename P::S S;
+  typedef typename P::A A;
   const int4 tl = tiles[tile0 + blockIdx.x];
   const AccTask t = tasks[tl.x];
   const int r = tl.y + threadIdx.x % kAccRows;
   const int jb = tl.z + (threadIdx.x / kAccRows) * 4;
   const bool rv = r < t.rows;
   const int d = t.d;
+  if (jb >= d) return;  // the whole warp lies past the last column
+  const int nq = d - jb < 4 ? d - jb : 4;  // uniform across the warp
   const int64_t rows = t.rows;
-  double2 acc[4] = {cz(), cz(), cz(), cz()};
+  A acc[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
   for (int s = 0; s < t.count; ++s) {
     const AccTerm T = terms[t.first + s];
+    const S* X = reinterpret_cast<const S*>(T.X);
     if (T.H == nullptr) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int j = jb + q;
-        if (rv && j < d) acc[q] = cadd(acc[q], __ldg(T.X + r + rows * j));
+        if (rv && j < d) P::add(acc[q], P::ld(X + r + rows * j));
       }
     } else {
-      const double2* hrow[4];
+      const S* H = reinterpret_cast<const S*>(T.H);
+      const S* hrow[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) hrow[q] = T.H + (jb + q < d ? jb + q : 0);
-      for (int jp = 0; jp < d; ++jp) {
-        const double2 x = rv ? __ldg(T.X + r + rows * jp) : cz();
+      for (int q = 0; q < 4; ++q) hrow[q] = H + (jb + q < d ? jb + q : 0);
+      if (nq == 4) {
+        for (int jp = 0; jp < d; ++jp) {
+          const S x = rv ? P::ld(X + r + rows * jp) : P::zero();
 #pragma unroll
-        for (int q = 0; q < 4; ++q) cfma(acc[q], __ldg(hrow[q] + (int64_t)d * jp), x);
+          for (int q = 0; q < 4; ++q) P::mac(acc[q], P::ld(hrow[q] + (int64_t)d * jp), x);
+          if (jp & 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) P::norm(acc[q]);
+          }
+        }
+      } else {
+        for (int jp = 0; jp < d; ++jp) {
+          const S x = rv ? P::ld(X + r + rows * jp) : P::zero();
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (q < nq) P::mac(acc[q], P::ld(hrow[q] + (int64_t)d * jp), x);
+          if (jp & 1) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) P::norm(acc[q]);
+          }
+        }
       }
     }
   }
-  const double2 alpha = t.alpha_ptr ? *t.alpha_ptr : t.alpha;
+  const double2 alpha64 = t.alpha_ptr ? *t.alpha_ptr : t.alpha;
+  const typename P::C alpha = P::coef(alpha64);
+  S* out = reinterpret_cast<S*>(t.out);
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int j = jb + q;
     if (rv && j < d) {
-      const double2 v = cmul(alpha, acc[q]);
-      double2* p = t.out + r + rows * j;
-      *p = t.add ? cadd(*p, v) : v;
+      const S v = P::scale(alpha, P::fin(acc[q]));
+      S* p = out + r + rows * j;
+      *p = t.add ? P::plus(*p, v) : v;
     }
   }
 }
 
 // out = sum_t c_t M_t (d x d), one block per output matrix.
+template <class P>
 __global__ void __launch_bounds__(kThreads) k_lin(const LinTask* __restrict__ tasks,
                                                   const LinTerm* __restrict__ terms, int64_t task0) {
+  typedef typename P::S S;
   const LinTask t = tasks[task0 + blockIdx.x];
   const int dd = t.d * t.d;
+  S* out = reinterpret_cast<S*>(t.out);
   for (int e = threadIdx.x; e < dd; e += kThreads) {
-    double2 acc = cz();
+    typename P::A acc = P::zero();
     for (int s = 0; s < t.count; ++s) {
       const LinTerm T = terms[t.first + s];
-      cfma(acc, T.c, __ldg(T.M + e));
+      P::cmac(acc, P::coef(T.c), P::ld(reinterpret_cast<const S*>(T.M) + e));
+      P::norm(acc);
     }
-    t.out[e] = acc;
+    out[e] = P::fin(acc);
+  }
+}
+
+// Precision conversions: dir 0 complex128 -> double-float, dir 1 back.
+__global__ void __launch_bounds__(kThreads) k_cvt(const CvtTask* __restrict__ tasks,
+                                                  const int2* __restrict__ tiles, int64_t tile0) {
+  const int2 tl = tiles[tile0 + blockIdx.x];
+  const CvtTask t = tasks[tl.x];
+  for (int q = 0; q < kCvtPerThread; ++q) {
+    const int64_t i = tl.y + threadIdx.x + (int64_t)q * kThreads;
+    if (i >= t.n) break;
+    if (t.dir == 0) {
+      const double2 v = reinterpret_cast<const double2*>(t.src)[i];
+      const float2 r = df_split(v.x), m = df_split(v.y);
+      reinterpret_cast<float4*>(t.dst)[i] = make_float4(r.x, r.y, m.x, m.y);
+    } else {
+      const float4 v = reinterpret_cast<const float4*>(t.src)[i];
+      reinterpret_cast<double2*>(t.dst)[i] =
+          make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    }
   }
 }
 
@@ -291,8 +369,83 @@ __device__ __forceinline__ void eig_body(const EigTask& t, double eps) {
     // Hermitian part
     A[e] = (i == j) ? make_double2(aij.x, 0.0)
                     : make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
-    U[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
+    // shifted copy for the positive-definiteness certificate below
+    U[e] = (i == j) ? make_double2(A[e].x - 100.0 * eps, 0.0) : A[e];
   }
+  __syncthreads();
+  // Fast path.  If every eigenvalue exceeds 50*eps, eps*exp(-w/eps) changes
+  // 1/w by less than 4e-24 relative, so the regularised inverse is the plain
+  // inverse.  A Cholesky factorisation of rho - 100*eps*I that succeeds
+  // certifies that bound (its backward error, ~d*2^-53*|rho|, is far below
+  // 50*eps for eps = 1e-10 and normalised states); then rho^-1 comes from a
+  // Gauss-Jordan inversion (no pivoting needed for a positive definite
+  // matrix) in O(d^3) instead of a Jacobi eigensolver.
+  __shared__ int not_pd;
+  __shared__ double2 piv_s;
+  if (threadIdx.x == 0) not_pd = 0;
+  __syncthreads();
+  for (int k = 0; k < d; ++k) {
+    const double dk = U[k + (int64_t)d * k].x;
+    if (!(dk > 0.0)) {
+      if (threadIdx.x == 0) not_pd = 1;
+      break;  // uniform: every thread reads the same value
+    }
+    const double l = sqrt(dk);
+    __syncthreads();
+    for (int i = k + threadIdx.x; i < d; i += kThreads) {
+      double2 v = U[i + (int64_t)d * k];
+      U[i + (int64_t)d * k] = make_double2(v.x / l, v.y / l);
+    }
+    __syncthreads();
+    // trailing update of the lower triangle: U(i,j) -= L(i,k) conj(L(j,k))
+    const int rem = d - k - 1;
+    for (int e = threadIdx.x; e < rem * rem; e += kThreads) {
+      const int i = k + 1 + e % rem, j = k + 1 + e / rem;
+      if (j > i) continue;
+      const double2 li = U[i + (int64_t)d * k], lj = U[j + (int64_t)d * k];
+      double2 u = U[i + (int64_t)d * j];
+      cfma(u, make_double2(-li.x, -li.y), make_double2(lj.x, -lj.y));
+      U[i + (int64_t)d * j] = u;
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (!not_pd) {
+    double2* X = t.rhoinv;
+    for (int e = threadIdx.x; e < d * d; e += kThreads)
+      X[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    for (int col = 0; col < d; ++col) {
+      if (threadIdx.x == 0) {
+        const double2 v = A[col + d * col];
+        const double den = v.x * v.x + v.y * v.y;
+        piv_s = make_double2(v.x / den, -v.y / den);
+      }
+      __syncthreads();
+      const double2 pinv = piv_s;
+      for (int j = threadIdx.x; j < d; j += kThreads) {
+        A[col + d * j] = cmul(A[col + d * j], pinv);
+        X[col + (int64_t)d * j] = cmul(X[col + (int64_t)d * j], pinv);
+      }
+      __syncthreads();
+      // column col of A before elimination (fw reused as the factor column)
+      for (int r = threadIdx.x; r < d; r += kThreads) fw[r] = A[r + d * col];
+      __syncthreads();
+      for (int e = threadIdx.x; e < d * d; e += kThreads) {
+        const int r = e % d, j = e / d;
+        if (r == col) continue;
+        const double2 f = fw[r];
+        double2 a = A[e], x = X[e];
+        cfma(a, make_double2(-f.x, -f.y), A[col + d * j]);
+        cfma(x, make_double2(-f.x, -f.y), X[col + (int64_t)d * j]);
+        A[e] = a;
+        X[e] = x;
+      }
+      __syncthreads();
+    }
+    return;
+  }
+  for (int e = threadIdx.x; e < d * d; e += kThreads) U[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
   __syncthreads();
   for (int sweep = 0; sweep < 40; ++sweep) {
     double off = 0.0, dg = 0.0;
@@ -509,9 +662,14 @@ __global__ void __launch_bounds__(kThreads) k_proj(const ProjTask* __restrict__ 
   }
 }
 
-__global__ void k_identity(double2* m, int d) {
-  for (int e = threadIdx.x; e < d * d; e += blockDim.x)
-    m[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
+__global__ void k_identity(double2* m, int d, int prec) {
+  for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
+    const bool diag = (e % d) == (e / d);
+    if (prec == 1)
+      reinterpret_cast<float4*>(m)[e] = make_float4(diag ? 1.f : 0.f, 0.f, 0.f, 0.f);
+    else
+      m[e] = make_double2(diag ? 1.0 : 0.0, 0.0);
+  }
 }
 
 // Eight independent FMA chains per thread; one store per thread keeps the
@@ -568,21 +726,26 @@ cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d,
-                         cudaStream_t s) {
+template <class P>
+cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int max_eig_d,
+                           cudaStream_t s) {
   switch (st.kind) {
     case ST_MP:
-      k_mp<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
+      k_mp<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
       break;
-    case ST_HP:
-      k_hp<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.hp, t.hp_tiles, st.first_tile);
+    case ST_HP: {
+      const int sm = hp_smem_bytes(kHpMaxDim, kHpMaxDim);
+      cudaError_t e = cudaFuncSetAttribute(k_hp<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      if (e != cudaSuccess) return e;
+      k_hp<P><<<(unsigned)st.n_tiles, kThreads, sm, s>>>(t.hp, t.hp_tiles, st.first_tile);
       break;
+    }
     case ST_ACC:
-      k_acc<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.acc, t.acc_terms, t.acc_tiles,
-                                                      st.first_tile);
+      k_acc<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.acc, t.acc_terms, t.acc_tiles,
+                                                         st.first_tile);
       break;
     case ST_LIN:
-      k_lin<<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.lin, t.lin_terms, st.first_task);
+      k_lin<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.lin, t.lin_terms, st.first_task);
       break;
     case ST_EIG: {
       const int64_t sm = eig_smem_bytes(max_eig_d);
@@ -595,14 +758,25 @@ cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int ma
     case ST_PROJ:
       k_proj<<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.proj, st.first_task);
       break;
+    case ST_CVT:
+      k_cvt<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.cvt, t.cvt_tiles, st.first_tile);
+      break;
     default:
       return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_set_identity(double2* m, int d, cudaStream_t s) {
-  k_identity<<<1, kThreads, 0, s>>>(m, d);
+cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d,
+                         int prec, cudaStream_t s) {
+  (void)cudaGetLastError();  // drop a stale error of an unrelated earlier call
+  return prec == 1 ? launch_stage_p<DF64>(st, t, eps, max_eig_d, s)
+                   : launch_stage_p<F64>(st, t, eps, max_eig_d, s);
+}
+
+cudaError_t launch_set_identity(double2* m, int d, int prec, cudaStream_t s) {
+  (void)cudaGetLastError();
+  k_identity<<<1, kThreads, 0, s>>>(m, d, prec);
   return cudaGetLastError();
 }
 
@@ -610,15 +784,22 @@ cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void*) {
   const int64_t total = (int64_t)task.before * task.a_out * task.after;
   const int64_t blocks = (total + kMpTile - 1) / kMpTile;
   if (blocks == 0) return cudaSuccess;
+  (void)cudaGetLastError();
   k_mp_single<<<(unsigned)blocks, kThreads, 0, s>>>(task);
   return cudaGetLastError();
 }
 
 cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void*) {
   const int aB = task.aB > 0 ? task.aB : task.a;
-  dim3 grid((task.a + kHpTile - 1) / kHpTile, (aB + kHpTile - 1) / kHpTile);
-  if (grid.x == 0 || grid.y == 0) return cudaSuccess;
-  k_hp_single<<<grid, kThreads, 0, s>>>(task);
+  const int64_t micro = (int64_t)((task.a + 1) / 2) * ((aB + 1) / 2);
+  const int64_t blocks = (micro + kThreads - 1) / kThreads;
+  if (blocks == 0) return cudaSuccess;
+  const int sm = hp_smem_bytes(task.a, aB);
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  (void)cudaGetLastError();
+  cudaError_t e = cudaFuncSetAttribute(k_hp_single, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e != cudaSuccess) return e;
+  k_hp_single<<<(unsigned)blocks, kThreads, sm, s>>>(task);
   return cudaGetLastError();
 }
 
@@ -693,6 +874,7 @@ cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n
     scratch = g_eig_scratch_addr[dev];
   }
   const int64_t sm = eig_smem_bytes(d);
+  (void)cudaGetLastError();
   e = cudaFuncSetAttribute(k_eig_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   k_eig_strided<<<(unsigned)n_mats, kThreads, sm, s>>>(rho, rhoinv, scratch, d, eps);

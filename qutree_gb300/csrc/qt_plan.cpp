@@ -43,7 +43,6 @@ namespace qt {
 namespace {
 
 constexpr int kMpTile = 1024;  // outputs per mode-product tile (256 threads x 4)
-constexpr int kHpTile = 32;    // hole-product output tile edge
 constexpr int kAccRows = 64, kAccCols = 16;
 constexpr int64_t kAlign = 16;  // elements (256 bytes)
 
@@ -77,15 +76,21 @@ struct Item {
 class Builder {
  public:
   Builder(Plan& P, const std::vector<NodeGeo>& nodes, const OpTable& ops, const SopDesc& sop,
-          int flavour, int64_t budget)
+          int flavour, int prec, int64_t budget)
       : P(P), nd(P.nodes), ops(ops), sop(sop), grouped(flavour == 1), budget(budget) {
     P.nodes = nodes;
+    P.prec = prec;
   }
 
   void run() {
     geometry();
     activity();
     layout();
+    if (P.prec == 1) {
+      int64_t c0 = (int64_t)P.cvt.size(), t0 = (int64_t)P.cvt_tiles.size();
+      add_cvt(Ref{B_PSI64, 0}, Ref{B_PSI, 0}, P.psi_packed, 0);
+      emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), t0, (int64_t)P.cvt_tiles.size(), "psi-in");
+    }
     stage_density();
     stage_inverse();
     stage_represent();
@@ -132,6 +137,8 @@ class Builder {
         b += 16.0 * 2 * (double)P.eig[t].d * P.eig[t].d;
       } else if (kind == ST_PROJ) {
         b += 16.0 * 6 * (double)P.proj[t].d * P.proj[t].d;
+      } else if (kind == ST_CVT) {
+        b += 32.0 * (double)P.cvt[t].n;
       }
     }
     return b;
@@ -277,9 +284,28 @@ class Builder {
         P.m2_off[i] = alloc_mat(d);
       }
     }
+    P.rho64_off = P.rho_off;
+    P.rhoinv64_off = P.rhoinv_off;
+    P.s64_off = P.s_off;
+    P.d64_off = P.d_off;
+    P.m2_64_off = P.m2_off;
+    if (P.prec == 1) {
+      for (int i = 0; i < n; ++i) {
+        int d = nd[i].dup();
+        P.rho64_off[i] = alloc_mat(d);
+        P.rhoinv64_off[i] = alloc_mat(d);
+        if (i != top) {
+          P.s64_off[i] = alloc_mat(d);
+          P.d64_off[i] = alloc_mat(d);
+          P.m2_64_off[i] = alloc_mat(d);
+        }
+      }
+    }
     int dt = nd[top].dup();
-    P.energy_off = alloc_mat(dt);
-    P.stop_off = alloc_mat(dt);
+    P.energy_dev_off = alloc_mat(dt);
+    P.stop_dev_off = alloc_mat(dt);
+    P.energy_off = P.prec == 1 ? alloc_mat(dt) : P.energy_dev_off;
+    P.stop_off = P.prec == 1 ? alloc_mat(dt) : P.stop_dev_off;
     int64_t ident_top = alloc_mat(dt);
     P.identities.push_back({ident_top, dt});
     P.identities.push_back({P.rho_off[top], dt});
@@ -352,6 +378,29 @@ class Builder {
     P.stats.exec_flops += diag ? 6.0 * g.N : 8.0 * g.N * g.shape[mode];
   }
 
+  void add_cvt(Ref src, Ref dst, int64_t n, int dir) {
+    Plan::SCvt t;
+    t.src = src;
+    t.dst = dst;
+    t.n = n;
+    t.dir = dir;
+    int task = (int)P.cvt.size();
+    P.cvt.push_back(t);
+    for (int64_t s = 0; s < n; s += 2048) P.cvt_tiles.push_back(make_int2(task, (int)s));
+  }
+
+  // one conversion stage over several matrices
+  void cvt_mats(const std::vector<int64_t>& src, const std::vector<int64_t>& dst, int dir,
+                const char* name, bool skip_top) {
+    int64_t c0 = (int64_t)P.cvt.size(), t0 = (int64_t)P.cvt_tiles.size();
+    for (int a = 0; a < n; ++a) {
+      if (skip_top && a == top) continue;
+      if (src[a] < 0 || dst[a] < 0) continue;
+      add_cvt(mat(src[a]), mat(dst[a]), (int64_t)nd[a].dup() * nd[a].dup(), dir);
+    }
+    emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), t0, (int64_t)P.cvt_tiles.size(), name);
+  }
+
   void add_hp(Ref A, Ref B, Ref S, int node, int mode) {
     const NodeGeo& g = nd[node];
     Plan::SHP t;
@@ -363,8 +412,9 @@ class Builder {
     t.after = (int)g.after(mode);
     int task = (int)P.hp.size();
     P.hp.push_back(t);
-    for (int i0 = 0; i0 < t.a; i0 += kHpTile)
-      for (int j0 = 0; j0 < t.a; j0 += kHpTile) P.hp_tiles.push_back(make_int4(task, i0, j0, 0));
+    // 2x2 micro-tiles of S, 256 per tile (one per thread)
+    const int64_t micro = (int64_t)((t.a + 1) / 2) * ((t.a + 1) / 2);
+    for (int64_t m0 = 0; m0 < micro; m0 += 256) P.hp_tiles.push_back(make_int4(task, (int)m0, 0, 0));
     P.stats.exec_flops += 8.0 * g.N * g.shape[mode];
   }
 
@@ -481,16 +531,18 @@ class Builder {
   }
 
   void stage_inverse() {
+    if (P.prec == 1) cvt_mats(P.rho_off, P.rho64_off, 1, "rho-to-f64", false);
     int64_t t0 = (int64_t)P.eig.size();
     for (int a = 0; a < n; ++a) {
       Plan::SEig e;
-      e.rho = mat(P.rho_off[a]);
-      e.rhoinv = mat(P.rhoinv_off[a]);
+      e.rho = mat(P.rho64_off[a]);
+      e.rhoinv = mat(P.rhoinv64_off[a]);
       e.U = mat(P.u_off[a]);
       e.d = nd[a].dup();
       P.eig.push_back(e);
     }
     emit_stage(ST_EIG, t0, (int64_t)P.eig.size(), t0, (int64_t)P.eig.size(), "inverse");
+    if (P.prec == 1) cvt_mats(P.rhoinv64_off, P.rhoinv_off, 0, "rhoinv-to-df", false);
   }
 
   // operators of term l at node a (represent / apply chain body)
@@ -629,29 +681,45 @@ class Builder {
     int64_t t0 = (int64_t)P.hp.size(), tile0 = (int64_t)P.hp_tiles.size();
     for (int a = 0; a < n; ++a) {
       if (a == top) {
-        add_hp(psi(a), hphi(a), mat(P.energy_off), a, nd[a].last());
-        add_hp(psi(a), psi(a), mat(P.stop_off), a, nd[a].last());
+        add_hp(psi(a), hphi(a), mat(P.energy_dev_off), a, nd[a].last());
+        add_hp(psi(a), psi(a), mat(P.stop_dev_off), a, nd[a].last());
       } else {
         add_hp(psi(a), psi(a), mat(P.s_off[a]), a, nd[a].last());
         add_hp(psi(a), hphi(a), mat(P.d_off[a]), a, nd[a].last());
       }
     }
     emit_stage(ST_HP, t0, (int64_t)P.hp.size(), tile0, (int64_t)P.hp_tiles.size(), "overlaps");
+    if (P.prec == 1) {
+      std::vector<int64_t> src = P.s_off, dst = P.s64_off;
+      src.insert(src.end(), P.d_off.begin(), P.d_off.end());
+      dst.insert(dst.end(), P.d64_off.begin(), P.d64_off.end());
+      int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
+      for (size_t i = 0; i < src.size(); ++i) {
+        int a = (int)(i % n);
+        if (a == top) continue;
+        add_cvt(mat(src[i]), mat(dst[i]), (int64_t)nd[a].dup() * nd[a].dup(), 1);
+      }
+      int dt = nd[top].dup();
+      add_cvt(mat(P.energy_dev_off), mat(P.energy_off), (int64_t)dt * dt, 1);
+      add_cvt(mat(P.stop_dev_off), mat(P.stop_off), (int64_t)dt * dt, 1);
+      emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "overlaps-to-f64");
+    }
     int64_t p0 = (int64_t)P.proj.size();
     for (int a = 0; a < n; ++a) {
       if (a == top) continue;
       Plan::SProj pj;
-      pj.S = mat(P.s_off[a]);
-      pj.D = mat(P.d_off[a]);
-      pj.rhoinv = mat(P.rhoinv_off[a]);
+      pj.S = mat(P.s64_off[a]);
+      pj.D = mat(P.d64_off[a]);
+      pj.rhoinv = mat(P.rhoinv64_off[a]);
       pj.Sinv = mat(P.sinv_off[a]);
       pj.P = mat(P.p_off[a]);
-      pj.M2 = mat(P.m2_off[a]);
+      pj.M2 = mat(P.m2_64_off[a]);
       pj.d = nd[a].dup();
       P.proj.push_back(pj);
       P.stats.exec_flops += 3 * 8.0 * pj.d * pj.d * pj.d;
     }
     emit_stage(ST_PROJ, p0, (int64_t)P.proj.size(), p0, (int64_t)P.proj.size(), "projector");
+    if (P.prec == 1) cvt_mats(P.m2_64_off, P.m2_off, 0, "m2-to-df", true);
     // dPsi = -i*phase * (H Phi - Phi P) rhoinv^T  (non-top);  -i*phase * H Phi (top)
     int64_t a0 = (int64_t)P.acc.size(), atile0 = (int64_t)P.acc_tiles.size();
     for (int a = 0; a < n; ++a) {
@@ -665,6 +733,11 @@ class Builder {
       add_acc(dpsi(a), true, c2(0, 0), a, terms, false);
     }
     emit_stage(ST_ACC, a0, (int64_t)P.acc.size(), atile0, (int64_t)P.acc_tiles.size(), "derivative");
+    if (P.prec == 1) {
+      int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
+      add_cvt(Ref{B_DPSI, 0}, Ref{B_DPSI64, 0}, P.psi_packed, 1);
+      emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "dpsi-out");
+    }
     P.mats_size = mats_cursor;
   }
 
@@ -722,10 +795,11 @@ class Builder {
 }  // namespace
 
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
-                       const SopDesc& sop, int flavour, int64_t scratch_budget_elems) {
+                       const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems) {
   plan = Plan();
   try {
-    Builder b(plan, nodes, ops, sop, flavour, scratch_budget_elems);
+    if (prec != 0 && prec != 1) throw std::runtime_error("unknown precision");
+    Builder b(plan, nodes, ops, sop, flavour, prec, scratch_budget_elems);
     b.run();
   } catch (const std::exception& e) {
     return e.what();

@@ -28,7 +28,7 @@ void* qtp_build(int n_nodes, const int* order, const int* dims, const int* paren
                 const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
                 const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
                 const int* term_ptr, const int* term_mode, const int* term_op, int flavour,
-                int64_t budget, char* err, int errlen) {
+                int prec, int64_t budget, char* err, int errlen) {
   std::vector<qt::NodeGeo> nodes(n_nodes);
   int p = 0;
   for (int i = 0; i < n_nodes; ++i) {
@@ -58,7 +58,7 @@ void* qtp_build(int n_nodes, const int* order, const int* dims, const int* paren
   s.mode.assign(term_mode, term_mode + s.ptr[n_terms]);
   s.op.assign(term_op, term_op + s.ptr[n_terms]);
   Handle* h = new Handle();
-  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, budget);
+  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, prec, budget);
   if (!msg.empty()) {
     if (err && errlen > 0) {
       std::strncpy(err, msg.c_str(), errlen - 1);
@@ -75,7 +75,7 @@ void qtp_free(void* h) { delete (Handle*)h; }
 
 // Table ids: 0 stages, 1 mp, 2 hp, 3 acc, 4 acc_terms, 5 lin, 6 lin_terms,
 // 7 eig, 8 proj, 9 sizes, 10 identities, 11 rho_off, 12 rhoinv_off,
-// 13 hslot, 14 cslot, 15 mp alphas, 16 lin coeffs, 17 stats (doubles).
+// 13 hslot, 14 cslot, 18 cvt, 15 mp alphas, 16 lin coeffs, 17 stats (doubles).
 // qtp_size returns the element count, qtp_get copies.
 static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vector<double>& dv) {
   v.clear();
@@ -160,7 +160,15 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       }
       break;
     case 9:
-      v = {P.psi_arena, P.mats_size, P.scratch_size, P.ops_size, P.energy_off, P.stop_off};
+      v = {P.psi_arena, P.mats_size, P.scratch_size, P.ops_size, P.energy_off, P.stop_off, P.prec};
+      break;
+    case 18:
+      for (auto& t : P.cvt) {
+        put_ref(v, t.src);
+        put_ref(v, t.dst);
+        v.push_back(t.n);
+        v.push_back(t.dir);
+      }
       break;
     case 10:
       for (auto& id : P.identities) {
@@ -169,10 +177,10 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       }
       break;
     case 11:
-      v = P.rho_off;
+      v = P.rho64_off;
       break;
     case 12:
-      v = P.rhoinv_off;
+      v = P.rhoinv64_off;
       break;
     case 13:
     case 14: {
@@ -202,18 +210,20 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
   }
 }
 
+static bool is_double_table(int what) { return what >= 15 && what <= 17; }
+
 int64_t qtp_size(void* h, int what) {
   std::vector<int64_t> v;
   std::vector<double> dv;
   table(((Handle*)h)->plan, what, v, dv);
-  return what >= 15 ? (int64_t)dv.size() : (int64_t)v.size();
+  return is_double_table(what) ? (int64_t)dv.size() : (int64_t)v.size();
 }
 
 void qtp_get(void* h, int what, void* out) {
   std::vector<int64_t> v;
   std::vector<double> dv;
   table(((Handle*)h)->plan, what, v, dv);
-  if (what >= 15)
+  if (is_double_table(what))
     std::memcpy(out, dv.data(), dv.size() * sizeof(double));
   else
     std::memcpy(out, v.data(), v.size() * sizeof(int64_t));

@@ -25,6 +25,8 @@ from .model import SOP, Tree, TensorTree
 QT_OK = 0
 QT_PLAN_REFERENCE = 0
 QT_PLAN_GROUPED = 1
+QT_PREC_F64 = 0x000
+QT_PREC_DF64 = 0x100
 QT_MAT_RHO, QT_MAT_RHOINV, QT_MAT_HMAT, QT_MAT_HCON = 0, 1, 2, 3
 ERRORS = {1: "QT_ERR_ARG", 2: "QT_ERR_SHAPE", 3: "QT_ERR_ALLOC", 4: "QT_ERR_CUDA",
           5: "QT_ERR_STATE", 6: "QT_ERR_NUMERIC"}

@@ -38,3 +38,36 @@ def rho_condition(tree, rho):
         w = np.linalg.eigvalsh(0.5 * (R + R.conj().T))
         worst = max(worst, w.max() / max(w.min(), 1e-300))
     return worst
+
+
+def deriv_errors(tree, dpsi, ref, rho):
+    """Compare derivatives node by node after multiplying each non-top node
+    back by its density matrix (C[r, m] = sum_n rho(m, n) dPsi[r, n]).
+
+    Returns (err, noise): err is the largest difference over nodes whose
+    derivative is not identically zero, relative to the largest reference
+    value; noise is the largest magnitude, relative to the same scale, on
+    nodes whose SPFs span their whole space (lastBefore == d_up): there the
+    projector (1-P) is zero and both derivatives are rounding noise of a
+    cancellation."""
+    off = tree.offsets()
+    ro = 0
+    scale = 0.0
+    parts = []
+    for n in tree.nodes:
+        d = n.d_up
+        R = rho[ro:ro + d * d].reshape((d, d), order="F")
+        ro += d * d
+        a = dpsi[off[n.address]:off[n.address + 1]].reshape((-1, d), order="F")
+        b = ref[off[n.address]:off[n.address + 1]].reshape((-1, d), order="F")
+        if not n.is_top:
+            a, b = a @ R.T, b @ R.T
+        degenerate = (not n.is_top) and n.size == d * d
+        parts.append((degenerate, a, b))
+        if not degenerate:
+            scale = max(scale, float(np.abs(b).max()))
+    scale = scale if scale > 0 else 1.0
+    err = max((float(np.abs(a - b).max()) for dg, a, b in parts if not dg), default=0.0) / scale
+    noise = max((max(float(np.abs(a).max()), float(np.abs(b).max())) for dg, a, b in parts if dg),
+                default=0.0) / scale
+    return err, noise

@@ -21,8 +21,8 @@ _i32 = _P(dtype=np.int32, flags="C_CONTIGUOUS")
 _i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
-B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM = range(7)
-ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ = range(6)
+B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64 = range(9)
+ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT = range(7)
 
 
 def lib():
@@ -32,7 +32,8 @@ def lib():
         L.qtp_build.restype = ctypes.c_void_p
         L.qtp_build.argtypes = [ctypes.c_int, _i32, _i32, _i32, _i32, _i32, ctypes.c_int, _i32, _i32,
                                 _i64, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _i32, _i32,
-                                _i32, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p, ctypes.c_int]
+                                _i32, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_char_p,
+                                ctypes.c_int]
         L.qtp_free.argtypes = [ctypes.c_void_p]
         L.qtp_size.restype = ctypes.c_int64
         L.qtp_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -57,7 +58,7 @@ def repack_ops(kind, dim, off, data):
 
 
 class PlanView:
-    def __init__(self, tree, sop, flavour=0, budget=1 << 28):
+    def __init__(self, tree, sop, flavour=0, budget=1 << 28, prec=0):
         L = lib()
         order, dims, parent, child_idx, leaf_mode = tree.descriptor()
         kind, odim, ooff, odata = sop.ops.descriptor()
@@ -68,14 +69,14 @@ class PlanView:
         err = ctypes.create_string_buffer(512)
         h = L.qtp_build(tree.n_nodes, order, dims, parent, child_idx, leaf_mode, len(kind), kind,
                         odim, ooff, odata.ctypes.data, len(sop), coeff.ctypes.data, ptr, modes,
-                        opids, flavour, budget, err, 512)
+                        opids, flavour, prec, budget, err, 512)
         if not h:
             raise ValueError(err.value.decode())
         self.h = h
         self.tree, self.sop = tree, sop
         self.tables = {}
-        widths = {0: 5, 1: 11, 2: 9, 3: 8, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2}
-        for what in range(15):
+        widths = {0: 5, 1: 11, 2: 9, 3: 8, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 18: 6}
+        for what in list(range(15)) + [18]:
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -99,19 +100,29 @@ class PlanView:
         s = self.tables[9]
         self.psi_arena, self.mats_size, self.scratch_size, self.ops_size = map(int, s[:4])
         self.energy_off, self.stop_off = int(s[4]), int(s[5])
+        self.prec = int(s[6])
         st = self.tables[17]
         self.stats = dict(ref_flops=st[0], exec_flops=st[1], launches=int(st[2]),
                           rep_chains=int(st[3]), mf_chains=int(st[4]), app_chains=int(st[5]))
 
     # -- interpreter -------------------------------------------------------
     def run(self, psi_flat, phase=1.0, eps=1e-10):
-        bufs = [np.asarray(psi_flat, np.complex128).copy(),
+        psi0 = np.asarray(psi_flat, np.complex128).copy()
+        bufs = [psi0,
                 np.zeros(self.psi_arena, np.complex128),
                 np.zeros(self.psi_arena, np.complex128),
                 np.zeros(max(self.mats_size, 16), np.complex128),
                 self.ops.copy(),
                 np.zeros(max(self.scratch_size, 16), np.complex128),
-                np.zeros(16, np.complex128)]
+                np.zeros(16, np.complex128), None, None]
+        if self.prec == 1:
+            # separate caller-facing complex128 arrays; conversions are copies here
+            bufs[B_PSI] = np.zeros_like(psi0)
+            bufs[B_PSI64] = psi0
+            bufs[B_DPSI64] = np.zeros_like(psi0)
+        else:
+            bufs[B_PSI64] = bufs[B_PSI]
+            bufs[B_DPSI64] = bufs[B_DPSI]
         bufs[B_PARAM][0] = -1j * complex(phase)
         for off, d in self.tables[10]:
             bufs[B_MATS][off:off + d * d] = np.eye(d).ravel(order="F")
@@ -167,6 +178,9 @@ class PlanView:
                     w, U = np.linalg.eigh(R)
                     f = 1.0 / (w + eps * np.exp(-w / eps))
                     view(ib, io, d * d)[:] = ((U * f) @ U.conj().T).ravel(order="F")
+                elif kind == ST_CVT:
+                    sb, so, db, do, n, _ = T[18][t]
+                    view(db, do, n)[:] = view(sb, so, n)
                 elif kind == ST_PROJ:
                     r = T[8][t]
                     d = r[12]
@@ -182,7 +196,7 @@ class PlanView:
         return bufs
 
     def dpsi(self):
-        return self.bufs[B_DPSI].copy()
+        return self.bufs[B_DPSI64].copy()
 
     def energy_parts(self):
         m = self.bufs[B_MATS]

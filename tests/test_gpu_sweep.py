@@ -1,25 +1,40 @@
-"""Full H.Psi sweeps on the GPU through the C ABI against the oracle.
+"""Full H.Psi sweeps on the GPU through the C ABI against the oracle, for
+both plan flavours and both arithmetics (complex128 on the FP64 pipe and
+double-float on the FP32 pipe).
 
-Tolerances: every contraction result (density matrices, represent and
+Tolerances (complex128 plans; double-float plans 10x looser, see TOL_DF):
+every contraction result (density matrices, represent and
 mean-field matrices, energy) within 1e-12 relative; the derivative compared
 after multiplying each non-top node back by its density matrix (undoing the
 regularised inverse, whose condition number amplifies rounding noise),
-within 1e-12 relative; the raw derivative within 1e-13 x cond(rho)."""
+within 1e-12 relative on every node whose derivative is not identically
+zero; on nodes whose SPFs span their whole space the projector (1-P)
+vanishes and |dPsi rho| must stay below 1e-11 (rounding noise); the raw
+derivative within 1e-13 x cond(rho) when no such node exists."""
 import numpy as np
 import pytest
 
 import oracle as O
-from helpers import rel_err, rho_condition, rho_weighted
+from helpers import deriv_errors, rel_err, rho_condition, rho_weighted
 from qutree_gb300 import qtgpu
 from qutree_gb300.model import (MLO, OP_DENSE, SOP, HOBasis, OperatorTable, balanced_tree,
                                 config_problem, coupled_oscillators, hartree_wavefunction,
                                 random_wavefunction)
 
 pytestmark = pytest.mark.gpu
+# complex128 (FP64 pipe): unit roundoff 2^-53
 TOL = 1e-12
+RAW = 1e-13
+# double-float (FP32 pipe): unit roundoff ~2^-48, so reductions of a few
+# thousand products with cancellation carry up to ~1e-12
+TOL_DF = 1e-11
+RAW_DF = 3e-12
+NOISE = 1e-11  # |dPsi rho| on nodes where (1-P) = 0 (rounding noise of a cancellation)
 
 
 def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
+    df = bool(flavour & qtgpu.QT_PREC_DF64)
+    TOL, RAW = (TOL_DF, RAW_DF) if df else (globals()["TOL"], globals()["RAW"])
     flat = psi.flat()
     r = O.derivative(tree, sop, flat, eps=eps, phase=phase)
     hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, eps=eps)
@@ -31,12 +46,14 @@ def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
         assert rel_err(rho, r.rho) <= TOL
         assert rel_err(hrep.matrices(qtgpu.QT_MAT_HMAT), r.hmat) <= TOL
         assert rel_err(hrep.matrices(qtgpu.QT_MAT_HCON), r.hcon) <= TOL
-        rw = rel_err(rho_weighted(tree, dpsi, r.rho), rho_weighted(tree, r.dpsi, r.rho))
-        assert rw <= TOL
+        err, noise = deriv_errors(tree, dpsi, r.dpsi, r.rho)
+        assert err <= TOL
+        assert noise <= NOISE
         cond = rho_condition(tree, r.rho)
-        assert rel_err(dpsi, r.dpsi) <= 1e-13 * max(cond, 10.0)
+        if noise == 0.0:  # no node whose derivative is pure rounding noise
+            assert rel_err(dpsi, r.dpsi) <= RAW * max(cond, 10.0)
         ri = hrep.matrices(qtgpu.QT_MAT_RHOINV)
-        assert rel_err(ri, r.rhoinv) <= 1e-13 * max(cond, 10.0)
+        assert rel_err(ri, r.rhoinv) <= RAW * max(cond, 10.0)
         # second call on the same graph reproduces bit for bit
         hrep.derivative(phase)
         assert np.array_equal(hrep.dpsi(), dpsi)
@@ -45,13 +62,17 @@ def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
         hrep.close()
 
 
-@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED])
+FLAVOURS = [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED,
+            qtgpu.QT_PLAN_REFERENCE | qtgpu.QT_PREC_DF64, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64]
+
+
+@pytest.mark.parametrize("flavour", FLAVOURS)
 def test_sweep_cfg0(flavour):
     tree, sop, psi = config_problem(0)
     _compare(tree, sop, psi, flavour)
 
 
-@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED])
+@pytest.mark.parametrize("flavour", FLAVOURS)
 def test_sweep_cfg4(flavour):
     tree, sop, psi = config_problem(4)
     _compare(tree, sop, psi, flavour)
@@ -64,7 +85,7 @@ def test_sweep_random_trees(leaves, p, b, seed):
     rng = np.random.default_rng(seed)
     sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
     psi = random_wavefunction(tree, seed)
-    for fl in (0, 1):
+    for fl in FLAVOURS:
         _compare(tree, sop, psi, fl, phase=np.exp(0.3j))
 
 
@@ -115,7 +136,7 @@ def test_multi_factor_terms():
     for k in range(6):
         sop.push_back(MLO([(k, kin)]), 1.0)
     psi = random_wavefunction(tree, 9)
-    for fl in (0, 1):
+    for fl in FLAVOURS:
         _compare(tree, sop, psi, fl)
 
 
@@ -129,7 +150,7 @@ def test_nodes_without_terms():
     sop.push_back(MLO([(0, kin)]), 1.0)
     sop.push_back(MLO([(1, x), (2, x)]), 0.3)
     psi = random_wavefunction(tree, 21)
-    for fl in (0, 1):
+    for fl in FLAVOURS:
         _compare(tree, sop, psi, fl)
 
 

@@ -11,10 +11,10 @@ from qutree_gb300.model import (MLO, OP_DENSE, SOP, HOBasis, OperatorTable, bala
                                 random_wavefunction)
 
 
-def _check(tree, sop, psi, flavour, budget=1 << 28, tol=1e-12):
+def _check(tree, sop, psi, flavour, budget=1 << 28, tol=1e-12, prec=0):
     flat = psi.flat()
     r = O.derivative(tree, sop, flat)
-    pv = PlanView(tree, sop, flavour, budget)
+    pv = PlanView(tree, sop, flavour, budget, prec=prec)
     pv.run(flat)
     h00, s00 = pv.energy_parts()
     assert abs(h00.real / s00.real - r.energy) < tol * max(1, abs(r.energy))
@@ -24,19 +24,21 @@ def _check(tree, sop, psi, flavour, budget=1 << 28, tol=1e-12):
     return pv
 
 
+@pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("flavour", [0, 1])
-def test_plan_cfg0(flavour):
+def test_plan_cfg0(flavour, prec):
     tree, sop, psi = config_problem(0)
-    pv = _check(tree, sop, psi, flavour)
+    pv = _check(tree, sop, psi, flavour, prec=prec)
     if flavour == 1:
         assert pv.stats["exec_flops"] < pv.stats["ref_flops"]
 
 
+@pytest.mark.parametrize("prec", [0, 1])
 @pytest.mark.parametrize("flavour", [0, 1])
-def test_plan_small_budget_chunks(flavour):
+def test_plan_small_budget_chunks(flavour, prec):
     # a tiny scratch budget forces every level into many chunks
     tree, sop, psi = config_problem(0)
-    _check(tree, sop, psi, flavour, budget=200)
+    _check(tree, sop, psi, flavour, budget=200, prec=prec)
 
 
 @pytest.mark.parametrize("leaves,p,b,seed", [(5, 4, 3, 1), (7, 5, 4, 2), (12, 3, 2, 3), (9, 6, 5, 4)])
@@ -47,6 +49,7 @@ def test_plan_random_trees(leaves, p, b, seed, flavour):
     sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
     psi = random_wavefunction(tree, seed)
     _check(tree, sop, psi, flavour)
+    _check(tree, sop, psi, flavour, prec=1)
 
 
 def test_plan_multi_factor_terms():
