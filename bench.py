@@ -43,6 +43,8 @@ def parse():
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--batch-trees", type=int, default=512,
+                    help="trees in the supplementary many-tree batch (0: skip)")
     return ap.parse_args()
 
 
@@ -316,6 +318,37 @@ def run_ours(args, ws, rank, local):
         head_dpsi = out_np.copy()
         h.close()
 
+    # supplementary: many uneven trees in one graph-captured plan
+    batch = None
+    if args.batch_trees > 0:
+        from qutree_gb300.model import batched_problem, forest, forest_psi, forest_sop
+        trees_b, sops_b, psis_b = batched_problem(args.batch_trees)
+        fb, _, mob = forest(trees_b)
+        sb, pb = forest_sop(sops_b, mob), forest_psi(fb, psis_b)
+        batch = {"trees": args.batch_trees, "nodes": fb.n_nodes,
+                 "workload": "uneven trees: modes in {8,16,32,48}, p in {8,16,32}, bonds 4..24 per "
+                             "edge (balanced), 2..6 couplings per mode, own SOP per tree"}
+        for label, fl in (("double_float", qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64),
+                          ("plain_complex128", qtgpu.QT_PLAN_REFERENCE)):
+            hb = qtgpu.HamiltonianRepresentation(sb, fb, flavour=fl, device=local)
+            sb_stream = torch.cuda.ExternalStream(hb.stream())
+            hb.upload(pb)
+            hb.derivative()
+            hb.sync()
+            nb = 3
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(sb_stream)
+            for _ in range(nb):
+                hb.derivative()
+            e1.record(sb_stream)
+            hb.sync()
+            ms = e0.elapsed_time(e1) / nb
+            batch[label] = {"ms_per_forest_sweep": ms, "tree_sweeps_per_s": args.batch_trees / (ms * 1e-3),
+                            "executed_gflop": hb.stats()["exec_flops"] / 1e9}
+            if label == "double_float":
+                batch["energies_first4"] = hb.energies()[:4].tolist()
+            hb.close()
+
     if rank != 0:
         return
     line = {
@@ -347,6 +380,8 @@ def run_ours(args, ws, rank, local):
     }
     if e2e:
         line["e2e"] = e2e
+    if batch:
+        line["batched_forest"] = batch
     if not args.no_cpu_baseline and args.config == 1:
         dt, cpu_e, blas = cpu_baseline_sweep(tree, sop, psi)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count(),

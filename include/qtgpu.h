@@ -138,8 +138,21 @@ int qt_derivative(qt_ctx* ctx, double phase_re, double phase_im);
 int qt_dpsi_download(qt_ctx* ctx, double* dpsi_host);
 int qt_dpsi_device(qt_ctx* ctx, const void** dpsi_dev);
 /* out[4] = { Re h00, Im h00, Re S00, Im S00 }, h00 = <Phi_top|H Phi_top>,
- * S00 = <Phi_top|Phi_top>; E = Re h00 / Re S00. Synchronises. */
+ * S00 = <Phi_top|Phi_top>; E = Re h00 / Re S00. Synchronises.  For a forest,
+ * the first tree. */
 int qt_energy(qt_ctx* ctx, double* out4);
+
+/* Forests.  The tree descriptor may hold several independent trees: every
+ * node with parent -1 closes one tree, whose nodes precede it.  Leaf modes
+ * are numbered across the whole forest and every SOP term acts on the leaves
+ * of one tree only (terms on several trees fail in qt_prepare with
+ * QT_ERR_SHAPE).  All trees advance together: each level's chains of every
+ * tree share one launch, one CUDA graph per sweep.  No counterpart in the
+ * reference, which handles one tree per HamiltonianRepresentation. */
+int qt_tree_count(const qt_ctx* ctx);
+/* out[4*t .. 4*t+3] = { Re h00, Im h00, Re S00, Im S00 } of tree t (roots in
+ * ascending address order), for t < n_trees. Synchronises. */
+int qt_energies(qt_ctx* ctx, double* out, int n_trees);
 
 /* Matrices of the last sweep.  Sparse layout (QT_MAT_HMAT / QT_MAT_HCON):
  * for each term, for each node on its leaf-to-root paths (SparseTree with

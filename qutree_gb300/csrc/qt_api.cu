@@ -510,18 +510,30 @@ int qt_dpsi_device(qt_ctx* c, const void** p) {
   return QT_OK;
 }
 
-int qt_energy(qt_ctx* c, double* out4) {
-  if (!c || !out4) return fail(c, QT_ERR_ARG, "null argument");
+int qt_energy(qt_ctx* c, double* out4) { return qt_energies(c, out4, 1); }
+
+int qt_tree_count(const qt_ctx* c) { return (c && c->prepared) ? (int)c->plan.tops.size() : -1; }
+
+int qt_energies(qt_ctx* c, double* out, int n_trees) {
+  if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
-  double2 v[2];
-  QT_CUDA(c, cudaMemcpyAsync(&v[0], c->buf[qt::B_MATS] + c->plan.energy_off, 16, cudaMemcpyDeviceToHost, c->stream));
-  QT_CUDA(c, cudaMemcpyAsync(&v[1], c->buf[qt::B_MATS] + c->plan.stop_off, 16, cudaMemcpyDeviceToHost, c->stream));
+  const int nt = (int)c->plan.tops.size();
+  if (n_trees < 1 || n_trees > nt) return fail(c, QT_ERR_ARG, "qt_energies: n_trees out of range");
+  std::vector<double2> v(2 * (size_t)n_trees);
+  for (int k = 0; k < n_trees; ++k) {
+    QT_CUDA(c, cudaMemcpyAsync(&v[2 * k], c->buf[qt::B_MATS] + c->plan.energy_off[k], 16,
+                               cudaMemcpyDeviceToHost, c->stream));
+    QT_CUDA(c, cudaMemcpyAsync(&v[2 * k + 1], c->buf[qt::B_MATS] + c->plan.stop_off[k], 16,
+                               cudaMemcpyDeviceToHost, c->stream));
+  }
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
-  out4[0] = v[0].x;
-  out4[1] = v[0].y;
-  out4[2] = v[1].x;
-  out4[3] = v[1].y;
-  if (!finite_all(out4, 4)) return fail(c, QT_ERR_NUMERIC, "non-finite energy");
+  for (int k = 0; k < n_trees; ++k) {
+    out[4 * k + 0] = v[2 * k].x;
+    out[4 * k + 1] = v[2 * k].y;
+    out[4 * k + 2] = v[2 * k + 1].x;
+    out[4 * k + 3] = v[2 * k + 1].y;
+  }
+  if (!finite_all(out, 4 * (int64_t)n_trees)) return fail(c, QT_ERR_NUMERIC, "non-finite energy");
   return QT_OK;
 }
 
@@ -535,9 +547,8 @@ int64_t qt_matrices_size(const qt_ctx* c, int which) {
     return s;
   }
   if (which == QT_MAT_HMAT || which == QT_MAT_HCON) {
-    for (size_t l = 0; l < P.hslot.size(); ++l)
-      for (int a = 0; a < n; ++a)
-        if (P.hslot[l][a] != -1) s += (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
+    for (const auto& nodes : P.term_nodes)
+      for (int a : nodes) s += (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
     return s;
   }
   return -1;
@@ -571,13 +582,13 @@ int qt_matrices_download(qt_ctx* c, int which, double* out) {
     return QT_OK;
   }
   if (which == QT_MAT_HMAT || which == QT_MAT_HCON) {
-    const auto& slot = which == QT_MAT_HMAT ? P.hslot : P.cslot;
-    for (size_t l = 0; l < P.hslot.size(); ++l)
-      for (int a = 0; a < n; ++a) {
-        if (P.hslot[l][a] == -1) continue;
+    const auto& slot = which == QT_MAT_HMAT ? P.term_hslot : P.term_cslot;
+    for (size_t l = 0; l < P.term_nodes.size(); ++l)
+      for (size_t i = 0; i < P.term_nodes[l].size(); ++i) {
+        const int a = P.term_nodes[l][i];
         int64_t dd = (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
-        if (slot[l][a] >= 0)
-          std::memcpy(o + cur, mats.data() + slot[l][a], dd * 16);
+        if (slot[l][i] >= 0)
+          std::memcpy(o + cur, mats.data() + slot[l][i], dd * 16);
         else
           std::memset((void*)(o + cur), 0, dd * 16);
         cur += dd;

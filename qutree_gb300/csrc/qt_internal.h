@@ -154,11 +154,15 @@ struct Plan {
   // complex128 copies (rho64 ... m2_64) alias the plain offsets when prec == 0
   std::vector<int64_t> rho_off, rhoinv_off, u_off, s_off, sinv_off, d_off, p_off, m2_off;
   std::vector<int64_t> rho64_off, rhoinv64_off, s64_off, d64_off, m2_64_off;
-  int64_t energy_off = 0, stop_off = 0;      // complex128 results read by qt_energy
-  int64_t energy_dev_off = 0, stop_dev_off = 0;  // written by the hole products
+  // per tree (root) of the forest, in ascending address order
+  std::vector<int> tops;
+  std::vector<int64_t> energy_off, stop_off;          // complex128 results read by qt_energy
+  std::vector<int64_t> energy_dev_off, stop_dev_off;  // written by the hole products
   int prec = 0;
-  // sparse (term, node) -> slot offset of hmat / hcon; -1 if inactive
-  std::vector<std::vector<int64_t>> hslot, cslot;
+  // per term: its active nodes (ascending) and their represent / mean-field
+  // slot offsets (-2: the top's represent matrix, zero by definition)
+  std::vector<std::vector<int>> term_nodes;
+  std::vector<std::vector<int64_t>> term_hslot, term_cslot;
   int64_t mats_size = 0;
   int64_t scratch_size = 0;
   int64_t ops_size = 0;

@@ -108,9 +108,28 @@ class Builder {
   const SopDesc& sop;
   bool grouped;
   int64_t budget;
-  int n = 0, L = 0, top = -1;
-  std::vector<std::vector<char>> act;  // [term][node]
-  std::vector<std::vector<char>> inside;  // [node][mode]
+  int n = 0, L = 0;
+  std::vector<int> tops;  // roots of the forest, ascending
+  bool is_top(int a) const { return nd[a].parent < 0; }
+  // sparse activity: the terms active at each node (ascending) with their
+  // represent / mean-field slots, and the active nodes of each term
+  std::vector<std::vector<int>> node_terms;
+  std::vector<std::vector<int64_t>> node_hslot, node_cslot;
+  std::vector<std::vector<int>> term_nodes;
+  std::vector<int> tin, tout;          // DFS interval of every node
+  std::map<int, int> leaf_node;        // mode -> bottom node
+  int idx_of(int l, int a) const {
+    const auto& v = node_terms[a];
+    auto it = std::lower_bound(v.begin(), v.end(), l);
+    return (it != v.end() && *it == l) ? (int)(it - v.begin()) : -1;
+  }
+  bool act(int l, int a) const { return idx_of(l, a) >= 0; }
+  int64_t hslot(int l, int a) const { return node_hslot[a][idx_of(l, a)]; }
+  int64_t cslot(int l, int a) const { return node_cslot[a][idx_of(l, a)]; }
+  bool inside_mode(int a, int m) const {
+    const int leaf = leaf_node.at(m);
+    return tin[a] <= tin[leaf] && tin[leaf] < tout[a];
+  }
   std::vector<std::vector<int>> gkey;  // apply group of (term) per node, filled per node
   int64_t mats_cursor = 0;
   double stage_flops_mark = 0;
@@ -159,8 +178,7 @@ class Builder {
   void geometry() {
     n = (int)nd.size();
     L = sop.n_terms;
-    top = n - 1;
-    if (n == 0 || !nd[top].top()) throw std::runtime_error("the last node must be the top node");
+    if (n == 0 || !nd[n - 1].top()) throw std::runtime_error("the last node must be a top node");
     int64_t off = 0, aoff = 0;
     for (int i = 0; i < n; ++i) {
       NodeGeo& g = nd[i];
@@ -187,8 +205,8 @@ class Builder {
         auto& ch = nd[nd[i].parent].children;
         if ((int)ch.size() <= nd[i].child_idx) ch.resize(nd[i].child_idx + 1, -1);
         ch[nd[i].child_idx] = i;
-      } else if (i != top) {
-        throw std::runtime_error("only the last node may have no parent");
+      } else {
+        tops.push_back(i);  // a forest: every root closes one tree
       }
     }
     for (int i = 0; i < n; ++i) {
@@ -213,23 +231,37 @@ class Builder {
   }
 
   void activity() {
-    int max_mode = -1;
-    std::map<int, int> leaf_node;
     for (int i = 0; i < n; ++i)
       if (nd[i].bottom()) {
         if (leaf_node.count(nd[i].leaf_mode)) throw std::runtime_error("duplicate leaf mode");
         leaf_node[nd[i].leaf_mode] = i;
-        max_mode = std::max(max_mode, nd[i].leaf_mode);
       }
-    inside.assign(n, std::vector<char>(max_mode + 1, 0));
-    for (int i = 0; i < n; ++i) {
-      if (nd[i].bottom()) inside[i][nd[i].leaf_mode] = 1;
-      for (int c : nd[i].children)
-        for (int m = 0; m <= max_mode; ++m) inside[i][m] |= inside[c][m];
+    // DFS intervals: node a's subtree holds exactly the nodes with tin in [tin[a], tout[a])
+    tin.assign(n, 0);
+    tout.assign(n, 0);
+    int clock = 0;
+    std::vector<std::pair<int, int>> stack;
+    for (int t : tops) {
+      stack.push_back({t, 0});
+      while (!stack.empty()) {
+        auto& top_ = stack.back();
+        const int a = top_.first;
+        if (top_.second == 0) tin[a] = clock++;
+        if (top_.second < (int)nd[a].children.size()) {
+          const int c = nd[a].children[top_.second++];
+          stack.push_back({c, 0});
+        } else {
+          tout[a] = clock;
+          stack.pop_back();
+        }
+      }
     }
-    act.assign(L, std::vector<char>(n, 0));
+    node_terms.assign(n, {});
+    term_nodes.assign(L, {});
+    std::vector<int> stamp(n, -1);
     for (int l = 0; l < L; ++l) {
       if (sop.ptr[l + 1] <= sop.ptr[l]) throw std::runtime_error("empty SOP term");
+      std::vector<int> nodes_l;
       for (int f = sop.ptr[l]; f < sop.ptr[l + 1]; ++f) {
         auto it = leaf_node.find(sop.mode[f]);
         if (it == leaf_node.end()) throw std::runtime_error("SOP factor on unknown mode");
@@ -237,8 +269,19 @@ class Builder {
         if (op < 0 || op >= (int)ops.kind.size()) throw std::runtime_error("bad operator id");
         if (ops.dim[op] != nd[it->second].shape[0])
           throw std::runtime_error("operator dim != leaf dim");
-        for (int a = it->second; a >= 0; a = nd[a].parent) act[l][a] = 1;
+        for (int a = it->second; a >= 0 && stamp[a] != l; a = nd[a].parent) {
+          stamp[a] = l;
+          nodes_l.push_back(a);
+        }
       }
+      std::sort(nodes_l.begin(), nodes_l.end());
+      int roots = 0;
+      for (int a : nodes_l) {
+        roots += is_top(a) ? 1 : 0;
+        node_terms[a].push_back(l);
+      }
+      if (roots != 1) throw std::runtime_error("an SOP term acts on leaves of several trees");
+      term_nodes[l] = std::move(nodes_l);
     }
   }
 
@@ -247,7 +290,7 @@ class Builder {
     std::vector<std::pair<int, int>> f;
     for (int x = sop.ptr[l]; x < sop.ptr[l + 1]; ++x) {
       int m = sop.mode[x];
-      if ((inside[a][m] != 0) == in) f.push_back({m, sop.op[x]});
+      if (inside_mode(a, m) == in) f.push_back({m, sop.op[x]});
     }
     std::stable_sort(f.begin(), f.end(),
                      [](const std::pair<int, int>& u, const std::pair<int, int>& v) {
@@ -276,7 +319,7 @@ class Builder {
       P.rhoinv_off[i] = alloc_mat(d);
       P.u_off[i] = alloc_mat(d);
       P.max_eig_d = std::max(P.max_eig_d, d);
-      if (i != top) {
+      if (!is_top(i)) {
         P.s_off[i] = alloc_mat(d);
         P.sinv_off[i] = alloc_mat(d);
         P.d_off[i] = alloc_mat(d);
@@ -294,30 +337,38 @@ class Builder {
         int d = nd[i].dup();
         P.rho64_off[i] = alloc_mat(d);
         P.rhoinv64_off[i] = alloc_mat(d);
-        if (i != top) {
+        if (!is_top(i)) {
           P.s64_off[i] = alloc_mat(d);
           P.d64_off[i] = alloc_mat(d);
           P.m2_64_off[i] = alloc_mat(d);
         }
       }
     }
-    int dt = nd[top].dup();
-    P.energy_dev_off = alloc_mat(dt);
-    P.stop_dev_off = alloc_mat(dt);
-    P.energy_off = P.prec == 1 ? alloc_mat(dt) : P.energy_dev_off;
-    P.stop_off = P.prec == 1 ? alloc_mat(dt) : P.stop_dev_off;
-    int64_t ident_top = alloc_mat(dt);
-    P.identities.push_back({ident_top, dt});
-    P.identities.push_back({P.rho_off[top], dt});
+    std::vector<int64_t> ident(n, -1);
+    for (int t : tops) {
+      int dt = nd[t].dup();
+      P.tops.push_back(t);
+      P.energy_dev_off.push_back(alloc_mat(dt));
+      P.stop_dev_off.push_back(alloc_mat(dt));
+      P.energy_off.push_back(P.prec == 1 ? alloc_mat(dt) : P.energy_dev_off.back());
+      P.stop_off.push_back(P.prec == 1 ? alloc_mat(dt) : P.stop_dev_off.back());
+      ident[t] = alloc_mat(dt);
+      P.identities.push_back({ident[t], dt});
+      P.identities.push_back({P.rho_off[t], dt});
+    }
     // represent / mean-field slots
-    P.hslot.assign(L, std::vector<int64_t>(n, -1));
-    P.cslot.assign(L, std::vector<int64_t>(n, -1));
-    for (int l = 0; l < L; ++l)
-      for (int a = 0; a < n; ++a) {
-        if (!act[l][a]) continue;
-        if (a == top) {
-          P.hslot[l][a] = -2;  // the reference leaves the top's represent matrix at zero
-          P.cslot[l][a] = ident_top;
+    node_hslot.assign(n, {});
+    node_cslot.assign(n, {});
+    for (int a = 0; a < n; ++a) {
+      node_hslot[a].assign(node_terms[a].size(), -1);
+      node_cslot[a].assign(node_terms[a].size(), -1);
+      hslot_of_key.clear();  // keys carry the node, so slots never cross nodes
+      cslot_of_key.clear();
+      for (size_t i = 0; i < node_terms[a].size(); ++i) {
+        const int l = node_terms[a][i];
+        if (is_top(a)) {
+          node_hslot[a][i] = -2;  // the reference leaves the top's represent matrix at zero
+          node_cslot[a][i] = ident[a];
           continue;
         }
         std::vector<int> kin = grouped ? key(l, a, true) : std::vector<int>{a, 1, l};
@@ -325,19 +376,29 @@ class Builder {
         if (it == hslot_of_key.end()) {
           int64_t o = alloc_mat(nd[a].dup());
           hslot_of_key[kin] = o;
-          P.hslot[l][a] = o;
+          node_hslot[a][i] = o;
         } else {
-          P.hslot[l][a] = it->second;
+          node_hslot[a][i] = it->second;
         }
         std::vector<int> kout = grouped ? key(l, a, false) : std::vector<int>{a, 0, l};
         auto jt = cslot_of_key.find(kout);
         if (jt == cslot_of_key.end()) {
           int64_t o = alloc_mat(nd[a].dup());
           cslot_of_key[kout] = o;
-          P.cslot[l][a] = o;
+          node_cslot[a][i] = o;
         } else {
-          P.cslot[l][a] = jt->second;
+          node_cslot[a][i] = jt->second;
         }
+      }
+    }
+    // per-term view for downloads (active nodes ascending)
+    P.term_nodes = term_nodes;
+    P.term_hslot.assign(L, {});
+    P.term_cslot.assign(L, {});
+    for (int l = 0; l < L; ++l)
+      for (int a : term_nodes[l]) {
+        P.term_hslot[l].push_back(hslot(l, a));
+        P.term_cslot[l].push_back(cslot(l, a));
       }
   }
 
@@ -394,7 +455,7 @@ class Builder {
                 const char* name, bool skip_top) {
     int64_t c0 = (int64_t)P.cvt.size(), t0 = (int64_t)P.cvt_tiles.size();
     for (int a = 0; a < n; ++a) {
-      if (skip_top && a == top) continue;
+      if (skip_top && is_top(a)) continue;
       if (src[a] < 0 || dst[a] < 0) continue;
       add_cvt(mat(src[a]), mat(dst[a]), (int64_t)nd[a].dup() * nd[a].dup(), dir);
     }
@@ -558,8 +619,8 @@ class Builder {
     } else {
       for (size_t k = 0; k < g.children.size(); ++k) {
         int c = g.children[k];
-        if (!act[l][c]) continue;
-        o.push_back(COp{0, (int)k, mat(P.hslot[l][c]), c2(1, 0)});
+        if (!act(l, c)) continue;
+        o.push_back(COp{0, (int)k, mat(hslot(l, c)), c2(1, 0)});
       }
     }
     if (!o.empty()) o[0].alpha = alpha;
@@ -567,15 +628,16 @@ class Builder {
   }
 
   void stage_represent() {
-    int maxh = nd[top].height;
+    int maxh = 0;
+    for (int t : tops) maxh = std::max(maxh, nd[t].height);
     for (int h = 0; h < maxh; ++h) {
       std::vector<Item> items;
       std::set<int64_t> done;
       for (int a = 0; a < n; ++a) {
-        if (nd[a].height != h || a == top) continue;
-        for (int l = 0; l < L; ++l) {
-          if (!act[l][a]) continue;
-          int64_t slot = P.hslot[l][a];
+        if (nd[a].height != h || is_top(a)) continue;
+        for (size_t i = 0; i < node_terms[a].size(); ++i) {
+          const int l = node_terms[a][i];
+          int64_t slot = node_hslot[a][i];
           if (!done.insert(slot).second) continue;
           Item it;
           it.node = a;
@@ -601,9 +663,9 @@ class Builder {
       for (int a = 0; a < n; ++a) {
         if (nd[a].depth != d) continue;
         int p = nd[a].parent;
-        for (int l = 0; l < L; ++l) {
-          if (!act[l][a]) continue;
-          int64_t slot = P.cslot[l][a];
+        for (size_t i = 0; i < node_terms[a].size(); ++i) {
+          const int l = node_terms[a][i];
+          int64_t slot = node_cslot[a][i];
           if (!done.insert(slot).second) continue;
           Item it;
           it.node = p;
@@ -611,10 +673,10 @@ class Builder {
           const NodeGeo& gp = nd[p];
           for (size_t k = 0; k < gp.children.size(); ++k) {
             int c = gp.children[k];
-            if ((int)k == nd[a].child_idx || !act[l][c]) continue;
-            it.ops.push_back(COp{0, (int)k, mat(P.hslot[l][c]), c2(1, 0)});
+            if ((int)k == nd[a].child_idx || !act(l, c)) continue;
+            it.ops.push_back(COp{0, (int)k, mat(hslot(l, c)), c2(1, 0)});
           }
-          if (!gp.top()) it.ops.push_back(COp{0, gp.last(), mat(P.cslot[l][p]), c2(1, 0)});
+          if (!gp.top()) it.ops.push_back(COp{0, gp.last(), mat(cslot(l, p)), c2(1, 0)});
           it.fin = 0;
           it.S = mat(slot);
           it.hp_mode = nd[a].child_idx;
@@ -633,8 +695,7 @@ class Builder {
     for (int a = 0; a < n; ++a) {
       std::map<std::vector<int>, std::vector<int>> groups;
       std::vector<std::vector<int>> order;
-      for (int l = 0; l < L; ++l) {
-        if (!act[l][a]) continue;
+      for (int l : node_terms[a]) {
         std::vector<int> k = grouped ? key(l, a, true) : std::vector<int>{a, 1, l};
         auto it = groups.find(k);
         if (it == groups.end()) {
@@ -653,7 +714,7 @@ class Builder {
         lt.d = d;
         lt.first = (int)P.lin_terms.size();
         lt.count = (int)terms.size();
-        for (int l : terms) P.lin_terms.push_back(Plan::SLinTerm{sop.coeff[l], mat(P.cslot[l][a])});
+        for (int l : terms) P.lin_terms.push_back(Plan::SLinTerm{sop.coeff[l], mat(cslot(l, a))});
         P.lin.push_back(lt);
         Item it;
         it.node = a;
@@ -680,9 +741,10 @@ class Builder {
     // overlaps S = Phi^dag Phi and D = Phi^dag (H Phi) of every node
     int64_t t0 = (int64_t)P.hp.size(), tile0 = (int64_t)P.hp_tiles.size();
     for (int a = 0; a < n; ++a) {
-      if (a == top) {
-        add_hp(psi(a), hphi(a), mat(P.energy_dev_off), a, nd[a].last());
-        add_hp(psi(a), psi(a), mat(P.stop_dev_off), a, nd[a].last());
+      if (is_top(a)) {
+        const size_t k = std::find(tops.begin(), tops.end(), a) - tops.begin();
+        add_hp(psi(a), hphi(a), mat(P.energy_dev_off[k]), a, nd[a].last());
+        add_hp(psi(a), psi(a), mat(P.stop_dev_off[k]), a, nd[a].last());
       } else {
         add_hp(psi(a), psi(a), mat(P.s_off[a]), a, nd[a].last());
         add_hp(psi(a), hphi(a), mat(P.d_off[a]), a, nd[a].last());
@@ -696,17 +758,19 @@ class Builder {
       int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
       for (size_t i = 0; i < src.size(); ++i) {
         int a = (int)(i % n);
-        if (a == top) continue;
+        if (is_top(a)) continue;
         add_cvt(mat(src[i]), mat(dst[i]), (int64_t)nd[a].dup() * nd[a].dup(), 1);
       }
-      int dt = nd[top].dup();
-      add_cvt(mat(P.energy_dev_off), mat(P.energy_off), (int64_t)dt * dt, 1);
-      add_cvt(mat(P.stop_dev_off), mat(P.stop_off), (int64_t)dt * dt, 1);
+      for (size_t k = 0; k < tops.size(); ++k) {
+        int dt = nd[tops[k]].dup();
+        add_cvt(mat(P.energy_dev_off[k]), mat(P.energy_off[k]), (int64_t)dt * dt, 1);
+        add_cvt(mat(P.stop_dev_off[k]), mat(P.stop_off[k]), (int64_t)dt * dt, 1);
+      }
       emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "overlaps-to-f64");
     }
     int64_t p0 = (int64_t)P.proj.size();
     for (int a = 0; a < n; ++a) {
-      if (a == top) continue;
+      if (is_top(a)) continue;
       Plan::SProj pj;
       pj.S = mat(P.s64_off[a]);
       pj.D = mat(P.d64_off[a]);
@@ -724,7 +788,7 @@ class Builder {
     int64_t a0 = (int64_t)P.acc.size(), atile0 = (int64_t)P.acc_tiles.size();
     for (int a = 0; a < n; ++a) {
       std::vector<Plan::SAccTerm> terms;
-      if (a == top) {
+      if (is_top(a)) {
         terms.push_back(Plan::SAccTerm{Ref{-1, 0}, hphi(a)});
       } else {
         terms.push_back(Plan::SAccTerm{mat(P.rhoinv_off[a]), hphi(a)});
@@ -747,7 +811,7 @@ class Builder {
   void count_reference_flops() {
     double F = 0;
     for (int a = 0; a < n; ++a) {
-      if (a == top) continue;
+      if (is_top(a)) continue;
       const NodeGeo& p = nd[nd[a].parent];
       F += 8.0 * p.N * p.dup() + 8.0 * p.N * nd[a].dup();
     }
@@ -759,30 +823,29 @@ class Builder {
           if (sop.mode[x] == g.leaf_mode) f += ops.kind[sop.op[x]] == 0 ? 8.0 * g.N * g.shape[0] : 6.0 * g.N;
       } else {
         for (size_t k = 0; k < g.children.size(); ++k)
-          if (act[l][g.children[k]]) f += 8.0 * g.N * g.shape[k];
+          if (act(l, g.children[k])) f += 8.0 * g.N * g.shape[k];
       }
       return f;
     };
     for (int l = 0; l < L; ++l)
-      for (int a = 0; a < n; ++a) {
-        if (!act[l][a]) continue;
+      for (int a : term_nodes[l]) {
         const NodeGeo& g = nd[a];
-        double app = 6.0 * g.N + body_flops(l, a) + (a == top ? 2.0 * g.N : 8.0 * g.N * g.dup() + 2.0 * g.N);
+        double app = 6.0 * g.N + body_flops(l, a) + (is_top(a) ? 2.0 * g.N : 8.0 * g.N * g.dup() + 2.0 * g.N);
         F += app;
-        if (a == top) {
+        if (is_top(a)) {
           F += app;  // Expectation repeats Apply at the top
           continue;
         }
         F += body_flops(l, a) + 8.0 * g.N * g.dup();  // represent
         const NodeGeo& p = nd[g.parent];
         for (size_t k = 0; k < p.children.size(); ++k)
-          if ((int)k != g.child_idx && act[l][p.children[k]]) F += 8.0 * p.N * p.shape[k];
+          if ((int)k != g.child_idx && act(l, p.children[k])) F += 8.0 * p.N * p.shape[k];
         if (!p.top()) F += 8.0 * p.N * p.dup();
         F += 8.0 * p.N * g.dup();  // mean field
       }
     for (int a = 0; a < n; ++a) {
       const NodeGeo& g = nd[a];
-      if (a == top) {
+      if (is_top(a)) {
         F += 6.0 * g.N + 8.0 * g.N * g.dup();
       } else {
         F += 24.0 * g.N * g.dup() + 2.0 * g.N + 8.0 * g.N * g.dup() + 6.0 * g.N;

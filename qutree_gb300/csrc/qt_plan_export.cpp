@@ -160,7 +160,13 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       }
       break;
     case 9:
-      v = {P.psi_arena, P.mats_size, P.scratch_size, P.ops_size, P.energy_off, P.stop_off, P.prec};
+      v = {P.psi_arena, P.mats_size, P.scratch_size, P.ops_size, P.energy_off[0], P.stop_off[0], P.prec,
+           (int64_t)P.tops.size()};
+      for (size_t k = 0; k < P.tops.size(); ++k) {
+        v.push_back(P.tops[k]);
+        v.push_back(P.energy_off[k]);
+        v.push_back(P.stop_off[k]);
+      }
       break;
     case 18:
       for (auto& t : P.cvt) {
@@ -182,13 +188,15 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
     case 12:
       v = P.rhoinv64_off;
       break;
-    case 13:
-    case 14: {
-      const auto& sl = what == 13 ? P.hslot : P.cslot;
-      for (auto& row : sl)
-        for (auto x : row) v.push_back(x);
+    case 13:  // (term, node, hslot, cslot) of every active pair
+      for (size_t l = 0; l < P.term_nodes.size(); ++l)
+        for (size_t i = 0; i < P.term_nodes[l].size(); ++i) {
+          v.push_back((int64_t)l);
+          v.push_back(P.term_nodes[l][i]);
+          v.push_back(P.term_hslot[l][i]);
+          v.push_back(P.term_cslot[l][i]);
+        }
       break;
-    }
     case 15:
       for (auto& t : P.mp) {
         dv.push_back(t.alpha.x);

@@ -653,3 +653,106 @@ def config_problem(cfg: int, seed_base: int = 20261203):
     tree, sop = config_tree_sop(cfg, seed_base)
     psi = random_wavefunction(tree, seed_base + cfg)
     return tree, sop, psi
+
+
+# --------------------------------------------------------------------------
+# Forests: many independent trees in one sweep
+# --------------------------------------------------------------------------
+def balance_bonds(tree: Tree) -> Tree:
+    """Clamp bonds so every density matrix can have full rank: top-down, a
+    child's bond may not exceed its parent's bond times the product of its
+    siblings' bonds (with a bond-1 top, both children of a binary top get the
+    same bond).  Shapes are edited in place; returns the tree."""
+    changed = True
+    while changed:
+        changed = False
+        for p in reversed(tree.nodes):
+            if p.is_bottom:
+                continue
+            dims = list(p.shape)
+            for k, c in enumerate(p.children):
+                cap = dims[-1]
+                for j in range(len(p.children)):
+                    if j != k:
+                        cap *= dims[j]
+                if dims[k] > cap:
+                    dims[k] = cap
+                    cn = tree.nodes[c]
+                    cn.shape = tuple(list(cn.shape[:-1]) + [cap])
+                    changed = True
+            p.shape = tuple(dims)
+    return tree
+
+
+def forest(trees):
+    """Concatenate independent trees into one forest descriptor: node
+    addresses and leaf modes are offset tree by tree (every tree's nodes
+    precede its root).  Returns (forest, node_offsets, mode_offsets)."""
+    f = Tree.__new__(Tree)
+    f.nodes = []
+    f.leaf_node = {}
+    node_off, mode_off = [], []
+    na = nm = 0
+    for t in trees:
+        node_off.append(na)
+        mode_off.append(nm)
+        for n in t.nodes:
+            m = Node(address=n.address + na, shape=n.shape,
+                     parent=(n.parent + na) if n.parent >= 0 else -1,
+                     children=[c + na for c in n.children], child_idx=n.child_idx,
+                     leaf_mode=(n.leaf_mode + nm) if n.leaf_mode >= 0 else -1, height=n.height)
+            f.nodes.append(m)
+            if m.leaf_mode >= 0:
+                f.leaf_node[m.leaf_mode] = m.address
+        na += t.n_nodes
+        nm += t.n_leaves
+    f.tops = [n.address for n in f.nodes if n.parent < 0]
+    return f, node_off, mode_off
+
+
+def forest_sop(sops, mode_off):
+    """One SOP over a forest: every term keeps its own tree's leaves (modes
+    offset), operators pooled into one table."""
+    ops = OperatorTable()
+    out = SOP(ops)
+    for sop, mo in zip(sops, mode_off):
+        remap = {}
+        for l, term in enumerate(sop.terms):
+            fac = []
+            for (m, o) in term.factors:
+                if o not in remap:
+                    remap[o] = ops.add(None, sop.ops.kind[o], sop.ops.dense(o) if sop.ops.kind[o] == OP_DENSE
+                                       else sop.ops.data[o])
+                fac.append((m + mo, remap[o]))
+            out.push_back(MLO(fac), sop.coeffs[l])
+    return out
+
+
+def forest_psi(f, psis):
+    return TensorTree(f, [t for p in psis for t in p.tensors])
+
+
+def batched_problem(n_trees: int, seed_base: int = 20261203, modes=(8, 16, 32, 48),
+                    pdims=(8, 16, 32), bond_range=(4, 24), couplings=(2, 6)):
+    """The many-tree batch: every tree draws its mode count, physical
+    dimension and per-edge bonds (uniform in bond_range, clamped to the
+    product of the child dims and to p at the bottom), and carries its own
+    seeded coupled-oscillator SOP with couplings[0]..couplings[1] random
+    partners per mode.  Bonds are then balanced (``balance_bonds``) so that
+    no density matrix is rank deficient by construction.  Returns
+    (trees, sops, psis)."""
+    trees, sops, psis = [], [], []
+    for t in range(n_trees):
+        rng = np.random.default_rng(seed_base + 2 + 7919 * t)
+        f = int(rng.choice(modes))
+        p = int(rng.choice(pdims))
+        edge_rng = np.random.default_rng(seed_base + 3 + 7919 * t)
+        tree = balance_bonds(balanced_tree(
+            f, p, bond_range[1],
+            bonds=lambda h, pp: int(edge_rng.integers(bond_range[0], bond_range[1] + 1))))
+        sop = coupled_oscillators(tree, coupling=0.1, rng=rng, pairs_per_mode=couplings)
+        psi = random_wavefunction(tree, seed_base + 4 + 7919 * t)
+        trees.append(tree)
+        sops.append(sop)
+        psis.append(psi)
+    return trees, sops, psis

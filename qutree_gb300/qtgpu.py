@@ -98,6 +98,8 @@ def load(build_if_missing: bool = True):
         "qt_probe_fp64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_rho_inverse_noalloc": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double],
                                    ctypes.c_int),
+        "qt_tree_count": ([_vp], ctypes.c_int),
+        "qt_energies": ([_vp, _vp, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -118,6 +120,7 @@ def exported_symbols():
         "qt_hole_product", "qt_last_mode_product", "qt_dev_alloc", "qt_dev_free",
         "qt_memcpy_h2d", "qt_memcpy_d2h", "qt_launch_count", "qt_stage_count",
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
+        "qt_tree_count", "qt_energies",
     ]
 
 
@@ -256,6 +259,14 @@ class HamiltonianRepresentation:
     def energy(self) -> float:
         h00, s00 = self.energy_parts()
         return h00.real / s00.real
+
+    def energies(self) -> np.ndarray:
+        """Energy of every tree of a forest (roots in ascending address order)."""
+        nt = int(self.ctx.L.qt_tree_count(self.ctx.h))
+        out = np.zeros(4 * nt)
+        self.ctx.check(self.ctx.L.qt_energies(self.ctx.h, _ptr(out), nt))
+        o = out.reshape(nt, 4)
+        return o[:, 0] / o[:, 2]
 
     def matrices(self, which: int) -> np.ndarray:
         n = int(self.ctx.L.qt_matrices_size(self.ctx.h, which))

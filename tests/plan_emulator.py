@@ -75,8 +75,8 @@ class PlanView:
         self.h = h
         self.tree, self.sop = tree, sop
         self.tables = {}
-        widths = {0: 5, 1: 11, 2: 9, 3: 8, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 18: 6}
-        for what in list(range(15)) + [18]:
+        widths = {0: 5, 1: 11, 2: 9, 3: 8, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6}
+        for what in list(range(14)) + [18]:
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -94,9 +94,7 @@ class PlanView:
         self.mp_alpha = self.tables[15].reshape(-1, 2) @ np.array([1, 1j]) if len(self.tables[15]) else np.zeros(0)
         self.lin_c = self.tables[16].reshape(-1, 2) @ np.array([1, 1j]) if len(self.tables[16]) else np.zeros(0)
         L.qtp_free(h)
-        n = tree.n_nodes
-        self.hslot = self.tables[13].reshape(len(sop), n)
-        self.cslot = self.tables[14].reshape(len(sop), n)
+        self.pairs = self.tables[13]  # rows (term, node, hslot, cslot), terms ascending
         s = self.tables[9]
         self.psi_arena, self.mats_size, self.scratch_size, self.ops_size = map(int, s[:4])
         self.energy_off, self.stop_off = int(s[4]), int(s[5])
@@ -204,14 +202,9 @@ class PlanView:
 
     def sparse(self, which):
         """hmat (which=0) or hcon (which=1) in the oracle's sparse layout."""
-        slots = self.hslot if which == 0 else self.cslot
         out = []
-        for l in range(len(self.sop)):
-            for n in self.tree.nodes:
-                s = self.hslot[l, n.address]
-                if s == -1:
-                    continue
-                dd = n.d_up * n.d_up
-                s2 = slots[l, n.address]
-                out.append(self.bufs[B_MATS][s2:s2 + dd] if s2 >= 0 else np.zeros(dd, np.complex128))
+        for l, a, hs, cs in self.pairs:
+            dd = self.tree.nodes[a].d_up ** 2
+            s2 = hs if which == 0 else cs
+            out.append(self.bufs[B_MATS][s2:s2 + dd] if s2 >= 0 else np.zeros(dd, np.complex128))
         return np.concatenate(out)

@@ -18,8 +18,8 @@ import oracle as O
 from helpers import deriv_errors, rel_err, rho_condition, rho_weighted
 from qutree_gb300 import qtgpu
 from qutree_gb300.model import (MLO, OP_DENSE, SOP, HOBasis, OperatorTable, balanced_tree,
-                                config_problem, coupled_oscillators, hartree_wavefunction,
-                                random_wavefunction)
+                                batched_problem, config_problem, coupled_oscillators, forest,
+                                forest_psi, forest_sop, hartree_wavefunction, random_wavefunction)
 
 pytestmark = pytest.mark.gpu
 # complex128 (FP64 pipe): unit roundoff 2^-53
@@ -163,5 +163,29 @@ def test_errors_are_reported_not_fatal():
         hrep.upload(psi)
         hrep.derivative()
         assert np.isfinite(hrep.energy())
+    finally:
+        hrep.close()
+
+
+@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64])
+def test_forest_of_uneven_trees(flavour):
+    # 24 trees of 8..48 modes, p in {8,16,32}, random bonds 4..24, one plan and
+    # one graph; every tree's slice and energy equal its own oracle sweep
+    df = bool(flavour & qtgpu.QT_PREC_DF64)
+    tol = TOL_DF if df else TOL
+    trees, sops, psis = batched_problem(24)
+    f, node_off, mode_off = forest(trees)
+    hrep = qtgpu.HamiltonianRepresentation(forest_sop(sops, mode_off), f, flavour=flavour)
+    try:
+        d = qtgpu.Derivative(hrep, forest_psi(f, psis).flat())
+        energies = hrep.energies()
+        assert len(energies) == len(trees)
+        off = f.offsets()
+        for k, (t, s, p) in enumerate(zip(trees, sops, psis)):
+            r = O.derivative(t, s, p.flat())
+            assert abs(energies[k] - r.energy) <= tol * max(1.0, abs(r.energy))
+            seg = d[off[node_off[k]]:off[node_off[k] + t.n_nodes]]
+            err, noise = deriv_errors(t, seg, r.dpsi, r.rho)
+            assert err <= tol and noise <= NOISE
     finally:
         hrep.close()

@@ -6,8 +6,10 @@ import pytest
 import oracle as O
 from helpers import rel_err, rho_weighted
 from plan_emulator import PlanView
+from helpers import deriv_errors
 from qutree_gb300.model import (MLO, OP_DENSE, SOP, HOBasis, OperatorTable, balanced_tree,
-                                config_problem, config_tree_sop, coupled_oscillators,
+                                batched_problem, config_problem, config_tree_sop,
+                                coupled_oscillators, forest, forest_psi, forest_sop,
                                 random_wavefunction)
 
 
@@ -108,3 +110,30 @@ def test_plan_rejects_bad_input():
     s.push_back(MLO([(0, bad)]), 1.0)
     with pytest.raises(ValueError, match="operator dim"):
         PlanView(tree, s, 0)
+
+
+@pytest.mark.parametrize("flavour,prec", [(0, 1), (1, 0)])
+def test_plan_forest(flavour, prec):
+    # many uneven trees in one plan: each tree's slice equals its own sweep
+    trees, sops, psis = batched_problem(5)
+    f, node_off, mode_off = forest(trees)
+    pv = PlanView(f, forest_sop(sops, mode_off), flavour, prec=prec)
+    pv.run(forest_psi(f, psis).flat())
+    d = pv.dpsi()
+    off = f.offsets()
+    for k, (t, s, p) in enumerate(zip(trees, sops, psis)):
+        r = O.derivative(t, s, p.flat())
+        seg = d[off[node_off[k]]:off[node_off[k] + t.n_nodes]]
+        err, noise = deriv_errors(t, seg, r.dpsi, r.rho)
+        assert err <= 1e-12 and noise <= 1e-11
+
+
+def test_plan_rejects_cross_tree_terms():
+    trees, sops, psis = batched_problem(2)
+    f, node_off, mode_off = forest(trees)
+    s = forest_sop(sops, mode_off)
+    a = s.ops.add(None, 1, np.ones(trees[0].leaf_dim(0), complex))
+    b = s.ops.add(None, 1, np.ones(trees[1].leaf_dim(0), complex))
+    s.push_back(MLO([(0, a), (mode_off[1], b)]), 1.0)
+    with pytest.raises(ValueError, match="several trees"):
+        PlanView(f, s, 1)
