@@ -61,6 +61,15 @@ extern "C" {
 #define QT_PREC_F64 0x000
 #define QT_PREC_DF64 0x100
 
+/* OR-ed into the plan flavour: every sweep also computes the gradient of
+ * E = <Psi|H|Psi>/<Psi|Psi> with respect to every node tensor,
+ * dE/dPhi_n^* (Wirtinger), assuming the orthonormal gauge QuTree keeps
+ * (all non-top nodes orthonormal): (Apply(n) + Phi_n x_last Eout[n]
+ * - E Phi_n x_last rho[n]) / <Psi|Psi>, with Eout[n] the mean field of the
+ * terms acting only outside n.  Read it with qt_gradient_download.  No
+ * counterpart in the reference (QuTree has no tree-network gradient). */
+#define QT_PLAN_GRADIENT 0x1000
+
 /* Matrix sets for qt_matrices_download. */
 #define QT_MAT_RHO 0     /* density matrices, per node, d_up x d_up          */
 #define QT_MAT_RHOINV 1  /* regularised inverse density matrices             */
@@ -136,6 +145,9 @@ int64_t qt_psi_size(const qt_ctx* ctx); /* complex elements, packed */
  * the context stream. */
 int qt_derivative(qt_ctx* ctx, double phase_re, double phase_im);
 int qt_dpsi_download(qt_ctx* ctx, double* dpsi_host);
+/* Energy gradient of the last sweep (plans prepared with QT_PLAN_GRADIENT),
+ * packed layout like the wavefunction.  Synchronises. */
+int qt_gradient_download(qt_ctx* ctx, double* grad_host);
 int qt_dpsi_device(qt_ctx* ctx, const void** dpsi_dev);
 /* out[4] = { Re h00, Im h00, Re S00, Im S00 }, h00 = <Phi_top|H Phi_top>,
  * S00 = <Phi_top|Phi_top>; E = Re h00 / Re S00. Synchronises.  For a forest,

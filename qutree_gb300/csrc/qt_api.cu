@@ -73,6 +73,7 @@ void release_arena(qt_ctx* c) {
   // B_PSI64 / B_DPSI64 alias B_PSI / B_DPSI in complex128 plans: free once
   if (c->buf[qt::B_PSI64] == c->buf[qt::B_PSI]) c->buf[qt::B_PSI64] = nullptr;
   if (c->buf[qt::B_DPSI64] == c->buf[qt::B_DPSI]) c->buf[qt::B_DPSI64] = nullptr;
+  if (c->buf[qt::B_GRAD64] == c->buf[qt::B_GRAD]) c->buf[qt::B_GRAD64] = nullptr;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if (c->buf[i]) cudaFree(c->buf[i]);
     c->buf[i] = nullptr;
@@ -241,9 +242,10 @@ int qt_prepare(qt_ctx* c, int flavour) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->have_tree || !c->have_sop) return fail(c, QT_ERR_STATE, "qt_prepare needs tree and SOP");
   const int prec = (flavour & QT_PREC_DF64) ? 1 : 0;
-  if ((flavour & ~QT_PREC_DF64) != QT_PLAN_REFERENCE && (flavour & ~QT_PREC_DF64) != QT_PLAN_GROUPED)
+  const bool grad = (flavour & QT_PLAN_GRADIENT) != 0;
+  flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT);
+  if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
-  flavour &= ~QT_PREC_DF64;
   QT_CUDA(c, cudaSetDevice(c->device));
   release_arena(c);
   int64_t budget = (int64_t)1 << 28;  // scratch elements (4 GiB)
@@ -251,7 +253,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     long v = std::atol(s);
     if (v > 0) budget = (int64_t)v * (1 << 20) / 16;
   }
-  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour, prec, budget);
+  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour, prec, budget, grad);
   if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
   Plan& P = c->plan;
   c->buf_elems[qt::B_PSI] = P.psi_arena;
@@ -263,9 +265,12 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_PARAM] = 16;
   c->buf_elems[qt::B_PSI64] = prec == 1 ? P.psi_arena : 0;
   c->buf_elems[qt::B_DPSI64] = prec == 1 ? P.psi_arena : 0;
+  c->buf_elems[qt::B_GRAD] = grad ? P.psi_arena : 0;
+  c->buf_elems[qt::B_GRAD64] = (grad && prec == 1) ? P.psi_arena : 0;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
-    if ((i == qt::B_PSI64 || i == qt::B_DPSI64) && prec == 0) continue;  // aliases, set below
+    if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
+    if ((i == qt::B_GRAD || i == qt::B_GRAD64) && !grad) continue;
     int64_t n = std::max<int64_t>(c->buf_elems[i], 16);
     cudaError_t e = cudaMalloc((void**)&c->buf[i], n * sizeof(double2));
     if (e != cudaSuccess) {
@@ -277,6 +282,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   if (prec == 0) {
     c->buf[qt::B_PSI64] = c->buf[qt::B_PSI];
     c->buf[qt::B_DPSI64] = c->buf[qt::B_DPSI];
+    c->buf[qt::B_GRAD64] = c->buf[qt::B_GRAD];
   }
   c->prec = prec;
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_MATS], 0, c->buf_elems[qt::B_MATS] * 16, c->stream));
@@ -330,7 +336,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   for (auto& s : P.acc) {
     qt::AccTask t;
     t.out = mptr_of(c, s.out);
-    t.alpha_ptr = s.alpha_param ? c->buf[qt::B_PARAM] : nullptr;
+    t.alpha_ptr = s.alpha_ref.buf >= 0 ? ptr_of(c, s.alpha_ref) : (s.alpha_param ? c->buf[qt::B_PARAM] : nullptr);
     t.alpha = s.alpha;
     t.rows = s.rows;
     t.d = s.d;
@@ -387,6 +393,19 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.pad = 0;
     cvt.push_back(t);
   }
+  std::vector<qt::GradTask> gtasks;
+  for (auto& s : P.grad) {
+    qt::GradTask t;
+    t.eout = ptr_of(c, s.eout);
+    t.rho = ptr_of(c, s.rho);
+    t.m3 = mptr_of(c, s.m3);
+    t.h00 = ptr_of(c, s.h00);
+    t.s00 = ptr_of(c, s.s00);
+    t.alpha = mptr_of(c, s.alpha);
+    t.d = s.d;
+    t.write_alpha = s.write_alpha;
+    gtasks.push_back(t);
+  }
   std::vector<char> blob;
   std::vector<int64_t> offs;
   put(blob, offs, mp);
@@ -402,6 +421,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, P.acc_tiles);
   put(blob, offs, cvt);
   put(blob, offs, P.cvt_tiles);
+  put(blob, offs, gtasks);
   {
     cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -425,6 +445,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.acc_tiles = (int4*)(base + offs[10]);
   c->tables.cvt = (qt::CvtTask*)(base + offs[11]);
   c->tables.cvt_tiles = (int2*)(base + offs[12]);
+  c->tables.grad = (qt::GradTask*)(base + offs[13]);
   for (auto& id : P.identities) {
     cudaError_t e = qt::launch_set_identity(c->buf[qt::B_MATS] + id.first, id.second, prec, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "set identity");
@@ -498,6 +519,16 @@ int qt_dpsi_download(qt_ctx* c, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_DPSI64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
+                             c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return QT_OK;
+}
+
+int qt_gradient_download(qt_ctx* c, double* out) {
+  if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
+  if (!c->plan.want_grad) return fail(c, QT_ERR_STATE, "plan prepared without QT_PLAN_GRADIENT");
+  QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_GRAD64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
                              c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   return QT_OK;

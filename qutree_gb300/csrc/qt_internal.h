@@ -92,7 +92,20 @@ struct CvtTask {
   int dir, pad;
 };
 
-enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT };
+// Energy-gradient preparation per node (orthonormal gauge):
+//   M3 = Eout - E * rho,  E = Re h00 / Re S00 of the node's tree,
+// and, on the tree's root task, alpha = 1 / Re S00 (complex128).
+struct GradTask {
+  const double2* eout;  // d x d, nullptr for a root (zero environment)
+  const double2* rho;   // d x d
+  double2* m3;          // d x d
+  const double2* h00;   // complex128 <Phi_top|H Phi_top> of the tree
+  const double2* s00;   // complex128 <Phi_top|Phi_top> of the tree
+  double2* alpha;       // complex128 1/S00, written when write_alpha != 0
+  int d, write_alpha;
+};
+
+enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD };
 
 struct Stage {
   int kind;
@@ -110,7 +123,12 @@ struct Stage {
 // With complex128 arithmetic they alias B_PSI / B_DPSI; with double-float
 // arithmetic B_PSI / B_HPHI / B_DPSI hold double-float numbers and conversion
 // stages move data across.
-enum Buf { B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_NBUF };
+// B_GRAD / B_GRAD64: energy gradient (arithmetic format / caller-facing
+// complex128; aliases with complex128 arithmetic), only when requested.
+enum Buf {
+  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64,
+  B_NBUF
+};
 
 struct Ref {
   int buf = -1;
@@ -182,6 +200,7 @@ struct Plan {
   };
   struct SAcc {
     Ref out;
+    Ref alpha_ref;  // device scalar (complex128) read as alpha when set
     bool alpha_param;
     double2 alpha;
     int rows, d, first, count, add;
@@ -216,6 +235,12 @@ struct Plan {
   std::vector<SEig> eig;
   std::vector<SProj> proj;
   std::vector<SCvt> cvt;
+  struct SGrad {
+    Ref eout, rho, m3, h00, s00, alpha;
+    int d, write_alpha;
+  };
+  std::vector<SGrad> grad;
+  bool want_grad = false;
   std::vector<Stage> stages;
   // tiles (bound with task indices only)
   std::vector<int2> mp_tiles;
@@ -241,9 +266,11 @@ struct SopDesc {
 };
 
 // planner entry point; returns "" on success or an error message
-// flavour: 0 reference call sequence, 1 grouped; prec: 0 complex128, 1 double-float
+// flavour: 0 reference call sequence, 1 grouped; prec: 0 complex128, 1 double-float;
+// grad: also compute the energy gradient with respect to every node tensor
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
-                       const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems);
+                       const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems,
+                       bool grad = false);
 
 // kernel launches (qt_kernels.cu)
 struct DevTables {
@@ -260,6 +287,7 @@ struct DevTables {
   int4* acc_tiles = nullptr;
   CvtTask* cvt = nullptr;
   int2* cvt_tiles = nullptr;
+  GradTask* grad = nullptr;
 };
 // prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe
 cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d, int prec,

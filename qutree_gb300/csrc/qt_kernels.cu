@@ -308,6 +308,24 @@ __global__ void __launch_bounds__(kThreads) k_lin(const LinTask* __restrict__ ta
   }
 }
 
+// Energy-gradient preparation: M3 = Eout - E rho per node, alpha = 1/S00.
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_grad(const GradTask* __restrict__ tasks, int64_t task0) {
+  typedef typename P::S S;
+  const GradTask t = tasks[task0 + blockIdx.x];
+  const double E = t.h00->x / t.s00->x;
+  const typename P::C mE = P::coef(make_double2(-E, 0.0));
+  const S* eout = reinterpret_cast<const S*>(t.eout);
+  const S* rho = reinterpret_cast<const S*>(t.rho);
+  S* m3 = reinterpret_cast<S*>(t.m3);
+  for (int e = threadIdx.x; e < t.d * t.d; e += kThreads) {
+    typename P::A acc = eout ? P::ld(eout + e) : P::zero();
+    P::cmac(acc, mE, P::ld(rho + e));
+    m3[e] = P::fin(acc);
+  }
+  if (t.write_alpha && threadIdx.x == 0) *t.alpha = make_double2(1.0 / t.s00->x, 0.0);
+}
+
 // Precision conversions: dir 0 complex128 -> double-float, dir 1 back.
 __global__ void __launch_bounds__(kThreads) k_cvt(const CvtTask* __restrict__ tasks,
                                                   const int2* __restrict__ tiles, int64_t tile0) {
@@ -760,6 +778,9 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       break;
     case ST_CVT:
       k_cvt<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.cvt, t.cvt_tiles, st.first_tile);
+      break;
+    case ST_GRAD:
+      k_grad<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.grad, st.first_task);
       break;
     default:
       return cudaErrorInvalidValue;

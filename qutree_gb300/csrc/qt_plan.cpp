@@ -96,7 +96,10 @@ class Builder {
     stage_represent();
     stage_meanfield();
     stage_apply();
+    if (P.want_grad) stage_environment();
     stage_final();
+    if (P.want_grad) stage_gradient();
+    P.mats_size = mats_cursor;
     count_reference_flops();
     P.stats.launches = (int64_t)P.stages.size();
   }
@@ -802,7 +805,149 @@ class Builder {
       add_cvt(Ref{B_DPSI, 0}, Ref{B_DPSI64, 0}, P.psi_packed, 1);
       emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "dpsi-out");
     }
-    P.mats_size = mats_cursor;
+  }
+
+  // ---- energy gradient (orthonormal gauge) --------------------------------
+  // dE/dPhi_n^* = (Apply(n) + Phi_n x_last Eout[n] - E Phi_n x_last rho[n]) / S00
+  // where Eout[n] is the mean field of every term acting entirely outside
+  // node n -- the terms the reference's sparse sweep leaves out because the
+  // MCTDH projector removes them.  Top-down: at the parent p, Eout[n] sums
+  //   (a) p's own environment Eout[p] on the parent index, and
+  //   (b) every term active at p but not at n: its represent matrices on the
+  //       siblings of n and its mean field H_l[p] on the parent index.
+  // Terms with the same sibling restriction share one chain; their mean
+  // fields are summed first (and Eout[p] joins the all-identity group).
+  std::vector<int64_t> eout_off;
+  void stage_environment() {
+    eout_off.assign(n, -1);
+    int maxdepth = 0;
+    for (auto& g : nd) maxdepth = std::max(maxdepth, g.depth);
+    for (int dep = 1; dep <= maxdepth; ++dep) {
+      std::vector<Item> items;
+      int64_t lin0 = (int64_t)P.lin.size();
+      std::vector<std::pair<int, std::vector<int64_t>>> sums;  // node -> temp slots
+      for (int a = 0; a < n; ++a) {
+        if (nd[a].depth != dep) continue;
+        const int p = nd[a].parent;
+        const NodeGeo& gp = nd[p];
+        eout_off[a] = alloc_mat(nd[a].dup());
+        // group the terms active at p but not at a by their sibling restrictions
+        std::map<std::vector<int>, std::vector<int>> groups;
+        std::vector<std::vector<int>> order;
+        for (int l : node_terms[p]) {
+          if (act(l, a)) continue;
+          std::vector<int> k;
+          for (size_t c = 0; c < gp.children.size(); ++c) {
+            const int ch = gp.children[c];
+            if (ch == a) continue;
+            if (act(l, ch)) {
+              std::vector<int> kk = key(l, ch, true);
+              k.insert(k.end(), kk.begin(), kk.end());
+            }
+            k.push_back(-1);
+          }
+          auto it = groups.find(k);
+          if (it == groups.end()) {
+            groups[k] = {l};
+            order.push_back(k);
+          } else {
+            it->second.push_back(l);
+          }
+        }
+        std::vector<int> idkey;
+        for (size_t c = 0; c + 1 < gp.children.size(); ++c) idkey.push_back(-1);
+        if (!gp.top() && !groups.count(idkey)) {
+          groups[idkey] = {};
+          order.push_back(idkey);
+        }
+        std::vector<int64_t> temps;
+        const int dp = gp.dup();
+        for (auto& k : order) {
+          const auto& terms = groups[k];
+          // G = sum_l c_l H_l[p] (+ Eout[p] for the all-identity group)
+          int64_t g = alloc_mat(dp);
+          Plan::SLin lt;
+          lt.out = mat(g);
+          lt.d = dp;
+          lt.first = (int)P.lin_terms.size();
+          for (int l : terms) P.lin_terms.push_back(Plan::SLinTerm{sop.coeff[l], mat(cslot(l, p))});
+          if (k == idkey && !gp.top()) P.lin_terms.push_back(Plan::SLinTerm{c2(1, 0), mat(eout_off[p])});
+          lt.count = (int)P.lin_terms.size() - lt.first;
+          P.lin.push_back(lt);
+          Item it;
+          it.node = p;
+          it.in = psi(p);
+          if (!terms.empty()) {
+            const int l0 = terms[0];
+            for (size_t c = 0; c < gp.children.size(); ++c) {
+              const int ch = gp.children[c];
+              if (ch == a || !act(l0, ch)) continue;
+              it.ops.push_back(COp{0, (int)c, mat(hslot(l0, ch)), c2(1, 0)});
+            }
+          }
+          it.ops.push_back(COp{0, gp.last(), mat(g), c2(1, 0)});
+          it.fin = 0;
+          int64_t tslot = alloc_mat(nd[a].dup());
+          it.S = mat(tslot);
+          it.hp_mode = nd[a].child_idx;
+          items.push_back(it);
+          temps.push_back(tslot);
+        }
+        sums.push_back({a, temps});
+      }
+      emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "environment-sums");
+      run_items(items, "environment", nullptr);
+      int64_t s0 = (int64_t)P.lin.size();
+      for (auto& pr : sums) {
+        Plan::SLin lt;
+        lt.out = mat(eout_off[pr.first]);
+        lt.d = nd[pr.first].dup();
+        lt.first = (int)P.lin_terms.size();
+        for (int64_t t : pr.second) P.lin_terms.push_back(Plan::SLinTerm{c2(1, 0), mat(t)});
+        lt.count = (int)pr.second.size();
+        P.lin.push_back(lt);
+      }
+      emit_stage(ST_LIN, s0, (int64_t)P.lin.size(), s0, (int64_t)P.lin.size(), "environment");
+    }
+  }
+
+  void stage_gradient() {
+    int64_t g0 = (int64_t)P.grad.size();
+    std::vector<int64_t> m3(n), alpha(tops.size());
+    for (size_t k = 0; k < tops.size(); ++k) alpha[k] = alloc_mat(1);
+    std::vector<int> tree_of(n, -1);
+    for (size_t k = 0; k < tops.size(); ++k)
+      for (int a = 0; a < n; ++a)
+        if (tin[a] >= tin[tops[k]] && tin[a] < tout[tops[k]]) tree_of[a] = (int)k;
+    for (int a = 0; a < n; ++a) {
+      const int k = tree_of[a];
+      Plan::SGrad t;
+      m3[a] = alloc_mat(nd[a].dup());
+      t.eout = is_top(a) ? Ref{-1, 0} : mat(eout_off[a]);
+      t.rho = mat(P.rho_off[a]);
+      t.m3 = mat(m3[a]);
+      t.h00 = mat(P.energy_off[k]);
+      t.s00 = mat(P.stop_off[k]);
+      t.alpha = mat(alpha[k]);
+      t.d = nd[a].dup();
+      t.write_alpha = is_top(a) ? 1 : 0;
+      P.grad.push_back(t);
+    }
+    emit_stage(ST_GRAD, g0, (int64_t)P.grad.size(), g0, (int64_t)P.grad.size(), "gradient-prep");
+    int64_t a0 = (int64_t)P.acc.size(), atile0 = (int64_t)P.acc_tiles.size();
+    for (int a = 0; a < n; ++a) {
+      std::vector<Plan::SAccTerm> terms;
+      terms.push_back(Plan::SAccTerm{Ref{-1, 0}, hphi(a)});
+      terms.push_back(Plan::SAccTerm{mat(m3[a]), psi(a)});
+      add_acc(Ref{B_GRAD, nd[a].aoff}, true, c2(1, 0), a, terms, false);
+      P.acc.back().alpha_ref = mat(alpha[tree_of[a]]);
+    }
+    emit_stage(ST_ACC, a0, (int64_t)P.acc.size(), atile0, (int64_t)P.acc_tiles.size(), "gradient");
+    if (P.prec == 1) {
+      int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
+      add_cvt(Ref{B_GRAD, 0}, Ref{B_GRAD64, 0}, P.psi_packed, 1);
+      emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "gradient-out");
+    }
   }
 
   // Flops of the reference call sequence (independent of this plan):
@@ -858,8 +1003,10 @@ class Builder {
 }  // namespace
 
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
-                       const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems) {
+                       const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems,
+                       bool grad) {
   plan = Plan();
+  plan.want_grad = grad;
   try {
     if (prec != 0 && prec != 1) throw std::runtime_error("unknown precision");
     Builder b(plan, nodes, ops, sop, flavour, prec, scratch_budget_elems);

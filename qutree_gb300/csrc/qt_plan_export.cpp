@@ -29,6 +29,8 @@ void* qtp_build(int n_nodes, const int* order, const int* dims, const int* paren
                 const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
                 const int* term_ptr, const int* term_mode, const int* term_op, int flavour,
                 int prec, int64_t budget, char* err, int errlen) {
+  const bool grad = (flavour & 0x1000) != 0;
+  flavour &= ~0x1000;
   std::vector<qt::NodeGeo> nodes(n_nodes);
   int p = 0;
   for (int i = 0; i < n_nodes; ++i) {
@@ -58,7 +60,7 @@ void* qtp_build(int n_nodes, const int* order, const int* dims, const int* paren
   s.mode.assign(term_mode, term_mode + s.ptr[n_terms]);
   s.op.assign(term_op, term_op + s.ptr[n_terms]);
   Handle* h = new Handle();
-  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, prec, budget);
+  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, prec, budget, grad);
   if (!msg.empty()) {
     if (err && errlen > 0) {
       std::strncpy(err, msg.c_str(), errlen - 1);
@@ -115,7 +117,8 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
     case 3:
       for (auto& t : P.acc) {
         put_ref(v, t.out);
-        v.push_back(t.alpha_param ? 1 : 0);
+        v.push_back(t.alpha_ref.buf >= 0 ? 2 : (t.alpha_param ? 1 : 0));
+        v.push_back(t.alpha_ref.off);
         v.push_back(t.rows);
         v.push_back(t.d);
         v.push_back(t.first);
@@ -166,6 +169,18 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
         v.push_back(P.tops[k]);
         v.push_back(P.energy_off[k]);
         v.push_back(P.stop_off[k]);
+      }
+      break;
+    case 19:
+      for (auto& t : P.grad) {
+        put_ref(v, t.eout);
+        put_ref(v, t.rho);
+        put_ref(v, t.m3);
+        put_ref(v, t.h00);
+        put_ref(v, t.s00);
+        put_ref(v, t.alpha);
+        v.push_back(t.d);
+        v.push_back(t.write_alpha);
       }
       break;
     case 18:

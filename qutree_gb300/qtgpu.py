@@ -27,6 +27,7 @@ QT_PLAN_REFERENCE = 0
 QT_PLAN_GROUPED = 1
 QT_PREC_F64 = 0x000
 QT_PREC_DF64 = 0x100
+QT_PLAN_GRADIENT = 0x1000
 QT_MAT_RHO, QT_MAT_RHOINV, QT_MAT_HMAT, QT_MAT_HCON = 0, 1, 2, 3
 ERRORS = {1: "QT_ERR_ARG", 2: "QT_ERR_SHAPE", 3: "QT_ERR_ALLOC", 4: "QT_ERR_CUDA",
           5: "QT_ERR_STATE", 6: "QT_ERR_NUMERIC"}
@@ -99,6 +100,7 @@ def load(build_if_missing: bool = True):
         "qt_rho_inverse_noalloc": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double],
                                    ctypes.c_int),
         "qt_tree_count": ([_vp], ctypes.c_int),
+        "qt_gradient_download": ([_vp, _vp], ctypes.c_int),
         "qt_energies": ([_vp, _vp, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -120,7 +122,7 @@ def exported_symbols():
         "qt_hole_product", "qt_last_mode_product", "qt_dev_alloc", "qt_dev_free",
         "qt_memcpy_h2d", "qt_memcpy_d2h", "qt_launch_count", "qt_stage_count",
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
-        "qt_tree_count", "qt_energies",
+        "qt_tree_count", "qt_energies", "qt_gradient_download",
     ]
 
 
@@ -241,6 +243,12 @@ class HamiltonianRepresentation:
     def dpsi(self) -> np.ndarray:
         out = np.zeros(self.n_psi, dtype=np.complex128)
         self.ctx.check(self.ctx.L.qt_dpsi_download(self.ctx.h, _ptr(out)))
+        return out
+
+    def gradient(self) -> np.ndarray:
+        """dE/dPhi^* of the last sweep (plans with QT_PLAN_GRADIENT)."""
+        out = np.zeros(self.n_psi, dtype=np.complex128)
+        self.ctx.check(self.ctx.L.qt_gradient_download(self.ctx.h, _ptr(out)))
         return out
 
     def dpsi_into(self, out: np.ndarray):

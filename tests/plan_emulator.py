@@ -21,8 +21,8 @@ _i32 = _P(dtype=np.int32, flags="C_CONTIGUOUS")
 _i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
-B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64 = range(9)
-ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT = range(7)
+B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64 = range(11)
+ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD = range(8)
 
 
 def lib():
@@ -75,8 +75,8 @@ class PlanView:
         self.h = h
         self.tree, self.sop = tree, sop
         self.tables = {}
-        widths = {0: 5, 1: 11, 2: 9, 3: 8, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6}
-        for what in list(range(14)) + [18]:
+        widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14}
+        for what in list(range(14)) + [18, 19]:
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -112,15 +112,18 @@ class PlanView:
                 np.zeros(max(self.mats_size, 16), np.complex128),
                 self.ops.copy(),
                 np.zeros(max(self.scratch_size, 16), np.complex128),
-                np.zeros(16, np.complex128), None, None]
+                np.zeros(16, np.complex128), None, None,
+                np.zeros(self.psi_arena, np.complex128), None]
         if self.prec == 1:
             # separate caller-facing complex128 arrays; conversions are copies here
             bufs[B_PSI] = np.zeros_like(psi0)
             bufs[B_PSI64] = psi0
             bufs[B_DPSI64] = np.zeros_like(psi0)
+            bufs[B_GRAD64] = np.zeros_like(psi0)
         else:
             bufs[B_PSI64] = bufs[B_PSI]
             bufs[B_DPSI64] = bufs[B_DPSI]
+            bufs[B_GRAD64] = bufs[B_GRAD]
         bufs[B_PARAM][0] = -1j * complex(phase)
         for off, d in self.tables[10]:
             bufs[B_MATS][off:off + d * d] = np.eye(d).ravel(order="F")
@@ -148,7 +151,7 @@ class PlanView:
                     S = np.einsum("bic,bjc->ij", A.conj(), B)
                     view(sb, so, a * a)[:] = S.ravel(order="F")
                 elif kind == ST_ACC:
-                    ob, oo, ap, rows, d, first, count, add = T[3][t]
+                    ob, oo, ap, aoff, rows, d, first, count, add = T[3][t]
                     acc = np.zeros((rows, d), np.complex128)
                     for s in range(first, first + count):
                         hb, ho, xb, xo = T[4][s]
@@ -158,7 +161,7 @@ class PlanView:
                         else:
                             H = view(hb, ho, d * d).reshape((d, d), order="F")
                             acc += X @ H.T
-                    alpha = bufs[B_PARAM][0] if ap else 1.0
+                    alpha = bufs[B_MATS][aoff] if ap == 2 else (bufs[B_PARAM][0] if ap else 1.0)
                     out = view(ob, oo, rows * d)
                     v = (alpha * acc).ravel(order="F")
                     out[:] = out + v if add else v
@@ -179,6 +182,14 @@ class PlanView:
                 elif kind == ST_CVT:
                     sb, so, db, do, n, _ = T[18][t]
                     view(db, do, n)[:] = view(sb, so, n)
+                elif kind == ST_GRAD:
+                    r = T[19][t]
+                    d = r[12]
+                    E = (view(r[6], r[7], 1)[0] / view(r[8], r[9], 1)[0]).real
+                    eo = view(r[0], r[1], d * d) if r[0] >= 0 else np.zeros(d * d, complex)
+                    view(r[4], r[5], d * d)[:] = eo - E * view(r[2], r[3], d * d)
+                    if r[13]:
+                        view(r[10], r[11], 1)[0] = 1.0 / view(r[8], r[9], 1)[0].real
                 elif kind == ST_PROJ:
                     r = T[8][t]
                     d = r[12]
@@ -195,6 +206,9 @@ class PlanView:
 
     def dpsi(self):
         return self.bufs[B_DPSI64].copy()
+
+    def gradient(self):
+        return self.bufs[B_GRAD64].copy()
 
     def energy_parts(self):
         m = self.bufs[B_MATS]

@@ -137,3 +137,26 @@ def test_plan_rejects_cross_tree_terms():
     s.push_back(MLO([(0, a), (mode_off[1], b)]), 1.0)
     with pytest.raises(ValueError, match="several trees"):
         PlanView(f, s, 1)
+
+
+@pytest.mark.parametrize("flavour,prec", [(0, 0), (1, 1)])
+def test_plan_gradient_finite_differences(flavour, prec):
+    # dE/dPhi^* of every node: 2 Re <G, delta> equals the central difference
+    # of E along random directions delta (all node tensors at once)
+    from tree_energy import energy, fd_directional
+    tree = balanced_tree(6, 4, 3)
+    rng = np.random.default_rng(31)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
+    psi = random_wavefunction(tree, 32)
+    pv = PlanView(tree, sop, flavour | 0x1000, prec=prec)
+    pv.run(psi.flat())
+    h00, s00 = pv.energy_parts()
+    assert abs(h00.real / s00.real - energy(tree, sop, psi.tensors)) < 1e-12
+    G = pv.gradient()
+    off = tree.offsets()
+    for k in range(4):
+        dirs = [rng.standard_normal(n.shape) + 1j * rng.standard_normal(n.shape) for n in tree.nodes]
+        flat_d = np.concatenate([d.ravel(order="F") for d in dirs])
+        analytic = 2.0 * np.vdot(G, flat_d).real
+        fd = fd_directional(tree, sop, psi, dirs)
+        assert abs(analytic - fd) <= 1e-7 * max(1.0, abs(fd)), (analytic, fd)
