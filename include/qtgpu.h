@@ -135,6 +135,13 @@ int qt_psi_upload(qt_ctx* ctx, const double* psi_host);
 int qt_psi_upload_device(qt_ctx* ctx, const void* psi_dev);
 int qt_psi_download(qt_ctx* ctx, double* psi_host);
 int64_t qt_psi_size(const qt_ctx* ctx); /* complex elements, packed */
+/* Checkpoint / resume in QuTree's TTre format ("TTre", int32 node count,
+ * then per node "TENS" + "TDIM" + int32 order + int32 dims + int32 16 +
+ * complex128 coefficients; TensorTree::write / read,
+ * include/TreeClasses/TensorTree_Implementation.h:78-132).  Loading checks
+ * every node shape against the uploaded tree (QT_ERR_SHAPE otherwise). */
+int qt_psi_save(qt_ctx* ctx, const char* path);
+int qt_psi_load(qt_ctx* ctx, const char* path);
 
 /* ---- sweep ---------------------------------------------------------------
  * One H.Psi sweep = Derivative(dPsi, hRep, t, Psi, H, tree, phase)
@@ -145,6 +152,29 @@ int64_t qt_psi_size(const qt_ctx* ctx); /* complex elements, packed */
  * the context stream. */
 int qt_derivative(qt_ctx* ctx, double phase_re, double phase_im);
 int qt_dpsi_download(qt_ctx* ctx, double* dpsi_host);
+
+/* The two halves of a sweep, for integrators that hold the matrices fixed
+ * over several derivative evaluations (constant mean fields):
+ * qt_build = HamiltonianRepresentation::build for the current Psi
+ * (include/TreeClasses/HamiltonianRepresentation.h:62-87);
+ * qt_layer_derivatives = LayerDerivative at every node with the matrices of
+ * the last qt_build / qt_derivative frozen and the current Psi
+ * (src/TreeClasses/HamiltonianRepresentation.cpp:53-72), into dPsi. */
+int qt_build(qt_ctx* ctx);
+int qt_layer_derivatives(qt_ctx* ctx, double phase_re, double phase_im);
+
+/* Fixed-step second-order constant-mean-field propagation of the device
+ * wavefunction (the scheme of CMFIntegrator::Integrate,
+ * src/Applications/CMFIntegrator.cpp:25-174, without its step-size control):
+ * per step, build at t, propagate the node tensors with frozen matrices to
+ * t+dt/2 (n_sub RK4 substeps), build at t+dt/2, propagate Psi(t) to t+dt
+ * (2*n_sub RK4 substeps) with those matrices.  phase = 1 real time,
+ * phase = -i imaginary time (d Psi/dt = -i*phase*H Psi).  No
+ * re-orthonormalisation: the projected equations keep the node tensors
+ * orthonormal to the integrator's accuracy.  Allocates three wavefunction-
+ * sized work vectors on first use.  Asynchronous. */
+int qt_cmf_propagate(qt_ctx* ctx, double dt, int n_steps, int n_sub, double phase_re,
+                     double phase_im);
 /* Energy gradient of the last sweep (plans prepared with QT_PLAN_GRADIENT),
  * packed layout like the wavefunction.  Synchronises. */
 int qt_gradient_download(qt_ctx* ctx, double* grad_host);

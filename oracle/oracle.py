@@ -75,6 +75,13 @@ def lib(fast: bool = False):
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
         ctypes.c_void_p]
     L.orc_set_zgemm.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.orc_cmf.restype = ctypes.c_int
+    L.orc_cmf.argtypes = [
+        ctypes.c_int, ctypes.c_int, _i32, _i32, _i32, _i32, _i32,
+        ctypes.c_int, _i32, _i32, _i64, ctypes.c_void_p,
+        ctypes.c_int, ctypes.c_void_p, _i32, _i32, _i32,
+        ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+        ctypes.c_double, ctypes.c_int, ctypes.c_int]
     _libs[fast] = L
     return L
 
@@ -203,6 +210,24 @@ def derivative(tree, sop, psi, eps=1e-10, phase=1.0, backend=LOOPS, fast=False,
         raise RuntimeError(f"oracle derivative failed: {rc}")
     return SweepResult(dpsi=dpsi, rho=rho, rhoinv=rhoinv, hmat=hmat, hcon=hcon,
                        h00=complex(energy[0], energy[1]), s00=complex(energy[2], energy[3]))
+
+
+def cmf(tree, sop, psi, dt, n_steps, n_sub=1, phase=1.0, eps=1e-10, backend=LOOPS, fast=False):
+    """Fixed-step constant-mean-field propagation (see qt_oracle.cpp orc_cmf);
+    returns the propagated flat wavefunction."""
+    order, dims, parent, child_idx, leaf_mode = tree.descriptor()
+    kind, odim, ooff, odata = sop.ops.descriptor()
+    coeff, ptr, modes, opids = sop.descriptor()
+    y = np.array(psi, dtype=np.complex128, copy=True)
+    odata = np.ascontiguousarray(odata)
+    coeff = np.ascontiguousarray(coeff)
+    rc = lib(fast).orc_cmf(backend, tree.n_nodes, order, dims, parent, child_idx, leaf_mode,
+                           len(kind), kind, odim, ooff, odata.ctypes.data, len(sop),
+                           coeff.ctypes.data, ptr, modes, opids, y.ctypes.data, eps,
+                           complex(phase).real, complex(phase).imag, dt, n_steps, n_sub)
+    if rc != 0:
+        raise RuntimeError(f"oracle cmf failed: {rc}")
+    return y
 
 
 def sparse_offsets(tree, sop):

@@ -424,7 +424,7 @@ struct Sweep {
   const Ops& ops;
   const Sop& s;
   Backend be;
-  const cd* psi;
+  const cd* psi;  // current wavefunction (the integrator re-points it)
   std::vector<std::vector<char>> act;          // [term][node]
   std::vector<std::vector<int64_t>> moff;      // sparse matrix offsets [term][node]
   std::vector<cd> hmat, hcon;                  // sparse matrix trees
@@ -713,6 +713,66 @@ int orc_derivative(int backend, int n_nodes, const int* order, const int* dims, 
     energy[1] = h[0].imag();
     energy[2] = S[0].real();
     energy[3] = S[0].imag();
+  }
+  return 0;
+}
+
+// Fixed-step second-order constant-mean-field propagation with RK4 substeps
+// (the scheme of CMFIntegrator::Integrate, src/Applications/CMFIntegrator.cpp:
+// 25-174, without step-size control or re-orthonormalisation): per step,
+// build at t; Psi_h = Psi(t) propagated to t+dt/2 with frozen matrices
+// (n_sub RK4 steps); build at Psi_h; Psi(t) propagated to t+dt (2*n_sub RK4
+// steps) with those matrices.  psi is updated in place.
+int orc_cmf(int backend, int n_nodes, const int* order, const int* dims, const int* parent,
+            const int* child_idx, const int* leaf_mode, int n_ops, const int* op_kind,
+            const int* op_dim, const int64_t* op_off, const double* op_data, int n_terms,
+            const double* coeff, const int* term_ptr, const int* term_mode, const int* term_op,
+            double* psi_io, double eps, double phase_re, double phase_im, double dt, int n_steps,
+            int n_sub) {
+  (void)n_ops;
+  Tree t = make_tree(n_nodes, order, dims, parent, child_idx, leaf_mode);
+  Ops ops{op_kind, op_dim, op_off, (const cd*)op_data};
+  Sop s{n_terms, (const cd*)coeff, term_ptr, term_mode, term_op};
+  const int64_t N = t.off[t.n];
+  cd* psi = (cd*)psi_io;
+  cd phase(phase_re, phase_im);
+  std::vector<cd> y0(N), y(N), in(N), k(N), acc(N);
+  Sweep sw(t, ops, s, (Backend)backend, psi, eps);
+  auto build = [&](const cd* at) {
+    sw.psi = at;
+    sw.density();
+    sw.invert();
+    sw.represent();
+    sw.meanfield();
+  };
+  auto deriv = [&](const cd* at, cd* out) {
+    sw.psi = at;
+    for (int n = 0; n < t.n; ++n) sw.layer_derivative(n, out + t.off[n], phase);
+  };
+  auto rk4 = [&](std::vector<cd>& Y, double h, int steps) {
+    for (int st = 0; st < steps; ++st) {
+      const double w[4] = {1.0, 2.0, 2.0, 1.0};
+      const double a[4] = {0.5 * h, 0.5 * h, h, 0.0};
+      in = Y;
+      for (int q = 0; q < 4; ++q) {
+        deriv(in.data(), k.data());
+        for (int64_t i = 0; i < N; ++i) acc[i] = (q == 0 ? cd(0) : acc[i]) + w[q] * k[i];
+        if (q < 3)
+          for (int64_t i = 0; i < N; ++i) in[i] = Y[i] + a[q] * k[i];
+      }
+      for (int64_t i = 0; i < N; ++i) Y[i] += (h / 6.0) * acc[i];
+    }
+  };
+  for (int step = 0; step < n_steps; ++step) {
+    y0.assign(psi, psi + N);
+    build(y0.data());
+    y = y0;
+    rk4(y, 0.5 * dt / n_sub, n_sub);
+    std::vector<cd> yh = y;
+    build(yh.data());
+    y = y0;
+    rk4(y, 0.5 * dt / n_sub, 2 * n_sub);
+    std::copy(y.begin(), y.end(), psi);
   }
   return 0;
 }

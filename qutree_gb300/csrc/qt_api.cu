@@ -27,6 +27,7 @@ struct qt_ctx {
   cudaStream_t stream = nullptr;
   std::string err;
   bool have_tree = false, have_sop = false, prepared = false, have_psi = false, swept = false;
+  bool built = false;  // matrices of the current plan computed (qt_build / qt_derivative)
   std::vector<qt::NodeGeo> nodes;
   qt::OpTable ops;
   qt::SopDesc sop;
@@ -38,6 +39,9 @@ struct qt_ctx {
   qt::DevTables tables;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  cudaGraphExec_t exec_build = nullptr;  // stages [0, apply_begin)
+  cudaGraphExec_t exec_apply = nullptr;  // [psi-in conversion] + stages [apply_begin, end)
+  double2* cmf_buf[3] = {nullptr, nullptr, nullptr};  // CMF work vectors, allocated on first use
   int64_t launches = 0;
   int prec = 0;
   std::vector<double> ops_df;  // double-float operator table staging (prec 1)
@@ -68,8 +72,16 @@ int cuda_fail(qt_ctx* c, cudaError_t e, const char* where) {
 void release_arena(qt_ctx* c) {
   if (c->exec) cudaGraphExecDestroy(c->exec);
   if (c->graph) cudaGraphDestroy(c->graph);
+  if (c->exec_build) cudaGraphExecDestroy(c->exec_build);
+  if (c->exec_apply) cudaGraphExecDestroy(c->exec_apply);
+  for (auto& b : c->cmf_buf) {
+    if (b) cudaFree(b);
+    b = nullptr;
+  }
   c->exec = nullptr;
   c->graph = nullptr;
+  c->exec_build = nullptr;
+  c->exec_apply = nullptr;
   // B_PSI64 / B_DPSI64 alias B_PSI / B_DPSI in complex128 plans: free once
   if (c->buf[qt::B_PSI64] == c->buf[qt::B_PSI]) c->buf[qt::B_PSI64] = nullptr;
   if (c->buf[qt::B_DPSI64] == c->buf[qt::B_DPSI]) c->buf[qt::B_DPSI64] = nullptr;
@@ -85,6 +97,7 @@ void release_arena(qt_ctx* c) {
   c->prepared = false;
   c->have_psi = false;
   c->swept = false;
+  c->built = false;
 }
 
 const double2* ptr_of(const qt_ctx* c, const Ref& r) {
@@ -466,6 +479,25 @@ int qt_prepare(qt_ctx* c, int flavour) {
   }
   QT_CUDA(c, cudaStreamEndCapture(c->stream, &c->graph));
   QT_CUDA(c, cudaGraphInstantiate(&c->exec, c->graph, 0));
+  // the same stages split into build / frozen-matrix derivative graphs (CMF)
+  for (int part = 0; part < 2; ++part) {
+    QT_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    const int64_t b0 = part == 0 ? 0 : P.apply_begin;
+    const int64_t b1 = part == 0 ? P.apply_begin : (int64_t)P.stages.size();
+    if (part == 1 && prec == 1) e = qt::launch_stage(P.stages[0], c->tables, c->eps, P.max_eig_d, prec, c->stream);
+    for (int64_t i = b0; i < b1 && e == cudaSuccess; ++i)
+      e = qt::launch_stage(P.stages[i], c->tables, c->eps, P.max_eig_d, prec, c->stream);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(part == 0 ? &c->exec_build : &c->exec_apply, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      release_arena(c);
+      return cuda_fail(c, e, "capture of the build / apply graphs");
+    }
+  }
   P.stats.arena_bytes = arena;
   P.stats.scratch_bytes = c->buf_elems[qt::B_SCR] * 16;
   c->prepared = true;
@@ -503,6 +535,71 @@ int qt_psi_download(qt_ctx* c, double* psi) {
   return QT_OK;
 }
 
+int qt_psi_save(qt_ctx* c, const char* path) {
+  if (!c || !path) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->have_psi) return fail(c, QT_ERR_STATE, "no wavefunction uploaded");
+  std::vector<double2> psi(c->plan.psi_packed);
+  QT_CUDA(c, cudaMemcpyAsync(psi.data(), c->buf[qt::B_PSI64], psi.size() * 16, cudaMemcpyDeviceToHost,
+                             c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(c, QT_ERR_ARG, std::string("qt_psi_save: cannot open ") + path);
+  const int32_t nn = (int32_t)c->plan.nodes.size();
+  bool ok = std::fwrite("TTre", 1, 4, f) == 4 && std::fwrite(&nn, 4, 1, f) == 1;
+  for (const auto& g : c->plan.nodes) {
+    const int32_t order = (int32_t)g.shape.size(), sz = 16;
+    ok = ok && std::fwrite("TENS", 1, 4, f) == 4 && std::fwrite("TDIM", 1, 4, f) == 4 &&
+         std::fwrite(&order, 4, 1, f) == 1;
+    for (int d : g.shape) {
+      const int32_t v = d;
+      ok = ok && std::fwrite(&v, 4, 1, f) == 1;
+    }
+    ok = ok && std::fwrite(&sz, 4, 1, f) == 1 &&
+         std::fwrite(psi.data() + g.off, 16, (size_t)g.N, f) == (size_t)g.N;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return fail(c, QT_ERR_ARG, std::string("qt_psi_save: write failed for ") + path);
+  return QT_OK;
+}
+
+int qt_psi_load(qt_ctx* c, const char* path) {
+  if (!c || !path) return fail(c, QT_ERR_ARG, "null argument");
+  if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_load before qt_prepare");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(c, QT_ERR_ARG, std::string("qt_psi_load: cannot open ") + path);
+  std::vector<double2> psi(c->plan.psi_packed);
+  char tag[4];
+  int32_t nn = 0;
+  std::string err;
+  if (std::fread(tag, 1, 4, f) != 4 || std::memcmp(tag, "TTre", 4) != 0) err = "not a TTre file";
+  if (err.empty() && (std::fread(&nn, 4, 1, f) != 1 || nn != (int32_t)c->plan.nodes.size()))
+    err = "node count differs from the tree";
+  for (size_t i = 0; err.empty() && i < c->plan.nodes.size(); ++i) {
+    const auto& g = c->plan.nodes[i];
+    int32_t order = 0, sz = 0;
+    if (std::fread(tag, 1, 4, f) != 4 || std::memcmp(tag, "TENS", 4) != 0) { err = "missing TENS"; break; }
+    if (std::fread(tag, 1, 4, f) != 4 || std::memcmp(tag, "TDIM", 4) != 0) { err = "missing TDIM"; break; }
+    if (std::fread(&order, 4, 1, f) != 1 || order != (int32_t)g.shape.size()) { err = "node order differs"; break; }
+    for (int k = 0; k < order; ++k) {
+      int32_t d = 0;
+      if (std::fread(&d, 4, 1, f) != 1 || d != g.shape[k]) { err = "node shape differs"; break; }
+    }
+    if (!err.empty()) break;
+    if (std::fread(&sz, 4, 1, f) != 1 || sz != 16) { err = "element size is not complex128"; break; }
+    if (std::fread(psi.data() + g.off, 16, (size_t)g.N, f) != (size_t)g.N) { err = "file truncated"; break; }
+  }
+  std::fclose(f);
+  if (!err.empty()) return fail(c, QT_ERR_SHAPE, std::string("qt_psi_load: ") + err + " (" + path + ")");
+  if (!finite_all((const double*)psi.data(), 2 * (int64_t)psi.size()))
+    return fail(c, QT_ERR_NUMERIC, "qt_psi_load: non-finite coefficient");
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI64], psi.data(), psi.size() * 16, cudaMemcpyHostToDevice,
+                             c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_psi = true;
+  c->swept = false;
+  return QT_OK;
+}
+
 int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_derivative needs qt_prepare and a wavefunction");
@@ -512,6 +609,100 @@ int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
   QT_CUDA(c, cudaGraphLaunch(c->exec, c->stream));
   c->launches += (int64_t)c->plan.stages.size();
   c->swept = true;
+  c->built = true;
+  return QT_OK;
+}
+
+int qt_build(qt_ctx* c) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_build needs qt_prepare and a wavefunction");
+  QT_CUDA(c, cudaGraphLaunch(c->exec_build, c->stream));
+  c->launches += c->plan.apply_begin;
+  c->built = true;
+  return QT_OK;
+}
+
+int qt_layer_derivatives(qt_ctx* c, double phase_re, double phase_im) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->prepared || !c->have_psi || !c->built)
+    return fail(c, QT_ERR_STATE, "qt_layer_derivatives needs a qt_build (or qt_derivative) first");
+  double2 alpha = make_double2(phase_im, -phase_re);
+  QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  QT_CUDA(c, cudaGraphLaunch(c->exec_apply, c->stream));
+  c->launches += (int64_t)c->plan.stages.size() - c->plan.apply_begin + (c->prec == 1 ? 1 : 0);
+  c->swept = true;
+  return QT_OK;
+}
+
+namespace {
+// RK4 with the matrices of the last build frozen, from Y over `steps` steps of
+// length h; uses B_PSI64 as the derivative input and ACC as workspace.
+int rk4_frozen(qt_ctx* c, double2* Y, double2* ACC, double h, int steps, double2 alpha) {
+  const int64_t n = c->plan.psi_packed;
+  double2* IN = c->buf[qt::B_PSI64];
+  const double2* K = c->buf[qt::B_DPSI64];
+  const double2 one = make_double2(1.0, 0.0);
+  for (int s = 0; s < steps; ++s) {
+    const double w[4] = {1.0, 2.0, 2.0, 1.0};
+    const double a[4] = {0.5 * h, 0.5 * h, h, 0.0};
+    QT_CUDA(c, cudaMemcpyAsync(IN, Y, n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    for (int k = 0; k < 4; ++k) {
+      QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+      QT_CUDA(c, cudaGraphLaunch(c->exec_apply, c->stream));
+      c->launches += (int64_t)c->plan.stages.size() - c->plan.apply_begin + (c->prec == 1 ? 1 : 0);
+      cudaError_t e = k == 0 ? cudaMemcpyAsync(ACC, K, n * 16, cudaMemcpyDeviceToDevice, c->stream)
+                             : qt::launch_axpy(ACC, ACC, make_double2(w[k], 0.0), K, n, c->stream);
+      if (e != cudaSuccess) return cuda_fail(c, e, "rk4 accumulate");
+      if (k < 3) {
+        e = qt::launch_axpy(IN, Y, make_double2(a[k], 0.0), K, n, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "rk4 stage");
+      }
+      c->launches += 2;
+    }
+    cudaError_t e = qt::launch_axpy(Y, Y, make_double2(h / 6.0, 0.0), ACC, n, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "rk4 update");
+    c->launches += 1;
+    (void)one;
+  }
+  return QT_OK;
+}
+}  // namespace
+
+int qt_cmf_propagate(qt_ctx* c, double dt, int n_steps, int n_sub, double phase_re, double phase_im) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_cmf_propagate needs qt_prepare and a wavefunction");
+  if (!(dt > 0) || !std::isfinite(dt) || n_steps < 0 || n_sub < 1)
+    return fail(c, QT_ERR_ARG, "qt_cmf_propagate: need dt > 0, n_steps >= 0, n_sub >= 1");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  const int64_t n = c->plan.psi_packed;
+  for (auto& b : c->cmf_buf)
+    if (!b) {
+      cudaError_t e = cudaMalloc((void**)&b, n * 16);
+      if (e != cudaSuccess) return fail(c, QT_ERR_ALLOC, "qt_cmf_propagate: work vectors");
+    }
+  double2* Y0 = c->cmf_buf[0];
+  double2* Y = c->cmf_buf[1];
+  double2* ACC = c->cmf_buf[2];
+  double2* PSI = c->buf[qt::B_PSI64];
+  const double2 alpha = make_double2(phase_im, -phase_re);  // -i * phase
+  for (int step = 0; step < n_steps; ++step) {
+    QT_CUDA(c, cudaMemcpyAsync(Y0, PSI, n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    // matrices at t, propagate to t + dt/2
+    QT_CUDA(c, cudaGraphLaunch(c->exec_build, c->stream));
+    QT_CUDA(c, cudaMemcpyAsync(Y, Y0, n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    int rc = rk4_frozen(c, Y, ACC, 0.5 * dt / n_sub, n_sub, alpha);
+    if (rc != QT_OK) return rc;
+    // matrices at t + dt/2, propagate Psi(t) over the full step
+    QT_CUDA(c, cudaMemcpyAsync(PSI, Y, n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    QT_CUDA(c, cudaGraphLaunch(c->exec_build, c->stream));
+    QT_CUDA(c, cudaMemcpyAsync(Y, Y0, n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    rc = rk4_frozen(c, Y, ACC, 0.5 * dt / n_sub, 2 * n_sub, alpha);
+    if (rc != QT_OK) return rc;
+    QT_CUDA(c, cudaMemcpyAsync(PSI, Y, n * 16, cudaMemcpyDeviceToDevice, c->stream));
+    c->launches += 2 * c->plan.apply_begin;
+  }
+  c->built = false;
+  c->swept = false;
   return QT_OK;
 }
 

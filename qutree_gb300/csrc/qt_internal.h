@@ -242,6 +242,10 @@ struct Plan {
   std::vector<SGrad> grad;
   bool want_grad = false;
   std::vector<Stage> stages;
+  // stages [0, apply_begin) build the matrices (HamiltonianRepresentation::
+  // build); stages [apply_begin, end) are LayerDerivative at every node with
+  // those matrices frozen.  With double-float arithmetic stage 0 converts Psi.
+  int64_t apply_begin = 0;
   // tiles (bound with task indices only)
   std::vector<int2> mp_tiles;
   std::vector<int4> hp_tiles;
@@ -301,6 +305,9 @@ int mp_outputs_per_tile();
 int64_t static_eig_capacity();
 cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n_mats, int d,
                                       double eps, cudaStream_t s);
+// out = x + a * y on n complex128 numbers (x may alias out)
+cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2* y, int64_t n,
+                        cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
 

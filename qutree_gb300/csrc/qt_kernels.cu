@@ -11,6 +11,7 @@
 //
 // Batched launches: each kernel reads a task table and a tile table; block b
 // processes tile b.  The planner (qt_plan.cpp) builds both once per tree.
+#include <algorithm>
 #include <cmath>
 #include <mutex>
 
@@ -715,6 +716,30 @@ inline int64_t eig_smem_bytes(int d) {
 }  // namespace
 
 int mp_outputs_per_tile() { return kMpTile; }
+
+namespace {
+__global__ void __launch_bounds__(kThreads) k_axpy(double2* out, const double2* x, double2 a,
+                                                   const double2* y, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+    double2 v = x[i];
+    cfma(v, a, y[i]);
+    out[i] = v;
+  }
+}
+}  // namespace
+
+cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2* y, int64_t n,
+                        cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t want = (n + kThreads - 1) / kThreads;
+  const int blocks = (int)std::min<int64_t>(want, (int64_t)sms * 8);
+  (void)cudaGetLastError();
+  k_axpy<<<blocks, kThreads, 0, s>>>(out, x, a, y, n);
+  return cudaGetLastError();
+}
 
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops) {
   int dev = 0, sms = 0;

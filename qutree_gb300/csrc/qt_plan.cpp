@@ -692,6 +692,7 @@ class Builder {
   }
 
   void stage_apply() {
+    P.apply_begin = (int64_t)P.stages.size();
     // group terms per node by their inside restriction; G_g = sum_l c_l H_l
     std::vector<Item> items;
     int64_t lin0 = (int64_t)P.lin.size();

@@ -101,6 +101,12 @@ def load(build_if_missing: bool = True):
                                    ctypes.c_int),
         "qt_tree_count": ([_vp], ctypes.c_int),
         "qt_gradient_download": ([_vp, _vp], ctypes.c_int),
+        "qt_psi_save": ([_vp, ctypes.c_char_p], ctypes.c_int),
+        "qt_build": ([_vp], ctypes.c_int),
+        "qt_layer_derivatives": ([_vp, ctypes.c_double, ctypes.c_double], ctypes.c_int),
+        "qt_cmf_propagate": ([_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                              ctypes.c_double], ctypes.c_int),
+        "qt_psi_load": ([_vp, ctypes.c_char_p], ctypes.c_int),
         "qt_energies": ([_vp, _vp, ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
@@ -122,7 +128,8 @@ def exported_symbols():
         "qt_hole_product", "qt_last_mode_product", "qt_dev_alloc", "qt_dev_free",
         "qt_memcpy_h2d", "qt_memcpy_d2h", "qt_launch_count", "qt_stage_count",
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
-        "qt_tree_count", "qt_energies", "qt_gradient_download",
+        "qt_tree_count", "qt_energies", "qt_gradient_download", "qt_psi_save", "qt_psi_load",
+        "qt_build", "qt_layer_derivatives", "qt_cmf_propagate",
     ]
 
 
@@ -233,12 +240,39 @@ class HamiltonianRepresentation:
         assert flat.size == self.n_psi
         self.ctx.check(self.ctx.L.qt_psi_upload(self.ctx.h, _ptr(flat)))
 
+    def save(self, path: str):
+        """Write the device wavefunction as a QuTree TTre file."""
+        self.ctx.check(self.ctx.L.qt_psi_save(self.ctx.h, path.encode()))
+
+    def load(self, path: str):
+        """Upload a QuTree TTre file (shapes checked against the tree)."""
+        self.ctx.check(self.ctx.L.qt_psi_load(self.ctx.h, path.encode()))
+
     def upload_device(self, ptr: int):
         self.ctx.check(self.ctx.L.qt_psi_upload_device(self.ctx.h, _vp(ptr)))
 
     # -- sweep -------------------------------------------------------------
     def derivative(self, phase: complex = 1.0):
         self.ctx.check(self.ctx.L.qt_derivative(self.ctx.h, complex(phase).real, complex(phase).imag))
+
+    def build(self):
+        """HamiltonianRepresentation::build for the current Psi."""
+        self.ctx.check(self.ctx.L.qt_build(self.ctx.h))
+
+    def layer_derivatives(self, phase: complex = 1.0):
+        """LayerDerivative at every node with the matrices of the last build frozen."""
+        self.ctx.check(self.ctx.L.qt_layer_derivatives(self.ctx.h, complex(phase).real,
+                                                       complex(phase).imag))
+
+    def cmf(self, dt: float, n_steps: int, n_sub: int = 1, phase: complex = 1.0):
+        """Fixed-step constant-mean-field propagation of the device wavefunction."""
+        self.ctx.check(self.ctx.L.qt_cmf_propagate(self.ctx.h, dt, n_steps, n_sub,
+                                                   complex(phase).real, complex(phase).imag))
+
+    def psi(self) -> np.ndarray:
+        out = np.zeros(self.n_psi, dtype=np.complex128)
+        self.ctx.check(self.ctx.L.qt_psi_download(self.ctx.h, _ptr(out)))
+        return out
 
     def dpsi(self) -> np.ndarray:
         out = np.zeros(self.n_psi, dtype=np.complex128)

@@ -1,0 +1,65 @@
+"""Constant-mean-field propagation on the GPU (qt_build, qt_layer_derivatives,
+qt_cmf_propagate) against the oracle's restatement of the same fixed-step
+scheme."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import rel_err
+from qutree_gb300 import qtgpu
+from qutree_gb300.model import config_problem
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64])
+def test_split_graphs_equal_the_sweep(flavour):
+    # build + frozen-matrix layer derivatives at the same Psi == one full sweep
+    tree, sop, psi = config_problem(4)
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour)
+    try:
+        d_full = qtgpu.Derivative(h, psi.flat())
+        h.upload(psi)
+        h.build()
+        h.layer_derivatives()
+        assert np.array_equal(h.dpsi(), d_full)
+    finally:
+        h.close()
+
+
+@pytest.mark.parametrize("flavour,tol", [(qtgpu.QT_PLAN_GROUPED, 1e-11),
+                                         (qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64, 1e-10)])
+def test_cmf_matches_oracle(flavour, tol):
+    tree, sop, psi = config_problem(0)
+    flat = psi.flat()
+    ref = O.cmf(tree, sop, flat, dt=1.0, n_steps=10, n_sub=2)
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour)
+    try:
+        h.upload(flat)
+        h.cmf(1.0, 10, n_sub=2)
+        got = h.psi()
+    finally:
+        h.close()
+    assert rel_err(got, ref) <= tol
+
+
+def test_cmf_conserves_energy_and_relaxes_in_imaginary_time():
+    tree, sop, psi = config_problem(0)
+    flat = psi.flat()
+    e0 = O.derivative(tree, sop, flat).energy
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64)
+    try:
+        h.upload(flat)
+        h.cmf(0.5, 40, n_sub=1)
+        e_real = O.derivative(tree, sop, h.psi()).energy
+        h.upload(flat)
+        h.cmf(20.0, 20, n_sub=2, phase=-1j)
+        y = h.psi()
+        t = tree.top
+        off = tree.offsets()
+        y[off[t.address]:] /= np.linalg.norm(y[off[t.address]:])
+        e_imag = O.derivative(tree, sop, y).energy
+    finally:
+        h.close()
+    assert abs(e_real - e0) <= 1e-4 * abs(e0)
+    assert e_imag < e0 - 0.1 * abs(e0)

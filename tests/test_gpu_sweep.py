@@ -189,3 +189,35 @@ def test_forest_of_uneven_trees(flavour):
             assert err <= tol and noise <= NOISE
     finally:
         hrep.close()
+
+
+def test_checkpoint_round_trip(tmp_path):
+    # qt_psi_save writes QuTree's TTre format; qt_psi_load reads it back
+    from qutree_gb300 import formats
+    tree, sop, psi = config_problem(0)
+    hrep = qtgpu.HamiltonianRepresentation(sop, tree)
+    try:
+        hrep.upload(psi)
+        p = str(tmp_path / "gpu.ttre")
+        hrep.save(p)
+        back = formats.read_tensor_tree(p, tree)
+        assert np.array_equal(back.flat(), psi.flat())
+        other = psi.copy()
+        other.tensors[-1] = other.tensors[-1] * (0.5 - 0.5j)
+        q = str(tmp_path / "host.ttre")
+        formats.write_tensor_tree(q, other)
+        hrep.load(q)
+        hrep.derivative()
+        hrep2 = qtgpu.HamiltonianRepresentation(sop, tree)
+        try:
+            ref = qtgpu.Derivative(hrep2, other.flat())
+        finally:
+            hrep2.close()
+        assert np.array_equal(hrep.dpsi(), ref)
+        tree4, _, psi4 = config_problem(4)
+        r = str(tmp_path / "wrong.ttre")
+        formats.write_tensor_tree(r, psi4)
+        with pytest.raises(qtgpu.QtError, match="QT_ERR_SHAPE"):
+            hrep.load(r)
+    finally:
+        hrep.close()

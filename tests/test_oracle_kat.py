@@ -224,3 +224,17 @@ def test_tensorblas_contractions_agree(blas):
                         B.reshape((before, dim, after), order="F")).ravel(order="F")
         assert np.abs(s1 - ref).max() < 1e-11
         assert np.abs(s2 - ref).max() < 1e-11
+
+
+def test_oracle_cmf_energy_converges_with_the_step():
+    # fixed-step constant-mean-field propagation conserves the energy better
+    # as dt shrinks (second-order scheme)
+    from qutree_gb300.model import config_problem
+    tree, sop, psi = config_problem(0)
+    flat = psi.flat()
+    e0 = O.derivative(tree, sop, flat).energy
+    d = []
+    for dt, n in ((2.0, 10), (1.0, 20)):
+        y = O.cmf(tree, sop, flat, dt, n, 1)
+        d.append(abs(O.derivative(tree, sop, y).energy - e0))
+    assert d[1] < d[0] / 3.5
