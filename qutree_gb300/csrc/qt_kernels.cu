@@ -77,26 +77,20 @@ __device__ __forceinline__ void mp_tile(const MPTask& t, int64_t start) {
 #pragma unroll
     for (int q = 0; q < kMpPerThread; ++q) acc[q] = P::zero();
     const int64_t hs = t.a_out, is = t.before;
-    int a = 0;
-    for (; a + 1 < t.a_in; a += 2) {
-      S h0[kMpPerThread], x0[kMpPerThread], h1[kMpPerThread], x1[kMpPerThread];
+    for (int a = 0; a < t.a_in; ++a) {
+      S h0[kMpPerThread], x0[kMpPerThread];
 #pragma unroll
       for (int q = 0; q < kMpPerThread; ++q) {
-        h0[q] = P::ld(hp[q] + a * hs);
-        x0[q] = P::ld(ip[q] + a * is);
-        h1[q] = P::ld(hp[q] + (a + 1) * hs);
-        x1[q] = P::ld(ip[q] + (a + 1) * is);
+        h0[q] = P::ld(hp[q]);
+        x0[q] = P::ld(ip[q]);
+        hp[q] += hs;
+        ip[q] += is;
       }
 #pragma unroll
       for (int q = 0; q < kMpPerThread; ++q) {
         P::mac(acc[q], h0[q], x0[q]);
-        P::mac(acc[q], h1[q], x1[q]);
-        P::norm(acc[q]);
+        if (a & 1) P::norm(acc[q]);
       }
-    }
-    for (; a < t.a_in; ++a) {
-#pragma unroll
-      for (int q = 0; q < kMpPerThread; ++q) P::mac(acc[q], P::ld(hp[q] + a * hs), P::ld(ip[q] + a * is));
     }
 #pragma unroll
     for (int q = 0; q < kMpPerThread; ++q) res[q] = P::fin(acc[q]);
@@ -129,10 +123,12 @@ __global__ void __launch_bounds__(kThreads) k_mp_single(MPTask t) {
 // ---------------------------------------------------------------------------
 template <class P>
 __device__ __forceinline__ void hp_tile(const HPTask& t, int mt0) {
-  // Output S is split into 2 x 2 micro-tiles, numbered column-major over the
-  // (ceil(aA/2) x ceil(aB/2)) micro-tile grid; thread x of the block owns
-  // micro-tile mt0 + x.  Threads past the last micro-tile form whole idle
-  // warps (they only help stage operands), so no lanes idle inside a warp.
+  // Output S is split into 2 x 2 micro-tiles {i, i + mi} x {j, j + mj}
+  // (mi = ceil(aA/2), mj = ceil(aB/2)), numbered column-major over the
+  // mi x mj grid; thread x of the block owns micro-tile mt0 + x.  Adjacent
+  // threads read adjacent rows of the staged operands (conflict-free shared
+  // loads).  Threads past the last micro-tile form whole idle warps (they
+  // only help stage operands), so no lanes idle inside a warp.
   typedef typename P::S S;
   typedef typename P::A A;
   extern __shared__ __align__(16) unsigned char hp_smem[];
@@ -148,9 +144,10 @@ __device__ __forceinline__ void hp_tile(const HPTask& t, int mt0) {
   const int mi = (aA + 1) / 2, mj = (aB + 1) / 2;
   const int mt = mt0 + threadIdx.x;
   const bool active = mt < mi * mj;
-  const int i = active ? 2 * (mt % mi) : 0;
-  const int j = active ? 2 * (mt / mi) : 0;
-  const int i1 = i + 1 < aA ? i + 1 : i, j1 = j + 1 < aB ? j + 1 : j;
+  const int i = active ? mt % mi : 0;
+  const int j = active ? mt / mi : 0;
+  const bool has_i1 = i + mi < aA, has_j1 = j + mj < aB;
+  const int i1 = has_i1 ? i + mi : i, j1 = has_j1 ? j + mj : j;
   A acc00 = P::zero(), acc01 = P::zero(), acc10 = P::zero(), acc11 = P::zero();
   const int nA = kHpK * aA, nAB = kHpK * (aA + aB);
   for (int64_t k0 = 0; k0 < K; k0 += kHpK) {
@@ -197,9 +194,9 @@ __device__ __forceinline__ void hp_tile(const HPTask& t, int mt0) {
   }
   if (!active) return;
   Sp[i + (int64_t)aA * j] = P::fin(acc00);
-  if (i + 1 < aA) Sp[i + 1 + (int64_t)aA * j] = P::fin(acc10);
-  if (j + 1 < aB) Sp[i + (int64_t)aA * (j + 1)] = P::fin(acc01);
-  if (i + 1 < aA && j + 1 < aB) Sp[i + 1 + (int64_t)aA * (j + 1)] = P::fin(acc11);
+  if (has_i1) Sp[i1 + (int64_t)aA * j] = P::fin(acc10);
+  if (has_j1) Sp[i + (int64_t)aA * j1] = P::fin(acc01);
+  if (has_i1 && has_j1) Sp[i1 + (int64_t)aA * j1] = P::fin(acc11);
 }
 
 template <class P>
