@@ -50,6 +50,13 @@ extern "C" {
 #define QT_PLAN_GROUPED 1   /* terms with identical restrictions share their
                                matrices and chains; Apply sums the mean fields
                                of terms with the same inside part first       */
+#define QT_PLAN_COMPRESSED 2 /* only the sums the sweep consumes: per node one
+                               block matrix of the terms inside its subtree,
+                               per boundary restriction one represent matrix
+                               and one summed mean field; represent chain
+                               outputs stay in device memory for Apply.  No
+                               per-term matrices (QT_MAT_HMAT / QT_MAT_HCON
+                               downloads return QT_ERR_STATE); no gradient   */
 
 /* Arithmetic of the sweep, OR-ed into the plan flavour of qt_prepare.
  * QT_PREC_F64: complex128 on the FP64 pipe.

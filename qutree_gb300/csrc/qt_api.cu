@@ -257,7 +257,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   const int prec = (flavour & QT_PREC_DF64) ? 1 : 0;
   const bool grad = (flavour & QT_PLAN_GRADIENT) != 0;
   flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT);
-  if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED)
+  if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED && flavour != QT_PLAN_COMPRESSED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
   QT_CUDA(c, cudaSetDevice(c->device));
   release_arena(c);
@@ -280,6 +280,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_DPSI64] = prec == 1 ? P.psi_arena : 0;
   c->buf_elems[qt::B_GRAD] = grad ? P.psi_arena : 0;
   c->buf_elems[qt::B_GRAD64] = (grad && prec == 1) ? P.psi_arena : 0;
+  c->buf_elems[qt::B_KEEP] = P.keep_size;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
@@ -467,7 +468,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   // capture the sweep
   QT_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-  for (const auto& st : P.stages) {
+  for (int64_t i = 0; i < P.main_end; ++i) {
+    const auto& st = P.stages[i];
     cudaError_t e = qt::launch_stage(st, c->tables, c->eps, P.max_eig_d, prec, c->stream);
     if (e != cudaSuccess) {
       cudaGraph_t g = nullptr;
@@ -483,8 +485,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
   for (int part = 0; part < 2; ++part) {
     QT_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    const int64_t b0 = part == 0 ? 0 : P.apply_begin;
-    const int64_t b1 = part == 0 ? P.apply_begin : (int64_t)P.stages.size();
+    const bool own = P.main_end < (int64_t)P.stages.size();  // separate frozen-matrix stages
+    const int64_t b0 = part == 0 ? 0 : (own ? P.main_end : P.apply_begin);
+    const int64_t b1 = part == 0 ? P.apply_begin : (own ? (int64_t)P.stages.size() : P.main_end);
     if (part == 1 && prec == 1) e = qt::launch_stage(P.stages[0], c->tables, c->eps, P.max_eig_d, prec, c->stream);
     for (int64_t i = b0; i < b1 && e == cudaSuccess; ++i)
       e = qt::launch_stage(P.stages[i], c->tables, c->eps, P.max_eig_d, prec, c->stream);
@@ -600,6 +603,16 @@ int qt_psi_load(qt_ctx* c, const char* path) {
   return QT_OK;
 }
 
+namespace {
+// launches of one frozen-matrix derivative graph
+int64_t apply_launches(const qt_ctx* c) {
+  const qt::Plan& P = c->plan;
+  const int64_t n = P.main_end < (int64_t)P.stages.size() ? (int64_t)P.stages.size() - P.main_end
+                                                          : P.main_end - P.apply_begin;
+  return n + (c->prec == 1 ? 1 : 0);
+}
+}  // namespace
+
 int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_derivative needs qt_prepare and a wavefunction");
@@ -607,7 +620,7 @@ int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
   double2 alpha = make_double2(phase_im, -phase_re);
   QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
   QT_CUDA(c, cudaGraphLaunch(c->exec, c->stream));
-  c->launches += (int64_t)c->plan.stages.size();
+  c->launches += c->plan.main_end;
   c->swept = true;
   c->built = true;
   return QT_OK;
@@ -629,7 +642,7 @@ int qt_layer_derivatives(qt_ctx* c, double phase_re, double phase_im) {
   double2 alpha = make_double2(phase_im, -phase_re);
   QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
   QT_CUDA(c, cudaGraphLaunch(c->exec_apply, c->stream));
-  c->launches += (int64_t)c->plan.stages.size() - c->plan.apply_begin + (c->prec == 1 ? 1 : 0);
+  c->launches += apply_launches(c);
   c->swept = true;
   return QT_OK;
 }
@@ -649,7 +662,7 @@ int rk4_frozen(qt_ctx* c, double2* Y, double2* ACC, double h, int steps, double2
     for (int k = 0; k < 4; ++k) {
       QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
       QT_CUDA(c, cudaGraphLaunch(c->exec_apply, c->stream));
-      c->launches += (int64_t)c->plan.stages.size() - c->plan.apply_begin + (c->prec == 1 ? 1 : 0);
+      c->launches += apply_launches(c);
       cudaError_t e = k == 0 ? cudaMemcpyAsync(ACC, K, n * 16, cudaMemcpyDeviceToDevice, c->stream)
                              : qt::launch_axpy(ACC, ACC, make_double2(w[k], 0.0), K, n, c->stream);
       if (e != cudaSuccess) return cuda_fail(c, e, "rk4 accumulate");
@@ -780,6 +793,8 @@ int qt_matrices_download(qt_ctx* c, int which, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   const Plan& P = c->plan;
+  if ((which == QT_MAT_HMAT || which == QT_MAT_HCON) && !P.per_term_mats)
+    return fail(c, QT_ERR_STATE, "the compressed plan keeps no per-term matrices");
   std::vector<double2> mats(P.mats_size);
   QT_CUDA(c, cudaMemcpyAsync(mats.data(), c->buf[qt::B_MATS], P.mats_size * 16, cudaMemcpyDeviceToHost, c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -826,7 +841,7 @@ int qt_plan_stats(const qt_ctx* c, double* out) {
   const auto& s = c->plan.stats;
   out[0] = s.ref_flops;
   out[1] = s.exec_flops;
-  out[2] = (double)c->plan.stages.size();
+  out[2] = (double)c->plan.main_end;
   out[3] = (double)s.arena_bytes;
   out[4] = (double)s.scratch_bytes;
   out[5] = (double)s.rep_chains;
@@ -917,10 +932,10 @@ int qt_memcpy_d2h(qt_ctx* c, void* dst, const void* src, int64_t bytes) {
 
 int64_t qt_launch_count(const qt_ctx* c) { return c ? c->launches : -1; }
 
-int qt_stage_count(const qt_ctx* c) { return (c && c->prepared) ? (int)c->plan.stages.size() : -1; }
+int qt_stage_count(const qt_ctx* c) { return (c && c->prepared) ? (int)c->plan.main_end : -1; }
 
 int qt_stage_info(const qt_ctx* c, int i, int* kind, int64_t* tiles, double* flops, double* bytes) {
-  if (!c || !c->prepared || i < 0 || i >= (int)c->plan.stages.size()) return QT_ERR_ARG;
+  if (!c || !c->prepared || i < 0 || i >= (int)c->plan.main_end) return QT_ERR_ARG;
   const auto& st = c->plan.stages[i];
   if (kind) *kind = st.kind;
   if (tiles) *tiles = st.kind == qt::ST_MP || st.kind == qt::ST_HP || st.kind == qt::ST_ACC ? st.n_tiles : st.n_tasks;
@@ -932,7 +947,7 @@ int qt_stage_info(const qt_ctx* c, int i, int* kind, int64_t* tiles, double* flo
 int qt_stage_launch(qt_ctx* c, int i) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_stage_launch needs a prepared context and a wavefunction");
-  if (i < 0 || i >= (int)c->plan.stages.size()) return fail(c, QT_ERR_ARG, "no such stage");
+  if (i < 0 || i >= (int)c->plan.main_end) return fail(c, QT_ERR_ARG, "no such stage");
   QT_CUDA(c, cudaSetDevice(c->device));
   cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->prec,
                                    c->stream);

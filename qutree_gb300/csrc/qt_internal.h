@@ -125,8 +125,10 @@ struct Stage {
 // stages move data across.
 // B_GRAD / B_GRAD64: energy gradient (arithmetic format / caller-facing
 // complex128; aliases with complex128 arithmetic), only when requested.
+// B_KEEP: node-sized tensors the compressed plan keeps from represent to
+// Apply (chain outputs and Phi x_last rho).
 enum Buf {
-  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64,
+  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP,
   B_NBUF
 };
 
@@ -181,8 +183,10 @@ struct Plan {
   // slot offsets (-2: the top's represent matrix, zero by definition)
   std::vector<std::vector<int>> term_nodes;
   std::vector<std::vector<int64_t>> term_hslot, term_cslot;
+  bool per_term_mats = true;  // false: the compressed plan keeps no per-term matrices
   int64_t mats_size = 0;
   int64_t scratch_size = 0;
+  int64_t keep_size = 0;
   int64_t ops_size = 0;
   // symbolic task lists (buffer-relative); bound to pointers by bind()
   struct SMP {
@@ -246,6 +250,9 @@ struct Plan {
   // build); stages [apply_begin, end) are LayerDerivative at every node with
   // those matrices frozen.  With double-float arithmetic stage 0 converts Psi.
   int64_t apply_begin = 0;
+  // stages [0, main_end) are the sweep.  Stages [main_end, end), when present,
+  // replace [apply_begin, main_end) in the frozen-matrix derivative graph.
+  int64_t main_end = 0;
   // tiles (bound with task indices only)
   std::vector<int2> mp_tiles;
   std::vector<int4> hp_tiles;

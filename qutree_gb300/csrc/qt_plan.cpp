@@ -77,7 +77,9 @@ class Builder {
  public:
   Builder(Plan& P, const std::vector<NodeGeo>& nodes, const OpTable& ops, const SopDesc& sop,
           int flavour, int prec, int64_t budget)
-      : P(P), nd(P.nodes), ops(ops), sop(sop), grouped(flavour == 1), budget(budget) {
+      : P(P), nd(P.nodes), ops(ops), sop(sop), grouped(flavour == 1), compressed(flavour == 2),
+        budget(budget) {
+    if (flavour < 0 || flavour > 2) throw std::runtime_error("unknown plan flavour");
     P.nodes = nodes;
     P.prec = prec;
   }
@@ -93,15 +95,33 @@ class Builder {
     }
     stage_density();
     stage_inverse();
-    stage_represent();
-    stage_meanfield();
-    stage_apply();
-    if (P.want_grad) stage_environment();
-    stage_final();
-    if (P.want_grad) stage_gradient();
+    if (compressed) {
+      if (P.want_grad) throw std::runtime_error("the energy gradient needs the grouped or reference plan");
+      comp_layout();
+      comp_represent();
+      comp_meanfield();
+      P.apply_begin = (int64_t)P.stages.size();
+      comp_apply();
+      stage_final();
+      P.main_end = (int64_t)P.stages.size();
+      const double sweep_flops = P.stats.exec_flops;
+      const PlanStats counts = P.stats;
+      comp_frozen_apply();
+      P.stats = counts;
+      P.stats.exec_flops = sweep_flops;
+    } else {
+      stage_represent();
+      stage_meanfield();
+      stage_apply();
+      if (P.want_grad) stage_environment();
+      stage_final();
+      if (P.want_grad) stage_gradient();
+      P.main_end = (int64_t)P.stages.size();
+    }
     P.mats_size = mats_cursor;
+    P.keep_size = keep_cursor;
     count_reference_flops();
-    P.stats.launches = (int64_t)P.stages.size();
+    P.stats.launches = P.main_end;
   }
 
  private:
@@ -109,7 +129,7 @@ class Builder {
   std::vector<NodeGeo>& nd;
   const OpTable& ops;
   const SopDesc& sop;
-  bool grouped;
+  bool grouped, compressed;
   int64_t budget;
   int n = 0, L = 0;
   std::vector<int> tops;  // roots of the forest, ascending
@@ -358,6 +378,17 @@ class Builder {
       ident[t] = alloc_mat(dt);
       P.identities.push_back({ident[t], dt});
       P.identities.push_back({P.rho_off[t], dt});
+    }
+    P.term_nodes = term_nodes;
+    if (compressed) {  // no per-term matrices
+      P.per_term_mats = false;
+      P.term_hslot.assign(L, {});
+      P.term_cslot.assign(L, {});
+      for (int l = 0; l < L; ++l) {
+        P.term_hslot[l].assign(term_nodes[l].size(), -1);
+        P.term_cslot[l].assign(term_nodes[l].size(), -1);
+      }
+      return;
     }
     // represent / mean-field slots
     node_hslot.assign(n, {});
@@ -949,6 +980,494 @@ class Builder {
       add_cvt(Ref{B_GRAD, 0}, Ref{B_GRAD64, 0}, P.psi_packed, 1);
       emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "gradient-out");
     }
+  }
+
+  // ---- compressed plan (QT_PLAN_COMPRESSED) ------------------------------
+  // At every node a the active terms split into internal terms (no factor
+  // outside a's subtree) and boundary terms.  Boundary terms with the same
+  // inside restriction u share
+  //   X(a,u) = (u's child represent matrices or leaf operators) Phi_a  [kept]
+  //   H(a,u) = hole_last(Phi_a, X(a,u))                               [represent]
+  //   C(a,u) = sum_l c_l MF_l(a)                          [their mean fields, summed]
+  // and the internal terms share
+  //   Y(a) = sum_l c_l body_l Phi_a  [kept],   Block(a) = hole_last(Phi_a, Y(a)).
+  // The mean field of an internal term is the density matrix rho_a (both obey
+  // the same top-down recursion from the identity at the top), so
+  //   Apply(a) = Y(a) x_last rho_a + sum_u X(a,u) x_last C(a,u),   Apply(top) = Y(top).
+  // Y(a) sums Block(c) on every child leg c and, for terms that span several
+  // children, chains of cover groups: terms sharing all child factors but one
+  // share one chain whose free factor is the summed sum_l c_l H_l on that leg.
+  // C(a,u) is built at the parent p: terms internal to p contribute their
+  // sibling represent matrices applied to Phi_p x_last rho_p (cover groups
+  // over the sibling legs); terms reaching outside p contribute their sibling
+  // matrices on Phi_p and C(p,w) on the parent index, w their restriction to p.
+  // Every matrix is still a sum over the reference's per-term objects
+  // (TreeFunctions::represent / contraction); only the order of the sums
+  // changes.  Per-term matrices are not materialised.
+  struct BKey {
+    std::vector<int> terms;  // boundary terms with this inside restriction
+    int64_t hslot = -1, cslot = -1;
+    Ref X;
+  };
+  struct Chain {
+    Ref in;
+    std::vector<COp> ops;
+    Ref H;  // factor on the last index applied when the chains are summed; buf -1: none
+  };
+  struct Job {
+    int node = -1;  // geometry of every tensor of the job
+    std::vector<Chain> chains;
+    Ref out;  // destination of the summed chains; buf -1: scratch
+    Ref S;    // buf >= 0: hole product of Phi_node with the sum over hp_mode into S
+    int hp_mode = 0;
+  };
+  struct Group {
+    int free_leg;
+    std::vector<int> members;
+  };
+  std::vector<std::vector<BKey>> bk;
+  std::vector<std::vector<int>> node_bk;  // aligned with node_terms: boundary key, -1 internal
+  std::vector<std::vector<int>> internal;
+  std::vector<int64_t> block_slot;
+  std::vector<Ref> Yref, rho_psi;
+  std::map<int, int64_t> ident_dim;
+  std::vector<Job> recompute;  // chains of Apply with the matrices frozen (CMF)
+  int64_t keep_cursor = 0;
+
+  Ref keep(int64_t nelem) {
+    Ref r{B_KEEP, keep_cursor};
+    keep_cursor += align_up(nelem);
+    return r;
+  }
+  int64_t identity_mat(int d) {
+    auto it = ident_dim.find(d);
+    if (it != ident_dim.end()) return it->second;
+    const int64_t o = alloc_mat(d);
+    P.identities.push_back({o, d});
+    ident_dim[d] = o;
+    return o;
+  }
+  // boundary key of term l at node a; -1: internal there, -2: inactive
+  int bk_index(int l, int a) const {
+    const int i = idx_of(l, a);
+    return i < 0 ? -2 : node_bk[a][i];
+  }
+  std::vector<int> fkey(int l, int a, bool in) const {
+    std::vector<int> k = key(l, a, in);
+    return std::vector<int>(k.begin() + 2, k.end());
+  }
+
+  void comp_layout() {
+    bk.assign(n, {});
+    node_bk.assign(n, {});
+    internal.assign(n, {});
+    block_slot.assign(n, -1);
+    Yref.assign(n, Ref{});
+    rho_psi.assign(n, Ref{});
+    for (int a = 0; a < n; ++a) {
+      std::map<std::vector<int>, int> of;
+      node_bk[a].assign(node_terms[a].size(), -1);
+      for (size_t i = 0; i < node_terms[a].size(); ++i) {
+        const int l = node_terms[a][i];
+        if (is_top(a) || fkey(l, a, false).empty()) {
+          internal[a].push_back(l);
+          continue;
+        }
+        auto r = of.insert({fkey(l, a, true), (int)bk[a].size()});
+        if (r.second) bk[a].push_back(BKey());
+        bk[a][r.first->second].terms.push_back(l);
+        node_bk[a][i] = r.first->second;
+      }
+      const int d = nd[a].dup();
+      for (auto& b : bk[a]) {
+        b.hslot = alloc_mat(d);
+        b.cslot = alloc_mat(d);
+        b.X = keep(nd[a].N);
+      }
+      if (!internal[a].empty()) {
+        if (is_top(a)) {
+          Yref[a] = hphi(a);
+        } else {
+          block_slot[a] = alloc_mat(d);
+          Yref[a] = keep(nd[a].N);
+        }
+      }
+    }
+  }
+
+  // Greedy cover of candidates by groups that agree on every leg but one.
+  // sig[t][k]: object of candidate t on leg k (-1: identity); free legs from `legs`.
+  std::vector<Group> cover(const std::vector<std::vector<int>>& sig, const std::vector<int>& legs) const {
+    std::vector<Group> out;
+    std::vector<char> done(sig.size(), 0);
+    size_t left = sig.size();
+    while (left > 0) {
+      int best_leg = -1;
+      size_t best_n = 0;
+      std::vector<int> best_key;
+      for (int f : legs) {
+        std::map<std::vector<int>, size_t> cnt;
+        for (size_t t = 0; t < sig.size(); ++t) {
+          if (done[t]) continue;
+          std::vector<int> k = sig[t];
+          k[f] = -3;
+          const size_t c = ++cnt[k];
+          if (c > best_n) {
+            best_n = c;
+            best_leg = f;
+            best_key = k;
+          }
+        }
+      }
+      Group g;
+      g.free_leg = best_leg;
+      for (size_t t = 0; t < sig.size(); ++t) {
+        if (done[t]) continue;
+        std::vector<int> k = sig[t];
+        k[best_leg] = -3;
+        if (k == best_key) {
+          g.members.push_back((int)t);
+          done[t] = 1;
+          --left;
+        }
+      }
+      out.push_back(g);
+    }
+    return out;
+  }
+
+  // mode products of a cover group at node a: the shared factors, and on the
+  // free leg sum_l c_l H_l (a single term: its matrix scaled by c_l)
+  std::vector<COp> group_ops(int a, const Group& G, const std::vector<std::vector<int>>& sig,
+                             const std::vector<int>& term_of) {
+    const NodeGeo& g = nd[a];
+    const std::vector<int>& s0 = sig[G.members[0]];
+    std::vector<COp> o;
+    double2 alpha = c2(1, 0);
+    for (size_t k = 0; k < g.children.size(); ++k) {
+      const int c = g.children[k];
+      if ((int)k != G.free_leg || G.members.size() == 1) {
+        if ((int)k == G.free_leg) alpha = sop.coeff[term_of[G.members[0]]];
+        if (s0[k] >= 0) o.push_back(COp{0, (int)k, mat(bk[c][s0[k]].hslot), c2(1, 0)});
+        continue;
+      }
+      const int d = g.shape[k];
+      Plan::SLin lt;
+      const int64_t m = alloc_mat(d);
+      lt.out = mat(m);
+      lt.d = d;
+      lt.first = (int)P.lin_terms.size();
+      for (int t : G.members) {
+        const int ob = sig[t][k];
+        P.lin_terms.push_back(
+            Plan::SLinTerm{sop.coeff[term_of[t]], mat(ob >= 0 ? bk[c][ob].hslot : identity_mat(d))});
+      }
+      lt.count = (int)G.members.size();
+      P.lin.push_back(lt);
+      o.push_back(COp{0, (int)k, mat(m), c2(1, 0)});
+    }
+    if (o.empty()) throw std::logic_error("compressed plan: a cover group without factors");
+    o[0].alpha = alpha;
+    return o;
+  }
+
+  // X(a,u) chain: the represent matrices of u on the children, or its leaf operators
+  std::vector<COp> comp_body(int l, int a) const {
+    const NodeGeo& g = nd[a];
+    if (g.bottom()) return body(l, a, c2(1, 0));
+    std::vector<COp> o;
+    for (size_t k = 0; k < g.children.size(); ++k) {
+      const int c = g.children[k];
+      const int b = bk_index(l, c);
+      if (b == -2) continue;
+      if (b < 0) throw std::logic_error("compressed plan: internal child factor in a boundary chain");
+      o.push_back(COp{0, (int)k, mat(bk[c][b].hslot), c2(1, 0)});
+    }
+    return o;
+  }
+
+  Job y_job(int a) {
+    Job J;
+    J.node = a;
+    J.out = Yref[a];
+    const NodeGeo& g = nd[a];
+    if (g.bottom()) {
+      for (int l : internal[a]) J.chains.push_back(Chain{psi(a), body(l, a, sop.coeff[l]), Ref{}});
+    } else {
+      for (size_t k = 0; k < g.children.size(); ++k) {
+        const int c = g.children[k];
+        if (block_slot[c] >= 0)
+          J.chains.push_back(Chain{psi(a), {COp{0, (int)k, mat(block_slot[c]), c2(1, 0)}}, Ref{}});
+      }
+      std::vector<std::vector<int>> sig;
+      std::vector<int> term_of;
+      for (int l : internal[a]) {
+        std::vector<int> s(g.children.size(), -1);
+        int nact = 0;
+        bool inside_one = false;
+        for (size_t k = 0; k < g.children.size(); ++k) {
+          const int b = bk_index(l, g.children[k]);
+          if (b == -2) continue;
+          ++nact;
+          inside_one = inside_one || b == -1;
+          s[k] = b;
+        }
+        if (nact < 2) continue;  // internal to one child: inside Block(child)
+        if (inside_one) throw std::logic_error("compressed plan: internal child factor in a cover group");
+        sig.push_back(s);
+        term_of.push_back(l);
+      }
+      std::vector<int> legs;
+      for (size_t k = 0; k < g.children.size(); ++k) legs.push_back((int)k);
+      for (auto& G : cover(sig, legs)) J.chains.push_back(Chain{psi(a), group_ops(a, G, sig, term_of), Ref{}});
+    }
+    if (!is_top(a)) {
+      J.S = mat(block_slot[a]);
+      J.hp_mode = g.last();
+    }
+    return J;
+  }
+
+  void comp_represent() {
+    int maxh = 0;
+    for (auto& g : nd) maxh = std::max(maxh, g.height);
+    for (int h = 0; h <= maxh; ++h) {
+      std::vector<Job> jobs;
+      const int64_t lin0 = (int64_t)P.lin.size();
+      for (int a = 0; a < n; ++a) {
+        if (nd[a].height != h) continue;
+        if (!is_top(a))
+          for (auto& b : bk[a]) {
+            Job J;
+            J.node = a;
+            J.out = b.X;
+            J.chains.push_back(Chain{psi(a), comp_body(b.terms[0], a), Ref{}});
+            J.S = mat(b.hslot);
+            J.hp_mode = nd[a].last();
+            jobs.push_back(J);
+          }
+        if (!internal[a].empty()) jobs.push_back(y_job(a));
+      }
+      emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "represent-sums");
+      for (auto& J : jobs) {
+        P.stats.rep_chains += (int64_t)J.chains.size();
+        Job R = J;
+        R.S = Ref{};
+        recompute.push_back(R);
+      }
+      run_jobs(jobs, "represent");
+    }
+  }
+
+  // C(a,u) for every boundary key u of a (built on the parent's tensor)
+  void c_jobs(int a, std::vector<Job>& jobs, std::vector<int>& need_rho) {
+    const int p = nd[a].parent;
+    const NodeGeo& gp = nd[p];
+    const int ia = nd[a].child_idx;
+    std::vector<int> legs;
+    for (size_t k = 0; k < gp.children.size(); ++k)
+      if ((int)k != ia) legs.push_back((int)k);
+    for (auto& b : bk[a]) {
+      Job J;
+      J.node = p;
+      J.S = mat(b.cslot);
+      J.hp_mode = ia;
+      std::vector<std::vector<int>> sig;
+      std::vector<int> term_of;
+      std::map<int, int> wterm;  // boundary key at p -> a term with it
+      for (int l : b.terms) {
+        const int bp = is_top(p) ? -1 : bk_index(l, p);
+        if (bp >= 0) {
+          wterm.insert({bp, l});
+          continue;
+        }
+        std::vector<int> s(gp.children.size(), -1);
+        for (size_t k = 0; k < gp.children.size(); ++k) {
+          if ((int)k == ia) continue;
+          const int bs = bk_index(l, gp.children[k]);
+          if (bs == -1) throw std::logic_error("compressed plan: internal sibling factor");
+          s[k] = bs >= 0 ? bs : -1;
+        }
+        sig.push_back(s);
+        term_of.push_back(l);
+      }
+      if (!sig.empty()) {
+        Ref in = psi(p);
+        if (!is_top(p)) {
+          if (rho_psi[p].buf < 0) {
+            rho_psi[p] = keep(gp.N);
+            need_rho.push_back(p);
+          }
+          in = rho_psi[p];
+        }
+        for (auto& G : cover(sig, legs)) J.chains.push_back(Chain{in, group_ops(p, G, sig, term_of), Ref{}});
+      }
+      for (auto& kv : wterm) {
+        const int l = kv.second;
+        Chain ch{psi(p), {}, mat(bk[p][kv.first].cslot)};
+        for (size_t k = 0; k < gp.children.size(); ++k) {
+          if ((int)k == ia) continue;
+          const int bs = bk_index(l, gp.children[k]);
+          if (bs >= 0) ch.ops.push_back(COp{0, (int)k, mat(bk[gp.children[k]][bs].hslot), c2(1, 0)});
+        }
+        J.chains.push_back(ch);
+      }
+      if (J.chains.size() == 1 && J.chains[0].H.buf >= 0) {  // one chain: its last factor is a mode product
+        J.chains[0].ops.push_back(COp{0, gp.last(), J.chains[0].H, c2(1, 0)});
+        J.chains[0].H = Ref{};
+      }
+      jobs.push_back(J);
+    }
+  }
+
+  void comp_meanfield() {
+    int maxdepth = 0;
+    for (auto& g : nd) maxdepth = std::max(maxdepth, g.depth);
+    for (int d = 1; d <= maxdepth; ++d) {
+      std::vector<Job> jobs;
+      std::vector<int> need_rho;
+      const int64_t lin0 = (int64_t)P.lin.size();
+      for (int a = 0; a < n; ++a)
+        if (nd[a].depth == d) c_jobs(a, jobs, need_rho);
+      std::vector<Job> rj;
+      for (int p : need_rho) {
+        Job J;
+        J.node = p;
+        J.out = rho_psi[p];
+        J.chains.push_back(Chain{psi(p), {COp{0, nd[p].last(), mat(P.rho_off[p]), c2(1, 0)}}, Ref{}});
+        rj.push_back(J);
+      }
+      run_jobs(rj, "meanfield-rho");
+      emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "meanfield-sums");
+      for (auto& J : jobs) P.stats.mf_chains += (int64_t)J.chains.size();
+      run_jobs(jobs, "meanfield");
+    }
+  }
+
+  void comp_apply() {
+    std::vector<Job> jobs;
+    std::vector<char> started(n, 0);
+    for (int a = 0; a < n; ++a) {
+      if (is_top(a)) {
+        started[a] = internal[a].empty() ? 0 : 1;  // Y(top) is H Phi_top
+        continue;
+      }
+      if (internal[a].empty() && bk[a].empty()) continue;
+      Job J;
+      J.node = a;
+      J.out = hphi(a);
+      if (!internal[a].empty()) J.chains.push_back(Chain{Yref[a], {}, mat(P.rho_off[a])});
+      for (auto& b : bk[a]) J.chains.push_back(Chain{b.X, {}, mat(b.cslot)});
+      P.stats.app_chains += (int64_t)J.chains.size();
+      jobs.push_back(J);
+      started[a] = 1;
+    }
+    run_jobs(jobs, "apply");
+    int64_t t0 = (int64_t)P.acc.size(), tile0 = (int64_t)P.acc_tiles.size();
+    for (int a = 0; a < n; ++a)
+      if (!started[a]) add_acc(hphi(a), false, c2(1.0, 0.0), a, {}, false);
+    emit_stage(ST_ACC, t0, (int64_t)P.acc.size(), tile0, (int64_t)P.acc_tiles.size(), "apply-zero");
+  }
+
+  static bool single_plain(const Job& J) { return J.chains.size() == 1 && J.chains[0].H.buf < 0; }
+  static bool needs_sum(const Job& J) {
+    return !single_plain(J) || (J.chains[0].ops.empty() && J.out.buf >= 0);
+  }
+
+  // Run independent jobs: per scratch chunk one stage per mode-product
+  // position, one accumulation stage for the sums, one hole-product stage.
+  void run_jobs(std::vector<Job>& jobs, const char* name) {
+    size_t i = 0;
+    while (i < jobs.size()) {
+      int64_t cursor = 0;
+      size_t j = i;
+      std::vector<std::vector<std::pair<int64_t, int64_t>>> cb;
+      std::vector<int64_t> tmp;
+      while (j < jobs.size()) {
+        const Job& J = jobs[j];
+        const int64_t Na = align_up(nd[J.node].N);
+        int64_t need = 0;
+        std::vector<std::pair<int64_t, int64_t>> b;
+        for (auto& ch : J.chains) {
+          const int nb = (int)std::min<size_t>(2, ch.ops.size());
+          b.push_back({nb > 0 ? cursor + need : -1, nb > 1 ? cursor + need + Na : -1});
+          need += nb * Na;
+        }
+        int64_t t = -1;
+        if (needs_sum(J) && J.out.buf < 0) {
+          t = cursor + need;
+          need += Na;
+        }
+        if (j > i && cursor + need > budget) break;
+        cursor += need;
+        cb.push_back(b);
+        tmp.push_back(t);
+        ++j;
+      }
+      P.scratch_size = std::max(P.scratch_size, cursor);
+      auto result = [&](size_t k, size_t c) -> Ref {
+        const Job& J = jobs[k];
+        const Chain& ch = J.chains[c];
+        const size_t no = ch.ops.size();
+        if (no == 0) return ch.in;
+        if (single_plain(J) && J.out.buf >= 0) return J.out;
+        const auto& b = cb[k - i][c];
+        return Ref{B_SCR, (no - 1) % 2 == 0 ? b.first : b.second};
+      };
+      auto final_ref = [&](size_t k) -> Ref {
+        const Job& J = jobs[k];
+        if (!needs_sum(J)) return result(k, 0);
+        return J.out.buf >= 0 ? J.out : Ref{B_SCR, tmp[k - i]};
+      };
+      size_t maxops = 0;
+      for (size_t k = i; k < j; ++k)
+        for (auto& ch : jobs[k].chains) maxops = std::max(maxops, ch.ops.size());
+      for (size_t pos = 0; pos < maxops; ++pos) {
+        const int64_t t0 = (int64_t)P.mp.size(), tile0 = (int64_t)P.mp_tiles.size();
+        for (size_t k = i; k < j; ++k) {
+          const Job& J = jobs[k];
+          for (size_t c = 0; c < J.chains.size(); ++c) {
+            const Chain& ch = J.chains[c];
+            if (pos >= ch.ops.size()) continue;
+            const auto& b = cb[k - i][c];
+            const Ref in = pos == 0 ? ch.in : Ref{B_SCR, (pos - 1) % 2 == 0 ? b.first : b.second};
+            const Ref out = pos + 1 == ch.ops.size() ? result(k, c) : Ref{B_SCR, pos % 2 == 0 ? b.first : b.second};
+            const COp& op = ch.ops[pos];
+            add_mp(in, out, op.mat, op.alpha, J.node, op.mode, op.kind == 1);
+          }
+        }
+        emit_stage(ST_MP, t0, (int64_t)P.mp.size(), tile0, (int64_t)P.mp_tiles.size(), name);
+      }
+      {
+        const int64_t t0 = (int64_t)P.acc.size(), tile0 = (int64_t)P.acc_tiles.size();
+        for (size_t k = i; k < j; ++k) {
+          const Job& J = jobs[k];
+          if (!needs_sum(J)) continue;
+          std::vector<Plan::SAccTerm> terms;
+          for (size_t c = 0; c < J.chains.size(); ++c) terms.push_back(Plan::SAccTerm{J.chains[c].H, result(k, c)});
+          add_acc(final_ref(k), false, c2(1.0, 0.0), J.node, terms, false);
+        }
+        emit_stage(ST_ACC, t0, (int64_t)P.acc.size(), tile0, (int64_t)P.acc_tiles.size(), name);
+      }
+      {
+        const int64_t t0 = (int64_t)P.hp.size(), tile0 = (int64_t)P.hp_tiles.size();
+        for (size_t k = i; k < j; ++k) {
+          const Job& J = jobs[k];
+          if (J.S.buf < 0) continue;
+          add_hp(psi(J.node), final_ref(k), J.S, J.node, J.hp_mode);
+        }
+        emit_stage(ST_HP, t0, (int64_t)P.hp.size(), tile0, (int64_t)P.hp_tiles.size(), name);
+      }
+      i = j;
+    }
+  }
+
+  // Apply and LayerDerivative with every matrix frozen (constant-mean-field
+  // steps): the kept chains are recomputed from the current Phi.
+  void comp_frozen_apply() {
+    run_jobs(recompute, "apply-chains");
+    comp_apply();
+    stage_final();
   }
 
   // Flops of the reference call sequence (independent of this plan):

@@ -164,7 +164,7 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       break;
     case 9:
       v = {P.psi_arena, P.mats_size, P.scratch_size, P.ops_size, P.energy_off[0], P.stop_off[0], P.prec,
-           (int64_t)P.tops.size()};
+           P.keep_size, P.main_end, (int64_t)P.tops.size()};
       for (size_t k = 0; k < P.tops.size(); ++k) {
         v.push_back(P.tops[k]);
         v.push_back(P.energy_off[k]);
@@ -225,7 +225,7 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       }
       break;
     case 17:
-      dv = {P.stats.ref_flops, P.stats.exec_flops, (double)P.stages.size(),
+      dv = {P.stats.ref_flops, P.stats.exec_flops, (double)P.main_end,
             (double)P.stats.rep_chains, (double)P.stats.mf_chains, (double)P.stats.app_chains};
       break;
     default:

@@ -25,6 +25,7 @@ from .model import SOP, Tree, TensorTree
 QT_OK = 0
 QT_PLAN_REFERENCE = 0
 QT_PLAN_GROUPED = 1
+QT_PLAN_COMPRESSED = 2
 QT_PREC_F64 = 0x000
 QT_PREC_DF64 = 0x100
 QT_PLAN_GRADIENT = 0x1000

@@ -21,7 +21,7 @@ _i32 = _P(dtype=np.int32, flags="C_CONTIGUOUS")
 _i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
-B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64 = range(11)
+B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP = range(12)
 ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD = range(8)
 
 
@@ -99,12 +99,15 @@ class PlanView:
         self.psi_arena, self.mats_size, self.scratch_size, self.ops_size = map(int, s[:4])
         self.energy_off, self.stop_off = int(s[4]), int(s[5])
         self.prec = int(s[6])
+        self.keep_size, self.main_end = int(s[7]), int(s[8])
         st = self.tables[17]
         self.stats = dict(ref_flops=st[0], exec_flops=st[1], launches=int(st[2]),
                           rep_chains=int(st[3]), mf_chains=int(st[4]), app_chains=int(st[5]))
 
     # -- interpreter -------------------------------------------------------
-    def run(self, psi_flat, phase=1.0, eps=1e-10):
+    def run(self, psi_flat, phase=1.0, eps=1e-10, frozen_after=False):
+        """Run the sweep (stages [0, main_end)).  ``frozen_after``: then run
+        the frozen-matrix derivative stages on the same Psi as well."""
         psi0 = np.asarray(psi_flat, np.complex128).copy()
         bufs = [psi0,
                 np.zeros(self.psi_arena, np.complex128),
@@ -113,7 +116,8 @@ class PlanView:
                 self.ops.copy(),
                 np.zeros(max(self.scratch_size, 16), np.complex128),
                 np.zeros(16, np.complex128), None, None,
-                np.zeros(self.psi_arena, np.complex128), None]
+                np.zeros(self.psi_arena, np.complex128), None,
+                np.zeros(max(self.keep_size, 16), np.complex128)]
         if self.prec == 1:
             # separate caller-facing complex128 arrays; conversions are copies here
             bufs[B_PSI] = np.zeros_like(psi0)
@@ -132,7 +136,10 @@ class PlanView:
             return bufs[buf][off:off + n]
 
         T = self.tables
-        for kind, t0, nt, _, _ in T[0]:
+        stages = list(T[0][:self.main_end])
+        if frozen_after:
+            stages += list(T[0][self.main_end:]) if len(T[0]) > self.main_end else []
+        for kind, t0, nt, _, _ in stages:
             for t in range(t0, t0 + nt):
                 if kind == ST_MP:
                     ib, io, ob, oo, hb, ho, bef, ain, aout, aft, diag = T[1][t]

@@ -12,7 +12,8 @@ from qutree_gb300.model import config_problem
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64])
+@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64,
+                                     qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64])
 def test_split_graphs_equal_the_sweep(flavour):
     # build + frozen-matrix layer derivatives at the same Psi == one full sweep
     tree, sop, psi = config_problem(4)
@@ -28,7 +29,9 @@ def test_split_graphs_equal_the_sweep(flavour):
 
 
 @pytest.mark.parametrize("flavour,tol", [(qtgpu.QT_PLAN_GROUPED, 1e-11),
-                                         (qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64, 1e-10)])
+                                         (qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64, 1e-10),
+                                         (qtgpu.QT_PLAN_COMPRESSED, 1e-11),
+                                         (qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64, 1e-10)])
 def test_cmf_matches_oracle(flavour, tol):
     tree, sop, psi = config_problem(0)
     flat = psi.flat()

@@ -44,8 +44,12 @@ def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
         assert abs(e - r.energy) <= TOL * max(1.0, abs(r.energy))
         rho = hrep.matrices(qtgpu.QT_MAT_RHO)
         assert rel_err(rho, r.rho) <= TOL
-        assert rel_err(hrep.matrices(qtgpu.QT_MAT_HMAT), r.hmat) <= TOL
-        assert rel_err(hrep.matrices(qtgpu.QT_MAT_HCON), r.hcon) <= TOL
+        if flavour & 0xFF == qtgpu.QT_PLAN_COMPRESSED:  # no per-term matrices
+            with pytest.raises(qtgpu.QtError, match="QT_ERR_STATE"):
+                hrep.matrices(qtgpu.QT_MAT_HMAT)
+        else:
+            assert rel_err(hrep.matrices(qtgpu.QT_MAT_HMAT), r.hmat) <= TOL
+            assert rel_err(hrep.matrices(qtgpu.QT_MAT_HCON), r.hcon) <= TOL
         err, noise = deriv_errors(tree, dpsi, r.dpsi, r.rho)
         assert err <= TOL
         assert noise <= NOISE
@@ -62,8 +66,9 @@ def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
         hrep.close()
 
 
-FLAVOURS = [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED,
-            qtgpu.QT_PLAN_REFERENCE | qtgpu.QT_PREC_DF64, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64]
+FLAVOURS = [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_COMPRESSED,
+            qtgpu.QT_PLAN_REFERENCE | qtgpu.QT_PREC_DF64, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64,
+            qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64]
 
 
 @pytest.mark.parametrize("flavour", FLAVOURS)
@@ -167,7 +172,8 @@ def test_errors_are_reported_not_fatal():
         hrep.close()
 
 
-@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64])
+@pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64,
+                                     qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64])
 def test_forest_of_uneven_trees(flavour):
     # 24 trees of 8..48 modes, p in {8,16,32}, random bonds 4..24, one plan and
     # one graph; every tree's slice and energy equal its own oracle sweep

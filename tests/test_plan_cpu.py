@@ -20,23 +20,24 @@ def _check(tree, sop, psi, flavour, budget=1 << 28, tol=1e-12, prec=0):
     pv.run(flat)
     h00, s00 = pv.energy_parts()
     assert abs(h00.real / s00.real - r.energy) < tol * max(1, abs(r.energy))
-    assert rel_err(pv.sparse(0), r.hmat) < tol
-    assert rel_err(pv.sparse(1), r.hcon) < tol
+    if flavour != 2:  # the compressed plan keeps no per-term matrices
+        assert rel_err(pv.sparse(0), r.hmat) < tol
+        assert rel_err(pv.sparse(1), r.hcon) < tol
     assert rel_err(rho_weighted(tree, pv.dpsi(), r.rho), rho_weighted(tree, r.dpsi, r.rho)) < tol
     return pv
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("flavour", [0, 1])
+@pytest.mark.parametrize("flavour", [0, 1, 2])
 def test_plan_cfg0(flavour, prec):
     tree, sop, psi = config_problem(0)
     pv = _check(tree, sop, psi, flavour, prec=prec)
-    if flavour == 1:
+    if flavour >= 1:
         assert pv.stats["exec_flops"] < pv.stats["ref_flops"]
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("flavour", [0, 1])
+@pytest.mark.parametrize("flavour", [0, 1, 2])
 def test_plan_small_budget_chunks(flavour, prec):
     # a tiny scratch budget forces every level into many chunks
     tree, sop, psi = config_problem(0)
@@ -44,7 +45,7 @@ def test_plan_small_budget_chunks(flavour, prec):
 
 
 @pytest.mark.parametrize("leaves,p,b,seed", [(5, 4, 3, 1), (7, 5, 4, 2), (12, 3, 2, 3), (9, 6, 5, 4)])
-@pytest.mark.parametrize("flavour", [0, 1])
+@pytest.mark.parametrize("flavour", [0, 1, 2])
 def test_plan_random_trees(leaves, p, b, seed, flavour):
     tree = balanced_tree(leaves, p, b)
     rng = np.random.default_rng(seed)
@@ -71,11 +72,11 @@ def test_plan_multi_factor_terms():
     for k in range(6):
         sop.push_back(MLO([(k, kin)]), 1.0)
     psi = random_wavefunction(tree, 9)
-    for fl in (0, 1):
+    for fl in (0, 1, 2):
         _check(tree, sop, psi, fl)
 
 
-@pytest.mark.parametrize("flavour", [0, 1])
+@pytest.mark.parametrize("flavour", [0, 1, 2])
 def test_plan_nodes_without_terms(flavour):
     # an SOP acting on a few leaves only: the other nodes get H Phi = 0
     tree = balanced_tree(8, 4, 3)
@@ -99,6 +100,9 @@ def test_plan_reference_flops_cfg1():
     pv1 = PlanView(tree, sop, 1)
     assert pv1.stats["exec_flops"] < 0.6 * pv.stats["exec_flops"]
     assert pv1.stats["ref_flops"] == pv.stats["ref_flops"]
+    pv2 = PlanView(tree, sop, 2)  # compressed: ~0.13 TFLOP per sweep
+    assert pv2.stats["exec_flops"] < 0.3 * pv1.stats["exec_flops"]
+    assert pv2.stats["ref_flops"] == pv.stats["ref_flops"]
 
 
 def test_plan_rejects_bad_input():
@@ -112,7 +116,7 @@ def test_plan_rejects_bad_input():
         PlanView(tree, s, 0)
 
 
-@pytest.mark.parametrize("flavour,prec", [(0, 1), (1, 0)])
+@pytest.mark.parametrize("flavour,prec", [(0, 1), (1, 0), (2, 1)])
 def test_plan_forest(flavour, prec):
     # many uneven trees in one plan: each tree's slice equals its own sweep
     trees, sops, psis = batched_problem(5)
@@ -160,3 +164,40 @@ def test_plan_gradient_finite_differences(flavour, prec):
         analytic = 2.0 * np.vdot(G, flat_d).real
         fd = fd_directional(tree, sop, psi, dirs)
         assert abs(analytic - fd) <= 1e-7 * max(1.0, abs(fd)), (analytic, fd)
+
+
+def test_plan_compressed_frozen_stages():
+    # the frozen-matrix derivative stages (constant-mean-field steps) recompute
+    # the kept chains from Psi; on the Psi the matrices were built from they
+    # reproduce the sweep's derivative
+    tree, sop, psi = config_problem(0)
+    pv = PlanView(tree, sop, 2)
+    pv.run(psi.flat())
+    d_sweep = pv.dpsi()
+    pv.run(psi.flat(), frozen_after=True)
+    assert len(pv.tables[0]) > pv.main_end
+    assert np.abs(pv.dpsi() - d_sweep).max() <= 1e-14 * np.abs(d_sweep).max()
+
+
+def test_plan_compressed_general_arity():
+    # nodes with three children: cover groups over several free legs
+    from qutree_gb300.model import Tree, _Build
+    groups = [_Build([3, 3, 3, 3], [_Build([4, 3], leaf=True) for _ in range(3)]) for _ in range(3)]
+    tree = Tree(_Build([3, 3, 3, 1], groups))
+    rng = np.random.default_rng(17)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
+    ops = sop.ops
+    b = HOBasis(4, omega=1.0)
+    x = ops.add("x3", 1, b.x.astype(complex))
+    for (i, j, k) in [(0, 4, 8), (1, 2, 7), (3, 5, 6), (0, 1, 2)]:
+        sop.push_back(MLO([(i, x), (j, x), (k, x)]), 0.05 * (i + 1))
+    psi = random_wavefunction(tree, 17)
+    for fl in (1, 2):
+        _check(tree, sop, psi, fl)
+        _check(tree, sop, psi, fl, prec=1)
+
+
+def test_plan_compressed_rejects_gradient():
+    tree, sop = config_tree_sop(0)
+    with pytest.raises(ValueError, match="gradient"):
+        PlanView(tree, sop, 2 | 0x1000)
