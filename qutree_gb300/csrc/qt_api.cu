@@ -281,6 +281,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_GRAD] = grad ? P.psi_arena : 0;
   c->buf_elems[qt::B_GRAD64] = (grad && prec == 1) ? P.psi_arena : 0;
   c->buf_elems[qt::B_KEEP] = P.keep_size;
+  c->buf_elems[qt::B_HPW] = P.hpw_size;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
@@ -344,6 +345,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.a = s.a;
     t.after = s.after;
     t.aB = 0;
+    t.splits = s.splits;
+    t.kchunk = s.kchunk;
+    t.ws = s.ws;
     hp.push_back(t);
   }
   std::vector<qt::AccTask> acc;
@@ -456,6 +460,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.proj = (qt::ProjTask*)(base + offs[7]);
   c->tables.mp_tiles = (int2*)(base + offs[8]);
   c->tables.hp_tiles = (int4*)(base + offs[9]);
+  c->tables.hp_ws = c->buf[qt::B_HPW];
   c->tables.acc_tiles = (int4*)(base + offs[10]);
   c->tables.cvt = (qt::CvtTask*)(base + offs[11]);
   c->tables.cvt_tiles = (int2*)(base + offs[12]);
@@ -604,11 +609,17 @@ int qt_psi_load(qt_ctx* c, const char* path) {
 }
 
 namespace {
+// kernel launches of stages [b0, b1) (a split hole-product stage launches two)
+int64_t kernels_in(const qt::Plan& P, int64_t b0, int64_t b1) {
+  int64_t n = 0;
+  for (int64_t i = b0; i < b1; ++i) n += 1 + (P.stages[i].aux ? 1 : 0);
+  return n;
+}
 // launches of one frozen-matrix derivative graph
 int64_t apply_launches(const qt_ctx* c) {
   const qt::Plan& P = c->plan;
-  const int64_t n = P.main_end < (int64_t)P.stages.size() ? (int64_t)P.stages.size() - P.main_end
-                                                          : P.main_end - P.apply_begin;
+  const int64_t n = P.main_end < (int64_t)P.stages.size() ? kernels_in(P, P.main_end, (int64_t)P.stages.size())
+                                                          : kernels_in(P, P.apply_begin, P.main_end);
   return n + (c->prec == 1 ? 1 : 0);
 }
 }  // namespace
@@ -620,7 +631,7 @@ int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
   double2 alpha = make_double2(phase_im, -phase_re);
   QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PARAM], &alpha, sizeof(double2), cudaMemcpyHostToDevice, c->stream));
   QT_CUDA(c, cudaGraphLaunch(c->exec, c->stream));
-  c->launches += c->plan.main_end;
+  c->launches += kernels_in(c->plan, 0, c->plan.main_end);
   c->swept = true;
   c->built = true;
   return QT_OK;
@@ -630,7 +641,7 @@ int qt_build(qt_ctx* c) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_build needs qt_prepare and a wavefunction");
   QT_CUDA(c, cudaGraphLaunch(c->exec_build, c->stream));
-  c->launches += c->plan.apply_begin;
+  c->launches += kernels_in(c->plan, 0, c->plan.apply_begin);
   c->built = true;
   return QT_OK;
 }
@@ -712,7 +723,7 @@ int qt_cmf_propagate(qt_ctx* c, double dt, int n_steps, int n_sub, double phase_
     rc = rk4_frozen(c, Y, ACC, 0.5 * dt / n_sub, 2 * n_sub, alpha);
     if (rc != QT_OK) return rc;
     QT_CUDA(c, cudaMemcpyAsync(PSI, Y, n * 16, cudaMemcpyDeviceToDevice, c->stream));
-    c->launches += 2 * c->plan.apply_begin;
+    c->launches += 2 * kernels_in(c->plan, 0, c->plan.apply_begin);
   }
   c->built = false;
   c->swept = false;
@@ -890,6 +901,9 @@ int qt_hole_product(qt_ctx* c, void* S, const void* A, const void* B, int64_t be
   t.a = (int)activeA;
   t.after = (int)after;
   t.aB = (int)activeB;
+  t.splits = 1;
+  t.kchunk = 0;
+  t.ws = 0;
   cudaError_t e = qt::launch_single_hp(t, c->stream, nullptr);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_hole_product");
   c->launches += 1;
@@ -952,7 +966,7 @@ int qt_stage_launch(qt_ctx* c, int i) {
   cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->prec,
                                    c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_stage_launch");
-  c->launches += 1;
+  c->launches += 1 + (c->plan.stages[i].aux ? 1 : 0);
   return QT_OK;
 }
 

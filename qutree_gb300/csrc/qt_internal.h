@@ -36,7 +36,10 @@ struct HPTask {
   const double2* B;
   double2* S;
   int before, a, after;
-  int aB;  // columns of S (activeB); 0 means aB == a
+  int aB;      // columns of S (activeB); 0 means aB == a
+  int splits;  // k ranges of kchunk rows; > 1: partial tiles go to the workspace
+  int kchunk;
+  int64_t ws;  // workspace offset (elements) of the partial tiles
 };
 
 // out[r, j] (+)= alpha * sum_t sum_j' H_t(j, j') X_t[r, j'] over the terms
@@ -112,6 +115,7 @@ struct Stage {
   int64_t first_task, n_tasks;
   int64_t first_tile, n_tiles;
   const char* name;
+  int aux = 0;       // hole-product stage with split tasks: a second kernel sums the partial tiles
   double flops = 0;  // executed flops of the stage
   double bytes = 0;  // algorithmic bytes: operands read once, results written once
 };
@@ -127,8 +131,9 @@ struct Stage {
 // complex128; aliases with complex128 arithmetic), only when requested.
 // B_KEEP: node-sized tensors the compressed plan keeps from represent to
 // Apply (chain outputs and Phi x_last rho).
+// B_HPW: partial tiles of hole products split over their reduction index.
 enum Buf {
-  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP,
+  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW,
   B_NBUF
 };
 
@@ -187,6 +192,7 @@ struct Plan {
   int64_t mats_size = 0;
   int64_t scratch_size = 0;
   int64_t keep_size = 0;
+  int64_t hpw_size = 0;
   int64_t ops_size = 0;
   // symbolic task lists (buffer-relative); bound to pointers by bind()
   struct SMP {
@@ -197,6 +203,8 @@ struct Plan {
   struct SHP {
     Ref A, B, S;
     int before, a, after;
+    int splits = 1, kchunk = 0;
+    int64_t ws = 0;
   };
   struct SAccTerm {
     Ref H;  // buf == -1: identity
@@ -299,6 +307,7 @@ struct DevTables {
   CvtTask* cvt = nullptr;
   int2* cvt_tiles = nullptr;
   GradTask* grad = nullptr;
+  void* hp_ws = nullptr;
 };
 // prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe
 cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d, int prec,

@@ -199,19 +199,164 @@ __device__ __forceinline__ void hp_tile(const HPTask& t, int mt0) {
   if (has_i1 && has_j1) Sp[i1 + (int64_t)aA * j1] = P::fin(acc11);
 }
 
-template <class P>
-__global__ void __launch_bounds__(kThreads) k_hp(const HPTask* __restrict__ tasks,
-                                                 const int4* __restrict__ tiles, int64_t tile0) {
-  const int4 tl = tiles[tile0 + blockIdx.x];
-  const HPTask t = tasks[tl.x];
-  hp_tile<P>(t, tl.y);
-}
-
 __global__ void __launch_bounds__(kThreads) k_hp_single(HPTask t) {
   hp_tile<F64>(t, blockIdx.x * kThreads);
 }
 
 inline int hp_smem_bytes(int aA, int aB) { return kHpK * (aA + aB) * 16; }
+
+// ---------------------------------------------------------------------------
+// Hole products of the sweep, split over the reduction index k.  A block owns
+// one output tile of up to 64 x 64 and one range of kchunk rows of k; its
+// thread (tx, ty) of the TA x TB grid (TA = ceil(tile rows / 4)) owns the
+// 4 x 4 outputs {tx + TA r} x {ty + TB c}, 16 independent accumulators.  The
+// operand rows move into shared memory 16 at a time with cp.async into two
+// buffers, so the next rows load while the current ones are consumed.  A
+// task cut into several k ranges writes normalised partial tiles to the
+// workspace; k_hp_sum adds them in range order (deterministic).
+// ---------------------------------------------------------------------------
+constexpr int kHpTile = 64;
+constexpr int kHpRows = 16;
+constexpr int kHpSmem = 2 * 2 * kHpRows * kHpTile * 16;  // two buffers of A and B rows: 64 KiB
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 16 : 0;  // 0: fill the 16 bytes with zeros, read nothing
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(n) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <class P>
+__global__ void __launch_bounds__(kThreads, 2) k_hp(const HPTask* __restrict__ tasks,
+                                                    const int4* __restrict__ tiles, int64_t tile0,
+                                                    typename P::S* __restrict__ ws) {
+  typedef typename P::S S;
+  typedef typename P::A A;
+  extern __shared__ __align__(16) unsigned char hp_smem[];
+  S* sm = reinterpret_cast<S*>(hp_smem);  // [buffer][A rows | B rows][kHpRows][kHpTile]
+  const int4 tl = tiles[tile0 + blockIdx.x];
+  const HPTask t = tasks[tl.x];
+  const int aA = t.a, aB = t.aB > 0 ? t.aB : t.a;
+  const int nti = (aA + kHpTile - 1) / kHpTile;
+  const int ti0 = (tl.y % nti) * kHpTile, tj0 = (tl.y / nti) * kHpTile;
+  const int mA = min(kHpTile, aA - ti0), mB = min(kHpTile, aB - tj0);
+  const int TA = (mA + 3) >> 2, TB = (mB + 3) >> 2;
+  const int before = t.before;
+  const int64_t K = (int64_t)before * t.after;
+  const int64_t kb = (int64_t)tl.z * t.kchunk;
+  const int64_t ke = min(K, kb + (int64_t)t.kchunk);
+  const S* __restrict__ Ap = reinterpret_cast<const S*>(t.A);
+  const S* __restrict__ Bp = reinterpret_cast<const S*>(t.B);
+  const int64_t sliceA = (int64_t)before * aA, sliceB = (int64_t)before * aB;
+  const int tid = threadIdx.x;
+  const bool active = tid < TA * TB;
+  const int tx = active ? tid % TA : 0, ty = active ? tid / TA : 0;
+  const int wA = 4 * TA, wB = 4 * TB;  // staged columns (zero beyond the tile)
+  const int nA = kHpRows * wA, nAB = kHpRows * (wA + wB);
+  auto stage = [&](int buf, int64_t k0) {
+    S* dA = sm + buf * 2 * kHpRows * kHpTile;
+    S* dB = dA + kHpRows * kHpTile;
+    for (int e = tid; e < nAB; e += kThreads) {
+      const bool isA = e < nA;
+      const int ee = isA ? e : e - nA;
+      const int w = isA ? wA : wB;
+      int kk, ii;
+      if (before == 1) {  // consecutive columns are contiguous
+        ii = ee % w;
+        kk = ee / w;
+      } else {  // consecutive rows are contiguous
+        kk = ee % kHpRows;
+        ii = ee / kHpRows;
+      }
+      const int64_t k = k0 + kk;
+      const bool ok = k < ke && ii < (isA ? mA : mB);
+      const S* src = isA ? Ap : Bp;
+      if (ok) {
+        const int64_t b = k % before, c = k / before;
+        src += b + (int64_t)before * ((isA ? ti0 : tj0) + ii) + (isA ? sliceA : sliceB) * c;
+      }
+      cp_async16((isA ? dA : dB) + kk * kHpTile + ii, src, ok);
+    }
+    cp_async_commit();
+  };
+  A acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = P::zero();
+  const int64_t nchunks = (ke - kb + kHpRows - 1) / kHpRows;
+  if (nchunks > 0) stage(0, kb);
+  for (int64_t ch = 0; ch < nchunks; ++ch) {
+    if (ch + 1 < nchunks) {
+      stage((int)((ch + 1) & 1), kb + (ch + 1) * kHpRows);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    if (active) {
+      const S* cA = sm + (ch & 1) * 2 * kHpRows * kHpTile;
+      const S* cB = cA + kHpRows * kHpTile;
+#pragma unroll 2
+      for (int kk = 0; kk < kHpRows; ++kk) {
+        S a[4], b[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) a[r] = cA[kk * kHpTile + tx + TA * r];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) b[c] = cB[kk * kHpTile + ty + TB * c];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) P::macc(acc[r][c], a[r], b[c]);
+        if (kk & 1) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) P::norm(acc[r][c]);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!active) return;
+  S* Sp = reinterpret_cast<S*>(t.S);
+  const int64_t nS = (int64_t)aA * aB;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int i = tx + TA * r, j = ty + TB * c;
+      if (i < mA && j < mB) {
+        const int64_t o = (ti0 + i) + (int64_t)aA * (tj0 + j);
+        if (t.splits <= 1)
+          Sp[o] = P::fin(acc[r][c]);
+        else
+          ws[t.ws + (int64_t)tl.z * nS + o] = P::fin(acc[r][c]);
+      }
+    }
+}
+
+// S = sum over the k ranges of the partial tiles (one block per task)
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_hp_sum(const HPTask* __restrict__ tasks, int64_t task0,
+                                                     const typename P::S* __restrict__ ws) {
+  typedef typename P::S S;
+  typedef typename P::A A;
+  const HPTask t = tasks[task0 + blockIdx.x];
+  if (t.splits <= 1) return;
+  const int aB = t.aB > 0 ? t.aB : t.a;
+  const int64_t n = (int64_t)t.a * aB;
+  S* Sp = reinterpret_cast<S*>(t.S);
+  for (int64_t e = threadIdx.x; e < n; e += kThreads) {
+    A acc = P::zero();
+    for (int z = 0; z < t.splits; ++z) P::add(acc, ws[t.ws + z * n + e]);
+    Sp[e] = P::fin(acc);
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Last-mode accumulation (multStateAB summed over terms):
@@ -774,10 +919,14 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       k_mp<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
       break;
     case ST_HP: {
-      const int sm = hp_smem_bytes(kHpMaxDim, kHpMaxDim);
-      cudaError_t e = cudaFuncSetAttribute(k_hp<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+      cudaError_t e = cudaFuncSetAttribute(k_hp<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, kHpSmem);
       if (e != cudaSuccess) return e;
-      k_hp<P><<<(unsigned)st.n_tiles, kThreads, sm, s>>>(t.hp, t.hp_tiles, st.first_tile);
+      typedef typename P::S S;
+      k_hp<P><<<(unsigned)st.n_tiles, kThreads, kHpSmem, s>>>(t.hp, t.hp_tiles, st.first_tile,
+                                                              reinterpret_cast<S*>(t.hp_ws));
+      if (st.aux)
+        k_hp_sum<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.hp, st.first_task,
+                                                             reinterpret_cast<const S*>(t.hp_ws));
       break;
     }
     case ST_ACC:

@@ -33,6 +33,7 @@
 // fields are summed first (sum_l c_l H_l) x_last X, which is linear algebra
 // on the same products.
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <set>
 #include <stdexcept>
@@ -437,9 +438,47 @@ class Builder {
   }
 
   // ---- stage emission ------------------------------------------------------
+  // Blocks of the hole products [t0, t1): output tiles of up to 64 x 64 times
+  // ranges of kchunk reduction rows, kchunk chosen so that the stage fills
+  // about four blocks per SM; tasks with several ranges get workspace slots
+  // for their partial tiles.  Returns whether any task was split.
+  bool hp_split(int64_t t0, int64_t t1, int64_t& tile0, int64_t& tile1) {
+    constexpr int kTile = 64, kRows = 16;
+    auto ntiles = [](const Plan::SHP& h) {
+      return (int64_t)((h.a + kTile - 1) / kTile) * ((h.a + kTile - 1) / kTile);
+    };
+    double work = 0;
+    for (int64_t t = t0; t < t1; ++t) work += (double)ntiles(P.hp[t]) * P.hp[t].before * P.hp[t].after;
+    const double target = 4.0 * 152;
+    int64_t kc = (int64_t)std::ceil(work / target / kRows) * kRows;
+    kc = std::max<int64_t>(kc, 256);
+    tile0 = (int64_t)P.hp_tiles.size();
+    int64_t ws = 0;
+    bool split = false;
+    for (int64_t t = t0; t < t1; ++t) {
+      Plan::SHP& h = P.hp[t];
+      const int64_t K = (int64_t)h.before * h.after;
+      h.splits = (int)((K + kc - 1) / kc);
+      h.kchunk = (int)std::min<int64_t>(K, kc);
+      h.ws = 0;
+      if (h.splits > 1) {
+        h.ws = ws;
+        ws += (int64_t)h.splits * h.a * h.a;
+        split = true;
+      }
+      for (int64_t y = 0; y < ntiles(h); ++y)
+        for (int z = 0; z < h.splits; ++z) P.hp_tiles.push_back(make_int4((int)t, (int)y, z, 0));
+    }
+    tile1 = (int64_t)P.hp_tiles.size();
+    P.hpw_size = std::max(P.hpw_size, ws);
+    return split;
+  }
+
   void emit_stage(int kind, int64_t t0, int64_t t1, int64_t tile0, int64_t tile1,
                   const char* name) {
     if (t1 <= t0) return;
+    bool split = false;
+    if (kind == ST_HP) split = hp_split(t0, t1, tile0, tile1);
     const double f1 = P.stats.exec_flops;
     Stage s;
     s.flops = f1 - stage_flops_mark;
@@ -451,6 +490,7 @@ class Builder {
     s.first_tile = tile0;
     s.n_tiles = tile1 - tile0;
     s.name = name;
+    s.aux = split ? 1 : 0;
     P.stages.push_back(s);
   }
 
@@ -505,11 +545,7 @@ class Builder {
     t.before = (int)g.before(mode);
     t.a = g.shape[mode];
     t.after = (int)g.after(mode);
-    int task = (int)P.hp.size();
-    P.hp.push_back(t);
-    // 2x2 micro-tiles of S, 256 per tile (one per thread)
-    const int64_t micro = (int64_t)((t.a + 1) / 2) * ((t.a + 1) / 2);
-    for (int64_t m0 = 0; m0 < micro; m0 += 256) P.hp_tiles.push_back(make_int4(task, (int)m0, 0, 0));
+    P.hp.push_back(t);  // tiles are cut per stage (hp_split)
     P.stats.exec_flops += 8.0 * g.N * g.shape[mode];
   }
 
