@@ -348,6 +348,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.splits = s.splits;
     t.kchunk = s.kchunk;
     t.ws = s.ws;
+    t.rows = s.rows;
+    t.cols = s.cols;
     hp.push_back(t);
   }
   std::vector<qt::AccTask> acc;
@@ -461,6 +463,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.mp_tiles = (int2*)(base + offs[8]);
   c->tables.hp_tiles = (int4*)(base + offs[9]);
   c->tables.hp_ws = c->buf[qt::B_HPW];
+  c->tables.hp_segs = P.hp_segs.data();
   c->tables.acc_tiles = (int4*)(base + offs[10]);
   c->tables.cvt = (qt::CvtTask*)(base + offs[11]);
   c->tables.cvt_tiles = (int2*)(base + offs[12]);
@@ -612,7 +615,8 @@ namespace {
 // kernel launches of stages [b0, b1) (a split hole-product stage launches two)
 int64_t kernels_in(const qt::Plan& P, int64_t b0, int64_t b1) {
   int64_t n = 0;
-  for (int64_t i = b0; i < b1; ++i) n += 1 + (P.stages[i].aux ? 1 : 0);
+  for (int64_t i = b0; i < b1; ++i)
+    n += (P.stages[i].kind == qt::ST_HP ? P.stages[i].nseg : 1) + (P.stages[i].aux ? 1 : 0);
   return n;
 }
 // launches of one frozen-matrix derivative graph
@@ -904,6 +908,7 @@ int qt_hole_product(qt_ctx* c, void* S, const void* A, const void* B, int64_t be
   t.splits = 1;
   t.kchunk = 0;
   t.ws = 0;
+  t.rows = t.cols = 4;
   cudaError_t e = qt::launch_single_hp(t, c->stream, nullptr);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_hole_product");
   c->launches += 1;
@@ -966,7 +971,7 @@ int qt_stage_launch(qt_ctx* c, int i) {
   cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->prec,
                                    c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_stage_launch");
-  c->launches += 1 + (c->plan.stages[i].aux ? 1 : 0);
+  c->launches += kernels_in(c->plan, i, i + 1);
   return QT_OK;
 }
 

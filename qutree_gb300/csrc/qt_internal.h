@@ -40,6 +40,7 @@ struct HPTask {
   int splits;  // k ranges of kchunk rows; > 1: partial tiles go to the workspace
   int kchunk;
   int64_t ws;  // workspace offset (elements) of the partial tiles
+  int rows, cols;  // outputs per thread along i and j (1..4)
 };
 
 // out[r, j] (+)= alpha * sum_t sum_j' H_t(j, j') X_t[r, j'] over the terms
@@ -116,6 +117,7 @@ struct Stage {
   int64_t first_tile, n_tiles;
   const char* name;
   int aux = 0;       // hole-product stage with split tasks: a second kernel sums the partial tiles
+  int seg0 = 0, nseg = 0;  // hole-product stage: its tile segments (one launch per micro-tile shape)
   double flops = 0;  // executed flops of the stage
   double bytes = 0;  // algorithmic bytes: operands read once, results written once
 };
@@ -205,6 +207,7 @@ struct Plan {
     int before, a, after;
     int splits = 1, kchunk = 0;
     int64_t ws = 0;
+    int rows = 4, cols = 4;
   };
   struct SAccTerm {
     Ref H;  // buf == -1: identity
@@ -264,6 +267,7 @@ struct Plan {
   // tiles (bound with task indices only)
   std::vector<int2> mp_tiles;
   std::vector<int4> hp_tiles;
+  std::vector<int4> hp_segs;  // (rows, cols, first tile, tile count) per hole-product launch
   std::vector<int4> acc_tiles;
   std::vector<int2> cvt_tiles;
   // constant matrices written once at prepare: (offset, d) identity
@@ -308,6 +312,7 @@ struct DevTables {
   int2* cvt_tiles = nullptr;
   GradTask* grad = nullptr;
   void* hp_ws = nullptr;
+  const int4* hp_segs = nullptr;  // host array: (rows, cols, first tile, tile count)
 };
 // prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe
 cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d, int prec,

@@ -208,12 +208,14 @@ inline int hp_smem_bytes(int aA, int aB) { return kHpK * (aA + aB) * 16; }
 // ---------------------------------------------------------------------------
 // Hole products of the sweep, split over the reduction index k.  A block owns
 // one output tile of up to 64 x 64 and one range of kchunk rows of k; its
-// thread (tx, ty) of the TA x TB grid (TA = ceil(tile rows / 4)) owns the
-// 4 x 4 outputs {tx + TA r} x {ty + TB c}, 16 independent accumulators.  The
-// operand rows move into shared memory 16 at a time with cp.async into two
-// buffers, so the next rows load while the current ones are consumed.  A
-// task cut into several k ranges writes normalised partial tiles to the
-// workspace; k_hp_sum adds them in range order (deterministic).
+// thread (tx, ty) of the TA x TB grid owns the R x C outputs
+// {tx + TA r} x {ty + TB c} (R, C in 1..4 chosen per task by the planner so
+// that small tiles still occupy most of the 256 threads; one kernel per
+// shape, launched once per shape present in a stage).  The operand rows
+// move into shared memory 16 at a time with cp.async into two buffers: the
+// next rows load while the current ones are consumed, one barrier per 16
+// rows.  A task cut into several k ranges writes normalised partial tiles to
+// the workspace; k_hp_sum adds them in range order (deterministic).
 // ---------------------------------------------------------------------------
 constexpr int kHpTile = 64;
 constexpr int kHpRows = 16;
@@ -230,10 +232,10 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-template <class P>
-__global__ void __launch_bounds__(kThreads, 2) k_hp(const HPTask* __restrict__ tasks,
-                                                    const int4* __restrict__ tiles, int64_t tile0,
-                                                    typename P::S* __restrict__ ws) {
+template <class P, int R, int C>
+__global__ void __launch_bounds__(kThreads, R * C > 9 ? 2 : 3)
+    k_hp(const HPTask* __restrict__ tasks, const int4* __restrict__ tiles, int64_t tile0,
+         typename P::S* __restrict__ ws) {
   typedef typename P::S S;
   typedef typename P::A A;
   extern __shared__ __align__(16) unsigned char hp_smem[];
@@ -244,7 +246,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_hp(const HPTask* __restrict__ t
   const int nti = (aA + kHpTile - 1) / kHpTile;
   const int ti0 = (tl.y % nti) * kHpTile, tj0 = (tl.y / nti) * kHpTile;
   const int mA = min(kHpTile, aA - ti0), mB = min(kHpTile, aB - tj0);
-  const int TA = (mA + 3) >> 2, TB = (mB + 3) >> 2;
+  const int TA = (mA + R - 1) / R, TB = (mB + C - 1) / C;
   const int before = t.before;
   const int64_t K = (int64_t)before * t.after;
   const int64_t kb = (int64_t)tl.z * t.kchunk;
@@ -255,7 +257,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_hp(const HPTask* __restrict__ t
   const int tid = threadIdx.x;
   const bool active = tid < TA * TB;
   const int tx = active ? tid % TA : 0, ty = active ? tid / TA : 0;
-  const int wA = 4 * TA, wB = 4 * TB;  // staged columns (zero beyond the tile)
+  const int wA = R * TA, wB = C * TB;  // staged columns (zero beyond the tile; <= 64)
   const int nA = kHpRows * wA, nAB = kHpRows * (wA + wB);
   auto stage = [&](int buf, int64_t k0) {
     S* dA = sm + buf * 2 * kHpRows * kHpTile;
@@ -283,52 +285,48 @@ __global__ void __launch_bounds__(kThreads, 2) k_hp(const HPTask* __restrict__ t
     }
     cp_async_commit();
   };
-  A acc[4][4];
+  A acc[R][C];
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < R; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) acc[r][c] = P::zero();
+    for (int c = 0; c < C; ++c) acc[r][c] = P::zero();
   const int64_t nchunks = (ke - kb + kHpRows - 1) / kHpRows;
   if (nchunks > 0) stage(0, kb);
   for (int64_t ch = 0; ch < nchunks; ++ch) {
-    if (ch + 1 < nchunks) {
-      stage((int)((ch + 1) & 1), kb + (ch + 1) * kHpRows);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
+    cp_async_wait<0>();
+    // chunk ch has landed, and every thread is done with buffer (ch + 1) & 1
     __syncthreads();
+    if (ch + 1 < nchunks) stage((int)((ch + 1) & 1), kb + (ch + 1) * kHpRows);
     if (active) {
       const S* cA = sm + (ch & 1) * 2 * kHpRows * kHpTile;
       const S* cB = cA + kHpRows * kHpTile;
 #pragma unroll 2
       for (int kk = 0; kk < kHpRows; ++kk) {
-        S a[4], b[4];
+        S a[R], b[C];
 #pragma unroll
-        for (int r = 0; r < 4; ++r) a[r] = cA[kk * kHpTile + tx + TA * r];
+        for (int r = 0; r < R; ++r) a[r] = cA[kk * kHpTile + tx + TA * r];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) b[c] = cB[kk * kHpTile + ty + TB * c];
+        for (int c = 0; c < C; ++c) b[c] = cB[kk * kHpTile + ty + TB * c];
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+        for (int r = 0; r < R; ++r)
 #pragma unroll
-          for (int c = 0; c < 4; ++c) P::macc(acc[r][c], a[r], b[c]);
+          for (int c = 0; c < C; ++c) P::macc(acc[r][c], a[r], b[c]);
         if (kk & 1) {
 #pragma unroll
-          for (int r = 0; r < 4; ++r)
+          for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) P::norm(acc[r][c]);
+            for (int c = 0; c < C; ++c) P::norm(acc[r][c]);
         }
       }
     }
-    __syncthreads();
   }
   if (!active) return;
   S* Sp = reinterpret_cast<S*>(t.S);
   const int64_t nS = (int64_t)aA * aB;
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < R; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < C; ++c) {
       const int i = tx + TA * r, j = ty + TB * c;
       if (i < mA && j < mB) {
         const int64_t o = (ti0 + i) + (int64_t)aA * (tj0 + j);
@@ -911,6 +909,33 @@ cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops) {
   return cudaGetLastError();
 }
 
+template <class P, int R, int C>
+cudaError_t launch_hp_rc(const HPTask* tasks, const int4* tiles, int64_t first, int64_t n,
+                         typename P::S* ws, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_hp<P, R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, kHpSmem);
+  if (e != cudaSuccess) return e;
+  k_hp<P, R, C><<<(unsigned)n, kThreads, kHpSmem, s>>>(tasks, tiles, first, ws);
+  return cudaSuccess;
+}
+
+// the micro-tile shapes the planner chooses (rows x cols of outputs per thread)
+template <class P>
+cudaError_t launch_hp_shape(int rows, int cols, const HPTask* tasks, const int4* tiles, int64_t first,
+                            int64_t n, typename P::S* ws, cudaStream_t s) {
+  switch (rows * 8 + cols) {
+    case 1 * 8 + 1: return launch_hp_rc<P, 1, 1>(tasks, tiles, first, n, ws, s);
+    case 1 * 8 + 2: return launch_hp_rc<P, 1, 2>(tasks, tiles, first, n, ws, s);
+    case 1 * 8 + 3: return launch_hp_rc<P, 1, 3>(tasks, tiles, first, n, ws, s);
+    case 1 * 8 + 4: return launch_hp_rc<P, 1, 4>(tasks, tiles, first, n, ws, s);
+    case 2 * 8 + 3: return launch_hp_rc<P, 2, 3>(tasks, tiles, first, n, ws, s);
+    case 2 * 8 + 4: return launch_hp_rc<P, 2, 4>(tasks, tiles, first, n, ws, s);
+    case 3 * 8 + 3: return launch_hp_rc<P, 3, 3>(tasks, tiles, first, n, ws, s);
+    case 3 * 8 + 4: return launch_hp_rc<P, 3, 4>(tasks, tiles, first, n, ws, s);
+    case 4 * 8 + 4: return launch_hp_rc<P, 4, 4>(tasks, tiles, first, n, ws, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 template <class P>
 cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int max_eig_d,
                            cudaStream_t s) {
@@ -919,11 +944,12 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       k_mp<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
       break;
     case ST_HP: {
-      cudaError_t e = cudaFuncSetAttribute(k_hp<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, kHpSmem);
-      if (e != cudaSuccess) return e;
       typedef typename P::S S;
-      k_hp<P><<<(unsigned)st.n_tiles, kThreads, kHpSmem, s>>>(t.hp, t.hp_tiles, st.first_tile,
-                                                              reinterpret_cast<S*>(t.hp_ws));
+      for (int g = st.seg0; g < st.seg0 + st.nseg; ++g) {
+        const int4 sg = t.hp_segs[g];
+        cudaError_t e = launch_hp_shape<P>(sg.x, sg.y, t.hp, t.hp_tiles, sg.z, sg.w, reinterpret_cast<S*>(t.hp_ws), s);
+        if (e != cudaSuccess) return e;
+      }
       if (st.aux)
         k_hp_sum<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.hp, st.first_task,
                                                              reinterpret_cast<const S*>(t.hp_ws));

@@ -457,6 +457,20 @@ class Builder {
     bool split = false;
     for (int64_t t = t0; t < t1; ++t) {
       Plan::SHP& h = P.hp[t];
+      // outputs per thread: the fewest (rows x cols) whose thread grid
+      // ceil(m/rows) x ceil(m/cols) fits 256 threads and 64 staged columns
+      const int m = std::min(h.a, kTile);
+      int best = 1 << 30;
+      for (int r = 1; r <= 4; ++r)
+        for (int c = 1; c <= 4; ++c) {
+          const int tr = (m + r - 1) / r, tc = (m + c - 1) / c;
+          if (tr * tc > 256 || tr * r > kTile || tc * c > kTile) continue;
+          if (r * c < best) {
+            best = r * c;
+            h.rows = r;
+            h.cols = c;
+          }
+        }
       const int64_t K = (int64_t)h.before * h.after;
       h.splits = (int)((K + kc - 1) / kc);
       h.kchunk = (int)std::min<int64_t>(K, kc);
@@ -466,8 +480,18 @@ class Builder {
         ws += (int64_t)h.splits * h.a * h.a;
         split = true;
       }
-      for (int64_t y = 0; y < ntiles(h); ++y)
-        for (int z = 0; z < h.splits; ++z) P.hp_tiles.push_back(make_int4((int)t, (int)y, z, 0));
+    }
+    // tiles grouped by micro-tile shape: one launch per shape
+    for (int shape = 0; shape < 16; ++shape) {
+      const int64_t first = (int64_t)P.hp_tiles.size();
+      for (int64_t t = t0; t < t1; ++t) {
+        const Plan::SHP& h = P.hp[t];
+        if ((h.rows - 1) * 4 + (h.cols - 1) != shape) continue;
+        for (int64_t y = 0; y < ntiles(h); ++y)
+          for (int z = 0; z < h.splits; ++z) P.hp_tiles.push_back(make_int4((int)t, (int)y, z, 0));
+      }
+      const int64_t n = (int64_t)P.hp_tiles.size() - first;
+      if (n > 0) P.hp_segs.push_back(make_int4(shape / 4 + 1, shape % 4 + 1, (int)first, (int)n));
     }
     tile1 = (int64_t)P.hp_tiles.size();
     P.hpw_size = std::max(P.hpw_size, ws);
@@ -478,6 +502,7 @@ class Builder {
                   const char* name) {
     if (t1 <= t0) return;
     bool split = false;
+    const int64_t seg0 = (int64_t)P.hp_segs.size();
     if (kind == ST_HP) split = hp_split(t0, t1, tile0, tile1);
     const double f1 = P.stats.exec_flops;
     Stage s;
@@ -491,6 +516,8 @@ class Builder {
     s.n_tiles = tile1 - tile0;
     s.name = name;
     s.aux = split ? 1 : 0;
+    s.seg0 = (int)seg0;
+    s.nseg = (int)((int64_t)P.hp_segs.size() - seg0);
     P.stages.push_back(s);
   }
 

@@ -233,6 +233,13 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
   }
 }
 
+// name of stage i of the plan (nullptr past the end)
+const char* qtp_stage_name(void* h, int i) {
+  const qt::Plan& P = static_cast<Handle*>(h)->plan;
+  if (i < 0 || i >= (int)P.stages.size()) return nullptr;
+  return P.stages[i].name;
+}
+
 static bool is_double_table(int what) { return what >= 15 && what <= 17; }
 
 int64_t qtp_size(void* h, int what) {

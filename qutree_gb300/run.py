@@ -1,6 +1,6 @@
 """Run H.Psi sweeps of a benchmark configuration from the command line.
 
-  python -m qutree_gb300.run --config 1 --sweeps 2 [--flavour grouped|reference] [--prec f64|df64]
+  python -m qutree_gb300.run --config 1 --sweeps 2 [--flavour compressed|grouped|reference] [--prec f64|df64]
 
 Prints one line per sweep (energy, milliseconds).  Used to profile the
 library (ncu) with a fixed, small launch sequence: qt_prepare, then
@@ -19,12 +19,13 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--sweeps", type=int, default=2)
-    ap.add_argument("--flavour", default="grouped", choices=["grouped", "reference"])
+    ap.add_argument("--flavour", default="compressed", choices=["compressed", "grouped", "reference"])
     ap.add_argument("--prec", default="f64", choices=["f64", "df64"])
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     tree, sop, psi = config_problem(a.config)
-    flavour = qtgpu.QT_PLAN_GROUPED if a.flavour == "grouped" else qtgpu.QT_PLAN_REFERENCE
+    flavour = {"compressed": qtgpu.QT_PLAN_COMPRESSED, "grouped": qtgpu.QT_PLAN_GROUPED,
+               "reference": qtgpu.QT_PLAN_REFERENCE}[a.flavour]
     if a.prec == "df64":
         flavour |= qtgpu.QT_PREC_DF64
     hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, device=a.device)

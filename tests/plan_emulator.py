@@ -38,6 +38,8 @@ def lib():
         L.qtp_size.restype = ctypes.c_int64
         L.qtp_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.qtp_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.qtp_stage_name.restype = ctypes.c_char_p
+        L.qtp_stage_name.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -93,6 +95,7 @@ class PlanView:
             self.tables[what] = a[:n]
         self.mp_alpha = self.tables[15].reshape(-1, 2) @ np.array([1, 1j]) if len(self.tables[15]) else np.zeros(0)
         self.lin_c = self.tables[16].reshape(-1, 2) @ np.array([1, 1j]) if len(self.tables[16]) else np.zeros(0)
+        self.stage_names = [L.qtp_stage_name(h, i).decode() for i in range(len(self.tables[0]))]
         L.qtp_free(h)
         self.pairs = self.tables[13]  # rows (term, node, hslot, cslot), terms ascending
         s = self.tables[9]
