@@ -134,8 +134,10 @@ struct Stage {
 // B_KEEP: node-sized tensors the compressed plan keeps from represent to
 // Apply (chain outputs and Phi x_last rho).
 // B_HPW: partial tiles of hole products split over their reduction index.
+// B_KRY: input and output tensor of the SCF effective Hamiltonian (2 x the
+// largest node).
 enum Buf {
-  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW,
+  B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY,
   B_NBUF
 };
 
@@ -264,6 +266,12 @@ struct Plan {
   // stages [0, main_end) are the sweep.  Stages [main_end, end), when present,
   // replace [apply_begin, main_end) in the frozen-matrix derivative graph.
   int64_t main_end = 0;
+  // SCF (QT_PLAN_SCF): per node the stage ranges [begin, end) of buildUp,
+  // buildDown and the effective Hamiltonian (B_KRY input at kry_in, output at
+  // kry_out); empty ranges where the reference does nothing
+  bool scf = false;
+  std::vector<int64_t> scf_up_b, scf_up_e, scf_down_b, scf_down_e, scf_apply_b, scf_apply_e;
+  int64_t kry_in = 0, kry_out = 0, kry_size = 0;
   // tiles (bound with task indices only)
   std::vector<int2> mp_tiles;
   std::vector<int4> hp_tiles;

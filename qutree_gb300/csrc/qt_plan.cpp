@@ -85,6 +85,8 @@ class Builder {
     P.prec = prec;
   }
 
+  void set_scf(bool on) { scf = on; }
+
   void run() {
     geometry();
     activity();
@@ -96,6 +98,8 @@ class Builder {
     }
     stage_density();
     stage_inverse();
+    if (scf && (!compressed || P.prec != 0))
+      throw std::runtime_error("the SCF sweep needs the compressed plan in complex128 arithmetic");
     if (compressed) {
       if (P.want_grad) throw std::runtime_error("the energy gradient needs the grouped or reference plan");
       comp_layout();
@@ -108,6 +112,7 @@ class Builder {
       const double sweep_flops = P.stats.exec_flops;
       const PlanStats counts = P.stats;
       comp_frozen_apply();
+      if (scf) scf_segments();
       P.stats = counts;
       P.stats.exec_flops = sweep_flops;
     } else {
@@ -131,6 +136,7 @@ class Builder {
   const OpTable& ops;
   const SopDesc& sop;
   bool grouped, compressed;
+  bool scf = false;
   int64_t budget;
   int n = 0, L = 0;
   std::vector<int> tops;  // roots of the forest, ascending
@@ -1533,6 +1539,246 @@ class Builder {
     stage_final();
   }
 
+
+  // ---- SCF sweep segments (QT_PLAN_SCF) ------------------------------------
+  // HamiltonianRepresentation(H, tree, tree, tail=false) of the SCF
+  // (src/Applications/SCF.cpp:267-341): every term's sparse tree ends at the
+  // lowest common ancestor (LCA) of its leaves.  Per node, on top of the
+  // compressed objects (H(a,u), Block(a) = hCorr[a]):
+  //   O_a      hole overlap <Phi_p|Phi_p> at a: the hole matrix of every term
+  //            whose LCA is a (its parent lies outside the term's tree)
+  //   C'(a,u)  sum_l c_l hCons_l(a) of the boundary terms with restriction u;
+  //            built at p from the sibling matrices on Phi_p x_last O_p (LCA = p)
+  //            and from C'(p,w) (LCA above p)
+  //   Eout(a)  hConCorr[a]: terms acting only outside a
+  //            (buildDownCorrection, src/TreeClasses/HamiltonianRepresentation.cpp:163-203)
+  // buildUp(a) = the compressed represent jobs of a; buildDown(a) = O_a,
+  // C'(a,.), Eout(a); the effective Hamiltonian of SCF.cpp:36-84 is
+  //   H_eff(a) A = [LCA-a terms on A] x_last O_a + sum_k Block(k) x_k A
+  //              + sum_u (u on A) x_last C'(a,u) + A x_last Eout(a).
+  std::vector<std::vector<int64_t>> scf_c;  // C'(a,u) slots
+  std::vector<int64_t> o_slot, eout_slot;
+  std::vector<Ref> o_psi;  // Phi_p x_last O_p
+  std::map<int, int64_t> zero_dim;
+
+  int64_t zero_mat(int d) {
+    auto it = zero_dim.find(d);
+    if (it != zero_dim.end()) return it->second;
+    const int64_t o = alloc_mat(d);  // B_MATS is zeroed once at prepare and never written here
+    zero_dim[d] = o;
+    return o;
+  }
+
+  // LCA-a terms of node a: internal terms that touch two or more children
+  // (their signatures over the child legs for the cover)
+  void lca_terms(int a, int skip_child, std::vector<std::vector<int>>& sig, std::vector<int>& term_of) {
+    const NodeGeo& g = nd[a];
+    for (int l : internal[a]) {
+      if (g.bottom()) continue;
+      std::vector<int> s(g.children.size(), -1);
+      int nact = 0;
+      bool touches_skip = false, inside_one = false;
+      for (size_t k = 0; k < g.children.size(); ++k) {
+        const int b = bk_index(l, g.children[k]);
+        if (b == -2) continue;
+        ++nact;
+        if ((int)k == skip_child) touches_skip = true;
+        inside_one = inside_one || b == -1;
+        s[k] = b;
+      }
+      if (nact < 2 || touches_skip) continue;
+      if (inside_one) throw std::logic_error("SCF plan: internal child factor in an LCA term");
+      sig.push_back(s);
+      term_of.push_back(l);
+    }
+  }
+
+  void scf_segments() {
+    P.scf = true;
+    scf_c.assign(n, {});
+    o_slot.assign(n, -1);
+    eout_slot.assign(n, -1);
+    o_psi.assign(n, Ref{});
+    int64_t maxN = 16;
+    for (int a = 0; a < n; ++a) {
+      maxN = std::max(maxN, nd[a].N);
+      const int d = nd[a].dup();
+      for (size_t u = 0; u < bk[a].size(); ++u) scf_c[a].push_back(alloc_mat(d));
+      if (!is_top(a)) {
+        o_slot[a] = alloc_mat(d);
+        eout_slot[a] = alloc_mat(d);
+      }
+      if (!is_top(a) && !nd[a].bottom()) o_psi[a] = keep(nd[a].N);
+    }
+    P.kry_in = 0;
+    P.kry_out = align_up(maxN);
+    P.kry_size = 2 * align_up(maxN);
+    const Ref kin{B_KRY, P.kry_in}, kout{B_KRY, P.kry_out};
+    P.scf_up_b.assign(n, 0);
+    P.scf_up_e.assign(n, 0);
+    P.scf_down_b.assign(n, 0);
+    P.scf_down_e.assign(n, 0);
+    P.scf_apply_b.assign(n, 0);
+    P.scf_apply_e.assign(n, 0);
+    for (int a = 0; a < n; ++a) {
+      const NodeGeo& g = nd[a];
+      // buildUp(a)
+      P.scf_up_b[a] = (int64_t)P.stages.size();
+      if (!is_top(a)) {
+        std::vector<Job> jobs;
+        const int64_t lin0 = (int64_t)P.lin.size();
+        for (auto& b : bk[a]) {
+          Job J;
+          J.node = a;
+          J.out = b.X;
+          J.chains.push_back(Chain{psi(a), comp_body(b.terms[0], a), Ref{}});
+          J.S = mat(b.hslot);
+          J.hp_mode = g.last();
+          jobs.push_back(J);
+        }
+        if (!internal[a].empty()) jobs.push_back(y_job(a));
+        emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "scf-up-sums");
+        run_jobs(jobs, "scf-up");
+      }
+      P.scf_up_e[a] = (int64_t)P.stages.size();
+      // buildDown(a)
+      P.scf_down_b[a] = (int64_t)P.stages.size();
+      if (!is_top(a)) scf_down(a);
+      P.scf_down_e[a] = (int64_t)P.stages.size();
+      // effective Hamiltonian at a
+      P.scf_apply_b[a] = (int64_t)P.stages.size();
+      {
+        const int64_t lin0 = (int64_t)P.lin.size();
+        Job J;
+        J.node = a;
+        J.out = kout;
+        const Ref oa = is_top(a) ? Ref{} : mat(o_slot[a]);
+        if (g.bottom()) {
+          for (int l : internal[a]) J.chains.push_back(Chain{kin, body(l, a, sop.coeff[l]), oa});
+        } else {
+          std::vector<std::vector<int>> sig;
+          std::vector<int> term_of;
+          lca_terms(a, -1, sig, term_of);
+          std::vector<int> legs;
+          for (size_t k = 0; k < g.children.size(); ++k) legs.push_back((int)k);
+          for (auto& G : cover(sig, legs)) J.chains.push_back(Chain{kin, group_ops(a, G, sig, term_of), oa});
+          for (size_t k = 0; k < g.children.size(); ++k) {
+            const int c = g.children[k];
+            if (block_slot[c] >= 0)
+              J.chains.push_back(Chain{kin, {COp{0, (int)k, mat(block_slot[c]), c2(1, 0)}}, Ref{}});
+          }
+        }
+        for (size_t u = 0; u < bk[a].size(); ++u)
+          J.chains.push_back(Chain{kin, comp_body(bk[a][u].terms[0], a), mat(scf_c[a][u])});
+        if (!is_top(a)) J.chains.push_back(Chain{kin, {}, mat(eout_slot[a])});
+        if (J.chains.empty()) J.chains.push_back(Chain{kin, {}, mat(zero_mat(g.dup()))});
+        emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "scf-apply-sums");
+        std::vector<Job> jobs{J};
+        run_jobs(jobs, "scf-apply");
+      }
+      P.scf_apply_e[a] = (int64_t)P.stages.size();
+    }
+  }
+
+  void scf_down(int a) {
+    const int p = nd[a].parent;
+    const NodeGeo& gp = nd[p];
+    const int ia = nd[a].child_idx;
+    // O_a = <Phi_p|Phi_p> with the hole at a, and Phi_p x_last O_p
+    {
+      std::vector<Job> jobs;
+      Job J;
+      J.node = p;
+      J.chains.push_back(Chain{psi(p), {}, Ref{}});
+      J.S = mat(o_slot[a]);
+      J.hp_mode = ia;
+      jobs.push_back(J);
+      if (!is_top(p)) {
+        Job R;
+        R.node = p;
+        R.out = o_psi[p];
+        R.chains.push_back(Chain{psi(p), {COp{0, gp.last(), mat(o_slot[p]), c2(1, 0)}}, Ref{}});
+        jobs.push_back(R);
+      }
+      run_jobs(jobs, "scf-down-overlap");
+    }
+    const Ref in_lca = is_top(p) ? psi(p) : o_psi[p];
+    std::vector<int> legs;
+    for (size_t k = 0; k < gp.children.size(); ++k)
+      if ((int)k != ia) legs.push_back((int)k);
+    std::vector<Job> jobs;
+    const int64_t lin0 = (int64_t)P.lin.size();
+    // C'(a,u)
+    for (size_t u = 0; u < bk[a].size(); ++u) {
+      Job J;
+      J.node = p;
+      J.S = mat(scf_c[a][u]);
+      J.hp_mode = ia;
+      std::vector<std::vector<int>> sig;
+      std::vector<int> term_of;
+      std::map<int, int> wterm;
+      for (int l : bk[a][u].terms) {
+        const int bp = is_top(p) ? -1 : bk_index(l, p);
+        if (bp >= 0) {
+          wterm.insert({bp, l});
+          continue;
+        }
+        std::vector<int> sg(gp.children.size(), -1);
+        for (size_t k = 0; k < gp.children.size(); ++k) {
+          if ((int)k == ia) continue;
+          const int bs = bk_index(l, gp.children[k]);
+          if (bs == -1) throw std::logic_error("SCF plan: internal sibling factor");
+          sg[k] = bs >= 0 ? bs : -1;
+        }
+        sig.push_back(sg);
+        term_of.push_back(l);
+      }
+      for (auto& G : cover(sig, legs)) J.chains.push_back(Chain{in_lca, group_ops(p, G, sig, term_of), Ref{}});
+      for (auto& kv : wterm) {
+        Chain ch{psi(p), {}, mat(scf_c[p][kv.first])};
+        for (size_t k = 0; k < gp.children.size(); ++k) {
+          if ((int)k == ia) continue;
+          const int bs = bk_index(kv.second, gp.children[k]);
+          if (bs >= 0) ch.ops.push_back(COp{0, (int)k, mat(bk[gp.children[k]][bs].hslot), c2(1, 0)});
+        }
+        J.chains.push_back(ch);
+      }
+      jobs.push_back(J);
+    }
+    // Eout(a)
+    {
+      Job J;
+      J.node = p;
+      J.S = mat(eout_slot[a]);
+      J.hp_mode = ia;
+      std::vector<std::vector<int>> sig;
+      std::vector<int> term_of;
+      lca_terms(p, ia, sig, term_of);
+      for (auto& G : cover(sig, legs)) J.chains.push_back(Chain{in_lca, group_ops(p, G, sig, term_of), Ref{}});
+      if (!is_top(p))
+        for (size_t w = 0; w < bk[p].size(); ++w) {
+          const int l = bk[p][w].terms[0];
+          if (bk_index(l, a) != -2) continue;  // the restriction w touches a
+          Chain ch{psi(p), {}, mat(scf_c[p][w])};
+          for (size_t k = 0; k < gp.children.size(); ++k) {
+            const int bs = bk_index(l, gp.children[k]);
+            if (bs >= 0) ch.ops.push_back(COp{0, (int)k, mat(bk[gp.children[k]][bs].hslot), c2(1, 0)});
+          }
+          J.chains.push_back(ch);
+        }
+      for (size_t k = 0; k < gp.children.size(); ++k) {
+        const int c = gp.children[k];
+        if ((int)k == ia || block_slot[c] < 0) continue;
+        J.chains.push_back(Chain{psi(p), {COp{0, (int)k, mat(block_slot[c]), c2(1, 0)}}, Ref{}});
+      }
+      if (!is_top(p)) J.chains.push_back(Chain{psi(p), {}, mat(eout_slot[p])});
+      if (J.chains.empty()) J.chains.push_back(Chain{psi(p), {}, mat(zero_mat(gp.dup()))});
+      jobs.push_back(J);
+    }
+    emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "scf-down-sums");
+    run_jobs(jobs, "scf-down");
+  }
+
   // Flops of the reference call sequence (independent of this plan):
   // mode product 8*N*a, hole product 8*N*a, diagonal leaf op 6*N, complex
   // scale 6*N, accumulate 2*N, projector 24*N*d + 2*N, rho^-1 8*N*d.
@@ -1592,7 +1838,9 @@ std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTa
   plan.want_grad = grad;
   try {
     if (prec != 0 && prec != 1) throw std::runtime_error("unknown precision");
-    Builder b(plan, nodes, ops, sop, flavour, prec, scratch_budget_elems);
+    const bool scf = (flavour & 0x2000) != 0;
+    Builder b(plan, nodes, ops, sop, flavour & ~0x2000, prec, scratch_budget_elems);
+    b.set_scf(scf);
     b.run();
   } catch (const std::exception& e) {
     return e.what();

@@ -171,6 +171,19 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
         v.push_back(P.stop_off[k]);
       }
       break;
+    case 20:  // SCF segments per node: up, down, apply stage ranges
+      for (size_t a = 0; a < P.scf_up_b.size(); ++a) {
+        v.push_back(P.scf_up_b[a]);
+        v.push_back(P.scf_up_e[a]);
+        v.push_back(P.scf_down_b[a]);
+        v.push_back(P.scf_down_e[a]);
+        v.push_back(P.scf_apply_b[a]);
+        v.push_back(P.scf_apply_e[a]);
+      }
+      break;
+    case 21:
+      v = {P.kry_in, P.kry_out, P.kry_size, P.scf ? 1 : 0};
+      break;
     case 19:
       for (auto& t : P.grad) {
         put_ref(v, t.eout);

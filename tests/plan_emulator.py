@@ -21,7 +21,7 @@ _i32 = _P(dtype=np.int32, flags="C_CONTIGUOUS")
 _i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
-B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP = range(12)
+B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY = range(14)
 ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD = range(8)
 
 
@@ -77,8 +77,9 @@ class PlanView:
         self.h = h
         self.tree, self.sop = tree, sop
         self.tables = {}
-        widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14}
-        for what in list(range(14)) + [18, 19]:
+        widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
+                  20: 6}
+        for what in list(range(14)) + [18, 19, 20, 21]:
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -111,6 +112,16 @@ class PlanView:
     def run(self, psi_flat, phase=1.0, eps=1e-10, frozen_after=False):
         """Run the sweep (stages [0, main_end)).  ``frozen_after``: then run
         the frozen-matrix derivative stages on the same Psi as well."""
+        self.init(psi_flat, phase)
+        T = self.tables
+        stages = list(range(self.main_end))
+        if frozen_after:
+            stages += list(range(self.main_end, len(T[0])))
+        self.exec(stages, eps)
+        return self.bufs
+
+    def init(self, psi_flat, phase=1.0):
+        """Fresh buffers with Psi loaded (identities set, matrices zero)."""
         psi0 = np.asarray(psi_flat, np.complex128).copy()
         bufs = [psi0,
                 np.zeros(self.psi_arena, np.complex128),
@@ -120,7 +131,8 @@ class PlanView:
                 np.zeros(max(self.scratch_size, 16), np.complex128),
                 np.zeros(16, np.complex128), None, None,
                 np.zeros(self.psi_arena, np.complex128), None,
-                np.zeros(max(self.keep_size, 16), np.complex128)]
+                np.zeros(max(self.keep_size, 16), np.complex128), np.zeros(16, np.complex128),
+                np.zeros(max(int(self.tables[21][2]) if len(self.tables[21]) else 16, 16), np.complex128)]
         if self.prec == 1:
             # separate caller-facing complex128 arrays; conversions are copies here
             bufs[B_PSI] = np.zeros_like(psi0)
@@ -134,15 +146,18 @@ class PlanView:
         bufs[B_PARAM][0] = -1j * complex(phase)
         for off, d in self.tables[10]:
             bufs[B_MATS][off:off + d * d] = np.eye(d).ravel(order="F")
+        self.bufs = bufs
+
+    def exec(self, stage_ids, eps=1e-10):
+        """Execute the given stages on the current buffers."""
+        bufs = self.bufs
 
         def view(buf, off, n):
             return bufs[buf][off:off + n]
 
         T = self.tables
-        stages = list(T[0][:self.main_end])
-        if frozen_after:
-            stages += list(T[0][self.main_end:]) if len(T[0]) > self.main_end else []
-        for kind, t0, nt, _, _ in stages:
+        for si in stage_ids:
+            kind, t0, nt, _, _ = T[0][si]
             for t in range(t0, t0 + nt):
                 if kind == ST_MP:
                     ib, io, ob, oo, hb, ho, bef, ain, aout, aft, diag = T[1][t]
@@ -211,8 +226,6 @@ class PlanView:
                     view(r[6], r[7], d * d)[:] = Sinv.ravel(order="F")
                     view(r[8], r[9], d * d)[:] = Pm.ravel(order="F")
                     view(r[10], r[11], d * d)[:] = M2.ravel(order="F")
-        self.bufs = bufs
-        return bufs
 
     def dpsi(self):
         return self.bufs[B_DPSI64].copy()
@@ -232,3 +245,121 @@ class PlanView:
             s2 = hs if which == 0 else cs
             out.append(self.bufs[B_MATS][s2:s2 + dd] if s2 >= 0 else np.zeros(dd, np.complex128))
         return np.concatenate(out)
+
+
+# --------------------------------------------------------------------------
+# SCF sweep on the emulated plan (the host logic qt_scf runs around the GPU
+# stages): Lanczos on the effective Hamiltonian of each node, Cholesky-QR
+# (twice) toward the next node, R into the next node, buildUp / buildDown.
+# --------------------------------------------------------------------------
+def _mp(h, x, k):
+    return np.moveaxis(np.tensordot(h, x, axes=([1], [k])), 0, k)
+
+
+def _hole(a, b, k):
+    am = np.moveaxis(a, k, -1).reshape(-1, a.shape[k])
+    bm = np.moveaxis(b, k, -1).reshape(-1, b.shape[k])
+    return am.conj().T @ bm
+
+
+def chol_qr(x, mode, cond_limit=1e-6):
+    """Q with orthonormal columns along `mode`: Cholesky-QR applied twice,
+    Householder QR when the Gram matrix is (near) singular -- the rule qt_scf
+    follows."""
+    q = x
+    for _ in range(2):
+        s = _hole(q, q, mode)
+        try:
+            L = np.linalg.cholesky(s)
+        except np.linalg.LinAlgError:
+            L = None
+        dg = np.abs(np.diag(L)) if L is not None else None
+        if L is None or dg.min() <= cond_limit * dg.max():
+            xm = np.moveaxis(x, mode, -1)
+            shp = xm.shape
+            qh, _ = np.linalg.qr(xm.reshape(-1, shp[-1]))
+            return np.moveaxis(qh.reshape(shp), -1, mode)
+        r = L.conj().T  # s = r^dag r, r upper triangular
+        q = _mp(np.linalg.inv(r).T, q, mode)
+    return q
+
+
+def scf_emulated(pv, tree, psi_flat, n_iter=1, n_krylov=5, n_itp=0, beta=1.0):
+    from scf import sweep_order  # oracle module: the reference's sweep order
+    pv.init(psi_flat)
+    arena = pv.bufs[B_PSI]
+    offs = tree.offsets()
+    seg = pv.tables[20]
+    kin, kout = int(pv.tables[21][0]), int(pv.tables[21][1])
+
+    def get(a):
+        n = tree.nodes[a]
+        return arena[offs[a]:offs[a + 1]].reshape(n.shape, order="F").copy()
+
+    def put(a, x):
+        arena[offs[a]:offs[a + 1]] = x.ravel(order="F")
+
+    def H(x, a):
+        K = pv.bufs[B_KRY]
+        n = x.size
+        K[kin:kin + n] = x.ravel(order="F")
+        pv.exec(range(seg[a][4], seg[a][5]))
+        return K[kout:kout + n].reshape(x.shape, order="F").copy()
+
+    for n in tree.nodes:
+        if n.parent >= 0:
+            pv.exec(range(seg[n.address][0], seg[n.address][1]))
+    order = sweep_order(tree)
+    energies = []
+    for it in range(n_iter):
+        for i, a in enumerate(order):
+            n = tree.nodes[a]
+            size = min(n_krylov, int(np.prod(n.shape)))
+            x = get(a)
+            x = x / np.sqrt(np.vdot(x, x).real)
+            space = [x]
+            alpha, betas = [], []
+            hx = H(x, a)
+            alpha.append(np.vdot(x, hx).real)
+            w = hx - alpha[-1] * x
+            for l in range(1, size):
+                nrm = np.sqrt(np.vdot(w, w).real)
+                betas.append(nrm)
+                v = w / nrm
+                space.append(v)
+                hx = H(v, a)
+                alpha.append(np.vdot(v, hx).real)
+                w = hx - alpha[-1] * space[l] - betas[-1] * space[l - 1]
+            T = np.diag(alpha)
+            for l in range(size - 1):
+                T[l + 1, l] = T[l, l + 1] = betas[l]
+            E, U = np.linalg.eigh(T)
+            energies.append(E[0])
+            if it < n_itp:
+                c = np.zeros(size, complex)
+                for l in range(size):
+                    c[l] += U[l, 0] * U[0, 0]
+                    for k in range(size):
+                        c[l] += U[l, k] * np.exp(-beta * (E[k] - E[0])) * U[0, k]
+                y = sum(c[l] * space[l] for l in range(size))
+                y = y / np.sqrt(np.vdot(y, y).real)
+            else:
+                y = sum(U[l, 0] * space[l] for l in range(size))
+            nxt = order[i + 1] if i + 1 < len(order) else None
+            out_idx = (n.children.index(nxt) if nxt is not None and nxt in n.children
+                       else len(n.shape) - 1)
+            q = chol_qr(y, out_idx)
+            put(a, q)
+            if nxt is None:
+                break
+            r = _hole(q, y, out_idx)
+            m = tree.nodes[nxt]
+            in_idx = m.children.index(a) if a in m.children else len(m.shape) - 1
+            put(nxt, _mp(r, get(nxt), in_idx))
+            up = n.parent == nxt
+            if up:
+                pv.exec(range(seg[a][0], seg[a][1]))
+            else:
+                pv.exec(range(seg[nxt][2], seg[nxt][3]))
+    psi_out = arena[:offs[-1]].copy()
+    return np.array(energies), psi_out
