@@ -77,6 +77,13 @@ extern "C" {
  * counterpart in the reference (QuTree has no tree-network gradient). */
 #define QT_PLAN_GRADIENT 0x1000
 
+/* OR-ed into QT_PLAN_COMPRESSED (complex128 arithmetic): also plan the SCF /
+ * Krylov sweep of qt_scf -- the HamiltonianRepresentation(H, tree, tree,
+ * tail = false) of QuTree's SCF with its correction matrices
+ * (include/TreeClasses/HamiltonianRepresentation.h:19-177,
+ * src/TreeClasses/HamiltonianRepresentation.cpp:117-203). */
+#define QT_PLAN_SCF 0x2000
+
 /* Matrix sets for qt_matrices_download. */
 #define QT_MAT_RHO 0     /* density matrices, per node, d_up x d_up          */
 #define QT_MAT_RHOINV 1  /* regularised inverse density matrices             */
@@ -182,6 +189,25 @@ int qt_layer_derivatives(qt_ctx* ctx, double phase_re, double phase_im);
  * sized work vectors on first use.  Asynchronous. */
 int qt_cmf_propagate(qt_ctx* ctx, double dt, int n_steps, int n_sub, double phase_re,
                      double phase_im);
+/* SCF / Krylov sweep of QuTree's scf() (src/Applications/SCF.cpp:267-341)
+ * on the wavefunction of the context (plans prepared with
+ * QT_PLAN_COMPRESSED | QT_PLAN_SCF, one tree): build the tail-free matrices
+ * and corrections bottom-up, then n_iter sweeps over the nodes in depth-first
+ * order (top, child subtree, top, ...): at every node a Lanczos space of
+ * n_krylov vectors of the effective Hamiltonian (SCF.cpp:36-84,138-195),
+ * imaginary-time propagation by beta for the first n_itp sweeps
+ * (SCF.cpp:197-222) or the lowest Ritz vector after them, isometrisation
+ * toward the next node (Cholesky-QR twice; Householder QR when the Gram
+ * matrix is near singular) with R multiplied into the next node, and the
+ * edge-local rebuild (buildUp / buildDown).  ritz (may be NULL) receives the
+ * lowest Ritz value of every Krylov solve, n_iter * (2 * nodes - 1) of them;
+ * ritz_count their number.  The optimised wavefunction stays in the context
+ * (qt_psi_download).  1 <= n_krylov <= 30.  When a Lanczos residual falls
+ * below 1e-12 of the Lanczos matrix norm the space is invariant and ends
+ * there (the reference divides by the vanishing norm, SCF.cpp:171-173, and
+ * continues on rounding noise).  Synchronises. */
+int qt_scf(qt_ctx* ctx, int n_iter, int n_krylov, int n_itp, double beta, double* ritz,
+           int64_t ritz_capacity, int64_t* ritz_count);
 /* Energy gradient of the last sweep (plans prepared with QT_PLAN_GRADIENT),
  * packed layout like the wavefunction.  Synchronises. */
 int qt_gradient_download(qt_ctx* ctx, double* grad_host);

@@ -223,7 +223,10 @@ class SCFOracle:
         return HA
 
     # -- Krylov ----------------------------------------------------------------
-    def solve_krylov(self, psi_node, a, size):
+    def solve_krylov(self, psi_node, a, size, breakdown=None):
+        """``breakdown``: None follows SCF.cpp (divide by any residual norm);
+        a number ends the Lanczos space when the residual norm falls below it
+        times the largest |alpha|, beta so far -- the rule qt_scf applies."""
         space = []
         x = psi_node.copy()
         x = x / np.sqrt(_full(x, x).real)
@@ -234,6 +237,9 @@ class SCFOracle:
         x = hx - alpha[-1] * x
         for l in range(1, size):
             nrm = np.sqrt(_full(x, x).real)
+            if breakdown is not None and nrm <= breakdown * max(np.abs(alpha).max(), max(beta, default=0.0)):
+                size = l
+                break
             beta.append(nrm)
             x = x / nrm
             space.append(x)
@@ -241,6 +247,7 @@ class SCFOracle:
             alpha.append(_full(x, hx).real)
             x = hx - alpha[-1] * space[l] - beta[-1] * space[l - 1]
         T = np.diag(alpha).astype(complex)
+        size = len(alpha)
         for l in range(size - 1):
             T[l + 1, l] = T[l, l + 1] = beta[l]
         E, U = np.linalg.eigh(T)
@@ -295,9 +302,9 @@ def _qr_mode(x, mode):
     return np.moveaxis(q.reshape(shp), -1, mode)
 
 
-def scf(tree, sop, psi_tensors, n_iter=1, n_krylov=5, n_itp=0, beta=1.0):
+def scf(tree, sop, psi_tensors, n_iter=1, n_krylov=5, n_itp=0, beta=1.0, breakdown=None):
     """Run the SCF sweep; returns (lowest Ritz value of every Krylov solve,
-    final node tensors)."""
+    final node tensors).  ``breakdown``: see SCFOracle.solve_krylov."""
     psi = [np.array(t, dtype=complex, copy=True) for t in psi_tensors]
     rep = SCFOracle(tree, sop)
     rep.initial_build(psi)
@@ -307,7 +314,7 @@ def scf(tree, sop, psi_tensors, n_iter=1, n_krylov=5, n_itp=0, beta=1.0):
         for i, a in enumerate(order):
             n = tree.nodes[a]
             size = min(n_krylov, psi[a].size)
-            space, E, U = rep.solve_krylov(psi[a], a, size)
+            space, E, U = rep.solve_krylov(psi[a], a, size, breakdown)
             energies.append(E[0])
             if it < n_itp:
                 psi[a] = rep.imaginary_time(space, E, U, beta)

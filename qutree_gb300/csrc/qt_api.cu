@@ -256,7 +256,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   if (!c->have_tree || !c->have_sop) return fail(c, QT_ERR_STATE, "qt_prepare needs tree and SOP");
   const int prec = (flavour & QT_PREC_DF64) ? 1 : 0;
   const bool grad = (flavour & QT_PLAN_GRADIENT) != 0;
-  flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT);
+  const bool scf = (flavour & QT_PLAN_SCF) != 0;
+  flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT | QT_PLAN_SCF);
   if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED && flavour != QT_PLAN_COMPRESSED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
   QT_CUDA(c, cudaSetDevice(c->device));
@@ -266,7 +267,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     long v = std::atol(s);
     if (v > 0) budget = (int64_t)v * (1 << 20) / 16;
   }
-  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour, prec, budget, grad);
+  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour | (scf ? 0x2000 : 0), prec, budget, grad);
   if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
   Plan& P = c->plan;
   c->buf_elems[qt::B_PSI] = P.psi_arena;
@@ -282,6 +283,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_GRAD64] = (grad && prec == 1) ? P.psi_arena : 0;
   c->buf_elems[qt::B_KEEP] = P.keep_size;
   c->buf_elems[qt::B_HPW] = P.hpw_size;
+  c->buf_elems[qt::B_KRY] = P.kry_size;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
@@ -1007,3 +1009,455 @@ int qt_probe_fp64_peak(qt_ctx* c, double* tflops) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// SCF / Krylov sweep (QT_PLAN_SCF): the scf() driver of QuTree
+// (src/Applications/SCF.cpp:267-341) around the plan's per-node segments.
+// ---------------------------------------------------------------------------
+namespace {
+
+using cd = double2;
+constexpr double kLanczosBreakdown = 1e-12;  // residual norm / |T| below which the space is invariant
+
+int run_stages(qt_ctx* c, int64_t b, int64_t e) {
+  const Plan& P = c->plan;
+  for (int64_t i = b; i < e; ++i) {
+    cudaError_t err = qt::launch_stage(P.stages[i], c->tables, c->eps, P.max_eig_d, c->prec, c->stream);
+    if (err != cudaSuccess) return cuda_fail(c, err, P.stages[i].name);
+  }
+  c->launches += kernels_in(P, b, e);
+  return QT_OK;
+}
+
+inline cd cmk(double x, double y) { return make_double2(x, y); }
+inline cd cmulh(cd a, cd b) { return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+inline cd cconj(cd a) { return cmk(a.x, -a.y); }
+
+// Eigen-decomposition of the symmetric tridiagonal Lanczos matrix (size <= 32)
+// by cyclic Jacobi rotations; eigenvalues ascending, U(:, k) the eigenvectors.
+void tridiag_eigh(const std::vector<double>& alpha, const std::vector<double>& beta, int m,
+                  std::vector<double>& E, std::vector<double>& U) {
+  std::vector<double> A(m * m, 0.0);
+  U.assign(m * m, 0.0);
+  for (int i = 0; i < m; ++i) {
+    A[i + m * i] = alpha[i];
+    U[i + m * i] = 1.0;
+    if (i + 1 < m) A[i + 1 + m * i] = A[i + m * (i + 1)] = beta[i];
+  }
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int j = 0; j < m; ++j)
+      for (int i = 0; i < m; ++i) {
+        tot += A[i + m * j] * A[i + m * j];
+        if (i != j) off += A[i + m * j] * A[i + m * j];
+      }
+    if (off <= 1e-32 * tot || off == 0.0) break;
+    for (int p = 0; p < m; ++p)
+      for (int q = p + 1; q < m; ++q) {
+        const double apq = A[p + m * q];
+        if (apq == 0.0) continue;
+        const double theta = (A[q + m * q] - A[p + m * p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < m; ++k) {  // columns p, q
+          const double akp = A[k + m * p], akq = A[k + m * q];
+          A[k + m * p] = cs * akp - sn * akq;
+          A[k + m * q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < m; ++k) {  // rows p, q
+          const double apk = A[p + m * k], aqk = A[q + m * k];
+          A[p + m * k] = cs * apk - sn * aqk;
+          A[q + m * k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < m; ++k) {
+          const double ukp = U[k + m * p], ukq = U[k + m * q];
+          U[k + m * p] = cs * ukp - sn * ukq;
+          U[k + m * q] = sn * ukp + cs * ukq;
+        }
+      }
+  }
+  std::vector<int> idx(m);
+  for (int i = 0; i < m; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return A[x + m * x] < A[y + m * y]; });
+  std::vector<double> U2(m * m);
+  E.assign(m, 0.0);
+  for (int k = 0; k < m; ++k) {
+    E[k] = A[idx[k] + m * idx[k]];
+    for (int i = 0; i < m; ++i) U2[i + m * k] = U[i + m * idx[k]];
+  }
+  U.swap(U2);
+}
+
+// S = R^dag R with R upper triangular (complex Cholesky); false when S is not
+// numerically positive definite (smallest pivot <= tol * largest)
+bool cholesky_upper(const std::vector<cd>& S, int d, std::vector<cd>& R, double tol) {
+  R.assign(d * d, cmk(0, 0));
+  double pmax = 0.0, pmin = 1e300;
+  for (int j = 0; j < d; ++j) {
+    // R(j, j) = sqrt(S(j,j) - sum_k |R(k,j)|^2)
+    double s = S[j + d * j].x;
+    for (int k = 0; k < j; ++k) s -= R[k + d * j].x * R[k + d * j].x + R[k + d * j].y * R[k + d * j].y;
+    if (!(s > 0.0) || !std::isfinite(s)) return false;
+    const double rjj = std::sqrt(s);
+    R[j + d * j] = cmk(rjj, 0);
+    pmax = std::max(pmax, rjj);
+    pmin = std::min(pmin, rjj);
+    for (int i = j + 1; i < d; ++i) {
+      // R(j, i) = (S(j, i) - sum_k conj(R(k, j)) R(k, i)) / R(j, j)
+      cd v = S[j + d * i];
+      for (int k = 0; k < j; ++k) {
+        const cd p = cmulh(cconj(R[k + d * j]), R[k + d * i]);
+        v.x -= p.x;
+        v.y -= p.y;
+      }
+      R[j + d * i] = cmk(v.x / rjj, v.y / rjj);
+    }
+  }
+  return pmin > tol * pmax;
+}
+
+// h = (R^-1)^T for an upper-triangular R, so that Y x_mode h = Y R^-1
+void inv_upper_transposed(const std::vector<cd>& R, int d, std::vector<cd>& h) {
+  std::vector<cd> X(d * d, cmk(0, 0));  // X = R^-1, upper triangular
+  for (int j = 0; j < d; ++j) {
+    const double den = R[j + d * j].x * R[j + d * j].x + R[j + d * j].y * R[j + d * j].y;
+    X[j + d * j] = cmk(R[j + d * j].x / den, -R[j + d * j].y / den);
+    for (int i = j - 1; i >= 0; --i) {
+      cd v = cmk(0, 0);
+      for (int k = i + 1; k <= j; ++k) {
+        const cd p = cmulh(R[i + d * k], X[k + d * j]);
+        v.x += p.x;
+        v.y += p.y;
+      }
+      const cd rii = R[i + d * i];
+      const double dd = rii.x * rii.x + rii.y * rii.y;
+      const cd inv = cmk(rii.x / dd, -rii.y / dd);
+      const cd q = cmulh(v, inv);
+      X[i + d * j] = cmk(-q.x, -q.y);
+    }
+  }
+  h.assign(d * d, cmk(0, 0));
+  for (int a = 0; a < d; ++a)
+    for (int b = 0; b < d; ++b) h[b + d * a] = X[a + d * b];
+}
+
+// Thin Q of the m x d column-major matrix M (m >= d) by Householder
+// reflections with LAPACK's convention (zgeqrf / zungqr: beta = -sign(Re alpha) |x|)
+void householder_thin_q(std::vector<cd>& M, int64_t m, int d) {
+  std::vector<cd> tau(d, cmk(0, 0));
+  for (int k = 0; k < d; ++k) {
+    cd* x = &M[(size_t)k * m + k];
+    const int64_t len = m - k;
+    double xn2 = 0.0;
+    for (int64_t i = 1; i < len; ++i) xn2 += x[i].x * x[i].x + x[i].y * x[i].y;
+    const cd alpha = x[0];
+    if (xn2 == 0.0 && alpha.y == 0.0) {
+      tau[k] = cmk(0, 0);
+    } else {
+      double beta = std::sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2);
+      if (alpha.x >= 0.0) beta = -beta;
+      tau[k] = cmk((beta - alpha.x) / beta, -alpha.y / beta);
+      const cd den = cmk(alpha.x - beta, alpha.y);
+      const double dd = den.x * den.x + den.y * den.y;
+      const cd inv = cmk(den.x / dd, -den.y / dd);
+      for (int64_t i = 1; i < len; ++i) x[i] = cmulh(x[i], inv);
+      x[0] = cmk(beta, 0);
+    }
+    // apply H^H = I - conj(tau) v v^H to the columns right of k (v(0) = 1)
+    const cd tc = cconj(tau[k]);
+    for (int j = k + 1; j < d; ++j) {
+      cd* y = &M[(size_t)j * m + k];
+      cd w = y[0];
+      for (int64_t i = 1; i < len; ++i) {
+        const cd p = cmulh(cconj(x[i]), y[i]);
+        w.x += p.x;
+        w.y += p.y;
+      }
+      const cd f = cmulh(tc, w);
+      y[0].x -= f.x;
+      y[0].y -= f.y;
+      for (int64_t i = 1; i < len; ++i) {
+        const cd p = cmulh(x[i], f);
+        y[i].x -= p.x;
+        y[i].y -= p.y;
+      }
+    }
+  }
+  // Q = H_0 H_1 ... H_{d-1} applied to the first d columns of the identity
+  std::vector<cd> Q((size_t)m * d, cmk(0, 0));
+  for (int j = 0; j < d; ++j) Q[(size_t)j * m + j] = cmk(1, 0);
+  for (int k = d - 1; k >= 0; --k) {
+    const cd* v = &M[(size_t)k * m + k];
+    const int64_t len = m - k;
+    for (int j = k; j < d; ++j) {
+      cd* y = &Q[(size_t)j * m + k];
+      cd w = y[0];
+      for (int64_t i = 1; i < len; ++i) {
+        const cd p = cmulh(cconj(v[i]), y[i]);
+        w.x += p.x;
+        w.y += p.y;
+      }
+      const cd f = cmulh(tau[k], w);
+      y[0].x -= f.x;
+      y[0].y -= f.y;
+      for (int64_t i = 1; i < len; ++i) {
+        const cd p = cmulh(v[i], f);
+        y[i].x -= p.x;
+        y[i].y -= p.y;
+      }
+    }
+  }
+  M.swap(Q);
+}
+
+// scf_sweep: depth first from the top, back to the node after each child
+void sweep_order(const std::vector<qt::NodeGeo>& nd, int a, std::vector<int>& out) {
+  out.push_back(a);
+  for (int c : nd[a].children) {
+    sweep_order(nd, c, out);
+    out.push_back(a);
+  }
+}
+
+struct DevFree {
+  void* p = nullptr;
+  ~DevFree() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* ritz, int64_t ritz_capacity,
+           int64_t* ritz_count) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_scf needs qt_prepare and a wavefunction");
+  const Plan& P = c->plan;
+  if (!P.scf) return fail(c, QT_ERR_STATE, "plan prepared without QT_PLAN_SCF");
+  if (P.tops.size() != 1) return fail(c, QT_ERR_SHAPE, "qt_scf sweeps one tree");
+  if (n_iter < 0 || n_krylov < 1 || n_krylov > qt::kLinCombMax - 2 || n_itp < 0)
+    return fail(c, QT_ERR_ARG, "qt_scf: n_iter >= 0, 1 <= n_krylov <= 30, n_itp >= 0");
+  const std::vector<qt::NodeGeo>& nd = P.nodes;
+  std::vector<int> order;
+  sweep_order(nd, P.tops[0], order);
+  const int64_t solves = (int64_t)n_iter * (int64_t)order.size();
+  if (ritz && ritz_capacity < solves) return fail(c, QT_ERR_ARG, "qt_scf: ritz buffer too small");
+  if (ritz_count) *ritz_count = 0;
+  QT_CUDA(c, cudaSetDevice(c->device));
+  int64_t maxN = 16;
+  int maxd = 1;
+  for (const auto& g : nd) {
+    maxN = std::max(maxN, g.N);
+    for (int x : g.shape) maxd = std::max(maxd, x);
+  }
+  const int64_t vstride = (maxN + 15) / 16 * 16, mstride = (int64_t)maxd * maxd;
+  // vectors V_0..V_{K-1}, W, Y, T; matrices S, H, R; one scalar
+  const int64_t total = (n_krylov + 3) * vstride + 3 * mstride + 16;
+  DevFree work;
+  {
+    cudaError_t e = cudaMalloc(&work.p, total * sizeof(cd));
+    if (e != cudaSuccess) return fail(c, QT_ERR_ALLOC, std::string("qt_scf: work allocation failed: ") + cudaGetErrorString(e));
+  }
+  cd* base = (cd*)work.p;
+  auto V = [&](int l) { return base + (int64_t)l * vstride; };
+  cd* W = V(n_krylov);
+  cd* Y = V(n_krylov + 1);
+  cd* T = V(n_krylov + 2);
+  cd* dS = base + (n_krylov + 3) * vstride;
+  cd* dH = dS + mstride;
+  cd* dR = dH + mstride;
+  cd* dscal = dR + mstride;
+  cd* psi = c->buf[qt::B_PSI];
+  cd* kin = c->buf[qt::B_KRY] + P.kry_in;
+  cd* kout = c->buf[qt::B_KRY] + P.kry_out;
+  auto dot = [&](const cd* a, const cd* b, int64_t n, cd& out) -> int {
+    cudaError_t e = qt::launch_dot(a, b, n, dscal, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf dot");
+    QT_CUDA(c, cudaMemcpyAsync(&out, dscal, sizeof(cd), cudaMemcpyDeviceToHost, c->stream));
+    QT_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->launches += 1;
+    return QT_OK;
+  };
+  auto lincomb = [&](cd* out, std::initializer_list<std::pair<const cd*, cd>> terms, int64_t n) -> int {
+    qt::LinComb lc;
+    lc.count = 0;
+    for (auto& t : terms) {
+      lc.v[lc.count] = t.first;
+      lc.c[lc.count] = t.second;
+      ++lc.count;
+    }
+    cudaError_t e = qt::launch_lincomb(out, lc, n, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf lincomb");
+    c->launches += 1;
+    return QT_OK;
+  };
+  auto hole = [&](const cd* A, const cd* B, const qt::NodeGeo& g, int mode, cd* S) -> int {
+    qt::HPTask t;
+    t.A = A;
+    t.B = B;
+    t.S = S;
+    t.before = (int)g.before(mode);
+    t.a = g.shape[mode];
+    t.after = (int)g.after(mode);
+    t.aB = 0;
+    t.splits = 1;
+    t.kchunk = 0;
+    t.ws = 0;
+    t.rows = t.cols = 4;
+    cudaError_t e = qt::launch_single_hp(t, c->stream, nullptr);
+    if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf hole product");
+    c->launches += 1;
+    return QT_OK;
+  };
+  auto mode_product = [&](const cd* h, const cd* in, cd* out, const qt::NodeGeo& g, int mode) -> int {
+    qt::MPTask t;
+    t.in = in;
+    t.out = out;
+    t.h = h;
+    t.alpha = cmk(1, 0);
+    t.before = (int)g.before(mode);
+    t.a_in = t.a_out = g.shape[mode];
+    t.after = (int)g.after(mode);
+    t.diag = 0;
+    t.add = 0;
+    cudaError_t e = qt::launch_single_mp(t, c->stream, nullptr);
+    if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf mode product");
+    c->launches += 1;
+    return QT_OK;
+  };
+  int rc;
+  // initial build: buildSCF(node, parent) for every non-top node, bottom-up
+  for (size_t a = 0; a < nd.size(); ++a)
+    if (!nd[a].top() && (rc = run_stages(c, P.scf_up_b[a], P.scf_up_e[a])) != QT_OK) return rc;
+  int64_t nritz = 0;
+  std::vector<cd> hS, hR, hR2, hh;
+  for (int it = 0; it < n_iter; ++it) {
+    for (size_t i = 0; i < order.size(); ++i) {
+      const int a = order[i];
+      const qt::NodeGeo& g = nd[a];
+      const int64_t N = g.N;
+      cd* pa = psi + g.aoff;
+      int size = (int)std::min<int64_t>(n_krylov, N);
+      // Lanczos on the effective Hamiltonian (solveKrylovSpace)
+      std::vector<double> al, be;
+      cd s;
+      if ((rc = dot(pa, pa, N, s)) != QT_OK) return rc;
+      if (!(s.x > 0.0) || !std::isfinite(s.x)) return fail(c, QT_ERR_NUMERIC, "qt_scf: zero or non-finite node tensor");
+      if ((rc = lincomb(V(0), {{pa, cmk(1.0 / std::sqrt(s.x), 0)}}, N)) != QT_OK) return rc;
+      for (int l = 0; l < size; ++l) {
+        QT_CUDA(c, cudaMemcpyAsync(kin, V(l), N * sizeof(cd), cudaMemcpyDeviceToDevice, c->stream));
+        if ((rc = run_stages(c, P.scf_apply_b[a], P.scf_apply_e[a])) != QT_OK) return rc;
+        if ((rc = dot(V(l), kout, N, s)) != QT_OK) return rc;
+        if (!std::isfinite(s.x)) return fail(c, QT_ERR_NUMERIC, "qt_scf: non-finite <v|H|v>");
+        al.push_back(s.x);
+        if (l + 1 == size) break;
+        if (l == 0)
+          rc = lincomb(W, {{kout, cmk(1, 0)}, {V(0), cmk(-al[0], 0)}}, N);
+        else
+          rc = lincomb(W, {{kout, cmk(1, 0)}, {V(l), cmk(-al[l], 0)}, {V(l - 1), cmk(-be[l - 1], 0)}}, N);
+        if (rc != QT_OK) return rc;
+        if ((rc = dot(W, W, N, s)) != QT_OK) return rc;
+        const double nrm = std::sqrt(std::max(s.x, 0.0));
+        if (!std::isfinite(nrm)) return fail(c, QT_ERR_NUMERIC, "qt_scf: non-finite Lanczos residual");
+        // an invariant subspace: the residual is rounding noise (the reference
+        // divides by it); the Lanczos space ends here
+        double scale = 0.0;
+        for (double x : al) scale = std::max(scale, std::fabs(x));
+        for (double x : be) scale = std::max(scale, x);
+        if (nrm <= kLanczosBreakdown * scale) {
+          size = l + 1;
+          break;
+        }
+        be.push_back(nrm);
+        if ((rc = lincomb(V(l + 1), {{W, cmk(1.0 / nrm, 0)}}, N)) != QT_OK) return rc;
+      }
+      std::vector<double> E, U;
+      tridiag_eigh(al, be, size, E, U);
+      if (ritz) ritz[nritz] = E[0];
+      ++nritz;
+      // imaginaryTimePropagation (the k = 0 term enters twice, SCF.cpp:208-214) or the Ritz vector
+      qt::LinComb lc;
+      lc.count = size;
+      for (int l = 0; l < size; ++l) {
+        lc.v[l] = V(l);
+        double cl;
+        if (it < n_itp) {
+          cl = U[l] * U[0];
+          for (int k = 0; k < size; ++k) cl += U[l + size * k] * std::exp(-beta * (E[k] - E[0])) * U[size * k];
+        } else {
+          cl = U[l];
+        }
+        lc.c[l] = cmk(cl, 0);
+      }
+      {
+        cudaError_t e = qt::launch_lincomb(Y, lc, N, c->stream);
+        if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf lincomb");
+        c->launches += 1;
+      }
+      if (it < n_itp) {
+        if ((rc = dot(Y, Y, N, s)) != QT_OK) return rc;
+        if ((rc = lincomb(Y, {{Y, cmk(1.0 / std::sqrt(s.x), 0)}}, N)) != QT_OK) return rc;
+      }
+      // isometrize toward the next node: Cholesky-QR twice, Householder when
+      // the Gram matrix is near singular
+      const int nxt = i + 1 < order.size() ? order[i + 1] : -1;
+      int out_idx = g.last();
+      for (size_t k = 0; k < g.children.size(); ++k)
+        if (g.children[k] == nxt) out_idx = (int)k;
+      const int d = g.shape[out_idx];
+      bool chol_ok = true;
+      const cd* src = Y;
+      for (int pass = 0; pass < 2 && chol_ok; ++pass) {
+        if ((rc = hole(src, src, g, out_idx, dS)) != QT_OK) return rc;
+        hS.resize((size_t)d * d);
+        QT_CUDA(c, cudaMemcpyAsync(hS.data(), dS, (size_t)d * d * sizeof(cd), cudaMemcpyDeviceToHost, c->stream));
+        QT_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (!cholesky_upper(hS, d, hR, 1e-6)) {
+          chol_ok = false;
+          break;
+        }
+        inv_upper_transposed(hR, d, hh);
+        QT_CUDA(c, cudaMemcpyAsync(dH, hh.data(), (size_t)d * d * sizeof(cd), cudaMemcpyHostToDevice, c->stream));
+        if ((rc = mode_product(dH, src, pass == 0 ? T : pa, g, out_idx)) != QT_OK) return rc;
+        src = T;
+      }
+      if (!chol_ok) {
+        const int64_t bef = g.before(out_idx), aft = g.after(out_idx), m = bef * aft;
+        if (m < d) return fail(c, QT_ERR_SHAPE, "qt_scf: node dimension below its bond");
+        std::vector<cd> hy(N), M((size_t)m * d);
+        QT_CUDA(c, cudaMemcpyAsync(hy.data(), Y, N * sizeof(cd), cudaMemcpyDeviceToHost, c->stream));
+        QT_CUDA(c, cudaStreamSynchronize(c->stream));
+        for (int64_t af = 0; af < aft; ++af)  // toMatrix(Y, mode): row = bef + aft * before
+          for (int x = 0; x < d; ++x)
+            for (int64_t bf = 0; bf < bef; ++bf) M[(size_t)x * m + bf + af * bef] = hy[bf + bef * (x + (int64_t)d * af)];
+        householder_thin_q(M, m, d);
+        for (int64_t af = 0; af < aft; ++af)
+          for (int x = 0; x < d; ++x)
+            for (int64_t bf = 0; bf < bef; ++bf) hy[bf + bef * (x + (int64_t)d * af)] = M[(size_t)x * m + bf + af * bef];
+        QT_CUDA(c, cudaMemcpyAsync(pa, hy.data(), N * sizeof(cd), cudaMemcpyHostToDevice, c->stream));
+        QT_CUDA(c, cudaStreamSynchronize(c->stream));
+      }
+      if (nxt < 0) break;
+      // r = <Q|Y> over out_idx, multiplied into the next node; rebuild toward it
+      if ((rc = hole(pa, Y, g, out_idx, dR)) != QT_OK) return rc;
+      const qt::NodeGeo& gn = nd[nxt];
+      int in_idx = gn.last();
+      for (size_t k = 0; k < gn.children.size(); ++k)
+        if (gn.children[k] == a) in_idx = (int)k;
+      cd* pn = psi + gn.aoff;
+      if ((rc = mode_product(dR, pn, T, gn, in_idx)) != QT_OK) return rc;
+      QT_CUDA(c, cudaMemcpyAsync(pn, T, gn.N * sizeof(cd), cudaMemcpyDeviceToDevice, c->stream));
+      const bool up = !g.top() && g.parent == nxt;
+      if (up)
+        rc = run_stages(c, P.scf_up_b[a], P.scf_up_e[a]);
+      else
+        rc = run_stages(c, P.scf_down_b[nxt], P.scf_down_e[nxt]);
+      if (rc != QT_OK) return rc;
+    }
+  }
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (ritz_count) *ritz_count = nritz;
+  c->swept = false;
+  c->built = false;
+  return QT_OK;
+}

@@ -335,6 +335,15 @@ int64_t static_eig_capacity();
 cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n_mats, int d,
                                       double eps, cudaStream_t s);
 // out = x + a * y on n complex128 numbers (x may alias out)
+// SCF Krylov helpers (complex128): out[0] = sum conj(a) b; out = sum_t c_t v_t
+constexpr int kLinCombMax = 32;
+struct LinComb {
+  const double2* v[kLinCombMax];
+  double2 c[kLinCombMax];
+  int count;
+};
+cudaError_t launch_dot(const double2* a, const double2* b, int64_t n, double2* out, cudaStream_t s);
+cudaError_t launch_lincomb(double2* out, const LinComb& lc, int64_t n, cudaStream_t s);
 cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2* y, int64_t n,
                         cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it

@@ -868,6 +868,54 @@ __global__ void __launch_bounds__(kThreads) k_axpy(double2* out, const double2* 
 }
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Krylov vector helpers of the SCF sweep (complex128).
+// k_dot: out = sum_i conj(a_i) b_i in one block; every thread sums a fixed
+// strided subset in order, then a fixed-order tree in shared memory, so the
+// result is reproducible run to run.
+// k_lincomb: out_i = sum_t c_t v_t,i over up to kLinCombMax vectors.
+// ---------------------------------------------------------------------------
+constexpr int kDotThreads = 512;
+
+__global__ void __launch_bounds__(kDotThreads) k_dot(const double2* __restrict__ a,
+                                                     const double2* __restrict__ b, int64_t n,
+                                                     double2* __restrict__ out) {
+  __shared__ double2 red[kDotThreads];
+  double2 acc = cz();
+  for (int64_t i = threadIdx.x; i < n; i += kDotThreads) cfmac(acc, a[i], b[i]);
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[0] = red[0];
+}
+
+__global__ void __launch_bounds__(kThreads) k_lincomb(double2* __restrict__ out, LinComb lc, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+    double2 acc = cz();
+    for (int t = 0; t < lc.count; ++t) cfma(acc, lc.c[t], lc.v[t][i]);
+    out[i] = acc;
+  }
+}
+
+cudaError_t launch_dot(const double2* a, const double2* b, int64_t n, double2* out, cudaStream_t s) {
+  (void)cudaGetLastError();
+  k_dot<<<1, kDotThreads, 0, s>>>(a, b, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lincomb(double2* out, const LinComb& lc, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  if (lc.count < 0 || lc.count > kLinCombMax) return cudaErrorInvalidValue;
+  const int64_t want = (n + kThreads - 1) / kThreads;
+  const int blocks = (int)std::min<int64_t>(want, 152 * 8);
+  (void)cudaGetLastError();
+  k_lincomb<<<blocks, kThreads, 0, s>>>(out, lc, n);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2* y, int64_t n,
                         cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

@@ -29,6 +29,7 @@ QT_PLAN_COMPRESSED = 2
 QT_PREC_F64 = 0x000
 QT_PREC_DF64 = 0x100
 QT_PLAN_GRADIENT = 0x1000
+QT_PLAN_SCF = 0x2000
 QT_MAT_RHO, QT_MAT_RHOINV, QT_MAT_HMAT, QT_MAT_HCON = 0, 1, 2, 3
 ERRORS = {1: "QT_ERR_ARG", 2: "QT_ERR_SHAPE", 3: "QT_ERR_ALLOC", 4: "QT_ERR_CUDA",
           5: "QT_ERR_STATE", 6: "QT_ERR_NUMERIC"}
@@ -109,6 +110,8 @@ def load(build_if_missing: bool = True):
                               ctypes.c_double], ctypes.c_int),
         "qt_psi_load": ([_vp, ctypes.c_char_p], ctypes.c_int),
         "qt_energies": ([_vp, _vp, ctypes.c_int], ctypes.c_int),
+        "qt_scf": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp, ctypes.c_int64,
+                    ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -130,7 +133,7 @@ def exported_symbols():
         "qt_memcpy_h2d", "qt_memcpy_d2h", "qt_launch_count", "qt_stage_count",
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
         "qt_tree_count", "qt_energies", "qt_gradient_download", "qt_psi_save", "qt_psi_load",
-        "qt_build", "qt_layer_derivatives", "qt_cmf_propagate",
+        "qt_build", "qt_layer_derivatives", "qt_cmf_propagate", "qt_scf",
     ]
 
 
@@ -269,6 +272,18 @@ class HamiltonianRepresentation:
         """Fixed-step constant-mean-field propagation of the device wavefunction."""
         self.ctx.check(self.ctx.L.qt_cmf_propagate(self.ctx.h, dt, n_steps, n_sub,
                                                    complex(phase).real, complex(phase).imag))
+
+    def scf(self, n_iter: int = 1, n_krylov: int = 5, n_itp: int = 0, beta: float = 1.0) -> np.ndarray:
+        """QuTree's SCF / Krylov sweep on the device wavefunction (plans with
+        QT_PLAN_COMPRESSED | QT_PLAN_SCF); returns the lowest Ritz value of every
+        Krylov solve.  The optimised wavefunction stays on the device (psi())."""
+        n_nodes = len(self.tree.nodes)
+        cap = max(1, n_iter * (2 * n_nodes - 1))
+        out = np.zeros(cap, dtype=np.float64)
+        cnt = ctypes.c_int64(0)
+        self.ctx.check(self.ctx.L.qt_scf(self.ctx.h, n_iter, n_krylov, n_itp, beta, _ptr(out), cap,
+                                         ctypes.byref(cnt)))
+        return out[:cnt.value].copy()
 
     def psi(self) -> np.ndarray:
         out = np.zeros(self.n_psi, dtype=np.complex128)
