@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--batch-trees", type=int, default=512,
                     help="trees in the supplementary many-tree batch (0: skip)")
+    ap.add_argument("--no-scf", action="store_true", help="skip the supplementary SCF sweep timing")
     return ap.parse_args()
 
 
@@ -357,6 +358,38 @@ def run_ours(args, ws, rank, local):
                 batch["energies_first4"] = hb.energies()[:4].tolist()
             hb.close()
 
+    # supplementary: QuTree's SCF / Krylov sweep (qt_scf), one sweep of 5 Krylov
+    # vectors per node; the oracle's numpy restatement timed on the 16-mode tree
+    scf = None
+    if not args.no_scf and rank == 0:
+        scf = {"sweep": "one SCF iteration: every node in depth-first order with returns, "
+                        "5 Lanczos vectors of the tail-free effective Hamiltonian, Ritz vector, "
+                        "isometrisation toward the next node, edge-local rebuild"}
+        for cfg in (1, 4):
+            t_s, s_s, p_s = config_problem(cfg)
+            hs = qtgpu.HamiltonianRepresentation(s_s, t_s, flavour=qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PLAN_SCF,
+                                                 device=local)
+            hs.upload(p_s.flat())
+            hs.scf(n_iter=1, n_krylov=5)  # warm-up
+            hs.upload(p_s.flat())
+            n0 = hs.ctx.launch_count()
+            t0 = time.perf_counter()
+            E = hs.scf(n_iter=1, n_krylov=5)
+            dt = time.perf_counter() - t0
+            scf[f"cfg{cfg}"] = {"ms_per_scf_sweep": 1e3 * dt, "krylov_solves": len(E),
+                                "krylov_solves_per_s": len(E) / dt, "final_ritz": float(E[-1]),
+                                "gpu_launches": hs.ctx.launch_count() - n0}
+            hs.close()
+            if cfg == 4 and not args.no_cpu_baseline:
+                sys.path.insert(0, os.path.join(ROOT, "oracle"))
+                import scf as scf_oracle
+                t0 = time.perf_counter()
+                E_cpu, _ = scf_oracle.scf(t_s, s_s, p_s.tensors, n_iter=1, n_krylov=5)
+                dt_cpu = time.perf_counter() - t0
+                scf["cfg4"]["cpu_oracle"] = {"ms_per_scf_sweep": 1e3 * dt_cpu, "kind": "port", "cores": 1,
+                                             "sample": "one SCF iteration of the 16-mode tree, numpy",
+                                             "max_abs_ritz_diff": float(np.abs(E_cpu - E).max())}
+
     if rank != 0:
         return
     line = {
@@ -393,6 +426,8 @@ def run_ours(args, ws, rank, local):
         line["e2e"] = e2e
     if batch:
         line["batched_forest"] = batch
+    if scf:
+        line["scf"] = scf
     if not args.no_cpu_baseline and args.config == 1:
         dt, cpu_e, blas = cpu_baseline_sweep(tree, sop, psi)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count(),

@@ -1251,8 +1251,9 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
     for (int x : g.shape) maxd = std::max(maxd, x);
   }
   const int64_t vstride = (maxN + 15) / 16 * 16, mstride = (int64_t)maxd * maxd;
-  // vectors V_0..V_{K-1}, W, Y, T; matrices S, H, R; one scalar
-  const int64_t total = (n_krylov + 3) * vstride + 3 * mstride + 16;
+  // vectors V_0..V_{K-1}, W, Y, T; matrices S, H, R; dot scratch; hole-product partial tiles
+  const int64_t ws_elems = 64 * mstride;
+  const int64_t total = (n_krylov + 3) * vstride + 3 * mstride + 512 + ws_elems;
   DevFree work;
   {
     cudaError_t e = cudaMalloc(&work.p, total * sizeof(cd));
@@ -1267,6 +1268,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
   cd* dH = dS + mstride;
   cd* dR = dH + mstride;
   cd* dscal = dR + mstride;
+  cd* hpws = dscal + 512;
   cd* psi = c->buf[qt::B_PSI];
   cd* kin = c->buf[qt::B_KRY] + P.kry_in;
   cd* kout = c->buf[qt::B_KRY] + P.kry_out;
@@ -1275,7 +1277,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
     if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf dot");
     QT_CUDA(c, cudaMemcpyAsync(&out, dscal, sizeof(cd), cudaMemcpyDeviceToHost, c->stream));
     QT_CUDA(c, cudaStreamSynchronize(c->stream));
-    c->launches += 1;
+    c->launches += 2;
     return QT_OK;
   };
   auto lincomb = [&](cd* out, std::initializer_list<std::pair<const cd*, cd>> terms, int64_t n) -> int {
@@ -1304,7 +1306,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
     t.kchunk = 0;
     t.ws = 0;
     t.rows = t.cols = 4;
-    cudaError_t e = qt::launch_single_hp(t, c->stream, nullptr);
+    cudaError_t e = qt::launch_hp_split(t, hpws, ws_elems, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf hole product");
     c->launches += 1;
     return QT_OK;

@@ -335,7 +335,28 @@ int64_t static_eig_capacity();
 cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n_mats, int d,
                                       double eps, cudaStream_t s);
 // out = x + a * y on n complex128 numbers (x may alias out)
-// SCF Krylov helpers (complex128): out[0] = sum conj(a) b; out = sum_t c_t v_t
+// Outputs per thread (rows x cols, 1..4 each) of a hole-product tile of m x m
+// (m <= 64): the fewest whose thread grid ceil(m/rows) x ceil(m/cols) fits
+// 256 threads and 64 staged columns.
+inline void hp_shape(int m, int* rows, int* cols) {
+  int best = 1 << 30;
+  *rows = *cols = 4;
+  for (int r = 1; r <= 4; ++r)
+    for (int c = 1; c <= 4; ++c) {
+      const int tr = (m + r - 1) / r, tc = (m + c - 1) / c;
+      if (tr * tc > 256 || tr * r > 64 || tc * c > 64) continue;
+      if (r * c < best) {
+        best = r * c;
+        *rows = r;
+        *cols = c;
+      }
+    }
+}
+// One complex128 hole product split over its reduction index (partial tiles
+// in ws, at most ws_elems elements); S written in full.
+cudaError_t launch_hp_split(const HPTask& task, double2* ws, int64_t ws_elems, cudaStream_t s);
+// SCF Krylov helpers (complex128): out[0] = sum conj(a) b (out needs 257
+// elements of workspace); out = sum_t c_t v_t
 constexpr int kLinCombMax = 32;
 struct LinComb {
   const double2* v[kLinCombMax];

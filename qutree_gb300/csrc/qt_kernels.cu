@@ -232,16 +232,13 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
+// one block: output tile tl.y, reduction range tl.z of task t
 template <class P, int R, int C>
-__global__ void __launch_bounds__(kThreads, R * C > 9 ? 2 : 3)
-    k_hp(const HPTask* __restrict__ tasks, const int4* __restrict__ tiles, int64_t tile0,
-         typename P::S* __restrict__ ws) {
+__device__ __forceinline__ void hp_split_tile(const HPTask& t, const int4 tl, typename P::S* __restrict__ ws) {
   typedef typename P::S S;
   typedef typename P::A A;
   extern __shared__ __align__(16) unsigned char hp_smem[];
   S* sm = reinterpret_cast<S*>(hp_smem);  // [buffer][A rows | B rows][kHpRows][kHpTile]
-  const int4 tl = tiles[tile0 + blockIdx.x];
-  const HPTask t = tasks[tl.x];
   const int aA = t.a, aB = t.aB > 0 ? t.aB : t.a;
   const int nti = (aA + kHpTile - 1) / kHpTile;
   const int ti0 = (tl.y % nti) * kHpTile, tj0 = (tl.y / nti) * kHpTile;
@@ -336,6 +333,36 @@ __global__ void __launch_bounds__(kThreads, R * C > 9 ? 2 : 3)
           ws[t.ws + (int64_t)tl.z * nS + o] = P::fin(acc[r][c]);
       }
     }
+}
+
+template <class P, int R, int C>
+__global__ void __launch_bounds__(kThreads, R * C > 9 ? 2 : 3)
+    k_hp(const HPTask* __restrict__ tasks, const int4* __restrict__ tiles, int64_t tile0,
+         typename P::S* __restrict__ ws) {
+  const int4 tl = tiles[tile0 + blockIdx.x];
+  const HPTask t = tasks[tl.x];
+  hp_split_tile<P, R, C>(t, tl, ws);
+}
+
+// one task passed by value: block b covers output tile b % ntiles, range b / ntiles
+template <class P, int R, int C>
+__global__ void __launch_bounds__(kThreads, R * C > 9 ? 2 : 3)
+    k_hp_one(HPTask t, int ntiles, typename P::S* __restrict__ ws) {
+  hp_split_tile<P, R, C>(t, make_int4(0, (int)(blockIdx.x % ntiles), (int)(blockIdx.x / ntiles), 0), ws);
+}
+
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_hp_sum_one(HPTask t, const typename P::S* __restrict__ ws) {
+  typedef typename P::S S;
+  typedef typename P::A A;
+  const int aB = t.aB > 0 ? t.aB : t.a;
+  const int64_t n = (int64_t)t.a * aB;
+  S* Sp = reinterpret_cast<S*>(t.S);
+  for (int64_t e = (int64_t)blockIdx.x * kThreads + threadIdx.x; e < n; e += (int64_t)gridDim.x * kThreads) {
+    A acc = P::zero();
+    for (int z = 0; z < t.splits; ++z) P::add(acc, ws[t.ws + z * n + e]);
+    Sp[e] = P::fin(acc);
+  }
 }
 
 // S = sum over the k ranges of the partial tiles (one block per task)
@@ -876,13 +903,19 @@ __global__ void __launch_bounds__(kThreads) k_axpy(double2* out, const double2* 
 // k_lincomb: out_i = sum_t c_t v_t,i over up to kLinCombMax vectors.
 // ---------------------------------------------------------------------------
 constexpr int kDotThreads = 512;
+constexpr int64_t kDotParts = 256;
 
 __global__ void __launch_bounds__(kDotThreads) k_dot(const double2* __restrict__ a,
                                                      const double2* __restrict__ b, int64_t n,
                                                      double2* __restrict__ out) {
   __shared__ double2 red[kDotThreads];
   double2 acc = cz();
-  for (int64_t i = threadIdx.x; i < n; i += kDotThreads) cfmac(acc, a[i], b[i]);
+  for (int64_t i = threadIdx.x; i < n; i += kDotThreads) {
+    if (b)
+      cfmac(acc, a[i], b[i]);
+    else
+      acc = cadd(acc, a[i]);
+  }
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int w = kDotThreads / 2; w > 0; w >>= 1) {
@@ -900,9 +933,60 @@ __global__ void __launch_bounds__(kThreads) k_lincomb(double2* __restrict__ out,
   }
 }
 
+// first pass: block b sums its contiguous slice in a fixed order
+__global__ void __launch_bounds__(kDotThreads) k_dot_part(const double2* __restrict__ a,
+                                                          const double2* __restrict__ b, int64_t n,
+                                                          int64_t slice, double2* __restrict__ part) {
+  __shared__ double2 red[kDotThreads];
+  const int64_t lo = (int64_t)blockIdx.x * slice, hi = min(n, lo + slice);
+  double2 acc = cz();
+  for (int64_t i = lo + threadIdx.x; i < hi; i += kDotThreads) cfmac(acc, a[i], b[i]);
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = kDotThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] = cadd(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
 cudaError_t launch_dot(const double2* a, const double2* b, int64_t n, double2* out, cudaStream_t s) {
   (void)cudaGetLastError();
-  k_dot<<<1, kDotThreads, 0, s>>>(a, b, n, out);
+  // slices of >= 8192 elements, at most kDotParts of them; the partial sums
+  // go to out[1 ..] and are added in order by one block into out[0]
+  int64_t parts = std::min<int64_t>(kDotParts, std::max<int64_t>(1, (n + 8191) / 8192));
+  const int64_t slice = (n + parts - 1) / parts;
+  parts = std::max<int64_t>(1, (n + slice - 1) / slice);
+  k_dot_part<<<(unsigned)parts, kDotThreads, 0, s>>>(a, b, n, slice, out + 1);
+  k_dot<<<1, kDotThreads, 0, s>>>(out + 1, nullptr, parts, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hp_one_shape(const HPTask& t, int ntiles, double2* ws, cudaStream_t s);
+
+cudaError_t launch_hp_split(const HPTask& task, double2* ws, int64_t ws_elems, cudaStream_t s) {
+  HPTask t = task;
+  const int aB = t.aB > 0 ? t.aB : t.a;
+  if (t.a > kHpMaxDim || aB > kHpMaxDim || t.a < 1 || aB < 1) return cudaErrorInvalidValue;
+  hp_shape(std::min(std::max(t.a, aB), kHpTile), &t.rows, &t.cols);
+  const int ntiles = ((t.a + kHpTile - 1) / kHpTile) * ((aB + kHpTile - 1) / kHpTile);
+  const int64_t K = (int64_t)t.before * t.after;
+  int64_t kc = std::max<int64_t>(256, (K * ntiles + 4 * 152 - 1) / (4 * 152));
+  kc = (kc + kHpRows - 1) / kHpRows * kHpRows;
+  int64_t splits = (K + kc - 1) / kc;
+  const int64_t per = (int64_t)t.a * aB;
+  if (splits > 1 && splits * per > ws_elems) {  // fewer, longer ranges to fit the workspace
+    splits = std::max<int64_t>(1, ws_elems / per);
+    kc = (K + splits - 1) / splits;
+    splits = (K + kc - 1) / kc;
+  }
+  t.splits = (int)splits;
+  t.kchunk = (int)std::min<int64_t>(K, kc);
+  t.ws = 0;
+  (void)cudaGetLastError();
+  cudaError_t e = launch_hp_one_shape(t, ntiles, ws, s);
+  if (e != cudaSuccess) return e;
+  if (t.splits > 1) k_hp_sum_one<F64><<<(unsigned)std::min<int64_t>(64, (per + kThreads - 1) / kThreads), kThreads, 0, s>>>(t, ws);
   return cudaGetLastError();
 }
 
@@ -980,6 +1064,29 @@ cudaError_t launch_hp_shape(int rows, int cols, const HPTask* tasks, const int4*
     case 3 * 8 + 3: return launch_hp_rc<P, 3, 3>(tasks, tiles, first, n, ws, s);
     case 3 * 8 + 4: return launch_hp_rc<P, 3, 4>(tasks, tiles, first, n, ws, s);
     case 4 * 8 + 4: return launch_hp_rc<P, 4, 4>(tasks, tiles, first, n, ws, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int R, int C>
+cudaError_t launch_hp_one_rc(const HPTask& t, int ntiles, double2* ws, cudaStream_t s) {
+  cudaError_t e = cudaFuncSetAttribute(k_hp_one<F64, R, C>, cudaFuncAttributeMaxDynamicSharedMemorySize, kHpSmem);
+  if (e != cudaSuccess) return e;
+  k_hp_one<F64, R, C><<<(unsigned)((int64_t)ntiles * t.splits), kThreads, kHpSmem, s>>>(t, ntiles, ws);
+  return cudaSuccess;
+}
+
+cudaError_t launch_hp_one_shape(const HPTask& t, int ntiles, double2* ws, cudaStream_t s) {
+  switch (t.rows * 8 + t.cols) {
+    case 1 * 8 + 1: return launch_hp_one_rc<1, 1>(t, ntiles, ws, s);
+    case 1 * 8 + 2: return launch_hp_one_rc<1, 2>(t, ntiles, ws, s);
+    case 1 * 8 + 3: return launch_hp_one_rc<1, 3>(t, ntiles, ws, s);
+    case 1 * 8 + 4: return launch_hp_one_rc<1, 4>(t, ntiles, ws, s);
+    case 2 * 8 + 3: return launch_hp_one_rc<2, 3>(t, ntiles, ws, s);
+    case 2 * 8 + 4: return launch_hp_one_rc<2, 4>(t, ntiles, ws, s);
+    case 3 * 8 + 3: return launch_hp_one_rc<3, 3>(t, ntiles, ws, s);
+    case 3 * 8 + 4: return launch_hp_one_rc<3, 4>(t, ntiles, ws, s);
+    case 4 * 8 + 4: return launch_hp_one_rc<4, 4>(t, ntiles, ws, s);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -465,18 +465,7 @@ class Builder {
       Plan::SHP& h = P.hp[t];
       // outputs per thread: the fewest (rows x cols) whose thread grid
       // ceil(m/rows) x ceil(m/cols) fits 256 threads and 64 staged columns
-      const int m = std::min(h.a, kTile);
-      int best = 1 << 30;
-      for (int r = 1; r <= 4; ++r)
-        for (int c = 1; c <= 4; ++c) {
-          const int tr = (m + r - 1) / r, tc = (m + c - 1) / c;
-          if (tr * tc > 256 || tr * r > kTile || tc * c > kTile) continue;
-          if (r * c < best) {
-            best = r * c;
-            h.rows = r;
-            h.cols = c;
-          }
-        }
+      hp_shape(std::min(h.a, kTile), &h.rows, &h.cols);
       const int64_t K = (int64_t)h.before * h.after;
       h.splits = (int)((K + kc - 1) / kc);
       h.kchunk = (int)std::min<int64_t>(K, kc);
