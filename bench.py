@@ -46,6 +46,9 @@ def parse():
     ap.add_argument("--batch-trees", type=int, default=512,
                     help="trees in the supplementary many-tree batch (0: skip)")
     ap.add_argument("--no-scf", action="store_true", help="skip the supplementary SCF sweep timing")
+    ap.add_argument("--precision-steps", type=int, default=0,
+                    help="CMF steps (dt 0.01) of the double-float vs complex128 study on the "
+                         "48..96-bond 64-mode tree (0: skip)")
     return ap.parse_args()
 
 
@@ -390,6 +393,43 @@ def run_ours(args, ws, rank, local):
                                              "sample": "one SCF iteration of the 16-mode tree, numpy",
                                              "max_abs_ritz_diff": float(np.abs(E_cpu - E).max())}
 
+    # optional: double-float against complex128 along a constant-mean-field
+    # propagation of the 48..96-bond tree (regularisation 1e-8, dt 0.01)
+    precision = None
+    if args.precision_steps > 0 and rank == 0:
+        t3, s3, p3 = config_problem(3)
+        hf = qtgpu.HamiltonianRepresentation(s3, t3, flavour=qtgpu.QT_PLAN_COMPRESSED, eps=1e-8, device=local)
+        hd = qtgpu.HamiltonianRepresentation(s3, t3, flavour=qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64,
+                                             eps=1e-8, device=local)
+        for hh in (hf, hd):
+            hh.upload(p3.flat())
+        rows, worst = [], {"abs_dE": 0.0, "dpsi_rel_rho_weighted": 0.0, "psi_rel": 0.0}
+        every = max(1, args.precision_steps // 10)
+        t0 = time.perf_counter()
+        for step in range(args.precision_steps + 1):
+            if step > 0:
+                hf.cmf(0.01, 1)
+                hd.cmf(0.01, 1)
+            if step % every and step != args.precision_steps:
+                continue
+            pf, pd = hf.psi(), hd.psi()
+            hf.derivative()
+            hd.derivative()
+            ef, ed = hf.energy(), hd.energy()
+            rho = hf.matrices(qtgpu.QT_MAT_RHO)
+            r = {"step": step, "energy": ef, "abs_dE": abs(ed - ef),
+                 "dpsi_rel_rho_weighted": _rho_weighted_err(t3, hd.dpsi(), hf.dpsi(), rho),
+                 "psi_rel": float(np.linalg.norm(pd - pf) / np.linalg.norm(pf))}
+            rows.append(r)
+            for k in worst:
+                worst[k] = max(worst[k], r[k])
+        precision = {"workload": "64 modes, p=32, bonds 32,58,67,77,86,96, 384 terms, regularisation 1e-8",
+                     "propagation": f"{args.precision_steps} constant-mean-field steps, dt = 0.01, "
+                                    "complex128 and double-float contexts in lockstep from the same Psi",
+                     "worst": worst, "trajectory": rows, "wall_s": time.perf_counter() - t0}
+        hf.close()
+        hd.close()
+
     if rank != 0:
         return
     line = {
@@ -428,6 +468,8 @@ def run_ours(args, ws, rank, local):
         line["batched_forest"] = batch
     if scf:
         line["scf"] = scf
+    if precision:
+        line["precision_study"] = precision
     if not args.no_cpu_baseline and args.config == 1:
         dt, cpu_e, blas = cpu_baseline_sweep(tree, sop, psi)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count(),
