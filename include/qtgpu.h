@@ -258,6 +258,12 @@ int qt_stage_launch(qt_ctx* ctx, int stage);
  * free FMA loop of the library's own; the roofline denominator of the
  * complex128 kernels. */
 int qt_probe_fp64_peak(qt_ctx* ctx, double* tflops);
+/* Ceiling of the double-float arithmetic (TFLOP/s, complex128-equivalent:
+ * 8 flops per complex multiply-add): the kernels' double-float complex
+ * multiply-add and renormalisation on register accumulators, no memory
+ * traffic; the roofline denominator of the QT_PREC_DF64 kernels.  No
+ * reference counterpart (diagnostic). */
+int qt_probe_df64_peak(qt_ctx* ctx, double* tflops);
 
 /* ---- primitives on device pointers ---------------------------------------
  * Mode-k product, the reference's matvec_ / matrixTensor

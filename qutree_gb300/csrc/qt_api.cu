@@ -997,6 +997,17 @@ int qt_rho_inverse_noalloc(qt_ctx* c, void* rhoinv, const void* rho, int n_mats,
   return QT_OK;
 }
 
+int qt_probe_df64_peak(qt_ctx* c, double* tflops) {
+  if (!c || !tflops) return fail(c, QT_ERR_ARG, "null argument");
+  QT_CUDA(c, cudaSetDevice(c->device));
+  double v = 0;
+  cudaError_t e = qt::probe_df64_peak(c->stream, &v);
+  if (e != cudaSuccess) return cuda_fail(c, e, "qt_probe_df64_peak");
+  c->launches += 2;
+  *tflops = v;
+  return QT_OK;
+}
+
 int qt_probe_fp64_peak(qt_ctx* c, double* tflops) {
   if (!c || !tflops) return fail(c, QT_ERR_ARG, "null argument");
   QT_CUDA(c, cudaSetDevice(c->device));

@@ -369,5 +369,6 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
                         cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
+cudaError_t probe_df64_peak(cudaStream_t s, double* tflops);
 
 }  // namespace qt

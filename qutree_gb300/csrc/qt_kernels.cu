@@ -874,6 +874,29 @@ __global__ void __launch_bounds__(kThreads) k_fp64_fma(double* out, int iters, d
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// The double-float complex multiply-add of the chain kernels (DF64::mac,
+// renormalised every second step) on eight register accumulators per thread:
+// the ceiling of double-float arithmetic on this GPU, no memory traffic.
+// Every product reads another accumulator (acc[i] += a * acc[i ^ 4]), so
+// nothing is loop-invariant; |a| = 1e-3 keeps the values finite.  One store
+// per thread, index < gridDim.x * blockDim.x.
+__global__ void __launch_bounds__(kThreads) k_df64_mac(float4* out, int iters, float4 a, float4 b) {
+  float4 acc[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) acc[i] = make_float4(threadIdx.x + i, 0.f, b.x * i, 0.f);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      DF64::mac(acc[i], a, acc[i ^ 4]);
+      if (it & 1) DF64::norm(acc[i]);
+    }
+  }
+  float4 s = acc[0];
+#pragma unroll
+  for (int i = 1; i < 8; ++i) s = DF64::plus(s, acc[i]);
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 inline int64_t eig_smem_bytes(int d) {
   const int m = d + (d & 1);
   const int np = m / 2;
@@ -1010,6 +1033,36 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
   const int blocks = (int)std::min<int64_t>(want, (int64_t)sms * 8);
   (void)cudaGetLastError();
   k_axpy<<<blocks, kThreads, 0, s>>>(out, x, a, y, n);
+  return cudaGetLastError();
+}
+
+cudaError_t probe_df64_peak(cudaStream_t s, double* tflops) {
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  const int blocks = sms * 8, iters = 2048;
+  float4* buf = nullptr;
+  e = cudaMallocAsync((void**)&buf, sizeof(float4) * blocks * kThreads, s);
+  if (e != cudaSuccess) return e;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const float4 a = make_float4(1e-3f, 1e-11f, 2e-4f, -1e-12f), b = make_float4(0.5f, 0.f, 0.f, 0.f);
+  k_df64_mac<<<blocks, kThreads, 0, s>>>(buf, iters, a, b);  // warm-up
+  cudaEventRecord(e0, s);
+  k_df64_mac<<<blocks, kThreads, 0, s>>>(buf, iters, a, b);
+  cudaEventRecord(e1, s);
+  e = cudaEventSynchronize(e1);
+  float ms = 0;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFreeAsync(buf, s);
+  cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return e;
+  // 8 flops (complex128-equivalent) per complex multiply-add
+  *tflops = 8.0 * 8.0 * iters * (double)blocks * kThreads / (ms * 1e-3) / 1e12;
   return cudaGetLastError();
 }
 

@@ -99,6 +99,7 @@ def load(build_if_missing: bool = True):
                            ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_stage_launch": ([_vp, ctypes.c_int], ctypes.c_int),
         "qt_probe_fp64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "qt_probe_df64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_rho_inverse_noalloc": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double],
                                    ctypes.c_int),
         "qt_tree_count": ([_vp], ctypes.c_int),
@@ -133,7 +134,7 @@ def exported_symbols():
         "qt_memcpy_h2d", "qt_memcpy_d2h", "qt_launch_count", "qt_stage_count",
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
         "qt_tree_count", "qt_energies", "qt_gradient_download", "qt_psi_save", "qt_psi_load",
-        "qt_build", "qt_layer_derivatives", "qt_cmf_propagate", "qt_scf",
+        "qt_build", "qt_layer_derivatives", "qt_cmf_propagate", "qt_scf", "qt_probe_df64_peak",
     ]
 
 
@@ -196,6 +197,11 @@ class Context:
     def fp64_peak(self) -> float:
         v = ctypes.c_double()
         self.check(self.L.qt_probe_fp64_peak(self.h, ctypes.byref(v)))
+        return v.value
+
+    def df64_peak(self) -> float:
+        v = ctypes.c_double()
+        self.check(self.L.qt_probe_df64_peak(self.h, ctypes.byref(v)))
         return v.value
 
     # -- primitives (device pointers) ------------------------------------
