@@ -428,6 +428,10 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.write_alpha = s.write_alpha;
     gtasks.push_back(t);
   }
+  std::vector<qt::MMTask> mmt;
+  for (auto& m : P.mm) mmt.push_back(qt::MMTask{mptr_of(c, m.out), m.d, m.first, m.count, m.trans_b});
+  std::vector<qt::MMTerm> mmterms;
+  for (auto& m : P.mm_terms) mmterms.push_back(qt::MMTerm{ptr_of(c, m.A), ptr_of(c, m.B)});
   std::vector<char> blob;
   std::vector<int64_t> offs;
   put(blob, offs, mp);
@@ -444,6 +448,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, cvt);
   put(blob, offs, P.cvt_tiles);
   put(blob, offs, gtasks);
+  put(blob, offs, mmt);
+  put(blob, offs, mmterms);
+  put(blob, offs, P.mm_tiles);
   {
     cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -470,6 +477,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.cvt = (qt::CvtTask*)(base + offs[11]);
   c->tables.cvt_tiles = (int2*)(base + offs[12]);
   c->tables.grad = (qt::GradTask*)(base + offs[13]);
+  c->tables.mm = (qt::MMTask*)(base + offs[14]);
+  c->tables.mm_terms = (qt::MMTerm*)(base + offs[15]);
+  c->tables.mm_tiles = (int2*)(base + offs[16]);
   for (auto& id : P.identities) {
     cudaError_t e = qt::launch_set_identity(c->buf[qt::B_MATS] + id.first, id.second, prec, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "set identity");
@@ -959,7 +969,10 @@ int qt_stage_info(const qt_ctx* c, int i, int* kind, int64_t* tiles, double* flo
   if (!c || !c->prepared || i < 0 || i >= (int)c->plan.main_end) return QT_ERR_ARG;
   const auto& st = c->plan.stages[i];
   if (kind) *kind = st.kind;
-  if (tiles) *tiles = st.kind == qt::ST_MP || st.kind == qt::ST_HP || st.kind == qt::ST_ACC ? st.n_tiles : st.n_tasks;
+  if (tiles)
+    *tiles = st.kind == qt::ST_MP || st.kind == qt::ST_HP || st.kind == qt::ST_ACC || st.kind == qt::ST_MM
+                 ? st.n_tiles
+                 : st.n_tasks;
   if (flops) *flops = st.flops;
   if (bytes) *bytes = st.bytes;
   return QT_OK;

@@ -68,6 +68,17 @@ struct LinTask {
   int d, first, count, pad;
 };
 
+// out = sum_t A_t op(B_t) for d x d matrices, op(B) = B^T when trans_b
+// (the small matrix products of the fused derivative).
+struct MMTerm {
+  const double2* A;
+  const double2* B;
+};
+struct MMTask {
+  double2* out;
+  int d, first, count, trans_b;
+};
+
 // Regularised inverse of a Hermitian d x d matrix via Jacobi eigensolver.
 struct EigTask {
   const double2* rho;
@@ -109,7 +120,7 @@ struct GradTask {
   int d, write_alpha;
 };
 
-enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD };
+enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD, ST_MM };
 
 struct Stage {
   int kind;
@@ -257,6 +268,16 @@ struct Plan {
     int d, write_alpha;
   };
   std::vector<SGrad> grad;
+  struct SMMTerm {
+    Ref A, B;
+  };
+  struct SMM {
+    Ref out;
+    int d, first, count, trans_b;
+  };
+  std::vector<SMM> mm;
+  std::vector<SMMTerm> mm_terms;
+  std::vector<int2> mm_tiles;  // (task, first output element), 256 outputs per tile
   bool want_grad = false;
   std::vector<Stage> stages;
   // stages [0, apply_begin) build the matrices (HamiltonianRepresentation::
@@ -320,6 +341,9 @@ struct DevTables {
   int2* cvt_tiles = nullptr;
   GradTask* grad = nullptr;
   void* hp_ws = nullptr;
+  MMTask* mm = nullptr;
+  MMTerm* mm_terms = nullptr;
+  int2* mm_tiles = nullptr;
   const int4* hp_segs = nullptr;  // host array: (rows, cols, first tile, tile count)
 };
 // prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe

@@ -476,6 +476,49 @@ __global__ void __launch_bounds__(kThreads) k_lin(const LinTask* __restrict__ ta
   }
 }
 
+// out(i, j) = sum_t sum_k A_t(i, k) op(B_t)(k, j), one output element per
+// thread, 256 per block (tiles of the task list).
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_mm(const MMTask* __restrict__ tasks, const MMTerm* __restrict__ terms,
+                                                 const int2* __restrict__ tiles, int64_t tile0) {
+  typedef typename P::S S;
+  const int2 tl = tiles[tile0 + blockIdx.x];
+  const MMTask t = tasks[tl.x];
+  const int d = t.d;
+  const int e = tl.y + threadIdx.x;
+  if (e >= d * d) return;
+  const int i = e % d, j = e / d;
+  // four independent accumulators over k mod 4 (instruction-level parallelism)
+  typename P::A acc[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
+  const int64_t bs = t.trans_b ? d : 1;  // B element (k, j): B[j + d k] or B[k + d j]
+  for (int s = 0; s < t.count; ++s) {
+    const MMTerm T = terms[t.first + s];
+    const S* A = reinterpret_cast<const S*>(T.A) + i;
+    const S* B = reinterpret_cast<const S*>(T.B) + (t.trans_b ? j : (int64_t)d * j);
+    int k = 0;
+    for (; k + 3 < d; k += 4) {
+      S a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = P::ld(A + (int64_t)d * (k + q));
+        b[q] = P::ld(B + bs * (k + q));
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) P::mac(acc[q], a[q], b[q]);
+      if (k & 4) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) P::norm(acc[q]);
+      }
+    }
+    for (; k < d; ++k) P::mac(acc[0], P::ld(A + (int64_t)d * k), P::ld(B + bs * k));
+#pragma unroll
+    for (int q = 0; q < 4; ++q) P::norm(acc[q]);
+  }
+#pragma unroll
+  for (int q = 1; q < 4; ++q) P::add(acc[0], P::fin(acc[q]));
+  reinterpret_cast<S*>(t.out)[e] = P::fin(acc[0]);
+}
+
 // Energy-gradient preparation: M3 = Eout - E rho per node, alpha = 1/S00.
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_grad(const GradTask* __restrict__ tasks, int64_t task0) {
@@ -1169,6 +1212,9 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       break;
     case ST_LIN:
       k_lin<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.lin, t.lin_terms, st.first_task);
+      break;
+    case ST_MM:
+      k_mm<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mm, t.mm_terms, t.mm_tiles, st.first_tile);
       break;
     case ST_EIG: {
       const int64_t sm = eig_smem_bytes(max_eig_d);

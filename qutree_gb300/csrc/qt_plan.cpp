@@ -106,8 +106,8 @@ class Builder {
       comp_represent();
       comp_meanfield();
       P.apply_begin = (int64_t)P.stages.size();
-      comp_apply();
-      stage_final();
+      comp_apply(true);
+      stage_final(true);
       P.main_end = (int64_t)P.stages.size();
       const double sweep_flops = P.stats.exec_flops;
       const PlanStats counts = P.stats;
@@ -188,6 +188,8 @@ class Builder {
         b += 16.0 * 6 * (double)P.proj[t].d * P.proj[t].d;
       } else if (kind == ST_CVT) {
         b += 32.0 * (double)P.cvt[t].n;
+      } else if (kind == ST_MM) {
+        b += 16.0 * (double)P.mm[t].d * P.mm[t].d * (2 * P.mm[t].count + 1);
       }
     }
     return b;
@@ -591,6 +593,21 @@ class Builder {
     for (auto& x : terms) P.stats.exec_flops += (x.H.buf < 0 ? 2.0 : 8.0 * t.d) * g.N;
   }
 
+  // out = sum_t A_t op(B_t), d x d (op = transpose when trans_b)
+  void add_mm(Ref out, int d, const std::vector<Plan::SMMTerm>& terms, bool trans_b) {
+    Plan::SMM t;
+    t.out = out;
+    t.d = d;
+    t.first = (int)P.mm_terms.size();
+    t.count = (int)terms.size();
+    t.trans_b = trans_b ? 1 : 0;
+    for (auto& x : terms) P.mm_terms.push_back(x);
+    const int task = (int)P.mm.size();
+    P.mm.push_back(t);
+    for (int e0 = 0; e0 < d * d; e0 += 256) P.mm_tiles.push_back(make_int2(task, e0));
+    P.stats.exec_flops += 8.0 * d * d * d * (double)terms.size();
+  }
+
   // Run a list of chains as one group (split into chunks by the scratch budget).
   void run_items(std::vector<Item>& items, const char* name, std::vector<char>* acc_started) {
     size_t i = 0;
@@ -830,7 +847,15 @@ class Builder {
     emit_stage(ST_ACC, t0, (int64_t)P.acc.size(), tile0, (int64_t)P.acc_tiles.size(), "apply-zero");
   }
 
-  void stage_final() {
+  // fused (compressed sweep only): H Phi of non-top nodes is never formed.
+  // With hphi(a) = Y(a) x_last rho_a + sum_u X(a,u) x_last C(a,u),
+  //   D_a = Phi_a^dag hphi_a = Block(a) rho_a^T + sum_u H(a,u) C(a,u)^T
+  // (a hole product on the last index commutes with last-index products), and
+  //   hphi_a x_last rhoinv_a = Y x_last (rhoinv rho) + sum_u X_u x_last (rhoinv C_u),
+  // so the derivative is one accumulation over the kept chain outputs.
+  std::vector<std::vector<int64_t>> fused_g;  // per node: rhoinv rho, then rhoinv C(a,u)
+
+  void stage_final(bool fused = false) {
     // overlaps S = Phi^dag Phi and D = Phi^dag (H Phi) of every node
     int64_t t0 = (int64_t)P.hp.size(), tile0 = (int64_t)P.hp_tiles.size();
     for (int a = 0; a < n; ++a) {
@@ -840,10 +865,33 @@ class Builder {
         add_hp(psi(a), psi(a), mat(P.stop_dev_off[k]), a, nd[a].last());
       } else {
         add_hp(psi(a), psi(a), mat(P.s_off[a]), a, nd[a].last());
-        add_hp(psi(a), hphi(a), mat(P.d_off[a]), a, nd[a].last());
+        if (!fused) add_hp(psi(a), hphi(a), mat(P.d_off[a]), a, nd[a].last());
       }
     }
     emit_stage(ST_HP, t0, (int64_t)P.hp.size(), tile0, (int64_t)P.hp_tiles.size(), "overlaps");
+    if (fused) {
+      fused_g.assign(n, {});
+      const int64_t m0 = (int64_t)P.mm.size(), mt0 = (int64_t)P.mm_tiles.size();
+      for (int a = 0; a < n; ++a) {
+        if (is_top(a)) continue;
+        const int d = nd[a].dup();
+        std::vector<Plan::SMMTerm> dt;
+        if (!internal[a].empty()) dt.push_back(Plan::SMMTerm{mat(block_slot[a]), mat(P.rho_off[a])});
+        for (auto& b : bk[a]) dt.push_back(Plan::SMMTerm{mat(b.hslot), mat(b.cslot)});
+        add_mm(mat(P.d_off[a]), d, dt, true);
+        if (!internal[a].empty()) {
+          fused_g[a].push_back(alloc_mat(d));
+          add_mm(mat(fused_g[a].back()), d, {Plan::SMMTerm{mat(P.rhoinv_off[a]), mat(P.rho_off[a])}}, false);
+        } else {
+          fused_g[a].push_back(-1);
+        }
+        for (auto& b : bk[a]) {
+          fused_g[a].push_back(alloc_mat(d));
+          add_mm(mat(fused_g[a].back()), d, {Plan::SMMTerm{mat(P.rhoinv_off[a]), mat(b.cslot)}}, false);
+        }
+      }
+      emit_stage(ST_MM, m0, (int64_t)P.mm.size(), mt0, (int64_t)P.mm_tiles.size(), "overlaps-fused");
+    }
     if (P.prec == 1) {
       std::vector<int64_t> src = P.s_off, dst = P.s64_off;
       src.insert(src.end(), P.d_off.begin(), P.d_off.end());
@@ -883,6 +931,11 @@ class Builder {
       std::vector<Plan::SAccTerm> terms;
       if (is_top(a)) {
         terms.push_back(Plan::SAccTerm{Ref{-1, 0}, hphi(a)});
+      } else if (fused) {
+        if (fused_g[a][0] >= 0) terms.push_back(Plan::SAccTerm{mat(fused_g[a][0]), Yref[a]});
+        for (size_t u = 0; u < bk[a].size(); ++u)
+          terms.push_back(Plan::SAccTerm{mat(fused_g[a][u + 1]), bk[a][u].X});
+        terms.push_back(Plan::SAccTerm{mat(P.m2_off[a]), psi(a)});
       } else {
         terms.push_back(Plan::SAccTerm{mat(P.rhoinv_off[a]), hphi(a)});
         terms.push_back(Plan::SAccTerm{mat(P.m2_off[a]), psi(a)});
@@ -1402,12 +1455,16 @@ class Builder {
     }
   }
 
-  void comp_apply() {
+  void comp_apply(bool fused = false) {
     std::vector<Job> jobs;
     std::vector<char> started(n, 0);
     for (int a = 0; a < n; ++a) {
       if (is_top(a)) {
         started[a] = internal[a].empty() ? 0 : 1;  // Y(top) is H Phi_top
+        continue;
+      }
+      if (fused) {  // the derivative accumulates the kept chains directly
+        started[a] = 1;
         continue;
       }
       if (internal[a].empty() && bk[a].empty()) continue;

@@ -184,6 +184,21 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
     case 21:
       v = {P.kry_in, P.kry_out, P.kry_size, P.scf ? 1 : 0};
       break;
+    case 22:  // matrix-product tasks: out ref, d, first, count, trans_b
+      for (auto& t : P.mm) {
+        put_ref(v, t.out);
+        v.push_back(t.d);
+        v.push_back(t.first);
+        v.push_back(t.count);
+        v.push_back(t.trans_b);
+      }
+      break;
+    case 23:
+      for (auto& t : P.mm_terms) {
+        put_ref(v, t.A);
+        put_ref(v, t.B);
+      }
+      break;
     case 19:
       for (auto& t : P.grad) {
         put_ref(v, t.eout);

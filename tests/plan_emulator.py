@@ -22,7 +22,7 @@ _i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
 B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY = range(14)
-ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD = range(8)
+ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD, ST_MM = range(9)
 
 
 def lib():
@@ -78,8 +78,8 @@ class PlanView:
         self.tree, self.sop = tree, sop
         self.tables = {}
         widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
-                  20: 6}
-        for what in list(range(14)) + [18, 19, 20, 21]:
+                  20: 6, 22: 6, 23: 4}
+        for what in list(range(14)) + [18, 19, 20, 21, 22, 23]:
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -204,6 +204,15 @@ class PlanView:
                     w, U = np.linalg.eigh(R)
                     f = 1.0 / (w + eps * np.exp(-w / eps))
                     view(ib, io, d * d)[:] = ((U * f) @ U.conj().T).ravel(order="F")
+                elif kind == ST_MM:
+                    ob, oo, d, first, count, trans = T[22][t]
+                    acc = np.zeros((d, d), np.complex128)
+                    for s_ in range(first, first + count):
+                        ab, ao, bb, bo = T[23][s_]
+                        A = view(ab, ao, d * d).reshape((d, d), order="F")
+                        B = view(bb, bo, d * d).reshape((d, d), order="F")
+                        acc += A @ (B.T if trans else B)
+                    view(ob, oo, d * d)[:] = acc.ravel(order="F")
                 elif kind == ST_CVT:
                     sb, so, db, do, n, _ = T[18][t]
                     view(db, do, n)[:] = view(sb, so, n)
