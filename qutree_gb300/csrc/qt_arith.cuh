@@ -57,6 +57,13 @@ struct F64 {
   static __device__ __forceinline__ S mul(const S& a, const S& b) { return cmul64(a, b); }
   static __device__ __forceinline__ void cmac(A& acc, const C& c, const S& b) { cfma64(acc, c, b); }
   static __device__ __forceinline__ void norm(A&) {}
+  // projector helpers: |x|^2, -x, 1/x
+  static __device__ __forceinline__ double mag2(const S& x) { return x.x * x.x + x.y * x.y; }
+  static __device__ __forceinline__ S neg(const S& x) { return make_double2(-x.x, -x.y); }
+  static __device__ __forceinline__ S recip(const S& x) {
+    const double den = x.x * x.x + x.y * x.y;
+    return make_double2(x.x / den, -x.y / den);
+  }
 };
 
 // ---- double-float helpers --------------------------------------------------
@@ -151,6 +158,17 @@ struct DF64 {
   static __device__ __forceinline__ void norm(A& a) {
     df_norm(a.x, a.y);
     df_norm(a.z, a.w);
+  }
+  // projector helpers: |x|^2 (from the hi parts), -x, 1/x (complex128 reciprocal, split)
+  static __device__ __forceinline__ double mag2(const S& x) {
+    return (double)x.x * (double)x.x + (double)x.z * (double)x.z;
+  }
+  static __device__ __forceinline__ S neg(const S& x) { return make_float4(-x.x, -x.y, -x.z, -x.w); }
+  static __device__ __forceinline__ S recip(const S& x) {
+    const double re = (double)x.x + (double)x.y, im = (double)x.z + (double)x.w;
+    const double den = re * re + im * im;
+    const float2 r = df_split(re / den), i = df_split(-im / den);
+    return make_float4(r.x, r.y, i.x, i.y);
   }
 };
 

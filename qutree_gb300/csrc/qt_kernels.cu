@@ -814,80 +814,106 @@ __global__ void __launch_bounds__(kThreads) k_eig(const EigTask* __restrict__ ta
 //   M2   = -(rhoinv P^T)
 // so that the derivative is dPsi = alpha ((H Phi) rhoinv^T + Phi M2^T).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads) k_proj(const ProjTask* __restrict__ tasks,
-                                                   int64_t task0) {
+// Projector of one node in the arithmetic of the plan: X = S^-1 by
+// Gauss-Jordan with partial pivoting (warp-parallel pivot search), then
+// P = X D and M2 = -rhoinv P^T.  S and X live in shared memory when
+// 2 d^2 elements fit (smem != 0), else in the task's Sinv / P slots.
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_proj2(const ProjTask* __restrict__ tasks, int64_t task0, int smem) {
+  typedef typename P::S S;
+  typedef typename P::A A;
+  extern __shared__ __align__(16) unsigned char proj_smem[];
   const ProjTask t = tasks[task0 + blockIdx.x];
   const int d = t.d;
-  double2* S = t.S;
-  double2* X = t.Sinv;
-  __shared__ double2 fcol[128];
+  S* W = smem ? reinterpret_cast<S*>(proj_smem) : reinterpret_cast<S*>(t.P);      // working S
+  S* X = smem ? W + d * d : reinterpret_cast<S*>(t.Sinv);                          // becomes S^-1
+  __shared__ S fcol[kHpMaxDim];
   __shared__ int piv;
-  __shared__ double2 pinv;
-  for (int e = threadIdx.x; e < d * d; e += kThreads)
-    X[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
+  __shared__ S pinv;
+  const S* Sin = reinterpret_cast<const S*>(t.S);
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    W[e] = Sin[e];
+    S z = P::zero();
+    if ((e % d) == (e / d)) z = P::coef(make_double2(1.0, 0.0));
+    X[e] = z;
+  }
   __syncthreads();
   for (int col = 0; col < d; ++col) {
-    if (threadIdx.x == 0) {
-      int best = col;
+    if (threadIdx.x < 32) {  // pivot: largest |S(r, col)|, r >= col
       double bv = -1.0;
-      for (int r = col; r < d; ++r) {
-        const double2 v = S[r + d * col];
-        const double a = v.x * v.x + v.y * v.y;
-        if (a > bv) bv = a, best = r;
+      int best = col;
+      for (int r = col + threadIdx.x; r < d; r += 32) {
+        const double m = P::mag2(W[r + d * col]);
+        if (m > bv) bv = m, best = r;
       }
-      piv = best;
+      for (int off = 16; off > 0; off >>= 1) {
+        const double ov = __shfl_down_sync(0xffffffffu, bv, off);
+        const int ob = __shfl_down_sync(0xffffffffu, best, off);
+        if (ov > bv || (ov == bv && ob < best)) bv = ov, best = ob;
+      }
+      if (threadIdx.x == 0) piv = best;
     }
     __syncthreads();
     const int pr = piv;
     if (pr != col) {
       for (int j = threadIdx.x; j < d; j += kThreads) {
-        double2 x = S[col + d * j];
-        S[col + d * j] = S[pr + d * j];
-        S[pr + d * j] = x;
+        S x = W[col + d * j];
+        W[col + d * j] = W[pr + d * j];
+        W[pr + d * j] = x;
         x = X[col + d * j];
         X[col + d * j] = X[pr + d * j];
         X[pr + d * j] = x;
       }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-      const double2 v = S[col + d * col];
-      const double den = v.x * v.x + v.y * v.y;
-      pinv = make_double2(v.x / den, -v.y / den);
-    }
+    if (threadIdx.x == 0) pinv = P::recip(W[col + d * col]);
     __syncthreads();
+    const S pv = pinv;
     for (int j = threadIdx.x; j < d; j += kThreads) {
-      S[col + d * j] = cmul(S[col + d * j], pinv);
-      X[col + d * j] = cmul(X[col + d * j], pinv);
+      W[col + d * j] = P::mul(W[col + d * j], pv);
+      X[col + d * j] = P::mul(X[col + d * j], pv);
     }
     __syncthreads();
-    for (int r = threadIdx.x; r < d; r += kThreads) fcol[r] = S[r + d * col];
+    for (int r = threadIdx.x; r < d; r += kThreads) fcol[r] = P::neg(W[r + d * col]);
     __syncthreads();
     for (int e = threadIdx.x; e < d * d; e += kThreads) {
       const int r = e % d, j = e / d;
       if (r == col) continue;
-      const double2 f = fcol[r];
-      const double2 sc = S[col + d * j], xc = X[col + d * j];
-      double2 s = S[e], x = X[e];
-      cfma(s, make_double2(-f.x, -f.y), sc);
-      cfma(x, make_double2(-f.x, -f.y), xc);
-      S[e] = s;
-      X[e] = x;
+      const S f = fcol[r];
+      if (j > col) {
+        A w = W[e];
+        P::mac(w, f, W[col + d * j]);
+        W[e] = P::fin(w);
+      }
+      A x = X[e];
+      P::mac(x, f, X[col + d * j]);
+      X[e] = P::fin(x);
     }
     __syncthreads();
   }
+  // P = X D into W (S is no longer needed)
+  const S* D = reinterpret_cast<const S*>(t.D);
   for (int e = threadIdx.x; e < d * d; e += kThreads) {
     const int i = e % d, j = e / d;
-    double2 acc = cz();
-    for (int k = 0; k < d; ++k) cfma(acc, X[i + d * k], t.D[k + d * j]);
-    t.P[e] = acc;
+    A acc = P::zero();
+    for (int k = 0; k < d; ++k) {
+      P::mac(acc, X[i + d * k], D[k + d * j]);
+      if (k & 1) P::norm(acc);
+    }
+    W[e] = P::fin(acc);
   }
   __syncthreads();
+  // M2 = -rhoinv P^T
+  const S* Ri = reinterpret_cast<const S*>(t.rhoinv);
+  S* M2 = reinterpret_cast<S*>(t.M2);
   for (int e = threadIdx.x; e < d * d; e += kThreads) {
     const int j = e % d, m = e / d;
-    double2 acc = cz();
-    for (int n = 0; n < d; ++n) cfma(acc, t.rhoinv[j + d * n], t.P[m + d * n]);
-    t.M2[e] = make_double2(-acc.x, -acc.y);
+    A acc = P::zero();
+    for (int k = 0; k < d; ++k) {
+      P::mac(acc, Ri[j + d * k], W[m + d * k]);
+      if (k & 1) P::norm(acc);
+    }
+    M2[e] = P::neg(P::fin(acc));
   }
 }
 
@@ -1224,9 +1250,17 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       k_eig<<<(unsigned)st.n_tasks, kThreads, sm, s>>>(t.eig, st.first_task, eps);
       break;
     }
-    case ST_PROJ:
-      k_proj<<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.proj, st.first_task);
+    case ST_PROJ: {
+      // max_eig_d bounds every node's bond
+      const int64_t need = 2 * (int64_t)max_eig_d * max_eig_d * 16;
+      const int sm = need <= 200 * 1024 ? (int)need : 0;
+      if (sm) {
+        cudaError_t e = cudaFuncSetAttribute(k_proj2<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+        if (e != cudaSuccess) return e;
+      }
+      k_proj2<P><<<(unsigned)st.n_tasks, kThreads, sm, s>>>(t.proj, st.first_task, sm);
       break;
+    }
     case ST_CVT:
       k_cvt<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.cvt, t.cvt_tiles, st.first_tile);
       break;

@@ -369,11 +369,6 @@ class Builder {
         int d = nd[i].dup();
         P.rho64_off[i] = alloc_mat(d);
         P.rhoinv64_off[i] = alloc_mat(d);
-        if (!is_top(i)) {
-          P.s64_off[i] = alloc_mat(d);
-          P.d64_off[i] = alloc_mat(d);
-          P.m2_64_off[i] = alloc_mat(d);
-        }
       }
     }
     std::vector<int64_t> ident(n, -1);
@@ -892,39 +887,33 @@ class Builder {
       }
       emit_stage(ST_MM, m0, (int64_t)P.mm.size(), mt0, (int64_t)P.mm_tiles.size(), "overlaps-fused");
     }
-    if (P.prec == 1) {
-      std::vector<int64_t> src = P.s_off, dst = P.s64_off;
-      src.insert(src.end(), P.d_off.begin(), P.d_off.end());
-      dst.insert(dst.end(), P.d64_off.begin(), P.d64_off.end());
+    if (P.prec == 1) {  // the tree energies to complex128 (qt_energy reads them)
       int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
-      for (size_t i = 0; i < src.size(); ++i) {
-        int a = (int)(i % n);
-        if (is_top(a)) continue;
-        add_cvt(mat(src[i]), mat(dst[i]), (int64_t)nd[a].dup() * nd[a].dup(), 1);
-      }
       for (size_t k = 0; k < tops.size(); ++k) {
         int dt = nd[tops[k]].dup();
         add_cvt(mat(P.energy_dev_off[k]), mat(P.energy_off[k]), (int64_t)dt * dt, 1);
         add_cvt(mat(P.stop_dev_off[k]), mat(P.stop_off[k]), (int64_t)dt * dt, 1);
       }
-      emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "overlaps-to-f64");
+      emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "energies-to-f64");
     }
+
     int64_t p0 = (int64_t)P.proj.size();
     for (int a = 0; a < n; ++a) {
       if (is_top(a)) continue;
       Plan::SProj pj;
-      pj.S = mat(P.s64_off[a]);
-      pj.D = mat(P.d64_off[a]);
-      pj.rhoinv = mat(P.rhoinv64_off[a]);
+      // the projector runs in the plan's arithmetic on its own matrices
+      pj.S = mat(P.s_off[a]);
+      pj.D = mat(P.d_off[a]);
+      pj.rhoinv = mat(P.rhoinv_off[a]);
       pj.Sinv = mat(P.sinv_off[a]);
       pj.P = mat(P.p_off[a]);
-      pj.M2 = mat(P.m2_64_off[a]);
+      pj.M2 = mat(P.m2_off[a]);
       pj.d = nd[a].dup();
       P.proj.push_back(pj);
       P.stats.exec_flops += 3 * 8.0 * pj.d * pj.d * pj.d;
     }
     emit_stage(ST_PROJ, p0, (int64_t)P.proj.size(), p0, (int64_t)P.proj.size(), "projector");
-    if (P.prec == 1) cvt_mats(P.m2_64_off, P.m2_off, 0, "m2-to-df", true);
+
     // dPsi = -i*phase * (H Phi - Phi P) rhoinv^T  (non-top);  -i*phase * H Phi (top)
     int64_t a0 = (int64_t)P.acc.size(), atile0 = (int64_t)P.acc_tiles.size();
     for (int a = 0; a < n; ++a) {
