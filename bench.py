@@ -442,7 +442,7 @@ def run_ours(args, ws, rank, local):
         "config": {"workload": WORKLOAD, "plan": "compressed (per node one block matrix of the terms "
                    "inside its subtree, summed mean fields per boundary restriction, represent chains "
                    "kept in HBM for Apply), double-float arithmetic on the FP32 pipe (complex128 in and "
-                   "out; density inverses and projector solves complex128)",
+                   "out; density inverses complex128)",
                    "parallelism": f"replicas x{ws}",
                    "l2": "flushed between timed sweeps (256 MB fill, outside the events)"},
         "energy": energy,

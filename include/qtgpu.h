@@ -62,9 +62,9 @@ extern "C" {
  * QT_PREC_F64: complex128 on the FP64 pipe.
  * QT_PREC_DF64: every real number carried as an unevaluated sum of two
  * floats (hi + lo, ~48-bit significand) and computed on the FP32 pipe, which
- * GB300 runs 61x faster than FP64; the density-matrix inverses and
- * projector solves stay complex128.  Inputs and outputs of the C ABI are
- * complex128 in both cases. */
+ * GB300 runs 61x faster than FP64; the density-matrix inverses stay
+ * complex128 (their regularisation acts on eigenvalues down to eps).  Inputs
+ * and outputs of the C ABI are complex128 in both cases. */
 #define QT_PREC_F64 0x000
 #define QT_PREC_DF64 0x100
 
