@@ -542,17 +542,35 @@ __global__ void __launch_bounds__(kThreads) k_cvt(const CvtTask* __restrict__ ta
                                                   const int2* __restrict__ tiles, int64_t tile0) {
   const int2 tl = tiles[tile0 + blockIdx.x];
   const CvtTask t = tasks[tl.x];
-  for (int q = 0; q < kCvtPerThread; ++q) {
-    const int64_t i = tl.y + threadIdx.x + (int64_t)q * kThreads;
-    if (i >= t.n) break;
-    if (t.dir == 0) {
-      const double2 v = reinterpret_cast<const double2*>(t.src)[i];
-      const float2 r = df_split(v.x), m = df_split(v.y);
-      reinterpret_cast<float4*>(t.dst)[i] = make_float4(r.x, r.y, m.x, m.y);
-    } else {
-      const float4 v = reinterpret_cast<const float4*>(t.src)[i];
-      reinterpret_cast<double2*>(t.dst)[i] =
-          make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+  // all loads of the thread first (eight 16-byte loads in flight), then convert
+  if (t.dir == 0) {
+    double2 v[kCvtPerThread];
+#pragma unroll
+    for (int q = 0; q < kCvtPerThread; ++q) {
+      const int64_t i = tl.y + threadIdx.x + (int64_t)q * kThreads;
+      v[q] = i < t.n ? __ldg(reinterpret_cast<const double2*>(t.src) + i) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int q = 0; q < kCvtPerThread; ++q) {
+      const int64_t i = tl.y + threadIdx.x + (int64_t)q * kThreads;
+      if (i < t.n) {
+        const float2 r = df_split(v[q].x), m = df_split(v[q].y);
+        reinterpret_cast<float4*>(t.dst)[i] = make_float4(r.x, r.y, m.x, m.y);
+      }
+    }
+  } else {
+    float4 w[kCvtPerThread];
+#pragma unroll
+    for (int q = 0; q < kCvtPerThread; ++q) {
+      const int64_t i = tl.y + threadIdx.x + (int64_t)q * kThreads;
+      w[q] = i < t.n ? __ldg(reinterpret_cast<const float4*>(t.src) + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int q = 0; q < kCvtPerThread; ++q) {
+      const int64_t i = tl.y + threadIdx.x + (int64_t)q * kThreads;
+      if (i < t.n)
+        reinterpret_cast<double2*>(t.dst)[i] =
+            make_double2((double)w[q].x + (double)w[q].y, (double)w[q].z + (double)w[q].w);
     }
   }
 }
