@@ -56,7 +56,7 @@ extern "C" {
                                and one summed mean field; represent chain
                                outputs stay in device memory for Apply.  No
                                per-term matrices (QT_MAT_HMAT / QT_MAT_HCON
-                               downloads return QT_ERR_STATE); no gradient   */
+                               downloads return QT_ERR_STATE)                */
 
 /* Arithmetic of the sweep, OR-ed into the plan flavour of qt_prepare.
  * QT_PREC_F64: complex128 on the FP64 pipe.

@@ -101,13 +101,14 @@ class Builder {
     if (scf && (!compressed || P.prec != 0))
       throw std::runtime_error("the SCF sweep needs the compressed plan in complex128 arithmetic");
     if (compressed) {
-      if (P.want_grad) throw std::runtime_error("the energy gradient needs the grouped or reference plan");
       comp_layout();
       comp_represent();
       comp_meanfield();
+      if (P.want_grad) comp_environment();
       P.apply_begin = (int64_t)P.stages.size();
       comp_apply(true);
       stage_final(true);
+      if (P.want_grad) stage_gradient();
       P.main_end = (int64_t)P.stages.size();
       const double sweep_flops = P.stats.exec_flops;
       const PlanStats counts = P.stats;
@@ -1069,7 +1070,12 @@ class Builder {
     int64_t a0 = (int64_t)P.acc.size(), atile0 = (int64_t)P.acc_tiles.size();
     for (int a = 0; a < n; ++a) {
       std::vector<Plan::SAccTerm> terms;
-      terms.push_back(Plan::SAccTerm{Ref{-1, 0}, hphi(a)});
+      if (compressed && !is_top(a)) {  // Apply(a) from the kept chains (H Phi is not formed)
+        if (!internal[a].empty()) terms.push_back(Plan::SAccTerm{mat(P.rho_off[a]), Yref[a]});
+        for (auto& b : bk[a]) terms.push_back(Plan::SAccTerm{mat(b.cslot), b.X});
+      } else {
+        terms.push_back(Plan::SAccTerm{Ref{-1, 0}, hphi(a)});
+      }
       terms.push_back(Plan::SAccTerm{mat(m3[a]), psi(a)});
       add_acc(Ref{B_GRAD, nd[a].aoff}, true, c2(1, 0), a, terms, false);
       P.acc.back().alpha_ref = mat(alpha[tree_of[a]]);
@@ -1574,6 +1580,78 @@ class Builder {
     stage_final();
   }
 
+
+  // ---- environment of the energy gradient, compressed plan -----------------
+  // E_out[a], the mean field of the terms acting only outside a, built at
+  // the parent p like the grouped plan's stage_environment: terms internal to
+  // p that miss a (Block of every sibling, LCA-p cover groups over the other
+  // siblings) on Phi_p x_last rho_p, boundary restrictions w of p that miss a
+  // with C(p,w) on the parent index, and E_out[p] on the parent index.
+  void comp_environment() {
+    eout_off.assign(n, -1);
+    std::vector<char> rho_done(n, 0);
+    for (int p = 0; p < n; ++p) rho_done[p] = rho_psi[p].buf >= 0;  // computed in comp_meanfield
+    int maxdepth = 0;
+    for (auto& g : nd) maxdepth = std::max(maxdepth, g.depth);
+    for (int dep = 1; dep <= maxdepth; ++dep) {
+      std::vector<Job> rj, jobs;
+      const int64_t lin0 = (int64_t)P.lin.size();
+      for (int a = 0; a < n; ++a) {
+        if (nd[a].depth != dep) continue;
+        const int p = nd[a].parent;
+        const NodeGeo& gp = nd[p];
+        const int ia = nd[a].child_idx;
+        eout_off[a] = alloc_mat(nd[a].dup());
+        Ref in_rho = psi(p);
+        if (!is_top(p)) {
+          if (rho_psi[p].buf < 0) rho_psi[p] = keep(gp.N);
+          if (!rho_done[p]) {
+            Job R;
+            R.node = p;
+            R.out = rho_psi[p];
+            R.chains.push_back(Chain{psi(p), {COp{0, gp.last(), mat(P.rho_off[p]), c2(1, 0)}}, Ref{}});
+            rj.push_back(R);
+            rho_done[p] = 1;
+          }
+          in_rho = rho_psi[p];
+        }
+        Job J;
+        J.node = p;
+        J.S = mat(eout_off[a]);
+        J.hp_mode = ia;
+        for (size_t k = 0; k < gp.children.size(); ++k) {
+          const int c = gp.children[k];
+          if ((int)k == ia || block_slot[c] < 0) continue;
+          J.chains.push_back(Chain{in_rho, {COp{0, (int)k, mat(block_slot[c]), c2(1, 0)}}, Ref{}});
+        }
+        std::vector<std::vector<int>> sig;
+        std::vector<int> term_of;
+        lca_terms(p, ia, sig, term_of);
+        std::vector<int> legs;
+        for (size_t k = 0; k < gp.children.size(); ++k)
+          if ((int)k != ia) legs.push_back((int)k);
+        for (auto& G : cover(sig, legs)) J.chains.push_back(Chain{in_rho, group_ops(p, G, sig, term_of), Ref{}});
+        if (!is_top(p)) {
+          for (auto& b : bk[p]) {
+            const int l = b.terms[0];
+            if (bk_index(l, a) != -2) continue;  // the restriction touches a
+            Chain ch{psi(p), {}, mat(b.cslot)};
+            for (size_t k = 0; k < gp.children.size(); ++k) {
+              const int bs = bk_index(l, gp.children[k]);
+              if (bs >= 0) ch.ops.push_back(COp{0, (int)k, mat(bk[gp.children[k]][bs].hslot), c2(1, 0)});
+            }
+            J.chains.push_back(ch);
+          }
+          J.chains.push_back(Chain{psi(p), {}, mat(eout_off[p])});
+        }
+        if (J.chains.empty()) J.chains.push_back(Chain{psi(p), {}, mat(zero_mat(gp.dup()))});
+        jobs.push_back(J);
+      }
+      run_jobs(rj, "environment-rho");
+      emit_stage(ST_LIN, lin0, (int64_t)P.lin.size(), lin0, (int64_t)P.lin.size(), "environment-sums");
+      run_jobs(jobs, "environment");
+    }
+  }
 
   // ---- SCF sweep segments (QT_PLAN_SCF) ------------------------------------
   // HamiltonianRepresentation(H, tree, tree, tail=false) of the SCF

@@ -17,8 +17,8 @@ def cfg4():
     return config_problem(4)
 
 
-def _gradient(tree, sop, psi, prec):
-    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PLAN_GRADIENT | prec)
+def _gradient(tree, sop, psi, prec, plan=qtgpu.QT_PLAN_GROUPED):
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=plan | qtgpu.QT_PLAN_GRADIENT | prec)
     try:
         dpsi = qtgpu.Derivative(h, psi.flat())
         g = h.gradient()
@@ -30,11 +30,13 @@ def _gradient(tree, sop, psi, prec):
     return g, dpsi, e, s00.real, arena
 
 
-@pytest.mark.parametrize("prec,n_dirs,tol", [(qtgpu.QT_PREC_F64, 64, 1e-6), (qtgpu.QT_PREC_DF64, 16, 1e-6)])
-def test_gradient_matches_finite_differences(cfg4, prec, n_dirs, tol):
+@pytest.mark.parametrize("plan,prec,n_dirs,tol", [
+    (qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PREC_F64, 64, 1e-6), (qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PREC_DF64, 16, 1e-6),
+    (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_F64, 32, 1e-6), (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_DF64, 16, 1e-6)])
+def test_gradient_matches_finite_differences(cfg4, plan, prec, n_dirs, tol):
     from tree_energy import energy, fd_directional
     tree, sop, psi = cfg4
-    g, _, e, _, arena = _gradient(tree, sop, psi, prec)
+    g, _, e, _, arena = _gradient(tree, sop, psi, prec, plan)
     assert abs(e - energy(tree, sop, psi.tensors)) <= 1e-11 * abs(e)
     assert arena < 2 << 30  # device arena of the gradient plan (bytes), stated in DESIGN
     rng = np.random.default_rng(1234)
@@ -96,3 +98,10 @@ def test_autograd_function(cfg4):
         assert np.allclose(got, 2.0 * lib, rtol=0, atol=1e-14 * np.abs(lib).max())
     finally:
         hrep.close()
+
+
+def test_gradient_compressed_equals_grouped(cfg4):
+    tree, sop, psi = cfg4
+    g1 = _gradient(tree, sop, psi, qtgpu.QT_PREC_F64)[0]
+    g2 = _gradient(tree, sop, psi, qtgpu.QT_PREC_F64, qtgpu.QT_PLAN_COMPRESSED)[0]
+    assert np.abs(g2 - g1).max() <= 1e-12 * np.abs(g1).max()

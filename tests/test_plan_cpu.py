@@ -143,7 +143,7 @@ def test_plan_rejects_cross_tree_terms():
         PlanView(f, s, 1)
 
 
-@pytest.mark.parametrize("flavour,prec", [(0, 0), (1, 1)])
+@pytest.mark.parametrize("flavour,prec", [(0, 0), (1, 1), (2, 0), (2, 1)])
 def test_plan_gradient_finite_differences(flavour, prec):
     # dE/dPhi^* of every node: 2 Re <G, delta> equals the central difference
     # of E along random directions delta (all node tensors at once)
@@ -197,7 +197,24 @@ def test_plan_compressed_general_arity():
         _check(tree, sop, psi, fl, prec=1)
 
 
-def test_plan_compressed_rejects_gradient():
-    tree, sop = config_tree_sop(0)
-    with pytest.raises(ValueError, match="gradient"):
-        PlanView(tree, sop, 2 | 0x1000)
+
+
+def test_plan_compressed_gradient_equals_grouped_on_a_ternary_tree():
+    # environments with several siblings (LCA cover groups, sibling blocks):
+    # the compressed plan's gradient equals the grouped plan's
+    from qutree_gb300.model import Tree, _Build
+    groups = [_Build([3, 3, 3, 3], [_Build([4, 3], leaf=True) for _ in range(3)]) for _ in range(3)]
+    tree = Tree(_Build([3, 3, 3, 1], groups))
+    rng = np.random.default_rng(41)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=rng, omega=1.0)
+    b = HOBasis(4, omega=1.0)
+    x = sop.ops.add("x3", 1, b.x.astype(complex))
+    for (i, j, k) in [(0, 4, 8), (1, 2, 7), (3, 5, 6), (0, 1, 2)]:
+        sop.push_back(MLO([(i, x), (j, x), (k, x)]), 0.05 * (i + 1))
+    psi = random_wavefunction(tree, 41)
+    grads = []
+    for fl in (1, 2):
+        pv = PlanView(tree, sop, fl | 0x1000)
+        pv.run(psi.flat())
+        grads.append(pv.gradient())
+    assert np.abs(grads[1] - grads[0]).max() <= 1e-12 * np.abs(grads[0]).max()
