@@ -369,11 +369,13 @@ def run_ours(args, ws, rank, local):
     if not args.no_scf and rank == 0:
         scf = {"sweep": "one SCF iteration: every node in depth-first order with returns, "
                         "5 Lanczos vectors of the tail-free effective Hamiltonian, Ritz vector, "
-                        "isometrisation toward the next node, edge-local rebuild"}
+                        "isometrisation toward the next node, edge-local rebuild",
+               "arithmetic": "effective Hamiltonian and rebuilds in double-float; Lanczos vectors, "
+                             "dot products and QR in complex128"}
         for cfg in (1, 4):
             t_s, s_s, p_s = config_problem(cfg)
-            hs = qtgpu.HamiltonianRepresentation(s_s, t_s, flavour=qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PLAN_SCF,
-                                                 device=local)
+            hs = qtgpu.HamiltonianRepresentation(s_s, t_s, flavour=qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PLAN_SCF
+                                                 | qtgpu.QT_PREC_DF64, device=local)
             hs.upload(p_s.flat())
             hs.scf(n_iter=1, n_krylov=5)  # warm-up
             hs.upload(p_s.flat())
@@ -394,6 +396,32 @@ def run_ours(args, ws, rank, local):
                 scf["cfg4"]["cpu_oracle"] = {"ms_per_scf_sweep": 1e3 * dt_cpu, "kind": "port", "cores": 1,
                                              "sample": "one SCF iteration of the 16-mode tree, numpy",
                                              "max_abs_ritz_diff": float(np.abs(E_cpu - E).max())}
+
+    # supplementary: the energy gradient (QT_PLAN_GRADIENT) on the 16-mode
+    # differentiation workload, compressed double-float vs the plain sequence
+    grad = None
+    if rank == 0:
+        t4, s4, p4 = config_problem(4)
+        grad = {"workload": "16 modes, p=32, bonds 32, 152 terms; one sweep = derivative + dE/dPhi* of every node"}
+        for label, fl in (("compressed_double_float", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64),
+                          ("plain_complex128", qtgpu.QT_PLAN_REFERENCE)):
+            hg4 = qtgpu.HamiltonianRepresentation(s4, t4, flavour=fl | qtgpu.QT_PLAN_GRADIENT, device=local)
+            g_stream = torch.cuda.ExternalStream(hg4.stream())
+            hg4.upload(p4.flat())
+            for _ in range(2):
+                hg4.derivative()
+            hg4.sync()
+            ng = 5
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(g_stream)
+            for _ in range(ng):
+                hg4.derivative()
+            e1.record(g_stream)
+            hg4.sync()
+            ms = e0.elapsed_time(e1) / ng
+            grad[label] = {"ms_per_gradient_sweep": ms, "gradient_sweeps_per_s": 1e3 / ms,
+                           "executed_gflop": hg4.stats()["exec_flops"] / 1e9}
+            hg4.close()
 
     # optional: double-float against complex128 along a constant-mean-field
     # propagation of the 48..96-bond tree (regularisation 1e-8, dt 0.01)
@@ -475,6 +503,8 @@ def run_ours(args, ws, rank, local):
         line["scf"] = scf
     if precision:
         line["precision_study"] = precision
+    if grad:
+        line["gradient"] = grad
     if not args.no_cpu_baseline and args.config == 1:
         dt, cpu_e, blas = cpu_baseline_sweep(tree, sop, psi)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count(),

@@ -1275,9 +1275,9 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
     for (int x : g.shape) maxd = std::max(maxd, x);
   }
   const int64_t vstride = (maxN + 15) / 16 * 16, mstride = (int64_t)maxd * maxd;
-  // vectors V_0..V_{K-1}, W, Y, T; matrices S, H, R; dot scratch; hole-product partial tiles
+  // vectors V_0..V_{K-1}, W, Y, T, U; matrices S, H, R; dot scratch; hole-product partial tiles
   const int64_t ws_elems = 64 * mstride;
-  const int64_t total = (n_krylov + 3) * vstride + 3 * mstride + 512 + ws_elems;
+  const int64_t total = (n_krylov + 4) * vstride + 3 * mstride + 512 + ws_elems;
   DevFree work;
   {
     cudaError_t e = cudaMalloc(&work.p, total * sizeof(cd));
@@ -1288,14 +1288,26 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
   cd* W = V(n_krylov);
   cd* Y = V(n_krylov + 1);
   cd* T = V(n_krylov + 2);
-  cd* dS = base + (n_krylov + 3) * vstride;
+  cd* U = V(n_krylov + 3);  // complex128 copy of H v (double-float plans)
+  cd* dS = base + (n_krylov + 4) * vstride;
   cd* dH = dS + mstride;
   cd* dR = dH + mstride;
   cd* dscal = dR + mstride;
   cd* hpws = dscal + 512;
-  cd* psi = c->buf[qt::B_PSI];
+  // the driver works on the complex128 wavefunction; with double-float
+  // arithmetic the plan's stages read B_PSI, refreshed node by node
+  const bool df = c->prec == 1;
+  cd* psi = c->buf[qt::B_PSI64];
+  cd* psi_ar = c->buf[qt::B_PSI];
   cd* kin = c->buf[qt::B_KRY] + P.kry_in;
   cd* kout = c->buf[qt::B_KRY] + P.kry_out;
+  cd* hv = df ? U : kout;  // H v in complex128
+  auto to_arith = [&](cd* dst, const cd* src, int64_t n) -> int {
+    cudaError_t e = qt::launch_convert(dst, src, n, 0, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf convert");
+    c->launches += 1;
+    return QT_OK;
+  };
   auto dot = [&](const cd* a, const cd* b, int64_t n, cd& out) -> int {
     cudaError_t e = qt::launch_dot(a, b, n, dscal, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf dot");
@@ -1352,6 +1364,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
     return QT_OK;
   };
   int rc;
+  if (df && (rc = to_arith(psi_ar, psi, P.psi_packed)) != QT_OK) return rc;
   // initial build: buildSCF(node, parent) for every non-top node, bottom-up
   for (size_t a = 0; a < nd.size(); ++a)
     if (!nd[a].top() && (rc = run_stages(c, P.scf_up_b[a], P.scf_up_e[a])) != QT_OK) return rc;
@@ -1371,16 +1384,25 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
       if (!(s.x > 0.0) || !std::isfinite(s.x)) return fail(c, QT_ERR_NUMERIC, "qt_scf: zero or non-finite node tensor");
       if ((rc = lincomb(V(0), {{pa, cmk(1.0 / std::sqrt(s.x), 0)}}, N)) != QT_OK) return rc;
       for (int l = 0; l < size; ++l) {
-        QT_CUDA(c, cudaMemcpyAsync(kin, V(l), N * sizeof(cd), cudaMemcpyDeviceToDevice, c->stream));
+        if (df) {
+          if ((rc = to_arith(kin, V(l), N)) != QT_OK) return rc;
+        } else {
+          QT_CUDA(c, cudaMemcpyAsync(kin, V(l), N * sizeof(cd), cudaMemcpyDeviceToDevice, c->stream));
+        }
         if ((rc = run_stages(c, P.scf_apply_b[a], P.scf_apply_e[a])) != QT_OK) return rc;
-        if ((rc = dot(V(l), kout, N, s)) != QT_OK) return rc;
+        if (df) {
+          cudaError_t e = qt::launch_convert(U, kout, N, 1, c->stream);
+          if (e != cudaSuccess) return cuda_fail(c, e, "qt_scf convert");
+          c->launches += 1;
+        }
+        if ((rc = dot(V(l), hv, N, s)) != QT_OK) return rc;
         if (!std::isfinite(s.x)) return fail(c, QT_ERR_NUMERIC, "qt_scf: non-finite <v|H|v>");
         al.push_back(s.x);
         if (l + 1 == size) break;
         if (l == 0)
-          rc = lincomb(W, {{kout, cmk(1, 0)}, {V(0), cmk(-al[0], 0)}}, N);
+          rc = lincomb(W, {{hv, cmk(1, 0)}, {V(0), cmk(-al[0], 0)}}, N);
         else
-          rc = lincomb(W, {{kout, cmk(1, 0)}, {V(l), cmk(-al[l], 0)}, {V(l - 1), cmk(-be[l - 1], 0)}}, N);
+          rc = lincomb(W, {{hv, cmk(1, 0)}, {V(l), cmk(-al[l], 0)}, {V(l - 1), cmk(-be[l - 1], 0)}}, N);
         if (rc != QT_OK) return rc;
         if ((rc = dot(W, W, N, s)) != QT_OK) return rc;
         const double nrm = std::sqrt(std::max(s.x, 0.0));
@@ -1473,6 +1495,10 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
       cd* pn = psi + gn.aoff;
       if ((rc = mode_product(dR, pn, T, gn, in_idx)) != QT_OK) return rc;
       QT_CUDA(c, cudaMemcpyAsync(pn, T, gn.N * sizeof(cd), cudaMemcpyDeviceToDevice, c->stream));
+      if (df) {
+        if ((rc = to_arith(psi_ar + g.aoff, pa, N)) != QT_OK) return rc;
+        if ((rc = to_arith(psi_ar + gn.aoff, pn, gn.N)) != QT_OK) return rc;
+      }
       const bool up = !g.top() && g.parent == nxt;
       if (up)
         rc = run_stages(c, P.scf_up_b[a], P.scf_up_e[a]);

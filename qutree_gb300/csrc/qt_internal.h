@@ -388,6 +388,8 @@ struct LinComb {
   int count;
 };
 cudaError_t launch_dot(const double2* a, const double2* b, int64_t n, double2* out, cudaStream_t s);
+// complex128 <-> double-float copy (dir 0: to double-float)
+cudaError_t launch_convert(void* dst, const void* src, int64_t n, int dir, cudaStream_t s);
 cudaError_t launch_lincomb(double2* out, const LinComb& lc, int64_t n, cudaStream_t s);
 cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2* y, int64_t n,
                         cudaStream_t s);

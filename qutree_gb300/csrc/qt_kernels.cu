@@ -1060,6 +1060,29 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_part(const double2* __restr
   if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
+// complex128 <-> double-float copy of n elements (dir 0: to double-float)
+__global__ void __launch_bounds__(kThreads) k_convert(void* __restrict__ dst, const void* __restrict__ src,
+                                                      int64_t n, int dir) {
+  for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+    if (dir == 0) {
+      const double2 v = reinterpret_cast<const double2*>(src)[i];
+      const float2 r = df_split(v.x), m = df_split(v.y);
+      reinterpret_cast<float4*>(dst)[i] = make_float4(r.x, r.y, m.x, m.y);
+    } else {
+      const float4 v = reinterpret_cast<const float4*>(src)[i];
+      reinterpret_cast<double2*>(dst)[i] = make_double2((double)v.x + (double)v.y, (double)v.z + (double)v.w);
+    }
+  }
+}
+
+cudaError_t launch_convert(void* dst, const void* src, int64_t n, int dir, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  const int blocks = (int)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 8);
+  (void)cudaGetLastError();
+  k_convert<<<blocks, kThreads, 0, s>>>(dst, src, n, dir);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_dot(const double2* a, const double2* b, int64_t n, double2* out, cudaStream_t s) {
   (void)cudaGetLastError();
   // slices of >= 8192 elements, at most kDotParts of them; the partial sums

@@ -98,8 +98,7 @@ class Builder {
     }
     stage_density();
     stage_inverse();
-    if (scf && (!compressed || P.prec != 0))
-      throw std::runtime_error("the SCF sweep needs the compressed plan in complex128 arithmetic");
+    if (scf && !compressed) throw std::runtime_error("the SCF sweep needs the compressed plan");
     if (compressed) {
       comp_layout();
       comp_represent();

@@ -296,6 +296,8 @@ def chol_qr(x, mode, cond_limit=1e-6):
 def scf_emulated(pv, tree, psi_flat, n_iter=1, n_krylov=5, n_itp=0, beta=1.0):
     from scf import sweep_order  # oracle module: the reference's sweep order
     pv.init(psi_flat)
+    if pv.prec == 1:  # the conversion qt_scf runs first (a copy here)
+        pv.bufs[B_PSI][:] = pv.bufs[B_PSI64]
     arena = pv.bufs[B_PSI]
     offs = tree.offsets()
     seg = pv.tables[20]

@@ -14,8 +14,8 @@ pytestmark = pytest.mark.gpu
 FL = qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PLAN_SCF
 
 
-def _gpu_scf(tree, sop, psi, **kw):
-    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=FL)
+def _gpu_scf(tree, sop, psi, prec=qtgpu.QT_PREC_F64, **kw):
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=FL | prec)
     try:
         h.upload(psi.flat())
         E = h.scf(**kw)
@@ -25,9 +25,9 @@ def _gpu_scf(tree, sop, psi, **kw):
     return E, fin
 
 
-def _check(tree, sop, psi, tol=1e-11, **kw):
+def _check(tree, sop, psi, tol=1e-11, prec=qtgpu.QT_PREC_F64, **kw):
     E0, fin0 = S.scf(tree, sop, psi.tensors, **kw)
-    E1, fin1 = _gpu_scf(tree, sop, psi, **kw)
+    E1, fin1 = _gpu_scf(tree, sop, psi, prec=prec, **kw)
     assert len(E1) == len(E0) == kw.get("n_iter", 1) * (2 * tree.n_nodes - 1)
     scale = max(1.0, np.abs(E0).max())
     assert np.abs(E1 - E0).max() <= tol * scale
@@ -46,6 +46,13 @@ def test_scf_cfg0(n_itp):
 def test_scf_cfg4():
     tree, sop, psi = config_problem(4)
     _check(tree, sop, psi, n_iter=1, n_krylov=4)
+
+
+@pytest.mark.parametrize("cfg", [0, 4])
+def test_scf_double_float(cfg):
+    # effective Hamiltonian in double-float, Lanczos and QR in complex128
+    tree, sop, psi = config_problem(cfg)
+    _check(tree, sop, psi, tol=1e-10, prec=qtgpu.QT_PREC_DF64, n_iter=1, n_krylov=5, n_itp=1, beta=200.0)
 
 
 def test_scf_ternary_tree_three_body_terms():
@@ -103,12 +110,13 @@ def test_scf_needs_its_plan():
         h.close()
 
 
-def test_scf_full_size_64_modes():
+@pytest.mark.parametrize("prec", [qtgpu.QT_PREC_F64, qtgpu.QT_PREC_DF64])
+def test_scf_full_size_64_modes(prec):
     # one SCF sweep on the 64-mode workload: the energy of the final state,
     # from an independent compressed sweep on the same context, equals the
     # last Ritz value, and the sweep lowers the energy
     tree, sop, psi = config_problem(1)
-    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=FL)
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=FL | prec)
     try:
         h.upload(psi.flat())
         h.derivative()

@@ -108,9 +108,16 @@ def test_plan_scf_partial_sop():
     assert np.abs(E0 - E1).max() <= 1e-12 * max(1.0, np.abs(E0).max())
 
 
-def test_plan_scf_needs_compressed_complex128():
+def test_plan_scf_needs_the_compressed_plan():
     tree, sop, _ = config_problem(0)
     with pytest.raises(ValueError, match="SCF"):
         PlanView(tree, sop, 1 | QT_PLAN_SCF)
-    with pytest.raises(ValueError, match="SCF"):
-        PlanView(tree, sop, QT_PLAN_COMPRESSED | QT_PLAN_SCF, prec=1)
+
+
+def test_plan_scf_double_float_segments():
+    # the double-float plan's SCF segments (conversions are copies here)
+    tree, sop, psi = config_problem(0)
+    E0, _ = S.scf(tree, sop, psi.tensors, n_iter=1, n_krylov=6)
+    pv = PlanView(tree, sop, QT_PLAN_COMPRESSED | QT_PLAN_SCF, prec=1)
+    E1, _ = scf_emulated(pv, tree, psi.flat(), n_iter=1, n_krylov=6)
+    assert np.abs(E0 - E1).max() <= 1e-12 * np.abs(E0).max()
