@@ -77,8 +77,9 @@ extern "C" {
  * counterpart in the reference (QuTree has no tree-network gradient). */
 #define QT_PLAN_GRADIENT 0x1000
 
-/* OR-ed into QT_PLAN_COMPRESSED (complex128 arithmetic): also plan the SCF /
- * Krylov sweep of qt_scf -- the HamiltonianRepresentation(H, tree, tree,
+/* OR-ed into QT_PLAN_COMPRESSED (either arithmetic; with QT_PREC_DF64 the
+ * effective Hamiltonian and the rebuilds run in double-float, the Lanczos
+ * vectors and the QR in complex128): also plan the SCF / Krylov sweep of qt_scf -- the HamiltonianRepresentation(H, tree, tree,
  * tail = false) of QuTree's SCF with its correction matrices
  * (include/TreeClasses/HamiltonianRepresentation.h:19-177,
  * src/TreeClasses/HamiltonianRepresentation.cpp:117-203). */
