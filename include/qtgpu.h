@@ -85,11 +85,29 @@ extern "C" {
  * src/TreeClasses/HamiltonianRepresentation.cpp:117-203). */
 #define QT_PLAN_SCF 0x2000
 
+/* OR-ed into QT_PLAN_REFERENCE or QT_PLAN_GROUPED (complex128, one tree):
+ * the Hamiltonian also has a potential, uploaded with qt_cdvr_upload, that
+ * the sweep applies by CDVR, as QuTree does when H.hasV
+ * (src/TreeClasses/HamiltonianRepresentation.cpp:30-32,
+ * include/TreeClasses/HamiltonianRepresentation.h:84-86): CDVR::Update
+ * (src/DVR/CDVR.cpp:150-175) inside every build and CDVR::apply
+ * (src/DVR/CDVR.cpp:90-123) added to Apply at every node.  Everything runs
+ * on the device inside the sweep's graph. */
+#define QT_PLAN_CDVR 0x4000
+
 /* Matrix sets for qt_matrices_download. */
 #define QT_MAT_RHO 0     /* density matrices, per node, d_up x d_up          */
 #define QT_MAT_RHOINV 1  /* regularised inverse density matrices             */
 #define QT_MAT_HMAT 2    /* represent matrices, sparse layout                */
 #define QT_MAT_HCON 3    /* mean-field (hole) matrices, sparse layout         */
+#define QT_MAT_CDVR 4    /* the whole CDVR arena (grids, transformations,
+                            potentials, correction tensors), complex128    */
+
+/* qt_cdvr_upload flag: hand every hole grid its own mode's diagonal.  The
+ * reference hands them out by rank among the node's active grid trees
+ * (setGrids, src/DVR/TDDVR.cpp:22-30), which on upper nodes gives some hole
+ * grids the diagonal of another mode's X matrix; the default reproduces it. */
+#define QT_CDVR_ALIGNED_HOLE_GRIDS 1
 
 typedef struct qt_ctx qt_ctx;
 
@@ -132,6 +150,22 @@ int qt_sop_upload(qt_ctx* ctx, int n_ops, const int* op_kind, const int* op_dim,
                   const int64_t* op_off, const double* op_data, int n_terms,
                   const double* coeff, const int* term_ptr, const int* term_mode,
                   const int* term_op);
+
+/* Potential of a Hamiltonian with hasV, applied by CDVR (QT_PLAN_CDVR).
+ * Replaces PotentialOperator / Potential::evaluate
+ * (include/TreeOperators/PotentialOperator.h:14-62,
+ * include/TreeOperators/Potential.h:9-18) and the leaves' DVR grids
+ * (LeafInterface::getX, include/TreeShape/LeafTypes/DVRBasis.h:27-29).
+ *   leaf_dim[m], leaf_x[]   the DVR grid points of every mode m, back to back
+ *   coeff[q], term_ptr[]    V(x) = sum_q coeff[q] prod x_{term_mode}^{term_power}
+ *   term_mode, term_power   over the factors [term_ptr[q], term_ptr[q+1]);
+ *                           a device-side polynomial stands in for the
+ *                           reference's C++ potential callback (e.g.
+ *                           contrib's CDVRModelV is 2f terms)
+ *   flags                   QT_CDVR_ALIGNED_HOLE_GRIDS or 0 */
+int qt_cdvr_upload(qt_ctx* ctx, int n_modes, const int* leaf_dim, const double* leaf_x,
+                   int n_terms, const double* coeff, const int* term_ptr,
+                   const int* term_mode, const int* term_power, int flags);
 
 /* Regularisation epsilon of the inverse density matrices,
  * lambda -> 1/(lambda + eps*exp(-lambda/eps)); default 1e-10 as

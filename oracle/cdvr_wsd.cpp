@@ -1,0 +1,393 @@
+// cdvr_wsd.cpp -- CPU restatement of the grid step of QuTree's CDVR: the
+// multi-matrix branch of LayerGrid (src/DVR/TDDVR.cpp:63-89) around the
+// weighted simultaneous diagonalisation
+// (src/Util/WeightedSimultaneousDiagonalization.cpp:5-378) and its Jacobi
+// rotation helpers (src/Core/JacobiRotationFramework.cpp:4-164).
+//
+// TEST INFRASTRUCTURE ONLY: loaded by oracle/cdvr.py as the checker of the
+// device kernel k_wsd; the product path never links it.
+//
+// The iteration is discontinuous in its inputs (accept / reject decisions of
+// the rational-function optimiser), so this file fixes one operation order
+// and the device kernel follows it bit for bit:
+//  * a complex product is (ac - bd) + i(ad + bc), sums are left to right and
+//    nothing is fused (compiled with -ffp-contract=off; the device file with
+//    -fmad=false);
+//  * a sum over the matrices of a problem puts matrix k into partial sum
+//    k mod 32 (ascending k) and adds the 32 partials by the butterfly
+//    v[t] += v[t ^ o] for o = 16, 8, 4, 2, 1 (one warp's shuffle reduction);
+//  * |z| is sqrt(re^2 + im^2) where the reference calls std::abs (hypot), and
+//    real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
+//  * the 3x3 symmetric eigenproblem of the optimiser (Matrix::rDiag, Eigen's
+//    SelfAdjointEigenSolver in the reference) is cyclic Jacobi; only the
+//    eigenvector of the largest eigenvalue is used, through ratios and its
+//    squared components, which do not depend on the solver's sign choice;
+//  * the two step-size searches stop after 64 rounds at the latest (the
+//    reference's own conditions end them far earlier).
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+struct cd {
+  double r, i;
+};
+inline cd mk(double r, double i) { return cd{r, i}; }
+inline cd cmul(cd a, cd b) { return cd{a.r * b.r - a.i * b.i, a.r * b.i + a.i * b.r}; }
+inline cd cadd(cd a, cd b) { return cd{a.r + b.r, a.i + b.i}; }
+inline cd csub(cd a, cd b) { return cd{a.r - b.r, a.i - b.i}; }
+inline cd cconj(cd a) { return cd{a.r, -a.i}; }
+inline double cabs_(cd a) { return std::sqrt(a.r * a.r + a.i * a.i); }
+inline double cdiv_re(cd x, cd w) { return (x.r * w.r + x.i * w.i) / (w.r * w.r + w.i * w.i); }
+
+double warp_sum(double* v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    double t[32];
+    for (int l = 0; l < 32; ++l) t[l] = v[l] + v[l ^ o];
+    std::memcpy(v, t, sizeof(t));
+  }
+  return v[0];
+}
+
+struct Mat {
+  int d;
+  std::vector<cd> a;
+  cd& operator()(int i, int j) { return a[i + (size_t)d * j]; }
+  cd operator()(int i, int j) const { return a[i + (size_t)d * j]; }
+};
+
+// Matrix::rDiag for a symmetric 3x3 matrix: the eigenvector of the largest
+// eigenvalue (cyclic Jacobi, rotations of Golub & Van Loan, sym.schur2).
+void eig3_top(const double H[9], double v[3]) {
+  double A[9], V[9];
+  std::memcpy(A, H, sizeof(A));
+  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    const double off = A[3] * A[3] + A[6] * A[6] + A[7] * A[7];
+    if (off == 0.0) break;
+    for (int pq = 0; pq < 3; ++pq) {
+      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+      const double apq = A[p + 3 * q];
+      if (apq == 0.0) continue;
+      const double theta = (A[q + 3 * q] - A[p + 3 * p]) / (2.0 * apq);
+      double t;
+      if (std::fabs(theta) > 1e150)
+        t = 0.5 / theta;
+      else
+        t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+      const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+      for (int k = 0; k < 3; ++k) {  // columns: A <- A J
+        const double akp = A[k + 3 * p], akq = A[k + 3 * q];
+        A[k + 3 * p] = c * akp - s * akq;
+        A[k + 3 * q] = s * akp + c * akq;
+        const double vkp = V[k + 3 * p], vkq = V[k + 3 * q];
+        V[k + 3 * p] = c * vkp - s * vkq;
+        V[k + 3 * q] = s * vkp + c * vkq;
+      }
+      for (int k = 0; k < 3; ++k) {  // rows: A <- J^T A
+        const double apk = A[p + 3 * k], aqk = A[q + 3 * k];
+        A[p + 3 * k] = c * apk - s * aqk;
+        A[q + 3 * k] = s * apk + c * aqk;
+      }
+      A[p + 3 * q] = 0.0;
+      A[q + 3 * p] = 0.0;
+    }
+  }
+  int top = 0;
+  for (int k = 1; k < 3; ++k)
+    if (A[k + 3 * k] > A[top + 3 * top]) top = k;
+  for (int k = 0; k < 3; ++k) v[k] = V[k + 3 * top];
+}
+
+// rotatedDiagonals (src/Core/JacobiRotationFramework.cpp:129-141)
+inline void rotated_diagonals(const Mat& A, int p, int q, cd c, cd s, double& a0, double& a1) {
+  const cd c00 = cadd(cmul(c, A(p, p)), cmul(s, A(p, q)));
+  const cd c01 = csub(cmul(c, A(p, q)), cmul(cconj(s), A(p, p)));
+  const cd c10 = cadd(cmul(c, A(q, p)), cmul(s, A(q, q)));
+  const cd c11 = csub(cmul(c, A(q, q)), cmul(cconj(s), A(q, p)));
+  a0 = cadd(cmul(c, c00), cmul(cconj(s), c10)).r;
+  a1 = csub(cmul(c, c11), cmul(s, c01)).r;
+}
+
+struct Problem {
+  int n, d;
+  std::vector<Mat> xw;  // weighted matrices
+  std::vector<Mat> xp;  // plain (shifted) matrices
+  Mat w, trafo;
+
+  // weightedJacobiLoc (WeightedSimultaneousDiagonalization.cpp:260-288)
+  double loc(int p, int q, cd c, cd s) const {
+    double w0, w1;
+    rotated_diagonals(w, p, q, c, s, w0, w1);
+    double o0[32] = {0}, o1[32] = {0}, n0[32] = {0}, n1[32] = {0};
+    for (int k = 0; k < n; ++k) {
+      const double x0 = xw[k](p, p).r, x1 = xw[k](q, q).r;
+      o0[k % 32] += x0 * x0;
+      o1[k % 32] += x1 * x1;
+    }
+    for (int k = 0; k < n; ++k) {
+      double r0, r1;
+      rotated_diagonals(xw[k], p, q, c, s, r0, r1);
+      n0[k % 32] += r0 * r0;
+      n1[k % 32] += r1 * r1;
+    }
+    const double xold0 = warp_sum(o0), xold1 = warp_sum(o1);
+    const double xnew0 = warp_sum(n0), xnew1 = warp_sum(n1);
+    double diff = 0;
+    diff += xnew0 / w0 - xold0 / w(p, p).r;
+    diff += xnew1 / w1 - xold1 / w(q, q).r;
+    return diff;
+  }
+
+  // weightedJacobiDerivatives (:290-324)
+  void derivatives(double grad[2], double pre[4], cd s_in, int p, int q, double delta) const {
+    const double s0 = s_in.r, s1 = s_in.i;
+    double y[9];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const double x0 = s0 + (double)(i - 1) * delta;
+        const double x1 = s1 + (double)(j - 1) * delta;
+        const double z = x0 * x0 + x1 * x1;
+        const cd cnow = mk(std::sqrt(std::fabs(1 - z)), 0.0);
+        y[i + 3 * j] = loc(p, q, cnow, mk(x0, x1));
+      }
+    auto Y = [&](int i, int j) { return y[i + 3 * j]; };
+    grad[0] = (Y(2, 1) - Y(0, 1)) / (2 * delta);
+    grad[1] = (Y(1, 2) - Y(1, 0)) / (2 * delta);
+    pre[0] = (Y(2, 1) + Y(0, 1) - 2 * Y(1, 1)) / (delta * delta);
+    pre[3] = (Y(1, 2) + Y(1, 0) - 2 * Y(1, 1)) / (delta * delta);
+    pre[2] = (Y(2, 2) + Y(0, 0) - Y(2, 0) - Y(0, 2)) / (4 * delta * delta);
+    pre[1] = pre[2];
+  }
+
+  // calculateWeightedAngles (:104-211): rational function optimisation
+  void angles(cd& c, cd& s, int p, int q) const {
+    int iter = 0;
+    const int maxiter = 30;
+    const double eps = 1E-3;
+    double diff_rel = 2 * eps * eps;
+    const double amin = 1E-12, amax = 1;
+    double a = amax;
+    const double delta = 1E-5;
+    double snew[2] = {0, 0}, cnew[2] = {0, 0};
+    c = mk(std::sqrt(1 - 2 * eps * eps), 0);
+    s = mk(eps, -eps);
+    double loc_alt = loc(p, q, c, s);
+    double loc_new = 0;
+    while (iter < maxiter && diff_rel > eps * eps && a > amin) {
+      double pre[4], grad[2];
+      derivatives(grad, pre, s, p, q, delta);
+      double diff = -1;
+      int guard = 0;
+      while (a > amin && diff < 0 && diff_rel > eps * eps && guard++ < 64) {
+        double z = 1;
+        double v[3] = {0, 0, 0};
+        int guard2 = 0;
+        while (a > amin && z > 0.5 && guard2++ < 64) {
+          // rfoBuildHessian (src/Core/JacobiRotationFramework.cpp:114-127)
+          double H[9];
+          H[0] = pre[0] * a * a;
+          H[1] = pre[1] * a * a;
+          H[3] = pre[2] * a * a;
+          H[4] = pre[3] * a * a;
+          H[2] = grad[0] * a;
+          H[6] = grad[0] * a;
+          H[5] = grad[1] * a;
+          H[7] = grad[1] * a;
+          H[8] = 0;
+          eig3_top(H, v);
+          const double ds0 = a * v[0] / v[2];
+          const double ds1 = a * v[1] / v[2];
+          snew[0] = s.r + ds0;
+          snew[1] = s.i + ds1;
+          const double zab = cabs_(mk(snew[0], snew[1]));
+          z = zab * zab;
+          if (z > 0.5) a /= 2;
+        }
+        cnew[0] = std::sqrt(std::fabs(1 - z));
+        cnew[1] = 0;
+        loc_new = loc(p, q, mk(cnew[0], cnew[1]), mk(snew[0], snew[1]));
+        const double trafoabs = v[0] * v[0] + v[1] * v[1];
+        const double sab = cabs_(s);
+        const double sabs = sab * sab + eps * eps;
+        diff_rel = trafoabs / sabs;
+        diff = loc_new - loc_alt;
+        if (diff < 0) {
+          a /= 2;
+        } else {
+          if (a < amax) a *= 2;
+        }
+      }
+      if (a > amin && diff > 0) {
+        c = mk(cnew[0], cnew[1]);
+        s = mk(snew[0], snew[1]);
+        loc_alt = loc_new;
+      }
+      iter++;
+    }
+  }
+
+  // givensRotation (src/Core/JacobiRotationFramework.cpp:4-30)
+  static void givens(Mat& B, cd c, cd s, int i, int j) {
+    const int d = B.d;
+    std::vector<cd> c0(d), c1(d);
+    for (int r = 0; r < d; ++r) {
+      c0[r] = cadd(cmul(c, B(r, i)), cmul(s, B(r, j)));
+      c1[r] = csub(cmul(c, B(r, j)), cmul(cconj(s), B(r, i)));
+    }
+    for (int r = 0; r < d; ++r) {
+      B(r, i) = c0[r];
+      B(r, j) = c1[r];
+    }
+    for (int r = 0; r < d; ++r) {
+      c0[r] = B(i, r);
+      c1[r] = B(j, r);
+    }
+    for (int r = 0; r < d; ++r) {
+      B(i, r) = cadd(cmul(c, c0[r]), cmul(cconj(s), c1[r]));
+      B(j, r) = csub(cmul(c, c1[r]), cmul(s, c0[r]));
+    }
+  }
+
+  // givensTrafoRotation (:40-54)
+  static void givens_trafo(Mat& T, cd c, cd s, int i, int j) {
+    for (int r = 0; r < T.d; ++r) {
+      const cd ti = T(r, i), tj = T(r, j);
+      T(r, i) = cadd(cmul(c, ti), cmul(s, tj));
+      T(r, j) = csub(cmul(c, tj), cmul(cconj(s), ti));
+    }
+  }
+
+  // weightedJacobiRotations (:75-102)
+  void rotations() {
+    for (int i = 0; i < d - 1; ++i)
+      for (int j = i + 1; j < d; ++j) {
+        cd c, s;
+        angles(c, s, i, j);
+        for (int k = 0; k < n; ++k) givens(xw[k], c, s, i, j);
+        givens(w, c, s, i, j);
+        givens_trafo(trafo, c, s, i, j);
+      }
+  }
+
+  // measureWeightedOffDiagonality (:326-353): sum_k Re tr(W (D_k - T^H X_k T)^2)
+  double offdiag_one(int k) const {
+    std::vector<cd> M(d * d), Y(d * d), Z(d * d);
+    const Mat& X = xp[k];
+    for (int j = 0; j < d; ++j)  // M = X T
+      for (int i = 0; i < d; ++i) {
+        cd acc = mk(0, 0);
+        for (int l = 0; l < d; ++l) acc = cadd(acc, cmul(X(i, l), trafo(l, j)));
+        M[i + d * j] = acc;
+      }
+    for (int j = 0; j < d; ++j)  // Y = diag(x) - T^H M
+      for (int i = 0; i < d; ++i) {
+        cd acc = mk(0, 0);
+        for (int l = 0; l < d; ++l) acc = cadd(acc, cmul(cconj(trafo(l, i)), M[l + d * j]));
+        cd dg = mk(0, 0);
+        if (i == j) dg = mk(cdiv_re(xw[k](i, i), w(i, i)), 0);
+        Y[i + d * j] = csub(dg, acc);
+      }
+    for (int j = 0; j < d; ++j)  // Z = Y Y
+      for (int i = 0; i < d; ++i) {
+        cd acc = mk(0, 0);
+        for (int l = 0; l < d; ++l) acc = cadd(acc, cmul(Y[i + d * l], Y[l + d * j]));
+        Z[i + d * j] = acc;
+      }
+    double tr = 0;  // Re tr(W Z)
+    for (int i = 0; i < d; ++i) {
+      cd acc = mk(0, 0);
+      for (int l = 0; l < d; ++l) acc = cadd(acc, cmul(w(i, l), Z[l + d * i]));
+      tr += acc.r;
+    }
+    return tr;
+  }
+  double offdiag() const {
+    double part[32] = {0};
+    for (int k = 0; k < n; ++k) part[k % 32] += offdiag_one(k);
+    return warp_sum(part);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+// LayerGrid, several matrices (src/DVR/TDDVR.cpp:72-88) with
+// WeightedSimultaneousDiagonalization::calculate (:5-53, :369-377):
+//   w = regularize(W, 1e-9); shift_k = |tr X_k|; X_k -= shift_k;
+//   Xw_k = (X_k w + w X_k) / 2; sweeps of weighted Jacobi rotations until the
+//   weighted off-diagonality or its change drops below eps (at most 25);
+//   grid_k(i) = Re(Xw_k(i,i) / w(i,i)) + shift_k;  trafo_out = T^dagger.
+// X: n matrices d x d (complex128, column-major, interleaved); W: d x d.
+// info[0] = sweeps run, info[1] = converged.
+int orc_layer_grid(int n, int d, const double* X, const double* W, double eps, double* trafo_out,
+                   double* grid, int* info) {
+  if (n < 1 || d < 1) return 1;
+  Problem P;
+  P.n = n;
+  P.d = d;
+  P.w.d = d;
+  P.w.a.assign((const cd*)W, (const cd*)W + (size_t)d * d);
+  for (int i = 0; i < d; ++i) {  // regularize (include/Core/Matrix_Implementation.h:717-725)
+    cd& x = P.w(i, i);
+    x.r += 1e-9 * std::exp(-cabs_(x) / 1e-9);
+  }
+  std::vector<double> shift(n);
+  P.xp.resize(n);
+  for (int k = 0; k < n; ++k) {
+    Mat& m = P.xp[k];
+    m.d = d;
+    m.a.assign((const cd*)X + (size_t)k * d * d, (const cd*)X + (size_t)(k + 1) * d * d);
+    cd tr = mk(0, 0);  // calculateShift (src/DVR/TDDVR.cpp:32-39)
+    for (int i = 0; i < d; ++i) tr = cadd(tr, m(i, i));
+    shift[k] = cabs_(tr);
+    for (int i = 0; i < d; ++i) m(i, i).r -= shift[k];
+  }
+  P.trafo.d = d;
+  P.trafo.a.assign((size_t)d * d, mk(0, 0));
+  for (int i = 0; i < d; ++i) P.trafo(i, i) = mk(1, 0);
+  // weightMatrices (src/Core/JacobiRotationFramework.cpp:104-112): (X W + W X) / 2
+  P.xw.resize(n);
+  for (int k = 0; k < n; ++k) {
+    Mat& o = P.xw[k];
+    o.d = d;
+    o.a.assign((size_t)d * d, mk(0, 0));
+    const Mat& x = P.xp[k];
+    for (int j = 0; j < d; ++j)
+      for (int i = 0; i < d; ++i) {
+        cd xw = mk(0, 0), wx = mk(0, 0);
+        for (int l = 0; l < d; ++l) {
+          xw = cadd(xw, cmul(x(i, l), P.w(l, j)));
+          wx = cadd(wx, cmul(P.w(i, l), x(l, j)));
+        }
+        const cd sum = cadd(xw, wx);
+        o(i, j) = mk(0.5 * sum.r, 0.5 * sum.i);
+      }
+  }
+  double delta = P.offdiag();
+  int iter = 0;
+  bool converged = false;
+  while (!converged && iter < 25) {
+    P.rotations();
+    const double delta_last = delta;
+    delta = P.offdiag();
+    const double change = std::fabs(delta_last - delta);
+    if (delta < eps || change < eps) converged = true;
+    iter++;
+  }
+  for (int k = 0; k < n; ++k)
+    for (int i = 0; i < d; ++i) grid[(size_t)k * d + i] = cdiv_re(P.xw[k](i, i), P.w(i, i)) + shift[k];
+  cd* T = (cd*)trafo_out;
+  for (int j = 0; j < d; ++j)
+    for (int i = 0; i < d; ++i) T[i + (size_t)d * j] = cconj(P.trafo(j, i));
+  if (info) {
+    info[0] = iter;
+    info[1] = converged ? 1 : 0;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -17,7 +17,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqtgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-SOURCES = ["qt_api.cu", "qt_kernels.cu", "qt_plan.cpp"]  # qt_plan_export.cpp: host-only lib
+SOURCES = ["qt_api.cu", "qt_kernels.cu", "qt_plan.cpp", "qt_cdvr_plan.cpp",
+           "qt_wsd.cu"]  # qt_plan_export.cpp: host-only lib
+# per-file flags: the simultaneous diagonalisation follows a fixed operation
+# order without fused multiply-adds (its CPU restatement does the same)
+EXTRA = {"qt_wsd.cu": ["-fmad=false"]}
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 
@@ -38,7 +42,7 @@ def _stale(target: str) -> bool:
 def _compile(src: str, verbose: bool) -> str:
     obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
     cmd = [NVCC, *ARCH, "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC",
-           "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
+           *EXTRA.get(src, []), "-I", INCLUDE, "-c", os.path.join(CSRC, src), "-o", obj]
     if src.endswith(".cpp"):
         cmd[cmd.index("-c"):cmd.index("-c")] = ["-x", "cu"]
     if verbose:
@@ -78,7 +82,8 @@ def build_plan_lib(force: bool = False) -> str:
     cuda_inc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "include")
     tmp = PLAN_LIB + ".tmp"
     cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-I", cuda_inc, "-I", INCLUDE,
-           os.path.join(CSRC, "qt_plan.cpp"), os.path.join(CSRC, "qt_plan_export.cpp"), "-o", tmp]
+           os.path.join(CSRC, "qt_plan.cpp"), os.path.join(CSRC, "qt_cdvr_plan.cpp"),
+           os.path.join(CSRC, "qt_plan_export.cpp"), "-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"g++ failed for the planner library:\n{r.stderr}")

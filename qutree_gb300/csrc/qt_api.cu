@@ -31,6 +31,8 @@ struct qt_ctx {
   std::vector<qt::NodeGeo> nodes;
   qt::OpTable ops;
   qt::SopDesc sop;
+  qt::CdvrDesc cdvr;  // potential of a Hamiltonian with hasV (qt_cdvr_upload)
+  bool have_cdvr = false;
   double eps = 1e-10;
   Plan plan;
   double2* buf[qt::B_NBUF] = {nullptr};
@@ -243,6 +245,43 @@ int qt_sop_upload(qt_ctx* c, int n_ops, const int* op_kind, const int* op_dim, c
   return QT_OK;
 }
 
+int qt_cdvr_upload(qt_ctx* c, int n_modes, const int* leaf_dim, const double* leaf_x, int n_terms,
+                   const double* coeff, const int* term_ptr, const int* term_mode, const int* term_power,
+                   int flags) {
+  if (!c || !leaf_dim || !leaf_x || (n_terms > 0 && (!coeff || !term_ptr || !term_mode || !term_power)))
+    return fail(c, QT_ERR_ARG, "null argument");
+  if (n_modes < 2 || n_terms < 0) return fail(c, QT_ERR_ARG, "qt_cdvr_upload: bad counts");
+  qt::CdvrDesc d;
+  int64_t off = 0;
+  for (int m = 0; m < n_modes; ++m) {
+    if (leaf_dim[m] < 1) return fail(c, QT_ERR_SHAPE, "qt_cdvr_upload: empty leaf grid");
+    d.leaf_x.emplace_back(leaf_x + off, leaf_x + off + leaf_dim[m]);
+    off += leaf_dim[m];
+    if (!finite_all(d.leaf_x.back().data(), leaf_dim[m]))
+      return fail(c, QT_ERR_NUMERIC, "qt_cdvr_upload: non-finite grid point");
+  }
+  if (n_terms > 0 && term_ptr[0] != 0) return fail(c, QT_ERR_ARG, "qt_cdvr_upload: term_ptr[0] != 0");
+  for (int q = 0; q < n_terms; ++q) {
+    if (term_ptr[q + 1] < term_ptr[q]) return fail(c, QT_ERR_ARG, "qt_cdvr_upload: term_ptr not ascending");
+    d.coeff.push_back(coeff[q]);
+  }
+  if (!finite_all(d.coeff.data(), (int64_t)d.coeff.size()))
+    return fail(c, QT_ERR_NUMERIC, "qt_cdvr_upload: non-finite coefficient");
+  d.ptr.assign(term_ptr, term_ptr + (n_terms > 0 ? n_terms + 1 : 0));
+  if (n_terms == 0) d.ptr.push_back(0);
+  const int nf = n_terms > 0 ? term_ptr[n_terms] : 0;
+  for (int q = 0; q < nf; ++q) {
+    if (term_mode[q] < 0 || term_mode[q] >= n_modes) return fail(c, QT_ERR_ARG, "qt_cdvr_upload: mode out of range");
+    if (term_power[q] < 0 || term_power[q] > 64) return fail(c, QT_ERR_ARG, "qt_cdvr_upload: power out of range");
+    d.mode.push_back(term_mode[q]);
+    d.power.push_back(term_power[q]);
+  }
+  d.aligned = (flags & QT_CDVR_ALIGNED_HOLE_GRIDS) != 0;
+  c->cdvr = std::move(d);
+  c->have_cdvr = true;
+  return QT_OK;
+}
+
 int qt_set_regularization(qt_ctx* c, double eps) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!(eps > 0) || !std::isfinite(eps)) return fail(c, QT_ERR_ARG, "eps must be positive and finite");
@@ -257,7 +296,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
   const int prec = (flavour & QT_PREC_DF64) ? 1 : 0;
   const bool grad = (flavour & QT_PLAN_GRADIENT) != 0;
   const bool scf = (flavour & QT_PLAN_SCF) != 0;
-  flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT | QT_PLAN_SCF);
+  const bool cdvr = (flavour & QT_PLAN_CDVR) != 0;
+  flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT | QT_PLAN_SCF | QT_PLAN_CDVR);
+  if (cdvr && !c->have_cdvr) return fail(c, QT_ERR_STATE, "QT_PLAN_CDVR needs qt_cdvr_upload first");
   if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED && flavour != QT_PLAN_COMPRESSED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
   QT_CUDA(c, cudaSetDevice(c->device));
@@ -267,7 +308,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
     long v = std::atol(s);
     if (v > 0) budget = (int64_t)v * (1 << 20) / 16;
   }
-  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour | (scf ? 0x2000 : 0), prec, budget, grad);
+  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour | (scf ? 0x2000 : 0), prec, budget,
+                                   grad, cdvr ? &c->cdvr : nullptr);
   if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
   Plan& P = c->plan;
   c->buf_elems[qt::B_PSI] = P.psi_arena;
@@ -284,6 +326,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_KEEP] = P.keep_size;
   c->buf_elems[qt::B_HPW] = P.hpw_size;
   c->buf_elems[qt::B_KRY] = P.kry_size;
+  c->buf_elems[qt::B_CDVR] = P.cdvr ? P.cdvr_size : 0;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
@@ -432,6 +475,74 @@ int qt_prepare(qt_ctx* c, int flavour) {
   for (auto& m : P.mm) mmt.push_back(qt::MMTask{mptr_of(c, m.out), m.d, m.first, m.count, m.trans_b});
   std::vector<qt::MMTerm> mmterms;
   for (auto& m : P.mm_terms) mmterms.push_back(qt::MMTerm{ptr_of(c, m.A), ptr_of(c, m.B)});
+  // CDVR tables
+  std::vector<qt::TCTask> tct;
+  for (auto& x : P.tc) {
+    qt::TCTask t;
+    t.A = ptr_of(c, x.A);
+    t.B = ptr_of(c, x.B);
+    t.C = mptr_of(c, x.C);
+    t.alpha = x.alpha;
+    t.M0 = x.M0;
+    t.M1 = x.M1;
+    t.N0 = x.N0;
+    t.N1 = x.N1;
+    t.K0 = x.K0;
+    t.K1 = x.K1;
+    t.conjA = x.conjA;
+    t.conjB = x.conjB;
+    t.add = x.add;
+    t.pad = 0;
+    t.am0 = x.am0;
+    t.am1 = x.am1;
+    t.ak0 = x.ak0;
+    t.ak1 = x.ak1;
+    t.bk0 = x.bk0;
+    t.bk1 = x.bk1;
+    t.bn0 = x.bn0;
+    t.bn1 = x.bn1;
+    t.cm0 = x.cm0;
+    t.cm1 = x.cm1;
+    t.cn0 = x.cn0;
+    t.cn1 = x.cn1;
+    tct.push_back(t);
+  }
+  std::vector<qt::GSTask> gst;
+  for (auto& x : P.gs) gst.push_back(qt::GSTask{ptr_of(c, x.in), ptr_of(c, x.noise), mptr_of(c, x.out), x.rows, x.cols});
+  std::vector<qt::EigFTask> eft;
+  for (auto& x : P.eigf)
+    eft.push_back(qt::EigFTask{ptr_of(c, x.A), mptr_of(c, x.out), mptr_of(c, x.U), mptr_of(c, x.W), mptr_of(c, x.vals),
+                               x.eps, x.d, x.fn});
+  std::vector<qt::WSDTask> wst;
+  for (auto& x : P.wsd)
+    wst.push_back(qt::WSDTask{ptr_of(c, x.W), mptr_of(c, x.trafo), mptr_of(c, x.grid), mptr_of(c, x.scratch), x.d, x.n,
+                              x.first, 0});
+  std::vector<qt::WSDTerm> wsterms;
+  for (auto& x : P.wsd_terms) wsterms.push_back(qt::WSDTerm{ptr_of(c, x)});
+  std::vector<qt::VPotTask> vpt;
+  for (auto& x : P.vpot) {
+    qt::VPotTask t;
+    t.out = mptr_of(c, x.out);
+    t.n = x.n;
+    t.order = x.order;
+    t.first = x.first;
+    for (int i = 0; i < 6; ++i) t.dims[i] = x.dims[i];
+    vpt.push_back(t);
+  }
+  std::vector<qt::VCoord> vco;
+  for (auto& x : P.vcoords) vco.push_back(qt::VCoord{ptr_of(c, x.grid), x.index, 0});
+  std::vector<qt::PotTerm> pterms;
+  std::vector<qt::PotFactor> pfacts;
+  if (P.cdvr) {
+    for (size_t q = 0; q < c->cdvr.coeff.size(); ++q)
+      pterms.push_back(qt::PotTerm{c->cdvr.coeff[q], c->cdvr.ptr[q], c->cdvr.ptr[q + 1] - c->cdvr.ptr[q]});
+    for (size_t q = 0; q < c->cdvr.mode.size(); ++q) pfacts.push_back(qt::PotFactor{c->cdvr.mode[q], c->cdvr.power[q]});
+  }
+  std::vector<qt::DVLTask> dvt;
+  for (auto& x : P.dvl)
+    dvt.push_back(qt::DVLTask{ptr_of(c, x.cup), ptr_of(c, x.vnode), ptr_of(c, x.vedge), mptr_of(c, x.dv), x.bef, x.d});
+  std::vector<qt::EWTask> ewt;
+  for (auto& x : P.ew) ewt.push_back(qt::EWTask{ptr_of(c, x.v), ptr_of(c, x.in), mptr_of(c, x.out), x.n, x.add, 0});
   std::vector<char> blob;
   std::vector<int64_t> offs;
   put(blob, offs, mp);
@@ -451,6 +562,21 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, mmt);
   put(blob, offs, mmterms);
   put(blob, offs, P.mm_tiles);
+  put(blob, offs, tct);
+  put(blob, offs, P.tc_tiles);
+  put(blob, offs, gst);
+  put(blob, offs, eft);
+  put(blob, offs, wst);
+  put(blob, offs, wsterms);
+  put(blob, offs, vpt);
+  put(blob, offs, vco);
+  put(blob, offs, P.vpot_tiles);
+  put(blob, offs, pterms);
+  put(blob, offs, pfacts);
+  put(blob, offs, dvt);
+  put(blob, offs, P.dvl_tiles);
+  put(blob, offs, ewt);
+  put(blob, offs, P.ew_tiles);
   {
     cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -480,6 +606,29 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.mm = (qt::MMTask*)(base + offs[14]);
   c->tables.mm_terms = (qt::MMTerm*)(base + offs[15]);
   c->tables.mm_tiles = (int2*)(base + offs[16]);
+  c->tables.tc = (qt::TCTask*)(base + offs[17]);
+  c->tables.tc_tiles = (int4*)(base + offs[18]);
+  c->tables.gs = (qt::GSTask*)(base + offs[19]);
+  c->tables.eigf = (qt::EigFTask*)(base + offs[20]);
+  c->tables.wsd = (qt::WSDTask*)(base + offs[21]);
+  c->tables.wsd_terms = (qt::WSDTerm*)(base + offs[22]);
+  c->tables.vpot = (qt::VPotTask*)(base + offs[23]);
+  c->tables.vcoords = (qt::VCoord*)(base + offs[24]);
+  c->tables.vpot_tiles = (int2*)(base + offs[25]);
+  c->tables.pot_terms = (qt::PotTerm*)(base + offs[26]);
+  c->tables.pot_factors = (qt::PotFactor*)(base + offs[27]);
+  c->tables.n_pot_terms = (int)pterms.size();
+  c->tables.n_modes = (int)c->cdvr.leaf_x.size();
+  c->tables.dvl = (qt::DVLTask*)(base + offs[28]);
+  c->tables.dvl_tiles = (int2*)(base + offs[29]);
+  c->tables.ew = (qt::EWTask*)(base + offs[30]);
+  c->tables.ew_tiles = (int2*)(base + offs[31]);
+  if (P.cdvr) {  // CDVR constants: seeded noise, leaf grids, identity
+    QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_CDVR], 0, c->buf_elems[qt::B_CDVR] * 16, c->stream));
+    for (auto& init : P.cdvr_init)
+      QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_CDVR] + init.first, init.second.data(), init.second.size() * 16,
+                                 cudaMemcpyHostToDevice, c->stream));
+  }
   for (auto& id : P.identities) {
     cudaError_t e = qt::launch_set_identity(c->buf[qt::B_MATS] + id.first, id.second, prec, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "set identity");
@@ -813,6 +962,7 @@ int64_t qt_matrices_size(const qt_ctx* c, int which) {
       for (int a : nodes) s += (int64_t)P.nodes[a].dup() * P.nodes[a].dup();
     return s;
   }
+  if (which == QT_MAT_CDVR) return P.cdvr ? P.cdvr_size : -1;
   return -1;
 }
 
@@ -820,6 +970,12 @@ int qt_matrices_download(qt_ctx* c, int which, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   const Plan& P = c->plan;
+  if (which == QT_MAT_CDVR) {
+    if (!P.cdvr) return fail(c, QT_ERR_STATE, "plan prepared without QT_PLAN_CDVR");
+    QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_CDVR], P.cdvr_size * 16, cudaMemcpyDeviceToHost, c->stream));
+    QT_CUDA(c, cudaStreamSynchronize(c->stream));
+    return QT_OK;
+  }
   if ((which == QT_MAT_HMAT || which == QT_MAT_HCON) && !P.per_term_mats)
     return fail(c, QT_ERR_STATE, "the compressed plan keeps no per-term matrices");
   std::vector<double2> mats(P.mats_size);

@@ -120,7 +120,109 @@ struct GradTask {
   int d, write_alpha;
 };
 
-enum StageKind { ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD, ST_MM };
+// ---- CDVR (potential on time-dependent grids) -----------------------------
+// Strided complex contraction, the workhorse of the CDVR stages:
+//   C[m, n] = alpha * sum_k opA(A)[m, k] opB(B)[k, n]  (+ C[m, n] when add)
+// with two-level indices m = (m0, m1), n = (n0, n1), k = (k0, k1); the
+// element of A at (m, k) sits at m0*am0 + m1*am1 + k0*ak0 + k1*ak1 (B, C
+// alike).  opX conjugates when conjX.  Covers mode products (plain,
+// transposed, adjoint matrices), hole products, double-hole contractions,
+// the d^4 x d^2 corrections and matrix products.
+struct TCTask {
+  const double2* A;
+  const double2* B;
+  double2* C;
+  double2 alpha;
+  int M0, M1, N0, N1, K0, K1;
+  int conjA, conjB, add, pad;
+  int64_t am0, am1, ak0, ak1;
+  int64_t bk0, bk1, bn0, bn1;
+  int64_t cm0, cm1, cn0, cn1;
+};
+constexpr int kTcTile = 32;  // output tile (kTcTile x kTcTile) of one block
+
+// out = gramSchmidt(in + noise) on the (rows x cols) matrix view of a node
+struct GSTask {
+  const double2* in;
+  const double2* noise;
+  double2* out;
+  int rows, cols;
+};
+
+// Spectral function of a Hermitian d x d matrix: out = U f(lambda) U^dagger.
+// fn: 0 regularised inverse 1/(l + eps e^(-l/eps)); 1 sqrt(max(l, 0));
+// 2 regularised inverse of the square root (g = sqrt(max(l, 0)));
+// 3 regularised square root g + eps e^(-g/eps); 4 eigenvectors only:
+// out = U^dagger and vals = ascending eigenvalues (real parts).
+struct EigFTask {
+  const double2* A;
+  double2* out;
+  double2* U;     // d x d scratch
+  double2* W;     // d x d scratch
+  double2* vals;  // fn 4: d eigenvalues
+  double eps;
+  int d, fn;
+};
+
+// Weighted simultaneous diagonalisation of n Hermitian matrices with weight
+// W (LayerGrid with several matrices): trafo = T^dagger, grid = n x d values;
+// scratch holds 2n + 2 matrices.  The matrices are terms [first, first + n).
+struct WSDTask {
+  const double2* W;
+  double2* trafo;
+  double2* grid;
+  double2* scratch;
+  int d, n, first, pad;
+};
+struct WSDTerm {
+  const double2* X;
+};
+
+// Potential on a grid tensor: element (i_0, ..., i_{order-1}) gets
+// V(x) with x_g = Re grid_g[i_{index_g}] for the f coordinates g
+// (coords [first, first + f)).  V is the polynomial term table.
+struct VCoord {
+  const double2* grid;
+  int index, pad;
+};
+struct VPotTask {
+  double2* out;
+  int64_t n;
+  int order, first;
+  int dims[6];
+};
+struct PotTerm {
+  double c;
+  int first, count;  // factors [first, first + count)
+};
+struct PotFactor {
+  int mode, power;
+};
+
+// Local part of the CDVR correction tensor of an edge:
+//   dv(l1, i0, m1, i0) = sum_b conj(cup(b, l1)) vnode(b, i0) cup(b, m1),
+//   dv(l0, l1, l0, l1) -= vedge(l0, l1), zero elsewhere.
+struct DVLTask {
+  const double2* cup;
+  const double2* vnode;
+  const double2* vedge;
+  double2* dv;
+  int bef, d;
+};
+
+// out[i] = (add ? out[i] : 0) + v[i] * in[i]
+struct EWTask {
+  const double2* v;
+  const double2* in;
+  double2* out;
+  int64_t n;
+  int add, pad;
+};
+
+enum StageKind {
+  ST_MP = 0, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD, ST_MM,
+  ST_TC, ST_GS, ST_EIGF, ST_WSD, ST_VPOT, ST_DVL, ST_EW
+};
 
 struct Stage {
   int kind;
@@ -147,9 +249,11 @@ struct Stage {
 // B_HPW: partial tiles of hole products split over their reduction index.
 // B_KRY: input and output tensor of the SCF effective Hamiltonian (2 x the
 // largest node).
+// B_CDVR: everything of the CDVR potential (grids, transformations, node and
+// edge potentials, correction tensors, their scratch and constants).
 enum Buf {
   B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY,
-  B_NBUF
+  B_CDVR, B_NBUF
 };
 
 struct Ref {
@@ -277,6 +381,77 @@ struct Plan {
   };
   std::vector<SMM> mm;
   std::vector<SMMTerm> mm_terms;
+  // CDVR stages (symbolic)
+  struct STC {
+    Ref A, B, C;
+    double2 alpha;
+    int M0, M1, N0, N1, K0, K1;
+    int conjA, conjB, add;
+    int64_t am0, am1, ak0, ak1, bk0, bk1, bn0, bn1, cm0, cm1, cn0, cn1;
+  };
+  struct SGS {
+    Ref in, noise, out;
+    int rows, cols;
+  };
+  struct SEigF {
+    Ref A, out, U, W, vals;
+    double eps;
+    int d, fn;
+  };
+  struct SWSD {
+    Ref W, trafo, grid, scratch;
+    int d, n, first;
+  };
+  struct SVCoord {
+    Ref grid;
+    int index;
+  };
+  struct SVPot {
+    Ref out;
+    int64_t n;
+    int order, first;
+    int dims[6];
+  };
+  struct SDVL {
+    Ref cup, vnode, vedge, dv;
+    int bef, d;
+  };
+  struct SEW {
+    Ref v, in, out;
+    int64_t n;
+    int add;
+  };
+  std::vector<STC> tc;
+  std::vector<int4> tc_tiles;  // (task, m tile, n tile, 0)
+  std::vector<SGS> gs;
+  std::vector<SEigF> eigf;
+  std::vector<SWSD> wsd;
+  std::vector<Ref> wsd_terms;
+  std::vector<SVPot> vpot;
+  std::vector<SVCoord> vcoords;
+  std::vector<int2> vpot_tiles;  // (task, first element)
+  std::vector<SDVL> dvl;
+  std::vector<int2> dvl_tiles;
+  std::vector<SEW> ew;
+  std::vector<int2> ew_tiles;
+  bool cdvr = false;
+  int64_t cdvr_size = 0;
+  // constant contents of B_CDVR written at prepare (offset, values)
+  std::vector<std::pair<int64_t, std::vector<double2>>> cdvr_init;
+  // offsets of the CDVR quantities (per node; -1 where absent)
+  struct CdvrLayout {
+    // per node (-1 where absent)
+    std::vector<int64_t> noise, chi, at, cup, cdown, vnode, xi, vx, tmpa, tmpb;
+    std::vector<int64_t> rho_chi, isq, trafo, htrafo, sqrt_rho, binv, g, sqrho, lm, edge1, edges,
+        vedge, dv;
+    std::vector<int64_t> grid, hgrid;  // grid values of the node / hole problem (n x d)
+    std::vector<std::vector<int>> grid_modes, hole_modes;  // X-matrix modes of the two problems
+    std::vector<std::vector<int64_t>> xmat, xhole_raw, xhole, xt;  // [mode][node]
+    std::vector<int64_t> leafx;  // per mode: its DVR grid (complex, real part)
+    std::vector<std::vector<int64_t>> corr_x, corr_y;  // [node][child]: hole and corrected matrix of apply
+    int64_t identity_top = -1;
+  } cd;
+  int64_t cdvr_update_begin = 0, cdvr_update_end = 0;  // stage range of CDVR::Update
   std::vector<int2> mm_tiles;  // (task, first output element), 256 outputs per tile
   bool want_grad = false;
   std::vector<Stage> stages;
@@ -317,12 +492,27 @@ struct SopDesc {
   std::vector<int> ptr, mode, op;
 };
 
+// Potential of a Hamiltonian with hasV (CDVR): the DVR grid of every leaf
+// (per mode, its leaf dimension) and a polynomial V(x) = sum_t c_t prod x_g^p.
+struct CdvrDesc {
+  std::vector<std::vector<double>> leaf_x;
+  std::vector<double> coeff;
+  std::vector<int> ptr, mode, power;
+  bool aligned = false;  // hole grids by mode instead of the reference's rank order
+};
+
+// CDVR stages (qt_cdvr_plan.cpp): part 0 lays out B_CDVR and emits the
+// stages of CDVR::Update, part 1 the stages of CDVR::apply that add to
+// B_HPHI.  Returns the executed flops of the emitted stages.
+double cdvr_plan(Plan& P, const CdvrDesc& D, int part);
+
 // planner entry point; returns "" on success or an error message
 // flavour: 0 reference call sequence, 1 grouped; prec: 0 complex128, 1 double-float;
 // grad: also compute the energy gradient with respect to every node tensor
+// cdvr: the potential of a Hamiltonian with hasV (nullptr: pure SOP)
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
                        const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems,
-                       bool grad = false);
+                       bool grad = false, const CdvrDesc* cdvr = nullptr);
 
 // kernel launches (qt_kernels.cu)
 struct DevTables {
@@ -345,6 +535,22 @@ struct DevTables {
   MMTerm* mm_terms = nullptr;
   int2* mm_tiles = nullptr;
   const int4* hp_segs = nullptr;  // host array: (rows, cols, first tile, tile count)
+  TCTask* tc = nullptr;
+  int4* tc_tiles = nullptr;
+  GSTask* gs = nullptr;
+  EigFTask* eigf = nullptr;
+  WSDTask* wsd = nullptr;
+  WSDTerm* wsd_terms = nullptr;
+  VPotTask* vpot = nullptr;
+  VCoord* vcoords = nullptr;
+  int2* vpot_tiles = nullptr;
+  PotTerm* pot_terms = nullptr;
+  PotFactor* pot_factors = nullptr;
+  int n_pot_terms = 0, n_modes = 0;
+  DVLTask* dvl = nullptr;
+  int2* dvl_tiles = nullptr;
+  EWTask* ew = nullptr;
+  int2* ew_tiles = nullptr;
 };
 // prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe
 cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d, int prec,
@@ -395,6 +601,9 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
                         cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
+// weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
+cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n,
+                       cudaStream_t s);
 cudaError_t probe_df64_peak(cudaStream_t s, double* tflops);
 
 }  // namespace qt

@@ -598,100 +598,13 @@ __device__ __forceinline__ void rr_pair(int m, int r, int i, int& p, int& q) {
   }
 }
 
-__device__ __forceinline__ void eig_body(const EigTask& t, double eps) {
-  extern __shared__ double2 smem[];
-  const int d = t.d;
+// Cyclic Jacobi on the Hermitian d x d matrix A (shared memory): A becomes
+// diagonal (the eigenvalues), U (global) the eigenvectors, A_in = U A U^dagger.
+// Scratch: rot / ph (np each), pq (2 np), red_off / red_diag (kThreads each).
+__device__ void herm_jacobi(double2* A, double2* U, int d, double2* rot, double2* ph, int* pq,
+                            double* red_off, double* red_diag) {
   const int m = d + (d & 1);
   const int np = m / 2;
-  double2* A = smem;                      // d*d
-  double2* rot = A + (int64_t)d * d;      // np entries: (c, s)
-  double2* ph = rot + np;                 // np entries: e
-  double2* fw = ph + np;                  // m entries: f(eigenvalue) in .x
-  int* pq = (int*)(fw + m);               // 2*np
-  __shared__ double red_off[kThreads], red_diag[kThreads];
-  double2* U = t.U;
-  for (int e = threadIdx.x; e < d * d; e += kThreads) {
-    const int i = e % d, j = e / d;
-    const double2 aij = t.rho[i + (int64_t)d * j], aji = t.rho[j + (int64_t)d * i];
-    // Hermitian part
-    A[e] = (i == j) ? make_double2(aij.x, 0.0)
-                    : make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
-    // shifted copy for the positive-definiteness certificate below
-    U[e] = (i == j) ? make_double2(A[e].x - 100.0 * eps, 0.0) : A[e];
-  }
-  __syncthreads();
-  // Fast path.  If every eigenvalue exceeds 50*eps, eps*exp(-w/eps) changes
-  // 1/w by less than 4e-24 relative, so the regularised inverse is the plain
-  // inverse.  A Cholesky factorisation of rho - 100*eps*I that succeeds
-  // certifies that bound (its backward error, ~d*2^-53*|rho|, is far below
-  // 50*eps for eps = 1e-10 and normalised states); then rho^-1 comes from a
-  // Gauss-Jordan inversion (no pivoting needed for a positive definite
-  // matrix) in O(d^3) instead of a Jacobi eigensolver.
-  __shared__ int not_pd;
-  __shared__ double2 piv_s;
-  if (threadIdx.x == 0) not_pd = 0;
-  __syncthreads();
-  for (int k = 0; k < d; ++k) {
-    const double dk = U[k + (int64_t)d * k].x;
-    if (!(dk > 0.0)) {
-      if (threadIdx.x == 0) not_pd = 1;
-      break;  // uniform: every thread reads the same value
-    }
-    const double l = sqrt(dk);
-    __syncthreads();
-    for (int i = k + threadIdx.x; i < d; i += kThreads) {
-      double2 v = U[i + (int64_t)d * k];
-      U[i + (int64_t)d * k] = make_double2(v.x / l, v.y / l);
-    }
-    __syncthreads();
-    // trailing update of the lower triangle: U(i,j) -= L(i,k) conj(L(j,k))
-    const int rem = d - k - 1;
-    for (int e = threadIdx.x; e < rem * rem; e += kThreads) {
-      const int i = k + 1 + e % rem, j = k + 1 + e / rem;
-      if (j > i) continue;
-      const double2 li = U[i + (int64_t)d * k], lj = U[j + (int64_t)d * k];
-      double2 u = U[i + (int64_t)d * j];
-      cfma(u, make_double2(-li.x, -li.y), make_double2(lj.x, -lj.y));
-      U[i + (int64_t)d * j] = u;
-    }
-    __syncthreads();
-  }
-  __syncthreads();
-  if (!not_pd) {
-    double2* X = t.rhoinv;
-    for (int e = threadIdx.x; e < d * d; e += kThreads)
-      X[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
-    __syncthreads();
-    for (int col = 0; col < d; ++col) {
-      if (threadIdx.x == 0) {
-        const double2 v = A[col + d * col];
-        const double den = v.x * v.x + v.y * v.y;
-        piv_s = make_double2(v.x / den, -v.y / den);
-      }
-      __syncthreads();
-      const double2 pinv = piv_s;
-      for (int j = threadIdx.x; j < d; j += kThreads) {
-        A[col + d * j] = cmul(A[col + d * j], pinv);
-        X[col + (int64_t)d * j] = cmul(X[col + (int64_t)d * j], pinv);
-      }
-      __syncthreads();
-      // column col of A before elimination (fw reused as the factor column)
-      for (int r = threadIdx.x; r < d; r += kThreads) fw[r] = A[r + d * col];
-      __syncthreads();
-      for (int e = threadIdx.x; e < d * d; e += kThreads) {
-        const int r = e % d, j = e / d;
-        if (r == col) continue;
-        const double2 f = fw[r];
-        double2 a = A[e], x = X[e];
-        cfma(a, make_double2(-f.x, -f.y), A[col + d * j]);
-        cfma(x, make_double2(-f.x, -f.y), X[col + (int64_t)d * j]);
-        A[e] = a;
-        X[e] = x;
-      }
-      __syncthreads();
-    }
-    return;
-  }
   for (int e = threadIdx.x; e < d * d; e += kThreads) U[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
   __syncthreads();
   for (int sweep = 0; sweep < 40; ++sweep) {
@@ -800,6 +713,103 @@ __device__ __forceinline__ void eig_body(const EigTask& t, double eps) {
       __syncthreads();
     }
   }
+}
+
+__device__ __forceinline__ void eig_body(const EigTask& t, double eps) {
+  extern __shared__ double2 smem[];
+  const int d = t.d;
+  const int m = d + (d & 1);
+  const int np = m / 2;
+  double2* A = smem;                      // d*d
+  double2* rot = A + (int64_t)d * d;      // np entries: (c, s)
+  double2* ph = rot + np;                 // np entries: e
+  double2* fw = ph + np;                  // m entries: f(eigenvalue) in .x
+  int* pq = (int*)(fw + m);               // 2*np
+  __shared__ double red_off[kThreads], red_diag[kThreads];
+  double2* U = t.U;
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int i = e % d, j = e / d;
+    const double2 aij = t.rho[i + (int64_t)d * j], aji = t.rho[j + (int64_t)d * i];
+    // Hermitian part
+    A[e] = (i == j) ? make_double2(aij.x, 0.0)
+                    : make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
+    // shifted copy for the positive-definiteness certificate below
+    U[e] = (i == j) ? make_double2(A[e].x - 100.0 * eps, 0.0) : A[e];
+  }
+  __syncthreads();
+  // Fast path.  If every eigenvalue exceeds 50*eps, eps*exp(-w/eps) changes
+  // 1/w by less than 4e-24 relative, so the regularised inverse is the plain
+  // inverse.  A Cholesky factorisation of rho - 100*eps*I that succeeds
+  // certifies that bound (its backward error, ~d*2^-53*|rho|, is far below
+  // 50*eps for eps = 1e-10 and normalised states); then rho^-1 comes from a
+  // Gauss-Jordan inversion (no pivoting needed for a positive definite
+  // matrix) in O(d^3) instead of a Jacobi eigensolver.
+  __shared__ int not_pd;
+  __shared__ double2 piv_s;
+  if (threadIdx.x == 0) not_pd = 0;
+  __syncthreads();
+  for (int k = 0; k < d; ++k) {
+    const double dk = U[k + (int64_t)d * k].x;
+    if (!(dk > 0.0)) {
+      if (threadIdx.x == 0) not_pd = 1;
+      break;  // uniform: every thread reads the same value
+    }
+    const double l = sqrt(dk);
+    __syncthreads();
+    for (int i = k + threadIdx.x; i < d; i += kThreads) {
+      double2 v = U[i + (int64_t)d * k];
+      U[i + (int64_t)d * k] = make_double2(v.x / l, v.y / l);
+    }
+    __syncthreads();
+    // trailing update of the lower triangle: U(i,j) -= L(i,k) conj(L(j,k))
+    const int rem = d - k - 1;
+    for (int e = threadIdx.x; e < rem * rem; e += kThreads) {
+      const int i = k + 1 + e % rem, j = k + 1 + e / rem;
+      if (j > i) continue;
+      const double2 li = U[i + (int64_t)d * k], lj = U[j + (int64_t)d * k];
+      double2 u = U[i + (int64_t)d * j];
+      cfma(u, make_double2(-li.x, -li.y), make_double2(lj.x, -lj.y));
+      U[i + (int64_t)d * j] = u;
+    }
+    __syncthreads();
+  }
+  __syncthreads();
+  if (!not_pd) {
+    double2* X = t.rhoinv;
+    for (int e = threadIdx.x; e < d * d; e += kThreads)
+      X[e] = make_double2((e % d) == (e / d) ? 1.0 : 0.0, 0.0);
+    __syncthreads();
+    for (int col = 0; col < d; ++col) {
+      if (threadIdx.x == 0) {
+        const double2 v = A[col + d * col];
+        const double den = v.x * v.x + v.y * v.y;
+        piv_s = make_double2(v.x / den, -v.y / den);
+      }
+      __syncthreads();
+      const double2 pinv = piv_s;
+      for (int j = threadIdx.x; j < d; j += kThreads) {
+        A[col + d * j] = cmul(A[col + d * j], pinv);
+        X[col + (int64_t)d * j] = cmul(X[col + (int64_t)d * j], pinv);
+      }
+      __syncthreads();
+      // column col of A before elimination (fw reused as the factor column)
+      for (int r = threadIdx.x; r < d; r += kThreads) fw[r] = A[r + d * col];
+      __syncthreads();
+      for (int e = threadIdx.x; e < d * d; e += kThreads) {
+        const int r = e % d, j = e / d;
+        if (r == col) continue;
+        const double2 f = fw[r];
+        double2 a = A[e], x = X[e];
+        cfma(a, make_double2(-f.x, -f.y), A[col + d * j]);
+        cfma(x, make_double2(-f.x, -f.y), X[col + (int64_t)d * j]);
+        A[e] = a;
+        X[e] = x;
+      }
+      __syncthreads();
+    }
+    return;
+  }
+  herm_jacobi(A, U, d, rot, ph, pq, red_off, red_diag);
   for (int i = threadIdx.x; i < d; i += kThreads) {
     const double w = A[i + d * i].x;
     fw[i].x = 1.0 / (w + eps * exp(-w / eps));
@@ -1254,6 +1264,311 @@ cudaError_t launch_hp_one_shape(const HPTask& t, int ntiles, double2* ws, cudaSt
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// CDVR kernels (complex128)
+// ---------------------------------------------------------------------------
+// Strided complex contraction (TCTask): one block per 32 x 32 output tile,
+// k in chunks of 16 staged through shared memory.  Operand tiles are read
+// along whichever of their two indices has unit stride.
+constexpr int kTcK = 16;
+__global__ void __launch_bounds__(kThreads) k_tc(const TCTask* __restrict__ tasks,
+                                                 const int4* __restrict__ tiles, int64_t tile0) {
+  const int4 tl = tiles[tile0 + blockIdx.x];
+  const TCTask t = tasks[tl.x];
+  const int64_t M = (int64_t)t.M0 * t.M1, N = (int64_t)t.N0 * t.N1, K = (int64_t)t.K0 * t.K1;
+  const int64_t mb = (int64_t)tl.y * kTcTile, nb = (int64_t)tl.z * kTcTile;
+  __shared__ double2 As[kTcK][kTcTile + 1];
+  __shared__ double2 Bs[kTcK][kTcTile + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double2 acc[2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) acc[i][j] = cz();
+  const bool a_mfast = t.am0 == 1 || t.M0 * (int64_t)t.M1 == 1;
+  const bool b_nfast = t.bn0 == 1 || t.N0 * (int64_t)t.N1 == 1;
+  for (int64_t k0 = 0; k0 < K; k0 += kTcK) {
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      const int e = threadIdx.x + r * kThreads;  // 512 elements of each tile
+      int mi, ki;
+      if (a_mfast) {
+        mi = e & 31;
+        ki = e >> 5;
+      } else {
+        ki = e & 15;
+        mi = e >> 4;
+      }
+      const int64_t m = mb + mi, k = k0 + ki;
+      double2 v = cz();
+      if (m < M && k < K) {
+        const int64_t m0 = m % t.M0, m1 = m / t.M0, kk0 = k % t.K0, kk1 = k / t.K0;
+        v = t.A[m0 * t.am0 + m1 * t.am1 + kk0 * t.ak0 + kk1 * t.ak1];
+        if (t.conjA) v.y = -v.y;
+      }
+      As[ki][mi] = v;
+      int ni, kj;
+      if (b_nfast) {
+        ni = e & 31;
+        kj = e >> 5;
+      } else {
+        kj = e & 15;
+        ni = e >> 4;
+      }
+      const int64_t nn = nb + ni, kb = k0 + kj;
+      double2 w = cz();
+      if (nn < N && kb < K) {
+        const int64_t n0 = nn % t.N0, n1 = nn / t.N0, kk0 = kb % t.K0, kk1 = kb / t.K0;
+        w = t.B[kk0 * t.bk0 + kk1 * t.bk1 + n0 * t.bn0 + n1 * t.bn1];
+        if (t.conjB) w.y = -w.y;
+      }
+      Bs[kj][ni] = w;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < kTcK; ++kk) {
+      const double2 a0 = As[kk][ty * 2], a1 = As[kk][ty * 2 + 1];
+      const double2 b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
+      cfma(acc[0][0], a0, b0);
+      cfma(acc[0][1], a0, b1);
+      cfma(acc[1][0], a1, b0);
+      cfma(acc[1][1], a1, b1);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int64_t m = mb + ty * 2 + i, nn = nb + tx * 2 + j;
+      if (m >= M || nn >= N) continue;
+      const int64_t off = (m % t.M0) * t.cm0 + (m / t.M0) * t.cm1 + (nn % t.N0) * t.cn0 + (nn / t.N0) * t.cn1;
+      const double2 v = cmul(t.alpha, acc[i][j]);
+      if (t.add) {
+        const double2 o = t.C[off];
+        t.C[off] = make_double2(o.x + v.x, o.y + v.y);
+      } else {
+        t.C[off] = v;
+      }
+    }
+}
+
+__device__ double2 block_sum2(double2 v, double2* red) {
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      red[threadIdx.x].x += red[threadIdx.x + s].x;
+      red[threadIdx.x].y += red[threadIdx.x + s].y;
+    }
+    __syncthreads();
+  }
+  const double2 r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// out = gramSchmidt(in + noise) (include/Core/Tensor_Implementation.h:805-853):
+// per column, up to 15 passes of projection on the previous columns and
+// normalisation, while the summed |overlap| of a pass exceeds 1e-12.
+__global__ void __launch_bounds__(kThreads) k_gs(const GSTask* __restrict__ tasks, int64_t task0) {
+  const GSTask t = tasks[task0 + blockIdx.x];
+  __shared__ double2 red[kThreads];
+  const int64_t rows = t.rows;
+  const int64_t tot = rows * t.cols;
+  for (int64_t e = threadIdx.x; e < tot; e += kThreads) {
+    const double2 a = t.in[e], z = t.noise[e];
+    t.out[e] = make_double2(a.x + z.x, a.y + z.y);
+  }
+  __syncthreads();
+  double2* A = t.out;
+  for (int n = 0; n < t.cols; ++n) {
+    double2* an = A + rows * n;
+    for (int iter = 0; iter < 15; ++iter) {
+      double accum = 0;
+      for (int m = 0; m < n; ++m) {
+        const double2* am = A + rows * m;
+        double2 part = cz();
+        for (int64_t i = threadIdx.x; i < rows; i += kThreads) cfmac(part, am[i], an[i]);
+        const double2 ov = block_sum2(part, red);
+        accum += sqrt(ov.x * ov.x + ov.y * ov.y);
+        for (int64_t i = threadIdx.x; i < rows; i += kThreads) {
+          const double2 x = cmul(ov, am[i]);
+          an[i] = make_double2(an[i].x - x.x, an[i].y - x.y);
+        }
+        __syncthreads();
+      }
+      double2 part = cz();
+      for (int64_t i = threadIdx.x; i < rows; i += kThreads) part.x += an[i].x * an[i].x + an[i].y * an[i].y;
+      const double nrm = block_sum2(part, red).x;
+      if (nrm != 0.0) {
+        const double sc = sqrt(nrm);
+        for (int64_t i = threadIdx.x; i < rows; i += kThreads) an[i] = make_double2(an[i].x / sc, an[i].y / sc);
+      }
+      __syncthreads();
+      if (!(accum > 1e-12)) break;
+    }
+  }
+}
+
+inline int64_t eigf_smem_bytes(int d) { return eig_smem_bytes(d) + 4 * (int64_t)(d + 1) + 16; }
+
+// spectral functions of a Hermitian matrix (EigFTask)
+__global__ void __launch_bounds__(kThreads) k_eigf(const EigFTask* __restrict__ tasks, int64_t task0) {
+  extern __shared__ double2 smem[];
+  const EigFTask t = tasks[task0 + blockIdx.x];
+  const int d = t.d;
+  const int m = d + (d & 1);
+  const int np = m / 2;
+  double2* A = smem;
+  double2* rot = A + (int64_t)d * d;
+  double2* ph = rot + np;
+  double2* fw = ph + np;
+  int* pq = (int*)(fw + m);
+  int* perm = pq + 2 * np;
+  __shared__ double red_off[kThreads], red_diag[kThreads];
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int i = e % d, j = e / d;
+    const double2 aij = t.A[i + (int64_t)d * j], aji = t.A[j + (int64_t)d * i];
+    A[e] = (i == j) ? make_double2(aij.x, 0.0) : make_double2(0.5 * (aij.x + aji.x), 0.5 * (aij.y - aji.y));
+  }
+  __syncthreads();
+  herm_jacobi(A, t.U, d, rot, ph, pq, red_off, red_diag);
+  __syncthreads();
+  const double2* U = t.U;
+  if (t.fn == 4) {
+    if (threadIdx.x == 0) {  // ascending order of the eigenvalues
+      for (int i = 0; i < d; ++i) perm[i] = i;
+      for (int i = 0; i < d; ++i) {
+        int best = i;
+        for (int j = i + 1; j < d; ++j)
+          if (A[perm[j] + d * perm[j]].x < A[perm[best] + d * perm[best]].x) best = j;
+        const int x = perm[i];
+        perm[i] = perm[best];
+        perm[best] = x;
+      }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < d * d; e += kThreads) {
+      const int i = e % d, j = e / d;
+      const double2 u = U[j + (int64_t)d * perm[i]];
+      t.out[e] = make_double2(u.x, -u.y);
+    }
+    for (int i = threadIdx.x; i < d; i += kThreads) t.vals[i] = make_double2(A[perm[i] + d * perm[i]].x, 0.0);
+    return;
+  }
+  const double eps = t.eps;
+  for (int i = threadIdx.x; i < d; i += kThreads) {
+    const double w = A[i + d * i].x;
+    double f;
+    if (t.fn == 0) {
+      f = 1.0 / (w + eps * exp(-w / eps));
+    } else {
+      const double g = sqrt(fmax(w, 0.0));
+      if (t.fn == 1)
+        f = g;
+      else if (t.fn == 2)
+        f = 1.0 / (g + eps * exp(-g / eps));
+      else
+        f = g + eps * exp(-g / eps);
+    }
+    fw[i].x = f;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < d * d; e += kThreads) {
+    const int i = e % d, j = e / d;
+    double2 acc = cz();
+    for (int k = 0; k < d; ++k) {
+      const double2 uik = U[i + (int64_t)d * k];
+      const double2 ujk = U[j + (int64_t)d * k];
+      const double fk = fw[k].x;
+      cfma(acc, make_double2(uik.x * fk, uik.y * fk), make_double2(ujk.x, -ujk.y));
+    }
+    t.out[e] = acc;
+  }
+}
+
+// polynomial potential on grid tensors (VPotTask): terms in order, each
+// product left to right, nothing fused (the CPU restatement does the same)
+__global__ void __launch_bounds__(kThreads) k_vpot(const VPotTask* __restrict__ tasks,
+                                                   const VCoord* __restrict__ coords,
+                                                   const int2* __restrict__ tiles, int64_t tile0,
+                                                   const PotTerm* __restrict__ terms,
+                                                   const PotFactor* __restrict__ factors, int n_terms) {
+  const int2 tl = tiles[tile0 + blockIdx.x];
+  const VPotTask t = tasks[tl.x];
+  const int64_t e = (int64_t)tl.y + threadIdx.x;
+  if (e >= t.n) return;
+  int idx[6];
+  int64_t r = e;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    if (k < t.order) {
+      idx[k] = (int)(r % t.dims[k]);
+      r /= t.dims[k];
+    } else {
+      idx[k] = 0;
+    }
+  }
+  double v = 0.0;
+  for (int q = 0; q < n_terms; ++q) {
+    const PotTerm pt = terms[q];
+    double tv = pt.c;
+    for (int fct = pt.first; fct < pt.first + pt.count; ++fct) {
+      const PotFactor pf = factors[fct];
+      const VCoord c = coords[t.first + pf.mode];
+      const double x = c.grid[idx[c.index]].x;
+      for (int p = 0; p < pf.power; ++p) tv = __dmul_rn(tv, x);
+    }
+    v = __dadd_rn(v, tv);
+  }
+  t.out[e] = make_double2(v, 0.0);
+}
+
+// local part of the correction tensor (DVLTask)
+__global__ void __launch_bounds__(kThreads) k_dvl(const DVLTask* __restrict__ tasks,
+                                                  const int2* __restrict__ tiles, int64_t tile0) {
+  const int2 tl = tiles[tile0 + blockIdx.x];
+  const DVLTask t = tasks[tl.x];
+  const int64_t d = t.d;
+  const int64_t e = (int64_t)tl.y + threadIdx.x;
+  if (e >= d * d * d * d) return;
+  const int64_t l1 = e % d, i0 = e / d % d, m1 = e / (d * d) % d, i3 = e / (d * d * d);
+  double2 v = cz();
+  if (i0 == i3) {
+    const int64_t bef = t.bef;
+    for (int64_t b = 0; b < bef; ++b) {
+      const double2 a = t.cup[b + bef * l1];
+      const double2 x = cmul(make_double2(a.x, -a.y), t.vnode[b + bef * i0]);
+      cfma(v, x, t.cup[b + bef * m1]);
+    }
+  }
+  if (l1 == m1 && i0 == i3) {
+    const double2 ve = t.vedge[l1 + d * i0];
+    v = make_double2(v.x - ve.x, v.y - ve.y);
+  }
+  t.dv[e] = v;
+}
+
+// out = (add ? out : 0) + v * in, elementwise (EWTask)
+__global__ void __launch_bounds__(kThreads) k_ew(const EWTask* __restrict__ tasks,
+                                                 const int2* __restrict__ tiles, int64_t tile0) {
+  const int2 tl = tiles[tile0 + blockIdx.x];
+  const EWTask t = tasks[tl.x];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int64_t e = (int64_t)tl.y + threadIdx.x + (int64_t)q * kThreads;
+    if (e >= t.n) continue;
+    double2 r = cmul(t.v[e], t.in[e]);
+    if (t.add) {
+      const double2 o = t.out[e];
+      r = make_double2(r.x + o.x, r.y + o.y);
+    }
+    t.out[e] = r;
+  }
+}
+
 template <class P>
 cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int max_eig_d,
                            cudaStream_t s) {
@@ -1307,6 +1622,31 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       break;
     case ST_GRAD:
       k_grad<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.grad, st.first_task);
+      break;
+    case ST_TC:
+      k_tc<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.tc, t.tc_tiles, st.first_tile);
+      break;
+    case ST_GS:
+      k_gs<<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.gs, st.first_task);
+      break;
+    case ST_EIGF: {
+      const int64_t sm = eigf_smem_bytes(max_eig_d);
+      cudaError_t e = cudaFuncSetAttribute(k_eigf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      if (e != cudaSuccess) return e;
+      k_eigf<<<(unsigned)st.n_tasks, kThreads, sm, s>>>(t.eigf, st.first_task);
+      break;
+    }
+    case ST_WSD:
+      return launch_wsd(t.wsd, t.wsd_terms, st.first_task, st.n_tasks, s);
+    case ST_VPOT:
+      k_vpot<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.vpot, t.vcoords, t.vpot_tiles, st.first_tile,
+                                                       t.pot_terms, t.pot_factors, t.n_pot_terms);
+      break;
+    case ST_DVL:
+      k_dvl<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.dvl, t.dvl_tiles, st.first_tile);
+      break;
+    case ST_EW:
+      k_ew<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.ew, t.ew_tiles, st.first_tile);
       break;
     default:
       return cudaErrorInvalidValue;

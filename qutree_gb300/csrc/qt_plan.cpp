@@ -86,6 +86,7 @@ class Builder {
   }
 
   void set_scf(bool on) { scf = on; }
+  void set_cdvr(const CdvrDesc* d) { cdvr = d; }
 
   void run() {
     geometry();
@@ -118,7 +119,16 @@ class Builder {
     } else {
       stage_represent();
       stage_meanfield();
+      if (cdvr) {  // CDVR::Update inside build, CDVR::apply added to Apply
+        P.cdvr = true;
+        P.stats.exec_flops += cdvr_plan(P, *cdvr, 0);
+        stage_flops_mark = P.stats.exec_flops;
+      }
       stage_apply();
+      if (cdvr) {
+        P.stats.exec_flops += cdvr_plan(P, *cdvr, 1);
+        stage_flops_mark = P.stats.exec_flops;
+      }
       if (P.want_grad) stage_environment();
       stage_final();
       if (P.want_grad) stage_gradient();
@@ -137,6 +147,7 @@ class Builder {
   const SopDesc& sop;
   bool grouped, compressed;
   bool scf = false;
+  const CdvrDesc* cdvr = nullptr;
   int64_t budget;
   int n = 0, L = 0;
   std::vector<int> tops;  // roots of the forest, ascending
@@ -1945,14 +1956,21 @@ class Builder {
 
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
                        const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems,
-                       bool grad) {
+                       bool grad, const CdvrDesc* cdvr) {
   plan = Plan();
   plan.want_grad = grad;
   try {
     if (prec != 0 && prec != 1) throw std::runtime_error("unknown precision");
     const bool scf = (flavour & 0x2000) != 0;
+    if (cdvr) {
+      if ((flavour & ~0x2000) == 2) throw std::runtime_error("the CDVR potential needs the reference or grouped plan");
+      if (prec != 0) throw std::runtime_error("the CDVR potential runs in complex128 arithmetic");
+      if (scf) throw std::runtime_error("the SCF sweep has no CDVR potential (nor has the reference's)");
+      if (grad) throw std::runtime_error("no energy gradient with the CDVR potential");
+    }
     Builder b(plan, nodes, ops, sop, flavour & ~0x2000, prec, scratch_budget_elems);
     b.set_scf(scf);
+    b.set_cdvr(cdvr);
     b.run();
   } catch (const std::exception& e) {
     return e.what();

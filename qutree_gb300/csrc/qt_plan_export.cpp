@@ -24,11 +24,11 @@ void put_ref(std::vector<int64_t>& v, const qt::Ref& r) {
 
 extern "C" {
 
-void* qtp_build(int n_nodes, const int* order, const int* dims, const int* parent, const int* child_idx,
-                const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
-                const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
-                const int* term_ptr, const int* term_mode, const int* term_op, int flavour,
-                int prec, int64_t budget, char* err, int errlen) {
+static void* build_handle(int n_nodes, const int* order, const int* dims, const int* parent, const int* child_idx,
+                          const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
+                          const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
+                          const int* term_ptr, const int* term_mode, const int* term_op, int flavour,
+                          int prec, int64_t budget, char* err, int errlen, const qt::CdvrDesc* cd) {
   const bool grad = (flavour & 0x1000) != 0;
   flavour &= ~0x1000;
   std::vector<qt::NodeGeo> nodes(n_nodes);
@@ -60,7 +60,7 @@ void* qtp_build(int n_nodes, const int* order, const int* dims, const int* paren
   s.mode.assign(term_mode, term_mode + s.ptr[n_terms]);
   s.op.assign(term_op, term_op + s.ptr[n_terms]);
   Handle* h = new Handle();
-  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, prec, budget, grad);
+  std::string msg = qt::build_plan(h->plan, nodes, ops, s, flavour, prec, budget, grad, cd);
   if (!msg.empty()) {
     if (err && errlen > 0) {
       std::strncpy(err, msg.c_str(), errlen - 1);
@@ -71,6 +71,40 @@ void* qtp_build(int n_nodes, const int* order, const int* dims, const int* paren
   }
   h->plan.ops_size = (int64_t)ops.data.size() / 2;
   return h;
+}
+
+void* qtp_build(int n_nodes, const int* order, const int* dims, const int* parent, const int* child_idx,
+                const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
+                const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
+                const int* term_ptr, const int* term_mode, const int* term_op, int flavour,
+                int prec, int64_t budget, char* err, int errlen) {
+  return build_handle(n_nodes, order, dims, parent, child_idx, leaf_mode, n_ops, op_kind, op_dim, op_off,
+                      op_data, n_terms, coeff, term_ptr, term_mode, term_op, flavour, prec, budget, err,
+                      errlen, nullptr);
+}
+
+// the same with a CDVR potential (arguments of qt_cdvr_upload appended)
+void* qtp_build_cdvr(int n_nodes, const int* order, const int* dims, const int* parent, const int* child_idx,
+                     const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
+                     const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
+                     const int* term_ptr, const int* term_mode, const int* term_op, int flavour, int prec,
+                     int64_t budget, char* err, int errlen, int n_modes, const int* leaf_dim,
+                     const double* leaf_x, int n_pterms, const double* pcoeff, const int* pptr,
+                     const int* pmode, const int* ppow, int flags) {
+  qt::CdvrDesc d;
+  int64_t off = 0;
+  for (int m = 0; m < n_modes; ++m) {
+    d.leaf_x.emplace_back(leaf_x + off, leaf_x + off + leaf_dim[m]);
+    off += leaf_dim[m];
+  }
+  d.coeff.assign(pcoeff, pcoeff + n_pterms);
+  d.ptr.assign(pptr, pptr + n_pterms + 1);
+  d.mode.assign(pmode, pmode + pptr[n_pterms]);
+  d.power.assign(ppow, ppow + pptr[n_pterms]);
+  d.aligned = (flags & 1) != 0;
+  return build_handle(n_nodes, order, dims, parent, child_idx, leaf_mode, n_ops, op_kind, op_dim, op_off,
+                      op_data, n_terms, coeff, term_ptr, term_mode, term_op, flavour, prec, budget, err,
+                      errlen, &d);
 }
 
 void qtp_free(void* h) { delete (Handle*)h; }
@@ -256,6 +290,142 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       dv = {P.stats.ref_flops, P.stats.exec_flops, (double)P.main_end,
             (double)P.stats.rep_chains, (double)P.stats.mf_chains, (double)P.stats.app_chains};
       break;
+    // ---- CDVR ----
+    case 24:
+      for (auto& t : P.tc) {
+        put_ref(v, t.A);
+        put_ref(v, t.B);
+        put_ref(v, t.C);
+        for (int64_t x : {(int64_t)t.M0, (int64_t)t.M1, (int64_t)t.N0, (int64_t)t.N1, (int64_t)t.K0,
+                          (int64_t)t.K1, (int64_t)t.conjA, (int64_t)t.conjB, (int64_t)t.add, t.am0, t.am1,
+                          t.ak0, t.ak1, t.bk0, t.bk1, t.bn0, t.bn1, t.cm0, t.cm1, t.cn0, t.cn1})
+          v.push_back(x);
+      }
+      break;
+    case 25:
+      for (auto& t : P.gs) {
+        put_ref(v, t.in);
+        put_ref(v, t.noise);
+        put_ref(v, t.out);
+        v.push_back(t.rows);
+        v.push_back(t.cols);
+      }
+      break;
+    case 26:
+      for (auto& t : P.eigf) {
+        put_ref(v, t.A);
+        put_ref(v, t.out);
+        put_ref(v, t.U);
+        put_ref(v, t.W);
+        put_ref(v, t.vals);
+        v.push_back(t.d);
+        v.push_back(t.fn);
+      }
+      break;
+    case 27:
+      for (auto& t : P.wsd) {
+        put_ref(v, t.W);
+        put_ref(v, t.trafo);
+        put_ref(v, t.grid);
+        put_ref(v, t.scratch);
+        v.push_back(t.d);
+        v.push_back(t.n);
+        v.push_back(t.first);
+      }
+      break;
+    case 28:
+      for (auto& r : P.wsd_terms) put_ref(v, r);
+      break;
+    case 29:
+      for (auto& t : P.vpot) {
+        put_ref(v, t.out);
+        v.push_back(t.n);
+        v.push_back(t.order);
+        v.push_back(t.first);
+        for (int i = 0; i < 6; ++i) v.push_back(t.dims[i]);
+      }
+      break;
+    case 30:
+      for (auto& t : P.tc) {
+        dv.push_back(t.alpha.x);
+        dv.push_back(t.alpha.y);
+      }
+      break;
+    case 31:
+      for (auto& t : P.eigf) dv.push_back(t.eps);
+      break;
+    case 32:
+      for (auto& init : P.cdvr_init)
+        for (auto& x : init.second) {
+          dv.push_back(x.x);
+          dv.push_back(x.y);
+        }
+      break;
+    case 33:
+      for (auto& c : P.vcoords) {
+        put_ref(v, c.grid);
+        v.push_back(c.index);
+      }
+      break;
+    case 34:
+      for (auto& t : P.dvl) {
+        put_ref(v, t.cup);
+        put_ref(v, t.vnode);
+        put_ref(v, t.vedge);
+        put_ref(v, t.dv);
+        v.push_back(t.bef);
+        v.push_back(t.d);
+      }
+      break;
+    case 35:
+      for (auto& t : P.ew) {
+        put_ref(v, t.v);
+        put_ref(v, t.in);
+        put_ref(v, t.out);
+        v.push_back(t.n);
+        v.push_back(t.add);
+      }
+      break;
+    case 36:
+      for (auto& init : P.cdvr_init) {
+        v.push_back(init.first);
+        v.push_back((int64_t)init.second.size());
+      }
+      break;
+    case 37:
+      v = {P.cdvr ? 1 : 0, P.cdvr_size, P.cdvr_update_begin, P.cdvr_update_end, P.apply_begin};
+      break;
+    case 38:  // per node: CDVR offsets
+      if (P.cdvr)
+        for (size_t a = 0; a < P.nodes.size(); ++a) {
+          const auto& L = P.cd;
+          v.push_back(L.trafo[a]);
+          v.push_back(L.htrafo[a]);
+          v.push_back(L.grid[a]);
+          v.push_back(L.hgrid[a]);
+          v.push_back((int64_t)L.grid_modes[a].size());
+          v.push_back((int64_t)L.hole_modes[a].size());
+          v.push_back(L.vnode[a]);
+          v.push_back(L.vedge[a]);
+          v.push_back(L.dv[a]);
+          v.push_back(L.cup[a]);
+          v.push_back(L.cdown[a]);
+          v.push_back(L.at[a]);
+          v.push_back(L.xi[a]);
+          v.push_back(L.vx[a]);
+        }
+      break;
+    case 39:  // (mode, node, X matrix, raw hole, unweighted hole)
+      if (P.cdvr)
+        for (size_t m = 0; m < P.cd.xmat.size(); ++m)
+          for (size_t a = 0; a < P.nodes.size(); ++a) {
+            v.push_back((int64_t)m);
+            v.push_back((int64_t)a);
+            v.push_back(P.cd.xmat[m][a]);
+            v.push_back(P.cd.xhole_raw[m][a]);
+            v.push_back(P.cd.xhole[m][a]);
+          }
+      break;
     default:
       break;
   }
@@ -268,7 +438,7 @@ const char* qtp_stage_name(void* h, int i) {
   return P.stages[i].name;
 }
 
-static bool is_double_table(int what) { return what >= 15 && what <= 17; }
+static bool is_double_table(int what) { return (what >= 15 && what <= 17) || (what >= 30 && what <= 32); }
 
 int64_t qtp_size(void* h, int what) {
   std::vector<int64_t> v;

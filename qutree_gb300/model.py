@@ -362,6 +362,54 @@ def gram_schmidt(a: np.ndarray) -> np.ndarray:
 
 
 # --------------------------------------------------------------------------
+# Potential (CDVR)
+# --------------------------------------------------------------------------
+class PolyPotential:
+    """Potential of a Hamiltonian with hasV, applied by CDVR: V(x) =
+    sum_t c_t prod_(g, p) x_g^p (a polynomial stands in for the reference's
+    Potential::evaluate callback, include/TreeOperators/Potential.h:9-18).
+    Evaluation: terms in order, each product left to right, as the device
+    kernel does."""
+
+    def __init__(self, n_modes: int, terms):
+        self.f = n_modes
+        self.terms = [(float(c), [(int(g), int(p)) for g, p in fac]) for c, fac in terms]
+
+    def __call__(self, X: np.ndarray) -> np.ndarray:
+        v = np.zeros(X.shape[:-1])
+        for c, fac in self.terms:
+            t = np.full(X.shape[:-1], c)
+            for g, p in fac:
+                for _ in range(p):
+                    t = t * X[..., g]
+            v = v + t
+        return v
+
+    def descriptor(self):
+        """(coeff[n_terms], ptr[n_terms+1], mode[], power[]) for qt_cdvr_upload."""
+        coeff = np.array([c for c, _ in self.terms], dtype=np.float64)
+        ptr = np.zeros(len(self.terms) + 1, dtype=np.int32)
+        modes, pows = [], []
+        for t, (_, fac) in enumerate(self.terms):
+            for g, p in fac:
+                modes.append(g)
+                pows.append(p)
+            ptr[t + 1] = len(modes)
+        return coeff, ptr, np.array(modes, dtype=np.int32), np.array(pows, dtype=np.int32)
+
+    @classmethod
+    def cdvr_model(cls, f: int, coupling: bool = True):
+        """contrib/Hamiltonians/PESs/CDVRModelV/CDVRModelV.cpp:7-28:
+        sum_i omega^2/2 x_i^2 + lambda^2 sum_i x_i x_(i+1 mod f)."""
+        cm = 219474.6313705
+        lam, om = 2000.0 / cm, 4000.0 / cm
+        terms = [(0.5 * om * om, [(i, 2)]) for i in range(f)]
+        if coupling:
+            terms += [(lam * lam, [(i, 1), ((i + 1) % f, 1)]) for i in range(f)]
+        return cls(f, terms)
+
+
+# --------------------------------------------------------------------------
 # Sum-of-products operator
 # --------------------------------------------------------------------------
 class OperatorTable:

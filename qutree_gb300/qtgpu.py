@@ -30,7 +30,9 @@ QT_PREC_F64 = 0x000
 QT_PREC_DF64 = 0x100
 QT_PLAN_GRADIENT = 0x1000
 QT_PLAN_SCF = 0x2000
-QT_MAT_RHO, QT_MAT_RHOINV, QT_MAT_HMAT, QT_MAT_HCON = 0, 1, 2, 3
+QT_PLAN_CDVR = 0x4000
+QT_MAT_RHO, QT_MAT_RHOINV, QT_MAT_HMAT, QT_MAT_HCON, QT_MAT_CDVR = 0, 1, 2, 3, 4
+QT_CDVR_ALIGNED_HOLE_GRIDS = 1
 ERRORS = {1: "QT_ERR_ARG", 2: "QT_ERR_SHAPE", 3: "QT_ERR_ALLOC", 4: "QT_ERR_CUDA",
           5: "QT_ERR_STATE", 6: "QT_ERR_NUMERIC"}
 
@@ -113,6 +115,8 @@ def load(build_if_missing: bool = True):
         "qt_energies": ([_vp, _vp, ctypes.c_int], ctypes.c_int),
         "qt_scf": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp, ctypes.c_int64,
                     ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+        "qt_cdvr_upload": ([_vp, ctypes.c_int, _i32, _vp, ctypes.c_int, _vp, _i32, _i32, _i32,
+                            ctypes.c_int], ctypes.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -135,6 +139,7 @@ def exported_symbols():
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
         "qt_tree_count", "qt_energies", "qt_gradient_download", "qt_psi_save", "qt_psi_load",
         "qt_build", "qt_layer_derivatives", "qt_cmf_propagate", "qt_scf", "qt_probe_df64_peak",
+        "qt_cdvr_upload",
     ]
 
 
@@ -229,7 +234,12 @@ class HamiltonianRepresentation:
     wavefunction it acts on."""
 
     def __init__(self, H: SOP, tree: Tree, flavour: int = QT_PLAN_REFERENCE, eps: float = 1e-10,
-                 device: int = 0, ctx: Context | None = None):
+                 device: int = 0, ctx: Context | None = None, potential=None, leaf_x=None,
+                 aligned_hole_grids: bool = False):
+        """potential (a PolyPotential) with leaf_x (mode -> DVR grid points):
+        the Hamiltonian also has that potential, applied by CDVR."""
+        if potential is not None:
+            flavour |= QT_PLAN_CDVR
         self.tree, self.H, self.flavour = tree, H, flavour
         self.ctx = ctx or Context(device)
         L, h = self.ctx.L, self.ctx.h
@@ -241,6 +251,15 @@ class HamiltonianRepresentation:
         self.ctx.check(L.qt_sop_upload(h, len(kind), kind, odim, ooff, _ptr(odata), len(H),
                                        _ptr(coeff), ptr, modes, opids))
         self.ctx.check(L.qt_set_regularization(h, eps))
+        if potential is not None:
+            f = tree.n_leaves
+            ldim = np.array([len(leaf_x[m]) for m in range(f)], dtype=np.int32)
+            lx = np.ascontiguousarray(np.concatenate([np.asarray(leaf_x[m], float) for m in range(f)]))
+            pc, pp, pm, pw = potential.descriptor()
+            pc = np.ascontiguousarray(pc)
+            self._keep_pot = (lx, pc)
+            self.ctx.check(L.qt_cdvr_upload(h, f, ldim, _ptr(lx), len(pc), _ptr(pc), pp, pm, pw,
+                                            QT_CDVR_ALIGNED_HOLE_GRIDS if aligned_hole_grids else 0))
         self.ctx.check(L.qt_prepare(h, flavour))
         self.n_psi = int(L.qt_psi_size(h))
 

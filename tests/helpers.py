@@ -71,3 +71,44 @@ def deriv_errors(tree, dpsi, ref, rho):
     noise = max((max(float(np.abs(a).max()), float(np.abs(b).max())) for dg, a, b in parts if dg),
                 default=0.0) / scale
     return err, noise
+
+
+def cdvr_device_wsd(tree, arena, xtab, rho_nodes, rtol=1e-10):
+    """Hook for the CDVR oracle's several-matrix grid solve: run the oracle's
+    (bit-fixed) solver on the device's own inputs -- its X matrices (from
+    the CDVR arena, offsets of plan table 39) and its density matrices -- after
+    checking they agree with the oracle's to ``rtol``.  The solver's accept /
+    reject steps make its output discontinuous in its inputs, so parity past
+    the grid step is only meaningful on identical inputs."""
+    import cdvr as C
+    offs = {(int(m), int(a)): (int(xm), int(xr), int(xh)) for m, a, xm, xr, xh in xtab}
+    f = tree.n_leaves
+    calls = []
+
+    def wsd(kind, a, xs, W):
+        d = tree.nodes[a].d_up
+        if kind == "grid":
+            modes = sorted(tree.subtree_modes(a))
+            src = [offs[(m, a)][0] for m in modes]
+        else:
+            modes = [m for m in range(f) if tree.leaf_node[m] != a]
+            src = [offs[(m, a)][2] for m in modes]
+        dev = [arena[o:o + d * d].reshape((d, d), order="F") for o in src]
+        for x, y in zip(dev, xs):
+            assert np.abs(x - y).max() <= rtol * max(np.abs(y).max(), 1e-300)
+        Wd = rho_nodes[a]
+        assert np.abs(Wd - W).max() <= rtol * np.abs(W).max()
+        calls.append((kind, a))
+        return C.layer_grid_multi(dev, Wd)
+    wsd.calls = calls
+    return wsd
+
+
+def node_matrices(tree, flat):
+    """Split a dense per-node matrix download (QT_MAT_RHO layout) into d x d blocks."""
+    out, off = [], 0
+    for n in tree.nodes:
+        d = n.d_up
+        out.append(flat[off:off + d * d].reshape((d, d), order="F"))
+        off += d * d
+    return out

@@ -21,8 +21,9 @@ _i32 = _P(dtype=np.int32, flags="C_CONTIGUOUS")
 _i64 = _P(dtype=np.int64, flags="C_CONTIGUOUS")
 _lib = None
 
-B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY = range(14)
-ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD, ST_MM = range(9)
+B_PSI, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY, B_CDVR = range(15)
+(ST_MP, ST_HP, ST_ACC, ST_LIN, ST_EIG, ST_PROJ, ST_CVT, ST_GRAD, ST_MM,
+ ST_TC, ST_GS, ST_EIGF, ST_WSD, ST_VPOT, ST_DVL, ST_EW) = range(16)
 
 
 def lib():
@@ -38,6 +39,9 @@ def lib():
         L.qtp_size.restype = ctypes.c_int64
         L.qtp_size.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.qtp_get.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.qtp_build_cdvr.restype = ctypes.c_void_p
+        L.qtp_build_cdvr.argtypes = L.qtp_build.argtypes + [
+            ctypes.c_int, _i32, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, _i32, _i32, _i32, ctypes.c_int]
         L.qtp_stage_name.restype = ctypes.c_char_p
         L.qtp_stage_name.argtypes = [ctypes.c_void_p, ctypes.c_int]
         _lib = L
@@ -60,7 +64,9 @@ def repack_ops(kind, dim, off, data):
 
 
 class PlanView:
-    def __init__(self, tree, sop, flavour=0, budget=1 << 28, prec=0):
+    def __init__(self, tree, sop, flavour=0, budget=1 << 28, prec=0, cdvr=None):
+        """cdvr: optional (leaf_x dict mode -> grid, PolyPotential, aligned) of a
+        Hamiltonian with a CDVR potential."""
         L = lib()
         order, dims, parent, child_idx, leaf_mode = tree.descriptor()
         kind, odim, ooff, odata = sop.ops.descriptor()
@@ -69,17 +75,31 @@ class PlanView:
         odata = np.ascontiguousarray(odata)
         coeff = np.ascontiguousarray(coeff)
         err = ctypes.create_string_buffer(512)
-        h = L.qtp_build(tree.n_nodes, order, dims, parent, child_idx, leaf_mode, len(kind), kind,
-                        odim, ooff, odata.ctypes.data, len(sop), coeff.ctypes.data, ptr, modes,
-                        opids, flavour, prec, budget, err, 512)
+        args = (tree.n_nodes, order, dims, parent, child_idx, leaf_mode, len(kind), kind,
+                odim, ooff, odata.ctypes.data, len(sop), coeff.ctypes.data, ptr, modes,
+                opids, flavour, prec, budget, err, 512)
+        self.potential = None
+        if cdvr is None:
+            h = L.qtp_build(*args)
+        else:
+            leaf_x, pot, aligned = cdvr
+            self.potential = pot
+            f = len(leaf_x)
+            ldim = np.array([len(leaf_x[m]) for m in range(f)], dtype=np.int32)
+            lx = np.ascontiguousarray(np.concatenate([np.asarray(leaf_x[m], float) for m in range(f)]))
+            pc, pp, pm, pw = pot.descriptor()
+            pc = np.ascontiguousarray(pc)
+            h = L.qtp_build_cdvr(*args, f, ldim, lx.ctypes.data, len(pc), pc.ctypes.data, pp, pm, pw,
+                                 1 if aligned else 0)
         if not h:
             raise ValueError(err.value.decode())
         self.h = h
         self.tree, self.sop = tree, sop
         self.tables = {}
         widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
-                  20: 6, 22: 6, 23: 4}
-        for what in list(range(14)) + [18, 19, 20, 21, 22, 23]:
+                  20: 6, 22: 6, 23: 4, 24: 27, 25: 8, 26: 12, 27: 11, 28: 2, 29: 11, 33: 3, 34: 10,
+                  35: 8, 36: 2, 38: 14, 39: 5}
+        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 40)):
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -88,7 +108,7 @@ class PlanView:
             if what in widths:
                 a = a.reshape(-1, widths[what])
             self.tables[what] = a
-        for what in (15, 16, 17):
+        for what in (15, 16, 17, 30, 31, 32):
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1))
             if n:
@@ -107,6 +127,10 @@ class PlanView:
         st = self.tables[17]
         self.stats = dict(ref_flops=st[0], exec_flops=st[1], launches=int(st[2]),
                           rep_chains=int(st[3]), mf_chains=int(st[4]), app_chains=int(st[5]))
+        ci = self.tables[37]
+        self.cdvr = bool(ci[0]) if len(ci) else False
+        self.cdvr_size = int(ci[1]) if len(ci) else 0
+        self.tc_alpha = self.tables[30].reshape(-1, 2) @ np.array([1, 1j]) if len(self.tables[30]) else np.zeros(0)
 
     # -- interpreter -------------------------------------------------------
     def run(self, psi_flat, phase=1.0, eps=1e-10, frozen_after=False):
@@ -143,6 +167,13 @@ class PlanView:
             bufs[B_PSI64] = bufs[B_PSI]
             bufs[B_DPSI64] = bufs[B_DPSI]
             bufs[B_GRAD64] = bufs[B_GRAD]
+        cd = np.zeros(max(self.cdvr_size, 16), np.complex128)
+        vals = self.tables[32].reshape(-1, 2) @ np.array([1, 1j]) if len(self.tables[32]) else []
+        pos = 0
+        for off, cnt in self.tables[36]:
+            cd[off:off + cnt] = vals[pos:pos + cnt]
+            pos += cnt
+        bufs.append(cd)
         bufs[B_PARAM][0] = -1j * complex(phase)
         for off, d in self.tables[10]:
             bufs[B_MATS][off:off + d * d] = np.eye(d).ravel(order="F")
@@ -224,6 +255,8 @@ class PlanView:
                     view(r[4], r[5], d * d)[:] = eo - E * view(r[2], r[3], d * d)
                     if r[13]:
                         view(r[10], r[11], 1)[0] = 1.0 / view(r[8], r[9], 1)[0].real
+                elif kind >= ST_TC:
+                    self._cdvr_task(kind, t, view, eps)
                 elif kind == ST_PROJ:
                     r = T[8][t]
                     d = r[12]
@@ -235,6 +268,100 @@ class PlanView:
                     view(r[6], r[7], d * d)[:] = Sinv.ravel(order="F")
                     view(r[8], r[9], d * d)[:] = Pm.ravel(order="F")
                     view(r[10], r[11], d * d)[:] = M2.ravel(order="F")
+
+    # -- CDVR tasks --------------------------------------------------------
+    def _cdvr_task(self, kind, t, view, eps):
+        T = self.tables
+        bufs = self.bufs
+        if kind == ST_TC:
+            r = T[24][t]
+            ab, ao, bb, bo, cb, co = r[:6]
+            M0, M1, N0, N1, K0, K1, cjA, cjB, add = r[6:15]
+            am0, am1, ak0, ak1, bk0, bk1, bn0, bn1, cm0, cm1, cn0, cn1 = r[15:27]
+
+            def ix(e0, s0, e1, s1):
+                return (np.arange(e0)[:, None] * s0 + np.arange(e1)[None, :] * s1).ravel(order="F")
+            mA, kA = ix(M0, am0, M1, am1), ix(K0, ak0, K1, ak1)
+            kB, nB = ix(K0, bk0, K1, bk1), ix(N0, bn0, N1, bn1)
+            mC, nC = ix(M0, cm0, M1, cm1), ix(N0, cn0, N1, cn1)
+            A = bufs[ab][ao + mA[:, None] + kA[None, :]]
+            B = bufs[bb][bo + kB[:, None] + nB[None, :]]
+            if cjA:
+                A = A.conj()
+            if cjB:
+                B = B.conj()
+            res = self.tc_alpha[t] * (A @ B)
+            idx = co + mC[:, None] + nC[None, :]
+            if add:
+                bufs[cb][idx] += res
+            else:
+                bufs[cb][idx] = res
+        elif kind == ST_GS:
+            from qutree_gb300.model import gram_schmidt
+            ib, io, nb, no, ob, oo, rows, cols = T[25][t]
+            a = (view(ib, io, rows * cols) + view(nb, no, rows * cols)).reshape((rows, cols), order="F")
+            view(ob, oo, rows * cols)[:] = gram_schmidt(a).ravel(order="F")
+        elif kind == ST_EIGF:
+            r = T[26][t]
+            d, fn = r[10], r[11]
+            e = T[31][t]
+            A = view(r[0], r[1], d * d).reshape((d, d), order="F")
+            A = 0.5 * (A + A.conj().T)
+            w, U = np.linalg.eigh(A)
+            if fn == 4:
+                view(r[2], r[3], d * d)[:] = U.conj().T.ravel(order="F")
+                view(r[8], r[9], d)[:] = w
+            else:
+                g = np.sqrt(np.maximum(w, 0.0))
+                f = {0: lambda: 1.0 / (w + e * np.exp(-w / e)), 1: lambda: g,
+                     2: lambda: 1.0 / (g + e * np.exp(-g / e)), 3: lambda: g + e * np.exp(-g / e)}[fn]()
+                view(r[2], r[3], d * d)[:] = ((U * f) @ U.conj().T).ravel(order="F")
+        elif kind == ST_WSD:
+            import cdvr as ocdvr
+            r = T[27][t]
+            d, n, first = r[8], r[9], r[10]
+            W = view(r[0], r[1], d * d).reshape((d, d), order="F")
+            xs = []
+            for q in range(first, first + n):
+                xb, xo = T[28][q]
+                xs.append(view(xb, xo, d * d).reshape((d, d), order="F"))
+            Tr, grids, _ = ocdvr.layer_grid_multi(xs, W)
+            view(r[2], r[3], d * d)[:] = Tr.ravel(order="F")
+            view(r[4], r[5], n * d)[:] = np.concatenate(grids)
+        elif kind == ST_VPOT:
+            r = T[29][t]
+            ob, oo, n, order, first = r[:5]
+            dims = tuple(int(x) for x in r[5:5 + order])
+            f = self.potential.f
+            X = np.zeros(dims + (f,))
+            for g in range(f):
+                gb, go, index = T[33][first + g]
+                vals = view(gb, go, dims[index]).real
+                sh = [1] * order
+                sh[index] = dims[index]
+                X[..., g] = np.broadcast_to(vals.reshape(sh), dims)
+            view(ob, oo, n)[:] = self.potential(X).ravel(order="F")
+        elif kind == ST_DVL:
+            cb, co, vb, vo, eb, eo, db, do, bef, d = T[34][t]
+            cu = view(cb, co, bef * d).reshape((bef, d), order="F")
+            vn = view(vb, vo, bef * d).reshape((bef, d), order="F")
+            ve = view(eb, eo, d * d).reshape((d, d), order="F")
+            Tl = np.einsum("bl,bi,bm->lim", cu.conj(), vn, cu)
+            dv = np.zeros((d, d, d, d), np.complex128)
+            for i0 in range(d):
+                dv[:, i0, :, i0] = Tl[:, i0, :]
+            for l0 in range(d):
+                for l1 in range(d):
+                    dv[l0, l1, l0, l1] -= ve[l0, l1]
+            view(db, do, d ** 4)[:] = dv.ravel(order="F")
+        elif kind == ST_EW:
+            vb, vo, ib, io, ob, oo, n, add = T[35][t]
+            res = view(vb, vo, n) * view(ib, io, n)
+            out = view(ob, oo, n)
+            out[:] = out + res if add else res
+
+    def cdvr_arena(self):
+        return self.bufs[B_CDVR].copy()
 
     def dpsi(self):
         return self.bufs[B_DPSI64].copy()
