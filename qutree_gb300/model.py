@@ -703,6 +703,26 @@ def config_problem(cfg: int, seed_base: int = 20261203):
     return tree, sop, psi
 
 
+def cdvr_problem(n_modes: int = 16, p: int = 16, bond: int = 12, seed: int = 20261203,
+                 coupling: bool = True):
+    """Hamiltonian with a CDVR potential: HO-DVR leaves (omega = 4000 cm^-1 in
+    atomic units, as the coupled-oscillator configs use), the kinetic energy
+    of every mode as the SOP part and contrib's CDVRModelV as the potential,
+    on a balanced binary tree.  Returns (tree, sop, psi, leaf_x, potential)."""
+    tree = balanced_tree(n_modes, p, bond)
+    basis = HOBasis(p, omega=4000.0 / 219474.6313705)
+    ops = OperatorTable()
+    kin = ops.add("kin", OP_DENSE, basis.kin.astype(np.complex128))
+    sop = SOP(ops)
+    for m in range(n_modes):
+        ml = MLO()
+        ml.push_back(kin, m)
+        sop.push_back(ml, 1.0)
+    psi = random_wavefunction(tree, seed)
+    leaf_x = {m: basis.x.copy() for m in range(n_modes)}
+    return tree, sop, psi, leaf_x, PolyPotential.cdvr_model(n_modes, coupling)
+
+
 # --------------------------------------------------------------------------
 # Forests: many independent trees in one sweep
 # --------------------------------------------------------------------------
