@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--batch-trees", type=int, default=512,
                     help="trees in the supplementary many-tree batch (0: skip)")
     ap.add_argument("--no-scf", action="store_true", help="skip the supplementary SCF sweep timing")
+    ap.add_argument("--no-cdvr", action="store_true", help="skip the supplementary CDVR sweep timing")
     ap.add_argument("--precision-steps", type=int, default=0,
                     help="CMF steps (dt 0.01) of the double-float vs complex128 study on the "
                          "48..96-bond 64-mode tree (0: skip)")
@@ -423,6 +424,13 @@ def run_ours(args, ws, rank, local):
                            "executed_gflop": hg4.stats()["exec_flops"] / 1e9}
             hg4.close()
 
+    # supplementary: a Hamiltonian with a CDVR potential (QT_PLAN_CDVR): one
+    # sweep = CDVR update (X matrices, grids, potentials on node and edge
+    # grids, correction tensors) + build + derivative with the CDVR term
+    cdvr = None
+    if not args.no_cdvr and rank == 0:
+        cdvr = cdvr_section(args, local, torch)
+
     # optional: double-float against complex128 along a constant-mean-field
     # propagation of the 48..96-bond tree (regularisation 1e-8, dt 0.01)
     precision = None
@@ -505,6 +513,8 @@ def run_ours(args, ws, rank, local):
         line["precision_study"] = precision
     if grad:
         line["gradient"] = grad
+    if cdvr:
+        line["cdvr"] = cdvr
     if not args.no_cpu_baseline and args.config == 1:
         dt, cpu_e, blas = cpu_baseline_sweep(tree, sop, psi)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": os.cpu_count(),
@@ -513,6 +523,94 @@ def run_ours(args, ws, rank, local):
                                           f"{'OpenBLAS' if blas else 'naive loops'}",
                                 "energy_diff": abs(cpu_e - energy)}
     print(json.dumps(line), flush=True)
+
+
+CDVR_KINDS = {0: "k_mp", 1: "k_hp", 2: "k_acc", 3: "k_lin", 4: "k_eig", 5: "k_proj", 9: "k_tc (strided contractions)",
+              10: "k_gs (Gram-Schmidt)", 11: "k_eigf (spectral functions)",
+              12: "k_wsd (joint diagonalisation)", 13: "k_vpot (potential on grids)",
+              14: "k_dvl (local corrections)", 15: "k_ew (V times Xi)"}
+
+
+def cdvr_section(args, local, torch):
+    """16 modes, HO-DVR p = 16, bonds 12, kinetic SOP + contrib's CDVRModelV."""
+    import numpy as np
+
+    from qutree_gb300 import qtgpu
+    from qutree_gb300.model import cdvr_problem
+
+    tree, sop, psi, xs, V = cdvr_problem(16, 16, 12)
+    flat = psi.flat()
+    out = {"workload": "16 modes, HO-DVR p=16, bonds 12, 16 kinetic terms + CDVRModelV(16) potential "
+                       "(32 polynomial terms); one sweep = CDVR update + build + derivative",
+           "metric": "H.Psi sweeps/s with the CDVR potential"}
+    for label, fl in (("grouped", qtgpu.QT_PLAN_GROUPED), ("reference_sequence", qtgpu.QT_PLAN_REFERENCE)):
+        h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=fl, potential=V, leaf_x=xs, device=local)
+        st = torch.cuda.ExternalStream(h.stream())
+        h.upload(flat)
+        for _ in range(2):
+            h.derivative()
+        h.sync()
+        steps = 5
+        n0 = h.ctx.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            h.derivative()
+        e1.record(st)
+        h.sync()
+        ms = e0.elapsed_time(e1) / steps
+        rec = {"ms_per_sweep": ms, "sweeps_per_s": 1e3 / ms, "energy": h.energy(),
+               "gpu_launches_per_sweep": (h.ctx.launch_count() - n0) // steps,
+               "executed_gflop": h.stats()["exec_flops"] / 1e9}
+        if label == "grouped":
+            stages = h.stages()
+            per = {}
+            evs = []
+            for i in range(len(stages)):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(st)
+                h.launch_stage(i)
+                b.record(st)
+                evs.append((a, b))
+            h.sync()
+            for i, (a, b) in enumerate(evs):
+                k = CDVR_KINDS.get(stages[i][0], str(stages[i][0]))
+                d = per.setdefault(k, {"ms": 0.0, "launches": 0})
+                d["ms"] += a.elapsed_time(b)
+                d["launches"] += 1
+            tot = sum(v["ms"] for v in per.values())
+            rec["kernels"] = {k: {"ms": round(v["ms"], 3), "share": round(v["ms"] / tot, 4),
+                                  "launches_per_sweep": v["launches"]} for k, v in per.items()}
+            # end to end through the C ABI: Psi from pinned host memory in, dPsi and the energy back
+            pin_in = torch.empty(flat.size * 2, dtype=torch.float64, pin_memory=True)
+            pin_out = torch.empty(flat.size * 2, dtype=torch.float64, pin_memory=True)
+            pin_in.numpy()[:] = flat.view(np.float64)
+            in_np = pin_in.numpy().view(np.complex128)
+            out_np = pin_out.numpy().view(np.complex128)
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                h.upload(in_np)
+                h.derivative()
+                h.dpsi_into(out_np)
+                h.energy()
+            dt = (time.perf_counter() - t0) / steps
+            rec["e2e"] = {"value": 1.0 / dt, "unit": "sweeps/s", "h2d_bytes_per_step": flat.nbytes,
+                          "d2h_bytes_per_step": flat.nbytes + 32}
+        out[label] = rec
+        h.close()
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import cdvr as cdvr_oracle
+        t0 = time.perf_counter()
+        res = cdvr_oracle.derivative(tree, sop, flat, cdvr_oracle.CDVROracle(tree, xs, V))
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": 1.0 / dt, "unit": "sweeps/s", "cores": 1, "kind": "port",
+                               "sample": "one sweep of the same workload: the oracle's numpy restatement "
+                                         "with its C joint diagonalisation",
+                               "energy": float((res.h00 / res.s00).real),
+                               "note": "energies differ at ~1e-9: the joint diagonalisation's accept/reject "
+                                       "steps make the grids discontinuous in rounding-level input changes"}
+    return out
 
 
 def main():

@@ -12,16 +12,18 @@
 // and the device kernel follows it bit for bit:
 //  * a complex product is (ac - bd) + i(ad + bc), sums are left to right and
 //    nothing is fused (compiled with -ffp-contract=off; the device file with
-//    -fmad=false);
-//  * a sum over the matrices of a problem puts matrix k into partial sum
-//    k mod 32 (ascending k) and adds the 32 partials by the butterfly
-//    v[t] += v[t ^ o] for o = 16, 8, 4, 2, 1 (one warp's shuffle reduction);
+//    -fmad=false); sums over the matrices of a problem run in index order,
+//    as the reference's loops do;
 //  * |z| is sqrt(re^2 + im^2) where the reference calls std::abs (hypot), and
 //    real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
 //  * the 3x3 symmetric eigenproblem of the optimiser (Matrix::rDiag, Eigen's
-//    SelfAdjointEigenSolver in the reference) is cyclic Jacobi; only the
-//    eigenvector of the largest eigenvalue is used, through ratios and its
-//    squared components, which do not depend on the solver's sign choice;
+//    SelfAdjointEigenSolver in the reference) is solved for what the
+//    optimiser uses of it -- the eigenvector of the largest eigenvalue as
+//    ratios v0/v2, v1/v2 and its squared first two components: the largest
+//    root of the characteristic polynomial by Newton's method from the
+//    Gershgorin bound (monotone from above), then v as the largest cross
+//    product of two rows of H - lambda (absolute accuracy like a rotation
+//    method's);
 //  * the two step-size searches stop after 64 rounds at the latest (the
 //    reference's own conditions end them far earlier).
 #include <cmath>
@@ -42,15 +44,6 @@ inline cd cconj(cd a) { return cd{a.r, -a.i}; }
 inline double cabs_(cd a) { return std::sqrt(a.r * a.r + a.i * a.i); }
 inline double cdiv_re(cd x, cd w) { return (x.r * w.r + x.i * w.i) / (w.r * w.r + w.i * w.i); }
 
-double warp_sum(double* v) {
-  for (int o = 16; o > 0; o >>= 1) {
-    double t[32];
-    for (int l = 0; l < 32; ++l) t[l] = v[l] + v[l ^ o];
-    std::memcpy(v, t, sizeof(t));
-  }
-  return v[0];
-}
-
 struct Mat {
   int d;
   std::vector<cd> a;
@@ -58,48 +51,56 @@ struct Mat {
   cd operator()(int i, int j) const { return a[i + (size_t)d * j]; }
 };
 
-// Matrix::rDiag for a symmetric 3x3 matrix: the eigenvector of the largest
-// eigenvalue (cyclic Jacobi, rotations of Golub & Van Loan, sym.schur2).
-void eig3_top(const double H[9], double v[3]) {
-  double A[9], V[9];
-  std::memcpy(A, H, sizeof(A));
-  for (int i = 0; i < 9; ++i) V[i] = (i % 4 == 0) ? 1.0 : 0.0;
-  for (int sweep = 0; sweep < 50; ++sweep) {
-    const double off = A[3] * A[3] + A[6] * A[6] + A[7] * A[7];
-    if (off == 0.0) break;
-    for (int pq = 0; pq < 3; ++pq) {
-      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
-      const double apq = A[p + 3 * q];
-      if (apq == 0.0) continue;
-      const double theta = (A[q + 3 * q] - A[p + 3 * p]) / (2.0 * apq);
-      double t;
-      if (std::fabs(theta) > 1e150)
-        t = 0.5 / theta;
-      else
-        t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-      const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-      for (int k = 0; k < 3; ++k) {  // columns: A <- A J
-        const double akp = A[k + 3 * p], akq = A[k + 3 * q];
-        A[k + 3 * p] = c * akp - s * akq;
-        A[k + 3 * q] = s * akp + c * akq;
-        const double vkp = V[k + 3 * p], vkq = V[k + 3 * q];
-        V[k + 3 * p] = c * vkp - s * vkq;
-        V[k + 3 * q] = s * vkp + c * vkq;
-      }
-      for (int k = 0; k < 3; ++k) {  // rows: A <- J^T A
-        const double apk = A[p + 3 * k], aqk = A[q + 3 * k];
-        A[p + 3 * k] = c * apk - s * aqk;
-        A[q + 3 * k] = s * apk + c * aqk;
-      }
-      A[p + 3 * q] = 0.0;
-      A[q + 3 * p] = 0.0;
-    }
+// Matrix::rDiag for the optimiser's symmetric 3x3 matrix H: the eigenvector
+// v of the largest eigenvalue as the ratios u0 = v0/v2, u1 = v1/v2 and the
+// squared norm of its first two components, v0^2 + v1^2 for |v| = 1.
+extern "C" void orc_eig3_top(const double H[9], double* u0, double* u1, double* top2);
+void eig3_top(const double H[9], double* u0, double* u1, double* top2) { orc_eig3_top(H, u0, u1, top2); }
+}  // namespace
+extern "C" void orc_eig3_top(const double H[9], double* u0, double* u1, double* top2) {
+  const double h00 = H[0], h01 = H[3], h02 = H[6], h11 = H[4], h12 = H[7], h22 = H[8];
+  const double tr = h00 + h11 + h22;
+  const double m = (h00 * h11 - h01 * h01) + (h00 * h22 - h02 * h02) + (h11 * h22 - h12 * h12);
+  const double det = h00 * (h11 * h22 - h12 * h12) - h01 * (h01 * h22 - h12 * h02) + h02 * (h01 * h12 - h11 * h02);
+  // Gershgorin upper bound of the largest eigenvalue
+  double lam = h00 + std::fabs(h01) + std::fabs(h02);
+  const double r1 = h11 + std::fabs(h01) + std::fabs(h12);
+  const double r2 = h22 + std::fabs(h02) + std::fabs(h12);
+  if (r1 > lam) lam = r1;
+  if (r2 > lam) lam = r2;
+  // p(l) = -l^3 + tr l^2 - m l + det; Newton decreases l monotonically to the largest root
+  for (int it = 0; it < 100; ++it) {
+    const double p = ((-lam + tr) * lam - m) * lam + det;
+    const double dp = (-3.0 * lam + 2.0 * tr) * lam - m;
+    if (!(dp < 0.0)) break;
+    const double nxt = lam - p / dp;
+    if (!(nxt < lam)) break;
+    lam = nxt;
   }
-  int top = 0;
-  for (int k = 1; k < 3; ++k)
-    if (A[k + 3 * k] > A[top + 3 * top]) top = k;
-  for (int k = 0; k < 3; ++k) v[k] = V[k + 3 * top];
+  // eigenvector: the largest cross product of two rows of H - lambda
+  const double m00 = h00 - lam, m11 = h11 - lam, m22 = h22 - lam;
+  const double c01[3] = {h01 * h12 - h02 * m11, h02 * h01 - m00 * h12, m00 * m11 - h01 * h01};
+  const double c02[3] = {h01 * m22 - h02 * h12, h02 * h02 - m00 * m22, m00 * h12 - h01 * h02};
+  const double c12[3] = {m11 * m22 - h12 * h12, h12 * h02 - h01 * m22, h01 * h12 - m11 * h02};
+  const double n01 = c01[0] * c01[0] + c01[1] * c01[1] + c01[2] * c01[2];
+  const double n02 = c02[0] * c02[0] + c02[1] * c02[1] + c02[2] * c02[2];
+  const double n12 = c12[0] * c12[0] + c12[1] * c12[1] + c12[2] * c12[2];
+  const double* v = c01;
+  double nv = n01;
+  if (n02 > nv) {
+    v = c02;
+    nv = n02;
+  }
+  if (n12 > nv) {
+    v = c12;
+    nv = n12;
+  }
+  *u0 = v[0] / v[2];
+  *u1 = v[1] / v[2];
+  const double q = v[0] * v[0] + v[1] * v[1];
+  *top2 = q / (q + v[2] * v[2]);
 }
+namespace {
 
 // rotatedDiagonals (src/Core/JacobiRotationFramework.cpp:129-141)
 inline void rotated_diagonals(const Mat& A, int p, int q, cd c, cd s, double& a0, double& a1) {
@@ -121,20 +122,18 @@ struct Problem {
   double loc(int p, int q, cd c, cd s) const {
     double w0, w1;
     rotated_diagonals(w, p, q, c, s, w0, w1);
-    double o0[32] = {0}, o1[32] = {0}, n0[32] = {0}, n1[32] = {0};
+    double xold0 = 0, xold1 = 0, xnew0 = 0, xnew1 = 0;
     for (int k = 0; k < n; ++k) {
       const double x0 = xw[k](p, p).r, x1 = xw[k](q, q).r;
-      o0[k % 32] += x0 * x0;
-      o1[k % 32] += x1 * x1;
+      xold0 += x0 * x0;
+      xold1 += x1 * x1;
     }
     for (int k = 0; k < n; ++k) {
       double r0, r1;
       rotated_diagonals(xw[k], p, q, c, s, r0, r1);
-      n0[k % 32] += r0 * r0;
-      n1[k % 32] += r1 * r1;
+      xnew0 += r0 * r0;
+      xnew1 += r1 * r1;
     }
-    const double xold0 = warp_sum(o0), xold1 = warp_sum(o1);
-    const double xnew0 = warp_sum(n0), xnew1 = warp_sum(n1);
     double diff = 0;
     diff += xnew0 / w0 - xold0 / w(p, p).r;
     diff += xnew1 / w1 - xold1 / w(q, q).r;
@@ -183,7 +182,7 @@ struct Problem {
       int guard = 0;
       while (a > amin && diff < 0 && diff_rel > eps * eps && guard++ < 64) {
         double z = 1;
-        double v[3] = {0, 0, 0};
+        double top2 = 0;
         int guard2 = 0;
         while (a > amin && z > 0.5 && guard2++ < 64) {
           // rfoBuildHessian (src/Core/JacobiRotationFramework.cpp:114-127)
@@ -197,9 +196,10 @@ struct Problem {
           H[5] = grad[1] * a;
           H[7] = grad[1] * a;
           H[8] = 0;
-          eig3_top(H, v);
-          const double ds0 = a * v[0] / v[2];
-          const double ds1 = a * v[1] / v[2];
+          double u0, u1;
+          eig3_top(H, &u0, &u1, &top2);
+          const double ds0 = a * u0;
+          const double ds1 = a * u1;
           snew[0] = s.r + ds0;
           snew[1] = s.i + ds1;
           const double zab = cabs_(mk(snew[0], snew[1]));
@@ -209,7 +209,7 @@ struct Problem {
         cnew[0] = std::sqrt(std::fabs(1 - z));
         cnew[1] = 0;
         loc_new = loc(p, q, mk(cnew[0], cnew[1]), mk(snew[0], snew[1]));
-        const double trafoabs = v[0] * v[0] + v[1] * v[1];
+        const double trafoabs = top2;
         const double sab = cabs_(s);
         const double sabs = sab * sab + eps * eps;
         diff_rel = trafoabs / sabs;
@@ -305,9 +305,9 @@ struct Problem {
     return tr;
   }
   double offdiag() const {
-    double part[32] = {0};
-    for (int k = 0; k < n; ++k) part[k % 32] += offdiag_one(k);
-    return warp_sum(part);
+    double loc = 0;
+    for (int k = 0; k < n; ++k) loc += offdiag_one(k);
+    return loc;
   }
 };
 

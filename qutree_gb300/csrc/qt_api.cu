@@ -619,6 +619,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.pot_factors = (qt::PotFactor*)(base + offs[27]);
   c->tables.n_pot_terms = (int)pterms.size();
   c->tables.n_modes = (int)c->cdvr.leaf_x.size();
+  c->tables.wsd_max_n = P.wsd_max_n;
+  c->tables.wsd_max_d = P.wsd_max_d;
   c->tables.dvl = (qt::DVLTask*)(base + offs[28]);
   c->tables.dvl_tiles = (int2*)(base + offs[29]);
   c->tables.ew = (qt::EWTask*)(base + offs[30]);

@@ -356,9 +356,9 @@ class CdvrBuilder {
     for (int a = 0; a < n; ++a) {
       if (top(a)) continue;
       const int64_t dd = (int64_t)dup(a) * dup(a);
-      // weighted and plain matrices, weight, transformation, 2 d^2 per lane
-      if (L.grid_modes[a].size() > 1) wsd_scr[a].first = take((2 * (int64_t)L.grid_modes[a].size() + 66) * dd);
-      if (L.hole_modes[a].size() > 1) wsd_scr[a].second = take((2 * (int64_t)L.hole_modes[a].size() + 66) * dd);
+      // weighted and plain matrices, weight, transformation, 3 d^2 of products
+      if (L.grid_modes[a].size() > 1) wsd_scr[a].first = take((2 * (int64_t)L.grid_modes[a].size() + 5) * dd);
+      if (L.hole_modes[a].size() > 1) wsd_scr[a].second = take((2 * (int64_t)L.hole_modes[a].size() + 5) * dd);
     }
     hole_t1.assign(f, std::vector<int64_t>(n, -1));
     hole_t2.assign(f, std::vector<int64_t>(n, -1));
@@ -569,6 +569,8 @@ class CdvrBuilder {
         w.first = (int)P.wsd_terms.size();
         for (int m : modes) P.wsd_terms.push_back(cd(kind == 0 ? L.xmat[m][a] : L.xhole[m][a]));
         P.wsd.push_back(w);
+        P.wsd_max_n = std::max(P.wsd_max_n, w.n);
+        P.wsd_max_d = std::max(P.wsd_max_d, w.d);
       }
     }
     emit(ST_WSD, w0, (int64_t)P.wsd.size(), w0, (int64_t)P.wsd.size(), "cdvr-grids-wsd", 0);

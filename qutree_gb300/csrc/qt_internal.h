@@ -436,6 +436,7 @@ struct Plan {
   std::vector<int2> ew_tiles;
   bool cdvr = false;
   int64_t cdvr_size = 0;
+  int wsd_max_n = 0, wsd_max_d = 0;  // largest joint-diagonalisation problem
   // constant contents of B_CDVR written at prepare (offset, values)
   std::vector<std::pair<int64_t, std::vector<double2>>> cdvr_init;
   // offsets of the CDVR quantities (per node; -1 where absent)
@@ -547,6 +548,7 @@ struct DevTables {
   PotTerm* pot_terms = nullptr;
   PotFactor* pot_factors = nullptr;
   int n_pot_terms = 0, n_modes = 0;
+  int wsd_max_n = 0, wsd_max_d = 0;
   DVLTask* dvl = nullptr;
   int2* dvl_tiles = nullptr;
   EWTask* ew = nullptr;
@@ -602,8 +604,9 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
 // weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
-cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n,
-                       cudaStream_t s);
+// max_n / max_d bound the tasks' matrix counts and orders (shared memory)
+cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,
+                       int max_d, cudaStream_t s);
 cudaError_t probe_df64_peak(cudaStream_t s, double* tflops);
 
 }  // namespace qt

@@ -1637,7 +1637,7 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       break;
     }
     case ST_WSD:
-      return launch_wsd(t.wsd, t.wsd_terms, st.first_task, st.n_tasks, s);
+      return launch_wsd(t.wsd, t.wsd_terms, st.first_task, st.n_tasks, t.wsd_max_n, t.wsd_max_d, s);
     case ST_VPOT:
       k_vpot<<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.vpot, t.vcoords, t.vpot_tiles, st.first_tile,
                                                        t.pot_terms, t.pot_factors, t.n_pot_terms);

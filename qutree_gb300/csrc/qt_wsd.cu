@@ -9,25 +9,26 @@
 // function of the inputs; this file therefore fixes one operation order,
 // which the CPU restatement follows bit for bit:
 //  * compiled with -fmad=false: no multiply-add is fused; a complex product
-//    is (ac - bd) + i(ad + bc), sums run left to right;
-//  * a sum over the matrices of a problem: lane t adds matrices t, t + 32,
-//    ... in order, then the lanes are combined by the xor butterfly
-//    (offsets 16, 8, 4, 2, 1), which leaves every lane with the same value;
+//    is (ac - bd) + i(ad + bc), sums run left to right, and sums over the
+//    matrices of a problem in index order (as the reference's loops);
 //  * |z| is sqrt(re^2 + im^2); real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
-//  * the 3x3 symmetric eigenproblem of the optimiser (Matrix::rDiag) is
-//    cyclic Jacobi; only ratios and squares of the eigenvector of the largest
-//    eigenvalue enter, which do not depend on the solver's sign choice.
-// The optimiser's control flow is uniform: every lane holds the same values
-// and runs it redundantly.  All loops are bounded (at most 25 sweeps, 30
-// optimiser iterations, 64 step halvings per search, 50 Jacobi sweeps).
+//  * the optimiser's 3x3 eigenvector (Matrix::rDiag) comes from the largest
+//    root of the characteristic polynomial (Newton from the Gershgorin bound)
+//    and the largest cross product of two rows of H - lambda.
+// Work is spread over the lanes item by item -- the rotated 2x2 diagonal
+// blocks of every matrix at every candidate rotation (nine at once for the
+// finite-difference derivatives), the elements of the matrix products of the
+// off-diagonality measure, the rows and columns of every Givens rotation --
+// and the ordered sums are taken by single lanes from shared memory.  The
+// scalar control flow is uniform (every lane holds the same values).  All
+// loops are bounded (at most 25 sweeps, 30 optimiser iterations, 64 step
+// halvings per search, 100 Newton steps).
 #include <cuda_runtime.h>
 
 #include "qt_internal.h"
 
 namespace qt {
 namespace {
-
-constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ double2 cm(double2 a, double2 b) {
   return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -39,72 +40,74 @@ __device__ __forceinline__ double cabs_(double2 a) { return sqrt(a.x * a.x + a.y
 __device__ __forceinline__ double cdiv_re(double2 x, double2 w) {
   return (x.x * w.x + x.y * w.y) / (w.x * w.x + w.y * w.y);
 }
-__device__ __forceinline__ double warp_sum(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = v + __shfl_xor_sync(kFull, v, o);
-  return v;
-}
 
 struct Prob {
   int d, n;
-  double2* xw;   // n weighted matrices
-  double2* xp;   // n plain (shifted) matrices
-  double2* w;    // weight
-  double2* T;    // transformation
-  double2* tmp;  // 2 d^2 per lane: X T and Y of the off-diagonality measure
-  __device__ double2& at(double2* m, int i, int j) const { return m[i + (int64_t)d * j]; }
+  double2* xw;   // n weighted matrices (global)
+  double2* xp;   // n plain (shifted) matrices (global)
+  double2* w;    // weight (global)
+  double2* T;    // transformation (global)
+  double2* tmp;  // 3 d^2: X T, Y and Y Y of the off-diagonality measure (global)
+  // shared memory
+  double2* blk;  // (n + 1) x 4: (pp, pq, qp, qq) of every matrix and of w at the current pair
+  double* sq;    // 2 x 9 x n: squared rotated diagonals per candidate
+  double* wd;    // 2 x 9: rotated diagonals of w per candidate
+  double2* cand; // 2 x 9: candidate (c, s)
+  double* red;   // 32 + d: xold (0, 1), measure (2), losses (8..16), traces (32..)
   __device__ double2* X(int k) const { return xw + (int64_t)k * d * d; }
   __device__ double2* Xp(int k) const { return xp + (int64_t)k * d * d; }
 };
 
-// Matrix::rDiag of a symmetric 3x3 matrix: eigenvector of the largest eigenvalue
-__device__ void eig3_top(const double H[9], double v[3]) {
-  double A[9], V[9];
-  for (int i = 0; i < 9; ++i) {
-    A[i] = H[i];
-    V[i] = (i % 4 == 0) ? 1.0 : 0.0;
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+
+// Matrix::rDiag of the optimiser's symmetric 3x3 matrix: eigenvector of the
+// largest eigenvalue as u0 = v0/v2, u1 = v1/v2 and v0^2 + v1^2 for |v| = 1
+__device__ void eig3_top(const double H[9], double* u0, double* u1, double* top2) {
+  const double h00 = H[0], h01 = H[3], h02 = H[6], h11 = H[4], h12 = H[7], h22 = H[8];
+  const double tr = h00 + h11 + h22;
+  const double m = (h00 * h11 - h01 * h01) + (h00 * h22 - h02 * h02) + (h11 * h22 - h12 * h12);
+  const double det = h00 * (h11 * h22 - h12 * h12) - h01 * (h01 * h22 - h12 * h02) + h02 * (h01 * h12 - h11 * h02);
+  double lam = h00 + fabs(h01) + fabs(h02);
+  const double r1 = h11 + fabs(h01) + fabs(h12);
+  const double r2 = h22 + fabs(h02) + fabs(h12);
+  if (r1 > lam) lam = r1;
+  if (r2 > lam) lam = r2;
+  for (int it = 0; it < 100; ++it) {
+    const double p = ((-lam + tr) * lam - m) * lam + det;
+    const double dp = (-3.0 * lam + 2.0 * tr) * lam - m;
+    if (!(dp < 0.0)) break;
+    const double nxt = lam - p / dp;
+    if (!(nxt < lam)) break;
+    lam = nxt;
   }
-  for (int sweep = 0; sweep < 50; ++sweep) {
-    const double off = A[3] * A[3] + A[6] * A[6] + A[7] * A[7];
-    if (off == 0.0) break;
-    for (int pq = 0; pq < 3; ++pq) {
-      const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
-      const double apq = A[p + 3 * q];
-      if (apq == 0.0) continue;
-      const double theta = (A[q + 3 * q] - A[p + 3 * p]) / (2.0 * apq);
-      double t;
-      if (fabs(theta) > 1e150)
-        t = 0.5 / theta;
-      else
-        t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-      const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-      for (int k = 0; k < 3; ++k) {
-        const double akp = A[k + 3 * p], akq = A[k + 3 * q];
-        A[k + 3 * p] = c * akp - s * akq;
-        A[k + 3 * q] = s * akp + c * akq;
-        const double vkp = V[k + 3 * p], vkq = V[k + 3 * q];
-        V[k + 3 * p] = c * vkp - s * vkq;
-        V[k + 3 * q] = s * vkp + c * vkq;
-      }
-      for (int k = 0; k < 3; ++k) {
-        const double apk = A[p + 3 * k], aqk = A[q + 3 * k];
-        A[p + 3 * k] = c * apk - s * aqk;
-        A[q + 3 * k] = s * apk + c * aqk;
-      }
-      A[p + 3 * q] = 0.0;
-      A[q + 3 * p] = 0.0;
-    }
+  const double m00 = h00 - lam, m11 = h11 - lam, m22 = h22 - lam;
+  const double c01[3] = {h01 * h12 - h02 * m11, h02 * h01 - m00 * h12, m00 * m11 - h01 * h01};
+  const double c02[3] = {h01 * m22 - h02 * h12, h02 * h02 - m00 * m22, m00 * h12 - h01 * h02};
+  const double c12[3] = {m11 * m22 - h12 * h12, h12 * h02 - h01 * m22, h01 * h12 - m11 * h02};
+  const double n01 = c01[0] * c01[0] + c01[1] * c01[1] + c01[2] * c01[2];
+  const double n02 = c02[0] * c02[0] + c02[1] * c02[1] + c02[2] * c02[2];
+  const double n12 = c12[0] * c12[0] + c12[1] * c12[1] + c12[2] * c12[2];
+  double v0 = c01[0], v1 = c01[1], v2 = c01[2], nv = n01;
+  if (n02 > nv) {
+    v0 = c02[0];
+    v1 = c02[1];
+    v2 = c02[2];
+    nv = n02;
   }
-  int top = 0;
-  for (int k = 1; k < 3; ++k)
-    if (A[k + 3 * k] > A[top + 3 * top]) top = k;
-  for (int k = 0; k < 3; ++k) v[k] = V[k + 3 * top];
+  if (n12 > nv) {
+    v0 = c12[0];
+    v1 = c12[1];
+    v2 = c12[2];
+  }
+  *u0 = v0 / v2;
+  *u1 = v1 / v2;
+  const double q = v0 * v0 + v1 * v1;
+  *top2 = q / (q + v2 * v2);
 }
 
-__device__ __forceinline__ void rotated_diagonals(const Prob& P, const double2* A, int p, int q, double2 c,
-                                                  double2 s, double& a0, double& a1) {
-  const int d = P.d;
-  const double2 App = A[p + (int64_t)d * p], Apq = A[p + (int64_t)d * q];
-  const double2 Aqp = A[q + (int64_t)d * p], Aqq = A[q + (int64_t)d * q];
+// rotatedDiagonals of a cached 2x2 block (pp, pq, qp, qq)
+__device__ __forceinline__ void rotated_diagonals(const double2* b, double2 c, double2 s, double& a0, double& a1) {
+  const double2 App = b[0], Apq = b[1], Aqp = b[2], Aqq = b[3];
   const double2 c00 = ca(cm(c, App), cm(s, Apq));
   const double2 c01 = cs(cm(c, Apq), cm(cc(s), App));
   const double2 c10 = ca(cm(c, Aqp), cm(s, Aqq));
@@ -113,45 +116,67 @@ __device__ __forceinline__ void rotated_diagonals(const Prob& P, const double2* 
   a1 = cs(cm(c, c11), cm(s, c01)).x;
 }
 
-// weightedJacobiLoc
-__device__ double loc(const Prob& P, int p, int q, double2 c, double2 s) {
-  const int lane = threadIdx.x & 31;
-  double w0, w1;
-  rotated_diagonals(P, P.w, p, q, c, s, w0, w1);
-  double o0 = 0, o1 = 0, n0 = 0, n1 = 0;
-  for (int k = lane; k < P.n; k += 32) {
-    const double2* X = P.X(k);
-    const double x0 = X[p + (int64_t)P.d * p].x, x1 = X[q + (int64_t)P.d * q].x;
-    o0 += x0 * x0;
-    o1 += x1 * x1;
-  }
-  for (int k = lane; k < P.n; k += 32) {
+// weightedJacobiLoc for `count` candidates at once (cand[0 .. 2 count)):
+// red[8 + j] = diff of candidate j
+__device__ void loc_many(const Prob& P, int count) {
+  const int n = P.n, lane = lane_id();
+  const int items = count * (n + 1);
+  for (int it = lane; it < items; it += 32) {
+    const int j = it / (n + 1), k = it % (n + 1);
     double r0, r1;
-    rotated_diagonals(P, P.X(k), p, q, c, s, r0, r1);
-    n0 += r0 * r0;
-    n1 += r1 * r1;
+    rotated_diagonals(P.blk + 4 * k, P.cand[2 * j], P.cand[2 * j + 1], r0, r1);
+    if (k < n) {
+      P.sq[j * n + k] = r0 * r0;
+      P.sq[9 * n + j * n + k] = r1 * r1;
+    } else {
+      P.wd[2 * j] = r0;
+      P.wd[2 * j + 1] = r1;
+    }
   }
-  const double xold0 = warp_sum(o0), xold1 = warp_sum(o1);
-  const double xnew0 = warp_sum(n0), xnew1 = warp_sum(n1);
-  double diff = 0;
-  diff += xnew0 / w0 - xold0 / P.w[p + (int64_t)P.d * p].x;
-  diff += xnew1 / w1 - xold1 / P.w[q + (int64_t)P.d * q].x;
-  return diff;
+  __syncwarp();
+  if (lane < count) {
+    const int j = lane;
+    double xnew0 = 0, xnew1 = 0;
+    for (int k = 0; k < n; ++k) {
+      xnew0 += P.sq[j * n + k];
+      xnew1 += P.sq[9 * n + j * n + k];
+    }
+    double diff = 0;
+    diff += xnew0 / P.wd[2 * j] - P.red[0] / P.blk[4 * n + 0].x;
+    diff += xnew1 / P.wd[2 * j + 1] - P.red[1] / P.blk[4 * n + 3].x;
+    P.red[8 + j] = diff;
+  }
+  __syncwarp();
 }
 
-// weightedJacobiDerivatives
-__device__ void derivatives(const Prob& P, double grad[2], double pre[4], double2 s_in, int p, int q,
-                            double delta) {
-  const double s0 = s_in.x, s1 = s_in.y;
+__device__ double loc1(const Prob& P, double2 c, double2 s) {
+  if (lane_id() == 0) {
+    P.cand[0] = c;
+    P.cand[1] = s;
+  }
+  __syncwarp();
+  loc_many(P, 1);
+  const double v = P.red[8];
+  __syncwarp();
+  return v;
+}
+
+// weightedJacobiDerivatives: the nine candidates of the central differences
+__device__ void derivatives(const Prob& P, double grad[2], double pre[4], double2 s_in, double delta) {
+  const int lane = lane_id();
+  if (lane < 9) {
+    const int i = lane % 3, j = lane / 3;
+    const double x0 = s_in.x + (double)(i - 1) * delta;
+    const double x1 = s_in.y + (double)(j - 1) * delta;
+    const double z = x0 * x0 + x1 * x1;
+    P.cand[2 * lane] = make_double2(sqrt(fabs(1 - z)), 0.0);
+    P.cand[2 * lane + 1] = make_double2(x0, x1);
+  }
+  __syncwarp();
+  loc_many(P, 9);
   double y[9];
-  for (int i = 0; i < 3; ++i)
-    for (int j = 0; j < 3; ++j) {
-      const double x0 = s0 + (double)(i - 1) * delta;
-      const double x1 = s1 + (double)(j - 1) * delta;
-      const double z = x0 * x0 + x1 * x1;
-      const double2 cnow = make_double2(sqrt(fabs(1 - z)), 0.0);
-      y[i + 3 * j] = loc(P, p, q, cnow, make_double2(x0, x1));
-    }
+  for (int q = 0; q < 9; ++q) y[q] = P.red[8 + q];
+  __syncwarp();
   grad[0] = (y[2 + 3 * 1] - y[0 + 3 * 1]) / (2 * delta);
   grad[1] = (y[1 + 3 * 2] - y[1 + 3 * 0]) / (2 * delta);
   pre[0] = (y[2 + 3 * 1] + y[0 + 3 * 1] - 2 * y[1 + 3 * 1]) / (delta * delta);
@@ -161,7 +186,7 @@ __device__ void derivatives(const Prob& P, double grad[2], double pre[4], double
 }
 
 // calculateWeightedAngles: rational function optimisation of (c, s)
-__device__ void angles(const Prob& P, double2& c, double2& s, int p, int q) {
+__device__ void angles(const Prob& P, double2& c, double2& s) {
   int iter = 0;
   const int maxiter = 30;
   const double eps = 1E-3;
@@ -172,16 +197,16 @@ __device__ void angles(const Prob& P, double2& c, double2& s, int p, int q) {
   double snew[2] = {0, 0}, cnew[2] = {0, 0};
   c = make_double2(sqrt(1 - 2 * eps * eps), 0);
   s = make_double2(eps, -eps);
-  double loc_alt = loc(P, p, q, c, s);
+  double loc_alt = loc1(P, c, s);
   double loc_new = 0;
   while (iter < maxiter && diff_rel > eps * eps && a > amin) {
     double pre[4], grad[2];
-    derivatives(P, grad, pre, s, p, q, delta);
+    derivatives(P, grad, pre, s, delta);
     double diff = -1;
     int guard = 0;
     while (a > amin && diff < 0 && diff_rel > eps * eps && guard++ < 64) {
       double z = 1;
-      double v[3] = {0, 0, 0};
+      double top2 = 0;
       int guard2 = 0;
       while (a > amin && z > 0.5 && guard2++ < 64) {
         double H[9];
@@ -194,9 +219,10 @@ __device__ void angles(const Prob& P, double2& c, double2& s, int p, int q) {
         H[5] = grad[1] * a;
         H[7] = grad[1] * a;
         H[8] = 0;
-        eig3_top(H, v);
-        const double ds0 = a * v[0] / v[2];
-        const double ds1 = a * v[1] / v[2];
+        double u0, u1;
+        eig3_top(H, &u0, &u1, &top2);
+        const double ds0 = a * u0;
+        const double ds1 = a * u1;
         snew[0] = s.x + ds0;
         snew[1] = s.y + ds1;
         const double zab = cabs_(make_double2(snew[0], snew[1]));
@@ -205,8 +231,8 @@ __device__ void angles(const Prob& P, double2& c, double2& s, int p, int q) {
       }
       cnew[0] = sqrt(fabs(1 - z));
       cnew[1] = 0;
-      loc_new = loc(P, p, q, make_double2(cnew[0], cnew[1]), make_double2(snew[0], snew[1]));
-      const double trafoabs = v[0] * v[0] + v[1] * v[1];
+      loc_new = loc1(P, make_double2(cnew[0], cnew[1]), make_double2(snew[0], snew[1]));
+      const double trafoabs = top2;
       const double sab = cabs_(s);
       const double sabs = sab * sab + eps * eps;
       diff_rel = trafoabs / sabs;
@@ -230,7 +256,7 @@ __device__ void angles(const Prob& P, double2& c, double2& s, int p, int q) {
 __device__ void givens_all(const Prob& P, double2* base, int m_count, int64_t stride, double2 c, double2 s,
                            int i, int j) {
   const int d = P.d;
-  const int lane = threadIdx.x & 31;
+  const int lane = lane_id();
   const int64_t tot = (int64_t)m_count * d;
   for (int64_t e = lane; e < tot; e += 32) {  // columns i, j
     double2* B = base + (e / d) * stride;
@@ -251,13 +277,32 @@ __device__ void givens_all(const Prob& P, double2* base, int m_count, int64_t st
 }
 
 __device__ void rotations(const Prob& P) {
-  const int d = P.d;
-  const int lane = threadIdx.x & 31;
+  const int d = P.d, n = P.n;
+  const int lane = lane_id();
   for (int i = 0; i < d - 1; ++i)
     for (int j = i + 1; j < d; ++j) {
+      for (int k = lane; k <= n; k += 32) {  // cache the (i, j) blocks
+        const double2* A = k < n ? P.X(k) : P.w;
+        P.blk[4 * k + 0] = A[i + (int64_t)d * i];
+        P.blk[4 * k + 1] = A[i + (int64_t)d * j];
+        P.blk[4 * k + 2] = A[j + (int64_t)d * i];
+        P.blk[4 * k + 3] = A[j + (int64_t)d * j];
+      }
+      __syncwarp();
+      if (lane == 0) {  // sum of the current squared diagonals, in matrix order
+        double o0 = 0, o1 = 0;
+        for (int k = 0; k < n; ++k) {
+          const double x0 = P.blk[4 * k].x, x1 = P.blk[4 * k + 3].x;
+          o0 += x0 * x0;
+          o1 += x1 * x1;
+        }
+        P.red[0] = o0;
+        P.red[1] = o1;
+      }
+      __syncwarp();
       double2 c, s;
-      angles(P, c, s, i, j);
-      givens_all(P, P.xw, P.n, (int64_t)d * d, c, s, i, j);
+      angles(P, c, s);
+      givens_all(P, P.xw, n, (int64_t)d * d, c, s, i, j);
       givens_all(P, P.w, 1, 0, c, s, i, j);
       for (int r = lane; r < d; r += 32) {  // givensTrafoRotation
         const double2 ti = P.T[r + (int64_t)d * i], tj = P.T[r + (int64_t)d * j];
@@ -268,43 +313,59 @@ __device__ void rotations(const Prob& P) {
     }
 }
 
-// measureWeightedOffDiagonality: sum_k Re tr(W (D_k - T^H X_k T)^2)
+// measureWeightedOffDiagonality: sum_k Re tr(W (D_k - T^H X_k T)^2), matrix by
+// matrix; the elements of each product in parallel, each an ordered sum
 __device__ double offdiag(const Prob& P) {
-  const int d = P.d;
-  const int lane = threadIdx.x & 31;
-  double2* M = P.tmp + (int64_t)lane * 2 * d * d;
-  double2* Y = M + (int64_t)d * d;
-  double part = 0;
-  for (int k = lane; k < P.n; k += 32) {
+  const int d = P.d, lane = lane_id();
+  const int64_t dd = (int64_t)d * d;
+  double2* M = P.tmp;
+  double2* Y = M + dd;
+  double2* Z = Y + dd;
+  double total = 0;
+  for (int k = 0; k < P.n; ++k) {
     const double2* X = P.Xp(k);
     const double2* Xw = P.X(k);
-    for (int j = 0; j < d; ++j)
-      for (int i = 0; i < d; ++i) {
-        double2 acc = make_double2(0, 0);
-        for (int l = 0; l < d; ++l) acc = ca(acc, cm(X[i + (int64_t)d * l], P.T[l + (int64_t)d * j]));
-        M[i + (int64_t)d * j] = acc;
-      }
-    for (int j = 0; j < d; ++j)
-      for (int i = 0; i < d; ++i) {
-        double2 acc = make_double2(0, 0);
-        for (int l = 0; l < d; ++l) acc = ca(acc, cm(cc(P.T[l + (int64_t)d * i]), M[l + (int64_t)d * j]));
-        double2 dg = make_double2(0, 0);
-        if (i == j) dg = make_double2(cdiv_re(Xw[i + (int64_t)d * i], P.w[i + (int64_t)d * i]), 0);
-        Y[i + (int64_t)d * j] = cs(dg, acc);
-      }
-    double tr = 0;
-    for (int i = 0; i < d; ++i) {
+    for (int64_t e = lane; e < dd; e += 32) {
+      const int i = (int)(e % d), j = (int)(e / d);
       double2 acc = make_double2(0, 0);
-      for (int l = 0; l < d; ++l) {
-        double2 z = make_double2(0, 0);  // (Y Y)(l, i)
-        for (int q = 0; q < d; ++q) z = ca(z, cm(Y[l + (int64_t)d * q], Y[q + (int64_t)d * i]));
-        acc = ca(acc, cm(P.w[i + (int64_t)d * l], z));
-      }
-      tr += acc.x;
+      for (int l = 0; l < d; ++l) acc = ca(acc, cm(X[i + (int64_t)d * l], P.T[l + (int64_t)d * j]));
+      M[e] = acc;
     }
-    part += tr;
+    __syncwarp();
+    for (int64_t e = lane; e < dd; e += 32) {
+      const int i = (int)(e % d), j = (int)(e / d);
+      double2 acc = make_double2(0, 0);
+      for (int l = 0; l < d; ++l) acc = ca(acc, cm(cc(P.T[l + (int64_t)d * i]), M[l + (int64_t)d * j]));
+      double2 dg = make_double2(0, 0);
+      if (i == j) dg = make_double2(cdiv_re(Xw[i + (int64_t)d * i], P.w[i + (int64_t)d * i]), 0);
+      Y[e] = cs(dg, acc);
+    }
+    __syncwarp();
+    for (int64_t e = lane; e < dd; e += 32) {
+      const int i = (int)(e % d), j = (int)(e / d);
+      double2 acc = make_double2(0, 0);
+      for (int l = 0; l < d; ++l) acc = ca(acc, cm(Y[i + (int64_t)d * l], Y[l + (int64_t)d * j]));
+      Z[e] = acc;
+    }
+    __syncwarp();
+    for (int i = lane; i < d; i += 32) {
+      double2 acc = make_double2(0, 0);
+      for (int l = 0; l < d; ++l) acc = ca(acc, cm(P.w[i + (int64_t)d * l], Z[l + (int64_t)d * i]));
+      P.red[32 + i] = acc.x;
+    }
+    __syncwarp();
+    if (lane == 0) {
+      double tr = 0;
+      for (int i = 0; i < d; ++i) tr += P.red[32 + i];
+      total += tr;
+    }
+    __syncwarp();
   }
-  return warp_sum(part);
+  if (lane == 0) P.red[2] = total;
+  __syncwarp();
+  const double v = P.red[2];
+  __syncwarp();
+  return v;
 }
 
 __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, const WSDTerm* __restrict__ terms,
@@ -313,6 +374,7 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
   const int d = t.d, n = t.n;
   const int lane = threadIdx.x;
   const int64_t dd = (int64_t)d * d;
+  extern __shared__ double2 wsd_smem[];
   Prob P;
   P.d = d;
   P.n = n;
@@ -321,6 +383,11 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
   P.w = t.scratch + 2 * n * dd;
   P.T = P.w + dd;
   P.tmp = P.T + dd;
+  P.blk = wsd_smem;
+  P.cand = P.blk + 4 * (n + 1);
+  P.sq = reinterpret_cast<double*>(P.cand + 18);
+  P.wd = P.sq + 18 * n;
+  P.red = P.wd + 18;
   // w = regularize(W, 1e-9), T = 1
   for (int64_t e = lane; e < dd; e += 32) {
     double2 v = t.W[e];
@@ -383,9 +450,19 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
 
 }  // namespace
 
-cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, cudaStream_t s) {
+// shared memory of a problem with n matrices of order d (see Prob)
+int64_t wsd_smem_bytes(int n, int d) {
+  return 16 * (4 * (int64_t)(n + 1) + 18) + 8 * (18 * (int64_t)n + 18 + 32 + d) + 64;
+}
+
+cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,
+                       int max_d, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_wsd<<<(unsigned)n, 32, 0, s>>>(tasks, terms, first);
+  const int64_t sm = wsd_smem_bytes(max_n, max_d);
+  if (sm > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_wsd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k_wsd<<<(unsigned)n, 32, sm, s>>>(tasks, terms, first);
   return cudaGetLastError();
 }
 
