@@ -12,8 +12,10 @@
 // and the device kernel follows it bit for bit:
 //  * a complex product is (ac - bd) + i(ad + bc), sums are left to right and
 //    nothing is fused (compiled with -ffp-contract=off; the device file with
-//    -fmad=false); sums over the matrices of a problem run in index order,
-//    as the reference's loops do;
+//    -fmad=false); a sum over the matrices of a problem is the pairwise tree
+//    of the values padded with zeros to a power of two (level by level,
+//    t[i] = t[2i] + t[2i+1]); the measure adds its per-matrix traces in
+//    index order;
 //  * |z| is sqrt(re^2 + im^2) where the reference calls std::abs (hypot), and
 //    real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
 //  * the 3x3 symmetric eigenproblem of the optimiser (Matrix::rDiag, Eigen's
@@ -43,6 +45,18 @@ inline cd csub(cd a, cd b) { return cd{a.r - b.r, a.i - b.i}; }
 inline cd cconj(cd a) { return cd{a.r, -a.i}; }
 inline double cabs_(cd a) { return std::sqrt(a.r * a.r + a.i * a.i); }
 inline double cdiv_re(cd x, cd w) { return (x.r * w.r + x.i * w.i) / (w.r * w.r + w.i * w.i); }
+
+constexpr int kMaxMats = 256;
+
+double tree_sum(const double* v, int n) {
+  int P = 1;
+  while (P < n) P <<= 1;
+  double t[kMaxMats];
+  for (int i = 0; i < P; ++i) t[i] = i < n ? v[i] : 0.0;
+  for (int s = P; s > 1; s >>= 1)
+    for (int i = 0; i < s / 2; ++i) t[i] = t[2 * i] + t[2 * i + 1];
+  return t[0];
+}
 
 struct Mat {
   int d;
@@ -122,18 +136,20 @@ struct Problem {
   double loc(int p, int q, cd c, cd s) const {
     double w0, w1;
     rotated_diagonals(w, p, q, c, s, w0, w1);
-    double xold0 = 0, xold1 = 0, xnew0 = 0, xnew1 = 0;
+    double o0[kMaxMats], o1[kMaxMats], n0[kMaxMats], n1[kMaxMats];
     for (int k = 0; k < n; ++k) {
       const double x0 = xw[k](p, p).r, x1 = xw[k](q, q).r;
-      xold0 += x0 * x0;
-      xold1 += x1 * x1;
+      o0[k] = x0 * x0;
+      o1[k] = x1 * x1;
     }
     for (int k = 0; k < n; ++k) {
       double r0, r1;
       rotated_diagonals(xw[k], p, q, c, s, r0, r1);
-      xnew0 += r0 * r0;
-      xnew1 += r1 * r1;
+      n0[k] = r0 * r0;
+      n1[k] = r1 * r1;
     }
+    const double xold0 = tree_sum(o0, n), xold1 = tree_sum(o1, n);
+    const double xnew0 = tree_sum(n0, n), xnew1 = tree_sum(n1, n);
     double diff = 0;
     diff += xnew0 / w0 - xold0 / w(p, p).r;
     diff += xnew1 / w1 - xold1 / w(q, q).r;
@@ -325,7 +341,7 @@ extern "C" {
 // info[0] = sweeps run, info[1] = converged.
 int orc_layer_grid(int n, int d, const double* X, const double* W, double eps, double* trafo_out,
                    double* grid, int* info) {
-  if (n < 1 || d < 1) return 1;
+  if (n < 1 || d < 1 || n > kMaxMats) return 1;
   Problem P;
   P.n = n;
   P.d = d;

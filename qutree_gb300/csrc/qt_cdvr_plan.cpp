@@ -218,6 +218,7 @@ class CdvrBuilder {
   void derive() {
     n = (int)nd.size();
     f = (int)D.leaf_x.size();
+    if (f > 256) throw std::runtime_error("CDVR: more than 256 modes");
     int roots = 0;
     for (int a = 0; a < n; ++a) roots += top(a) ? 1 : 0;
     if (roots != 1) throw std::runtime_error("CDVR needs a single tree");

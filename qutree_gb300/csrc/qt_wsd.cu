@@ -4,23 +4,26 @@
 // src/Util/WeightedSimultaneousDiagonalization.cpp:5-378, and the Jacobi
 // rotation helpers of src/Core/JacobiRotationFramework.cpp:4-164).
 //
-// One warp per problem.  The iteration accepts or rejects optimiser steps on
+// One block of four warps per problem (one warp per FP64 unit of the SM).  The
+// iteration accepts or rejects optimiser steps on
 // comparisons of nearly equal numbers, so its result is a discontinuous
 // function of the inputs; this file therefore fixes one operation order,
 // which the CPU restatement follows bit for bit:
 //  * compiled with -fmad=false: no multiply-add is fused; a complex product
-//    is (ac - bd) + i(ad + bc), sums run left to right, and sums over the
-//    matrices of a problem in index order (as the reference's loops);
+//    is (ac - bd) + i(ad + bc), sums run left to right; a sum over the
+//    matrices of a problem is the pairwise tree of the values padded with
+//    zeros to a power of two, and the measure adds its per-matrix traces in
+//    index order;
 //  * |z| is sqrt(re^2 + im^2); real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
 //  * the optimiser's 3x3 eigenvector (Matrix::rDiag) comes from the largest
 //    root of the characteristic polynomial (Newton from the Gershgorin bound)
 //    and the largest cross product of two rows of H - lambda.
-// Work is spread over the lanes item by item -- the rotated 2x2 diagonal
+// Work is spread over the threads item by item -- the rotated 2x2 diagonal
 // blocks of every matrix at every candidate rotation (nine at once for the
-// finite-difference derivatives), the elements of the matrix products of the
-// off-diagonality measure, the rows and columns of every Givens rotation --
-// and the ordered sums are taken by single lanes from shared memory.  The
-// scalar control flow is uniform (every lane holds the same values).  All
+// finite-difference derivatives), the levels of the tree sums, the elements
+// of the matrix products of the off-diagonality measure, the rows and
+// columns of every Givens rotation.  The scalar control flow is uniform
+// (every thread holds the same values and runs it redundantly).  All
 // loops are bounded (at most 25 sweeps, 30 optimiser iterations, 64 step
 // halvings per search, 100 Newton steps).
 #include <cuda_runtime.h>
@@ -50,7 +53,8 @@ struct Prob {
   double2* tmp;  // 3 d^2: X T, Y and Y Y of the off-diagonality measure (global)
   // shared memory
   double2* blk;  // (n + 1) x 4: (pp, pq, qp, qq) of every matrix and of w at the current pair
-  double* sq;    // 2 x 9 x n: squared rotated diagonals per candidate
+  double* sq;    // 2 x (2 x 9 x P): squared rotated diagonals per candidate, two tree buffers
+  int P2;        // n padded to a power of two
   double* wd;    // 2 x 9: rotated diagonals of w per candidate
   double2* cand; // 2 x 9: candidate (c, s)
   double* red;   // 32 + d: xold (0, 1), measure (2), losses (8..16), traces (32..)
@@ -58,7 +62,9 @@ struct Prob {
   __device__ double2* Xp(int k) const { return xp + (int64_t)k * d * d; }
 };
 
-__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+constexpr int kWsdThreads = 128;
+__device__ __forceinline__ int lane_id() { return threadIdx.x; }
+__device__ __forceinline__ void wsync() { __syncthreads(); }
 
 // Matrix::rDiag of the optimiser's symmetric 3x3 matrix: eigenvector of the
 // largest eigenvalue as u0 = v0/v2, u1 = v1/v2 and v0^2 + v1^2 for |v| = 1
@@ -117,36 +123,54 @@ __device__ __forceinline__ void rotated_diagonals(const double2* b, double2 c, d
 }
 
 // weightedJacobiLoc for `count` candidates at once (cand[0 .. 2 count)):
-// red[8 + j] = diff of candidate j
+// red[8 + j] = diff of candidate j; red[4], red[5] hold xold / w of the pair
 __device__ void loc_many(const Prob& P, int count) {
-  const int n = P.n, lane = lane_id();
-  const int items = count * (n + 1);
-  for (int it = lane; it < items; it += 32) {
+  const int n = P.n, tid = lane_id(), P2 = P.P2;
+  double* buf = P.sq;                     // [comp][cand][P2], level 0
+  double* alt = P.sq + 2 * 9 * (int64_t)P2;
+  const int items = count * P2;
+  for (int it = tid; it < count * (n + 1); it += kWsdThreads) {
     const int j = it / (n + 1), k = it % (n + 1);
     double r0, r1;
     rotated_diagonals(P.blk + 4 * k, P.cand[2 * j], P.cand[2 * j + 1], r0, r1);
     if (k < n) {
-      P.sq[j * n + k] = r0 * r0;
-      P.sq[9 * n + j * n + k] = r1 * r1;
+      buf[j * P2 + k] = r0 * r0;
+      buf[9 * P2 + j * P2 + k] = r1 * r1;
     } else {
       P.wd[2 * j] = r0;
       P.wd[2 * j + 1] = r1;
     }
   }
-  __syncwarp();
-  if (lane < count) {
-    const int j = lane;
-    double xnew0 = 0, xnew1 = 0;
-    for (int k = 0; k < n; ++k) {
-      xnew0 += P.sq[j * n + k];
-      xnew1 += P.sq[9 * n + j * n + k];
+  for (int it = tid; it < items; it += kWsdThreads) {  // zero padding
+    const int j = it / P2, k = it % P2;
+    if (k >= n) {
+      buf[j * P2 + k] = 0.0;
+      buf[9 * P2 + j * P2 + k] = 0.0;
     }
+  }
+  wsync();
+  for (int size = P2; size > 1; size >>= 1) {  // pairwise tree, both components
+    const int half = size >> 1;
+    for (int it = tid; it < 2 * count * half; it += kWsdThreads) {
+      const int comp = it / (count * half), rem = it % (count * half);
+      const int j = rem / half, i = rem % half;
+      const double* src = buf + comp * 9 * P2 + j * P2;
+      alt[comp * 9 * P2 + j * P2 + i] = src[2 * i] + src[2 * i + 1];
+    }
+    wsync();
+    double* t = buf;
+    buf = alt;
+    alt = t;
+  }
+  if (tid < count) {
+    const int j = tid;
+    const double xnew0 = buf[j * P2], xnew1 = buf[9 * P2 + j * P2];
     double diff = 0;
-    diff += xnew0 / P.wd[2 * j] - P.red[0] / P.blk[4 * n + 0].x;
-    diff += xnew1 / P.wd[2 * j + 1] - P.red[1] / P.blk[4 * n + 3].x;
+    diff += xnew0 / P.wd[2 * j] - P.red[4];
+    diff += xnew1 / P.wd[2 * j + 1] - P.red[5];
     P.red[8 + j] = diff;
   }
-  __syncwarp();
+  wsync();
 }
 
 __device__ double loc1(const Prob& P, double2 c, double2 s) {
@@ -154,10 +178,10 @@ __device__ double loc1(const Prob& P, double2 c, double2 s) {
     P.cand[0] = c;
     P.cand[1] = s;
   }
-  __syncwarp();
+  wsync();
   loc_many(P, 1);
   const double v = P.red[8];
-  __syncwarp();
+  wsync();
   return v;
 }
 
@@ -172,11 +196,11 @@ __device__ void derivatives(const Prob& P, double grad[2], double pre[4], double
     P.cand[2 * lane] = make_double2(sqrt(fabs(1 - z)), 0.0);
     P.cand[2 * lane + 1] = make_double2(x0, x1);
   }
-  __syncwarp();
+  wsync();
   loc_many(P, 9);
   double y[9];
   for (int q = 0; q < 9; ++q) y[q] = P.red[8 + q];
-  __syncwarp();
+  wsync();
   grad[0] = (y[2 + 3 * 1] - y[0 + 3 * 1]) / (2 * delta);
   grad[1] = (y[1 + 3 * 2] - y[1 + 3 * 0]) / (2 * delta);
   pre[0] = (y[2 + 3 * 1] + y[0 + 3 * 1] - 2 * y[1 + 3 * 1]) / (delta * delta);
@@ -258,22 +282,22 @@ __device__ void givens_all(const Prob& P, double2* base, int m_count, int64_t st
   const int d = P.d;
   const int lane = lane_id();
   const int64_t tot = (int64_t)m_count * d;
-  for (int64_t e = lane; e < tot; e += 32) {  // columns i, j
+  for (int64_t e = lane; e < tot; e += kWsdThreads) {  // columns i, j
     double2* B = base + (e / d) * stride;
     const int r = (int)(e % d);
     const double2 bri = B[r + (int64_t)d * i], brj = B[r + (int64_t)d * j];
     B[r + (int64_t)d * i] = ca(cm(c, bri), cm(s, brj));
     B[r + (int64_t)d * j] = cs(cm(c, brj), cm(cc(s), bri));
   }
-  __syncwarp();
-  for (int64_t e = lane; e < tot; e += 32) {  // rows i, j
+  wsync();
+  for (int64_t e = lane; e < tot; e += kWsdThreads) {  // rows i, j
     double2* B = base + (e / d) * stride;
     const int r = (int)(e % d);
     const double2 c0 = B[i + (int64_t)d * r], c1 = B[j + (int64_t)d * r];
     B[i + (int64_t)d * r] = ca(cm(c, c0), cm(cc(s), c1));
     B[j + (int64_t)d * r] = cs(cm(c, c1), cm(s, c0));
   }
-  __syncwarp();
+  wsync();
 }
 
 __device__ void rotations(const Prob& P) {
@@ -281,35 +305,53 @@ __device__ void rotations(const Prob& P) {
   const int lane = lane_id();
   for (int i = 0; i < d - 1; ++i)
     for (int j = i + 1; j < d; ++j) {
-      for (int k = lane; k <= n; k += 32) {  // cache the (i, j) blocks
+      for (int k = lane; k <= n; k += kWsdThreads) {  // cache the (i, j) blocks
         const double2* A = k < n ? P.X(k) : P.w;
         P.blk[4 * k + 0] = A[i + (int64_t)d * i];
         P.blk[4 * k + 1] = A[i + (int64_t)d * j];
         P.blk[4 * k + 2] = A[j + (int64_t)d * i];
         P.blk[4 * k + 3] = A[j + (int64_t)d * j];
       }
-      __syncwarp();
-      if (lane == 0) {  // sum of the current squared diagonals, in matrix order
-        double o0 = 0, o1 = 0;
-        for (int k = 0; k < n; ++k) {
-          const double x0 = P.blk[4 * k].x, x1 = P.blk[4 * k + 3].x;
-          o0 += x0 * x0;
-          o1 += x1 * x1;
-        }
-        P.red[0] = o0;
-        P.red[1] = o1;
+      wsync();
+      // sums of the current squared diagonals (tree order) and xold / w
+      for (int k = lane; k < P.P2; k += kWsdThreads) {
+        const double x0 = k < n ? P.blk[4 * k].x : 0.0, x1 = k < n ? P.blk[4 * k + 3].x : 0.0;
+        P.sq[k] = k < n ? x0 * x0 : 0.0;
+        P.sq[9 * P.P2 + k] = k < n ? x1 * x1 : 0.0;
       }
-      __syncwarp();
+      wsync();
+      {
+        double* buf = P.sq;
+        double* alt = P.sq + 2 * 9 * (int64_t)P.P2;
+        for (int size = P.P2; size > 1; size >>= 1) {
+          const int half = size >> 1;
+          for (int it = lane; it < 2 * half; it += kWsdThreads) {
+            const int comp = it / half, q = it % half;
+            alt[comp * 9 * P.P2 + q] = buf[comp * 9 * P.P2 + 2 * q] + buf[comp * 9 * P.P2 + 2 * q + 1];
+          }
+          wsync();
+          double* t = buf;
+          buf = alt;
+          alt = t;
+        }
+        if (lane == 0) {
+          P.red[0] = buf[0];
+          P.red[1] = buf[9 * P.P2];
+          P.red[4] = buf[0] / P.blk[4 * n + 0].x;
+          P.red[5] = buf[9 * P.P2] / P.blk[4 * n + 3].x;
+        }
+        wsync();
+      }
       double2 c, s;
       angles(P, c, s);
       givens_all(P, P.xw, n, (int64_t)d * d, c, s, i, j);
       givens_all(P, P.w, 1, 0, c, s, i, j);
-      for (int r = lane; r < d; r += 32) {  // givensTrafoRotation
+      for (int r = lane; r < d; r += kWsdThreads) {  // givensTrafoRotation
         const double2 ti = P.T[r + (int64_t)d * i], tj = P.T[r + (int64_t)d * j];
         P.T[r + (int64_t)d * i] = ca(cm(c, ti), cm(s, tj));
         P.T[r + (int64_t)d * j] = cs(cm(c, tj), cm(cc(s), ti));
       }
-      __syncwarp();
+      wsync();
     }
 }
 
@@ -325,14 +367,14 @@ __device__ double offdiag(const Prob& P) {
   for (int k = 0; k < P.n; ++k) {
     const double2* X = P.Xp(k);
     const double2* Xw = P.X(k);
-    for (int64_t e = lane; e < dd; e += 32) {
+    for (int64_t e = lane; e < dd; e += kWsdThreads) {
       const int i = (int)(e % d), j = (int)(e / d);
       double2 acc = make_double2(0, 0);
       for (int l = 0; l < d; ++l) acc = ca(acc, cm(X[i + (int64_t)d * l], P.T[l + (int64_t)d * j]));
       M[e] = acc;
     }
-    __syncwarp();
-    for (int64_t e = lane; e < dd; e += 32) {
+    wsync();
+    for (int64_t e = lane; e < dd; e += kWsdThreads) {
       const int i = (int)(e % d), j = (int)(e / d);
       double2 acc = make_double2(0, 0);
       for (int l = 0; l < d; ++l) acc = ca(acc, cm(cc(P.T[l + (int64_t)d * i]), M[l + (int64_t)d * j]));
@@ -340,35 +382,35 @@ __device__ double offdiag(const Prob& P) {
       if (i == j) dg = make_double2(cdiv_re(Xw[i + (int64_t)d * i], P.w[i + (int64_t)d * i]), 0);
       Y[e] = cs(dg, acc);
     }
-    __syncwarp();
-    for (int64_t e = lane; e < dd; e += 32) {
+    wsync();
+    for (int64_t e = lane; e < dd; e += kWsdThreads) {
       const int i = (int)(e % d), j = (int)(e / d);
       double2 acc = make_double2(0, 0);
       for (int l = 0; l < d; ++l) acc = ca(acc, cm(Y[i + (int64_t)d * l], Y[l + (int64_t)d * j]));
       Z[e] = acc;
     }
-    __syncwarp();
-    for (int i = lane; i < d; i += 32) {
+    wsync();
+    for (int i = lane; i < d; i += kWsdThreads) {
       double2 acc = make_double2(0, 0);
       for (int l = 0; l < d; ++l) acc = ca(acc, cm(P.w[i + (int64_t)d * l], Z[l + (int64_t)d * i]));
       P.red[32 + i] = acc.x;
     }
-    __syncwarp();
+    wsync();
     if (lane == 0) {
       double tr = 0;
       for (int i = 0; i < d; ++i) tr += P.red[32 + i];
       total += tr;
     }
-    __syncwarp();
+    wsync();
   }
   if (lane == 0) P.red[2] = total;
-  __syncwarp();
+  wsync();
   const double v = P.red[2];
-  __syncwarp();
+  wsync();
   return v;
 }
 
-__global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, const WSDTerm* __restrict__ terms,
+__global__ void __launch_bounds__(kWsdThreads) k_wsd(const WSDTask* __restrict__ tasks, const WSDTerm* __restrict__ terms,
                                             int64_t first) {
   const WSDTask t = tasks[first + blockIdx.x];
   const int d = t.d, n = t.n;
@@ -384,12 +426,14 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
   P.T = P.w + dd;
   P.tmp = P.T + dd;
   P.blk = wsd_smem;
+  P.P2 = 1;
+  while (P.P2 < n) P.P2 <<= 1;
   P.cand = P.blk + 4 * (n + 1);
   P.sq = reinterpret_cast<double*>(P.cand + 18);
-  P.wd = P.sq + 18 * n;
+  P.wd = P.sq + 4 * 9 * (int64_t)P.P2;
   P.red = P.wd + 18;
   // w = regularize(W, 1e-9), T = 1
-  for (int64_t e = lane; e < dd; e += 32) {
+  for (int64_t e = lane; e < dd; e += kWsdThreads) {
     double2 v = t.W[e];
     const int i = (int)(e % d), j = (int)(e / d);
     if (i == j) v.x += 1e-9 * exp(-cabs_(v) / 1e-9);
@@ -397,7 +441,7 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
     P.T[e] = make_double2(i == j ? 1.0 : 0.0, 0.0);
   }
   // plain matrices shifted by |tr X| (calculateShift / shift)
-  for (int k = lane; k < n; k += 32) {
+  for (int k = lane; k < n; k += kWsdThreads) {
     const double2* X = terms[t.first + k].X;
     double2* Xp = P.Xp(k);
     double2 tr = make_double2(0, 0);
@@ -407,9 +451,9 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
     for (int i = 0; i < d; ++i) Xp[i + (int64_t)d * i].x -= sh;
     t.grid[(int64_t)k * d].y = sh;  // kept until the end (the grid's imaginary parts are zero)
   }
-  __syncwarp();
+  wsync();
   // weightMatrices: (X w + w X) / 2
-  for (int64_t e = lane; e < (int64_t)n * dd; e += 32) {
+  for (int64_t e = lane; e < (int64_t)n * dd; e += kWsdThreads) {
     const int k = (int)(e / dd);
     const int i = (int)(e % dd % d), j = (int)(e % dd / d);
     const double2* x = P.Xp(k);
@@ -421,9 +465,9 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
     const double2 sum = ca(xw, wx);
     P.X(k)[i + (int64_t)d * j] = make_double2(0.5 * sum.x, 0.5 * sum.y);
   }
-  __syncwarp();
+  wsync();
   double delta = offdiag(P);
-  __syncwarp();
+  wsync();
   int iter = 0;
   bool converged = false;
   const double eps = 1e-5;
@@ -431,18 +475,18 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
     rotations(P);
     const double delta_last = delta;
     delta = offdiag(P);
-    __syncwarp();
+    wsync();
     const double change = fabs(delta_last - delta);
     if (delta < eps || change < eps) converged = true;
     iter++;
   }
   // grid = Re(Xw(i,i) / w(i,i)) + shift; trafo = T^dagger
-  for (int k = lane; k < n; k += 32) {
+  for (int k = lane; k < n; k += kWsdThreads) {
     const double sh = t.grid[(int64_t)k * d].y;
     for (int i = 0; i < d; ++i)
       t.grid[(int64_t)k * d + i] = make_double2(cdiv_re(P.X(k)[i + (int64_t)d * i], P.w[i + (int64_t)d * i]) + sh, 0.0);
   }
-  for (int64_t e = lane; e < dd; e += 32) {
+  for (int64_t e = lane; e < dd; e += kWsdThreads) {
     const int i = (int)(e % d), j = (int)(e / d);
     t.trafo[e] = cc(P.T[j + (int64_t)d * i]);
   }
@@ -452,7 +496,9 @@ __global__ void __launch_bounds__(32) k_wsd(const WSDTask* __restrict__ tasks, c
 
 // shared memory of a problem with n matrices of order d (see Prob)
 int64_t wsd_smem_bytes(int n, int d) {
-  return 16 * (4 * (int64_t)(n + 1) + 18) + 8 * (18 * (int64_t)n + 18 + 32 + d) + 64;
+  int64_t p2 = 1;
+  while (p2 < n) p2 <<= 1;
+  return 16 * (4 * (int64_t)(n + 1) + 18) + 8 * (36 * p2 + 18 + 32 + d) + 64;
 }
 
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,
@@ -462,7 +508,7 @@ cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first
   if (sm > 200 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(k_wsd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k_wsd<<<(unsigned)n, 32, sm, s>>>(tasks, terms, first);
+  k_wsd<<<(unsigned)n, kWsdThreads, sm, s>>>(tasks, terms, first);
   return cudaGetLastError();
 }
 
