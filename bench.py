@@ -47,6 +47,8 @@ def parse():
                     help="trees in the supplementary many-tree batch (0: skip)")
     ap.add_argument("--no-scf", action="store_true", help="skip the supplementary SCF sweep timing")
     ap.add_argument("--no-cdvr", action="store_true", help="skip the supplementary CDVR sweep timing")
+    ap.add_argument("--cdvr-sweeps", type=int, default=0,
+                    help="only run this many CDVR sweeps of the CDVR workload (for profilers) and exit")
     ap.add_argument("--precision-steps", type=int, default=0,
                     help="CMF steps (dt 0.01) of the double-float vs complex128 study on the "
                          "48..96-bond 64-mode tree (0: skip)")
@@ -616,6 +618,19 @@ def cdvr_section(args, local, torch):
 def main():
     args = parse()
     ws, rank, local = dist_setup()
+    if args.cdvr_sweeps > 0:  # profiling aid: the CDVR workload's sweeps, nothing else
+        from qutree_gb300 import qtgpu
+        from qutree_gb300.model import cdvr_problem
+        tree, sop, psi, xs, V = cdvr_problem(16, 16, 12)
+        h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_GROUPED, potential=V, leaf_x=xs,
+                                            device=local)
+        h.upload(psi.flat())
+        for _ in range(args.cdvr_sweeps):
+            h.derivative()
+        h.sync()
+        print(json.dumps({"cdvr_sweeps": args.cdvr_sweeps, "energy": h.energy()}))
+        h.close()
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
     else:
