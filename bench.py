@@ -475,7 +475,7 @@ def run_ours(args, ws, rank, local):
     line = {
         "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "scaling": "weak", "vs_baseline": None, "dtype": "df64",
         "data": "synthetic (seeded N(0,1) node tensors, QR-orthonormalised)",
         "config": {"workload": WORKLOAD, "plan": "compressed (per node one block matrix of the terms "
                    "inside its subtree, summed mean fields per boundary restriction, represent chains "
