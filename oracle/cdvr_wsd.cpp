@@ -17,7 +17,8 @@
 //    t[i] = t[2i] + t[2i+1]); the measure adds its per-matrix traces in
 //    index order;
 //  * |z| is sqrt(re^2 + im^2) where the reference calls std::abs (hypot), and
-//    real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
+//    real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2); the rotated diagonals
+//    of a candidate rotation use the Hermitian form (below);
 //  * the 3x3 symmetric eigenproblem of the optimiser (Matrix::rDiag, Eigen's
 //    SelfAdjointEigenSolver in the reference) is solved for what the
 //    optimiser uses of it -- the eigenvector of the largest eigenvalue as
@@ -116,14 +117,19 @@ extern "C" void orc_eig3_top(const double H[9], double* u0, double* u1, double* 
 }
 namespace {
 
-// rotatedDiagonals (src/Core/JacobiRotationFramework.cpp:129-141)
+// rotatedDiagonals (src/Core/JacobiRotationFramework.cpp:129-141) for a
+// Hermitian A and a real c (the optimiser's c is always real):
+//   a0 = c^2 A_pp + 2c Re(s A_pq) + |s|^2 A_qq,  a1 = c^2 A_qq - 2c Re(s A_pq) + |s|^2 A_pp,
+// equal to the reference's complex expression up to rounding
 inline void rotated_diagonals(const Mat& A, int p, int q, cd c, cd s, double& a0, double& a1) {
-  const cd c00 = cadd(cmul(c, A(p, p)), cmul(s, A(p, q)));
-  const cd c01 = csub(cmul(c, A(p, q)), cmul(cconj(s), A(p, p)));
-  const cd c10 = cadd(cmul(c, A(q, p)), cmul(s, A(q, q)));
-  const cd c11 = csub(cmul(c, A(q, q)), cmul(cconj(s), A(q, p)));
-  a0 = cadd(cmul(c, c00), cmul(cconj(s), c10)).r;
-  a1 = csub(cmul(c, c11), cmul(s, c01)).r;
+  const double cc2 = c.r * c.r;
+  const double ss2 = s.r * s.r + s.i * s.i;
+  const double c2 = 2.0 * c.r;
+  const cd apq = A(p, q);
+  const double t = s.r * apq.r - s.i * apq.i;
+  const double ct = c2 * t;
+  a0 = (cc2 * A(p, p).r + ct) + ss2 * A(q, q).r;
+  a1 = (cc2 * A(q, q).r - ct) + ss2 * A(p, p).r;
 }
 
 struct Problem {

@@ -15,6 +15,8 @@
 //    zeros to a power of two, and the measure adds its per-matrix traces in
 //    index order;
 //  * |z| is sqrt(re^2 + im^2); real(x / w) is (xr wr + xi wi) / (wr^2 + wi^2);
+//    the rotated diagonals of a candidate rotation use the Hermitian form
+//    c^2 A_pp + 2c Re(s A_pq) + |s|^2 A_qq (c is real);
 //  * the optimiser's 3x3 eigenvector (Matrix::rDiag) comes from the largest
 //    root of the characteristic polynomial (Newton from the Gershgorin bound)
 //    and the largest cross product of two rows of H - lambda.
@@ -111,15 +113,18 @@ __device__ void eig3_top(const double H[9], double* u0, double* u1, double* top2
   *top2 = q / (q + v2 * v2);
 }
 
-// rotatedDiagonals of a cached 2x2 block (pp, pq, qp, qq)
+// rotatedDiagonals of a cached 2x2 block (pp, pq, qp, qq) of a Hermitian
+// matrix for a real c: a0 = c^2 A_pp + 2c Re(s A_pq) + |s|^2 A_qq and
+// a1 = c^2 A_qq - 2c Re(s A_pq) + |s|^2 A_pp
 __device__ __forceinline__ void rotated_diagonals(const double2* b, double2 c, double2 s, double& a0, double& a1) {
-  const double2 App = b[0], Apq = b[1], Aqp = b[2], Aqq = b[3];
-  const double2 c00 = ca(cm(c, App), cm(s, Apq));
-  const double2 c01 = cs(cm(c, Apq), cm(cc(s), App));
-  const double2 c10 = ca(cm(c, Aqp), cm(s, Aqq));
-  const double2 c11 = cs(cm(c, Aqq), cm(cc(s), Aqp));
-  a0 = ca(cm(c, c00), cm(cc(s), c10)).x;
-  a1 = cs(cm(c, c11), cm(s, c01)).x;
+  const double cc2 = c.x * c.x;
+  const double ss2 = s.x * s.x + s.y * s.y;
+  const double c2 = 2.0 * c.x;
+  const double2 apq = b[1];
+  const double t = s.x * apq.x - s.y * apq.y;
+  const double ct = c2 * t;
+  a0 = (cc2 * b[0].x + ct) + ss2 * b[3].x;
+  a1 = (cc2 * b[3].x - ct) + ss2 * b[0].x;
 }
 
 // weightedJacobiLoc for `count` candidates at once (cand[0 .. 2 count)):
