@@ -55,11 +55,11 @@ struct Prob {
   double2* tmp;  // 3 d^2: X T, Y and Y Y of the off-diagonality measure (global)
   // shared memory
   double2* blk;  // (n + 1) x 4: (pp, pq, qp, qq) of every matrix and of w at the current pair
-  double* sq;    // 2 x (2 x 9 x P): squared rotated diagonals per candidate, two tree buffers
+  double* sq;    // 2 x (2 x 10 x P): squared rotated diagonals per candidate, two tree buffers
   int P2;        // n padded to a power of two
-  double* wd;    // 2 x 9: rotated diagonals of w per candidate
-  double2* cand; // 2 x 9: candidate (c, s)
-  double* red;   // 32 + d: xold (0, 1), measure (2), losses (8..16), traces (32..)
+  double* wd;    // 2 x 10: rotated diagonals of w per candidate
+  double2* cand; // 2 x 10: candidate (c, s)
+  double* red;   // 32 + d: xold (0, 1), measure (2), xold / w (4, 5), losses (8..17), traces (32..)
   __device__ double2* X(int k) const { return xw + (int64_t)k * d * d; }
   __device__ double2* Xp(int k) const { return xp + (int64_t)k * d * d; }
 };
@@ -132,7 +132,7 @@ __device__ __forceinline__ void rotated_diagonals(const double2* b, double2 c, d
 __device__ void loc_many(const Prob& P, int count) {
   const int n = P.n, tid = lane_id(), P2 = P.P2;
   double* buf = P.sq;                     // [comp][cand][P2], level 0
-  double* alt = P.sq + 2 * 9 * (int64_t)P2;
+  double* alt = P.sq + 2 * 10 * (int64_t)P2;
   const int items = count * P2;
   for (int it = tid; it < count * (n + 1); it += kWsdThreads) {
     const int j = it / (n + 1), k = it % (n + 1);
@@ -140,7 +140,7 @@ __device__ void loc_many(const Prob& P, int count) {
     rotated_diagonals(P.blk + 4 * k, P.cand[2 * j], P.cand[2 * j + 1], r0, r1);
     if (k < n) {
       buf[j * P2 + k] = r0 * r0;
-      buf[9 * P2 + j * P2 + k] = r1 * r1;
+      buf[10 * P2 + j * P2 + k] = r1 * r1;
     } else {
       P.wd[2 * j] = r0;
       P.wd[2 * j + 1] = r1;
@@ -150,7 +150,7 @@ __device__ void loc_many(const Prob& P, int count) {
     const int j = it / P2, k = it % P2;
     if (k >= n) {
       buf[j * P2 + k] = 0.0;
-      buf[9 * P2 + j * P2 + k] = 0.0;
+      buf[10 * P2 + j * P2 + k] = 0.0;
     }
   }
   wsync();
@@ -159,8 +159,8 @@ __device__ void loc_many(const Prob& P, int count) {
     for (int it = tid; it < 2 * count * half; it += kWsdThreads) {
       const int comp = it / (count * half), rem = it % (count * half);
       const int j = rem / half, i = rem % half;
-      const double* src = buf + comp * 9 * P2 + j * P2;
-      alt[comp * 9 * P2 + j * P2 + i] = src[2 * i] + src[2 * i + 1];
+      const double* src = buf + comp * 10 * P2 + j * P2;
+      alt[comp * 10 * P2 + j * P2 + i] = src[2 * i] + src[2 * i + 1];
     }
     wsync();
     double* t = buf;
@@ -169,7 +169,7 @@ __device__ void loc_many(const Prob& P, int count) {
   }
   if (tid < count) {
     const int j = tid;
-    const double xnew0 = buf[j * P2], xnew1 = buf[9 * P2 + j * P2];
+    const double xnew0 = buf[j * P2], xnew1 = buf[10 * P2 + j * P2];
     double diff = 0;
     diff += xnew0 / P.wd[2 * j] - P.red[4];
     diff += xnew1 / P.wd[2 * j + 1] - P.red[5];
@@ -178,34 +178,23 @@ __device__ void loc_many(const Prob& P, int count) {
   wsync();
 }
 
-__device__ double loc1(const Prob& P, double2 c, double2 s) {
-  if (lane_id() == 0) {
-    P.cand[0] = c;
-    P.cand[1] = s;
-  }
-  wsync();
-  loc_many(P, 1);
-  const double v = P.red[8];
-  wsync();
-  return v;
-}
-
-// weightedJacobiDerivatives: the nine candidates of the central differences
-__device__ void derivatives(const Prob& P, double grad[2], double pre[4], double2 s_in, double delta) {
-  const int lane = lane_id();
-  if (lane < 9) {
-    const int i = lane % 3, j = lane / 3;
+// weightedJacobiDerivatives: the loss at the nine points of the central
+// differences around s_in (as candidates 1..9, after `first` candidates the
+// caller placed at 0 .. first-1); y[q] of point q = i + 3 j gets
+// red[8 + first + q]
+__device__ void set_samples(const Prob& P, double2 s_in, double delta, int first) {
+  const int t = lane_id();
+  if (t >= first && t < first + 9) {
+    const int q = t - first;
+    const int i = q % 3, j = q / 3;
     const double x0 = s_in.x + (double)(i - 1) * delta;
     const double x1 = s_in.y + (double)(j - 1) * delta;
     const double z = x0 * x0 + x1 * x1;
-    P.cand[2 * lane] = make_double2(sqrt(fabs(1 - z)), 0.0);
-    P.cand[2 * lane + 1] = make_double2(x0, x1);
+    P.cand[2 * t] = make_double2(sqrt(fabs(1 - z)), 0.0);
+    P.cand[2 * t + 1] = make_double2(x0, x1);
   }
-  wsync();
-  loc_many(P, 9);
-  double y[9];
-  for (int q = 0; q < 9; ++q) y[q] = P.red[8 + q];
-  wsync();
+}
+__device__ void grad_pre(const double y[9], double grad[2], double pre[4], double delta) {
   grad[0] = (y[2 + 3 * 1] - y[0 + 3 * 1]) / (2 * delta);
   grad[1] = (y[1 + 3 * 2] - y[1 + 3 * 0]) / (2 * delta);
   pre[0] = (y[2 + 3 * 1] + y[0 + 3 * 1] - 2 * y[1 + 3 * 1]) / (delta * delta);
@@ -214,7 +203,11 @@ __device__ void derivatives(const Prob& P, double grad[2], double pre[4], double
   pre[1] = pre[2];
 }
 
-// calculateWeightedAngles: rational function optimisation of (c, s)
+// calculateWeightedAngles: rational function optimisation of (c, s).  The
+// loss of every new candidate is evaluated together with the nine samples of
+// the central differences around it: if the candidate is accepted they are
+// the next iteration's derivatives, if not the derivatives at the unchanged
+// point are still valid -- the same numbers the reference recomputes.
 __device__ void angles(const Prob& P, double2& c, double2& s) {
   int iter = 0;
   const int maxiter = 30;
@@ -226,11 +219,22 @@ __device__ void angles(const Prob& P, double2& c, double2& s) {
   double snew[2] = {0, 0}, cnew[2] = {0, 0};
   c = make_double2(sqrt(1 - 2 * eps * eps), 0);
   s = make_double2(eps, -eps);
-  double loc_alt = loc1(P, c, s);
+  // loss at the start point and the samples around it
+  if (lane_id() == 0) {
+    P.cand[0] = c;
+    P.cand[1] = s;
+  }
+  set_samples(P, s, delta, 1);
+  wsync();
+  loc_many(P, 10);
+  double loc_alt = P.red[8];
+  double ycur[9], ynew[9];
+  for (int q = 0; q < 9; ++q) ycur[q] = P.red[9 + q];
+  wsync();
   double loc_new = 0;
   while (iter < maxiter && diff_rel > eps * eps && a > amin) {
     double pre[4], grad[2];
-    derivatives(P, grad, pre, s, delta);
+    grad_pre(ycur, grad, pre, delta);
     double diff = -1;
     int guard = 0;
     while (a > amin && diff < 0 && diff_rel > eps * eps && guard++ < 64) {
@@ -260,7 +264,16 @@ __device__ void angles(const Prob& P, double2& c, double2& s) {
       }
       cnew[0] = sqrt(fabs(1 - z));
       cnew[1] = 0;
-      loc_new = loc1(P, make_double2(cnew[0], cnew[1]), make_double2(snew[0], snew[1]));
+      if (lane_id() == 0) {
+        P.cand[0] = make_double2(cnew[0], cnew[1]);
+        P.cand[1] = make_double2(snew[0], snew[1]);
+      }
+      set_samples(P, make_double2(snew[0], snew[1]), delta, 1);
+      wsync();
+      loc_many(P, 10);
+      loc_new = P.red[8];
+      for (int q = 0; q < 9; ++q) ynew[q] = P.red[9 + q];
+      wsync();
       const double trafoabs = top2;
       const double sab = cabs_(s);
       const double sabs = sab * sab + eps * eps;
@@ -276,6 +289,7 @@ __device__ void angles(const Prob& P, double2& c, double2& s) {
       c = make_double2(cnew[0], cnew[1]);
       s = make_double2(snew[0], snew[1]);
       loc_alt = loc_new;
+      for (int q = 0; q < 9; ++q) ycur[q] = ynew[q];
     }
     iter++;
   }
@@ -322,17 +336,17 @@ __device__ void rotations(const Prob& P) {
       for (int k = lane; k < P.P2; k += kWsdThreads) {
         const double x0 = k < n ? P.blk[4 * k].x : 0.0, x1 = k < n ? P.blk[4 * k + 3].x : 0.0;
         P.sq[k] = k < n ? x0 * x0 : 0.0;
-        P.sq[9 * P.P2 + k] = k < n ? x1 * x1 : 0.0;
+        P.sq[10 * P.P2 + k] = k < n ? x1 * x1 : 0.0;
       }
       wsync();
       {
         double* buf = P.sq;
-        double* alt = P.sq + 2 * 9 * (int64_t)P.P2;
+        double* alt = P.sq + 2 * 10 * (int64_t)P.P2;
         for (int size = P.P2; size > 1; size >>= 1) {
           const int half = size >> 1;
           for (int it = lane; it < 2 * half; it += kWsdThreads) {
             const int comp = it / half, q = it % half;
-            alt[comp * 9 * P.P2 + q] = buf[comp * 9 * P.P2 + 2 * q] + buf[comp * 9 * P.P2 + 2 * q + 1];
+            alt[comp * 10 * P.P2 + q] = buf[comp * 10 * P.P2 + 2 * q] + buf[comp * 10 * P.P2 + 2 * q + 1];
           }
           wsync();
           double* t = buf;
@@ -341,9 +355,9 @@ __device__ void rotations(const Prob& P) {
         }
         if (lane == 0) {
           P.red[0] = buf[0];
-          P.red[1] = buf[9 * P.P2];
+          P.red[1] = buf[10 * P.P2];
           P.red[4] = buf[0] / P.blk[4 * n + 0].x;
-          P.red[5] = buf[9 * P.P2] / P.blk[4 * n + 3].x;
+          P.red[5] = buf[10 * P.P2] / P.blk[4 * n + 3].x;
         }
         wsync();
       }
@@ -434,9 +448,9 @@ __global__ void __launch_bounds__(kWsdThreads) k_wsd(const WSDTask* __restrict__
   P.P2 = 1;
   while (P.P2 < n) P.P2 <<= 1;
   P.cand = P.blk + 4 * (n + 1);
-  P.sq = reinterpret_cast<double*>(P.cand + 18);
-  P.wd = P.sq + 4 * 9 * (int64_t)P.P2;
-  P.red = P.wd + 18;
+  P.sq = reinterpret_cast<double*>(P.cand + 20);
+  P.wd = P.sq + 4 * 10 * (int64_t)P.P2;
+  P.red = P.wd + 20;
   // w = regularize(W, 1e-9), T = 1
   for (int64_t e = lane; e < dd; e += kWsdThreads) {
     double2 v = t.W[e];
@@ -503,7 +517,7 @@ __global__ void __launch_bounds__(kWsdThreads) k_wsd(const WSDTask* __restrict__
 int64_t wsd_smem_bytes(int n, int d) {
   int64_t p2 = 1;
   while (p2 < n) p2 <<= 1;
-  return 16 * (4 * (int64_t)(n + 1) + 18) + 8 * (36 * p2 + 18 + 32 + d) + 64;
+  return 16 * (4 * (int64_t)(n + 1) + 20) + 8 * (40 * p2 + 20 + 32 + d) + 64;
 }
 
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,
