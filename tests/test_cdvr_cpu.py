@@ -30,6 +30,16 @@ def binary8(p, d1, d2, d3):
     return Tree(_Build([d3, d3, 1], children=l2))
 
 
+def uneven6(p):
+    """Six modes: a node with three children, a branch one layer deeper
+    than the other; bonds no larger than the density matrices' ranks allow."""
+    lv = [_Build([p, 3], leaf=True) for _ in range(6)]
+    n3 = _Build([3, 3, 3, 4], children=lv[0:3])
+    n2 = _Build([3, 3, 4], children=lv[3:5])
+    n2b = _Build([4, 3, 4], children=[n2, lv[5]])
+    return Tree(_Build([4, 4, 1], children=[n3, n2b]))
+
+
 def two_leaf(p):
     leaves = [_Build([p, p], leaf=True) for _ in range(2)]
     return Tree(_Build([p, p, 1], children=leaves))
@@ -166,7 +176,8 @@ def test_wsd_of_commuting_matrices_finds_their_eigenvalues():
 # --------------------------------------------------------------------------
 # planned CDVR stages against the oracle
 # --------------------------------------------------------------------------
-CASES = [("binary4", lambda: binary4(5, 4, 3), 5), ("binary8", lambda: binary8(6, 4, 5, 4), 6)]
+CASES = [("binary4", lambda: binary4(5, 4, 3), 5), ("binary8", lambda: binary8(6, 4, 5, 4), 6),
+         ("uneven6", lambda: uneven6(5), 5)]
 
 
 @pytest.mark.parametrize("name,mk,p", CASES)
@@ -179,6 +190,7 @@ def test_emulated_cdvr_sweep_matches_oracle(name, mk, p, flavour, aligned):
     xs = {m: basis.x for m in range(f)}
     sop = kinetic_sop(tree, basis)
     V = PolyPotential.cdvr_model(f)
+    V.terms.append((0.01, [(0, 1), (f // 2, 1), (f - 1, 2)]))  # a three-mode term
     psi = random_wavefunction(tree, 7)
     pv = PlanView(tree, sop, flavour=flavour, cdvr=(xs, V, aligned))
     pv.run(psi.flat())

@@ -16,11 +16,24 @@ from qutree_gb300.model import cdvr_problem
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(8, 8, 6), (16, 12, 8)]
+CASES = [(8, 8, 6), (16, 12, 8), ("uneven6", 5, 0)]
+
+
+def problem(n_modes, p, bond, seed):
+    if n_modes == "uneven6":  # a three-child node and uneven depth (tests/test_cdvr_cpu.py)
+        from test_cdvr_cpu import kinetic_sop, uneven6
+        from qutree_gb300.model import HOBasis, PolyPotential, random_wavefunction
+        tree = uneven6(p)
+        basis = HOBasis(p)
+        V = PolyPotential.cdvr_model(6)
+        V.terms.append((0.01, [(0, 1), (3, 1), (5, 2)]))
+        return tree, kinetic_sop(tree, basis), random_wavefunction(tree, seed), \
+            {m: basis.x for m in range(6)}, V
+    return cdvr_problem(n_modes, p, bond, seed=seed)
 
 
 def run(n_modes, p, bond, flavour, aligned, seed=5):
-    tree, sop, psi, xs, V = cdvr_problem(n_modes, p, bond, seed=seed)
+    tree, sop, psi, xs, V = problem(n_modes, p, bond, seed)
     h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, potential=V, leaf_x=xs,
                                         aligned_hole_grids=aligned)
     try:
