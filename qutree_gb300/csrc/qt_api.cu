@@ -293,11 +293,12 @@ int qt_set_regularization(qt_ctx* c, double eps) {
 int qt_prepare(qt_ctx* c, int flavour) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->have_tree || !c->have_sop) return fail(c, QT_ERR_STATE, "qt_prepare needs tree and SOP");
-  const int prec = (flavour & QT_PREC_DF64) ? 1 : 0;
+  const bool tensor_mp = (flavour & QT_PREC_DF64_TC) != 0;
+  const int prec = (flavour & (QT_PREC_DF64 | QT_PREC_DF64_TC)) ? 1 : 0;
   const bool grad = (flavour & QT_PLAN_GRADIENT) != 0;
   const bool scf = (flavour & QT_PLAN_SCF) != 0;
   const bool cdvr = (flavour & QT_PLAN_CDVR) != 0;
-  flavour &= ~(QT_PREC_DF64 | QT_PLAN_GRADIENT | QT_PLAN_SCF | QT_PLAN_CDVR);
+  flavour &= ~(QT_PREC_DF64 | QT_PREC_DF64_TC | QT_PLAN_GRADIENT | QT_PLAN_SCF | QT_PLAN_CDVR);
   if (cdvr && !c->have_cdvr) return fail(c, QT_ERR_STATE, "QT_PLAN_CDVR needs qt_cdvr_upload first");
   if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED && flavour != QT_PLAN_COMPRESSED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
@@ -308,8 +309,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
     long v = std::atol(s);
     if (v > 0) budget = (int64_t)v * (1 << 20) / 16;
   }
-  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop, flavour | (scf ? 0x2000 : 0), prec, budget,
-                                   grad, cdvr ? &c->cdvr : nullptr);
+  std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop,
+                                   flavour | (scf ? 0x2000 : 0) | (tensor_mp ? 0x8000 : 0), prec, budget, grad,
+                                   cdvr ? &c->cdvr : nullptr);
   if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
   Plan& P = c->plan;
   c->buf_elems[qt::B_PSI] = P.psi_arena;
@@ -327,6 +329,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_HPW] = P.hpw_size;
   c->buf_elems[qt::B_KRY] = P.kry_size;
   c->buf_elems[qt::B_CDVR] = P.cdvr ? P.cdvr_size : 0;
+  c->buf_elems[qt::B_OZ] = (P.oz_bytes + 15) / 16;
   int64_t arena = 0;
   for (int i = 0; i < qt::B_NBUF; ++i) {
     if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
@@ -378,6 +381,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.after = s.after;
     t.diag = s.diag;
     t.add = 0;
+    t.oz_h = s.oz_h >= 0 ? (void*)((char*)c->buf[qt::B_OZ] + s.oz_h) : nullptr;
     mp.push_back(t);
   }
   std::vector<qt::HPTask> hp;
@@ -577,6 +581,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, P.dvl_tiles);
   put(blob, offs, ewt);
   put(blob, offs, P.ew_tiles);
+  put(blob, offs, P.mp_oz_tiles);
+  put(blob, offs, P.mp_oz_tasks);
   {
     cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -625,6 +631,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.dvl_tiles = (int2*)(base + offs[29]);
   c->tables.ew = (qt::EWTask*)(base + offs[30]);
   c->tables.ew_tiles = (int2*)(base + offs[31]);
+  c->tables.mp_oz_tiles = (int2*)(base + offs[32]);
+  c->tables.mp_oz_tasks = (int*)(base + offs[33]);
   if (P.cdvr) {  // CDVR constants: seeded noise, leaf grids, identity
     QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_CDVR], 0, c->buf_elems[qt::B_CDVR] * 16, c->stream));
     for (auto& init : P.cdvr_init)

@@ -28,6 +28,7 @@ struct MPTask {
   int before, a_in, a_out, after;
   int diag;
   int add;  // 1: out += result
+  void* oz_h = nullptr;  // tensor-core path: digits of h (written by the stage's pre-pass)
 };
 
 // Hole product: S(i, j) = sum_{b, c} conj(A[b, i, c]) * B[b, j, c].
@@ -231,6 +232,8 @@ struct Stage {
   const char* name;
   int aux = 0;       // hole-product stage with split tasks: a second kernel sums the partial tiles
   int seg0 = 0, nseg = 0;  // hole-product stage: its tile segments (one launch per micro-tile shape)
+  int64_t oz0 = 0, noz = 0;  // mode-product stage: its tensor-core tiles (mp_oz_tiles)
+  int64_t ozt0 = 0, nozt = 0;  // and its tensor-core tasks (mp_oz_tasks, digits of h)
   double flops = 0;  // executed flops of the stage
   double bytes = 0;  // algorithmic bytes: operands read once, results written once
 };
@@ -253,7 +256,7 @@ struct Stage {
 // edge potentials, correction tensors, their scratch and constants).
 enum Buf {
   B_PSI = 0, B_HPHI, B_DPSI, B_MATS, B_OPS, B_SCR, B_PARAM, B_PSI64, B_DPSI64, B_GRAD, B_GRAD64, B_KEEP, B_HPW, B_KRY,
-  B_CDVR, B_NBUF
+  B_CDVR, B_OZ, B_NBUF
 };
 
 struct Ref {
@@ -318,6 +321,7 @@ struct Plan {
     Ref in, out, h;
     double2 alpha;
     int before, a_in, a_out, after, diag;
+    int64_t oz_h = -1;  // tensor-core path: offset (bytes) of the digits of h in B_OZ
   };
   struct SHP {
     Ref A, B, S;
@@ -473,6 +477,11 @@ struct Plan {
   std::vector<int2> mp_tiles;
   std::vector<int4> hp_tiles;
   std::vector<int4> hp_segs;  // (rows, cols, first tile, tile count) per hole-product launch
+  // double-float plans with tensor-core mode products: (task, block of 32 rows)
+  bool mp_tensor = false;
+  std::vector<int2> mp_oz_tiles;
+  std::vector<int> mp_oz_tasks;
+  int64_t oz_bytes = 0;  // B_OZ: digits of h per tensor-core task
   std::vector<int4> acc_tiles;
   std::vector<int2> cvt_tiles;
   // constant matrices written once at prepare: (offset, d) identity
@@ -536,6 +545,8 @@ struct DevTables {
   MMTerm* mm_terms = nullptr;
   int2* mm_tiles = nullptr;
   const int4* hp_segs = nullptr;  // host array: (rows, cols, first tile, tile count)
+  int2* mp_oz_tiles = nullptr;
+  int* mp_oz_tasks = nullptr;
   TCTask* tc = nullptr;
   int4* tc_tiles = nullptr;
   GSTask* gs = nullptr;
@@ -603,6 +614,14 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
                         cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
+// double-float mode products on the tensor cores (qt_ozaki.cu): a task
+// qualifies when it is not diagonal and a_in, a_out <= 64
+cudaError_t launch_mp_oz(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
+                         const int* oz_tasks, int64_t first_task, int64_t n_tasks, cudaStream_t s);
+constexpr int kMpOzRows = 32;  // rows (b, c) per tensor-core mode-product tile
+constexpr int kMpOzDig = 7, kMpOzN = 64, kMpOzPitch = 72;
+// digits of one h: [digit][re/im][j][k] bf16 plus 64 row exponents (int)
+inline int64_t mp_oz_h_bytes() { return (int64_t)kMpOzDig * 2 * kMpOzN * kMpOzPitch * 2 + kMpOzN * 4; }
 // weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
 // max_n / max_d bound the tasks' matrix counts and orders (shared memory)
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,

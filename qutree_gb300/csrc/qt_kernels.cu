@@ -1574,7 +1574,11 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
                            cudaStream_t s) {
   switch (st.kind) {
     case ST_MP:
-      k_mp<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
+      if (st.n_tiles > 0) k_mp<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
+      if (st.noz > 0) {
+        cudaError_t e = launch_mp_oz(t.mp, t.mp_oz_tiles, st.oz0, st.noz, t.mp_oz_tasks, st.ozt0, st.nozt, s);
+        if (e != cudaSuccess) return e;
+      }
       break;
     case ST_HP: {
       typedef typename P::S S;

@@ -507,6 +507,9 @@ class Builder {
     bool split = false;
     const int64_t seg0 = (int64_t)P.hp_segs.size();
     if (kind == ST_HP) split = hp_split(t0, t1, tile0, tile1);
+    const int64_t oz0 = (int64_t)P.mp_oz_tiles.size();
+    const int64_t ozt0 = (int64_t)P.mp_oz_tasks.size();
+    if (kind == ST_MP && P.mp_tensor) tile1 = mp_tensor_tiles(t0, t1, tile0, tile1);
     const double f1 = P.stats.exec_flops;
     Stage s;
     s.flops = f1 - stage_flops_mark;
@@ -521,7 +524,35 @@ class Builder {
     s.aux = split ? 1 : 0;
     s.seg0 = (int)seg0;
     s.nseg = (int)((int64_t)P.hp_segs.size() - seg0);
+    s.oz0 = oz0;
+    s.noz = (int64_t)P.mp_oz_tiles.size() - oz0;
+    s.ozt0 = ozt0;
+    s.nozt = (int64_t)P.mp_oz_tasks.size() - ozt0;
     P.stages.push_back(s);
+  }
+
+  // Tensor-core mode products: the qualifying tasks of a stage [t0, t1) get
+  // tiles of kMpOzRows rows; their classic tiles are dropped from
+  // [tile0, tile1).  Returns the new end of the classic tiles.
+  int64_t mp_tensor_tiles(int64_t t0, int64_t t1, int64_t tile0, int64_t tile1) {
+    std::vector<char> oz(t1 - t0, 0);
+    for (int64_t t = t0; t < t1; ++t) {
+      auto& m = P.mp[t];
+      if (m.diag || m.a_in > 64 || m.a_out > 64) continue;
+      oz[t - t0] = 1;
+      m.oz_h = P.oz_bytes;
+      P.oz_bytes += mp_oz_h_bytes();
+      P.mp_oz_tasks.push_back((int)t);
+      const int64_t rows = (int64_t)m.before * m.after;
+      for (int64_t r = 0; r * kMpOzRows < rows; ++r) P.mp_oz_tiles.push_back(make_int2((int)t, (int)r));
+    }
+    int64_t w = tile0;
+    for (int64_t i = tile0; i < tile1; ++i) {
+      const int2 tl = P.mp_tiles[i];
+      if (tl.x >= t0 && tl.x < t1 && oz[tl.x - t0]) continue;
+      P.mp_tiles[w++] = tl;
+    }
+    return w;
   }
 
   void add_mp(Ref in, Ref out, Ref h, double2 alpha, int node, int mode, bool diag) {
@@ -1963,12 +1994,15 @@ std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTa
     if (prec != 0 && prec != 1) throw std::runtime_error("unknown precision");
     const bool scf = (flavour & 0x2000) != 0;
     if (cdvr) {
-      if ((flavour & ~0x2000) == 2) throw std::runtime_error("the CDVR potential needs the reference or grouped plan");
+      if ((flavour & ~0xA000) == 2) throw std::runtime_error("the CDVR potential needs the reference or grouped plan");
       if (prec != 0) throw std::runtime_error("the CDVR potential runs in complex128 arithmetic");
       if (scf) throw std::runtime_error("the SCF sweep has no CDVR potential (nor has the reference's)");
       if (grad) throw std::runtime_error("no energy gradient with the CDVR potential");
     }
-    Builder b(plan, nodes, ops, sop, flavour & ~0x2000, prec, scratch_budget_elems);
+    if ((flavour & 0x8000) && prec != 1)
+      throw std::runtime_error("tensor-core mode products need double-float arithmetic");
+    plan.mp_tensor = (flavour & 0x8000) != 0;
+    Builder b(plan, nodes, ops, sop, flavour & ~0xA000, prec, scratch_budget_elems);
     b.set_scf(scf);
     b.set_cdvr(cdvr);
     b.run();

@@ -33,7 +33,7 @@ NOISE = 1e-11  # |dPsi rho| on nodes where (1-P) = 0 (rounding noise of a cancel
 
 
 def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
-    df = bool(flavour & qtgpu.QT_PREC_DF64)
+    df = bool(flavour & (qtgpu.QT_PREC_DF64 | qtgpu.QT_PREC_DF64_TC))
     TOL, RAW = (TOL_DF, RAW_DF) if df else (globals()["TOL"], globals()["RAW"])
     flat = psi.flat()
     r = O.derivative(tree, sop, flat, eps=eps, phase=phase)
@@ -75,6 +75,30 @@ FLAVOURS = [qtgpu.QT_PLAN_REFERENCE, qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_COMPRE
 def test_sweep_cfg0(flavour):
     tree, sop, psi = config_problem(0)
     _compare(tree, sop, psi, flavour)
+
+
+# mode products with k <= 64 on the tensor cores (seven 7-bit digits per
+# operand, exact digit products and sums): the double-float tolerances hold
+TC_FLAVOURS = [qtgpu.QT_PLAN_REFERENCE | qtgpu.QT_PREC_DF64_TC, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64_TC,
+               qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC]
+
+
+@pytest.mark.parametrize("cfg", [0, 4])
+@pytest.mark.parametrize("flavour", TC_FLAVOURS)
+def test_sweep_tensor_core_mode_products(cfg, flavour):
+    tree, sop, psi = config_problem(cfg)
+    _compare(tree, sop, psi, flavour)
+
+
+def test_tensor_core_mode_products_with_wide_leaves():
+    """Leaves of 80 grid points: their mode products (k = 80 > 64) stay on
+    the FP32 pipe beside the tensor-core ones of the same stages."""
+    tree = balanced_tree(4, 80, 12)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=np.random.default_rng(8),
+                              omega=1.0)
+    psi = random_wavefunction(tree, 8)
+    for fl in TC_FLAVOURS:
+        _compare(tree, sop, psi, fl, phase=np.exp(0.3j))
 
 
 @pytest.mark.parametrize("flavour", FLAVOURS)
