@@ -618,7 +618,8 @@ cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
 // qualifies when it is not diagonal and a_in, a_out <= 64
 cudaError_t launch_mp_oz(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
                          const int* oz_tasks, int64_t first_task, int64_t n_tasks, cudaStream_t s);
-constexpr int kMpOzRows = 32;  // rows (b, c) per tensor-core mode-product tile
+constexpr int kMpOzRows = 32;  // rows (b, c) per tensor-core sub-tile
+constexpr int kMpOzSub = 4;    // sub-tiles per tile (one block: h's digits loaded once)
 constexpr int kMpOzDig = 7, kMpOzN = 64, kMpOzPitch = 72;
 // digits of one h: [digit][re/im][j][k] bf16 plus 64 row exponents (int)
 inline int64_t mp_oz_h_bytes() { return (int64_t)kMpOzDig * 2 * kMpOzN * kMpOzPitch * 2 + kMpOzN * 4; }

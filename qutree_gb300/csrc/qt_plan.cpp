@@ -532,7 +532,7 @@ class Builder {
   }
 
   // Tensor-core mode products: the qualifying tasks of a stage [t0, t1) get
-  // tiles of kMpOzRows rows; their classic tiles are dropped from
+  // tiles of kMpOzSub x kMpOzRows rows; their classic tiles are dropped from
   // [tile0, tile1).  Returns the new end of the classic tiles.
   int64_t mp_tensor_tiles(int64_t t0, int64_t t1, int64_t tile0, int64_t tile1) {
     std::vector<char> oz(t1 - t0, 0);
@@ -544,7 +544,8 @@ class Builder {
       P.oz_bytes += mp_oz_h_bytes();
       P.mp_oz_tasks.push_back((int)t);
       const int64_t rows = (int64_t)m.before * m.after;
-      for (int64_t r = 0; r * kMpOzRows < rows; ++r) P.mp_oz_tiles.push_back(make_int2((int)t, (int)r));
+      for (int64_t r = 0; r * kMpOzRows * kMpOzSub < rows; ++r)
+        P.mp_oz_tiles.push_back(make_int2((int)t, (int)r));
     }
     int64_t w = tile0;
     for (int64_t i = tile0; i < tile1; ++i) {
