@@ -69,11 +69,11 @@ extern "C" {
 #define QT_PREC_DF64 0x100
 /* Double-float arithmetic as QT_PREC_DF64, with the mode products (k <= 64
  * indices in and out) on the tensor cores: each operand cut into seven 7-bit
- * integer digits against its row exponent, digit products exact in bf16
- * warp-level MMA with exact fp32 sums per level, levels recombined in
- * double-float (error below ~2^-48 of the row maxima per product term).
+ * integer digits against its row exponent (rounded), digit products exact
+ * in bf16 warp-level MMA with exact fp32 sums per level, levels recombined
+ * in double-float (error below ~2^-48 of the row maxima per product term).
  * Same accuracy class and parity tolerances as QT_PREC_DF64; on GB300 the
- * 64-mode sweep runs in 29.5 ms against 34.0 ms. */
+ * 64-mode sweep runs in 29.4 ms against 34.0 ms. */
 #define QT_PREC_DF64_TC 0x200
 
 /* OR-ed into the plan flavour: every sweep also computes the gradient of

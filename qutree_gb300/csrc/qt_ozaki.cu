@@ -4,18 +4,17 @@
 // r = (b, c): X is R x a_in, H^T is a_in x a_out (a_in, a_out <= 64).
 // Each operand value v (double-float: hi + lo) is written against the
 // exponent E of its row of X (resp. its row j of h) as an integer
-//   m = trunc(v 2^(49 - E)),  |v| < 2^E,
-// cut into seven 7-bit digits q_s (sign-magnitude, q_0 most significant):
-//   v = 2^E sum_s q_s 2^(-7 (s + 1)) + (truncation below 2^(E - 49)).
-// Every digit is an integer of magnitude <= 128, exact in bf16; a digit
-// product is exact, and the sum over a_in <= 64 products of one level
-// L = s + t of (at most seven) digit pairs stays below 2^23, so the tensor
-// core's fp32 accumulation is exact.  The levels L = 0..6 (pairs with
-// s + t > 6 fall below the 2^-49 truncation) are scaled by 2^(-7 (L + 2))
-// and summed in double-float, then multiplied by 2^(E_r + F_j) and alpha.
-// The error is below ~2^-48 of |row max of X| |row max of h| per product
-// term, the order of double-float rounding.  Complex products use four real
-// digit products (re re, im im, re im, im re).
+//   m = round(v 2^(49 - E)),  |v| < 2^E,  |m| <= 2^49,
+// cut into seven 7-bit digits q_s (sign-magnitude, q_0 most significant, at
+// most 128): v = 2^E sum_s q_s 2^(-7 (s + 1)) within one unit of 2^(E - 49).
+// Every digit is exact in bf16 and a digit product is exact.  Each level
+// L = s + t <= 6 (pairs with s + t > 6 fall below the 2^-49 rounding) keeps
+// its own fp32 sums of re and im; the real part takes X_re H_re and
+// (-X_im) H_im in one accumulator, at most 2 * 7 * 64 * 128^2 < 2^24 in
+// magnitude, so the tensor core's fp32 sums are exact.  The levels are scaled
+// by 2^(-7 (L + 2)), summed in double-float and multiplied by 2^(E_r + F_j)
+// and alpha.  The error is below ~2^-48 of |row max of X| |row max of h| per
+// product term, the order of double-float rounding, and unbiased.
 //
 // Warp-level mma.sync (m16n8k16, bf16 -> f32) on fragments loaded with
 // ldmatrix.  A block of eight warps takes a tile of kMpOzSub sub-tiles of
@@ -69,53 +68,34 @@ __device__ __forceinline__ float scale2(float v, int k) {
   return v * pow2f(k);
 }
 
-// digits of hi + lo against exponent E (|hi + lo| < 2^E): 7 x 7 bits, with
-// 32-bit integer and float operations only.  In units of 2^(E - 28) the
-// value is I + fr (|fr| < 1): the four top digits come from the integer I,
-// the three low ones from trunc(fr 2^21); the two parts carry their own
-// signs, and v = 2^E sum_s q_s 2^(-7 (s + 1)) up to 2^(E - 49).
-__device__ __forceinline__ void digits(float hi, float lo, int E, uint16_t* dst, int stride) {
-  const float x1 = scale2(hi, 28 - E), y1 = scale2(lo, 28 - E);
-  const float A = truncf(x1), B = truncf(y1);
-  float fr = (x1 - A) + (y1 - B);
-  const float tt = truncf(fr);
-  const int I = (int)A + (int)B + (int)tt;
-  fr -= tt;
-  const int F = (int)truncf(scale2(fr, 21));
-  const unsigned uI = (unsigned)(I < 0 ? -I : I), uF = (unsigned)(F < 0 ? -F : F);
-  const float sI = I < 0 ? -1.f : 1.f, sF = F < 0 ? -1.f : 1.f;
-  const unsigned q[kOzDig] = {uI >> 21, (uI >> 14) & 127u, (uI >> 7) & 127u, uI & 127u,
-                              (uF >> 14) & 127u, (uF >> 7) & 127u, uF & 127u};
-#pragma unroll
-  for (int s = 0; s < kOzDig; ++s) {
-    const float f = (s < 4 ? sI : sF) * (float)q[s];
-    dst[s * stride] = __bfloat16_as_ushort(__float2bfloat16_rn(f));
-  }
-}
-
-// |hi + lo| in units of 2^(E - 49), E = eb - 126, truncated (below two units
-// off), from the floats' bits: no conversions.  eb >= 1 is the largest
-// biased exponent of the row's hi parts (subnormals count as exponent 1).
+// |hi + lo| in units of 2^(E - 49), E = eb - 126, rounded to nearest (within
+// one unit), from the floats' bits: no conversions.  eb >= 1 is the largest
+// biased exponent of the row's hi parts (subnormals count as exponent 1), so
+// the result is at most 2^49.  The parts are taken with four bits more
+// (units of 2^(E - 53)) and the sum rounded.
 __device__ __forceinline__ uint64_t mag49(float hi, float lo, int eb, uint32_t& neg) {
   const uint32_t bh = __float_as_uint(hi), bl = __float_as_uint(lo);
   const int eh = (bh >> 23) & 0xff, el = (bl >> 23) & 0xff;
   const uint32_t mh = (bh & 0x7fffffu) | (eh ? 0x800000u : 0u);
   const uint32_t ml = (bl & 0x7fffffu) | (el ? 0x800000u : 0u);
-  const int sh = max(eh, 1) - eb + 25, sl = max(el, 1) - eb + 25;  // <= 25, resp. <= 1
+  const int sh = max(eh, 1) - eb + 29, sl = max(el, 1) - eb + 29;  // <= 29, resp. <= 5
   const uint64_t uh = sh >= 0 ? (uint64_t)mh << sh : (sh > -24 ? (uint64_t)(mh >> -sh) : 0ull);
   const uint64_t ul = sl >= 0 ? (uint64_t)ml << sl : (sl > -24 ? (uint64_t)(ml >> -sl) : 0ull);
+  uint64_t u2;
   if (((bh ^ bl) >> 31) == 0) {
     neg = bh >> 31;
-    return uh + ul;
+    u2 = uh + ul;
+  } else {
+    neg = uh >= ul ? bh >> 31 : bl >> 31;
+    u2 = uh >= ul ? uh - ul : ul - uh;
   }
-  neg = uh >= ul ? bh >> 31 : bl >> 31;
-  return uh >= ul ? uh - ul : ul - uh;
+  return (u2 + 8) >> 4;
 }
 
-// digit s (7 bits, s = 0 most significant) of a 49-bit magnitude, as the
+// digit s (7 bits, s = 0 most significant) of a magnitude <= 2^49, as the
 // bits of the float q (exact: 2^23 + q - 2^23); its upper half is the bf16
 __device__ __forceinline__ uint32_t digit_f32(uint64_t u, int s) {
-  const uint32_t q = (uint32_t)(u >> (42 - 7 * s)) & 127u;
+  const uint32_t q = s == 0 ? (uint32_t)(u >> 42) : (uint32_t)(u >> (42 - 7 * s)) & 127u;  // q_0 <= 128
   return __float_as_uint(__fsub_rn(__uint_as_float(0x4B000000u | q), 8388608.0f));
 }
 
@@ -151,7 +131,7 @@ __global__ void __launch_bounds__(256) k_mp_oz_h(const MPTask* __restrict__ task
   const int K = t.a_in, N = t.a_out;
   const int Kp = (K + 15) & ~15;
   __shared__ int fx[kOzN];
-  for (int i = threadIdx.x; i < kOzN; i += blockDim.x) fx[i] = 0;
+  for (int i = threadIdx.x; i < kOzN; i += blockDim.x) fx[i] = 1;
   __syncthreads();
   for (int e = threadIdx.x; e < N * K; e += blockDim.x) {
     const int j = e % N, a = e / N;
@@ -163,12 +143,16 @@ __global__ void __launch_bounds__(256) k_mp_oz_h(const MPTask* __restrict__ task
     const int j = e / kOzPitch, a = e % kOzPitch;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
     if (j < N && a < K) v = h[j + (int64_t)N * a];
-    if (a < Kp || a >= kOzPitch) {
-      const int F = fx[j] - 126;
-      digits(v.x, v.y, F, &o->hd[0][0][j][a], 2 * kOzN * kOzPitch);
-      digits(v.z, v.w, F, &o->hd[0][1][j][a], 2 * kOzN * kOzPitch);
-    } else {
-      for (int d = 0; d < kOzDig; ++d) o->hd[d][0][j][a] = o->hd[d][1][j][a] = 0;
+    uint32_t nr = 0, ni = 0;
+    uint64_t ur = 0, ui = 0;
+    if (a < Kp) {
+      ur = mag49(v.x, v.y, fx[j], nr);
+      ui = mag49(v.z, v.w, fx[j], ni);
+    }
+#pragma unroll
+    for (int d = 0; d < kOzDig; ++d) {
+      o->hd[d][0][j][a] = (uint16_t)((digit_f32(ur, d) >> 16) | (nr << 15));
+      o->hd[d][1][j][a] = (uint16_t)((digit_f32(ui, d) >> 16) | (ni << 15));
     }
   }
   for (int i = threadIdx.x; i < kOzN; i += blockDim.x) o->fx[i] = fx[i];
@@ -239,7 +223,12 @@ __device__ __forceinline__ void oz_warp_tile(const OzSmem& sm, const int* ex, in
         h2[z] = acc[0][z][e] * pow2f(-14);
         l2[z] = 0.f;
 #pragma unroll
-        for (int L = 1; L < kOzDig; ++L) df_add(h2[z], l2[z], acc[L][z][e] * pow2f(-7 * (L + 2)), 0.f);
+        for (int L = 1; L < 4; ++L) df_add(h2[z], l2[z], acc[L][z][e] * pow2f(-7 * (L + 2)), 0.f);
+        // levels 4-6 lie below 2^-18 of the row scale: their fp32 sum errs
+        // by less than 2^-42 of it, the size of the digits' truncation
+        // over 64 terms
+        df_add(h2[z], l2[z], fmaf(acc[4][z][e], pow2f(-42), fmaf(acc[5][z][e], pow2f(-49), acc[6][z][e] * pow2f(-56))),
+               0.f);
       }
       const int sh = er + (sm.h.fx[j] - 126);
       float4 v;
