@@ -298,10 +298,13 @@ def run_ours(args, ws, rank, local):
     hg.close()
     others = {}
     for label, fl in (("compressed_complex128", qtgpu.QT_PLAN_COMPRESSED),
-                      ("grouped_double_float", qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64)):
+                      ("grouped_double_float", qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64),
+                      ("compressed_double_float_tensor_core_mode_products",
+                       qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC)):
         ho, otimes, _, _ = timed_sweeps(fl, plain_steps, 1)
         others[label] = {"value": plain_steps / (sum(otimes) * 1e-3), "unit": "sweeps/s",
-                         "steps": plain_steps, "executed_gflop": ho.stats()["exec_flops"] / 1e9}
+                         "steps": plain_steps, "executed_gflop": ho.stats()["exec_flops"] / 1e9,
+                         "energy_rel_err_vs_plain": abs(ho.energy() - plain_energy) / abs(plain_energy)}
         ho.close()
 
     # error of the headline arithmetic against the complex128 plain plan
