@@ -454,8 +454,10 @@ class Builder {
   // ---- stage emission ------------------------------------------------------
   // Blocks of the hole products [t0, t1): output tiles of up to 64 x 64 times
   // ranges of kchunk reduction rows, kchunk chosen so that the stage fills
-  // about four blocks per SM; tasks with several ranges get workspace slots
-  // for their partial tiles.  Returns whether any task was split.
+  // about six blocks per SM, and at least 64 rows (below that, writing and
+  // summing a partial tile costs more than its products); tasks with several
+  // ranges get workspace slots for their partial tiles.  Returns whether any
+  // task was split.
   bool hp_split(int64_t t0, int64_t t1, int64_t& tile0, int64_t& tile1) {
     constexpr int kTile = 64, kRows = 16;
     auto ntiles = [](const Plan::SHP& h) {
@@ -463,9 +465,9 @@ class Builder {
     };
     double work = 0;
     for (int64_t t = t0; t < t1; ++t) work += (double)ntiles(P.hp[t]) * P.hp[t].before * P.hp[t].after;
-    const double target = 4.0 * 152;
+    const double target = 6.0 * 152;
     int64_t kc = (int64_t)std::ceil(work / target / kRows) * kRows;
-    kc = std::max<int64_t>(kc, 256);
+    kc = std::max<int64_t>(kc, 64);
     tile0 = (int64_t)P.hp_tiles.size();
     int64_t ws = 0;
     bool split = false;
