@@ -365,19 +365,23 @@ __global__ void __launch_bounds__(kThreads) k_hp_sum_one(HPTask t, const typenam
   }
 }
 
-// S = sum over the k ranges of the partial tiles (one block per task)
+// S = sum over the k ranges of the partial tiles, in range order; kHpSumChunks
+// blocks of 256 outputs per task (the loads of four ranges in flight)
+constexpr int kHpSumChunks = 16;
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_hp_sum(const HPTask* __restrict__ tasks, int64_t task0,
                                                      const typename P::S* __restrict__ ws) {
   typedef typename P::S S;
   typedef typename P::A A;
-  const HPTask t = tasks[task0 + blockIdx.x];
+  const HPTask t = tasks[task0 + blockIdx.x / kHpSumChunks];
   if (t.splits <= 1) return;
   const int aB = t.aB > 0 ? t.aB : t.a;
   const int64_t n = (int64_t)t.a * aB;
   S* Sp = reinterpret_cast<S*>(t.S);
-  for (int64_t e = threadIdx.x; e < n; e += kThreads) {
+  for (int64_t e = (int64_t)(blockIdx.x % kHpSumChunks) * kThreads + threadIdx.x; e < n;
+       e += (int64_t)kHpSumChunks * kThreads) {
     A acc = P::zero();
+#pragma unroll 4
     for (int z = 0; z < t.splits; ++z) P::add(acc, ws[t.ws + z * n + e]);
     Sp[e] = P::fin(acc);
   }
@@ -1588,7 +1592,7 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
         if (e != cudaSuccess) return e;
       }
       if (st.aux)
-        k_hp_sum<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.hp, st.first_task,
+        k_hp_sum<P><<<(unsigned)(st.n_tasks * kHpSumChunks), kThreads, 0, s>>>(t.hp, st.first_task,
                                                              reinterpret_cast<const S*>(t.hp_ws));
       break;
     }
