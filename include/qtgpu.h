@@ -71,7 +71,8 @@ extern "C" {
  * indices in and out) on the tensor cores: each operand cut into seven 7-bit
  * integer digits against its row exponent (rounded), digit products exact
  * in bf16 warp-level MMA with exact fp32 sums per level, levels recombined
- * in double-float (error below ~2^-48 of the row maxima per product term).
+ * in double-float (error below 2^-44 of the product of the row maxima per
+ * term; measured near 2^-48).
  * Same accuracy class and parity tolerances as QT_PREC_DF64; on GB300 the
  * 64-mode sweep runs in 28.3 ms against 32.9 ms. */
 #define QT_PREC_DF64_TC 0x200

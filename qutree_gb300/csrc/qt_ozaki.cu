@@ -13,8 +13,9 @@
 // (-X_im) H_im in one accumulator, at most 2 * 7 * 64 * 128^2 < 2^24 in
 // magnitude, so the tensor core's fp32 sums are exact.  The levels are scaled
 // by 2^(-7 (L + 2)), summed in double-float and multiplied by 2^(E_r + F_j)
-// and alpha.  The error is below ~2^-48 of |row max of X| |row max of h| per
-// product term, the order of double-float rounding, and unbiased.
+// and alpha.  The error is below 2^-44 of |row max of X| |row max of h| per
+// real product term (the dropped pairs s + t >= 7 and the rounding of both
+// operands); measured errors sit near 2^-48 of it.
 //
 // Warp-level mma.sync (m16n8k16, bf16 -> f32) on fragments loaded with
 // ldmatrix.  A block of eight warps takes a tile of kMpOzSub sub-tiles of

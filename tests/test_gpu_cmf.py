@@ -13,7 +13,8 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64,
-                                     qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64])
+                                     qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64,
+                                     qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC])
 def test_split_graphs_equal_the_sweep(flavour):
     # build + frozen-matrix layer derivatives at the same Psi == one full sweep;
     # bit for bit where both run the same stages, within rounding where the
@@ -29,7 +30,7 @@ def test_split_graphs_equal_the_sweep(flavour):
         h.layer_derivatives()
         if flavour & 0xFF == qtgpu.QT_PLAN_COMPRESSED:
             err, noise = deriv_errors(tree, h.dpsi(), d_full, rho)
-            tol = 1e-11 if flavour & qtgpu.QT_PREC_DF64 else 1e-12
+            tol = 1e-11 if flavour & (qtgpu.QT_PREC_DF64 | qtgpu.QT_PREC_DF64_TC) else 1e-12
             assert err <= tol and noise <= 1e-11
         else:
             assert np.array_equal(h.dpsi(), d_full)
@@ -40,7 +41,8 @@ def test_split_graphs_equal_the_sweep(flavour):
 @pytest.mark.parametrize("flavour,tol", [(qtgpu.QT_PLAN_GROUPED, 1e-11),
                                          (qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64, 1e-10),
                                          (qtgpu.QT_PLAN_COMPRESSED, 1e-11),
-                                         (qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64, 1e-10)])
+                                         (qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64, 1e-10),
+                                         (qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC, 1e-10)])
 def test_cmf_matches_oracle(flavour, tol):
     tree, sop, psi = config_problem(0)
     flat = psi.flat()

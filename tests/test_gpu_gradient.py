@@ -32,7 +32,8 @@ def _gradient(tree, sop, psi, prec, plan=qtgpu.QT_PLAN_GROUPED):
 
 @pytest.mark.parametrize("plan,prec,n_dirs,tol", [
     (qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PREC_F64, 64, 1e-6), (qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PREC_DF64, 16, 1e-6),
-    (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_F64, 32, 1e-6), (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_DF64, 16, 1e-6)])
+    (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_F64, 32, 1e-6), (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_DF64, 16, 1e-6),
+    (qtgpu.QT_PLAN_COMPRESSED, qtgpu.QT_PREC_DF64_TC, 16, 1e-6)])
 def test_gradient_matches_finite_differences(cfg4, plan, prec, n_dirs, tol):
     from tree_energy import energy, fd_directional
     tree, sop, psi = cfg4

@@ -48,11 +48,13 @@ def test_scf_cfg4():
     _check(tree, sop, psi, n_iter=1, n_krylov=4)
 
 
+@pytest.mark.parametrize("prec", [qtgpu.QT_PREC_DF64, qtgpu.QT_PREC_DF64_TC])
 @pytest.mark.parametrize("cfg", [0, 4])
-def test_scf_double_float(cfg):
-    # effective Hamiltonian in double-float, Lanczos and QR in complex128
+def test_scf_double_float(cfg, prec):
+    # effective Hamiltonian in double-float (mode products on the FP32 pipe
+    # or on the tensor cores), Lanczos and QR in complex128
     tree, sop, psi = config_problem(cfg)
-    _check(tree, sop, psi, tol=1e-10, prec=qtgpu.QT_PREC_DF64, n_iter=1, n_krylov=5, n_itp=1, beta=200.0)
+    _check(tree, sop, psi, tol=1e-10, prec=prec, n_iter=1, n_krylov=5, n_itp=1, beta=200.0)
 
 
 def test_scf_ternary_tree_three_body_terms():

@@ -197,11 +197,12 @@ def test_errors_are_reported_not_fatal():
 
 
 @pytest.mark.parametrize("flavour", [qtgpu.QT_PLAN_GROUPED, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64,
-                                     qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64])
+                                     qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64,
+                                     qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC])
 def test_forest_of_uneven_trees(flavour):
     # 24 trees of 8..48 modes, p in {8,16,32}, random bonds 4..24, one plan and
     # one graph; every tree's slice and energy equal its own oracle sweep
-    df = bool(flavour & qtgpu.QT_PREC_DF64)
+    df = bool(flavour & (qtgpu.QT_PREC_DF64 | qtgpu.QT_PREC_DF64_TC))
     tol = TOL_DF if df else TOL
     trees, sops, psis = batched_problem(24)
     f, node_off, mode_off = forest(trees)
