@@ -111,7 +111,8 @@ void qtp_free(void* h) { delete (Handle*)h; }
 
 // Table ids: 0 stages, 1 mp, 2 hp, 3 acc, 4 acc_terms, 5 lin, 6 lin_terms,
 // 7 eig, 8 proj, 9 sizes, 10 identities, 11 rho_off, 12 rhoinv_off,
-// 13 hslot, 14 cslot, 18 cvt, 15 mp alphas, 16 lin coeffs, 17 stats (doubles).
+// 13 hslot, 14 cslot, 18 cvt, 15 mp alphas, 16 lin coeffs, 17 stats (doubles),
+// 40-43 tensor-core mode-product tiles, stage ranges, tasks and classic tiles.
 // qtp_size returns the element count, qtp_get copies.
 static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vector<double>& dv) {
   v.clear();
@@ -425,6 +426,32 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
             v.push_back(P.cd.xhole_raw[m][a]);
             v.push_back(P.cd.xhole[m][a]);
           }
+      break;
+    case 40:  // tensor-core mode-product tiles: (task, tile of kMpOzSub x kMpOzRows rows)
+      for (auto& t : P.mp_oz_tiles) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+      }
+      break;
+    case 41:  // per stage: its tensor-core tiles and tasks (first, count, first, count)
+      for (auto& st : P.stages) {
+        v.push_back(st.oz0);
+        v.push_back(st.noz);
+        v.push_back(st.ozt0);
+        v.push_back(st.nozt);
+      }
+      break;
+    case 42:  // tensor-core tasks: (task, byte offset of its digits of h in B_OZ)
+      for (int t : P.mp_oz_tasks) {
+        v.push_back(t);
+        v.push_back(P.mp[t].oz_h);
+      }
+      break;
+    case 43:  // classic mode-product tiles: (task, first output)
+      for (auto& t : P.mp_tiles) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+      }
       break;
     default:
       break;
