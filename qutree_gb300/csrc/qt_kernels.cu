@@ -22,8 +22,7 @@ namespace qt {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kMpPerThread = 4;
-constexpr int kMpTile = kThreads * kMpPerThread;  // 1024, as in the planner
+constexpr int kMpTile = kThreads;  // slots (up to four outputs each) per mode-product tile, as in the planner
 constexpr int kHpMaxDim = 112;  // largest bond the planner admits
 constexpr int kHpK = 16;
 constexpr int kAccRows = 64;
@@ -36,70 +35,65 @@ __device__ __forceinline__ void cfmac(double2& acc, double2 a, double2 b) { cfma
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return cadd64(a, b); }
 
 // ---------------------------------------------------------------------------
-// Mode-k product (matvec / matrixTensor): one thread per 4 outputs, each a
-// length-a_in dot product of a row of h with a fiber of the input.  Along
-// mode 0 consecutive threads read consecutive rows of h (coalesced) and share
-// the input fiber; along higher modes they read consecutive input elements
-// (coalesced) and share h.
+// Mode-k product (matvec / matrixTensor): one thread per slot (b, j0..j0+3, c)
+// of up to four outputs that share the input fiber in[b, :, c]: per a one
+// input load and four h loads feed four products.  Slots run b fastest:
+// along higher modes consecutive threads read consecutive input elements
+// (coalesced) and share h; along mode 0 (before = 1) they read consecutive
+// groups of h's rows and share the input fiber.
 // ---------------------------------------------------------------------------
 template <class P>
-__device__ __forceinline__ void mp_tile(const MPTask& t, int64_t start) {
+__device__ __forceinline__ void mp_tile(const MPTask& t, int64_t slot0) {
   typedef typename P::S S;
   typedef typename P::A A;
   const S* __restrict__ in = reinterpret_cast<const S*>(t.in);
   const S* __restrict__ h = reinterpret_cast<const S*>(t.h);
   S* out = reinterpret_cast<S*>(t.out);
-  const int64_t total = (int64_t)t.before * t.a_out * t.after;
-  const int64_t slice_in = (int64_t)t.before * t.a_in;
-  int64_t o[kMpPerThread];
-  const S* hp[kMpPerThread];
-  const S* ip[kMpPerThread];
-#pragma unroll
-  for (int q = 0; q < kMpPerThread; ++q) {
-    o[q] = start + threadIdx.x + (int64_t)q * kThreads;
-    int64_t oo = o[q] < total ? o[q] : 0;
-    int64_t b = oo % t.before;
-    int64_t r = oo / t.before;
-    int j = (int)(r % t.a_out);
-    int64_t c = r / t.a_out;
-    hp[q] = h + j;
-    ip[q] = in + b + slice_in * c;
-    if (t.diag) ip[q] += (int64_t)j * t.before;
-  }
+  const int nq = (t.a_out + 3) / 4;
+  const int64_t before = t.before;
+  const int64_t slot = slot0 + threadIdx.x;
+  if (slot >= before * nq * t.after) return;
+  const int64_t b = slot % before;
+  const int64_t r = slot / before;
+  const int j0 = 4 * (int)(r % nq);
+  const int64_t c = r / nq;
+  const int nj = t.a_out - j0 < 4 ? t.a_out - j0 : 4;
+  const S* ip = in + b + before * t.a_in * c;  // in[b, a, c] = ip[before a]
   const bool unit = t.alpha.x == 1.0 && t.alpha.y == 0.0;
   const typename P::C alpha = P::coef(t.alpha);
-  S res[kMpPerThread];
+  S res[4];
   if (t.diag) {
 #pragma unroll
-    for (int q = 0; q < kMpPerThread; ++q) res[q] = P::mul(P::ld(hp[q]), P::ld(ip[q]));
+    for (int q = 0; q < 4; ++q) {
+      const int j = j0 + (q < nj ? q : 0);
+      res[q] = P::mul(P::ld(h + j), P::ld(ip + before * j));
+    }
   } else {
-    A acc[kMpPerThread];
-#pragma unroll
-    for (int q = 0; q < kMpPerThread; ++q) acc[q] = P::zero();
-    const int64_t hs = t.a_out, is = t.before;
+    A acc[4] = {P::zero(), P::zero(), P::zero(), P::zero()};
+    const S* hp = h + j0;  // h(j, a) = h[j + a_out a]
+    const int64_t hs = t.a_out;
     for (int a = 0; a < t.a_in; ++a) {
-      S h0[kMpPerThread], x0[kMpPerThread];
+      const S x = P::ld(ip);
+      S h0[4];
 #pragma unroll
-      for (int q = 0; q < kMpPerThread; ++q) {
-        h0[q] = P::ld(hp[q]);
-        x0[q] = P::ld(ip[q]);
-        hp[q] += hs;
-        ip[q] += is;
-      }
+      for (int q = 0; q < 4; ++q) h0[q] = P::ld(hp + (q < nj ? q : 0));
+      ip += before;
+      hp += hs;
 #pragma unroll
-      for (int q = 0; q < kMpPerThread; ++q) {
-        P::mac(acc[q], h0[q], x0[q]);
+      for (int q = 0; q < 4; ++q) {
+        P::mac(acc[q], h0[q], x);
         if (a & 1) P::norm(acc[q]);
       }
     }
 #pragma unroll
-    for (int q = 0; q < kMpPerThread; ++q) res[q] = P::fin(acc[q]);
+    for (int q = 0; q < 4; ++q) res[q] = P::fin(acc[q]);
   }
 #pragma unroll
-  for (int q = 0; q < kMpPerThread; ++q)
-    if (o[q] < total) {
+  for (int q = 0; q < 4; ++q)
+    if (q < nj) {
+      const int64_t o = b + before * ((j0 + q) + (int64_t)t.a_out * c);
       const S v = unit ? res[q] : P::scale(alpha, res[q]);
-      out[o[q]] = t.add ? P::plus(out[o[q]], v) : v;
+      out[o] = t.add ? P::plus(out[o], v) : v;
     }
 }
 
@@ -1676,8 +1670,8 @@ cudaError_t launch_set_identity(double2* m, int d, int prec, cudaStream_t s) {
 }
 
 cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void*) {
-  const int64_t total = (int64_t)task.before * task.a_out * task.after;
-  const int64_t blocks = (total + kMpTile - 1) / kMpTile;
+  const int64_t slots = (int64_t)task.before * ((task.a_out + 3) / 4) * task.after;
+  const int64_t blocks = (slots + kMpTile - 1) / kMpTile;
   if (blocks == 0) return cudaSuccess;
   (void)cudaGetLastError();
   k_mp_single<<<(unsigned)blocks, kThreads, 0, s>>>(task);

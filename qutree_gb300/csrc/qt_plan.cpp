@@ -43,7 +43,7 @@
 namespace qt {
 namespace {
 
-constexpr int kMpTile = 1024;  // outputs per mode-product tile (256 threads x 4)
+constexpr int kMpTile = 256;  // slots per mode-product tile: (b, four consecutive j, c), one per thread
 constexpr int kAccRows = 64, kAccCols = 16;
 constexpr int64_t kAlign = 16;  // elements (256 bytes)
 
@@ -572,8 +572,8 @@ class Builder {
     t.diag = diag ? 1 : 0;
     int task = (int)P.mp.size();
     P.mp.push_back(t);
-    int64_t outs = g.N;
-    for (int64_t s = 0; s < outs; s += kMpTile) P.mp_tiles.push_back(make_int2(task, (int)s));
+    const int64_t slots = (int64_t)t.before * ((t.a_out + 3) / 4) * t.after;
+    for (int64_t s = 0; s < slots; s += kMpTile) P.mp_tiles.push_back(make_int2(task, (int)s));
     P.stats.exec_flops += diag ? 6.0 * g.N : 8.0 * g.N * g.shape[mode];
   }
 

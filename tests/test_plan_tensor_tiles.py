@@ -2,7 +2,7 @@
 double-float arithmetic), on the CPU: in every mode-product stage the tasks
 with a_in, a_out <= 64 (not diagonal) get tensor-core tiles covering their
 rows exactly once and a private slot for the digits of h; every other task
-keeps its classic tiles, which cover its outputs exactly once."""
+keeps its classic tiles, which cover its output slots exactly once."""
 import numpy as np
 import pytest
 
@@ -11,7 +11,7 @@ from qutree_gb300.model import balanced_tree, config_problem, coupled_oscillator
 
 TENSOR = 0x8000
 OZ_ROWS = 16 * 8  # rows of one tensor-core tile (sub-tiles x rows per sub-tile)
-MP_TILE = 1024    # outputs of one classic tile
+MP_TILE = 256     # slots of one classic tile (b, four consecutive j, c)
 OZ_H_BYTES = 7 * 2 * 64 * 72 * 2 + 64 * 4
 
 
@@ -62,8 +62,8 @@ def test_tensor_core_tiles_cover_eligible_tasks(problem, plan):
             cl.setdefault(int(task), []).append(int(e0))
         assert set(cl) == set(range(t0, t0 + nt)) - eligible
         for t, starts in cl.items():
-            outs = int(mp[t][6]) * int(mp[t][8]) * int(mp[t][9])
-            assert sorted(starts) == list(range(0, outs, MP_TILE))
+            n_slots = int(mp[t][6]) * (-(-int(mp[t][8]) // 4)) * int(mp[t][9])
+            assert sorted(starts) == list(range(0, n_slots, MP_TILE))
         n_oz += len(eligible)
     offs = sorted(slots.values())
     assert len(offs) == len(set(offs)) == n_oz
