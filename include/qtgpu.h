@@ -74,7 +74,7 @@ extern "C" {
  * in double-float (error below 2^-44 of the product of the row maxima per
  * term; measured near 2^-48).
  * Same accuracy class and parity tolerances as QT_PREC_DF64; on GB300 the
- * 64-mode sweep runs in 28.3 ms against 32.9 ms. */
+ * 64-mode sweep runs in 28.3 ms against 32.6 ms. */
 #define QT_PREC_DF64_TC 0x200
 
 /* OR-ed into the plan flavour: every sweep also computes the gradient of
