@@ -8,8 +8,8 @@
 // cut into seven 7-bit digits q_s (sign-magnitude, q_0 most significant, at
 // most 128): v = 2^E sum_s q_s 2^(-7 (s + 1)) within one unit of 2^(E - 49).
 // Every digit is exact in bf16 and a digit product is exact.  Each level
-// L = s + t <= 6 (pairs with s + t > 6 fall below the 2^-49 rounding) keeps
-// its own fp32 sums of re and im; the real part takes X_re H_re and
+// L = s + t <= 6 (pairs with s + t > 6 are dropped) keeps its own fp32 sums
+// of re and im; the real part takes X_re H_re and
 // (-X_im) H_im in one accumulator, at most 2 * 7 * 64 * 128^2 < 2^24 in
 // magnitude, so the tensor core's fp32 sums are exact.  The levels are scaled
 // by 2^(-7 (L + 2)), summed in double-float and multiplied by 2^(E_r + F_j)
@@ -18,11 +18,13 @@
 // operands); measured errors sit near 2^-48 of it.
 //
 // Warp-level mma.sync (m16n8k16, bf16 -> f32) on fragments loaded with
-// ldmatrix.  A block of eight warps takes a tile of kMpOzSub sub-tiles of
-// 32 rows x 64 columns (each warp 16 x 16): h's digits are copied into shared
-// memory once per tile (cp.async, all in flight), and while the warps run the
-// products of one sub-tile, the next sub-tile's X is already on its way into
-// registers.
+// ldmatrix.  A pre-pass writes each task's digits of h once per stage.  A
+// block of sixteen warps copies them into shared memory (cp.async, all in
+// flight) and takes kMpOzSub sub-tiles of 32 rows x 64 columns, each warp a
+// 16 x 8 tile.  The seven levels' sums stay in registers; the loops run digit
+// s of X, k-step, digit u of h, so one A fragment serves every u, and the
+// levels are combined once per sub-tile.  While the warps run the products of
+// one sub-tile, the next sub-tile's X is already on its way into registers.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
