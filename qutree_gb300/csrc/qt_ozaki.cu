@@ -242,6 +242,10 @@ __device__ __forceinline__ void oz_warp_tile(const OzSmem& sm, const int* ex, in
       df_norm(v.x, v.y);
       df_norm(v.z, v.w);
       if (!o.unit) v = DF64::mul(o.alpha, v);
+      if (ex[rl] == 255 || sm.h.fx[j] == 255) {  // an Inf or NaN in the row: propagate it
+        const float nan = __int_as_float(0x7fffffff);
+        v = make_float4(nan, nan, nan, nan);
+      }
       orow[o.before * j] = v;
     }
   }

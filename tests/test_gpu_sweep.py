@@ -252,3 +252,22 @@ def test_checkpoint_round_trip(tmp_path):
             hrep.load(r)
     finally:
         hrep.close()
+
+
+@pytest.mark.parametrize("prec", [qtgpu.QT_PREC_DF64, qtgpu.QT_PREC_DF64_TC])
+def test_non_finite_device_input_is_reported(prec):
+    # a NaN in a Psi uploaded from device memory (no host-side check) reaches
+    # the energy through either arithmetic of the mode products
+    import torch
+    tree, sop, psi = config_problem(0)
+    flat = psi.flat().copy()
+    flat[3] = np.nan
+    dev = torch.from_numpy(flat.view(np.float64)).cuda()
+    hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_COMPRESSED | prec)
+    try:
+        hrep.upload_device(dev.data_ptr())
+        hrep.derivative()
+        with pytest.raises(qtgpu.QtError, match="QT_ERR_NUMERIC"):
+            hrep.energy()
+    finally:
+        hrep.close()
