@@ -572,7 +572,6 @@ cudaError_t launch_set_identity(double2* m, int d, int prec, cudaStream_t s);
 // single-op launches for the primitive C ABI calls
 cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void* scratch);
 cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void* scratch);
-int mp_outputs_per_tile();
 // allocation-free density inverse (scratch in a static device array)
 int64_t static_eig_capacity();
 cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n_mats, int d,

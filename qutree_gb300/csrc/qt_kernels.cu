@@ -998,11 +998,6 @@ inline int64_t eig_smem_bytes(int d) {
   return 16 * ((int64_t)d * d + 2 * np + m) + 8 * (int64_t)np + 16;
 }
 
-}  // namespace
-
-int mp_outputs_per_tile() { return kMpTile; }
-
-namespace {
 __global__ void __launch_bounds__(kThreads) k_axpy(double2* out, const double2* x, double2 a,
                                                    const double2* y, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
