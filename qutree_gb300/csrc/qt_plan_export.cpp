@@ -112,7 +112,8 @@ void qtp_free(void* h) { delete (Handle*)h; }
 // Table ids: 0 stages, 1 mp, 2 hp, 3 acc, 4 acc_terms, 5 lin, 6 lin_terms,
 // 7 eig, 8 proj, 9 sizes, 10 identities, 11 rho_off, 12 rhoinv_off,
 // 13 hslot, 14 cslot, 18 cvt, 15 mp alphas, 16 lin coeffs, 17 stats (doubles),
-// 40-43 tensor-core mode-product tiles, stage ranges, tasks and classic tiles.
+// 40-43 tensor-core mode-product tiles, stage ranges, tasks and classic tiles,
+// 44-48 hole-product splits, tiles, launches, stage launch ranges, workspace.
 // qtp_size returns the element count, qtp_get copies.
 static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vector<double>& dv) {
   v.clear();
@@ -447,11 +448,45 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
         v.push_back(P.mp[t].oz_h);
       }
       break;
-    case 43:  // classic mode-product tiles: (task, first output)
+    case 43:  // classic mode-product tiles: (task, first slot)
       for (auto& t : P.mp_tiles) {
         v.push_back(t.x);
         v.push_back(t.y);
       }
+      break;
+    case 44:  // hole-product tasks: (splits, kchunk, workspace offset, register tile rows, cols)
+      for (auto& t : P.hp) {
+        v.push_back(t.splits);
+        v.push_back(t.kchunk);
+        v.push_back(t.ws);
+        v.push_back(t.rows);
+        v.push_back(t.cols);
+      }
+      break;
+    case 45:  // hole-product tiles: (task, output tile, reduction range)
+      for (auto& t : P.hp_tiles) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+        v.push_back(t.z);
+      }
+      break;
+    case 46:  // hole-product launches: (rows, cols, first tile, tile count)
+      for (auto& t : P.hp_segs) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+        v.push_back(t.z);
+        v.push_back(t.w);
+      }
+      break;
+    case 47:  // per stage: first launch, launches, partial tiles summed (0/1)
+      for (auto& st : P.stages) {
+        v.push_back(st.seg0);
+        v.push_back(st.nseg);
+        v.push_back(st.aux);
+      }
+      break;
+    case 48:  // hole-product workspace size (elements)
+      v.push_back(P.hpw_size);
       break;
     default:
       break;
