@@ -113,7 +113,8 @@ void qtp_free(void* h) { delete (Handle*)h; }
 // 7 eig, 8 proj, 9 sizes, 10 identities, 11 rho_off, 12 rhoinv_off,
 // 13 hslot, 14 cslot, 18 cvt, 15 mp alphas, 16 lin coeffs, 17 stats (doubles),
 // 40-43 tensor-core mode-product tiles, stage ranges, tasks and classic tiles,
-// 44-48 hole-product splits, tiles, launches, stage launch ranges, workspace.
+// 44-48 hole-product splits, tiles, launches, stage launch ranges, workspace,
+// 49-51 accumulation, small matrix-product and conversion tiles.
 // qtp_size returns the element count, qtp_get copies.
 static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vector<double>& dv) {
   v.clear();
@@ -487,6 +488,25 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
       break;
     case 48:  // hole-product workspace size (elements)
       v.push_back(P.hpw_size);
+      break;
+    case 49:  // accumulation tiles: (task, first row, first column)
+      for (auto& t : P.acc_tiles) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+        v.push_back(t.z);
+      }
+      break;
+    case 50:  // small matrix-product tiles: (task, first output)
+      for (auto& t : P.mm_tiles) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+      }
+      break;
+    case 51:  // conversion tiles: (task, first element)
+      for (auto& t : P.cvt_tiles) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+      }
       break;
     default:
       break;

@@ -98,8 +98,8 @@ class PlanView:
         self.tables = {}
         widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
                   20: 6, 22: 6, 23: 4, 24: 27, 25: 8, 26: 12, 27: 11, 28: 2, 29: 11, 33: 3, 34: 10,
-                  35: 8, 36: 2, 38: 14, 39: 5, 40: 2, 41: 4, 42: 2, 43: 2, 44: 5, 45: 3, 46: 4, 47: 3}
-        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 49)):
+                  35: 8, 36: 2, 38: 14, 39: 5, 40: 2, 41: 4, 42: 2, 43: 2, 44: 5, 45: 3, 46: 4, 47: 3, 49: 3, 50: 2, 51: 2}
+        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 52)):
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
