@@ -95,6 +95,7 @@ class PlanView:
             raise ValueError(err.value.decode())
         self.h = h
         self.tree, self.sop = tree, sop
+        self.tensor = bool(flavour & 0x8000)  # mode products with the tensor-core digit arithmetic
         self.tables = {}
         widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
                   20: 6, 22: 6, 23: 4, 24: 27, 25: 8, 26: 12, 27: 11, 28: 2, 29: 11, 33: 3, 34: 10,
@@ -198,7 +199,10 @@ class PlanView:
                         y = x * h[None, :, None]
                     else:
                         h = view(hb, ho, aout * ain).reshape((aout, ain), order="F")
-                        y = np.einsum("ja,bac->bjc", h, x)
+                        if self.tensor and ain <= 64 and aout <= 64:
+                            y = oz_mode_product(h, x)
+                        else:
+                            y = np.einsum("ja,bac->bjc", h, x)
                     view(ob, oo, bef * aout * aft)[:] = (self.mp_alpha[t] * y).ravel(order="F")
                 elif kind == ST_HP:
                     ab, ao, bb, bo, sb, so, bef, a, aft = T[2][t]
@@ -388,6 +392,79 @@ class PlanView:
 # stages): Lanczos on the effective Hamiltonian of each node, Cholesky-QR
 # (twice) toward the next node, R into the next node, buildUp / buildDown.
 # --------------------------------------------------------------------------
+OZ_DIGITS = 7
+
+
+def _oz_mag49(hi, lo, eb):
+    """Vectorised digit magnitudes of hi + lo (float32 arrays) against the
+    rows' largest biased exponents eb (broadcast): (negative, round(|v|
+    2^(49 - E))), from the floats' bits with four guard bits, as qt_ozaki.cu."""
+    bh = hi.view(np.uint32).astype(np.int64)
+    bl = lo.view(np.uint32).astype(np.int64)
+    eh, el = (bh >> 23) & 0xFF, (bl >> 23) & 0xFF
+    mh = (bh & 0x7FFFFF) | np.where(eh > 0, 0x800000, 0)
+    ml = (bl & 0x7FFFFF) | np.where(el > 0, 0x800000, 0)
+    sh = np.maximum(eh, 1) - eb + 29
+    sl = np.maximum(el, 1) - eb + 29
+
+    def shift(m, k):
+        up = np.left_shift(m, np.clip(k, 0, 40))
+        down = np.where(k > -24, np.right_shift(m, np.clip(-k, 0, 40)), 0)
+        return np.where(k >= 0, up, down)
+    uh, ul = shift(mh, sh), shift(ml, sl)
+    same = ((bh ^ bl) >> 31) == 0
+    bigger = uh >= ul
+    u2 = np.where(same, uh + ul, np.abs(uh - ul))
+    neg = np.where(same | bigger, bh >> 31, bl >> 31)
+    return neg, (u2 + 8) >> 4
+
+
+def _oz_digits(v):
+    """Digits of the rows of a complex matrix v (rows x k): the value split
+    into double-float parts, seven signed 7-bit digits per real part against
+    the row's largest exponent.  Returns (E per row, re digits, im digits),
+    digits as float64 arrays (digit, row, k)."""
+    parts = []
+    for comp in (v.real, v.imag):
+        hi = comp.astype(np.float32)
+        lo = (comp - hi.astype(np.float64)).astype(np.float32)
+        parts.append((hi, lo))
+    ex = np.maximum.reduce([(p[0].view(np.uint32) >> 23) & 0xFF for p in parts])
+    eb = np.maximum(ex.max(axis=1, initial=0), 1).astype(np.int64)[:, None]
+    out = []
+    for hi, lo in parts:
+        neg, u = _oz_mag49(hi, lo, eb)
+        sgn = np.where(neg == 1, -1.0, 1.0)
+        dig = [u >> 42] + [(u >> (42 - 7 * s)) & 127 for s in range(1, OZ_DIGITS)]
+        out.append(np.stack([sgn * d for d in dig]).astype(np.float64))
+    return (eb[:, 0] - 126).astype(np.float64), out[0], out[1]
+
+
+def oz_mode_product(h, x):
+    """out[b, j, c] = sum_a h(j, a) x[b, a, c] with the digit arithmetic of
+    the tensor-core mode products: the level sums are exact (float64 holds
+    them exactly), the levels L <= 6 are combined in float64 and scaled by
+    2^(E_r + F_j)."""
+    bef, ain, aft = x.shape
+    X = np.moveaxis(x, 1, -1).reshape(-1, ain)  # one row per (b, c)
+    Ex, xr, xi = _oz_digits(X)
+    Fh, hr, hi = _oz_digits(h)
+    re = np.zeros((X.shape[0], h.shape[0]))
+    im = np.zeros_like(re)
+    for L in range(OZ_DIGITS):
+        sr = np.zeros_like(re)
+        si = np.zeros_like(re)
+        for s in range(L + 1):
+            u = L - s
+            sr += xr[s] @ hr[u].T - xi[s] @ hi[u].T
+            si += xr[s] @ hi[u].T + xi[s] @ hr[u].T
+        re += sr * 2.0 ** (-7 * (L + 2))
+        im += si * 2.0 ** (-7 * (L + 2))
+    scale = np.exp2(Ex[:, None] + Fh[None, :])
+    y = (re + 1j * im) * scale
+    return np.moveaxis(y.reshape(bef, aft, -1), -1, 1)
+
+
 def _mp(h, x, k):
     return np.moveaxis(np.tensordot(h, x, axes=([1], [k])), 0, k)
 

@@ -1,0 +1,61 @@
+"""The tensor-core mode products (QT_PREC_DF64_TC) at the level of a whole
+sweep, on the CPU: the plan interpreter (tests/plan_emulator.py) runs every
+eligible mode product through the same digit arithmetic as qt_ozaki.cu
+(double-float operands, seven 7-bit digits against row exponents, exact
+level sums, levels L <= 6) and the sweep is compared with the oracle at the
+double-float tolerances the GPU tests use."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import deriv_errors, rel_err, rho_weighted
+from plan_emulator import PlanView, oz_mode_product
+from qutree_gb300.model import balanced_tree, config_problem, coupled_oscillators, random_wavefunction
+
+TENSOR = 0x8000
+TOL_DF = 1e-11
+
+
+def test_digit_mode_product_within_bound():
+    rng = np.random.default_rng(4)
+    for bef, ain, aout, aft in ((3, 16, 16, 5), (1, 40, 33, 7), (6, 64, 64, 2)):
+        h = (rng.standard_normal((aout, ain)) + 1j * rng.standard_normal((aout, ain))) * 10.0 ** rng.uniform(-3, 3)
+        x = rng.standard_normal((bef, ain, aft)) + 1j * rng.standard_normal((bef, ain, aft))
+        x[:, : ain // 3] *= 1e-6  # rows with a wide dynamic range
+        got = oz_mode_product(h, x)
+        want = np.einsum("ja,bac->bjc", h, x)
+        xmax = np.abs(np.moveaxis(x, 1, -1)).max(axis=-1)  # per row (b, c)
+        hmax = np.abs(h).max(axis=1)
+        bound = 2.0 ** -43 * ain * np.sqrt(2) * xmax[:, None, :] * hmax[None, :, None]
+        assert np.all(np.abs(got - want) <= bound)
+
+
+def _check(tree, sop, psi, flavour):
+    flat = psi.flat()
+    r = O.derivative(tree, sop, flat)
+    pv = PlanView(tree, sop, flavour | TENSOR, prec=1)
+    pv.run(flat)
+    h00, s00 = pv.energy_parts()
+    assert abs(h00.real / s00.real - r.energy) < TOL_DF * max(1, abs(r.energy))
+    assert rel_err(rho_weighted(tree, pv.dpsi(), r.rho), rho_weighted(tree, r.dpsi, r.rho)) < TOL_DF
+    err, noise = deriv_errors(tree, pv.dpsi(), r.dpsi, r.rho)
+    assert err <= TOL_DF and noise <= 1e-11
+    # the digit arithmetic ran: the same plan without the tensor bit differs at rounding level
+    exact = PlanView(tree, sop, flavour, prec=1)
+    exact.run(flat)
+    assert not np.array_equal(pv.dpsi(), exact.dpsi())
+
+
+@pytest.mark.parametrize("flavour", [0, 1, 2])
+def test_emulated_tensor_core_sweep_cfg0(flavour):
+    tree, sop, psi = config_problem(0)
+    _check(tree, sop, psi, flavour)
+
+
+@pytest.mark.parametrize("leaves,p,b,seed", [(7, 5, 4, 2), (5, 80, 12, 3)])
+def test_emulated_tensor_core_sweep_random_trees(leaves, p, b, seed):
+    # p = 80: the leaf products (k = 80) stay exact, the rest use digits
+    tree = balanced_tree(leaves, p, b)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=np.random.default_rng(seed),
+                              omega=1.0)
+    _check(tree, sop, random_wavefunction(tree, seed), 2)
