@@ -59,3 +59,21 @@ def test_emulated_tensor_core_sweep_random_trees(leaves, p, b, seed):
     sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=np.random.default_rng(seed),
                               omega=1.0)
     _check(tree, sop, random_wavefunction(tree, seed), 2)
+
+
+def test_emulated_tensor_core_forest():
+    # five uneven trees in one compressed plan: small and ragged mode products
+    # (bonds 4..24, k not a multiple of 16) through the digit arithmetic;
+    # each tree's slice equals its own oracle sweep at the double-float tolerances
+    from qutree_gb300.model import batched_problem, forest, forest_psi, forest_sop
+    trees, sops, psis = batched_problem(5)
+    f, node_off, mode_off = forest(trees)
+    pv = PlanView(f, forest_sop(sops, mode_off), 2 | TENSOR, prec=1)
+    pv.run(forest_psi(f, psis).flat())
+    d = pv.dpsi()
+    off = f.offsets()
+    for k, (t, s, p) in enumerate(zip(trees, sops, psis)):
+        r = O.derivative(t, s, p.flat())
+        seg = d[off[node_off[k]]:off[node_off[k] + t.n_nodes]]
+        err, noise = deriv_errors(t, seg, r.dpsi, r.rho)
+        assert err <= TOL_DF and noise <= 1e-11
