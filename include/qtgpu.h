@@ -20,6 +20,14 @@
  *
  * Every call returns a status (QT_OK on success).  The library never exits
  * the process; qt_last_error() describes the last failure of a context.
+ * A call makes its context's device current while it runs and restores the
+ * caller's current device before it returns.  A CUDA error that earlier work
+ * of the calling thread left pending is reported (QT_ERR_CUDA, named as
+ * pending in qt_last_error) rather than cleared silently.
+ * Fault injection for tests: with QT_FAULT_INJECT=alloc:N in the
+ * environment, the N-th device allocation of the library (counted from the
+ * moment the variable took that value) fails as if the device were out of
+ * memory, and the call that made it returns QT_ERR_ALLOC.
  * Calls on one context are ordered on that context's CUDA stream; a context
  * must not be used from two host threads at once.
  */
@@ -76,6 +84,19 @@ extern "C" {
  * Same accuracy class and parity tolerances as QT_PREC_DF64; on GB300 the
  * 64-mode sweep runs in 28.3 ms against 32.6 ms. */
 #define QT_PREC_DF64_TC 0x200
+/* Complex64 arithmetic: every contraction of the sweep computes in complex
+ * FP32 (FP32 multiply-adds and sums, unit roundoff 2^-24) on the FP32 pipe;
+ * node tensors and matrices keep the 16-byte layout of the other
+ * arithmetics (their low words unused).  The density-matrix inverses stay
+ * complex128 as in QT_PREC_DF64.  Error against complex128 ~1e-7 relative
+ * per contraction: the mixed-precision end of the scale, with the error of
+ * every result stated against the complex128 path.  Inputs and outputs of
+ * the C ABI stay complex128. */
+#define QT_PREC_C32 0x400
+/* QT_PREC_C32 with the mode products on the tensor cores as split-TF32
+ * (3 passes: hi*hi + hi*lo + lo*hi of TF32 halves, FP32 accumulation in
+ * tensor memory).  Same accuracy class as QT_PREC_C32. */
+#define QT_PREC_TF32X3 0x800
 
 /* OR-ed into the plan flavour: every sweep also computes the gradient of
  * E = <Psi|H|Psi>/<Psi|Psi> with respect to every node tensor,
@@ -328,7 +349,9 @@ int qt_last_mode_product(qt_ctx* ctx, void* C, const void* A, const void* B,
 
 /* Regularised inverses rhoinv[b] = U diag(1/(w + eps*exp(-w/eps))) U^dagger
  * of n_mats Hermitian d x d matrices rho[b] (column-major, back to back) that
- * already live on the device, without any device allocation.
+ * already live on the device, without any device allocation.  The ranges
+ * rho[0 .. n_mats*d*d) and rhoinv[0 .. n_mats*d*d) must not overlap
+ * (QT_ERR_ARG otherwise).
  *
  * This entry point has no counterpart in the reference.  It exists for
  * callers that cannot call cudaMalloc: code that runs while a CUDA stream is
@@ -341,8 +364,10 @@ int qt_last_mode_product(qt_ctx* ctx, void* C, const void* A, const void* B,
  *   - n_mats * d * d must be <= 524288 (complex elements) and d <= 112;
  *     larger requests fail with QT_ERR_SHAPE and launch nothing.
  *   - The first call on a device looks up the array's device address
- *     (cudaGetSymbolAddress); make that first call before any stream
- *     capture starts.
+ *     (cudaGetSymbolAddress), and so does the first call after the
+ *     device's context was replaced (cudaDeviceReset); make those calls
+ *     before any stream capture starts (inside a capture they fail with
+ *     QT_ERR_CUDA rather than use a stale address).
  *   - All calls share the workspace: calls that overlap on the GPU (other
  *     streams, contexts or threads) race and must be serialised by the
  *     caller.  The workspace needs no clearing between calls.

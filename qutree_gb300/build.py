@@ -18,7 +18,7 @@ LIB = os.path.join(BUILD, "libqtgpu.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 SOURCES = ["qt_api.cu", "qt_kernels.cu", "qt_plan.cpp", "qt_cdvr_plan.cpp",
-           "qt_wsd.cu", "qt_ozaki.cu"]  # qt_plan_export.cpp: host-only lib
+           "qt_wsd.cu", "qt_umma.cu"]  # qt_plan_export.cpp: host-only lib
 # per-file flags: the simultaneous diagonalisation follows a fixed operation
 # order without fused multiply-adds (its CPU restatement does the same)
 EXTRA = {"qt_wsd.cu": ["-fmad=false"]}

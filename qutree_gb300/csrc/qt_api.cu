@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -70,6 +71,72 @@ int cuda_fail(qt_ctx* c, cudaError_t e, const char* where) {
     cudaError_t e_ = (call);                              \
     if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
   } while (0)
+
+// Makes the context's device current for the duration of one entry point and
+// restores the caller's current device on return, so that a host application
+// driving several GPUs keeps its own device selection.  It also reports a
+// CUDA error left pending by earlier, unrelated work of the calling thread
+// instead of silently clearing it.
+struct DevScope {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  bool pending = false;
+  explicit DevScope(int device) {
+    err = cudaGetDevice(&prev);
+    if (err != cudaSuccess) {
+      prev = -1;
+      return;
+    }
+    if (prev != device) err = cudaSetDevice(device);
+    if (err != cudaSuccess) return;
+    err = cudaGetLastError();
+    pending = err != cudaSuccess;
+  }
+  ~DevScope() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+#define QT_DEVICE(c)                                                                                       \
+  DevScope dev_scope_((c)->device);                                                                        \
+  do {                                                                                                     \
+    if (dev_scope_.err != cudaSuccess)                                                                     \
+      return fail(c, QT_ERR_CUDA,                                                                          \
+                  std::string(__func__) +                                                                  \
+                      (dev_scope_.pending ? ": a CUDA error was pending from earlier work of this thread: " \
+                                          : ": cannot make the context's device current: ") +              \
+                      cudaGetErrorString(dev_scope_.err));                                                 \
+  } while (0)
+
+// Every device allocation of the library goes through dev_malloc, so that a
+// test can make a chosen one fail without exhausting the GPU:
+// QT_FAULT_INJECT=alloc:N makes the N-th allocation counted from the moment
+// the variable took its current value fail with cudaErrorMemoryAllocation.
+cudaError_t dev_malloc(void** p, size_t bytes) {
+  static std::mutex mu;
+  static std::string spec;
+  static long count = 0;
+  long nth = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    const char* v = std::getenv("QT_FAULT_INJECT");
+    const std::string cur = v ? v : "";
+    if (cur != spec) {
+      spec = cur;
+      count = 0;
+    }
+    if (spec.compare(0, 6, "alloc:") == 0) {
+      nth = std::atol(spec.c_str() + 6);
+      ++count;
+    }
+  }
+  if (nth > 0 && count == nth) {
+    *p = nullptr;
+    return cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
 
 void release_arena(qt_ctx* c) {
   if (c->exec) cudaGraphExecDestroy(c->exec);
@@ -139,8 +206,15 @@ int qt_ctx_create(qt_ctx** out, int device) {
   qt_ctx* c = new (std::nothrow) qt_ctx();
   if (!c) return fail(nullptr, QT_ERR_ALLOC, "qt_ctx_create: out of host memory");
   c->device = device;
-  e = cudaSetDevice(device);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  DevScope scope(device);
+  if (scope.err != cudaSuccess) {
+    delete c;
+    return fail(nullptr, QT_ERR_CUDA,
+                std::string("qt_ctx_create: ") +
+                    (scope.pending ? "a CUDA error was pending from earlier work of this thread: " : "") +
+                    cudaGetErrorString(scope.err));
+  }
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete c;
     return fail(nullptr, QT_ERR_CUDA, std::string("qt_ctx_create: ") + cudaGetErrorString(e));
@@ -151,7 +225,7 @@ int qt_ctx_create(qt_ctx** out, int device) {
 
 void qt_ctx_destroy(qt_ctx* c) {
   if (!c) return;
-  cudaSetDevice(c->device);
+  DevScope scope(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   release_arena(c);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -162,6 +236,7 @@ const char* qt_last_error(const qt_ctx* c) { return c ? c->err.c_str() : g_noctx
 
 int qt_sync(qt_ctx* c) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   return QT_OK;
 }
@@ -175,6 +250,7 @@ int qt_get_stream(qt_ctx* c, void** s) {
 int qt_tree_upload(qt_ctx* c, int n_nodes, const int* order, const int* dims, const int* parent,
                    const int* child_idx, const int* leaf_mode) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   if (n_nodes <= 0 || !order || !dims || !parent || !child_idx || !leaf_mode)
     return fail(c, QT_ERR_ARG, "qt_tree_upload: null or empty descriptor");
   release_arena(c);
@@ -199,6 +275,7 @@ int qt_sop_upload(qt_ctx* c, int n_ops, const int* op_kind, const int* op_dim, c
                   const double* op_data, int n_terms, const double* coeff, const int* term_ptr,
                   const int* term_mode, const int* term_op) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   if (n_ops <= 0 || n_terms <= 0 || !op_kind || !op_dim || !op_off || !op_data || !coeff ||
       !term_ptr || !term_mode || !term_op)
     return fail(c, QT_ERR_ARG, "qt_sop_upload: null or empty descriptor");
@@ -250,6 +327,7 @@ int qt_cdvr_upload(qt_ctx* c, int n_modes, const int* leaf_dim, const double* le
                    int flags) {
   if (!c || !leaf_dim || !leaf_x || (n_terms > 0 && (!coeff || !term_ptr || !term_mode || !term_power)))
     return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (n_modes < 2 || n_terms < 0) return fail(c, QT_ERR_ARG, "qt_cdvr_upload: bad counts");
   qt::CdvrDesc d;
   int64_t off = 0;
@@ -293,16 +371,19 @@ int qt_set_regularization(qt_ctx* c, double eps) {
 int qt_prepare(qt_ctx* c, int flavour) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->have_tree || !c->have_sop) return fail(c, QT_ERR_STATE, "qt_prepare needs tree and SOP");
-  const bool tensor_mp = (flavour & QT_PREC_DF64_TC) != 0;
-  const int prec = (flavour & (QT_PREC_DF64 | QT_PREC_DF64_TC)) ? 1 : 0;
+  const int prec_bits = flavour & (QT_PREC_DF64 | QT_PREC_DF64_TC | QT_PREC_C32 | QT_PREC_TF32X3);
+  if (prec_bits & (prec_bits - 1)) return fail(c, QT_ERR_ARG, "qt_prepare: more than one QT_PREC_* bit");
+  const bool tensor_mp = (prec_bits & (QT_PREC_DF64_TC | QT_PREC_TF32X3)) != 0;
+  // storage / arithmetic: 0 complex128, 1 double-float, 2 complex64 arithmetic
+  const int prec = (prec_bits & (QT_PREC_DF64 | QT_PREC_DF64_TC)) ? 1 : (prec_bits ? 2 : 0);
   const bool grad = (flavour & QT_PLAN_GRADIENT) != 0;
   const bool scf = (flavour & QT_PLAN_SCF) != 0;
   const bool cdvr = (flavour & QT_PLAN_CDVR) != 0;
-  flavour &= ~(QT_PREC_DF64 | QT_PREC_DF64_TC | QT_PLAN_GRADIENT | QT_PLAN_SCF | QT_PLAN_CDVR);
+  flavour &= ~(prec_bits | QT_PLAN_GRADIENT | QT_PLAN_SCF | QT_PLAN_CDVR);
   if (cdvr && !c->have_cdvr) return fail(c, QT_ERR_STATE, "QT_PLAN_CDVR needs qt_cdvr_upload first");
   if (flavour != QT_PLAN_REFERENCE && flavour != QT_PLAN_GROUPED && flavour != QT_PLAN_COMPRESSED)
     return fail(c, QT_ERR_ARG, "unknown plan flavour");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   release_arena(c);
   int64_t budget = (int64_t)1 << 28;  // scratch elements (4 GiB)
   if (const char* s = std::getenv("QT_SCRATCH_MIB")) {
@@ -321,10 +402,10 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->buf_elems[qt::B_OPS] = (int64_t)c->ops.data.size() / 2;
   c->buf_elems[qt::B_SCR] = std::max<int64_t>(P.scratch_size, 16);
   c->buf_elems[qt::B_PARAM] = 16;
-  c->buf_elems[qt::B_PSI64] = prec == 1 ? P.psi_arena : 0;
-  c->buf_elems[qt::B_DPSI64] = prec == 1 ? P.psi_arena : 0;
+  c->buf_elems[qt::B_PSI64] = prec >= 1 ? P.psi_arena : 0;
+  c->buf_elems[qt::B_DPSI64] = prec >= 1 ? P.psi_arena : 0;
   c->buf_elems[qt::B_GRAD] = grad ? P.psi_arena : 0;
-  c->buf_elems[qt::B_GRAD64] = (grad && prec == 1) ? P.psi_arena : 0;
+  c->buf_elems[qt::B_GRAD64] = (grad && prec >= 1) ? P.psi_arena : 0;
   c->buf_elems[qt::B_KEEP] = P.keep_size;
   c->buf_elems[qt::B_HPW] = P.hpw_size;
   c->buf_elems[qt::B_KRY] = P.kry_size;
@@ -335,7 +416,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     if ((i == qt::B_PSI64 || i == qt::B_DPSI64 || i == qt::B_GRAD64) && prec == 0) continue;  // aliases
     if ((i == qt::B_GRAD || i == qt::B_GRAD64) && !grad) continue;
     int64_t n = std::max<int64_t>(c->buf_elems[i], 16);
-    cudaError_t e = cudaMalloc((void**)&c->buf[i], n * sizeof(double2));
+    cudaError_t e = dev_malloc((void**)&c->buf[i], n * sizeof(double2));
     if (e != cudaSuccess) {
       release_arena(c);
       return fail(c, QT_ERR_ALLOC, std::string("qt_prepare: device allocation failed: ") + cudaGetErrorString(e));
@@ -351,7 +432,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_MATS], 0, c->buf_elems[qt::B_MATS] * 16, c->stream));
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_HPHI], 0, c->buf_elems[qt::B_HPHI] * 16, c->stream));
   QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_DPSI], 0, c->buf_elems[qt::B_DPSI] * 16, c->stream));
-  if (prec == 1) {
+  QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_PARAM], 0, c->buf_elems[qt::B_PARAM] * 16, c->stream));
+  if (prec >= 1) {
     // operator table as double-float pairs (hi, lo) per real number
     c->ops_df.resize(c->ops.data.size());
     float* f = (float*)c->ops_df.data();
@@ -584,7 +666,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, P.mp_oz_tiles);
   put(blob, offs, P.mp_oz_tasks);
   {
-    cudaError_t e = cudaMalloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
+    cudaError_t e = dev_malloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
       release_arena(c);
       return fail(c, QT_ERR_ALLOC, std::string("qt_prepare: task table allocation failed: ") + cudaGetErrorString(e));
@@ -631,6 +713,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.dvl_tiles = (int2*)(base + offs[29]);
   c->tables.ew = (qt::EWTask*)(base + offs[30]);
   c->tables.ew_tiles = (int2*)(base + offs[31]);
+  c->tables.status = reinterpret_cast<int*>(c->buf[qt::B_PARAM] + 15);
   c->tables.mp_oz_tiles = (int2*)(base + offs[32]);
   c->tables.mp_oz_tasks = (int*)(base + offs[33]);
   if (P.cdvr) {  // CDVR constants: seeded noise, leaf grids, identity
@@ -667,7 +750,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     const bool own = P.main_end < (int64_t)P.stages.size();  // separate frozen-matrix stages
     const int64_t b0 = part == 0 ? 0 : (own ? P.main_end : P.apply_begin);
     const int64_t b1 = part == 0 ? P.apply_begin : (own ? (int64_t)P.stages.size() : P.main_end);
-    if (part == 1 && prec == 1) e = qt::launch_stage(P.stages[0], c->tables, c->eps, P.max_eig_d, prec, c->stream);
+    if (part == 1 && prec >= 1) e = qt::launch_stage(P.stages[0], c->tables, c->eps, P.max_eig_d, prec, c->stream);
     for (int64_t i = b0; i < b1 && e == cudaSuccess; ++i)
       e = qt::launch_stage(P.stages[i], c->tables, c->eps, P.max_eig_d, prec, c->stream);
     cudaGraph_t g = nullptr;
@@ -690,6 +773,7 @@ int64_t qt_psi_size(const qt_ctx* c) { return (c && c->prepared) ? c->plan.psi_p
 
 int qt_psi_upload(qt_ctx* c, const double* psi) {
   if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_upload before qt_prepare");
   QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI64], psi, c->plan.psi_packed * 16, cudaMemcpyHostToDevice,
                              c->stream));
@@ -700,6 +784,7 @@ int qt_psi_upload(qt_ctx* c, const double* psi) {
 
 int qt_psi_upload_device(qt_ctx* c, const void* psi) {
   if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_upload_device before qt_prepare");
   QT_CUDA(c, cudaMemcpyAsync(c->buf[qt::B_PSI64], psi, c->plan.psi_packed * 16, cudaMemcpyDeviceToDevice,
                              c->stream));
@@ -710,6 +795,7 @@ int qt_psi_upload_device(qt_ctx* c, const void* psi) {
 
 int qt_psi_download(qt_ctx* c, double* psi) {
   if (!c || !psi) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->have_psi) return fail(c, QT_ERR_STATE, "no wavefunction uploaded");
   QT_CUDA(c, cudaMemcpyAsync(psi, c->buf[qt::B_PSI64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
                              c->stream));
@@ -719,6 +805,7 @@ int qt_psi_download(qt_ctx* c, double* psi) {
 
 int qt_psi_save(qt_ctx* c, const char* path) {
   if (!c || !path) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->have_psi) return fail(c, QT_ERR_STATE, "no wavefunction uploaded");
   std::vector<double2> psi(c->plan.psi_packed);
   QT_CUDA(c, cudaMemcpyAsync(psi.data(), c->buf[qt::B_PSI64], psi.size() * 16, cudaMemcpyDeviceToHost,
@@ -746,6 +833,7 @@ int qt_psi_save(qt_ctx* c, const char* path) {
 
 int qt_psi_load(qt_ctx* c, const char* path) {
   if (!c || !path) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_psi_load before qt_prepare");
   FILE* f = std::fopen(path, "rb");
   if (!f) return fail(c, QT_ERR_ARG, std::string("qt_psi_load: cannot open ") + path);
@@ -795,12 +883,13 @@ int64_t apply_launches(const qt_ctx* c) {
   const qt::Plan& P = c->plan;
   const int64_t n = P.main_end < (int64_t)P.stages.size() ? kernels_in(P, P.main_end, (int64_t)P.stages.size())
                                                           : kernels_in(P, P.apply_begin, P.main_end);
-  return n + (c->prec == 1 ? 1 : 0);
+  return n + (c->prec >= 1 ? 1 : 0);
 }
 }  // namespace
 
 int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_derivative needs qt_prepare and a wavefunction");
   // alpha = -i * phase
   double2 alpha = make_double2(phase_im, -phase_re);
@@ -814,6 +903,7 @@ int qt_derivative(qt_ctx* c, double phase_re, double phase_im) {
 
 int qt_build(qt_ctx* c) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_build needs qt_prepare and a wavefunction");
   QT_CUDA(c, cudaGraphLaunch(c->exec_build, c->stream));
   c->launches += kernels_in(c->plan, 0, c->plan.apply_begin);
@@ -823,6 +913,7 @@ int qt_build(qt_ctx* c) {
 
 int qt_layer_derivatives(qt_ctx* c, double phase_re, double phase_im) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   if (!c->prepared || !c->have_psi || !c->built)
     return fail(c, QT_ERR_STATE, "qt_layer_derivatives needs a qt_build (or qt_derivative) first");
   double2 alpha = make_double2(phase_im, -phase_re);
@@ -872,11 +963,11 @@ int qt_cmf_propagate(qt_ctx* c, double dt, int n_steps, int n_sub, double phase_
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_cmf_propagate needs qt_prepare and a wavefunction");
   if (!(dt > 0) || !std::isfinite(dt) || n_steps < 0 || n_sub < 1)
     return fail(c, QT_ERR_ARG, "qt_cmf_propagate: need dt > 0, n_steps >= 0, n_sub >= 1");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   const int64_t n = c->plan.psi_packed;
   for (auto& b : c->cmf_buf)
     if (!b) {
-      cudaError_t e = cudaMalloc((void**)&b, n * 16);
+      cudaError_t e = dev_malloc((void**)&b, n * 16);
       if (e != cudaSuccess) return fail(c, QT_ERR_ALLOC, "qt_cmf_propagate: work vectors");
     }
   double2* Y0 = c->cmf_buf[0];
@@ -907,6 +998,7 @@ int qt_cmf_propagate(qt_ctx* c, double dt, int n_steps, int n_sub, double phase_
 
 int qt_dpsi_download(qt_ctx* c, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_DPSI64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
                              c->stream));
@@ -916,6 +1008,7 @@ int qt_dpsi_download(qt_ctx* c, double* out) {
 
 int qt_gradient_download(qt_ctx* c, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   if (!c->plan.want_grad) return fail(c, QT_ERR_STATE, "plan prepared without QT_PLAN_GRADIENT");
   QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_GRAD64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
@@ -937,6 +1030,7 @@ int qt_tree_count(const qt_ctx* c) { return (c && c->prepared) ? (int)c->plan.to
 
 int qt_energies(qt_ctx* c, double* out, int n_trees) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   const int nt = (int)c->plan.tops.size();
   if (n_trees < 1 || n_trees > nt) return fail(c, QT_ERR_ARG, "qt_energies: n_trees out of range");
@@ -978,6 +1072,7 @@ int64_t qt_matrices_size(const qt_ctx* c, int which) {
 
 int qt_matrices_download(qt_ctx* c, int which, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
+  QT_DEVICE(c);
   if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
   const Plan& P = c->plan;
   if (which == QT_MAT_CDVR) {
@@ -994,7 +1089,7 @@ int qt_matrices_download(qt_ctx* c, int which, double* out) {
   double2* o = (double2*)out;
   int n = (int)P.nodes.size();
   int64_t cur = 0;
-  if (c->prec == 1 && (which == QT_MAT_HMAT || which == QT_MAT_HCON)) {
+  if (c->prec >= 1 && (which == QT_MAT_HMAT || which == QT_MAT_HCON)) {
     // double-float slots -> complex128
     for (auto& v : mats) {
       float4 f;
@@ -1050,7 +1145,7 @@ int qt_mode_product(qt_ctx* c, void* C, const void* h, const void* B, int64_t be
       before * activeC * after > ((int64_t)1 << 31))
     return fail(c, QT_ERR_SHAPE, "qt_mode_product: bad geometry");
   if (C == B) return fail(c, QT_ERR_ARG, "qt_mode_product: C must not alias B");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   qt::MPTask t;
   t.in = (const double2*)B;
   t.out = (double2*)C;
@@ -1074,7 +1169,7 @@ int qt_hole_product(qt_ctx* c, void* S, const void* A, const void* B, int64_t be
   if (before < 1 || activeA < 1 || activeB < 1 || after < 1 || before * activeA * after > ((int64_t)1 << 31) ||
       before * activeB * after > ((int64_t)1 << 31) || activeA + activeB > 800)
     return fail(c, QT_ERR_SHAPE, "qt_hole_product: bad geometry");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   qt::HPTask t;
   t.A = (const double2*)A;
   t.B = (const double2*)B;
@@ -1100,14 +1195,15 @@ int qt_last_mode_product(qt_ctx* c, void* C, const void* A, const void* B, int64
 
 int qt_dev_alloc(qt_ctx* c, int64_t bytes, void** p) {
   if (!c || !p || bytes <= 0) return fail(c, QT_ERR_ARG, "qt_dev_alloc: bad argument");
-  QT_CUDA(c, cudaSetDevice(c->device));
-  cudaError_t e = cudaMalloc(p, (size_t)bytes);
+  QT_DEVICE(c);
+  cudaError_t e = dev_malloc(p, (size_t)bytes);
   if (e != cudaSuccess) return fail(c, QT_ERR_ALLOC, std::string("qt_dev_alloc: ") + cudaGetErrorString(e));
   return QT_OK;
 }
 
 int qt_dev_free(qt_ctx* c, void* p) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   QT_CUDA(c, cudaFree(p));
   return QT_OK;
@@ -1115,6 +1211,7 @@ int qt_dev_free(qt_ctx* c, void* p) {
 
 int qt_memcpy_h2d(qt_ctx* c, void* dst, const void* src, int64_t bytes) {
   if (!c || !dst || !src || bytes < 0) return fail(c, QT_ERR_ARG, "qt_memcpy_h2d: bad argument");
+  QT_DEVICE(c);
   QT_CUDA(c, cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   return QT_OK;
@@ -1122,6 +1219,7 @@ int qt_memcpy_h2d(qt_ctx* c, void* dst, const void* src, int64_t bytes) {
 
 int qt_memcpy_d2h(qt_ctx* c, void* dst, const void* src, int64_t bytes) {
   if (!c || !dst || !src || bytes < 0) return fail(c, QT_ERR_ARG, "qt_memcpy_d2h: bad argument");
+  QT_DEVICE(c);
   QT_CUDA(c, cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyDeviceToHost, c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
   return QT_OK;
@@ -1148,7 +1246,7 @@ int qt_stage_launch(qt_ctx* c, int i) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!c->prepared || !c->have_psi) return fail(c, QT_ERR_STATE, "qt_stage_launch needs a prepared context and a wavefunction");
   if (i < 0 || i >= (int)c->plan.main_end) return fail(c, QT_ERR_ARG, "no such stage");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   cudaError_t e = qt::launch_stage(c->plan.stages[i], c->tables, c->eps, c->plan.max_eig_d, c->prec,
                                    c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_stage_launch");
@@ -1167,8 +1265,13 @@ int qt_rho_inverse_noalloc(qt_ctx* c, void* rhoinv, const void* rho, int n_mats,
                 "qt_rho_inverse_noalloc: n_mats*d*d = " + std::to_string(need) +
                     " exceeds the static scratch of " + std::to_string(qt::static_eig_capacity()) +
                     " complex elements (8 MiB)");
-  if (rho == rhoinv) return fail(c, QT_ERR_ARG, "qt_rho_inverse_noalloc: rhoinv must not alias rho");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  {
+    // the kernel reads rho while other blocks write rhoinv: the ranges must not overlap at all
+    const uintptr_t r0 = (uintptr_t)rho, w0 = (uintptr_t)rhoinv, bytes = (uintptr_t)need * 16;
+    if (r0 < w0 + bytes && w0 < r0 + bytes)
+      return fail(c, QT_ERR_ARG, "qt_rho_inverse_noalloc: the rho and rhoinv ranges overlap");
+  }
+  QT_DEVICE(c);
   cudaError_t e = qt::launch_rho_inverse_static((const double2*)rho, (double2*)rhoinv, n_mats, d, eps,
                                                 c->stream);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_rho_inverse_noalloc");
@@ -1178,7 +1281,7 @@ int qt_rho_inverse_noalloc(qt_ctx* c, void* rhoinv, const void* rho, int n_mats,
 
 int qt_probe_df64_peak(qt_ctx* c, double* tflops) {
   if (!c || !tflops) return fail(c, QT_ERR_ARG, "null argument");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   double v = 0;
   cudaError_t e = qt::probe_df64_peak(c->stream, &v);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_probe_df64_peak");
@@ -1189,7 +1292,7 @@ int qt_probe_df64_peak(qt_ctx* c, double* tflops) {
 
 int qt_probe_fp64_peak(qt_ctx* c, double* tflops) {
   if (!c || !tflops) return fail(c, QT_ERR_ARG, "null argument");
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   double v = 0;
   cudaError_t e = qt::probe_fp64_peak(c->stream, &v);
   if (e != cudaSuccess) return cuda_fail(c, e, "qt_probe_fp64_peak");
@@ -1433,7 +1536,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
   const int64_t solves = (int64_t)n_iter * (int64_t)order.size();
   if (ritz && ritz_capacity < solves) return fail(c, QT_ERR_ARG, "qt_scf: ritz buffer too small");
   if (ritz_count) *ritz_count = 0;
-  QT_CUDA(c, cudaSetDevice(c->device));
+  QT_DEVICE(c);
   int64_t maxN = 16;
   int maxd = 1;
   for (const auto& g : nd) {
@@ -1446,7 +1549,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
   const int64_t total = (n_krylov + 4) * vstride + 3 * mstride + 512 + ws_elems;
   DevFree work;
   {
-    cudaError_t e = cudaMalloc(&work.p, total * sizeof(cd));
+    cudaError_t e = dev_malloc(&work.p, total * sizeof(cd));
     if (e != cudaSuccess) return fail(c, QT_ERR_ALLOC, std::string("qt_scf: work allocation failed: ") + cudaGetErrorString(e));
   }
   cd* base = (cd*)work.p;
@@ -1462,7 +1565,7 @@ int qt_scf(qt_ctx* c, int n_iter, int n_krylov, int n_itp, double beta, double* 
   cd* hpws = dscal + 512;
   // the driver works on the complex128 wavefunction; with double-float
   // arithmetic the plan's stages read B_PSI, refreshed node by node
-  const bool df = c->prec == 1;
+  const bool df = c->prec >= 1;
   cd* psi = c->buf[qt::B_PSI64];
   cd* psi_ar = c->buf[qt::B_PSI];
   cd* kin = c->buf[qt::B_KRY] + P.kry_in;

@@ -1,6 +1,8 @@
 // qt_arith.cuh -- complex arithmetic policies of the chain kernels.
 //
 // F64   complex128 on the FP64 pipe (double2).
+// C32   complex64 arithmetic on the FP32 pipe in the DF64 storage layout
+//       (below).
 // DF64  complex numbers whose real and imaginary parts are each an
 //       unevaluated sum of two floats, hi + lo ("double-float"), computed on
 //       the FP32 pipe.  GB300 runs FP32 61x faster than FP64; a double-float
@@ -169,6 +171,57 @@ struct DF64 {
     const double den = re * re + im * im;
     const float2 r = df_split(re / den), i = df_split(-im / den);
     return make_float4(r.x, r.y, i.x, i.y);
+  }
+};
+
+// ---- complex64 arithmetic ---------------------------------------------------
+// C32: complex FP32 on the FP32 pipe (four FFMA per complex multiply-add).
+// Storage stays the 16-byte float4 of DF64, (re, re_lo, im, im_lo): loads use
+// the hi words only (a double-float input is rounded to FP32), results are
+// written with zero lo words, so conversions and arenas are shared with DF64.
+struct C32 {
+  typedef float4 S;
+  typedef float4 A;  // (re, 0, im, 0)
+  typedef float4 C;
+  static __device__ __forceinline__ A zero() { return make_float4(0.f, 0.f, 0.f, 0.f); }
+  static __device__ __forceinline__ S ld(const S* p) { return __ldg(p); }
+  static __device__ __forceinline__ void mac(A& acc, const S& a, const S& b) {
+    acc.x = __fmaf_rn(a.x, b.x, acc.x);
+    acc.x = __fmaf_rn(-a.z, b.z, acc.x);
+    acc.z = __fmaf_rn(a.x, b.z, acc.z);
+    acc.z = __fmaf_rn(a.z, b.x, acc.z);
+  }
+  static __device__ __forceinline__ void macc(A& acc, const S& a, const S& b) {
+    acc.x = __fmaf_rn(a.x, b.x, acc.x);
+    acc.x = __fmaf_rn(a.z, b.z, acc.x);
+    acc.z = __fmaf_rn(a.x, b.z, acc.z);
+    acc.z = __fmaf_rn(-a.z, b.x, acc.z);
+  }
+  static __device__ __forceinline__ void add(A& acc, const S& b) {
+    acc.x = __fadd_rn(acc.x, b.x);
+    acc.z = __fadd_rn(acc.z, b.z);
+  }
+  static __device__ __forceinline__ C coef(double2 c) { return make_float4((float)c.x, 0.f, (float)c.y, 0.f); }
+  static __device__ __forceinline__ S fin(const A& a) { return make_float4(a.x, 0.f, a.z, 0.f); }
+  static __device__ __forceinline__ S mul(const S& a, const S& b) {
+    A acc = zero();
+    mac(acc, a, b);
+    return fin(acc);
+  }
+  static __device__ __forceinline__ S scale(const C& c, const S& v) { return mul(c, v); }
+  static __device__ __forceinline__ S plus(const S& a, const S& b) {
+    return make_float4(__fadd_rn(a.x, b.x), 0.f, __fadd_rn(a.z, b.z), 0.f);
+  }
+  static __device__ __forceinline__ void cmac(A& acc, const C& c, const S& b) { mac(acc, c, b); }
+  static __device__ __forceinline__ void norm(A&) {}
+  static __device__ __forceinline__ double mag2(const S& x) {
+    return (double)x.x * (double)x.x + (double)x.z * (double)x.z;
+  }
+  static __device__ __forceinline__ S neg(const S& x) { return make_float4(-x.x, 0.f, -x.z, 0.f); }
+  static __device__ __forceinline__ S recip(const S& x) {
+    const double re = x.x, im = x.z;
+    const double den = re * re + im * im;
+    return make_float4((float)(re / den), 0.f, (float)(-im / den), 0.f);
   }
 };
 

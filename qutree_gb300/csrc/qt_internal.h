@@ -564,6 +564,7 @@ struct DevTables {
   int2* dvl_tiles = nullptr;
   EWTask* ew = nullptr;
   int2* ew_tiles = nullptr;
+  int* status = nullptr;  // device status word: non-zero when a tensor-core stage gave up waiting
 };
 // prec 0: complex128 on the FP64 pipe; 1: double-float on the FP32 pipe
 cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d, int prec,
@@ -613,15 +614,18 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
                         cudaStream_t s);
 // FP64 FMA throughput probe (TFLOP/s) on the given stream; synchronises it
 cudaError_t probe_fp64_peak(cudaStream_t s, double* tflops);
-// double-float mode products on the tensor cores (qt_ozaki.cu): a task
-// qualifies when it is not diagonal and a_in, a_out <= 64
-cudaError_t launch_mp_oz(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
-                         const int* oz_tasks, int64_t first_task, int64_t n_tasks, cudaStream_t s);
-constexpr int kMpOzRows = 32;  // rows (b, c) per tensor-core sub-tile
-constexpr int kMpOzSub = 4;    // sub-tiles per tile (one block: h's digits loaded once)
-constexpr int kMpOzDig = 7, kMpOzN = 64, kMpOzPitch = 72;
-// digits of one h: [digit][re/im][j][k] bf16 plus 64 row exponents (int)
-inline int64_t mp_oz_h_bytes() { return (int64_t)kMpOzDig * 2 * kMpOzN * kMpOzPitch * 2 + kMpOzN * 4; }
+// mode products on the tensor cores (qt_umma.cu, tcgen05): oz = true runs the
+// double-float digit arithmetic, false split-TF32 for complex64 plans; a task
+// qualifies when it is not diagonal and a_in, a_out <= 64.  A wait that runs
+// out writes a non-zero code to *status.
+cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
+                         const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s);
+constexpr int kMpOzRows = 32;  // the planner's tensor-core tiles: kMpOzSub x kMpOzRows = 128 rows (b, c)
+constexpr int kMpOzSub = 4;
+// bytes per task of the h operand's shared-memory image (written by the
+// stage's pre-pass): 4 chunks of 16 k x 7 digits x re/im x 64 x 16 bf16, then
+// 64 row exponents (int)
+inline int64_t mp_oz_h_bytes() { return (int64_t)4 * 7 * 2 * 64 * 16 * 2 + 64 * 4; }
 // weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
 // max_n / max_d bound the tasks' matrix counts and orders (shared memory)
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,

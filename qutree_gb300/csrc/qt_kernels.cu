@@ -14,6 +14,9 @@
 #include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <type_traits>
+
+#include <cuda.h>
 
 #include "qt_arith.cuh"
 #include "qt_internal.h"
@@ -946,7 +949,7 @@ __global__ void __launch_bounds__(kThreads) k_proj2(const ProjTask* __restrict__
 __global__ void k_identity(double2* m, int d, int prec) {
   for (int e = threadIdx.x; e < d * d; e += blockDim.x) {
     const bool diag = (e % d) == (e / d);
-    if (prec == 1)
+    if (prec >= 1)
       reinterpret_cast<float4*>(m)[e] = make_float4(diag ? 1.f : 0.f, 0.f, 0.f, 0.f);
     else
       m[e] = make_double2(diag ? 1.0 : 0.0, 0.0);
@@ -1081,13 +1084,11 @@ __global__ void __launch_bounds__(kThreads) k_convert(void* __restrict__ dst, co
 cudaError_t launch_convert(void* dst, const void* src, int64_t n, int dir, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   const int blocks = (int)std::min<int64_t>((n + kThreads - 1) / kThreads, 152 * 8);
-  (void)cudaGetLastError();
   k_convert<<<blocks, kThreads, 0, s>>>(dst, src, n, dir);
   return cudaGetLastError();
 }
 
 cudaError_t launch_dot(const double2* a, const double2* b, int64_t n, double2* out, cudaStream_t s) {
-  (void)cudaGetLastError();
   // slices of >= 8192 elements, at most kDotParts of them; the partial sums
   // go to out[1 ..] and are added in order by one block into out[0]
   int64_t parts = std::min<int64_t>(kDotParts, std::max<int64_t>(1, (n + 8191) / 8192));
@@ -1119,7 +1120,6 @@ cudaError_t launch_hp_split(const HPTask& task, double2* ws, int64_t ws_elems, c
   t.splits = (int)splits;
   t.kchunk = (int)std::min<int64_t>(K, kc);
   t.ws = 0;
-  (void)cudaGetLastError();
   cudaError_t e = launch_hp_one_shape(t, ntiles, ws, s);
   if (e != cudaSuccess) return e;
   if (t.splits > 1) k_hp_sum_one<F64><<<(unsigned)std::min<int64_t>(64, (per + kThreads - 1) / kThreads), kThreads, 0, s>>>(t, ws);
@@ -1131,7 +1131,6 @@ cudaError_t launch_lincomb(double2* out, const LinComb& lc, int64_t n, cudaStrea
   if (lc.count < 0 || lc.count > kLinCombMax) return cudaErrorInvalidValue;
   const int64_t want = (n + kThreads - 1) / kThreads;
   const int blocks = (int)std::min<int64_t>(want, 152 * 8);
-  (void)cudaGetLastError();
   k_lincomb<<<blocks, kThreads, 0, s>>>(out, lc, n);
   return cudaGetLastError();
 }
@@ -1144,7 +1143,6 @@ cudaError_t launch_axpy(double2* out, const double2* x, double2 a, const double2
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t want = (n + kThreads - 1) / kThreads;
   const int blocks = (int)std::min<int64_t>(want, (int64_t)sms * 8);
-  (void)cudaGetLastError();
   k_axpy<<<blocks, kThreads, 0, s>>>(out, x, a, y, n);
   return cudaGetLastError();
 }
@@ -1569,7 +1567,8 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
     case ST_MP:
       if (st.n_tiles > 0) k_mp<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.mp, t.mp_tiles, st.first_tile);
       if (st.noz > 0) {
-        cudaError_t e = launch_mp_oz(t.mp, t.mp_oz_tiles, st.oz0, st.noz, t.mp_oz_tasks, st.ozt0, st.nozt, s);
+        cudaError_t e = launch_mp_tc(std::is_same<P, DF64>::value, t.mp, t.mp_oz_tiles, st.oz0, st.noz,
+                                     t.mp_oz_tasks, st.ozt0, st.nozt, t.status, s);
         if (e != cudaSuccess) return e;
       }
       break;
@@ -1653,13 +1652,14 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
 
 cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int max_eig_d,
                          int prec, cudaStream_t s) {
-  (void)cudaGetLastError();  // drop a stale error of an unrelated earlier call
-  return prec == 1 ? launch_stage_p<DF64>(st, t, eps, max_eig_d, s)
-                   : launch_stage_p<F64>(st, t, eps, max_eig_d, s);
+  switch (prec) {
+    case 1: return launch_stage_p<DF64>(st, t, eps, max_eig_d, s);
+    case 2: return launch_stage_p<C32>(st, t, eps, max_eig_d, s);
+    default: return launch_stage_p<F64>(st, t, eps, max_eig_d, s);
+  }
 }
 
 cudaError_t launch_set_identity(double2* m, int d, int prec, cudaStream_t s) {
-  (void)cudaGetLastError();
   k_identity<<<1, kThreads, 0, s>>>(m, d, prec);
   return cudaGetLastError();
 }
@@ -1668,7 +1668,6 @@ cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void*) {
   const int64_t slots = (int64_t)task.before * ((task.a_out + 3) / 4) * task.after;
   const int64_t blocks = (slots + kMpTile - 1) / kMpTile;
   if (blocks == 0) return cudaSuccess;
-  (void)cudaGetLastError();
   k_mp_single<<<(unsigned)blocks, kThreads, 0, s>>>(task);
   return cudaGetLastError();
 }
@@ -1680,7 +1679,6 @@ cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void*) {
   if (blocks == 0) return cudaSuccess;
   const int sm = hp_smem_bytes(task.a, aB);
   if (sm > 200 * 1024) return cudaErrorInvalidValue;
-  (void)cudaGetLastError();
   cudaError_t e = cudaFuncSetAttribute(k_hp_single, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (e != cudaSuccess) return e;
   k_hp_single<<<(unsigned)blocks, kThreads, sm, s>>>(task);
@@ -1708,9 +1706,11 @@ cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void*) {
 //     overlap on the GPU (different streams, contexts or host threads) race
 //     on the array and must be ordered by the caller.
 // Host code cannot use the array's name as a device address, so the address
-// is looked up once per device with cudaGetSymbolAddress (with that device
-// current) on the first call that device sees.  That first call should
-// therefore happen before any stream capture begins.
+// is looked up with cudaGetSymbolAddress (with that device current) on the
+// first call that a device sees, and again on the first call after the
+// device's context was replaced (cudaDeviceReset).  Those first calls must
+// happen outside any stream capture; inside one they fail with
+// cudaErrorStreamCaptureUnsupported instead of using a stale address.
 // ---------------------------------------------------------------------------
 constexpr int64_t kStaticEigElems = (int64_t)(8 << 20) / 16;
 static __device__ __align__(256) double2 g_eig_scratch[kStaticEigElems];
@@ -1718,8 +1718,44 @@ static __device__ __align__(256) double2 g_eig_scratch[kStaticEigElems];
 namespace {
 
 constexpr int kMaxDevices = 64;
-double2* g_eig_scratch_addr[kMaxDevices] = {nullptr};
+
+// The array's device address, cached per device together with the identity
+// of the CUDA context it was looked up in.  A device reset (cudaDeviceReset)
+// destroys the primary context and the module with it; the next context may
+// load the module at another address.  Context handles can be reused after a
+// reset, context IDs (cuCtxGetId) are unique for the life of the process, so
+// the cache is keyed by the ID.
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  double2* addr = nullptr;
+};
+ScratchAddr g_eig_scratch_addr[kMaxDevices];
 std::mutex g_eig_scratch_mutex;
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
+
+// ID of the calling thread's current CUDA context (0 and an error if unknown)
+cudaError_t current_ctx_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+    if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess) return e;
+    if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return cudaErrorNotSupported;
+    get_current = (PfnCtxGetCurrent)f1;
+    get_id = (PfnCtxGetId)f2;
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return cudaErrorDeviceUninitialized;
+  if (get_id(ctx, id) != CUDA_SUCCESS) return cudaErrorDeviceUninitialized;
+  return cudaSuccess;
+}
 
 // U[b] = g_eig_scratch + b*d*d; matrix b of the batch is one block
 __global__ void __launch_bounds__(kThreads) k_eig_strided(const double2* __restrict__ rho,
@@ -1747,18 +1783,27 @@ cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n
   if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
   double2* scratch = nullptr;
   {
+    unsigned long long id = 0;
+    e = current_ctx_id(&id);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_eig_scratch_mutex);
-    if (!g_eig_scratch_addr[dev]) {
-      // set-up once per device, with that device current
+    ScratchAddr& cache = g_eig_scratch_addr[dev];
+    if (!cache.addr || cache.ctx_id != id) {
+      // set-up once per device and context, with that device current; it
+      // may load the module, so it must not happen inside a stream capture
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      e = cudaStreamIsCapturing(s, &cs);
+      if (e != cudaSuccess) return e;
+      if (cs != cudaStreamCaptureStatusNone) return cudaErrorStreamCaptureUnsupported;
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_eig_scratch);
       if (e != cudaSuccess) return e;
-      g_eig_scratch_addr[dev] = (double2*)p;
+      cache.addr = (double2*)p;
+      cache.ctx_id = id;
     }
-    scratch = g_eig_scratch_addr[dev];
+    scratch = cache.addr;
   }
   const int64_t sm = eig_smem_bytes(d);
-  (void)cudaGetLastError();
   e = cudaFuncSetAttribute(k_eig_strided, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   k_eig_strided<<<(unsigned)n_mats, kThreads, sm, s>>>(rho, rhoinv, scratch, d, eps);

@@ -92,7 +92,7 @@ class Builder {
     geometry();
     activity();
     layout();
-    if (P.prec == 1) {
+    if (P.prec >= 1) {
       int64_t c0 = (int64_t)P.cvt.size(), t0 = (int64_t)P.cvt_tiles.size();
       add_cvt(Ref{B_PSI64, 0}, Ref{B_PSI, 0}, P.psi_packed, 0);
       emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), t0, (int64_t)P.cvt_tiles.size(), "psi-in");
@@ -375,7 +375,7 @@ class Builder {
     P.s64_off = P.s_off;
     P.d64_off = P.d_off;
     P.m2_64_off = P.m2_off;
-    if (P.prec == 1) {
+    if (P.prec >= 1) {
       for (int i = 0; i < n; ++i) {
         int d = nd[i].dup();
         P.rho64_off[i] = alloc_mat(d);
@@ -388,8 +388,8 @@ class Builder {
       P.tops.push_back(t);
       P.energy_dev_off.push_back(alloc_mat(dt));
       P.stop_dev_off.push_back(alloc_mat(dt));
-      P.energy_off.push_back(P.prec == 1 ? alloc_mat(dt) : P.energy_dev_off.back());
-      P.stop_off.push_back(P.prec == 1 ? alloc_mat(dt) : P.stop_dev_off.back());
+      P.energy_off.push_back(P.prec >= 1 ? alloc_mat(dt) : P.energy_dev_off.back());
+      P.stop_off.push_back(P.prec >= 1 ? alloc_mat(dt) : P.stop_dev_off.back());
       ident[t] = alloc_mat(dt);
       P.identities.push_back({ident[t], dt});
       P.identities.push_back({P.rho_off[t], dt});
@@ -741,7 +741,7 @@ class Builder {
   }
 
   void stage_inverse() {
-    if (P.prec == 1) cvt_mats(P.rho_off, P.rho64_off, 1, "rho-to-f64", false);
+    if (P.prec >= 1) cvt_mats(P.rho_off, P.rho64_off, 1, "rho-to-f64", false);
     int64_t t0 = (int64_t)P.eig.size();
     for (int a = 0; a < n; ++a) {
       Plan::SEig e;
@@ -752,7 +752,7 @@ class Builder {
       P.eig.push_back(e);
     }
     emit_stage(ST_EIG, t0, (int64_t)P.eig.size(), t0, (int64_t)P.eig.size(), "inverse");
-    if (P.prec == 1) cvt_mats(P.rhoinv64_off, P.rhoinv_off, 0, "rhoinv-to-df", false);
+    if (P.prec >= 1) cvt_mats(P.rhoinv64_off, P.rhoinv_off, 0, "rhoinv-to-df", false);
   }
 
   // operators of term l at node a (represent / apply chain body)
@@ -932,7 +932,7 @@ class Builder {
       }
       emit_stage(ST_MM, m0, (int64_t)P.mm.size(), mt0, (int64_t)P.mm_tiles.size(), "overlaps-fused");
     }
-    if (P.prec == 1) {  // the tree energies to complex128 (qt_energy reads them)
+    if (P.prec >= 1) {  // the tree energies to complex128 (qt_energy reads them)
       int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
       for (size_t k = 0; k < tops.size(); ++k) {
         int dt = nd[tops[k]].dup();
@@ -977,7 +977,7 @@ class Builder {
       add_acc(dpsi(a), true, c2(0, 0), a, terms, false);
     }
     emit_stage(ST_ACC, a0, (int64_t)P.acc.size(), atile0, (int64_t)P.acc_tiles.size(), "derivative");
-    if (P.prec == 1) {
+    if (P.prec >= 1) {
       int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
       add_cvt(Ref{B_DPSI, 0}, Ref{B_DPSI64, 0}, P.psi_packed, 1);
       emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "dpsi-out");
@@ -1125,7 +1125,7 @@ class Builder {
       P.acc.back().alpha_ref = mat(alpha[tree_of[a]]);
     }
     emit_stage(ST_ACC, a0, (int64_t)P.acc.size(), atile0, (int64_t)P.acc_tiles.size(), "gradient");
-    if (P.prec == 1) {
+    if (P.prec >= 1) {
       int64_t c0 = (int64_t)P.cvt.size(), ct0 = (int64_t)P.cvt_tiles.size();
       add_cvt(Ref{B_GRAD, 0}, Ref{B_GRAD64, 0}, P.psi_packed, 1);
       emit_stage(ST_CVT, c0, (int64_t)P.cvt.size(), ct0, (int64_t)P.cvt_tiles.size(), "gradient-out");
@@ -1994,7 +1994,7 @@ std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTa
   plan = Plan();
   plan.want_grad = grad;
   try {
-    if (prec != 0 && prec != 1) throw std::runtime_error("unknown precision");
+    if (prec < 0 || prec > 2) throw std::runtime_error("unknown precision");
     const bool scf = (flavour & 0x2000) != 0;
     if (cdvr) {
       if ((flavour & ~0xA000) == 2) throw std::runtime_error("the CDVR potential needs the reference or grouped plan");
@@ -2002,8 +2002,8 @@ std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTa
       if (scf) throw std::runtime_error("the SCF sweep has no CDVR potential (nor has the reference's)");
       if (grad) throw std::runtime_error("no energy gradient with the CDVR potential");
     }
-    if ((flavour & 0x8000) && prec != 1)
-      throw std::runtime_error("tensor-core mode products need double-float arithmetic");
+    if ((flavour & 0x8000) && prec == 0)
+      throw std::runtime_error("tensor-core mode products need double-float or complex64 arithmetic");
     plan.mp_tensor = (flavour & 0x8000) != 0;
     Builder b(plan, nodes, ops, sop, flavour & ~0xA000, prec, scratch_budget_elems);
     b.set_scf(scf);

@@ -29,6 +29,8 @@ QT_PLAN_COMPRESSED = 2
 QT_PREC_F64 = 0x000
 QT_PREC_DF64 = 0x100
 QT_PREC_DF64_TC = 0x200
+QT_PREC_C32 = 0x400
+QT_PREC_TF32X3 = 0x800
 QT_PLAN_GRADIENT = 0x1000
 QT_PLAN_SCF = 0x2000
 QT_PLAN_CDVR = 0x4000

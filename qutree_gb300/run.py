@@ -1,6 +1,7 @@
 """Run H.Psi sweeps of a benchmark configuration from the command line.
 
-  python -m qutree_gb300.run --config 1 --sweeps 2 [--flavour compressed|grouped|reference] [--prec f64|df64|df64_tc]
+  python -m qutree_gb300.run --config 1 --sweeps 2 [--flavour compressed|grouped|reference]
+                             [--prec f64|df64|df64_tc|c32|tf32x3]
 
 Prints one line per sweep (energy, milliseconds).  Used to profile the
 library (ncu) with a fixed, small launch sequence: qt_prepare, then
@@ -20,16 +21,14 @@ def main(argv=None):
     ap.add_argument("--config", type=int, default=1)
     ap.add_argument("--sweeps", type=int, default=2)
     ap.add_argument("--flavour", default="compressed", choices=["compressed", "grouped", "reference"])
-    ap.add_argument("--prec", default="f64", choices=["f64", "df64", "df64_tc"])
+    ap.add_argument("--prec", default="f64", choices=["f64", "df64", "df64_tc", "c32", "tf32x3"])
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     tree, sop, psi = config_problem(a.config)
     flavour = {"compressed": qtgpu.QT_PLAN_COMPRESSED, "grouped": qtgpu.QT_PLAN_GROUPED,
                "reference": qtgpu.QT_PLAN_REFERENCE}[a.flavour]
-    if a.prec == "df64":
-        flavour |= qtgpu.QT_PREC_DF64
-    elif a.prec == "df64_tc":
-        flavour |= qtgpu.QT_PREC_DF64_TC
+    flavour |= {"f64": qtgpu.QT_PREC_F64, "df64": qtgpu.QT_PREC_DF64, "df64_tc": qtgpu.QT_PREC_DF64_TC,
+                "c32": qtgpu.QT_PREC_C32, "tf32x3": qtgpu.QT_PREC_TF32X3}[a.prec]
     hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, device=a.device)
     hrep.upload(psi)
     for i in range(a.sweeps):

@@ -398,7 +398,7 @@ OZ_DIGITS = 7
 def _oz_mag49(hi, lo, eb):
     """Vectorised digit magnitudes of hi + lo (float32 arrays) against the
     rows' largest biased exponents eb (broadcast): (negative, round(|v|
-    2^(49 - E))), from the floats' bits with four guard bits, as qt_ozaki.cu."""
+    2^(49 - E))), from the floats' bits with four guard bits, as qt_umma.cu."""
     bh = hi.view(np.uint32).astype(np.int64)
     bl = lo.view(np.uint32).astype(np.int64)
     eh, el = (bh >> 23) & 0xFF, (bl >> 23) & 0xFF
@@ -442,15 +442,18 @@ def _oz_digits(v):
 
 def oz_mode_product(h, x):
     """out[b, j, c] = sum_a h(j, a) x[b, a, c] with the digit arithmetic of
-    the tensor-core mode products: the level sums are exact (float64 holds
-    them exactly), the levels L <= 6 are combined in float64 and scaled by
-    2^(E_r + F_j)."""
+    the tensor-core mode products: the level sums L = 0, 1, 2 are exact
+    (float64 holds them exactly), the levels 3..6 share one sum rounded to
+    float32 as the device's fourth accumulator is, and everything is scaled
+    by 2^(E_r + F_j)."""
     bef, ain, aft = x.shape
     X = np.moveaxis(x, 1, -1).reshape(-1, ain)  # one row per (b, c)
     Ex, xr, xi = _oz_digits(X)
     Fh, hr, hi = _oz_digits(h)
     re = np.zeros((X.shape[0], h.shape[0]))
     im = np.zeros_like(re)
+    r3 = np.zeros_like(re)
+    i3 = np.zeros_like(re)
     for L in range(OZ_DIGITS):
         sr = np.zeros_like(re)
         si = np.zeros_like(re)
@@ -458,8 +461,14 @@ def oz_mode_product(h, x):
             u = L - s
             sr += xr[s] @ hr[u].T - xi[s] @ hi[u].T
             si += xr[s] @ hi[u].T + xi[s] @ hr[u].T
-        re += sr * 2.0 ** (-7 * (L + 2))
-        im += si * 2.0 ** (-7 * (L + 2))
+        if L < 3:
+            re += sr * 2.0 ** (-7 * (L + 2))
+            im += si * 2.0 ** (-7 * (L + 2))
+        else:
+            r3 += sr * 2.0 ** (-7 * (L - 3))
+            i3 += si * 2.0 ** (-7 * (L - 3))
+    re += r3.astype(np.float32).astype(np.float64) * 2.0 ** (-35)
+    im += i3.astype(np.float32).astype(np.float64) * 2.0 ** (-35)
     scale = np.exp2(Ex[:, None] + Fh[None, :])
     y = (re + 1j * im) * scale
     return np.moveaxis(y.reshape(bef, aft, -1), -1, 1)

@@ -6,8 +6,11 @@ seven 7-bit digits; the digit products of one level L = s + t sum exactly in
 fp32 (magnitude below 2^24); the levels L <= 6 combined give the product
 within 2^-44 of |row max of X| |row max of h| per real product term (the
 dropped pairs s + t >= 7 and the rounding of both operands, with 2^(E + F)
-at most 4 times the product of the row maxima).  The GPU kernel (qt_ozaki.cu) is held to the oracle by the
-sweep parity tests; this file pins the arithmetic those tests rely on."""
+at most 4 times the product of the row maxima).  The GPU kernel
+(qt_umma.cu, tcgen05) sums levels 0, 1 and 2 exactly and levels 3..6 in one
+fp32 accumulator, whose rounding adds at most about 2^-45 of the level-0
+scale per accumulation step; it is held to the oracle by the sweep parity
+tests, this file pins the digit arithmetic those tests rely on."""
 import struct
 from fractions import Fraction
 

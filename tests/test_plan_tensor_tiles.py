@@ -12,7 +12,7 @@ from qutree_gb300.model import balanced_tree, config_problem, coupled_oscillator
 TENSOR = 0x8000
 OZ_ROWS = 16 * 8  # rows of one tensor-core tile (sub-tiles x rows per sub-tile)
 MP_TILE = 256     # slots of one classic tile (b, four consecutive j, c)
-OZ_H_BYTES = 7 * 2 * 64 * 72 * 2 + 64 * 4
+OZ_H_BYTES = 4 * 7 * 2 * 64 * 16 * 2 + 64 * 4  # h image per task: 4 k-chunks x 7 digits x re/im x 64 x 16 bf16, exponents
 
 
 def wide_leaf_problem():
