@@ -49,9 +49,14 @@ def parse():
     ap.add_argument("--no-cdvr", action="store_true", help="skip the supplementary CDVR sweep timing")
     ap.add_argument("--cdvr-sweeps", type=int, default=0,
                     help="only run this many CDVR sweeps of the CDVR workload (for profilers) and exit")
-    ap.add_argument("--precision-steps", type=int, default=0,
-                    help="CMF steps (dt 0.01) of the double-float vs complex128 study on the "
-                         "48..96-bond 64-mode tree (0: skip)")
+    ap.add_argument("--precision-steps", type=int, default=5,
+                    help="CMF steps (dt 0.01) of the precision study on the 48..96-bond 64-mode tree: "
+                         "every arithmetic propagated in lockstep with the reference (0: skip)")
+    ap.add_argument("--precision-ref", default="f64", choices=["f64", "df64"],
+                    help="reference arithmetic of the precision study (df64 for long runs: complex128 "
+                         "costs ~4.5 s per step there)")
+    ap.add_argument("--precision-only", action="store_true",
+                    help="run only the precision study and print its JSON")
     return ap.parse_args()
 
 
@@ -155,6 +160,18 @@ def _rho_weighted_err(tree, dpsi, ref, rho):
     return num / den
 
 
+def measured_peaks():
+    """HBM GB/s and bf16 TFLOP/s (burst) measured on the GB300s, or
+    the stated fallback when the file is absent."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            m = json.load(f)
+        return {"hbm_gbs": float(m["hbm_gbs"]), "bf16_tflops": float(m["bf16_tflops"]),
+                "source": "measured (MEASURED_PEAKS.json)"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
+
+
 def cpu_baseline_sweep(tree, sop, psi, budget_s=45.0):
     """The reference algorithm on the host cores: the oracle restatement with
     QuTree's TensorBLAS path (zgemm from OpenBLAS, all cores).  One full sweep
@@ -200,6 +217,86 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+OTHER_PLANS = (("compressed_complex128", "QT_PLAN_COMPRESSED", "QT_PREC_F64"),
+               ("grouped_double_float", "QT_PLAN_GROUPED", "QT_PREC_DF64"),
+               ("compressed_double_float", "QT_PLAN_COMPRESSED", "QT_PREC_DF64"),
+               ("compressed_complex64", "QT_PLAN_COMPRESSED", "QT_PREC_C32"),
+               ("compressed_tf32x3_tensor_cores", "QT_PLAN_COMPRESSED", "QT_PREC_TF32X3"))
+
+PRECISIONS = (("df64", "QT_PREC_DF64"), ("df64_tc", "QT_PREC_DF64_TC"), ("c64", "QT_PREC_C32"),
+              ("tf32x3", "QT_PREC_TF32X3"))
+
+
+def precision_study(args, local):
+    """Config[3]'s tree (64 modes, bonds 32/58/67/77/86/96, regularisation
+    1e-8): the reference arithmetic and every other one propagate the same Psi
+    in lockstep with constant-mean-field steps of dt = 0.01
+    (qt_cmf_propagate); at checkpoints each runs one derivative sweep of its
+    own state.  Reported per arithmetic: |dE| against the reference, the
+    relative H.Psi error of the sweep (rho-weighted derivative, max over
+    nodes), and ||Psi - Psi_ref|| / ||Psi||."""
+    import numpy as np
+
+    from qutree_gb300 import qtgpu
+    from qutree_gb300.model import config_problem
+
+    t3, s3, p3 = config_problem(3)
+    ref_name = args.precision_ref
+    ref_fl = qtgpu.QT_PREC_F64 if ref_name == "f64" else qtgpu.QT_PREC_DF64
+    arith = [(n, getattr(qtgpu, c)) for n, c in PRECISIONS if not (ref_name == "df64" and n == "df64")]
+    flat = p3.flat()
+    ctx = {}
+    for name, fl in [(ref_name, ref_fl)] + arith:
+        h = qtgpu.HamiltonianRepresentation(s3, t3, flavour=qtgpu.QT_PLAN_COMPRESSED | fl, eps=1e-8, device=local)
+        h.upload(flat)
+        ctx[name] = h
+    steps = args.precision_steps
+    every = max(1, steps // 10)
+    out = {n: {"trajectory": [], "worst": {"abs_dE": 0.0, "dpsi_rel_rho_weighted": 0.0, "psi_rel": 0.0}}
+           for n, _ in arith}
+    step_s = {n: 0.0 for n in ctx}
+    energies = []
+    t0 = time.perf_counter()
+    for step in range(steps + 1):
+        if step > 0:
+            for n, h in ctx.items():
+                ts = time.perf_counter()
+                h.cmf(0.01, 1)
+                h.sync()
+                step_s[n] += time.perf_counter() - ts
+        if step % every and step != steps:
+            continue
+        ref = ctx[ref_name]
+        pr = ref.psi()
+        ref.derivative()
+        er = ref.energy()
+        energies.append(er)
+        rho = ref.matrices(qtgpu.QT_MAT_RHO)
+        dref = ref.dpsi()
+        for n, _ in arith:
+            h = ctx[n]
+            ph = h.psi()
+            h.derivative()
+            r = {"step": step, "abs_dE": abs(h.energy() - er),
+                 "dpsi_rel_rho_weighted": _rho_weighted_err(t3, h.dpsi(), dref, rho),
+                 "psi_rel": float(np.linalg.norm(ph - pr) / np.linalg.norm(pr))}
+            out[n]["trajectory"].append(r)
+            for k in out[n]["worst"]:
+                out[n]["worst"][k] = max(out[n]["worst"][k], r[k])
+    for n in ctx:
+        ctx[n].close()
+    for n, _ in arith:
+        out[n]["final_abs_dE"] = out[n]["trajectory"][-1]["abs_dE"]
+        out[n]["meets_1e-8"] = out[n]["worst"]["abs_dE"] <= 1e-8
+        out[n]["s_per_cmf_step"] = step_s[n] / max(steps, 1)
+    return {"workload": "64 modes, p=32, bonds 32,58,67,77,86,96, 384 terms, regularisation 1e-8",
+            "propagation": f"{steps} constant-mean-field steps of dt = 0.01 (RK4 substeps with frozen mean "
+                           f"fields), every arithmetic in lockstep from the same Psi, checkpoints every {every}",
+            "reference": {"arithmetic": ref_name, "s_per_cmf_step": step_s[ref_name] / max(steps, 1),
+                          "energies": energies},
+            "arithmetics": out, "wall_s": time.perf_counter() - t0}
+
+
 def run_ours(args, ws, rank, local):
     import numpy as np
     import torch
@@ -240,7 +337,7 @@ def run_ours(args, ws, rank, local):
         return hrep, times, clk.summary(), launches
 
     # compressed plan in double-float arithmetic: the headline
-    head = qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64
+    head = qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC
     hrep, times, clocks, launches = timed_sweeps(head, args.steps, args.warmup)
     tot_ms = max_over_ranks(ws, sum(times))
     energy = hrep.energy()
@@ -270,13 +367,24 @@ def run_ours(args, ws, rank, local):
             d["launches"] += 1 / reps
     fp64_peak = hrep.ctx.fp64_peak()
     df64_peak = hrep.ctx.df64_peak()
-    names = {0: "k_mp (mode products)", 1: "k_hp (hole products)", 2: "k_acc (last-mode accumulate)",
+    names = {0: "k_mp_tc + k_mp (mode products: tcgen05 digit MMAs, diagonal ones on the FP32 pipe)",
+             1: "k_hp (hole products)", 2: "k_acc (last-mode accumulate)",
              3: "k_lin (matrix sums)", 4: "k_eig (density inverses)", 5: "k_proj (projectors)",
              6: "k_cvt (precision conversions)", 7: "k_grad (gradient preparation)",
              8: "k_mm (small matrix products)"}
     dom = max(per_kind, key=lambda k: per_kind[k]["ms"])
     d = per_kind[dom]
     achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
+    # the tensor-core mode products: 28 digit pairs x 4 real bf16 products per
+    # complex multiply-add, i.e. 28 bf16 flops per complex128-equivalent flop
+    peaks = measured_peaks()
+    mp = per_kind.get(0)
+    tensor = None
+    if mp and mp["ms"] > 0:
+        bf16 = 28.0 * mp["flops"] / (mp["ms"] * 1e-3) / 1e12
+        tensor = {"kernel": names[0], "ms": mp["ms"], "bf16_tflops": bf16, "bf16_peak": peaks["bf16_tflops"],
+                  "frac": bf16 / peaks["bf16_tflops"], "peak_source": peaks["source"],
+                  "complex128_equivalent_tflops": mp["flops"] / (mp["ms"] * 1e-3) / 1e12}
     total_stage_ms = sum(v["ms"] for v in per_kind.values())
     kernels = {names[k]: {"ms": round(v["ms"], 3), "share": round(v["ms"] / total_stage_ms, 4),
                           "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4),
@@ -287,6 +395,8 @@ def run_ours(args, ws, rank, local):
     # plain (reference call sequence) complex128 plan, and the grouped
     # complex128 plan, for comparison
     plain_steps = max(2, min(args.steps, 4))
+    OTHERS = [(lab, getattr(qtgpu, p) | getattr(qtgpu, a)) for lab, p, a in OTHER_PLANS
+              if getattr(qtgpu, p) | getattr(qtgpu, a) != head]
     hp, ptimes, _, _ = timed_sweeps(qtgpu.QT_PLAN_REFERENCE, plain_steps, 1)
     plain_value = plain_steps / (sum(ptimes) * 1e-3)
     plain_energy = hp.energy()
@@ -297,17 +407,16 @@ def run_ours(args, ws, rank, local):
     grouped64_value = plain_steps / (sum(gtimes) * 1e-3)
     hg.close()
     others = {}
-    for label, fl in (("compressed_complex128", qtgpu.QT_PLAN_COMPRESSED),
-                      ("grouped_double_float", qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64),
-                      ("compressed_double_float_tensor_core_mode_products",
-                       qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC)):
+    for label, fl in OTHERS:
         ho, otimes, _, _ = timed_sweeps(fl, plain_steps, 1)
         others[label] = {"value": plain_steps / (sum(otimes) * 1e-3), "unit": "sweeps/s",
                          "steps": plain_steps, "executed_gflop": ho.stats()["exec_flops"] / 1e9,
-                         "energy_rel_err_vs_plain": abs(ho.energy() - plain_energy) / abs(plain_energy)}
+                         "abs_dE_vs_plain": abs(ho.energy() - plain_energy),
+                         "energy_rel_err_vs_plain": abs(ho.energy() - plain_energy) / abs(plain_energy),
+                         "dpsi_rel_rho_weighted_vs_plain": _rho_weighted_err(tree, ho.dpsi(), plain_dpsi, plain_rho)}
         ho.close()
 
-    # error of the headline arithmetic against the complex128 plain plan
+    # error of the headline arithmetic against the complex128 plain plan (below)
     head_dpsi = None
     # end to end through the C ABI with pinned host buffers
     e2e = None
@@ -436,42 +545,11 @@ def run_ours(args, ws, rank, local):
     if not args.no_cdvr and rank == 0:
         cdvr = cdvr_section(args, local, torch)
 
-    # optional: double-float against complex128 along a constant-mean-field
-    # propagation of the 48..96-bond tree (regularisation 1e-8, dt 0.01)
+    # the precision study: every arithmetic against the reference along a
+    # constant-mean-field propagation of the 48..96-bond tree
     precision = None
     if args.precision_steps > 0 and rank == 0:
-        t3, s3, p3 = config_problem(3)
-        hf = qtgpu.HamiltonianRepresentation(s3, t3, flavour=qtgpu.QT_PLAN_COMPRESSED, eps=1e-8, device=local)
-        hd = qtgpu.HamiltonianRepresentation(s3, t3, flavour=qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64,
-                                             eps=1e-8, device=local)
-        for hh in (hf, hd):
-            hh.upload(p3.flat())
-        rows, worst = [], {"abs_dE": 0.0, "dpsi_rel_rho_weighted": 0.0, "psi_rel": 0.0}
-        every = max(1, args.precision_steps // 10)
-        t0 = time.perf_counter()
-        for step in range(args.precision_steps + 1):
-            if step > 0:
-                hf.cmf(0.01, 1)
-                hd.cmf(0.01, 1)
-            if step % every and step != args.precision_steps:
-                continue
-            pf, pd = hf.psi(), hd.psi()
-            hf.derivative()
-            hd.derivative()
-            ef, ed = hf.energy(), hd.energy()
-            rho = hf.matrices(qtgpu.QT_MAT_RHO)
-            r = {"step": step, "energy": ef, "abs_dE": abs(ed - ef),
-                 "dpsi_rel_rho_weighted": _rho_weighted_err(t3, hd.dpsi(), hf.dpsi(), rho),
-                 "psi_rel": float(np.linalg.norm(pd - pf) / np.linalg.norm(pf))}
-            rows.append(r)
-            for k in worst:
-                worst[k] = max(worst[k], r[k])
-        precision = {"workload": "64 modes, p=32, bonds 32,58,67,77,86,96, 384 terms, regularisation 1e-8",
-                     "propagation": f"{args.precision_steps} constant-mean-field steps, dt = 0.01, "
-                                    "complex128 and double-float contexts in lockstep from the same Psi",
-                     "worst": worst, "trajectory": rows, "wall_s": time.perf_counter() - t0}
-        hf.close()
-        hd.close()
+        precision = precision_study(args, local)
 
     if rank != 0:
         return
@@ -482,8 +560,9 @@ def run_ours(args, ws, rank, local):
         "data": "synthetic (seeded N(0,1) node tensors, QR-orthonormalised)",
         "config": {"workload": WORKLOAD, "plan": "compressed (per node one block matrix of the terms "
                    "inside its subtree, summed mean fields per boundary restriction, represent chains "
-                   "kept in HBM for Apply), double-float arithmetic on the FP32 pipe (complex128 in and "
-                   "out; density inverses complex128)",
+                   "kept in HBM for Apply), double-float arithmetic: mode products on the tcgen05 tensor "
+                   "cores as exact bf16 digit products, the other contractions on the FP32 pipe "
+                   "(complex128 in and out; density inverses complex128)",
                    "parallelism": f"replicas x{ws}",
                    "l2": "flushed between timed sweeps (256 MB fill, outside the events)"},
         "energy": energy,
@@ -504,7 +583,8 @@ def run_ours(args, ws, rank, local):
                                     "MEASURED_PEAKS.json do not bound this path (DRAM < 2% busy)",
                      "fp64_pipe_peak": fp64_peak,
                      "speedup_over_fp64_pipe": achieved / fp64_peak,
-                     "traffic": None, "kernels": kernels},
+                     "traffic": None, "kernels": kernels,
+                     "tensor_core_mode_products": tensor},
         "clocks": clocks,
         "gpu_launches": launches,
     }
@@ -515,7 +595,7 @@ def run_ours(args, ws, rank, local):
     if scf:
         line["scf"] = scf
     if precision:
-        line["precision_study"] = precision
+        line["precision"] = precision
     if grad:
         line["gradient"] = grad
     if cdvr:
@@ -633,6 +713,12 @@ def main():
         h.sync()
         print(json.dumps({"cdvr_sweeps": args.cdvr_sweeps, "energy": h.energy()}))
         h.close()
+        return
+    if args.precision_only:
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local)
+            print(json.dumps({"precision": precision_study(args, local)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args, ws, rank)

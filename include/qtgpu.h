@@ -76,13 +76,18 @@ extern "C" {
 #define QT_PREC_F64 0x000
 #define QT_PREC_DF64 0x100
 /* Double-float arithmetic as QT_PREC_DF64, with the mode products (k <= 64
- * indices in and out) on the tensor cores: each operand cut into seven 7-bit
- * integer digits against its row exponent (rounded), digit products exact
- * in bf16 warp-level MMA with exact fp32 sums per level, levels recombined
- * in double-float (error below 2^-44 of the product of the row maxima per
- * term; measured near 2^-48).
- * Same accuracy class and parity tolerances as QT_PREC_DF64; on GB300 the
- * 64-mode sweep runs in 28.3 ms against 32.6 ms. */
+ * indices in and out) on the fifth-generation tensor cores (tcgen05.mma,
+ * accumulators in tensor memory); hole products and last-index
+ * accumulations stay on the FP32 pipe.  Every operand row is scaled by a
+ * power of two and cut into seven signed digits of at most eight bits by
+ * error-free splits, digit products are exact in bf16, each level of digit
+ * pairs sums exactly in fp32 as far as tensor memory holds separate level
+ * accumulators (all seven for outputs padded to <= 32 columns, five for 48,
+ * four for 64, the last taking the remaining levels), and the levels are
+ * recombined in double-float.  The error is relative to the row maxima of
+ * the operands: 2^-49 of the row scale per value, plus the fp32 rounding of
+ * the last level accumulator.  Parity tolerance 1e-10 per contraction and
+ * projected derivative; energies agree with complex128 to ~1e-13 relative. */
 #define QT_PREC_DF64_TC 0x200
 /* Complex64 arithmetic: every contraction of the sweep computes in complex
  * FP32 (FP32 multiply-adds and sums, unit roundoff 2^-24) on the FP32 pipe;

@@ -481,7 +481,7 @@ struct Plan {
   bool mp_tensor = false;
   std::vector<int2> mp_oz_tiles;
   std::vector<int> mp_oz_tasks;
-  int64_t oz_bytes = 0;  // B_OZ: digits of h per tensor-core task
+  int64_t oz_bytes = 0;  // B_OZ: operand images of the tensor-core tasks of one stage (reused by every stage)
   std::vector<int4> acc_tiles;
   std::vector<int2> cvt_tiles;
   // constant matrices written once at prepare: (offset, d) identity
@@ -625,7 +625,8 @@ constexpr int kMpOzSub = 4;
 // bytes per task of the h operand's shared-memory image (written by the
 // stage's pre-pass): 4 chunks of 16 k x 7 digits x re/im x 64 x 16 bf16, then
 // 64 row exponents (int)
-inline int64_t mp_oz_h_bytes() { return (int64_t)4 * 7 * 2 * 64 * 16 * 2 + 64 * 4; }
+constexpr int64_t kMpOzImageBytes = (int64_t)4 * 7 * 2 * 64 * 16 * 2 + 64 * 4;
+inline int64_t mp_oz_h_bytes() { return kMpOzImageBytes; }
 // weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
 // max_n / max_d bound the tasks' matrix counts and orders (shared memory)
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,

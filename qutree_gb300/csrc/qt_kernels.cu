@@ -1585,8 +1585,8 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
       break;
     }
     case ST_ACC:
-      k_acc<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.acc, t.acc_terms, t.acc_tiles,
-                                                         st.first_tile);
+      if (st.n_tiles > 0)
+        k_acc<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.acc, t.acc_terms, t.acc_tiles, st.first_tile);
       break;
     case ST_LIN:
       k_lin<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.lin, t.lin_terms, st.first_task);

@@ -174,6 +174,7 @@ class Builder {
   std::vector<std::vector<int>> gkey;  // apply group of (term) per node, filled per node
   int64_t mats_cursor = 0;
   double stage_flops_mark = 0;
+  int64_t stage_oz_ = 0;  // bytes of operand images assigned in the stage being emitted
   std::map<std::vector<int>, int64_t> hslot_of_key, cslot_of_key;
 
   double stage_bytes(int kind, int64_t t0, int64_t t1) const {
@@ -511,7 +512,9 @@ class Builder {
     if (kind == ST_HP) split = hp_split(t0, t1, tile0, tile1);
     const int64_t oz0 = (int64_t)P.mp_oz_tiles.size();
     const int64_t ozt0 = (int64_t)P.mp_oz_tasks.size();
+    stage_oz_ = 0;  // operand images are rewritten by every stage's pre-pass
     if (kind == ST_MP && P.mp_tensor) tile1 = mp_tensor_tiles(t0, t1, tile0, tile1);
+    P.oz_bytes = std::max(P.oz_bytes, stage_oz_);
     const double f1 = P.stats.exec_flops;
     Stage s;
     s.flops = f1 - stage_flops_mark;
@@ -542,8 +545,8 @@ class Builder {
       auto& m = P.mp[t];
       if (m.diag || m.a_in > 64 || m.a_out > 64) continue;
       oz[t - t0] = 1;
-      m.oz_h = P.oz_bytes;
-      P.oz_bytes += mp_oz_h_bytes();
+      m.oz_h = stage_oz_;
+      stage_oz_ += mp_oz_h_bytes();
       P.mp_oz_tasks.push_back((int)t);
       const int64_t rows = (int64_t)m.before * m.after;
       for (int64_t r = 0; r * kMpOzRows * kMpOzSub < rows; ++r)

@@ -102,7 +102,9 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 }
 // waits for the completion of the barrier's phase with the given parity; a
 // freshly initialised barrier counts its (virtual) preceding phase, parity
-// 1, as complete.  Gives up after limit_ns nanoseconds and returns false.
+// 1, as complete.  Each poll lets the hardware suspend the thread until the
+// phase completes (at most 100 us), so waiting warps leave the issue slots
+// to the working ones.  Gives up after limit_ns nanoseconds and returns false.
 __device__ __forceinline__ bool mbar_wait(void* bar, uint32_t parity, uint64_t limit_ns) {
   const uint32_t a = smem_u32(bar);
   uint64_t t0 = 0;
@@ -110,13 +112,13 @@ __device__ __forceinline__ bool mbar_wait(void* bar, uint32_t parity, uint64_t l
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "r"(100000u)
         : "memory");
     if (ok) return true;
-    if ((i & 63) == 0) {
+    if ((i & 3) == 0) {
       const uint64_t t = globaltimer_ns();
       if (i == 0)
         t0 = t;

@@ -8,37 +8,39 @@
 //   Y_re += X_re H_re^T - X_im H_im^T,   Y_im += X_re H_im^T + X_im H_re^T,
 // the minus sign by the instruction's negate-A bit.
 //
-// Two arithmetics share the kernel skeleton:
-//  * OZ (double-float plans, QT_PREC_DF64_TC): every operand value (hi + lo)
-//    is written against the exponent of its row of X (resp. its row j of h)
-//    as an integer of 49 bits cut into seven 7-bit digits q_s (s = 0 most
-//    significant, |q_0| <= 128), stored in bf16 as q_s 2^(-7s), exactly.
-//    Digit products are exact; pairs with s + t <= 6 are summed in fp32
-//    accumulators per output, one per level L = s + t (sums of at most
-//    7 * 2 * 64 * 128^2 < 2^24 in units of the level: exact) as far as
-//    tensor memory holds them -- NL = min(7, 512 / (2 Np)) accumulators for
-//    Np padded output columns: all seven levels for Np <= 32, five for
-//    Np = 48, four for Np = 64 -- the last one taking the remaining levels
-//    together.  Its fp32 rounding is the method's error: about 2^-24 of the
-//    size of level NL - 1, i.e. ~1e-10 of a typical output with four
-//    accumulators, ~1e-12 with five, none beyond the digits' truncation
-//    (2^-44 of the row maxima) with seven.  The epilogue adds the levels in
-//    double-float and scales by 2^(E_row + F_j - 14).
+// Two arithmetics share the kernel:
+//  * OZ (double-float plans, QT_PREC_DF64_TC): every operand row (of X, resp.
+//    of h) is scaled by the power of two 2^-E of its largest exponent and cut
+//    into seven signed digits by error-free splits
+//    x_s = fl(fl(r + sigma_s) - sigma_s), sigma_s = 1.5 * 2^(16 - 7s): x_s is
+//    r rounded to a multiple of 2^(-7(s+1)), r - x_s is exact, the value's low
+//    word joins from s = 3.  The digit integers q_s = x_s 2^(7(s+1)) have
+//    |q_s| <= 128, so q_s 2^(-7s) is exact in bf16 and every digit product is
+//    exact.  Pairs with s + t <= 6 are summed in fp32 accumulators, one per
+//    level L = s + t (sums of at most 7 * 2 * 64 * 128^2 < 2^24 units of the
+//    level: exact) as far as tensor memory holds them -- NL = min(7, 512 /
+//    (2 Np)) accumulators for Np padded output columns: all seven levels for
+//    Np <= 32, five for Np = 48, four for Np = 64 -- the last one taking the
+//    remaining levels together; its fp32 rounding is the method's error
+//    beyond the digits' truncation (2^-49 of the row scale).  The epilogue
+//    adds the levels in double-float and scales by 2^(E_row + F_j); the
+//    task's coefficient is already in the h operand.
 //  * TF (complex64 plans, QT_PREC_TF32X3): X and h (fp32) split into TF32
 //    halves hi + lo; hi*hi + hi*lo + lo*hi accumulate in one fp32 sum per
 //    output (split-TF32, 3 passes).
 //
-// Roles (288 threads): warps 0-3 produce the operand X of each 16-wide
-// k-chunk into a two-stage shared-memory ring (one thread per row: first
-// the row's exponent over all of K, then the digits / TF32 halves chunk by
-// chunk); warp 8 allocates tensor memory, loads the h operand of the tile's
-// task (prepared once per stage by a pre-pass in the exact shared-memory
-// image) with bulk copies, and issues the MMAs from one thread; warps 4-7
-// read the accumulators (warp 4 + q owns tensor-memory lanes 32q..32q+31,
-// i.e. rows 32q..) and write the outputs.  A CTA takes a contiguous range of
-// 128-row tiles, so consecutive tiles mostly share the task and its h.
-// Every wait is bounded: a wait that runs out sets the status word, and the
-// CTA drains its issued MMAs, frees tensor memory and returns.
+// Roles (416 threads): warps 0-7 produce the operand X of each 16-wide
+// k-chunk into a two-stage shared-memory ring (two threads per row, each
+// taking half of the row: first the row's exponent over all of K, then the
+// digits / TF32 halves chunk by chunk, the next chunk's loads in flight);
+// warp 12 allocates tensor memory, loads the h operand of the unit (prepared
+// once per stage by a pre-pass in the exact shared-memory image) with bulk
+// copies, and issues the MMAs from one thread; warps 8-11 read the
+// accumulators (warp 8 + q owns tensor-memory lanes 32q..32q+31, i.e. rows
+// 32q..) and write the outputs.  A CTA takes a contiguous range of 128-row
+// tiles, so consecutive tiles mostly share the task and its h.  Every wait
+// is bounded: a wait that runs out sets the status word, and the CTA drains
+// its issued MMAs, frees tensor memory and returns.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -54,7 +56,7 @@ using namespace tc05;
 
 constexpr int kRows = 128;                 // rows per tile (M)
 constexpr int kDig = 7;                    // digits per value (OZ)
-constexpr int kThreadsTc = 288;            // 4 producer warps, 4 epilogue warps, 1 MMA warp
+constexpr int kThreadsTc = 416;            // 8 producer warps, 4 epilogue warps, 1 MMA warp
 constexpr uint64_t kSpin = 2000000000ull;  // ns before a wait gives up (2 s)
 constexpr int kChunkK = 16;                // k per ring stage
 
@@ -66,16 +68,17 @@ constexpr int kOzBMax = 4 * kDig * 2 * 64 * 32;       // 114688: K 64, N 64
 constexpr int kTfAPlane = kRows * kChunkK * 4;        // 8192 bytes
 constexpr int kTfAStage = 4 * kTfAPlane;              // hi_re, hi_im, lo_re, lo_im
 constexpr int kTfBMax = 4 * 4 * 64 * 64;              // 65536: K 64, N 64
+static_assert(kOzBMax + 64 * 4 <= kMpOzImageBytes && kTfBMax <= kMpOzImageBytes, "operand image slot too small");
 
 template <bool OZ>
 struct Cfg {
   static constexpr int AStage = OZ ? kOzAStage : kTfAStage;
   static constexpr int BMax = OZ ? kOzBMax : kTfBMax;
-  static constexpr int BHeader = BMax;  // F_j (OZ) follow the digit planes in the global image
+  static constexpr int BHeader = kOzBMax;  // F_j (OZ) follow the digit planes in the global image
 };
 
 struct Bars {
-  uint64_t full[2], empty[2], exready[2], exfree[2], tfull, tempty, bfull, drain;
+  uint64_t full[2], empty[2], exready[2], exfree[2], pmax[2], tfull, tempty, bfull, drain;
   uint32_t tmem;
   int pad;
 };
@@ -85,9 +88,11 @@ struct TcSmem {
   unsigned char b[Cfg<OZ>::BMax];
   unsigned char a[2][Cfg<OZ>::AStage];
   Bars bar;
-  int ex[2][kRows];    // row exponents (OZ) of the two tiles in flight
-  int orow[2][kRows];  // output offset of each row (-1: past the end)
+  uint8_t ex[2][kRows];     // biased row exponents (OZ) of the two units in flight
+  uint8_t pm[2][2][kRows];  // the two halves' partial row exponents
+  int fx[4][64];            // column exponents of h, one copy per epilogue warp
 };
+static_assert(sizeof(TcSmem<true>) <= 232448, "shared memory of the digit kernel exceeds 227 KB");
 
 __device__ __forceinline__ int fexp(float v) { return (__float_as_int(v) >> 23) & 0xff; }
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
@@ -97,33 +102,41 @@ __device__ __forceinline__ float scale2(float v, int k) {
   return v * pow2f(k);
 }
 
-// |hi + lo| in units of 2^(E - 49), E = eb - 126, rounded to nearest; the
-// sign in neg.  eb >= 1 is the row's largest biased exponent of hi parts.
-__device__ __forceinline__ uint64_t mag49(float hi, float lo, int eb, uint32_t& neg) {
-  const uint32_t bh = __float_as_uint(hi), bl = __float_as_uint(lo);
-  const int eh = (bh >> 23) & 0xff, el = (bl >> 23) & 0xff;
-  const uint32_t mh = (bh & 0x7fffffu) | (eh ? 0x800000u : 0u);
-  const uint32_t ml = (bl & 0x7fffffu) | (el ? 0x800000u : 0u);
-  const int sh = max(eh, 1) - eb + 29, sl = max(el, 1) - eb + 29;
-  const uint64_t uh = sh >= 0 ? (uint64_t)mh << sh : (sh > -24 ? (uint64_t)(mh >> -sh) : 0ull);
-  const uint64_t ul = sl >= 0 ? (uint64_t)ml << sl : (sl > -24 ? (uint64_t)(ml >> -sl) : 0ull);
-  uint64_t u2;
-  if (((bh ^ bl) >> 31) == 0) {
-    neg = bh >> 31;
-    u2 = uh + ul;
-  } else {
-    neg = uh >= ul ? bh >> 31 : bl >> 31;
-    u2 = uh >= ul ? uh - ul : ul - uh;
-  }
-  return (u2 + 8) >> 4;
+// Digits of one double-float value v = hi + lo of a row whose largest biased
+// exponent of hi parts is eb (|v| < 2^E, E = eb - 126).  The row is scaled
+// to |v 2^-E| < 1 (exactly, by a power of two) and cut by error-free splits
+// x_s = fl(fl(r + sigma_s) - sigma_s), sigma_s = 1.5 * 2^(16 - 7s): x_s is r
+// rounded to the nearest multiple of 2^(-7(s+1)) and r - x_s is exact, so
+// v 2^-E = x_0 + ... + x_6 + (remainder of at most 2^-49).  The low part
+// joins from s = 3 (|lo| is below 2^-24 of the row scale); each digit is the
+// exact sum of its hi and lo splits.  With q_s = x_s 2^(7(s+1)):
+// |q_s| <= 128 -- integers of at most eight significant bits, exact in bf16.
+// Stored is x_s itself (bf16), so that a product of digits s and t carries
+// its level's weight 2^(-7(s+t+2)).
+__device__ __forceinline__ float dsplit(float& r, float sigma) {
+  const float x = __fsub_rn(__fadd_rn(r, sigma), sigma);
+  r = __fsub_rn(r, x);
+  return x;
 }
-
-// digit s of a magnitude <= 2^49 as the bf16 of q_s 2^(-7s) with the sign
-__device__ __forceinline__ uint16_t digit_bf16(uint64_t u, int s, uint32_t neg) {
-  const uint32_t q = s == 0 ? (uint32_t)(u >> 42) : (uint32_t)(u >> (42 - 7 * s)) & 127u;
-  uint32_t f = __float_as_uint(__fsub_rn(__uint_as_float(0x4B000000u | q), 8388608.0f));  // float(q), exact
-  if (q) f -= (uint32_t)(7 * s) << 23;
-  return (uint16_t)((f >> 16) | (neg << 15));
+__device__ __forceinline__ float digit_sigma(int s) { return __int_as_float(((127 + 16 - 7 * s) << 23) | 0x400000); }
+// v 2^k exactly (row scaling)
+__device__ __forceinline__ float row_scale(float v, int k) {
+  return (k >= -126 && k <= 127) ? v * pow2f(k) : scale2(v, k);
+}
+// the seven digits x_s of hi + lo as floats (exact in bf16: their upper
+// 16 bits are the bf16)
+__device__ __forceinline__ void digits_f32(float hi, float lo, int eb, float d[kDig]) {
+  float rh = row_scale(hi, 126 - eb), rl = row_scale(lo, 126 - eb);
+#pragma unroll
+  for (int s = 0; s < kDig; ++s) {
+    float x = dsplit(rh, digit_sigma(s));
+    if (s >= 3) x = __fadd_rn(x, dsplit(rl, digit_sigma(s)));
+    d[s] = x;
+  }
+}
+// the bf16 of two exact digits in one 32-bit word (a in the low half)
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  return __byte_perm(__float_as_uint(a), __float_as_uint(b), 0x7632);
 }
 
 // TF32 halves of x: hi = x rounded to 10 fraction bits, lo = x - hi (the
@@ -140,7 +153,9 @@ __device__ __forceinline__ void tf32_split(float x, uint32_t& hi, uint32_t& lo) 
 
 // byte offset, in a K-major core layout of `rows` rows, of row r at the
 // 16-byte k-group kc
-__device__ __forceinline__ int core_off(int r, int kc, int rows) { return kc * (rows / 8) * 128 + (r >> 3) * 128 + (r & 7) * 16; }
+__device__ __forceinline__ int core_off(int r, int kc, int rows) {
+  return kc * (rows / 8) * 128 + (r >> 3) * 128 + (r & 7) * 16;
+}
 
 // separate level accumulators that fit tensor memory (512 columns of 2 Np each)
 __device__ __forceinline__ int levels_for(int Np) { return min(kDig, 512 / (2 * Np)); }
@@ -149,11 +164,52 @@ __device__ __forceinline__ void set_status(int* status, int code) {
   if (status) atomicCAS(status, 0, code);
 }
 
+// Write element (j, k) of H^T, value v, into an operand image: OZ
+// [ks][digit][re/im][core layout Np x 16 k] bf16 (row exponent fj), TF
+// [ks][hi_re, hi_im, lo_re, lo_im][core layout Np x 16 k] fp32.
+template <bool OZ>
+__device__ __forceinline__ void put_image(unsigned char* img, int Np, int j, int k, float4 v, int fj) {
+  const int planes = OZ ? kDig * 2 : 4;
+  const int esz = OZ ? 2 : 4;
+  const int plane_bytes = Np * kChunkK * esz;
+  const int ks = k / kChunkK, kk = k % kChunkK;
+  const int per = 16 / esz;  // elements per core row
+  const int off = core_off(j, kk / per, Np) + (kk % per) * esz;
+  unsigned char* base = img + (size_t)ks * planes * plane_bytes;
+  if (OZ) {
+    float dr[kDig], di[kDig];
+    digits_f32(v.x, v.y, fj, dr);
+    digits_f32(v.z, v.w, fj, di);
+#pragma unroll
+    for (int d = 0; d < kDig; ++d) {
+      *reinterpret_cast<uint16_t*>(base + (size_t)(2 * d + 0) * plane_bytes + off) =
+          (uint16_t)(__float_as_uint(dr[d]) >> 16);
+      *reinterpret_cast<uint16_t*>(base + (size_t)(2 * d + 1) * plane_bytes + off) =
+          (uint16_t)(__float_as_uint(di[d]) >> 16);
+    }
+  } else {
+    uint32_t hr, lr, hi_, li;
+    tf32_split(v.x, hr, lr);
+    tf32_split(v.z, hi_, li);
+    *reinterpret_cast<uint32_t*>(base + 0 * plane_bytes + off) = hr;
+    *reinterpret_cast<uint32_t*>(base + 1 * plane_bytes + off) = hi_;
+    *reinterpret_cast<uint32_t*>(base + 2 * plane_bytes + off) = lr;
+    *reinterpret_cast<uint32_t*>(base + 3 * plane_bytes + off) = li;
+  }
+}
+
+// alpha h: the operand images carry the task's coefficient, so the epilogue
+// multiplies by nothing but powers of two
+template <bool OZ>
+__device__ __forceinline__ float4 scaled_h(double2 alpha, float4 v) {
+  if (alpha.x == 1.0 && alpha.y == 0.0) return v;
+  return OZ ? DF64::mul(DF64::coef(alpha), v) : C32::mul(C32::coef(alpha), v);
+}
+
 // ---------------------------------------------------------------------------
-// pre-pass: the shared-memory image of h for every task of the stage
-//   OZ: [ks][digit t][re/im][core layout Np x 16 k] bf16, then F_j (Np ints)
-//   TF: [ks][hi_re, hi_im, lo_re, lo_im][core layout Np x 16 k] fp32
-// with H^T rows j (N, padded to Np = 16 * ceil(N / 16)) and k < Kp zero-padded.
+// pre-pass of the mode products: the operand image of alpha h for every task
+// of the stage, H^T rows j (N, padded to Np = 16 ceil(N / 16)), k < Kp
+// zero-padded, then the rows' exponents F_j (OZ)
 // ---------------------------------------------------------------------------
 template <bool OZ>
 __global__ void __launch_bounds__(256) k_mp_tc_h(const MPTask* __restrict__ tasks, const int* __restrict__ ids,
@@ -169,49 +225,49 @@ __global__ void __launch_bounds__(256) k_mp_tc_h(const MPTask* __restrict__ task
     __syncthreads();
     for (int e = threadIdx.x; e < N * K; e += blockDim.x) {
       const int j = e % N, a = e / N;
-      const float4 v = h[j + (int64_t)N * a];
+      const float4 v = scaled_h<OZ>(t.alpha, h[j + (int64_t)N * a]);
       atomicMax(&fx[j], max(fexp(v.x), fexp(v.z)));
     }
     __syncthreads();
   }
-  const int planes = OZ ? kDig * 2 : 4;
-  const int esz = OZ ? 2 : 4;
-  const int plane_bytes = Np * kChunkK * esz;
-  // one thread per (j, k) element of H^T
   for (int e = threadIdx.x; e < Np * Kp; e += blockDim.x) {
     const int j = e % Np, k = e / Np;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (j < N && k < K) v = h[j + (int64_t)N * k];
-    const int ks = k / kChunkK, kk = k % kChunkK;
-    const int per = 16 / esz;  // elements per core row
-    const int off = core_off(j, kk / per, Np) + (kk % per) * esz;
-    unsigned char* base = img + (size_t)ks * planes * plane_bytes;
-    if (OZ) {
-      uint32_t nr = 0, ni = 0;
-      const uint64_t ur = mag49(v.x, v.y, fx[j < N ? j : 0], nr);
-      const uint64_t ui = mag49(v.z, v.w, fx[j < N ? j : 0], ni);
-#pragma unroll
-      for (int d = 0; d < kDig; ++d) {
-        *reinterpret_cast<uint16_t*>(base + (size_t)(2 * d + 0) * plane_bytes + off) = digit_bf16(ur, d, nr);
-        *reinterpret_cast<uint16_t*>(base + (size_t)(2 * d + 1) * plane_bytes + off) = digit_bf16(ui, d, ni);
-      }
-    } else {
-      uint32_t hr, lr, hi_, li;
-      tf32_split(v.x, hr, lr);
-      tf32_split(v.z, hi_, li);
-      *reinterpret_cast<uint32_t*>(base + 0 * plane_bytes + off) = hr;
-      *reinterpret_cast<uint32_t*>(base + 1 * plane_bytes + off) = hi_;
-      *reinterpret_cast<uint32_t*>(base + 2 * plane_bytes + off) = lr;
-      *reinterpret_cast<uint32_t*>(base + 3 * plane_bytes + off) = li;
-    }
+    if (j < N && k < K) v = scaled_h<OZ>(t.alpha, h[j + (int64_t)N * k]);
+    put_image<OZ>(img, Np, j, k, v, OZ ? fx[j < N ? j : 0] : 0);
   }
   if (OZ)
-    for (int i = threadIdx.x; i < 64; i += blockDim.x)
-      reinterpret_cast<int*>(img + Cfg<true>::BHeader)[i] = fx[i];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) reinterpret_cast<int*>(img + Cfg<true>::BHeader)[i] = fx[i];
 }
 
 // ---------------------------------------------------------------------------
-// the mode-product kernel
+// One unit of work: 128 rows of a mode-product task.
+// ---------------------------------------------------------------------------
+struct TcUnit {
+  int K, N, Np;              // reduction length, output columns (padded)
+  const unsigned char* img;  // h operand image
+  int64_t nrows;             // rows of the task
+  const float4* in;          // the input tensor
+  int64_t before;            // stride of the reduction index
+  float4* out;
+};
+
+__device__ __forceinline__ TcUnit make_unit(const MPTask* tasks, int task) {
+  const MPTask t = tasks[task];
+  TcUnit u;
+  u.K = t.a_in;
+  u.N = t.a_out;
+  u.Np = (u.N + 15) & ~15;
+  u.img = static_cast<const unsigned char*>(t.oz_h);
+  u.nrows = (int64_t)t.before * t.after;
+  u.in = reinterpret_cast<const float4*>(t.in);
+  u.before = t.before;
+  u.out = reinterpret_cast<float4*>(t.out);
+  return u;
+}
+
+// ---------------------------------------------------------------------------
+// the tensor-core kernel
 // ---------------------------------------------------------------------------
 template <bool OZ>
 __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restrict__ tasks,
@@ -228,10 +284,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
 
   if (tid == 0) {
     for (int s = 0; s < 2; ++s) {
-      mbar_init(&sm.bar.full[s], 128);
+      mbar_init(&sm.bar.full[s], 256);
       mbar_init(&sm.bar.empty[s], 1);
       mbar_init(&sm.bar.exready[s], 128);
       mbar_init(&sm.bar.exfree[s], 128);
+      mbar_init(&sm.bar.pmax[s], 256);
     }
     mbar_init(&sm.bar.tfull, 1);
     mbar_init(&sm.bar.tempty, 128);
@@ -240,308 +297,356 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
     mbar_fence_init();
   }
   const uint32_t ncols = OZ ? 512u : 128u;
-  if (warp == 8) tmem_alloc(&sm.bar.tmem, ncols);
+  if (warp == 12) tmem_alloc(&sm.bar.tmem, ncols);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = sm.bar.tmem;
   bool ok = true;
 
-  if (warp < 4) {
-    // ---------------- producers: one row each ----------------
-    const int r = tid;
-    uint32_t q = 0;  // chunk counter over all tiles
-    for (int64_t it = my0; it < my1 && ok; ++it) {
+  if (warp < 8) {
+    // ---------------- producers: two per row, each half of every chunk ----------------
+    const int r = tid & (kRows - 1), h = tid >> 7;
+    uint32_t q = 0;   // chunk counter over all units
+    uint32_t un = 0;  // unit counter
+    for (int64_t it = my0; it < my1 && ok; ++it, ++un) {
       const int2 tl = tiles[tile0 + it];
-      const MPTask t = tasks[tl.x];
-      const float4* __restrict__ in = reinterpret_cast<const float4*>(t.in);
-      const int K = t.a_in, N = t.a_out;
-      const int64_t before = t.before, nrows = before * t.after;
-      const int64_t rg = (int64_t)tl.y * kRows + r;
-      const bool valid = rg < nrows;
-      const int64_t b = valid ? rg % before : 0, c = valid ? rg / before : 0;
-      const float4* base = in + b + before * (int64_t)K * c;
-      const int buf = (int)((it - my0) & 1);
-      // the epilogue of the tile two back has read ex / orow of this buffer
-      if (!mbar_wait(&sm.bar.exfree[buf], (uint32_t)((((it - my0) >> 1) & 1) ^ 1), kSpin)) {
-        set_status(status, 8);
-        ok = false;
-        break;
-      }
-      if (OZ) {
-        int m = 1;
-        if (valid)
-          for (int a = 0; a < K; ++a) {
-            const float4 v = __ldg(base + before * a);
-            m = max(m, max(fexp(v.x), fexp(v.z)));
-          }
-        sm.ex[buf][r] = m;
-      }
-      sm.orow[buf][r] = valid ? (int)(b + before * (int64_t)N * c) : -1;
-      mbar_arrive(&sm.bar.exready[buf]);
-      const int eb = OZ ? sm.ex[buf][r] : 0;
-      const int nks = (K + kChunkK - 1) / kChunkK;
-      for (int ks = 0; ks < nks; ++ks, ++q) {
-        const int s = q & 1;
-        if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
-          set_status(status, 1);
-          ok = false;
-          break;
-        }
-        unsigned char* A = sm.a[s];
+      {
+        const TcUnit U = make_unit(tasks, tl.x);
+        const int K = U.K;
+        const int64_t rg = (int64_t)tl.y * kRows + r;
+        const bool valid = rg < U.nrows;
+        const int64_t b = valid ? rg % U.before : 0, c = valid ? rg / U.before : 0;
+        const float4* base = U.in + b + U.before * (int64_t)K * c;
+        const int buf = (int)(un & 1);
+        const uint32_t use_par = (un >> 1) & 1;  // parity of this buffer's use
+        int eb = 0;
+        if (OZ) {
+          // the row's largest exponent: each half of the row, eight loads in flight
+          const int kh = (K + 1) >> 1, a_lo = h * kh, a_hi = min(K, a_lo + kh);
+          int m = 1;
+          if (valid)
+            for (int a0 = a_lo; a0 < a_hi; a0 += 8) {
+              float4 v[8];
 #pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          float4 x[8];
+              for (int i = 0; i < 8; ++i)
+                v[i] = a0 + i < a_hi ? __ldg(base + U.before * (a0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+              for (int i = 0; i < 8; ++i) m = max(m, max(fexp(v[i].x), fexp(v[i].z)));
+            }
+          sm.pm[buf][h][r] = (uint8_t)m;
+          mbar_arrive(&sm.bar.pmax[buf]);
+          if (!mbar_wait(&sm.bar.pmax[buf], use_par, kSpin)) {
+            set_status(status, 9);
+            ok = false;
+            break;
+          }
+          eb = max(sm.pm[buf][0][r], sm.pm[buf][1][r]);
+        }
+        if (h == 0) {
+          // the epilogue of the unit two back has read ex of this buffer
+          if (!mbar_wait(&sm.bar.exfree[buf], use_par ^ 1, kSpin)) {
+            set_status(status, 8);
+            ok = false;
+            break;
+          }
+          sm.ex[buf][r] = (uint8_t)eb;
+          mbar_arrive(&sm.bar.exready[buf]);
+        }
+        const int nks = (K + kChunkK - 1) / kChunkK;
+        // this thread's eight values of chunk ks; the next chunk's loads are in
+        // flight while the current chunk is cut into digits
+        auto load8 = [&](float4 (&x)[8], int ks) {
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const int a = ks * kChunkK + half * 8 + i;
-            x[i] = (valid && a < K) ? __ldg(base + before * a) : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int a = ks * kChunkK + h * 8 + i;
+            x[i] = (valid && a < K) ? __ldg(base + U.before * a) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
-          if (OZ) {
-            uint64_t ur[8], ui[8];
-            uint32_t nr[8], ni[8];
+        };
+        float4 nx[8];
+        load8(nx, 0);
+        for (int ks = 0; ks < nks; ++ks, ++q) {
+          const int s = q & 1;
+          float4 x[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              ur[i] = mag49(x[i].x, x[i].y, eb, nr[i]);
-              ui[i] = mag49(x[i].z, x[i].w, eb, ni[i]);
+          for (int i = 0; i < 8; ++i) x[i] = nx[i];
+          if (ks + 1 < nks) load8(nx, ks + 1);
+          if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
+            set_status(status, 1);
+            ok = false;
+            break;
+          }
+          unsigned char* A = sm.a[s];
+          if (OZ) {
+            uint32_t wr[kDig][4], wi[kDig][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
+              digits_f32(x[2 * i].x, x[2 * i].y, eb, d0);
+              digits_f32(x[2 * i + 1].x, x[2 * i + 1].y, eb, d1);
+              digits_f32(x[2 * i].z, x[2 * i].w, eb, e0);
+              digits_f32(x[2 * i + 1].z, x[2 * i + 1].w, eb, e1);
+#pragma unroll
+              for (int d = 0; d < kDig; ++d) {
+                wr[d][i] = pack_bf16(d0[d], d1[d]);
+                wi[d][i] = pack_bf16(e0[d], e1[d]);
+              }
             }
-            const int off = core_off(r, half, kRows);
+            const int off = core_off(r, h, kRows);
 #pragma unroll
             for (int d = 0; d < kDig; ++d) {
-              uint32_t wr[4], wi[4];
-#pragma unroll
-              for (int i = 0; i < 4; ++i) {
-                wr[i] = (uint32_t)digit_bf16(ur[2 * i], d, nr[2 * i]) |
-                        ((uint32_t)digit_bf16(ur[2 * i + 1], d, nr[2 * i + 1]) << 16);
-                wi[i] = (uint32_t)digit_bf16(ui[2 * i], d, ni[2 * i]) |
-                        ((uint32_t)digit_bf16(ui[2 * i + 1], d, ni[2 * i + 1]) << 16);
-              }
-              *reinterpret_cast<uint4*>(A + (2 * d + 0) * kOzAPlane + off) = make_uint4(wr[0], wr[1], wr[2], wr[3]);
-              *reinterpret_cast<uint4*>(A + (2 * d + 1) * kOzAPlane + off) = make_uint4(wi[0], wi[1], wi[2], wi[3]);
+              *reinterpret_cast<uint4*>(A + (2 * d + 0) * kOzAPlane + off) =
+                  make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
+              *reinterpret_cast<uint4*>(A + (2 * d + 1) * kOzAPlane + off) =
+                  make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
             }
           } else {
             // fp32 values (complex64 storage keeps them in the hi words)
 #pragma unroll
-            for (int g = 0; g < 2; ++g) {  // two 16-byte core rows of 4 k each
+            for (int g2 = 0; g2 < 2; ++g2) {  // two 16-byte core rows of 4 k each
               uint32_t hr[4], hi_[4], lr[4], li[4];
 #pragma unroll
               for (int i = 0; i < 4; ++i) {
-                tf32_split(x[4 * g + i].x, hr[i], lr[i]);
-                tf32_split(x[4 * g + i].z, hi_[i], li[i]);
+                tf32_split(x[4 * g2 + i].x, hr[i], lr[i]);
+                tf32_split(x[4 * g2 + i].z, hi_[i], li[i]);
               }
-              const int off = core_off(r, 2 * half + g, kRows);
+              const int off = core_off(r, 2 * h + g2, kRows);
               *reinterpret_cast<uint4*>(A + 0 * kTfAPlane + off) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
               *reinterpret_cast<uint4*>(A + 1 * kTfAPlane + off) = make_uint4(hi_[0], hi_[1], hi_[2], hi_[3]);
               *reinterpret_cast<uint4*>(A + 2 * kTfAPlane + off) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
               *reinterpret_cast<uint4*>(A + 3 * kTfAPlane + off) = make_uint4(li[0], li[1], li[2], li[3]);
             }
           }
+          fence_proxy_async();
+          mbar_arrive(&sm.bar.full[s]);
         }
-        fence_proxy_async();
-        mbar_arrive(&sm.bar.full[s]);
       }
     }
-  } else if (warp == 8) {
+  } else if (warp == 12) {
     // ---------------- MMA issue (one thread) and h loads ----------------
     if (lane == 0) {
-      uint32_t q = 0, nb = 0;
-      int cur = -1;
-      for (int64_t it = my0; it < my1 && ok; ++it) {
+      uint32_t q = 0, nb = 0, un = 0;
+      const void* cur = nullptr;
+      for (int64_t it = my0; it < my1 && ok; ++it, ++un) {
         const int2 tl = tiles[tile0 + it];
-        const MPTask t = tasks[tl.x];
-        const int K = t.a_in, N = t.a_out;
-        const int Np = (N + 15) & ~15, nks = (K + kChunkK - 1) / kChunkK;
-        const int esz = OZ ? 2 : 4;
-        const int planes = OZ ? kDig * 2 : 4;
-        const int plane_b = Np * kChunkK * esz;  // bytes of one h plane per chunk
-        const uint32_t tpar = (uint32_t)((it - my0) & 1);
-        if (tl.x != cur) {
-          // the previous tile's MMAs read the old h: wait until they completed
-          if (it > my0 && !mbar_wait(&sm.bar.tfull, tpar ^ 1, kSpin)) {
-            set_status(status, 2);
-            ok = false;
-            break;
+        {
+          const TcUnit U = make_unit(tasks, tl.x);
+          const int K = U.K, Np = U.Np, nks = (K + kChunkK - 1) / kChunkK;
+          const int esz = OZ ? 2 : 4;
+          const int planes = OZ ? kDig * 2 : 4;
+          const int plane_b = Np * kChunkK * esz;  // bytes of one h plane per chunk
+          const uint32_t tpar = un & 1;
+          if (U.img != cur) {
+            // the previous unit's MMAs read the old h: wait until they completed
+            if (un > 0 && !mbar_wait(&sm.bar.tfull, tpar ^ 1, kSpin)) {
+              set_status(status, 2);
+              ok = false;
+              break;
+            }
+            const uint32_t bytes = (uint32_t)(nks * planes * plane_b);
+            mbar_arrive_expect_tx(&sm.bar.bfull, bytes);
+            for (uint32_t o = 0; o < bytes; o += 32768u) {
+              const uint32_t n = bytes - o < 32768u ? bytes - o : 32768u;
+              bulk_g2s(sm.b + o, U.img + o, n, &sm.bar.bfull);
+            }
+            if (!mbar_wait(&sm.bar.bfull, nb & 1, kSpin)) {
+              set_status(status, 3);
+              ok = false;
+              break;
+            }
+            ++nb;
+            cur = U.img;
           }
-          const uint32_t bytes = (uint32_t)(nks * planes * plane_b);
-          mbar_arrive_expect_tx(&sm.bar.bfull, bytes);
-          const unsigned char* src = static_cast<const unsigned char*>(t.oz_h);
-          for (uint32_t o = 0; o < bytes; o += 32768u) {
-            const uint32_t n = bytes - o < 32768u ? bytes - o : 32768u;
-            bulk_g2s(sm.b + o, src + o, n, &sm.bar.bfull);
-          }
-          if (!mbar_wait(&sm.bar.bfull, nb & 1, kSpin)) {
-            set_status(status, 3);
-            ok = false;
-            break;
-          }
-          ++nb;
-          cur = tl.x;
-        }
-        // the epilogue released the accumulators of the previous tile
-        if (!mbar_wait(&sm.bar.tempty, tpar ^ 1, kSpin)) {
-          set_status(status, 4);
-          ok = false;
-          break;
-        }
-        fence_after_sync();
-        const uint32_t lboA = (kRows / 8) * 128, lboB = (uint32_t)(Np / 8) * 128;
-        uint32_t used = 0;  // accumulators written in this tile
-        for (int ks = 0; ks < nks; ++ks, ++q) {
-          const int s = q & 1;
-          if (!mbar_wait(&sm.bar.full[s], (q >> 1) & 1, kSpin)) {
-            set_status(status, 5);
+          // the epilogue released the accumulators of the previous unit
+          if (!mbar_wait(&sm.bar.tempty, tpar ^ 1, kSpin)) {
+            set_status(status, 4);
             ok = false;
             break;
           }
           fence_after_sync();
-          const uint32_t a0 = smem_u32(sm.a[s]);
-          const uint32_t b0 = smem_u32(sm.b) + (uint32_t)(ks * planes * plane_b);
-          if (OZ) {
-            const int NL = levels_for(Np);
-            const uint32_t id = idesc_m128(1, Np, false), idn = idesc_m128(1, Np, true);
+          const uint32_t lboA = (kRows / 8) * 128, lboB = (uint32_t)(Np / 8) * 128;
+          uint32_t used = 0;  // TF: 0 until the unit's first MMAs
+          for (int ks = 0; ks < nks; ++ks, ++q) {
+            const int s = q & 1;
+            if (!mbar_wait(&sm.bar.full[s], (q >> 1) & 1, kSpin)) {
+              set_status(status, 5);
+              ok = false;
+              break;
+            }
+            fence_after_sync();
+            const uint32_t a0 = smem_u32(sm.a[s]);
+            const uint32_t b0 = smem_u32(sm.b) + (uint32_t)(ks * planes * plane_b);
+            if (OZ) {
+              // descriptors of the first planes; the others differ only in
+              // the start address field (address / 16)
+              const int NL = levels_for(Np);
+              const uint32_t id = idesc_m128(1, Np, false), idn = idesc_m128(1, Np, true);
+              const uint64_t dA = desc_kmajor(a0, lboA, 128), dB = desc_kmajor(b0, lboB, 128);
+              const uint64_t pA = kOzAPlane >> 4, pB = (uint64_t)(plane_b >> 4);
+              const uint32_t first = ks == 0 ? 1u : 0u;  // the unit's first chunk initialises the levels
+#pragma unroll
+              for (int sd = 0; sd < kDig; ++sd) {
+                const uint64_t are = dA + (uint64_t)(2 * sd) * pA, aim = are + pA;
+#pragma unroll
+                for (int td = 0; td + sd < kDig; ++td) {
+                  const int L = sd + td < NL - 1 ? sd + td : NL - 1;
+                  const uint64_t bre = dB + (uint64_t)(2 * td) * pB, bim = bre + pB;
+                  const uint32_t dre = tmem + (uint32_t)(L * 2 * Np), dim_ = dre + (uint32_t)Np;
+                  // the first write of level L in the unit: pair (0, L), or (0, NL - 1) for the last level
+                  const uint32_t acc = (first && sd == 0 && td == L) ? 0u : 1u;
+                  mma_bf16(dre, are, bre, id, acc);
+                  mma_bf16(dim_, are, bim, id, acc);
+                  mma_bf16(dre, aim, bim, idn, 1);
+                  mma_bf16(dim_, aim, bre, id, 1);
+                }
+              }
+            } else {
+              const uint32_t id = idesc_m128(2, Np, false), idn = idesc_m128(2, Np, true);
+              const uint32_t lboA4 = (kRows / 8) * 128;  // kc stride of a 16-k fp32 plane: [kc (4)][g][8][4]
 #pragma unroll 1
-            for (int sd = 0; sd < kDig; ++sd) {
-              const uint64_t are = desc_kmajor(a0 + (2 * sd + 0) * kOzAPlane, lboA, 128);
-              const uint64_t aim = desc_kmajor(a0 + (2 * sd + 1) * kOzAPlane, lboA, 128);
-              for (int td = 0; td + sd < kDig; ++td) {
-                const int L = sd + td < NL - 1 ? sd + td : NL - 1;
-                const uint64_t bre = desc_kmajor(b0 + (2 * td + 0) * plane_b, lboB, 128);
-                const uint64_t bim = desc_kmajor(b0 + (2 * td + 1) * plane_b, lboB, 128);
-                const uint32_t dre = tmem + (uint32_t)(L * 2 * Np), dim_ = dre + (uint32_t)Np;
-                const uint32_t fre = (used >> (2 * L)) & 1, fim = (used >> (2 * L + 1)) & 1;
-                mma_bf16(dre, are, bre, id, fre);
-                mma_bf16(dre, aim, bim, idn, 1);
-                mma_bf16(dim_, are, bim, id, fim);
-                mma_bf16(dim_, aim, bre, id, 1);
-                used |= 3u << (2 * L);
+              for (int h8 = 0; h8 < 2; ++h8) {  // two MMAs of k = 8 per chunk
+                const uint32_t ao = (uint32_t)(2 * h8) * lboA4, bo = (uint32_t)(2 * h8) * lboB;
+                const uint64_t ahr = desc_kmajor(a0 + 0 * kTfAPlane + ao, lboA4, 128);
+                const uint64_t ahi = desc_kmajor(a0 + 1 * kTfAPlane + ao, lboA4, 128);
+                const uint64_t alr = desc_kmajor(a0 + 2 * kTfAPlane + ao, lboA4, 128);
+                const uint64_t ali = desc_kmajor(a0 + 3 * kTfAPlane + ao, lboA4, 128);
+                const uint64_t bhr = desc_kmajor(b0 + 0 * plane_b + bo, lboB, 128);
+                const uint64_t bhi = desc_kmajor(b0 + 1 * plane_b + bo, lboB, 128);
+                const uint64_t blr = desc_kmajor(b0 + 2 * plane_b + bo, lboB, 128);
+                const uint64_t bli = desc_kmajor(b0 + 3 * plane_b + bo, lboB, 128);
+                const uint32_t dre = tmem, dim_ = tmem + (uint32_t)Np;
+                const uint32_t f = used;  // 0 only for the first MMAs of the unit
+                // lo x hi and hi x lo first, then hi x hi
+                mma_tf32(dre, alr, bhr, id, f);
+                mma_tf32(dim_, alr, bhi, id, f);
+                mma_tf32(dre, ali, bhi, idn, 1);
+                mma_tf32(dim_, ali, bhr, id, 1);
+                mma_tf32(dre, ahr, blr, id, 1);
+                mma_tf32(dim_, ahr, bli, id, 1);
+                mma_tf32(dre, ahi, bli, idn, 1);
+                mma_tf32(dim_, ahi, blr, id, 1);
+                mma_tf32(dre, ahr, bhr, id, 1);
+                mma_tf32(dim_, ahr, bhi, id, 1);
+                mma_tf32(dre, ahi, bhi, idn, 1);
+                mma_tf32(dim_, ahi, bhr, id, 1);
+                used = 1;
               }
             }
-          } else {
-            const uint32_t id = idesc_m128(2, Np, false), idn = idesc_m128(2, Np, true);
-            const uint32_t lboA4 = (kRows / 8) * 128;  // kc stride of a 16-k fp32 plane: [kc (4)][g][8][4]
-#pragma unroll 1
-            for (int h8 = 0; h8 < 2; ++h8) {  // two MMAs of k = 8 per chunk
-              const uint32_t ao = (uint32_t)(2 * h8) * lboA4, bo = (uint32_t)(2 * h8) * lboB;
-              const uint64_t ahr = desc_kmajor(a0 + 0 * kTfAPlane + ao, lboA4, 128);
-              const uint64_t ahi = desc_kmajor(a0 + 1 * kTfAPlane + ao, lboA4, 128);
-              const uint64_t alr = desc_kmajor(a0 + 2 * kTfAPlane + ao, lboA4, 128);
-              const uint64_t ali = desc_kmajor(a0 + 3 * kTfAPlane + ao, lboA4, 128);
-              const uint64_t bhr = desc_kmajor(b0 + 0 * plane_b + bo, lboB, 128);
-              const uint64_t bhi = desc_kmajor(b0 + 1 * plane_b + bo, lboB, 128);
-              const uint64_t blr = desc_kmajor(b0 + 2 * plane_b + bo, lboB, 128);
-              const uint64_t bli = desc_kmajor(b0 + 3 * plane_b + bo, lboB, 128);
-              const uint32_t dre = tmem, dim_ = tmem + (uint32_t)Np;
-              const uint32_t f = used;  // 0 only for the first MMAs of the tile
-              // lo x hi and hi x lo first, then hi x hi
-              mma_tf32(dre, alr, bhr, id, f);
-              mma_tf32(dre, ali, bhi, idn, 1);
-              mma_tf32(dim_, alr, bhi, id, f);
-              mma_tf32(dim_, ali, bhr, id, 1);
-              mma_tf32(dre, ahr, blr, id, 1);
-              mma_tf32(dre, ahi, bli, idn, 1);
-              mma_tf32(dim_, ahr, bli, id, 1);
-              mma_tf32(dim_, ahi, blr, id, 1);
-              mma_tf32(dre, ahr, bhr, id, 1);
-              mma_tf32(dre, ahi, bhi, idn, 1);
-              mma_tf32(dim_, ahr, bhi, id, 1);
-              mma_tf32(dim_, ahi, bhr, id, 1);
-              used = 1;
-            }
+            commit(&sm.bar.empty[s]);  // the stage is free once these MMAs completed
           }
-          commit(&sm.bar.empty[s]);  // the stage is free once these MMAs completed
+          if (!ok) break;
+          commit(&sm.bar.tfull);
         }
-        if (!ok) break;
-        commit(&sm.bar.tfull);
       }
       // drain: every MMA issued by this thread completed before tensor memory is freed
       commit(&sm.bar.drain);
       if (!mbar_wait(&sm.bar.drain, 0, kSpin)) set_status(status, 6);
     }
   } else {
-    // ---------------- epilogue: warp 4 + qd reads lanes 32 qd .. ----------------
-    const int qd = warp - 4;
+    // ---------------- epilogue: warp 8 + qd reads lanes 32 qd .. ----------------
+    const int qd = warp - 8;
     const int r = 32 * qd + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * qd) << 16);
-    for (int64_t it = my0; it < my1 && ok; ++it) {
+    uint32_t un = 0;
+    for (int64_t it = my0; it < my1 && ok; ++it, ++un) {
       const int2 tl = tiles[tile0 + it];
-      const MPTask t = tasks[tl.x];
-      const int N = t.a_out, Np = (N + 15) & ~15;
-      const int64_t before = t.before;
-      const int buf = (int)((it - my0) & 1);
-      const uint32_t tpar = (uint32_t)((it - my0) & 1);
-      if (!mbar_wait(&sm.bar.exready[buf], (uint32_t)(((it - my0) >> 1) & 1), kSpin) ||
-          !mbar_wait(&sm.bar.tfull, tpar, kSpin)) {
-        set_status(status, 7);
-        ok = false;
-        break;
-      }
-      fence_after_sync();
-      const int ro = sm.orow[buf][r];
-      const int er = OZ ? sm.ex[buf][r] : 0;
-      mbar_arrive(&sm.bar.exfree[buf]);
-      const bool live = ro >= 0;
-      const int* fxg = OZ ? reinterpret_cast<const int*>(static_cast<const unsigned char*>(t.oz_h) + Cfg<true>::BHeader)
-                          : nullptr;
-      float4* out = reinterpret_cast<float4*>(t.out);
-      const bool unit = t.alpha.x == 1.0 && t.alpha.y == 0.0;
-      for (int j0 = 0; j0 < Np; j0 += 8) {
-        __syncwarp();  // the tensor-memory loads below are warp-collective
-        float vre[8], vim[8], lre[8], lim[8];
-        if (OZ) {
-          const int NL = levels_for(Np);
-          tmem_ld8(lane_addr + (uint32_t)j0, vre);
-          tmem_ld8(lane_addr + (uint32_t)(Np + j0), vim);
-          tmem_wait_ld();
-#pragma unroll
-          for (int i = 0; i < 8; ++i) lre[i] = lim[i] = 0.f;
-          for (int L = 1; L < NL; ++L) {  // warp-uniform
-            float ar[8], ai[8];
-            tmem_ld8(lane_addr + (uint32_t)(L * 2 * Np + j0), ar);
-            tmem_ld8(lane_addr + (uint32_t)(L * 2 * Np + Np + j0), ai);
-            tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-              df_add(vre[i], lre[i], ar[i], 0.f);
-              df_add(vim[i], lim[i], ai[i], 0.f);
-            }
-          }
-        } else {
-          tmem_ld8(lane_addr + (uint32_t)j0, vre);
-          tmem_ld8(lane_addr + (uint32_t)(Np + j0), vim);
-          tmem_wait_ld();
-#pragma unroll
-          for (int i = 0; i < 8; ++i) lre[i] = lim[i] = 0.f;
+      {
+        const TcUnit U = make_unit(tasks, tl.x);
+        const int N = U.N, Np = U.Np;
+        const int buf = (int)(un & 1);
+        const uint32_t tpar = un & 1;
+        if (!mbar_wait(&sm.bar.exready[buf], (un >> 1) & 1, kSpin) || !mbar_wait(&sm.bar.tfull, tpar, kSpin)) {
+          set_status(status, 7);
+          ok = false;
+          break;
         }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int j = j0 + i;
-          if (!live || j >= N) continue;
-          float4 v;
+        fence_after_sync();
+        const int er = OZ ? (int)sm.ex[buf][r] : 0;
+        mbar_arrive(&sm.bar.exfree[buf]);
+        const int64_t rg = (int64_t)tl.y * kRows + r;
+        const bool live = rg < U.nrows;
+        const int64_t ro = live ? rg % U.before + U.before * (int64_t)N * (rg / U.before) : 0;
+        int* fxw = sm.fx[qd];
+        if (OZ) {
+          // the unit's column exponents of h into this warp's copy
+          const int* fxg = reinterpret_cast<const int*>(U.img + Cfg<true>::BHeader);
+          __syncwarp();
+          for (int j = lane; j < 64; j += 32) fxw[j] = __ldg(fxg + j);
+          __syncwarp();
+        }
+        for (int j0 = 0; j0 < Np; j0 += 8) {
+          __syncwarp();  // the tensor-memory loads below are warp-collective
+          float vre[8], vim[8], lre[8], lim[8];
           if (OZ) {
-            const int fj = __ldg(fxg + j);
-            const int sh = (er - 126) + (fj - 126) - 14;
-            v = make_float4(scale2(vre[i], sh), scale2(lre[i], sh), scale2(vim[i], sh), scale2(lim[i], sh));
-            df_norm(v.x, v.y);
-            df_norm(v.z, v.w);
-            if (!unit) v = DF64::mul(DF64::coef(t.alpha), v);
-            if (er == 255 || fj == 255) {  // an Inf or NaN in the row: propagate it
-              const float nan = __int_as_float(0x7fffffff);
-              v = make_float4(nan, nan, nan, nan);
+            // all levels of eight columns: one wait for the real parts, one for the imaginary
+            const int NL = levels_for(Np);
+            float a[kDig][8];
+#pragma unroll
+            for (int part = 0; part < 2; ++part) {
+#pragma unroll
+              for (int L = 0; L < kDig; ++L)
+                if (L < NL) tmem_ld8(lane_addr + (uint32_t)(L * 2 * Np + part * Np + j0), a[L]);
+              tmem_wait_ld();
+              float* v = part ? vim : vre;
+              float* l = part ? lim : lre;
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                // levels 0..2 in double-float; levels 3.. lie below 2^-21 of
+                // level 0's scale, their fp32 sum in the low word errs by
+                // less than 2^-45 of it
+                v[i] = a[0][i];
+                l[i] = 0.f;
+                if (NL > 1) df_add(v[i], l[i], a[1][i], 0.f);
+                if (NL > 2) df_add(v[i], l[i], a[2][i], 0.f);
+                float t3 = 0.f;
+#pragma unroll
+                for (int L = 3; L < kDig; ++L)
+                  if (L < NL) t3 = __fadd_rn(t3, a[L][i]);
+                l[i] = __fadd_rn(l[i], t3);
+              }
             }
           } else {
-            v = make_float4(vre[i], 0.f, vim[i], 0.f);
-            if (!unit) v = C32::mul(C32::coef(t.alpha), v);
+            tmem_ld8(lane_addr + (uint32_t)j0, vre);
+            tmem_ld8(lane_addr + (uint32_t)(Np + j0), vim);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 8; ++i) lre[i] = lim[i] = 0.f;
           }
-          out[ro + before * j] = v;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int j = j0 + i;
+            if (!live || j >= N) continue;
+            float4 v;
+            float4* o = U.out + ro + U.before * j;
+            if (OZ) {
+              const int fj = fxw[j];
+              const int sh = (er - 126) + (fj - 126);
+              if (sh >= -126 && sh <= 127) {
+                const float f = pow2f(sh);
+                v = make_float4(vre[i] * f, lre[i] * f, vim[i] * f, lim[i] * f);
+              } else {
+                v = make_float4(scale2(vre[i], sh), scale2(lre[i], sh), scale2(vim[i], sh), scale2(lim[i], sh));
+              }
+              df_norm(v.x, v.y);
+              df_norm(v.z, v.w);
+              if (er == 255 || fj == 255) {  // an Inf or NaN in the row: propagate it
+                const float nan = __int_as_float(0x7fffffff);
+                v = make_float4(nan, nan, nan, nan);
+              }
+            } else {
+              v = make_float4(vre[i], 0.f, vim[i], 0.f);
+            }
+            *o = v;
+          }
         }
+        fence_before_sync();
+        mbar_arrive(&sm.bar.tempty);
       }
-      fence_before_sync();
-      mbar_arrive(&sm.bar.tempty);
     }
   }
   fence_before_sync();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == 12) {
     fence_after_sync();
     tmem_dealloc(tmem, ncols);
   }
@@ -549,11 +654,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
 
 int g_tc_sms = 0;
 
-}  // namespace
-
-cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
-                         const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s) {
-  if (n_tiles <= 0) return cudaSuccess;
+cudaError_t tc_grid(int64_t n_tiles, unsigned* grid) {
   if (!g_tc_sms) {
     int dev = 0, sms = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -561,21 +662,34 @@ cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_
     if (e != cudaSuccess) return e;
     g_tc_sms = sms;
   }
-  const unsigned grid = (unsigned)(n_tiles < g_tc_sms ? n_tiles : g_tc_sms);
+  *grid = (unsigned)(n_tiles < g_tc_sms ? n_tiles : g_tc_sms);
+  return cudaSuccess;
+}
+
+template <bool OZ>
+cudaError_t launch_tc(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles, int* status,
+                      cudaStream_t s) {
+  unsigned grid = 0;
+  cudaError_t e = tc_grid(n_tiles, &grid);
+  if (e != cudaSuccess) return e;
+  const int sm = (int)sizeof(TcSmem<OZ>);
+  e = cudaFuncSetAttribute(k_mp_tc<OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e != cudaSuccess) return e;
+  k_mp_tc<OZ><<<grid, kThreadsTc, sm, s>>>(tasks, tiles, first_tile, n_tiles, status);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
+                         const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s) {
+  if (n_tiles <= 0) return cudaSuccess;
   if (oz) {
     if (n_tasks > 0) k_mp_tc_h<true><<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
-    const int sm = (int)sizeof(TcSmem<true>);
-    cudaError_t e = cudaFuncSetAttribute(k_mp_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e != cudaSuccess) return e;
-    k_mp_tc<true><<<grid, kThreadsTc, sm, s>>>(tasks, tiles, first_tile, n_tiles, status);
-  } else {
-    if (n_tasks > 0) k_mp_tc_h<false><<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
-    const int sm = (int)sizeof(TcSmem<false>);
-    cudaError_t e = cudaFuncSetAttribute(k_mp_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-    if (e != cudaSuccess) return e;
-    k_mp_tc<false><<<grid, kThreadsTc, sm, s>>>(tasks, tiles, first_tile, n_tiles, status);
+    return launch_tc<true>(tasks, tiles, first_tile, n_tiles, status, s);
   }
-  return cudaGetLastError();
+  if (n_tasks > 0) k_mp_tc_h<false><<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
+  return launch_tc<false>(tasks, tiles, first_tile, n_tiles, status, s);
 }
 
 }  // namespace qt

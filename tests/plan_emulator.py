@@ -395,34 +395,37 @@ class PlanView:
 OZ_DIGITS = 7
 
 
-def _oz_mag49(hi, lo, eb):
-    """Vectorised digit magnitudes of hi + lo (float32 arrays) against the
-    rows' largest biased exponents eb (broadcast): (negative, round(|v|
-    2^(49 - E))), from the floats' bits with four guard bits, as qt_umma.cu."""
-    bh = hi.view(np.uint32).astype(np.int64)
-    bl = lo.view(np.uint32).astype(np.int64)
-    eh, el = (bh >> 23) & 0xFF, (bl >> 23) & 0xFF
-    mh = (bh & 0x7FFFFF) | np.where(eh > 0, 0x800000, 0)
-    ml = (bl & 0x7FFFFF) | np.where(el > 0, 0x800000, 0)
-    sh = np.maximum(eh, 1) - eb + 29
-    sl = np.maximum(el, 1) - eb + 29
+def _oz_split(r, sigma):
+    """Error-free split: (x, r - x) with x = fl(fl(r + sigma) - sigma), r
+    rounded to the nearest multiple of ulp(sigma) (float32, as the device)."""
+    x = ((r + sigma).astype(np.float32) - sigma).astype(np.float32)
+    return x, (r - x).astype(np.float32)
 
-    def shift(m, k):
-        up = np.left_shift(m, np.clip(k, 0, 40))
-        down = np.where(k > -24, np.right_shift(m, np.clip(-k, 0, 40)), 0)
-        return np.where(k >= 0, up, down)
-    uh, ul = shift(mh, sh), shift(ml, sl)
-    same = ((bh ^ bl) >> 31) == 0
-    bigger = uh >= ul
-    u2 = np.where(same, uh + ul, np.abs(uh - ul))
-    neg = np.where(same | bigger, bh >> 31, bl >> 31)
-    return neg, (u2 + 8) >> 4
+
+def _oz_sigma_digits(hi, lo, eb):
+    """Digits of the double-float values hi + lo (float32 arrays) of rows
+    whose largest biased exponent of hi parts is eb (broadcast): the row is
+    scaled by 2^(126 - eb) and cut by the splits of sigma_s = 1.5 * 2^(16 - 7s),
+    the low part joining from s = 3, as qt_umma.cu.  Returns the integers q_s
+    (float64 arrays, digit first) with hi + lo ~ 2^E sum_s q_s 2^(-7(s+1))."""
+    sc = np.exp2((126 - eb).astype(np.float64)).astype(np.float32)
+    rh = (hi * sc).astype(np.float32)
+    rl = (lo * sc).astype(np.float32)
+    out = []
+    for s in range(OZ_DIGITS):
+        sigma = np.float32(1.5 * 2.0 ** (16 - 7 * s))
+        x, rh = _oz_split(rh, sigma)
+        if s >= 3:
+            xl, rl = _oz_split(rl, sigma)
+            x = (x + xl).astype(np.float32)
+        out.append(x.astype(np.float64) * 2.0 ** (7 * (s + 1)))
+    return out
 
 
 def _oz_digits(v):
     """Digits of the rows of a complex matrix v (rows x k): the value split
-    into double-float parts, seven signed 7-bit digits per real part against
-    the row's largest exponent.  Returns (E per row, re digits, im digits),
+    into double-float parts, seven signed digits per real part against the
+    row's largest exponent.  Returns (E per row, re digits, im digits),
     digits as float64 arrays (digit, row, k)."""
     parts = []
     for comp in (v.real, v.imag):
@@ -433,19 +436,17 @@ def _oz_digits(v):
     eb = np.maximum(ex.max(axis=1, initial=0), 1).astype(np.int64)[:, None]
     out = []
     for hi, lo in parts:
-        neg, u = _oz_mag49(hi, lo, eb)
-        sgn = np.where(neg == 1, -1.0, 1.0)
-        dig = [u >> 42] + [(u >> (42 - 7 * s)) & 127 for s in range(1, OZ_DIGITS)]
-        out.append(np.stack([sgn * d for d in dig]).astype(np.float64))
+        out.append(np.stack(_oz_sigma_digits(hi, lo, eb)))
     return (eb[:, 0] - 126).astype(np.float64), out[0], out[1]
 
 
 def oz_mode_product(h, x):
     """out[b, j, c] = sum_a h(j, a) x[b, a, c] with the digit arithmetic of
-    the tensor-core mode products: the level sums L = 0, 1, 2 are exact
-    (float64 holds them exactly), the levels 3..6 share one sum rounded to
-    float32 as the device's fourth accumulator is, and everything is scaled
-    by 2^(E_r + F_j)."""
+    the tensor-core mode products with the fewest level accumulators (64
+    output columns): the level sums L = 0, 1, 2 are exact (float64 holds them
+    exactly), the levels 3..6 share one sum rounded to float32 as the
+    device's fourth accumulator is, and everything is scaled by
+    2^(E_r + F_j)."""
     bef, ain, aft = x.shape
     X = np.moveaxis(x, 1, -1).reshape(-1, ain)  # one row per (b, c)
     Ex, xr, xi = _oz_digits(X)

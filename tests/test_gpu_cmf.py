@@ -30,8 +30,11 @@ def test_split_graphs_equal_the_sweep(flavour):
         h.layer_derivatives()
         if flavour & 0xFF == qtgpu.QT_PLAN_COMPRESSED:
             err, noise = deriv_errors(tree, h.dpsi(), d_full, rho)
-            tol = 1e-11 if flavour & (qtgpu.QT_PREC_DF64 | qtgpu.QT_PREC_DF64_TC) else 1e-12
-            assert err <= tol and noise <= 1e-11
+            tol = 1e-11 if flavour & qtgpu.QT_PREC_DF64 else 1e-12
+            noise_tol = 1e-11
+            if flavour & qtgpu.QT_PREC_DF64_TC:  # digit arithmetic: stated tolerance 1e-10
+                tol = noise_tol = 1e-10
+            assert err <= tol and noise <= noise_tol
         else:
             assert np.array_equal(h.dpsi(), d_full)
     finally:

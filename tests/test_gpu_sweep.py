@@ -30,11 +30,22 @@ RAW = 1e-13
 TOL_DF = 1e-11
 RAW_DF = 3e-12
 NOISE = 1e-11  # |dPsi rho| on nodes where (1-P) = 0 (rounding noise of a cancellation)
+# double-float with the mode products and accumulations on the tensor cores:
+# the digit arithmetic's error is relative to the row maxima of its operands
+# (2^-49 of the row scale per value, plus the fp32 rounding of the last level
+# accumulator when bonds exceed 32), so where the projector cancels large
+# terms the derivative carries up to ~1e-10 of its scale
+TOL_TC = 1e-10
+RAW_TC = 3e-11
+NOISE_TC = 1e-10
 
 
 def _compare(tree, sop, psi, flavour, phase=1.0, eps=1e-10):
     df = bool(flavour & (qtgpu.QT_PREC_DF64 | qtgpu.QT_PREC_DF64_TC))
     TOL, RAW = (TOL_DF, RAW_DF) if df else (globals()["TOL"], globals()["RAW"])
+    NOISE = globals()["NOISE"]
+    if flavour & qtgpu.QT_PREC_DF64_TC:
+        TOL, RAW, NOISE = TOL_TC, RAW_TC, NOISE_TC
     flat = psi.flat()
     r = O.derivative(tree, sop, flat, eps=eps, phase=phase)
     hrep = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour, eps=eps)
@@ -77,8 +88,8 @@ def test_sweep_cfg0(flavour):
     _compare(tree, sop, psi, flavour)
 
 
-# mode products with k <= 64 on the tensor cores (seven 7-bit digits per
-# operand, exact digit products and sums): the double-float tolerances hold
+# mode products and accumulations with k <= 64 on the tensor cores (seven
+# digits per operand, exact digit products and level sums): TOL_TC
 TC_FLAVOURS = [qtgpu.QT_PLAN_REFERENCE | qtgpu.QT_PREC_DF64_TC, qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64_TC,
                qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC]
 
@@ -204,6 +215,9 @@ def test_forest_of_uneven_trees(flavour):
     # one graph; every tree's slice and energy equal its own oracle sweep
     df = bool(flavour & (qtgpu.QT_PREC_DF64 | qtgpu.QT_PREC_DF64_TC))
     tol = TOL_DF if df else TOL
+    noise_tol = NOISE
+    if flavour & qtgpu.QT_PREC_DF64_TC:
+        tol, noise_tol = TOL_TC, NOISE_TC
     trees, sops, psis = batched_problem(24)
     f, node_off, mode_off = forest(trees)
     hrep = qtgpu.HamiltonianRepresentation(forest_sop(sops, mode_off), f, flavour=flavour)
@@ -217,7 +231,7 @@ def test_forest_of_uneven_trees(flavour):
             assert abs(energies[k] - r.energy) <= tol * max(1.0, abs(r.energy))
             seg = d[off[node_off[k]]:off[node_off[k] + t.n_nodes]]
             err, noise = deriv_errors(t, seg, r.dpsi, r.rho)
-            assert err <= tol and noise <= NOISE
+            assert err <= tol and noise <= noise_tol
     finally:
         hrep.close()
 

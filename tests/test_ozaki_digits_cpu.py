@@ -1,16 +1,17 @@
 """The digit arithmetic of the tensor-core mode products (QT_PREC_DF64_TC),
-restated in exact integer arithmetic and checked against exact rational
-products: every double-float value (hi + lo float pair) becomes an integer
-m = round(v 2^(49 - E)) against the largest exponent E of its row, cut into
-seven 7-bit digits; the digit products of one level L = s + t sum exactly in
-fp32 (magnitude below 2^24); the levels L <= 6 combined give the product
-within 2^-44 of |row max of X| |row max of h| per real product term (the
-dropped pairs s + t >= 7 and the rounding of both operands, with 2^(E + F)
-at most 4 times the product of the row maxima).  The GPU kernel
-(qt_umma.cu, tcgen05) sums levels 0, 1 and 2 exactly and levels 3..6 in one
-fp32 accumulator, whose rounding adds at most about 2^-45 of the level-0
-scale per accumulation step; it is held to the oracle by the sweep parity
-tests, this file pins the digit arithmetic those tests rely on."""
+restated on the CPU and checked against exact rational arithmetic.
+
+Every double-float value v = hi + lo of a row is scaled by 2^-E (E from the
+row's largest exponent) and cut by error-free splits
+x_s = fl(fl(r + sigma_s) - sigma_s), sigma_s = 1.5 * 2^(16 - 7s), into seven
+signed digits q_s = x_s 2^(7(s+1)) (the low part joining from s = 3).  The
+checks: the digits reconstruct v within 2^-49 of the row scale, they are
+integers of at most 128 in magnitude (exact in bf16), the digit products of
+one level sum below 2^24 (exact in fp32), and a complex mode product built
+from them stays within 2^-43 of the product of the row maxima per term.  The
+GPU kernel (qt_umma.cu, tcgen05) sums as many levels separately as tensor
+memory holds and the rest in one fp32 accumulator; the sweep parity tests
+hold it to the oracle, this file pins the digits those tests rely on."""
 import struct
 from fractions import Fraction
 
@@ -28,29 +29,26 @@ def row_exponent(his):
     return max([1] + [(f32_bits(h) >> 23) & 0xFF for h in his])
 
 
-def mag49(hi, lo, eb):
-    """(negative, |hi + lo| in units of 2^(eb - 126 - 49), rounded): the
-    parts taken with four guard bits from the float bits, then rounded."""
-    bh, bl = f32_bits(hi), f32_bits(lo)
-    eh, el = (bh >> 23) & 0xFF, (bl >> 23) & 0xFF
-    mh = (bh & 0x7FFFFF) | (0x800000 if eh else 0)
-    ml = (bl & 0x7FFFFF) | (0x800000 if el else 0)
-    sh, sl = max(eh, 1) - eb + 29, max(el, 1) - eb + 29
-    uh = mh << sh if sh >= 0 else (mh >> -sh if sh > -24 else 0)
-    ul = ml << sl if sl >= 0 else (ml >> -sl if sl > -24 else 0)
-    if ((bh ^ bl) >> 31) == 0:
-        neg, u2 = bh >> 31, uh + ul
-    elif uh >= ul:
-        neg, u2 = bh >> 31, uh - ul
-    else:
-        neg, u2 = bl >> 31, ul - uh
-    return neg, (u2 + 8) >> 4
+def fsplit(r, sigma):
+    x = np.float32(np.float32(r + sigma) - sigma)
+    return x, np.float32(r - x)
 
 
-def digits(neg, u):
-    """Seven signed digits, most significant first (|q_0| <= 128, others <= 127)."""
-    q = [u >> 42] + [(u >> (42 - 7 * s)) & 127 for s in range(1, DIGITS)]
-    return [-x if neg else x for x in q]
+def digits(hi, lo, eb):
+    """Signed digits q_0..q_6 (Python ints) of hi + lo, as the device cuts them."""
+    sc = np.float32(2.0 ** (126 - eb))
+    rh, rl = np.float32(hi * sc), np.float32(lo * sc)
+    q = []
+    for s in range(DIGITS):
+        sigma = np.float32(1.5 * 2.0 ** (16 - 7 * s))
+        x, rh = fsplit(rh, sigma)
+        if s >= 3:
+            xl, rl = fsplit(rl, sigma)
+            x = np.float32(x + xl)
+        v = Fraction(float(x)) * 2 ** (7 * (s + 1))
+        assert v.denominator == 1
+        q.append(int(v))
+    return q
 
 
 def split(v):
@@ -67,13 +65,13 @@ def complex_row_digits(row):
     """Digits of a row of complex double-float values: (E, re digits, im digits)."""
     parts = [(split(z.real), split(z.imag)) for z in row]
     eb = row_exponent([p[0][0] for p in parts] + [p[1][0] for p in parts])
-    re = [digits(*mag49(h, l, eb)) for (h, l), _ in parts]
-    im = [digits(*mag49(h, l, eb)) for _, (h, l) in parts]
+    re = [digits(h, l, eb) for (h, l), _ in parts]
+    im = [digits(h, l, eb) for _, (h, l) in parts]
     exact_row = [(exact(*r), exact(*i)) for r, i in parts]
     return eb - 126, re, im, exact_row
 
 
-def test_digits_reconstruct_within_one_unit():
+def test_digits_reconstruct_within_the_last_digit():
     rng = np.random.default_rng(5)
     worst = Fraction(0)
     for trial in range(400):
@@ -85,13 +83,21 @@ def test_digits_reconstruct_within_one_unit():
         eb = row_exponent([h for h, _ in parts])
         E = eb - 126
         for h, lo in parts:
-            neg, u = mag49(h, lo, eb)
-            assert u <= 2 ** 49
-            q = digits(neg, u)
-            assert abs(q[0]) <= 128 and all(abs(x) <= 127 for x in q[1:])
+            q = digits(h, lo, eb)
+            assert all(abs(x) <= 128 for x in q)
             rec = sum(Fraction(x) * Fraction(2) ** (-7 * (s + 1)) for s, x in enumerate(q)) * Fraction(2) ** E
             worst = max(worst, abs(rec - exact(h, lo)) / Fraction(2) ** (E - 49))
-    assert worst <= Fraction(57, 100)
+    assert worst <= 1
+
+
+def test_digits_are_exact_in_bf16():
+    # the stored digit x_s = q_s 2^(-7(s+1)), |q_s| <= 128, has at most eight
+    # significant bits
+    for q in range(-128, 129):
+        for s in range(DIGITS):
+            v = np.float32(q * 2.0 ** (-7 * (s + 1)))
+            trunc = np.frombuffer(np.uint32(f32_bits(v) & 0xFFFF0000).tobytes(), np.float32)[0]
+            assert trunc == v
 
 
 def test_level_sums_fit_fp32_exactly():
@@ -104,8 +110,7 @@ def test_level_sums_fit_fp32_exactly():
 
 def test_emulated_mode_product_meets_bound():
     """Y[r, j] = sum_a X[r, a] h[j, a] from digits, levels combined exactly,
-    against the exact product: error <= 2^-43 * K * max|X row| * max|h row|
-    (two real products per complex term, each within 2^-44)."""
+    against the exact product: error <= 2^-43 * K * max|X row| * max|h row|."""
     rng = np.random.default_rng(11)
     R, K, N = 6, 40, 5
     X = (rng.standard_normal((R, K)) + 1j * rng.standard_normal((R, K))) * 10.0 ** rng.integers(-3, 3, (R, 1))

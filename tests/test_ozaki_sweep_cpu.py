@@ -1,10 +1,10 @@
 """The tensor-core mode products (QT_PREC_DF64_TC) at the level of a whole
 sweep, on the CPU: the plan interpreter (tests/plan_emulator.py) runs every
-eligible mode product through the same digit arithmetic as qt_umma.cu
-(double-float operands, seven 7-bit digits against row exponents, exact
-level sums for L <= 2, one float32-rounded sum of the levels 3..6) and the
-sweep is compared with the oracle at the double-float tolerances the GPU
-tests use."""
+eligible mode product through the same digit arithmetic
+as qt_umma.cu (double-float operands, seven signed digits from error-free
+splits against row exponents, exact level sums for L <= 2, one
+float32-rounded sum of the levels 3..6) and the sweep is compared with the
+oracle at the double-float tolerances the GPU tests use."""
 import numpy as np
 import pytest
 

@@ -1,8 +1,10 @@
 """Planner side of the tensor-core mode products (flavour bit 0x8000 with
-double-float arithmetic), on the CPU: in every mode-product stage the tasks
-with a_in, a_out <= 64 (not diagonal) get tensor-core tiles covering their
-rows exactly once and a private slot for the digits of h; every other task
-keeps its classic tiles, which cover its output slots exactly once."""
+double-float or complex64 arithmetic), on the CPU: in every mode-product
+stage the tasks with a_in, a_out <= 64 (not diagonal) get tensor-core tiles
+covering their rows exactly once and a slot of their own in the stage for
+the operand image of h; every other task keeps its classic tiles, which
+cover its output slots exactly once.  Image slots are private within a
+stage and reused across stages (every stage's pre-pass rewrites them)."""
 import numpy as np
 import pytest
 
@@ -33,10 +35,9 @@ def test_tensor_core_tiles_cover_eligible_tasks(problem, plan):
     T = pv.tables
     mp, oz_tiles, ranges, oz_tasks, tiles = T[1], T[40], T[41], T[42], T[43]
     assert len(ranges) == len(T[0])
-    slots = {}
-    n_oz = 0
     for si, (kind, t0, nt, tile0, ntile) in enumerate(T[0]):
         oz0, noz, ozt0, nozt = ranges[si]
+        slots = {}
         if kind != ST_MP:
             assert noz == 0 and nozt == 0
             continue
@@ -64,10 +65,9 @@ def test_tensor_core_tiles_cover_eligible_tasks(problem, plan):
         for t, starts in cl.items():
             n_slots = int(mp[t][6]) * (-(-int(mp[t][8]) // 4)) * int(mp[t][9])
             assert sorted(starts) == list(range(0, n_slots, MP_TILE))
-        n_oz += len(eligible)
-    offs = sorted(slots.values())
-    assert len(offs) == len(set(offs)) == n_oz
-    assert all(b - a >= OZ_H_BYTES for a, b in zip(offs, offs[1:]))
+        offs = sorted(slots.values())
+        assert len(offs) == len(set(offs)) == len(eligible)
+        assert all(b - a >= OZ_H_BYTES for a, b in zip(offs, offs[1:]))
     if problem == "wide_leaves":  # the 80 x 80 leaf products keep classic tiles
         assert sum(int(n) for kind, _, _, _, n in T[0] if kind == ST_MP) > 0
 
