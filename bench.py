@@ -172,13 +172,14 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def cpu_baseline_sweep(tree, sop, psi, budget_s=45.0):
+def cpu_baseline_sweep(tree, sop, psi, threads=None):
     """The reference algorithm on the host cores: the oracle restatement with
-    QuTree's TensorBLAS path (zgemm from OpenBLAS, all cores).  One full sweep
-    is the sample."""
+    QuTree's TensorBLAS path (zgemm from OpenBLAS, all cores, or `threads`).
+    One full sweep is the sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     blas = oracle.attach_openblas(fast=True)
+    oracle.set_blas_threads(threads or os.cpu_count())
     flat = psi.flat()
     t0 = time.perf_counter()
     r = oracle.derivative(tree, sop, flat, backend=oracle.BLAS, fast=True, want_mats=False)
@@ -453,11 +454,15 @@ def run_ours(args, ws, rank, local):
         trees_b, sops_b, psis_b = batched_problem(args.batch_trees)
         fb, _, mob = forest(trees_b)
         sb, pb = forest_sop(sops_b, mob), forest_psi(fb, psis_b)
+        forest_e = {}
         batch = {"trees": args.batch_trees, "nodes": fb.n_nodes,
                  "workload": "uneven trees: modes in {8,16,32,48}, p in {8,16,32}, bonds 4..24 per "
                              "edge (balanced), 2..6 couplings per mode, own SOP per tree"}
         for label, fl in (("double_float", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64),
+                          ("double_float_tensor_cores", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC),
                           ("grouped_double_float", qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64),
+                          ("complex64", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_C32),
+                          ("complex64_tf32x3_tensor_cores", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_TF32X3),
                           ("plain_complex128", qtgpu.QT_PLAN_REFERENCE)):
             hb = qtgpu.HamiltonianRepresentation(sb, fb, flavour=fl, device=local)
             sb_stream = torch.cuda.ExternalStream(hb.stream())
@@ -474,9 +479,15 @@ def run_ours(args, ws, rank, local):
             ms = e0.elapsed_time(e1) / nb
             batch[label] = {"ms_per_forest_sweep": ms, "tree_sweeps_per_s": args.batch_trees / (ms * 1e-3),
                             "executed_gflop": hb.stats()["exec_flops"] / 1e9}
+            forest_e[label] = hb.energies()
             if label == "double_float":
-                batch["energies_first4"] = hb.energies()[:4].tolist()
+                batch["energies_first4"] = forest_e[label][:4].tolist()
             hb.close()
+        ep = forest_e["plain_complex128"]
+        for label, e in forest_e.items():
+            if label != "plain_complex128":
+                batch[label]["max_rel_dE_vs_plain_complex128"] = float(
+                    np.max(np.abs(e - ep) / np.maximum(1.0, np.abs(ep))))
 
     # supplementary: QuTree's SCF / Krylov sweep (qt_scf), one sweep of 5 Krylov
     # vectors per node; the oracle's numpy restatement timed on the 16-mode tree
@@ -518,7 +529,10 @@ def run_ours(args, ws, rank, local):
     if rank == 0:
         t4, s4, p4 = config_problem(4)
         grad = {"workload": "16 modes, p=32, bonds 32, 152 terms; one sweep = derivative + dE/dPhi* of every node"}
+        grads = {}
         for label, fl in (("compressed_double_float", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64),
+                          ("compressed_double_float_tensor_cores", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64_TC),
+                          ("compressed_complex64", qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_C32),
                           ("plain_complex128", qtgpu.QT_PLAN_REFERENCE)):
             hg4 = qtgpu.HamiltonianRepresentation(s4, t4, flavour=fl | qtgpu.QT_PLAN_GRADIENT, device=local)
             g_stream = torch.cuda.ExternalStream(hg4.stream())
@@ -536,7 +550,13 @@ def run_ours(args, ws, rank, local):
             ms = e0.elapsed_time(e1) / ng
             grad[label] = {"ms_per_gradient_sweep": ms, "gradient_sweeps_per_s": 1e3 / ms,
                            "executed_gflop": hg4.stats()["exec_flops"] / 1e9}
+            grads[label] = hg4.gradient()
             hg4.close()
+        gp = grads["plain_complex128"]
+        for label, g in grads.items():
+            if label != "plain_complex128":
+                grad[label]["gradient_rel_err_vs_plain_complex128"] = float(
+                    np.abs(g - gp).max() / np.abs(gp).max())
 
     # supplementary: a Hamiltonian with a CDVR potential (QT_PLAN_CDVR): one
     # sweep = CDVR update (X matrices, grids, potentials on node and edge
@@ -607,6 +627,9 @@ def run_ours(args, ws, rank, local):
                                 "sample": "one full cfg1 sweep, reference call sequence, zgemm via "
                                           f"{'OpenBLAS' if blas else 'naive loops'}",
                                 "energy_diff": abs(cpu_e - energy)}
+        dt1, _, _ = cpu_baseline_sweep(tree, sop, psi, threads=1)
+        line["cpu_baseline"]["single_thread"] = {"value": 1.0 / dt1, "unit": "sweeps/s", "cores": 1,
+                                                 "sample": "the same sweep, OpenBLAS on one thread"}
     print(json.dumps(line), flush=True)
 
 

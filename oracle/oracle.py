@@ -113,6 +113,19 @@ def attach_openblas(fast: bool = True) -> str | None:
     return None
 
 
+def set_blas_threads(n: int) -> bool:
+    """Thread count of the attached OpenBLAS (all cores by default); False
+    when no OpenBLAS is attached or it has no such control."""
+    for ob in _libs.get("_keep", []):
+        for sym in ("scipy_openblas_set_num_threads", "scipy_openblas_set_num_threads64_",
+                    "openblas_set_num_threads"):
+            fn = getattr(ob, sym, None)
+            if fn is not None:
+                fn(int(n))
+                return True
+    return False
+
+
 def detach_blas(fast: bool = True):
     lib(fast).orc_set_zgemm(None, 0)
 

@@ -30,7 +30,7 @@ RAW = 1e-13
 TOL_DF = 1e-11
 RAW_DF = 3e-12
 NOISE = 1e-11  # |dPsi rho| on nodes where (1-P) = 0 (rounding noise of a cancellation)
-# double-float with the mode products and accumulations on the tensor cores:
+# double-float with the mode products on the tensor cores:
 # the digit arithmetic's error is relative to the row maxima of its operands
 # (2^-49 of the row scale per value, plus the fp32 rounding of the last level
 # accumulator when bonds exceed 32), so where the projector cancels large
