@@ -57,6 +57,8 @@ def parse():
                          "costs ~4.5 s per step there)")
     ap.add_argument("--precision-only", action="store_true",
                     help="run only the precision study and print its JSON")
+    ap.add_argument("--precision-log", default=None,
+                    help="append every checkpoint of the precision study to this file as a JSON line")
     return ap.parse_args()
 
 
@@ -252,7 +254,7 @@ def precision_study(args, local):
         h.upload(flat)
         ctx[name] = h
     steps = args.precision_steps
-    every = max(1, steps // 10)
+    every = max(1, steps // 20)
     out = {n: {"trajectory": [], "worst": {"abs_dE": 0.0, "dpsi_rel_rho_weighted": 0.0, "psi_rel": 0.0}}
            for n, _ in arith}
     step_s = {n: 0.0 for n in ctx}
@@ -284,6 +286,10 @@ def precision_study(args, local):
             out[n]["trajectory"].append(r)
             for k in out[n]["worst"]:
                 out[n]["worst"][k] = max(out[n]["worst"][k], r[k])
+        if args.precision_log:
+            with open(args.precision_log, "a") as f:
+                f.write(json.dumps({"step": step, "energy_ref": er, "wall_s": time.perf_counter() - t0,
+                                    **{n: out[n]["trajectory"][-1] for n, _ in arith}}) + "\n")
     for n in ctx:
         ctx[n].close()
     for n, _ in arith:
