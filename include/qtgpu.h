@@ -47,6 +47,10 @@ extern "C" {
 #define QT_ERR_CUDA 4    /* a CUDA runtime call failed                       */
 #define QT_ERR_STATE 5   /* call needs an earlier step (upload, prepare, ...) */
 #define QT_ERR_NUMERIC 6 /* non-finite input or result                       */
+#define QT_ERR_TIMEOUT 7 /* a tensor-core kernel's wait ran out (its CTAs
+                            freed their resources and returned; the results
+                            of that sweep are void); reported, and cleared, by
+                            the next qt_sync, qt_energies or qt_dpsi_download */
 
 /* Leaf operator kinds of the operator table. */
 #define QT_OP_DENSE 0 /* p x p complex matrix, column-major                  */

@@ -234,11 +234,26 @@ void qt_ctx_destroy(qt_ctx* c) {
 
 const char* qt_last_error(const qt_ctx* c) { return c ? c->err.c_str() : g_noctx_err.c_str(); }
 
+namespace {
+// the status word the tensor-core kernels set when a wait runs out (read
+// after the stream synchronised; cleared once reported)
+int check_status(qt_ctx* c) {
+  if (!c->prepared || !c->tables.status) return QT_OK;
+  int st = 0;
+  QT_CUDA(c, cudaMemcpyAsync(&st, c->tables.status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (st == 0) return QT_OK;
+  QT_CUDA(c, cudaMemsetAsync(c->tables.status, 0, sizeof(int), c->stream));
+  return fail(c, QT_ERR_TIMEOUT, "a tensor-core kernel gave up waiting (code " + std::to_string(st) +
+                                     "); the results of that sweep are void");
+}
+}  // namespace
+
 int qt_sync(qt_ctx* c) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   QT_DEVICE(c);
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
-  return QT_OK;
+  return check_status(c);
 }
 
 int qt_get_stream(qt_ctx* c, void** s) {
@@ -483,6 +498,20 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.cols = s.cols;
     hp.push_back(t);
   }
+  std::vector<qt::HpTcGroup> hp_tc;
+  for (auto& s : P.hp_tc_groups) {
+    qt::HpTcGroup g;
+    g.A = ptr_of(c, s.A);
+    g.img = (unsigned char*)c->buf[qt::B_OZ] + s.img;
+    g.before = s.before;
+    g.a = s.a;
+    g.after = s.after;
+    g.ap = (s.a + 7) & ~7;
+    g.n = s.n;
+    g.nchunks = s.nchunks;
+    for (int m = 0; m < qt::kHpTcMembers; ++m) g.member[m] = s.member[m];
+    hp_tc.push_back(g);
+  }
   std::vector<qt::AccTask> acc;
   for (auto& s : P.acc) {
     qt::AccTask t;
@@ -665,6 +694,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, P.ew_tiles);
   put(blob, offs, P.mp_oz_tiles);
   put(blob, offs, P.mp_oz_tasks);
+  put(blob, offs, hp_tc);
+  put(blob, offs, P.hp_tc_items);
+  put(blob, offs, P.hp_tc_imgs);
   {
     cudaError_t e = dev_malloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -716,6 +748,9 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.status = reinterpret_cast<int*>(c->buf[qt::B_PARAM] + 15);
   c->tables.mp_oz_tiles = (int2*)(base + offs[32]);
   c->tables.mp_oz_tasks = (int*)(base + offs[33]);
+  c->tables.hp_tc_groups = (qt::HpTcGroup*)(base + offs[34]);
+  c->tables.hp_tc_items = (int4*)(base + offs[35]);
+  c->tables.hp_tc_imgs = (int2*)(base + offs[36]);
   if (P.cdvr) {  // CDVR constants: seeded noise, leaf grids, identity
     QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_CDVR], 0, c->buf_elems[qt::B_CDVR] * 16, c->stream));
     for (auto& init : P.cdvr_init)
@@ -871,11 +906,21 @@ int qt_psi_load(qt_ctx* c, const char* path) {
 }
 
 namespace {
-// kernel launches of stages [b0, b1) (a split hole-product stage launches two)
+// kernel launches of stages [b0, b1): a hole-product stage one per tile
+// shape, two for its tensor-core items (image pre-pass and products), one
+// for the partial sums of split tasks; a mode-product stage one for its
+// FP32-pipe tiles and two for its tensor-core tiles (pre-pass and products)
 int64_t kernels_in(const qt::Plan& P, int64_t b0, int64_t b1) {
   int64_t n = 0;
-  for (int64_t i = b0; i < b1; ++i)
-    n += (P.stages[i].kind == qt::ST_HP ? P.stages[i].nseg : 1) + (P.stages[i].aux ? 1 : 0);
+  for (int64_t i = b0; i < b1; ++i) {
+    const qt::Stage& st = P.stages[i];
+    if (st.kind == qt::ST_HP)
+      n += st.nseg + (st.nhti > 0 ? (st.nhtu > 0 ? 2 : 1) : 0) + (st.aux ? 1 : 0);
+    else if (st.kind == qt::ST_MP || st.kind == qt::ST_ACC)
+      n += (st.n_tiles > 0 ? 1 : 0) + (st.noz > 0 ? (st.nozt > 0 ? 2 : 1) : 0);
+    else
+      n += 1;
+  }
   return n;
 }
 // launches of one frozen-matrix derivative graph
@@ -1003,7 +1048,7 @@ int qt_dpsi_download(qt_ctx* c, double* out) {
   QT_CUDA(c, cudaMemcpyAsync(out, c->buf[qt::B_DPSI64], c->plan.psi_packed * 16, cudaMemcpyDeviceToHost,
                              c->stream));
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
-  return QT_OK;
+  return check_status(c);
 }
 
 int qt_gradient_download(qt_ctx* c, double* out) {
@@ -1042,6 +1087,7 @@ int qt_energies(qt_ctx* c, double* out, int n_trees) {
                                cudaMemcpyDeviceToHost, c->stream));
   }
   QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (int st = check_status(c)) return st;
   for (int k = 0; k < n_trees; ++k) {
     out[4 * k + 0] = v[2 * k].x;
     out[4 * k + 1] = v[2 * k].y;

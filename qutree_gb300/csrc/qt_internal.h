@@ -44,6 +44,33 @@ struct HPTask {
   int rows, cols;  // outputs per thread along i and j (1..4)
 };
 
+// hole products on the tensor cores (qt_umma.cu, double-float plans): groups
+// of up to eight tasks that share the operand A form one 128-row accumulator
+// tile (rows: the tasks' B columns j, columns: A's i, real and imaginary
+// parts); the reduction runs in chunks of 64 k, each chunk with its own
+// power-of-two scales.  A group's member tasks (indices into the task table)
+// all have the same a, before and after.
+constexpr int kHpTcChunk = 64;     // k per chunk
+constexpr int kHpTcMembers = 8;    // tasks per group (a >= 16)
+struct HpTcGroup {
+  const double2* A;
+  unsigned char* img;  // A's operand images, one per chunk (hp_tc_chunk_bytes)
+  int before, a, after;
+  int ap;              // a padded to a multiple of 8
+  int n, nchunks;
+  int member[kHpTcMembers];
+};
+// a qualifying task: 16 <= a <= 64 and at least two chunks of reduction
+inline bool hp_tc_eligible(int before, int a, int after) {
+  return a >= 16 && a <= 64 && (int64_t)before * after >= 2 * kHpTcChunk;
+}
+// bytes of one chunk of A's image: 4 steps of 16 k x 7 digits x rows
+// [Ai | Ar | -Ai] (3 ap) x 16 bf16, then ap column exponents (int, 64 slots)
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+constexpr int64_t hp_tc_chunk_bytes(int ap) { return (int64_t)4 * 7 * 3 * ap * 16 * 2 + 64 * 4; }
+
 // out[r, j] (+)= alpha * sum_t sum_j' H_t(j, j') X_t[r, j'] over the terms
 // [first, first+count) of the AccTerm table; H == nullptr means identity.
 struct AccTerm {
@@ -234,6 +261,8 @@ struct Stage {
   int seg0 = 0, nseg = 0;  // hole-product stage: its tile segments (one launch per micro-tile shape)
   int64_t oz0 = 0, noz = 0;  // mode-product stage: its tensor-core tiles (mp_oz_tiles)
   int64_t ozt0 = 0, nozt = 0;  // and its tensor-core tasks (mp_oz_tasks, digits of h)
+  int64_t hti0 = 0, nhti = 0;  // hole-product stage: its tensor-core items (hp_tc_items)
+  int64_t htu0 = 0, nhtu = 0;  // and the units of its image pre-pass (hp_tc_imgs)
   double flops = 0;  // executed flops of the stage
   double bytes = 0;  // algorithmic bytes: operands read once, results written once
 };
@@ -482,6 +511,17 @@ struct Plan {
   std::vector<int2> mp_oz_tiles;
   std::vector<int> mp_oz_tasks;
   int64_t oz_bytes = 0;  // B_OZ: operand images of the tensor-core tasks of one stage (reused by every stage)
+  // double-float plans with tensor-core hole products (groups bound to HpTcGroup)
+  bool hp_tensor = false;
+  struct SHpTcGroup {
+    Ref A;
+    int before = 0, a = 0, after = 0, n = 0, nchunks = 0;
+    int member[kHpTcMembers] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int64_t img = 0;  // byte offset of the images in B_OZ
+  };
+  std::vector<SHpTcGroup> hp_tc_groups;
+  std::vector<int4> hp_tc_items;  // (group, z, first chunk, end chunk)
+  std::vector<int2> hp_tc_imgs;   // (group, chunk) of the image pre-pass
   std::vector<int4> acc_tiles;
   std::vector<int2> cvt_tiles;
   // constant matrices written once at prepare: (offset, d) identity
@@ -547,6 +587,9 @@ struct DevTables {
   const int4* hp_segs = nullptr;  // host array: (rows, cols, first tile, tile count)
   int2* mp_oz_tiles = nullptr;
   int* mp_oz_tasks = nullptr;
+  HpTcGroup* hp_tc_groups = nullptr;
+  int4* hp_tc_items = nullptr;
+  int2* hp_tc_imgs = nullptr;
   TCTask* tc = nullptr;
   int4* tc_tiles = nullptr;
   GSTask* gs = nullptr;
@@ -627,6 +670,12 @@ constexpr int kMpOzSub = 4;
 // 64 row exponents (int)
 constexpr int64_t kMpOzImageBytes = (int64_t)4 * 7 * 2 * 64 * 16 * 2 + 64 * 4;
 inline int64_t mp_oz_h_bytes() { return kMpOzImageBytes; }
+// hole products on the tensor cores: items (group, range z, first chunk, end
+// chunk) of one stage, a CTA takes a contiguous run of them; image units
+// (group, chunk) of the pre-pass that writes A's images
+cudaError_t launch_hp_tc(const HPTask* tasks, const HpTcGroup* groups, const int4* items, int64_t first_item,
+                         int64_t n_items, const int2* img_units, int64_t first_unit, int64_t n_units,
+                         double2* ws, int* status, cudaStream_t s);
 // weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
 // max_n / max_d bound the tasks' matrix counts and orders (shared memory)
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,

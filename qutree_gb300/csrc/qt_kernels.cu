@@ -1579,6 +1579,12 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
         cudaError_t e = launch_hp_shape<P>(sg.x, sg.y, t.hp, t.hp_tiles, sg.z, sg.w, reinterpret_cast<S*>(t.hp_ws), s);
         if (e != cudaSuccess) return e;
       }
+      if (st.nhti > 0) {
+        if (!std::is_same<P, DF64>::value) return cudaErrorInvalidValue;  // the planner emits none
+        cudaError_t e = launch_hp_tc(t.hp, t.hp_tc_groups, t.hp_tc_items, st.hti0, st.nhti, t.hp_tc_imgs, st.htu0,
+                                     st.nhtu, reinterpret_cast<double2*>(t.hp_ws), t.status, s);
+        if (e != cudaSuccess) return e;
+      }
       if (st.aux)
         k_hp_sum<P><<<(unsigned)(st.n_tasks * kHpSumChunks), kThreads, 0, s>>>(t.hp, st.first_task,
                                                              reinterpret_cast<const S*>(t.hp_ws));

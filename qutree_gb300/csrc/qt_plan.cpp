@@ -37,6 +37,7 @@
 #include <map>
 #include <set>
 #include <stdexcept>
+#include <tuple>
 
 #include "qt_internal.h"
 
@@ -464,8 +465,14 @@ class Builder {
     auto ntiles = [](const Plan::SHP& h) {
       return (int64_t)((h.a + kTile - 1) / kTile) * ((h.a + kTile - 1) / kTile);
     };
+    // double-float plans with tensor-core hole products: the qualifying tasks
+    // take the tensor-core path (hp_tensor_items), the others the tiles below
+    std::vector<char> tc(t1 - t0, 0);
+    if (P.hp_tensor)
+      for (int64_t t = t0; t < t1; ++t) tc[t - t0] = hp_tc_eligible(P.hp[t].before, P.hp[t].a, P.hp[t].after);
     double work = 0;
-    for (int64_t t = t0; t < t1; ++t) work += (double)ntiles(P.hp[t]) * P.hp[t].before * P.hp[t].after;
+    for (int64_t t = t0; t < t1; ++t)
+      if (!tc[t - t0]) work += (double)ntiles(P.hp[t]) * P.hp[t].before * P.hp[t].after;
     const double target = 6.0 * 152;
     int64_t kc = (int64_t)std::ceil(work / target / kRows) * kRows;
     kc = std::max<int64_t>(kc, 64);
@@ -473,6 +480,7 @@ class Builder {
     int64_t ws = 0;
     bool split = false;
     for (int64_t t = t0; t < t1; ++t) {
+      if (tc[t - t0]) continue;
       Plan::SHP& h = P.hp[t];
       // outputs per thread: the fewest (rows x cols) whose thread grid
       // ceil(m/rows) x ceil(m/cols) fits 256 threads and 64 staged columns
@@ -487,12 +495,13 @@ class Builder {
         split = true;
       }
     }
+    if (P.hp_tensor && hp_tensor_items(t0, t1, tc, ws)) split = true;
     // tiles grouped by micro-tile shape: one launch per shape
     for (int shape = 0; shape < 16; ++shape) {
       const int64_t first = (int64_t)P.hp_tiles.size();
       for (int64_t t = t0; t < t1; ++t) {
         const Plan::SHP& h = P.hp[t];
-        if ((h.rows - 1) * 4 + (h.cols - 1) != shape) continue;
+        if (tc[t - t0] || (h.rows - 1) * 4 + (h.cols - 1) != shape) continue;
         for (int64_t y = 0; y < ntiles(h); ++y)
           for (int z = 0; z < h.splits; ++z) P.hp_tiles.push_back(make_int4((int)t, (int)y, z, 0));
       }
@@ -504,15 +513,79 @@ class Builder {
     return split;
   }
 
+  // Tensor-core hole products of the stage: the qualifying tasks (tc) in
+  // groups of up to 128 / a tasks sharing A, one image of A per distinct A in
+  // the stage's part of B_OZ, and work items of about equal length: ranges of
+  // cpi chunks, cpi chosen so that the stage has about two items per SM.  A
+  // task cut into several ranges gets workspace slots for its partial tiles.
+  // Returns whether any task was cut.
+  bool hp_tensor_items(int64_t t0, int64_t t1, const std::vector<char>& tc, int64_t& ws) {
+    const int64_t g0 = (int64_t)P.hp_tc_groups.size();
+    std::map<std::tuple<int, int64_t, int, int, int>, int64_t> open, img;
+    for (int64_t t = t0; t < t1; ++t) {
+      if (!tc[t - t0]) continue;
+      const Plan::SHP& h = P.hp[t];
+      const auto key = std::make_tuple(h.A.buf, h.A.off, h.before, h.a, h.after);
+      auto it = open.find(key);
+      if (it == open.end() || P.hp_tc_groups[it->second].n >= std::min(kHpTcMembers, 128 / h.a)) {
+        Plan::SHpTcGroup g;
+        g.A = h.A;
+        g.before = h.before;
+        g.a = h.a;
+        g.after = h.after;
+        g.nchunks = (int)(((int64_t)h.before * h.after + kHpTcChunk - 1) / kHpTcChunk);
+        const int64_t gi = (int64_t)P.hp_tc_groups.size();
+        auto im = img.find(key);
+        if (im == img.end()) {  // this group's pre-pass writes A's images
+          g.img = stage_oz_;
+          stage_oz_ += g.nchunks * hp_tc_chunk_bytes((h.a + 7) & ~7);
+          img[key] = g.img;
+          for (int c = 0; c < g.nchunks; ++c) P.hp_tc_imgs.push_back(make_int2((int)gi, c));
+        } else {
+          g.img = im->second;
+        }
+        P.hp_tc_groups.push_back(g);
+        open[key] = gi;
+        it = open.find(key);
+      }
+      Plan::SHpTcGroup& g = P.hp_tc_groups[it->second];
+      g.member[g.n++] = (int)t;
+    }
+    const int64_t g1 = (int64_t)P.hp_tc_groups.size();
+    int64_t units = 0;
+    for (int64_t g = g0; g < g1; ++g) units += P.hp_tc_groups[g].nchunks;
+    const int cpi = (int)std::max<int64_t>(1, (units + 2 * 152 - 1) / (2 * 152));
+    bool split = false;
+    for (int64_t g = g0; g < g1; ++g) {
+      const Plan::SHpTcGroup& G = P.hp_tc_groups[g];
+      const int splits = (G.nchunks + cpi - 1) / cpi;
+      for (int m = 0; m < G.n; ++m) {
+        Plan::SHP& h = P.hp[G.member[m]];
+        h.splits = splits;
+        h.kchunk = cpi * kHpTcChunk;
+        h.ws = 0;
+        if (splits > 1) {
+          h.ws = ws;
+          ws += (int64_t)splits * h.a * h.a;
+          split = true;
+        }
+      }
+      for (int z = 0; z < splits; ++z)
+        P.hp_tc_items.push_back(make_int4((int)g, z, z * cpi, std::min(G.nchunks, (z + 1) * cpi)));
+    }
+    return split;
+  }
+
   void emit_stage(int kind, int64_t t0, int64_t t1, int64_t tile0, int64_t tile1,
                   const char* name) {
     if (t1 <= t0) return;
     bool split = false;
     const int64_t seg0 = (int64_t)P.hp_segs.size();
+    const int64_t hti0 = (int64_t)P.hp_tc_items.size(), htu0 = (int64_t)P.hp_tc_imgs.size();
+    stage_oz_ = 0;  // operand images are rewritten by every stage's pre-pass
     if (kind == ST_HP) split = hp_split(t0, t1, tile0, tile1);
     const int64_t oz0 = (int64_t)P.mp_oz_tiles.size();
     const int64_t ozt0 = (int64_t)P.mp_oz_tasks.size();
-    stage_oz_ = 0;  // operand images are rewritten by every stage's pre-pass
     if (kind == ST_MP && P.mp_tensor) tile1 = mp_tensor_tiles(t0, t1, tile0, tile1);
     P.oz_bytes = std::max(P.oz_bytes, stage_oz_);
     const double f1 = P.stats.exec_flops;
@@ -533,6 +606,10 @@ class Builder {
     s.noz = (int64_t)P.mp_oz_tiles.size() - oz0;
     s.ozt0 = ozt0;
     s.nozt = (int64_t)P.mp_oz_tasks.size() - ozt0;
+    s.hti0 = hti0;
+    s.nhti = (int64_t)P.hp_tc_items.size() - hti0;
+    s.htu0 = htu0;
+    s.nhtu = (int64_t)P.hp_tc_imgs.size() - htu0;
     P.stages.push_back(s);
   }
 
@@ -2008,6 +2085,7 @@ std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTa
     if ((flavour & 0x8000) && prec == 0)
       throw std::runtime_error("tensor-core mode products need double-float or complex64 arithmetic");
     plan.mp_tensor = (flavour & 0x8000) != 0;
+    plan.hp_tensor = plan.mp_tensor && prec == 1;
     Builder b(plan, nodes, ops, sop, flavour & ~0xA000, prec, scratch_budget_elems);
     b.set_scf(scf);
     b.set_cdvr(cdvr);

@@ -508,6 +508,44 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
         v.push_back(t.y);
       }
       break;
+    case 52:  // tensor-core hole-product groups: (A buf, A off, before, a, after, n, nchunks, image, members x 8)
+      for (auto& g : P.hp_tc_groups) {
+        v.push_back(g.A.buf);
+        v.push_back(g.A.off);
+        v.push_back(g.before);
+        v.push_back(g.a);
+        v.push_back(g.after);
+        v.push_back(g.n);
+        v.push_back(g.nchunks);
+        v.push_back(g.img);
+        for (int m = 0; m < qt::kHpTcMembers; ++m) v.push_back(m < g.n ? g.member[m] : -1);
+      }
+      break;
+    case 53:  // tensor-core hole-product items: (group, range, first chunk, end chunk)
+      for (auto& t : P.hp_tc_items) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+        v.push_back(t.z);
+        v.push_back(t.w);
+      }
+      break;
+    case 54:  // image pre-pass units: (group, chunk)
+      for (auto& t : P.hp_tc_imgs) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+      }
+      break;
+    case 55:  // per stage: tensor-core hole-product items and image units (first, count, first, count)
+      for (auto& st : P.stages) {
+        v.push_back(st.hti0);
+        v.push_back(st.nhti);
+        v.push_back(st.htu0);
+        v.push_back(st.nhtu);
+      }
+      break;
+    case 56:  // B_OZ bytes
+      v.push_back(P.oz_bytes);
+      break;
     default:
       break;
   }

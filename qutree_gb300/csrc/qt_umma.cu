@@ -652,6 +652,404 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
   }
 }
 
+// ---------------------------------------------------------------------------
+// Hole products on the tensor cores (double-float plans).
+//
+// S_t(i, j) = sum_k conj(A[k; i]) B_t[k; j] for the tasks t of a group that
+// share A.  The accumulator tile has one row per (task, j) of the group --
+// the M side, B_t's digits cut by the producers -- and 2 ap columns: the real
+// parts for i < ap, the imaginary parts after them.  With A = Ar + i Ai and
+// B = Br + i Bi,
+//   Re = Br Ar + Bi Ai,   Im = Bi Ar - Br Ai,
+// i.e. two MMAs of N = 2 ap per digit pair: Br x [Ar | -Ai] and
+// Bi x [Ai | Ar].  The N side stores rows [Ai | Ar | -Ai] once; the two
+// operands are its rows ap.. and 0.. .  A's digits come from a pre-pass (one
+// image per 64-k chunk, with the chunk's column exponents); the reduction
+// runs chunk by chunk, every chunk with its own row and column scales, its
+// level sums exact in fp32 (at most 7 pairs x 2 x 64 products of |digit
+// products| <= 2^14 units per level), recombined in double-float by the
+// epilogue and added to the task's output (or to its partial tile for the
+// item's range of chunks; the sweep's partial-tile sum adds the ranges).
+// ---------------------------------------------------------------------------
+constexpr int kHpNStage = kDig * 3 * 64 * 32;  // N side of one 16-k step at ap = 64
+
+struct HpSmem {
+  unsigned char a[2][kOzAStage];
+  unsigned char n[2][kHpNStage];
+  Bars bar;
+  uint8_t ex[2][kRows];
+  uint8_t pm[2][2][kRows];
+  int fx[4][64];
+};
+static_assert(sizeof(HpSmem) <= 232448, "shared memory of the hole-product kernel exceeds 227 KB");
+
+// element k of row `row` of a hole-product operand of shape (before, a, after):
+// k = b + before c, offset b + before row + before a c; walked in steps of one
+struct KWalk {
+  int b, c;
+  __device__ __forceinline__ KWalk(int k, int before) : c(k / before), b(k - (k / before) * before) {}
+  __device__ __forceinline__ int64_t off(int row, int before, int a) const {
+    return b + (int64_t)before * row + (int64_t)before * a * c;
+  }
+  __device__ __forceinline__ void next(int before) {
+    if (++b == before) {
+      b = 0;
+      ++c;
+    }
+  }
+};
+
+// pre-pass: the digits of A for one chunk of 64 k of a group -- per 16-k
+// step and digit a plane of 3 ap rows: Ai at row i, Ar at ap + i, -Ai at
+// 2 ap + i (rows a..ap of each block zero) -- and the chunk's column
+// exponents.  Thread (i, ks) takes row i of the 16-k step ks.
+__global__ void __launch_bounds__(256) k_hp_tc_img(const HpTcGroup* __restrict__ groups,
+                                                   const int2* __restrict__ units, int64_t first) {
+  const int2 u = units[first + blockIdx.x];
+  const HpTcGroup G = groups[u.x];
+  const int c = u.y, ap = G.ap, a = G.a, before = G.before;
+  const int K = before * G.after;
+  unsigned char* img = G.img + (size_t)c * hp_tc_chunk_bytes(ap);
+  const float4* __restrict__ A = reinterpret_cast<const float4*>(G.A);
+  __shared__ int fx[64];
+  const int i = threadIdx.x & 63, ks = threadIdx.x >> 6;
+  if (threadIdx.x < 64) fx[threadIdx.x] = 1;
+  __syncthreads();
+  float4 v[16];
+  const int k0 = c * kHpTcChunk + ks * kChunkK;
+  int m = 1;
+  {
+    KWalk w(min(k0, K), before);
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      v[kk] = (i < a && k0 + kk < K) ? __ldg(A + w.off(i, before, a)) : make_float4(0.f, 0.f, 0.f, 0.f);
+      w.next(before);
+      m = max(m, max(fexp(v[kk].x), fexp(v[kk].z)));
+    }
+  }
+  atomicMax(&fx[i], m);
+  __syncthreads();
+  if (i < ap) {
+    const int f = fx[i];
+    const int rows = 3 * ap, plane = rows * 32;
+    unsigned char* base = img + (size_t)ks * kDig * plane;
+#pragma unroll
+    for (int g = 0; g < 2; ++g) {  // the two 8-k core rows of the step
+      uint32_t wr[kDig][4], wi[kDig][4];
+#pragma unroll
+      for (int p = 0; p < 4; ++p) {
+        float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
+        digits_f32(v[8 * g + 2 * p].x, v[8 * g + 2 * p].y, f, d0);
+        digits_f32(v[8 * g + 2 * p + 1].x, v[8 * g + 2 * p + 1].y, f, d1);
+        digits_f32(v[8 * g + 2 * p].z, v[8 * g + 2 * p].w, f, e0);
+        digits_f32(v[8 * g + 2 * p + 1].z, v[8 * g + 2 * p + 1].w, f, e1);
+#pragma unroll
+        for (int d = 0; d < kDig; ++d) {
+          wr[d][p] = pack_bf16(d0[d], d1[d]);
+          wi[d][p] = pack_bf16(e0[d], e1[d]);
+        }
+      }
+#pragma unroll
+      for (int d = 0; d < kDig; ++d) {
+        unsigned char* pl = base + (size_t)d * plane;
+        const uint4 re = make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
+        const uint4 im = make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
+        const uint4 nim = make_uint4(im.x ^ 0x80008000u, im.y ^ 0x80008000u, im.z ^ 0x80008000u, im.w ^ 0x80008000u);
+        *reinterpret_cast<uint4*>(pl + core_off(i, g, rows)) = im;
+        *reinterpret_cast<uint4*>(pl + core_off(ap + i, g, rows)) = re;
+        *reinterpret_cast<uint4*>(pl + core_off(2 * ap + i, g, rows)) = nim;
+      }
+    }
+  }
+  if (threadIdx.x < 64) reinterpret_cast<int*>(img + (size_t)4 * kDig * 3 * ap * 32)[threadIdx.x] = fx[threadIdx.x];
+}
+
+__global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restrict__ tasks,
+                                                          const HpTcGroup* __restrict__ groups,
+                                                          const int4* __restrict__ items, int64_t item0,
+                                                          int64_t n_items, double2* __restrict__ ws, int* status) {
+  extern __shared__ __align__(128) unsigned char hp_raw[];
+  HpSmem& sm = *reinterpret_cast<HpSmem*>(hp_raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t per = n_items / gridDim.x, extra = n_items % gridDim.x;
+  const int64_t my0 = blockIdx.x * per + min((int64_t)blockIdx.x, extra);
+  const int64_t my1 = my0 + per + (blockIdx.x < extra ? 1 : 0);
+
+  if (tid == 0) {
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&sm.bar.full[s], 256);
+      mbar_init(&sm.bar.empty[s], 1);
+      mbar_init(&sm.bar.exready[s], 128);
+      mbar_init(&sm.bar.exfree[s], 128);
+      mbar_init(&sm.bar.pmax[s], 256);
+    }
+    mbar_init(&sm.bar.tfull, 1);
+    mbar_init(&sm.bar.tempty, 128);
+    mbar_init(&sm.bar.drain, 1);
+    mbar_fence_init();
+  }
+  if (warp == 12) tmem_alloc(&sm.bar.tmem, 512u);
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tmem = sm.bar.tmem;
+  bool ok = true;
+
+  if (warp < 8) {
+    // ---------------- producers: two per row, each 8 k of every 16-k step ----------------
+    const int r = tid & (kRows - 1), h = tid >> 7;
+    uint32_t q = 0, un = 0;
+    for (int64_t it = my0; it < my1 && ok; ++it) {
+      const int4 itm = items[item0 + it];
+      const HpTcGroup& G = groups[itm.x];
+      const int before = G.before, a = G.a, ap = G.ap;
+      const int K = before * G.after;
+      const int mi = r / a, j = r - mi * a;
+      const bool valid = mi < G.n;
+      const float4* __restrict__ B = valid ? reinterpret_cast<const float4*>(tasks[G.member[mi]].B) : nullptr;
+      const uint32_t nbytes = (uint32_t)(kDig * 3 * ap * 32);
+      const unsigned char* img = G.img;
+      for (int c = itm.z; c < itm.w; ++c, ++un) {
+        const int buf = (int)(un & 1);
+        const uint32_t use_par = (un >> 1) & 1;
+        // this thread's 32 values of the chunk: k = 64 c + 16 ks + 8 h + i
+        auto load8 = [&](float4 (&x)[8], int ks) {
+          const int k0 = c * kHpTcChunk + ks * kChunkK + h * 8;
+          KWalk w(min(k0, K), before);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            x[i] = (valid && k0 + i < K) ? __ldg(B + w.off(j, before, a)) : make_float4(0.f, 0.f, 0.f, 0.f);
+            w.next(before);
+          }
+        };
+        int m = 1;
+        if (valid)
+          for (int ks = 0; ks < 4; ++ks) {
+            float4 x[8];
+            load8(x, ks);
+#pragma unroll
+            for (int i = 0; i < 8; ++i) m = max(m, max(fexp(x[i].x), fexp(x[i].z)));
+          }
+        sm.pm[buf][h][r] = (uint8_t)m;
+        mbar_arrive(&sm.bar.pmax[buf]);
+        if (!mbar_wait(&sm.bar.pmax[buf], use_par, kSpin)) {
+          set_status(status, 19);
+          ok = false;
+          break;
+        }
+        const int eb = max(sm.pm[buf][0][r], sm.pm[buf][1][r]);
+        if (h == 0) {
+          if (!mbar_wait(&sm.bar.exfree[buf], use_par ^ 1, kSpin)) {
+            set_status(status, 18);
+            ok = false;
+            break;
+          }
+          sm.ex[buf][r] = (uint8_t)eb;
+          mbar_arrive(&sm.bar.exready[buf]);
+        }
+        float4 nx[8];
+        load8(nx, 0);
+        for (int ks = 0; ks < 4; ++ks, ++q) {
+          const int s = q & 1;
+          float4 x[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) x[i] = nx[i];
+          if (ks + 1 < 4) load8(nx, ks + 1);
+          if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
+            set_status(status, 11);
+            ok = false;
+            break;
+          }
+          if (tid == 0) {
+            // A's digits of this step; the copy completes on full[s] (it
+            // finishes within microseconds, before any wait could run out)
+            mbar_expect_tx(&sm.bar.full[s], nbytes);
+            bulk_g2s(sm.n[s], img + (size_t)c * hp_tc_chunk_bytes(ap) + (size_t)ks * nbytes, nbytes,
+                     &sm.bar.full[s]);
+          }
+          unsigned char* As = sm.a[s];
+          uint32_t wr[kDig][4], wi[kDig][4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
+            digits_f32(x[2 * i].x, x[2 * i].y, eb, d0);
+            digits_f32(x[2 * i + 1].x, x[2 * i + 1].y, eb, d1);
+            digits_f32(x[2 * i].z, x[2 * i].w, eb, e0);
+            digits_f32(x[2 * i + 1].z, x[2 * i + 1].w, eb, e1);
+#pragma unroll
+            for (int d = 0; d < kDig; ++d) {
+              wr[d][i] = pack_bf16(d0[d], d1[d]);
+              wi[d][i] = pack_bf16(e0[d], e1[d]);
+            }
+          }
+          const int off = core_off(r, h, kRows);
+#pragma unroll
+          for (int d = 0; d < kDig; ++d) {
+            *reinterpret_cast<uint4*>(As + (2 * d + 0) * kOzAPlane + off) =
+                make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
+            *reinterpret_cast<uint4*>(As + (2 * d + 1) * kOzAPlane + off) =
+                make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
+          }
+          fence_proxy_async();
+          mbar_arrive(&sm.bar.full[s]);
+        }
+        if (!ok) break;
+      }
+    }
+  } else if (warp == 12) {
+    // ---------------- MMA issue (one thread) ----------------
+    if (lane == 0) {
+      uint32_t q = 0, un = 0;
+      for (int64_t it = my0; it < my1 && ok; ++it) {
+        const int4 itm = items[item0 + it];
+        const int ap = groups[itm.x].ap;
+        const int NL = levels_for(ap);
+        const uint32_t id = idesc_m128(1, 2 * ap, false);
+        const uint32_t lboA = (kRows / 8) * 128, lboN = (uint32_t)(3 * ap / 8) * 128;
+        const uint64_t pA = kOzAPlane >> 4, pN = (uint64_t)((3 * ap * 32) >> 4);
+        const uint64_t p1 = (uint64_t)((ap / 8) * 128 >> 4);  // rows ap..: [Ar | -Ai]
+        for (int c = itm.z; c < itm.w && ok; ++c, ++un) {
+          const uint32_t tpar = un & 1;
+          if (!mbar_wait(&sm.bar.tempty, tpar ^ 1, kSpin)) {
+            set_status(status, 14);
+            ok = false;
+            break;
+          }
+          fence_after_sync();
+          for (int ks = 0; ks < 4; ++ks, ++q) {
+            const int s = q & 1;
+            if (!mbar_wait(&sm.bar.full[s], (q >> 1) & 1, kSpin)) {
+              set_status(status, 15);
+              ok = false;
+              break;
+            }
+            fence_after_sync();
+            const uint64_t dA = desc_kmajor(smem_u32(sm.a[s]), lboA, 128);
+            const uint64_t dN = desc_kmajor(smem_u32(sm.n[s]), lboN, 128);
+            const uint32_t first = ks == 0 ? 1u : 0u;
+#pragma unroll
+            for (int sd = 0; sd < kDig; ++sd) {
+              const uint64_t ar = dA + (uint64_t)(2 * sd) * pA, ai = ar + pA;
+#pragma unroll
+              for (int td = 0; td + sd < kDig; ++td) {
+                const int L = sd + td < NL - 1 ? sd + td : NL - 1;
+                const uint64_t nb = dN + (uint64_t)td * pN;
+                const uint32_t d = tmem + (uint32_t)(L * 2 * ap);
+                const uint32_t acc = (first && sd == 0 && td == L) ? 0u : 1u;
+                mma_bf16(d, ar, nb + p1, id, acc);  // Br x [Ar | -Ai]
+                mma_bf16(d, ai, nb, id, 1);         // Bi x [Ai | Ar]
+              }
+            }
+            commit(&sm.bar.empty[s]);
+          }
+          if (!ok) break;
+          commit(&sm.bar.tfull);
+        }
+      }
+      commit(&sm.bar.drain);
+      if (!mbar_wait(&sm.bar.drain, 0, kSpin)) set_status(status, 16);
+    }
+  } else if (warp < 12) {
+    // ---------------- epilogue: warp 8 + qd reads lanes 32 qd .. ----------------
+    const int qd = warp - 8;
+    const int r = 32 * qd + lane;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * qd) << 16);
+    int* fxw = sm.fx[qd];
+    uint32_t un = 0;
+    for (int64_t it = my0; it < my1 && ok; ++it) {
+      const int4 itm = items[item0 + it];
+      const HpTcGroup& G = groups[itm.x];
+      const int a = G.a, ap = G.ap, NL = levels_for(ap);
+      const int mi = r / a, j = r - mi * a;
+      const bool live = mi < G.n;
+      float4* row = nullptr;
+      if (live) {
+        const HPTask& t = tasks[G.member[mi]];
+        double2* dst = t.splits <= 1 ? t.S : ws + t.ws + (int64_t)itm.y * a * a;
+        row = reinterpret_cast<float4*>(dst) + (int64_t)a * j;
+      }
+      for (int c = itm.z; c < itm.w; ++c, ++un) {
+        const int buf = (int)(un & 1);
+        if (!mbar_wait(&sm.bar.exready[buf], (un >> 1) & 1, kSpin) || !mbar_wait(&sm.bar.tfull, un & 1, kSpin)) {
+          set_status(status, 17);
+          ok = false;
+          break;
+        }
+        fence_after_sync();
+        const int er = (int)sm.ex[buf][r];
+        mbar_arrive(&sm.bar.exfree[buf]);
+        const int* fxg = reinterpret_cast<const int*>(G.img + (size_t)c * hp_tc_chunk_bytes(ap) +
+                                                      (size_t)4 * kDig * 3 * ap * 32);
+        __syncwarp();
+        for (int i = lane; i < 64; i += 32) fxw[i] = __ldg(fxg + i);
+        __syncwarp();
+        const bool first = c == itm.z;
+        for (int i0 = 0; i0 < ap; i0 += 8) {
+          __syncwarp();
+          float vre[8], vim[8], lre[8], lim[8];
+          float lv[kDig][8];
+#pragma unroll
+          for (int part = 0; part < 2; ++part) {
+#pragma unroll
+            for (int L = 0; L < kDig; ++L)
+              if (L < NL) tmem_ld8(lane_addr + (uint32_t)(L * 2 * ap + part * ap + i0), lv[L]);
+            tmem_wait_ld();
+            float* v = part ? vim : vre;
+            float* l = part ? lim : lre;
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+              v[i] = lv[0][i];
+              l[i] = 0.f;
+              if (NL > 1) df_add(v[i], l[i], lv[1][i], 0.f);
+              if (NL > 2) df_add(v[i], l[i], lv[2][i], 0.f);
+              float t3 = 0.f;
+#pragma unroll
+              for (int L = 3; L < kDig; ++L)
+                if (L < NL) t3 = __fadd_rn(t3, lv[L][i]);
+              l[i] = __fadd_rn(l[i], t3);
+            }
+          }
+          if (!live) continue;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int col = i0 + i;
+            if (col >= a) continue;
+            const int fi = fxw[col];
+            const int sh = (er - 126) + (fi - 126);
+            float4 v;
+            if (sh >= -126 && sh <= 127) {
+              const float f = pow2f(sh);
+              v = make_float4(vre[i] * f, lre[i] * f, vim[i] * f, lim[i] * f);
+            } else {
+              v = make_float4(scale2(vre[i], sh), scale2(lre[i], sh), scale2(vim[i], sh), scale2(lim[i], sh));
+            }
+            if (!first) {
+              const float4 p = row[col];
+              df_add(v.x, v.y, p.x, p.y);
+              df_add(v.z, v.w, p.z, p.w);
+            }
+            df_norm(v.x, v.y);
+            df_norm(v.z, v.w);
+            if (er == 255 || fi == 255) {  // an Inf or NaN among the operands: propagate it
+              const float nan = __int_as_float(0x7fffffff);
+              v = make_float4(nan, nan, nan, nan);
+            }
+            row[col] = v;
+          }
+        }
+        fence_before_sync();
+        mbar_arrive(&sm.bar.tempty);
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 12) {
+    fence_after_sync();
+    tmem_dealloc(tmem, 512u);
+  }
+}
+
 int g_tc_sms = 0;
 
 cudaError_t tc_grid(int64_t n_tiles, unsigned* grid) {
@@ -679,7 +1077,28 @@ cudaError_t launch_tc(const MPTask* tasks, const int2* tiles, int64_t first_tile
   return cudaGetLastError();
 }
 
+cudaError_t launch_hp_tc_p(const HPTask* tasks, const HpTcGroup* groups, const int4* items, int64_t first_item,
+                           int64_t n_items, const int2* img_units, int64_t first_unit, int64_t n_units,
+                           double2* ws, int* status, cudaStream_t s) {
+  if (n_units > 0) k_hp_tc_img<<<(unsigned)n_units, 256, 0, s>>>(groups, img_units, first_unit);
+  unsigned grid = 0;
+  cudaError_t e = tc_grid(n_items, &grid);
+  if (e != cudaSuccess) return e;
+  const int smem = (int)sizeof(HpSmem);
+  e = cudaFuncSetAttribute(k_hp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k_hp_tc<<<grid, kThreadsTc, smem, s>>>(tasks, groups, items, first_item, n_items, ws, status);
+  return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_hp_tc(const HPTask* tasks, const HpTcGroup* groups, const int4* items, int64_t first_item,
+                         int64_t n_items, const int2* img_units, int64_t first_unit, int64_t n_units,
+                         double2* ws, int* status, cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  return launch_hp_tc_p(tasks, groups, items, first_item, n_items, img_units, first_unit, n_units, ws, status, s);
+}
 
 cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
                          const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s) {

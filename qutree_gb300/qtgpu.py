@@ -37,7 +37,7 @@ QT_PLAN_CDVR = 0x4000
 QT_MAT_RHO, QT_MAT_RHOINV, QT_MAT_HMAT, QT_MAT_HCON, QT_MAT_CDVR = 0, 1, 2, 3, 4
 QT_CDVR_ALIGNED_HOLE_GRIDS = 1
 ERRORS = {1: "QT_ERR_ARG", 2: "QT_ERR_SHAPE", 3: "QT_ERR_ALLOC", 4: "QT_ERR_CUDA",
-          5: "QT_ERR_STATE", 6: "QT_ERR_NUMERIC"}
+          5: "QT_ERR_STATE", 6: "QT_ERR_NUMERIC", 7: "QT_ERR_TIMEOUT"}
 
 _lib = None
 _P = np.ctypeslib.ndpointer

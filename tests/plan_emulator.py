@@ -99,8 +99,9 @@ class PlanView:
         self.tables = {}
         widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
                   20: 6, 22: 6, 23: 4, 24: 27, 25: 8, 26: 12, 27: 11, 28: 2, 29: 11, 33: 3, 34: 10,
-                  35: 8, 36: 2, 38: 14, 39: 5, 40: 2, 41: 4, 42: 2, 43: 2, 44: 5, 45: 3, 46: 4, 47: 3, 49: 3, 50: 2, 51: 2}
-        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 52)):
+                  35: 8, 36: 2, 38: 14, 39: 5, 40: 2, 41: 4, 42: 2, 43: 2, 44: 5, 45: 3, 46: 4, 47: 3, 49: 3, 50: 2, 51: 2,
+                  52: 16, 53: 4, 54: 2, 55: 4}
+        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 57)):
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -208,7 +209,10 @@ class PlanView:
                     ab, ao, bb, bo, sb, so, bef, a, aft = T[2][t]
                     A = view(ab, ao, bef * a * aft).reshape((bef, a, aft), order="F")
                     B = view(bb, bo, bef * a * aft).reshape((bef, a, aft), order="F")
-                    S = np.einsum("bic,bjc->ij", A.conj(), B)
+                    if self.tensor and self.prec == 1 and hp_tc_eligible(bef, a, aft):
+                        S = oz_hole_product(A, B)
+                    else:
+                        S = np.einsum("bic,bjc->ij", A.conj(), B)
                     view(sb, so, a * a)[:] = S.ravel(order="F")
                 elif kind == ST_ACC:
                     ob, oo, ap, aoff, rows, d, first, count, add = T[3][t]
@@ -473,6 +477,53 @@ def oz_mode_product(h, x):
     scale = np.exp2(Ex[:, None] + Fh[None, :])
     y = (re + 1j * im) * scale
     return np.moveaxis(y.reshape(bef, aft, -1), -1, 1)
+
+
+HP_CHUNK = 64
+
+
+def hp_tc_eligible(before, a, after):
+    """The hole products the planner puts on the tensor cores (qt_internal.h)."""
+    return 16 <= a <= 64 and before * after >= 2 * HP_CHUNK
+
+
+def oz_hole_product(A, B):
+    """S(i, j) = sum_k conj(A[b, i, c]) B[b, j, c], k = b + before c, with
+    the digit arithmetic of the tensor-core hole products: the reduction in
+    chunks of 64 k, every chunk with its own exponents per row of B (per j)
+    and of A (per i); complex products as Re = Br Ar + Bi Ai and
+    Im = Bi Ar - Br Ai; levels 0..2 exact, levels 3..6 in one float32 sum
+    (the fewest accumulators), each chunk scaled by 2^(E_j + F_i) and the
+    chunks summed."""
+    bef, a, aft = A.shape
+    XA = np.transpose(A, (2, 0, 1)).reshape(-1, a)  # row k = c * before + b
+    XB = np.transpose(B, (2, 0, 1)).reshape(-1, B.shape[1])
+    K = XA.shape[0]
+    S = np.zeros((B.shape[1], a), np.complex128)  # rows j, columns i
+    for k0 in range(0, K, HP_CHUNK):
+        Eb, br, bi = _oz_digits(XB[k0:k0 + HP_CHUNK].T)
+        Fa, ar, ai = _oz_digits(XA[k0:k0 + HP_CHUNK].T)
+        re = np.zeros((br.shape[1], ar.shape[1]))
+        im = np.zeros_like(re)
+        r3 = np.zeros_like(re)
+        i3 = np.zeros_like(re)
+        for L in range(OZ_DIGITS):
+            sr = np.zeros_like(re)
+            si = np.zeros_like(re)
+            for s in range(L + 1):
+                u = L - s
+                sr += br[s] @ ar[u].T + bi[s] @ ai[u].T
+                si += bi[s] @ ar[u].T - br[s] @ ai[u].T
+            if L < 3:
+                re += sr * 2.0 ** (-7 * (L + 2))
+                im += si * 2.0 ** (-7 * (L + 2))
+            else:
+                r3 += sr * 2.0 ** (-7 * (L - 3))
+                i3 += si * 2.0 ** (-7 * (L - 3))
+        re += r3.astype(np.float32).astype(np.float64) * 2.0 ** (-35)
+        im += i3.astype(np.float32).astype(np.float64) * 2.0 ** (-35)
+        S += (re + 1j * im) * np.exp2(Eb[:, None] + Fa[None, :])
+    return S.T
 
 
 def _mp(h, x, k):
