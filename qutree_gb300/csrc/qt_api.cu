@@ -524,6 +524,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     t.count = s.count;
     t.add = s.add;
     t.pad = 0;
+    t.tc_img = s.tc_img >= 0 ? (void*)((char*)c->buf[qt::B_OZ] + s.tc_img) : nullptr;
     acc.push_back(t);
   }
   std::vector<qt::AccTerm> acc_terms;
@@ -697,6 +698,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   put(blob, offs, hp_tc);
   put(blob, offs, P.hp_tc_items);
   put(blob, offs, P.hp_tc_imgs);
+  put(blob, offs, P.acc_tc_items);
+  put(blob, offs, P.acc_tc_imgs);
   {
     cudaError_t e = dev_malloc(&c->tables_mem, std::max<size_t>(blob.size(), 256));
     if (e != cudaSuccess) {
@@ -751,6 +754,8 @@ int qt_prepare(qt_ctx* c, int flavour) {
   c->tables.hp_tc_groups = (qt::HpTcGroup*)(base + offs[34]);
   c->tables.hp_tc_items = (int4*)(base + offs[35]);
   c->tables.hp_tc_imgs = (int2*)(base + offs[36]);
+  c->tables.acc_tc_items = (int4*)(base + offs[37]);
+  c->tables.acc_tc_imgs = (int2*)(base + offs[38]);
   if (P.cdvr) {  // CDVR constants: seeded noise, leaf grids, identity
     QT_CUDA(c, cudaMemsetAsync(c->buf[qt::B_CDVR], 0, c->buf_elems[qt::B_CDVR] * 16, c->stream));
     for (auto& init : P.cdvr_init)
@@ -916,8 +921,10 @@ int64_t kernels_in(const qt::Plan& P, int64_t b0, int64_t b1) {
     const qt::Stage& st = P.stages[i];
     if (st.kind == qt::ST_HP)
       n += st.nseg + (st.nhti > 0 ? (st.nhtu > 0 ? 2 : 1) : 0) + (st.aux ? 1 : 0);
-    else if (st.kind == qt::ST_MP || st.kind == qt::ST_ACC)
+    else if (st.kind == qt::ST_MP)
       n += (st.n_tiles > 0 ? 1 : 0) + (st.noz > 0 ? (st.nozt > 0 ? 2 : 1) : 0);
+    else if (st.kind == qt::ST_ACC)
+      n += (st.n_tiles > 0 ? 1 : 0) + (st.nati > 0 ? (st.natu > 0 ? 2 : 1) : 0);
     else
       n += 1;
   }

@@ -84,7 +84,10 @@ struct AccTask {
   int rows, d;
   int first, count;
   int add, pad;
+  void* tc_img = nullptr;  // tensor-core path: images of alpha H_t, one per term (hp_tc_chunk_bytes)
 };
+// an accumulation the planner puts on the tensor cores (double-float plans)
+inline bool acc_tc_eligible(int rows, int d) { return d >= 16 && d <= 64 && rows >= 64; }
 
 // out = sum_t c_t * M_t for d x d matrices (grouped mean fields).
 struct LinTerm {
@@ -263,6 +266,9 @@ struct Stage {
   int64_t ozt0 = 0, nozt = 0;  // and its tensor-core tasks (mp_oz_tasks, digits of h)
   int64_t hti0 = 0, nhti = 0;  // hole-product stage: its tensor-core items (hp_tc_items)
   int64_t htu0 = 0, nhtu = 0;  // and the units of its image pre-pass (hp_tc_imgs)
+  int64_t ati0 = 0, nati = 0;  // accumulation stage: its tensor-core items (acc_tc_items)
+  int64_t atu0 = 0, natu = 0;  // and the units of its image pre-pass (acc_tc_imgs)
+  int64_t atc_units = 0;       // units (terms) of all its items
   double flops = 0;  // executed flops of the stage
   double bytes = 0;  // algorithmic bytes: operands read once, results written once
 };
@@ -369,6 +375,7 @@ struct Plan {
     bool alpha_param;
     double2 alpha;
     int rows, d, first, count, add;
+    int64_t tc_img = -1;  // tensor-core path: byte offset of the term images in B_OZ
   };
   struct SLinTerm {
     double2 c;
@@ -522,6 +529,8 @@ struct Plan {
   std::vector<SHpTcGroup> hp_tc_groups;
   std::vector<int4> hp_tc_items;  // (group, z, first chunk, end chunk)
   std::vector<int2> hp_tc_imgs;   // (group, chunk) of the image pre-pass
+  std::vector<int4> acc_tc_items;  // (task, 128-row block, units before the item in its stage, 0)
+  std::vector<int2> acc_tc_imgs;   // (task, term) of the image pre-pass
   std::vector<int4> acc_tiles;
   std::vector<int2> cvt_tiles;
   // constant matrices written once at prepare: (offset, d) identity
@@ -590,6 +599,8 @@ struct DevTables {
   HpTcGroup* hp_tc_groups = nullptr;
   int4* hp_tc_items = nullptr;
   int2* hp_tc_imgs = nullptr;
+  int4* acc_tc_items = nullptr;
+  int2* acc_tc_imgs = nullptr;
   TCTask* tc = nullptr;
   int4* tc_tiles = nullptr;
   GSTask* gs = nullptr;
@@ -676,6 +687,12 @@ inline int64_t mp_oz_h_bytes() { return kMpOzImageBytes; }
 cudaError_t launch_hp_tc(const HPTask* tasks, const HpTcGroup* groups, const int4* items, int64_t first_item,
                          int64_t n_items, const int2* img_units, int64_t first_unit, int64_t n_units,
                          double2* ws, int* status, cudaStream_t s);
+// accumulations on the tensor cores: items (task, 128-row block, units
+// before the item in the stage, 0), one unit per term; image units (task,
+// term) of the pre-pass that writes alpha H_t
+cudaError_t launch_acc_tc(const AccTask* tasks, const AccTerm* terms, const int4* items, int64_t first_item,
+                          int64_t n_items, int64_t units, const int2* img_units, int64_t first_unit,
+                          int64_t n_units, int* status, cudaStream_t s);
 // weighted simultaneous diagonalisation, one warp per task (qt_wsd.cu)
 // max_n / max_d bound the tasks' matrix counts and orders (shared memory)
 cudaError_t launch_wsd(const WSDTask* tasks, const WSDTerm* terms, int64_t first, int64_t n, int max_n,

@@ -1593,6 +1593,12 @@ cudaError_t launch_stage_p(const Stage& st, const DevTables& t, double eps, int 
     case ST_ACC:
       if (st.n_tiles > 0)
         k_acc<P><<<(unsigned)st.n_tiles, kThreads, 0, s>>>(t.acc, t.acc_terms, t.acc_tiles, st.first_tile);
+      if (st.nati > 0) {
+        if (!std::is_same<P, DF64>::value) return cudaErrorInvalidValue;  // the planner emits none
+        cudaError_t e = launch_acc_tc(t.acc, t.acc_terms, t.acc_tc_items, st.ati0, st.nati, st.atc_units,
+                                      t.acc_tc_imgs, st.atu0, st.natu, t.status, s);
+        if (e != cudaSuccess) return e;
+      }
       break;
     case ST_LIN:
       k_lin<P><<<(unsigned)st.n_tasks, kThreads, 0, s>>>(t.lin, t.lin_terms, st.first_task);

@@ -576,6 +576,35 @@ class Builder {
     return split;
   }
 
+  // Tensor-core accumulations of a stage [t0, t1): the qualifying tasks get
+  // one item per block of 128 rows (the task's terms in order, one unit
+  // each) and an image slot per term in the stage's part of B_OZ; their
+  // classic tiles are dropped from [tile0, tile1).  Returns the new end of
+  // the classic tiles; units = the units of all items.
+  int64_t acc_tensor_items(int64_t t0, int64_t t1, int64_t tile0, int64_t tile1, int64_t& units) {
+    std::vector<char> tc(t1 - t0, 0);
+    units = 0;
+    for (int64_t t = t0; t < t1; ++t) {
+      Plan::SAcc& a = P.acc[t];
+      if (a.count < 1 || !acc_tc_eligible(a.rows, a.d)) continue;
+      tc[t - t0] = 1;
+      a.tc_img = stage_oz_;
+      stage_oz_ += (int64_t)a.count * hp_tc_chunk_bytes((a.d + 7) & ~7);
+      for (int s = 0; s < a.count; ++s) P.acc_tc_imgs.push_back(make_int2((int)t, s));
+      for (int64_t b = 0; b * 128 < a.rows; ++b) {
+        P.acc_tc_items.push_back(make_int4((int)t, (int)b, (int)units, 0));
+        units += a.count;
+      }
+    }
+    int64_t w = tile0;
+    for (int64_t i = tile0; i < tile1; ++i) {
+      const int4 tl = P.acc_tiles[i];
+      if (tl.x >= t0 && tl.x < t1 && tc[tl.x - t0]) continue;
+      P.acc_tiles[w++] = tl;
+    }
+    return w;
+  }
+
   void emit_stage(int kind, int64_t t0, int64_t t1, int64_t tile0, int64_t tile1,
                   const char* name) {
     if (t1 <= t0) return;
@@ -587,6 +616,9 @@ class Builder {
     const int64_t oz0 = (int64_t)P.mp_oz_tiles.size();
     const int64_t ozt0 = (int64_t)P.mp_oz_tasks.size();
     if (kind == ST_MP && P.mp_tensor) tile1 = mp_tensor_tiles(t0, t1, tile0, tile1);
+    const int64_t ati0 = (int64_t)P.acc_tc_items.size(), atu0 = (int64_t)P.acc_tc_imgs.size();
+    int64_t atc_units = 0;
+    if (kind == ST_ACC && P.hp_tensor) tile1 = acc_tensor_items(t0, t1, tile0, tile1, atc_units);
     P.oz_bytes = std::max(P.oz_bytes, stage_oz_);
     const double f1 = P.stats.exec_flops;
     Stage s;
@@ -610,6 +642,11 @@ class Builder {
     s.nhti = (int64_t)P.hp_tc_items.size() - hti0;
     s.htu0 = htu0;
     s.nhtu = (int64_t)P.hp_tc_imgs.size() - htu0;
+    s.ati0 = ati0;
+    s.nati = (int64_t)P.acc_tc_items.size() - ati0;
+    s.atu0 = atu0;
+    s.natu = (int64_t)P.acc_tc_imgs.size() - atu0;
+    s.atc_units = atc_units;
     P.stages.push_back(s);
   }
 

@@ -546,6 +546,32 @@ static void table(const qt::Plan& P, int what, std::vector<int64_t>& v, std::vec
     case 56:  // B_OZ bytes
       v.push_back(P.oz_bytes);
       break;
+    case 57:  // tensor-core accumulation items: (task, 128-row block, units before the item, 0)
+      for (auto& t : P.acc_tc_items) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+        v.push_back(t.z);
+        v.push_back(t.w);
+      }
+      break;
+    case 58:  // image pre-pass units of the accumulations: (task, term)
+      for (auto& t : P.acc_tc_imgs) {
+        v.push_back(t.x);
+        v.push_back(t.y);
+      }
+      break;
+    case 59:  // per stage: accumulation items and image units (first, count, first, count, units)
+      for (auto& st : P.stages) {
+        v.push_back(st.ati0);
+        v.push_back(st.nati);
+        v.push_back(st.atu0);
+        v.push_back(st.natu);
+        v.push_back(st.atc_units);
+      }
+      break;
+    case 60:  // accumulation tasks: byte offset of the term images in B_OZ (-1: classic)
+      for (auto& t : P.acc) v.push_back(t.tc_img);
+      break;
     default:
       break;
   }

@@ -653,41 +653,62 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
 }
 
 // ---------------------------------------------------------------------------
-// Hole products on the tensor cores (double-float plans).
-//
-// S_t(i, j) = sum_k conj(A[k; i]) B_t[k; j] for the tasks t of a group that
-// share A.  The accumulator tile has one row per (task, j) of the group --
-// the M side, B_t's digits cut by the producers -- and 2 ap columns: the real
-// parts for i < ap, the imaginary parts after them.  With A = Ar + i Ai and
-// B = Br + i Bi,
-//   Re = Br Ar + Bi Ai,   Im = Bi Ar - Br Ai,
-// i.e. two MMAs of N = 2 ap per digit pair: Br x [Ar | -Ai] and
-// Bi x [Ai | Ar].  The N side stores rows [Ai | Ar | -Ai] once; the two
-// operands are its rows ap.. and 0.. .  A's digits come from a pre-pass (one
-// image per 64-k chunk, with the chunk's column exponents); the reduction
-// runs chunk by chunk, every chunk with its own row and column scales, its
-// level sums exact in fp32 (at most 7 pairs x 2 x 64 products of |digit
-// products| <= 2^14 units per level), recombined in double-float by the
-// epilogue and added to the task's output (or to its partial tile for the
-// item's range of chunks; the sweep's partial-tile sum adds the ranges).
+// Sums of products on the tensor cores (double-float plans): the hole
+// products and the last-index accumulations.  Both compute, per output row
+// m and column n,
+//   D(m, n) = sum over units u of  sum_k X_u(m, k) W_u(n, k)     (complex)
+// in units of at most 64 k, every unit with its own power-of-two scales per
+// row of X_u (E_m) and per row of W_u (F_n):
+//  * hole products S_t(i, j) = sum_k conj(A[k; i]) B_t[k; j]: the rows m are
+//    the (task t, j) of a group of tasks that share A (X = B_t), n = i and
+//    W = conj(A); the units are the 64-k chunks of the reduction;
+//  * accumulations out[r, j] (+)= alpha sum_t sum_j' H_t(j, j') X_t[r, j']:
+//    rows m = r (a block of 128), n = j, one unit per term t with X = X_t
+//    and W = alpha H_t (alpha I for identity terms).
+// The accumulator tile has 2 np columns, the real parts for n < np and the
+// imaginary parts after them, so
+//   Re D = Xr Wr - Xi Wi,   Im D = Xr Wi + Xi Wr
+// are two MMAs of N = 2 np per digit pair: Xr x [Wr | Wi] and
+// Xi x [-Wi | Wr].  W's image, written by a pre-pass per unit, stores the
+// rows [-Wi | Wr | Wi] (np each) once per 16-k step and digit; the two
+// operands are its rows np.. and 0.. .  The producers cut X's digits; the
+// image steps arrive by bulk copies on the same barrier.  A unit's level
+// sums are exact in fp32 (at most 7 pairs x 2 x 64 products of |digit
+// products| <= 2^14 units per level); the epilogue recombines them in
+// double-float, scales by 2^(E_m + F_n) and adds them to the output in
+// double-float (a work item's first unit stores, or adds to the old output
+// where the accumulation asks for it).
 // ---------------------------------------------------------------------------
-constexpr int kHpNStage = kDig * 3 * 64 * 32;  // N side of one 16-k step at ap = 64
+constexpr int kTcsNStage = kDig * 3 * 64 * 32;  // W side of one 16-k step at np = 64
+enum { TCS_HP = 0, TCS_ACC = 1 };
 
-struct HpSmem {
+struct TcsSmem {
   unsigned char a[2][kOzAStage];
-  unsigned char n[2][kHpNStage];
+  unsigned char n[2][kTcsNStage];
   Bars bar;
   uint8_t ex[2][kRows];
   uint8_t pm[2][2][kRows];
   int fx[4][64];
 };
-static_assert(sizeof(HpSmem) <= 232448, "shared memory of the hole-product kernel exceeds 227 KB");
+static_assert(sizeof(TcsSmem) <= 232448, "shared memory of the sum-of-products kernel exceeds 227 KB");
+
+struct TcsArgs {
+  const HPTask* hp;          // hole products: tasks, groups, partial tiles
+  const HpTcGroup* groups;
+  double2* ws;
+  const AccTask* acc;        // accumulations: tasks and terms
+  const AccTerm* terms;
+  const int4* items;         // HP (group, range z, first chunk, end chunk); ACC (task, block, units before, 0)
+  int64_t item0, n_items;
+  int64_t units;             // ACC: units of all items (weighted split over the CTAs)
+  int* status;
+};
 
 // element k of row `row` of a hole-product operand of shape (before, a, after):
 // k = b + before c, offset b + before row + before a c; walked in steps of one
 struct KWalk {
   int b, c;
-  __device__ __forceinline__ KWalk(int k, int before) : c(k / before), b(k - (k / before) * before) {}
+  __device__ __forceinline__ KWalk(int k, int before) : b(k - (k / before) * before), c(k / before) {}
   __device__ __forceinline__ int64_t off(int row, int before, int a) const {
     return b + (int64_t)before * row + (int64_t)before * a * c;
   }
@@ -699,50 +720,130 @@ struct KWalk {
   }
 };
 
-// pre-pass: the digits of A for one chunk of 64 k of a group -- per 16-k
-// step and digit a plane of 3 ap rows: Ai at row i, Ar at ap + i, -Ai at
-// 2 ap + i (rows a..ap of each block zero) -- and the chunk's column
-// exponents.  Thread (i, ks) takes row i of the 16-k step ks.
-__global__ void __launch_bounds__(256) k_hp_tc_img(const HpTcGroup* __restrict__ groups,
-                                                   const int2* __restrict__ units, int64_t first) {
+// the CTA's run of items: equal counts (HP: items of about equal length), or
+// the items whose first unit falls into the CTA's equal share of all units
+template <int OP>
+__device__ __forceinline__ void tcs_range(const TcsArgs& g, int64_t& i0, int64_t& i1) {
+  if (OP == TCS_HP) {
+    const int64_t per = g.n_items / gridDim.x, extra = g.n_items % gridDim.x;
+    i0 = blockIdx.x * per + min((int64_t)blockIdx.x, extra);
+    i1 = i0 + per + (blockIdx.x < extra ? 1 : 0);
+    return;
+  }
+  auto first_at = [&](int64_t u) {  // first item with units-before >= u
+    int64_t lo = 0, hi = g.n_items;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)g.items[g.item0 + mid].z < u) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo;
+  };
+  i0 = first_at(g.units * blockIdx.x / gridDim.x);
+  i1 = first_at(g.units * (blockIdx.x + 1) / gridDim.x);
+}
+
+// per item: padded columns np, real columns, units, 16-k steps per unit
+struct TcsItem {
+  int np, ncols, nunits, nks;
+};
+template <int OP>
+__device__ __forceinline__ TcsItem tcs_item(const TcsArgs& g, int4 itm) {
+  TcsItem v;
+  if (OP == TCS_HP) {
+    const HpTcGroup& G = g.groups[itm.x];
+    v.np = G.ap;
+    v.ncols = G.a;
+    v.nunits = itm.w - itm.z;
+    v.nks = kHpTcChunk / kChunkK;
+  } else {
+    const AccTask& T = g.acc[itm.x];
+    v.np = (T.d + 7) & ~7;
+    v.ncols = T.d;
+    v.nunits = T.count;
+    v.nks = (T.d + kChunkK - 1) / kChunkK;
+  }
+  return v;
+}
+template <int OP>
+__device__ __forceinline__ const unsigned char* tcs_image(const TcsArgs& g, int4 itm, int u, int np) {
+  if (OP == TCS_HP) return g.groups[itm.x].img + (size_t)(itm.z + u) * hp_tc_chunk_bytes(np);
+  return static_cast<const unsigned char*>(g.acc[itm.x].tc_img) + (size_t)u * hp_tc_chunk_bytes(np);
+}
+
+// pre-pass: the image of W for one unit -- per 16-k step and digit a plane of
+// 3 np rows, -Wi at row n, Wr at np + n, Wi at 2 np + n (rows past the last
+// column zero) -- and the unit's row exponents F_n.  Thread (n, ks) takes
+// row n of the 16-k step ks.  HP units (group, chunk): W(i, k) = conj(A[k; i]);
+// ACC units (task, term): W(j, k) = alpha H(j, k), alpha I for identity terms.
+template <int OP>
+__global__ void __launch_bounds__(256) k_tcs_img(TcsArgs g, const int2* __restrict__ units, int64_t first) {
   const int2 u = units[first + blockIdx.x];
-  const HpTcGroup G = groups[u.x];
-  const int c = u.y, ap = G.ap, a = G.a, before = G.before;
-  const int K = before * G.after;
-  unsigned char* img = G.img + (size_t)c * hp_tc_chunk_bytes(ap);
-  const float4* __restrict__ A = reinterpret_cast<const float4*>(G.A);
-  __shared__ int fx[64];
-  const int i = threadIdx.x & 63, ks = threadIdx.x >> 6;
-  if (threadIdx.x < 64) fx[threadIdx.x] = 1;
-  __syncthreads();
+  const int n = threadIdx.x & 63, ks = threadIdx.x >> 6;
+  int np, ncols;
+  unsigned char* img;
   float4 v[16];
-  const int k0 = c * kHpTcChunk + ks * kChunkK;
-  int m = 1;
-  {
-    KWalk w(min(k0, K), before);
+  if (OP == TCS_HP) {
+    const HpTcGroup G = g.groups[u.x];
+    np = G.ap;
+    ncols = G.a;
+    const int K = G.before * G.after, k0 = u.y * kHpTcChunk + ks * kChunkK;
+    img = G.img + (size_t)u.y * hp_tc_chunk_bytes(np);
+    const float4* __restrict__ A = reinterpret_cast<const float4*>(G.A);
+    KWalk w(min(k0, K), G.before);
 #pragma unroll
     for (int kk = 0; kk < 16; ++kk) {
-      v[kk] = (i < a && k0 + kk < K) ? __ldg(A + w.off(i, before, a)) : make_float4(0.f, 0.f, 0.f, 0.f);
-      w.next(before);
-      m = max(m, max(fexp(v[kk].x), fexp(v[kk].z)));
+      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (n < ncols && k0 + kk < K) {
+        x = __ldg(A + w.off(n, G.before, G.a));
+        x.z = -x.z;
+        x.w = -x.w;
+      }
+      v[kk] = x;
+      w.next(G.before);
+    }
+  } else {
+    const AccTask T = g.acc[u.x];
+    const AccTerm tm = g.terms[T.first + u.y];
+    np = (T.d + 7) & ~7;
+    ncols = T.d;
+    img = static_cast<unsigned char*>(T.tc_img) + (size_t)u.y * hp_tc_chunk_bytes(np);
+    const double2 alpha = T.alpha_ptr ? *T.alpha_ptr : T.alpha;
+    const float4 cf = DF64::coef(alpha);
+    const float4* __restrict__ H = reinterpret_cast<const float4*>(tm.H);
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      const int k = ks * kChunkK + kk;
+      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (n < ncols && k < ncols) {
+        if (H) x = DF64::mul(cf, __ldg(H + n + (int64_t)ncols * k));
+        else if (n == k) x = cf;
+      }
+      v[kk] = x;
     }
   }
-  atomicMax(&fx[i], m);
+  __shared__ int fx[64];
+  if (threadIdx.x < 64) fx[threadIdx.x] = 1;
   __syncthreads();
-  if (i < ap) {
-    const int f = fx[i];
-    const int rows = 3 * ap, plane = rows * 32;
+  int m = 1;
+#pragma unroll
+  for (int kk = 0; kk < 16; ++kk) m = max(m, max(fexp(v[kk].x), fexp(v[kk].z)));
+  atomicMax(&fx[n], m);
+  __syncthreads();
+  if (n < np) {
+    const int f = fx[n];
+    const int rows = 3 * np, plane = rows * 32;
     unsigned char* base = img + (size_t)ks * kDig * plane;
 #pragma unroll
-    for (int g = 0; g < 2; ++g) {  // the two 8-k core rows of the step
+    for (int c = 0; c < 2; ++c) {  // the two 8-k core rows of the step
       uint32_t wr[kDig][4], wi[kDig][4];
 #pragma unroll
       for (int p = 0; p < 4; ++p) {
         float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
-        digits_f32(v[8 * g + 2 * p].x, v[8 * g + 2 * p].y, f, d0);
-        digits_f32(v[8 * g + 2 * p + 1].x, v[8 * g + 2 * p + 1].y, f, d1);
-        digits_f32(v[8 * g + 2 * p].z, v[8 * g + 2 * p].w, f, e0);
-        digits_f32(v[8 * g + 2 * p + 1].z, v[8 * g + 2 * p + 1].w, f, e1);
+        digits_f32(v[8 * c + 2 * p].x, v[8 * c + 2 * p].y, f, d0);
+        digits_f32(v[8 * c + 2 * p + 1].x, v[8 * c + 2 * p + 1].y, f, d1);
+        digits_f32(v[8 * c + 2 * p].z, v[8 * c + 2 * p].w, f, e0);
+        digits_f32(v[8 * c + 2 * p + 1].z, v[8 * c + 2 * p + 1].w, f, e1);
 #pragma unroll
         for (int d = 0; d < kDig; ++d) {
           wr[d][p] = pack_bf16(d0[d], d1[d]);
@@ -755,25 +856,31 @@ __global__ void __launch_bounds__(256) k_hp_tc_img(const HpTcGroup* __restrict__
         const uint4 re = make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
         const uint4 im = make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
         const uint4 nim = make_uint4(im.x ^ 0x80008000u, im.y ^ 0x80008000u, im.z ^ 0x80008000u, im.w ^ 0x80008000u);
-        *reinterpret_cast<uint4*>(pl + core_off(i, g, rows)) = im;
-        *reinterpret_cast<uint4*>(pl + core_off(ap + i, g, rows)) = re;
-        *reinterpret_cast<uint4*>(pl + core_off(2 * ap + i, g, rows)) = nim;
+        *reinterpret_cast<uint4*>(pl + core_off(n, c, rows)) = nim;
+        *reinterpret_cast<uint4*>(pl + core_off(np + n, c, rows)) = re;
+        *reinterpret_cast<uint4*>(pl + core_off(2 * np + n, c, rows)) = im;
       }
     }
   }
-  if (threadIdx.x < 64) reinterpret_cast<int*>(img + (size_t)4 * kDig * 3 * ap * 32)[threadIdx.x] = fx[threadIdx.x];
+  if (threadIdx.x < 64) reinterpret_cast<int*>(img + (size_t)4 * kDig * 3 * np * 32)[threadIdx.x] = fx[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restrict__ tasks,
-                                                          const HpTcGroup* __restrict__ groups,
-                                                          const int4* __restrict__ items, int64_t item0,
-                                                          int64_t n_items, double2* __restrict__ ws, int* status) {
-  extern __shared__ __align__(128) unsigned char hp_raw[];
-  HpSmem& sm = *reinterpret_cast<HpSmem*>(hp_raw);
+// the producers' view of row r of an item: its source of X and validity
+struct TcsRow {
+  bool valid;
+  const float4* src;  // HP: B_t; ACC: unused (the term's X)
+  int64_t rg;         // ACC: row of the task
+  int j;              // HP: column of S_t
+};
+
+template <int OP>
+__global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
+  extern __shared__ __align__(128) unsigned char tcs_raw[];
+  TcsSmem& sm = *reinterpret_cast<TcsSmem*>(tcs_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int64_t per = n_items / gridDim.x, extra = n_items % gridDim.x;
-  const int64_t my0 = blockIdx.x * per + min((int64_t)blockIdx.x, extra);
-  const int64_t my1 = my0 + per + (blockIdx.x < extra ? 1 : 0);
+  int64_t my0, my1;
+  tcs_range<OP>(g, my0, my1);
+  int* status = g.status;
 
   if (tid == 0) {
     for (int s = 0; s < 2; ++s) {
@@ -800,31 +907,58 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
     const int r = tid & (kRows - 1), h = tid >> 7;
     uint32_t q = 0, un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it) {
-      const int4 itm = items[item0 + it];
-      const HpTcGroup& G = groups[itm.x];
-      const int before = G.before, a = G.a, ap = G.ap;
-      const int K = before * G.after;
-      const int mi = r / a, j = r - mi * a;
-      const bool valid = mi < G.n;
-      const float4* __restrict__ B = valid ? reinterpret_cast<const float4*>(tasks[G.member[mi]].B) : nullptr;
-      const uint32_t nbytes = (uint32_t)(kDig * 3 * ap * 32);
-      const unsigned char* img = G.img;
-      for (int c = itm.z; c < itm.w; ++c, ++un) {
+      const int4 itm = g.items[g.item0 + it];
+      const TcsItem I = tcs_item<OP>(g, itm);
+      const uint32_t nbytes = (uint32_t)(kDig * 3 * I.np * 32);
+      // row r of the item
+      TcsRow R;
+      int before = 1, a = 1, K = 0;
+      int64_t rows = 0;
+      int tfirst = 0;
+      if (OP == TCS_HP) {
+        const HpTcGroup& G = g.groups[itm.x];
+        before = G.before;
+        a = G.a;
+        K = before * G.after;
+        const int mi = r / a;
+        R.j = r - mi * a;
+        R.valid = mi < G.n;
+        R.src = R.valid ? reinterpret_cast<const float4*>(g.hp[G.member[mi]].B) : nullptr;
+        R.rg = 0;
+      } else {
+        const AccTask& T = g.acc[itm.x];
+        rows = T.rows;
+        K = T.d;
+        tfirst = T.first;
+        R.rg = (int64_t)itm.y * kRows + r;
+        R.valid = R.rg < rows;
+        R.src = nullptr;
+        R.j = 0;
+      }
+      for (int u = 0; u < I.nunits; ++u, ++un) {
         const int buf = (int)(un & 1);
         const uint32_t use_par = (un >> 1) & 1;
-        // this thread's 32 values of the chunk: k = 64 c + 16 ks + 8 h + i
+        const float4* X = OP == TCS_HP ? R.src : reinterpret_cast<const float4*>(g.terms[tfirst + u].X);
+        const int kbase = OP == TCS_HP ? (itm.z + u) * kHpTcChunk : 0;
+        // this thread's values of step ks: k = kbase + 16 ks + 8 h + i
         auto load8 = [&](float4 (&x)[8], int ks) {
-          const int k0 = c * kHpTcChunk + ks * kChunkK + h * 8;
-          KWalk w(min(k0, K), before);
+          const int k0 = kbase + ks * kChunkK + h * 8;
+          if (OP == TCS_HP) {
+            KWalk w(min(k0, K), before);
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            x[i] = (valid && k0 + i < K) ? __ldg(B + w.off(j, before, a)) : make_float4(0.f, 0.f, 0.f, 0.f);
-            w.next(before);
+            for (int i = 0; i < 8; ++i) {
+              x[i] = (R.valid && k0 + i < K) ? __ldg(X + w.off(R.j, before, a)) : make_float4(0.f, 0.f, 0.f, 0.f);
+              w.next(before);
+            }
+          } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+              x[i] = (R.valid && k0 + i < K) ? __ldg(X + R.rg + rows * (k0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         };
         int m = 1;
-        if (valid)
-          for (int ks = 0; ks < 4; ++ks) {
+        if (R.valid)
+          for (int ks = 0; ks < I.nks; ++ks) {
             float4 x[8];
             load8(x, ks);
 #pragma unroll
@@ -847,25 +981,25 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
           sm.ex[buf][r] = (uint8_t)eb;
           mbar_arrive(&sm.bar.exready[buf]);
         }
+        const unsigned char* img = tcs_image<OP>(g, itm, u, I.np);
         float4 nx[8];
         load8(nx, 0);
-        for (int ks = 0; ks < 4; ++ks, ++q) {
+        for (int ks = 0; ks < I.nks; ++ks, ++q) {
           const int s = q & 1;
           float4 x[8];
 #pragma unroll
           for (int i = 0; i < 8; ++i) x[i] = nx[i];
-          if (ks + 1 < 4) load8(nx, ks + 1);
+          if (ks + 1 < I.nks) load8(nx, ks + 1);
           if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
             set_status(status, 11);
             ok = false;
             break;
           }
           if (tid == 0) {
-            // A's digits of this step; the copy completes on full[s] (it
+            // W's digits of this step; the copy completes on full[s] (it
             // finishes within microseconds, before any wait could run out)
             mbar_expect_tx(&sm.bar.full[s], nbytes);
-            bulk_g2s(sm.n[s], img + (size_t)c * hp_tc_chunk_bytes(ap) + (size_t)ks * nbytes, nbytes,
-                     &sm.bar.full[s]);
+            bulk_g2s(sm.n[s], img + (size_t)ks * nbytes, nbytes, &sm.bar.full[s]);
           }
           unsigned char* As = sm.a[s];
           uint32_t wr[kDig][4], wi[kDig][4];
@@ -901,22 +1035,21 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
     if (lane == 0) {
       uint32_t q = 0, un = 0;
       for (int64_t it = my0; it < my1 && ok; ++it) {
-        const int4 itm = items[item0 + it];
-        const int ap = groups[itm.x].ap;
-        const int NL = levels_for(ap);
-        const uint32_t id = idesc_m128(1, 2 * ap, false);
-        const uint32_t lboA = (kRows / 8) * 128, lboN = (uint32_t)(3 * ap / 8) * 128;
-        const uint64_t pA = kOzAPlane >> 4, pN = (uint64_t)((3 * ap * 32) >> 4);
-        const uint64_t p1 = (uint64_t)((ap / 8) * 128 >> 4);  // rows ap..: [Ar | -Ai]
-        for (int c = itm.z; c < itm.w && ok; ++c, ++un) {
-          const uint32_t tpar = un & 1;
-          if (!mbar_wait(&sm.bar.tempty, tpar ^ 1, kSpin)) {
+        const int4 itm = g.items[g.item0 + it];
+        const TcsItem I = tcs_item<OP>(g, itm);
+        const int np = I.np, NL = levels_for(np);
+        const uint32_t id = idesc_m128(1, 2 * np, false);
+        const uint32_t lboA = (kRows / 8) * 128, lboN = (uint32_t)(3 * np / 8) * 128;
+        const uint64_t pA = kOzAPlane >> 4, pN = (uint64_t)((3 * np * 32) >> 4);
+        const uint64_t p1 = (uint64_t)((np / 8) * 128 >> 4);  // rows np..: [Wr | Wi]
+        for (int u = 0; u < I.nunits && ok; ++u, ++un) {
+          if (!mbar_wait(&sm.bar.tempty, (un & 1) ^ 1, kSpin)) {
             set_status(status, 14);
             ok = false;
             break;
           }
           fence_after_sync();
-          for (int ks = 0; ks < 4; ++ks, ++q) {
+          for (int ks = 0; ks < I.nks; ++ks, ++q) {
             const int s = q & 1;
             if (!mbar_wait(&sm.bar.full[s], (q >> 1) & 1, kSpin)) {
               set_status(status, 15);
@@ -934,10 +1067,10 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
               for (int td = 0; td + sd < kDig; ++td) {
                 const int L = sd + td < NL - 1 ? sd + td : NL - 1;
                 const uint64_t nb = dN + (uint64_t)td * pN;
-                const uint32_t d = tmem + (uint32_t)(L * 2 * ap);
+                const uint32_t d = tmem + (uint32_t)(L * 2 * np);
                 const uint32_t acc = (first && sd == 0 && td == L) ? 0u : 1u;
-                mma_bf16(d, ar, nb + p1, id, acc);  // Br x [Ar | -Ai]
-                mma_bf16(d, ai, nb, id, 1);         // Bi x [Ai | Ar]
+                mma_bf16(d, ar, nb + p1, id, acc);  // Xr x [Wr | Wi]
+                mma_bf16(d, ai, nb, id, 1);         // Xi x [-Wi | Wr]
               }
             }
             commit(&sm.bar.empty[s]);
@@ -957,18 +1090,29 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
     int* fxw = sm.fx[qd];
     uint32_t un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it) {
-      const int4 itm = items[item0 + it];
-      const HpTcGroup& G = groups[itm.x];
-      const int a = G.a, ap = G.ap, NL = levels_for(ap);
-      const int mi = r / a, j = r - mi * a;
-      const bool live = mi < G.n;
-      float4* row = nullptr;
-      if (live) {
-        const HPTask& t = tasks[G.member[mi]];
-        double2* dst = t.splits <= 1 ? t.S : ws + t.ws + (int64_t)itm.y * a * a;
-        row = reinterpret_cast<float4*>(dst) + (int64_t)a * j;
+      const int4 itm = g.items[g.item0 + it];
+      const TcsItem I = tcs_item<OP>(g, itm);
+      const int np = I.np, NL = levels_for(np);
+      // output row r: element n at base[n * stride]
+      float4* base = nullptr;
+      int64_t stride = 1;
+      bool add_first = false;
+      if (OP == TCS_HP) {
+        const HpTcGroup& G = g.groups[itm.x];
+        const int mi = r / G.a, j = r - mi * G.a;
+        if (mi < G.n) {
+          const HPTask& t = g.hp[G.member[mi]];
+          double2* dst = t.splits <= 1 ? t.S : g.ws + t.ws + (int64_t)itm.y * G.a * G.a;
+          base = reinterpret_cast<float4*>(dst) + (int64_t)G.a * j;
+        }
+      } else {
+        const AccTask& T = g.acc[itm.x];
+        const int64_t rg = (int64_t)itm.y * kRows + r;
+        if (rg < T.rows) base = reinterpret_cast<float4*>(T.out) + rg;
+        stride = T.rows;
+        add_first = T.add != 0;
       }
-      for (int c = itm.z; c < itm.w; ++c, ++un) {
+      for (int u = 0; u < I.nunits; ++u, ++un) {
         const int buf = (int)(un & 1);
         if (!mbar_wait(&sm.bar.exready[buf], (un >> 1) & 1, kSpin) || !mbar_wait(&sm.bar.tfull, un & 1, kSpin)) {
           set_status(status, 17);
@@ -978,13 +1122,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
         fence_after_sync();
         const int er = (int)sm.ex[buf][r];
         mbar_arrive(&sm.bar.exfree[buf]);
-        const int* fxg = reinterpret_cast<const int*>(G.img + (size_t)c * hp_tc_chunk_bytes(ap) +
-                                                      (size_t)4 * kDig * 3 * ap * 32);
+        const int* fxg =
+            reinterpret_cast<const int*>(tcs_image<OP>(g, itm, u, np) + (size_t)4 * kDig * 3 * np * 32);
         __syncwarp();
         for (int i = lane; i < 64; i += 32) fxw[i] = __ldg(fxg + i);
         __syncwarp();
-        const bool first = c == itm.z;
-        for (int i0 = 0; i0 < ap; i0 += 8) {
+        const bool store = u == 0 && !add_first;
+        for (int n0 = 0; n0 < np; n0 += 8) {
           __syncwarp();
           float vre[8], vim[8], lre[8], lim[8];
           float lv[kDig][8];
@@ -992,7 +1136,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
           for (int part = 0; part < 2; ++part) {
 #pragma unroll
             for (int L = 0; L < kDig; ++L)
-              if (L < NL) tmem_ld8(lane_addr + (uint32_t)(L * 2 * ap + part * ap + i0), lv[L]);
+              if (L < NL) tmem_ld8(lane_addr + (uint32_t)(L * 2 * np + part * np + n0), lv[L]);
             tmem_wait_ld();
             float* v = part ? vim : vre;
             float* l = part ? lim : lre;
@@ -1009,13 +1153,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
               l[i] = __fadd_rn(l[i], t3);
             }
           }
-          if (!live) continue;
+          if (!base) continue;
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
-            const int col = i0 + i;
-            if (col >= a) continue;
-            const int fi = fxw[col];
-            const int sh = (er - 126) + (fi - 126);
+            const int col = n0 + i;
+            if (col >= I.ncols) continue;
+            const int fn = fxw[col];
+            const int sh = (er - 126) + (fn - 126);
             float4 v;
             if (sh >= -126 && sh <= 127) {
               const float f = pow2f(sh);
@@ -1023,18 +1167,19 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_hp_tc(const HPTask* __restric
             } else {
               v = make_float4(scale2(vre[i], sh), scale2(lre[i], sh), scale2(vim[i], sh), scale2(lim[i], sh));
             }
-            if (!first) {
-              const float4 p = row[col];
+            float4* o = base + stride * col;
+            if (!store) {
+              const float4 p = *o;
               df_add(v.x, v.y, p.x, p.y);
               df_add(v.z, v.w, p.z, p.w);
             }
             df_norm(v.x, v.y);
             df_norm(v.z, v.w);
-            if (er == 255 || fi == 255) {  // an Inf or NaN among the operands: propagate it
+            if (er == 255 || fn == 255) {  // an Inf or NaN among the operands: propagate it
               const float nan = __int_as_float(0x7fffffff);
               v = make_float4(nan, nan, nan, nan);
             }
-            row[col] = v;
+            *o = v;
           }
         }
         fence_before_sync();
@@ -1077,17 +1222,16 @@ cudaError_t launch_tc(const MPTask* tasks, const int2* tiles, int64_t first_tile
   return cudaGetLastError();
 }
 
-cudaError_t launch_hp_tc_p(const HPTask* tasks, const HpTcGroup* groups, const int4* items, int64_t first_item,
-                           int64_t n_items, const int2* img_units, int64_t first_unit, int64_t n_units,
-                           double2* ws, int* status, cudaStream_t s) {
-  if (n_units > 0) k_hp_tc_img<<<(unsigned)n_units, 256, 0, s>>>(groups, img_units, first_unit);
+template <int OP>
+cudaError_t launch_tcs(const TcsArgs& g, const int2* img_units, int64_t first_unit, int64_t n_units, cudaStream_t s) {
+  if (n_units > 0) k_tcs_img<OP><<<(unsigned)n_units, 256, 0, s>>>(g, img_units, first_unit);
   unsigned grid = 0;
-  cudaError_t e = tc_grid(n_items, &grid);
+  cudaError_t e = tc_grid(g.n_items, &grid);
   if (e != cudaSuccess) return e;
-  const int smem = (int)sizeof(HpSmem);
-  e = cudaFuncSetAttribute(k_hp_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const int smem = (int)sizeof(TcsSmem);
+  e = cudaFuncSetAttribute(k_tcs<OP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  k_hp_tc<<<grid, kThreadsTc, smem, s>>>(tasks, groups, items, first_item, n_items, ws, status);
+  k_tcs<OP><<<grid, kThreadsTc, smem, s>>>(g);
   return cudaGetLastError();
 }
 
@@ -1097,7 +1241,30 @@ cudaError_t launch_hp_tc(const HPTask* tasks, const HpTcGroup* groups, const int
                          int64_t n_items, const int2* img_units, int64_t first_unit, int64_t n_units,
                          double2* ws, int* status, cudaStream_t s) {
   if (n_items <= 0) return cudaSuccess;
-  return launch_hp_tc_p(tasks, groups, items, first_item, n_items, img_units, first_unit, n_units, ws, status, s);
+  TcsArgs g{};
+  g.hp = tasks;
+  g.groups = groups;
+  g.ws = ws;
+  g.items = items;
+  g.item0 = first_item;
+  g.n_items = n_items;
+  g.status = status;
+  return launch_tcs<TCS_HP>(g, img_units, first_unit, n_units, s);
+}
+
+cudaError_t launch_acc_tc(const AccTask* tasks, const AccTerm* terms, const int4* items, int64_t first_item,
+                          int64_t n_items, int64_t units, const int2* img_units, int64_t first_unit,
+                          int64_t n_units, int* status, cudaStream_t s) {
+  if (n_items <= 0) return cudaSuccess;
+  TcsArgs g{};
+  g.acc = tasks;
+  g.terms = terms;
+  g.items = items;
+  g.item0 = first_item;
+  g.n_items = n_items;
+  g.units = units;
+  g.status = status;
+  return launch_tcs<TCS_ACC>(g, img_units, first_unit, n_units, s);
 }
 
 cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,

@@ -100,8 +100,8 @@ class PlanView:
         widths = {0: 5, 1: 11, 2: 9, 3: 9, 4: 4, 5: 5, 6: 2, 7: 7, 8: 13, 10: 2, 13: 4, 18: 6, 19: 14,
                   20: 6, 22: 6, 23: 4, 24: 27, 25: 8, 26: 12, 27: 11, 28: 2, 29: 11, 33: 3, 34: 10,
                   35: 8, 36: 2, 38: 14, 39: 5, 40: 2, 41: 4, 42: 2, 43: 2, 44: 5, 45: 3, 46: 4, 47: 3, 49: 3, 50: 2, 51: 2,
-                  52: 16, 53: 4, 54: 2, 55: 4}
-        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 57)):
+                  52: 16, 53: 4, 54: 2, 55: 4, 57: 4, 58: 2, 59: 5}
+        for what in list(range(14)) + [18, 19, 20, 21, 22, 23] + list(range(24, 30)) + list(range(33, 61)):
             n = int(L.qtp_size(h, what))
             a = np.zeros(max(n, 1), np.int64)
             if n:
@@ -216,18 +216,21 @@ class PlanView:
                     view(sb, so, a * a)[:] = S.ravel(order="F")
                 elif kind == ST_ACC:
                     ob, oo, ap, aoff, rows, d, first, count, add = T[3][t]
+                    alpha = bufs[B_MATS][aoff] if ap == 2 else (bufs[B_PARAM][0] if ap else 1.0)
+                    tc = self.tensor and self.prec == 1 and acc_tc_eligible(rows, d)
                     acc = np.zeros((rows, d), np.complex128)
                     for s in range(first, first + count):
                         hb, ho, xb, xo = T[4][s]
                         X = view(xb, xo, rows * d).reshape((rows, d), order="F")
-                        if hb < 0:
+                        H = np.eye(d) if hb < 0 else view(hb, ho, d * d).reshape((d, d), order="F")
+                        if tc:  # alpha H_t in the digit arithmetic, term by term
+                            acc += oz_mode_product(alpha * H, X[:, :, None])[:, :, 0]
+                        elif hb < 0:
                             acc += X
                         else:
-                            H = view(hb, ho, d * d).reshape((d, d), order="F")
                             acc += X @ H.T
-                    alpha = bufs[B_MATS][aoff] if ap == 2 else (bufs[B_PARAM][0] if ap else 1.0)
                     out = view(ob, oo, rows * d)
-                    v = (alpha * acc).ravel(order="F")
+                    v = (acc if tc else alpha * acc).ravel(order="F")
                     out[:] = out + v if add else v
                 elif kind == ST_LIN:
                     ob, oo, d, first, count = T[5][t]
@@ -480,6 +483,11 @@ def oz_mode_product(h, x):
 
 
 HP_CHUNK = 64
+
+
+def acc_tc_eligible(rows, d):
+    """The accumulations the planner puts on the tensor cores (qt_internal.h)."""
+    return 16 <= d <= 64 and rows >= 64
 
 
 def hp_tc_eligible(before, a, after):

@@ -1,6 +1,6 @@
-"""The tensor-core mode products (QT_PREC_DF64_TC) at the level of a whole
-sweep, on the CPU: the plan interpreter (tests/plan_emulator.py) runs every
-eligible mode product through the same digit arithmetic
+"""The tensor-core sums of products (QT_PREC_DF64_TC) at the level of a
+whole sweep, on the CPU: the plan interpreter (tests/plan_emulator.py) runs every
+eligible mode product, hole product and accumulation through the same digit arithmetic
 as qt_umma.cu (double-float operands, seven signed digits from error-free
 splits against row exponents, exact level sums for L <= 2, one
 float32-rounded sum of the levels 3..6) and the sweep is compared with the
@@ -31,16 +31,17 @@ def test_digit_mode_product_within_bound():
         assert np.all(np.abs(got - want) <= bound)
 
 
-def _check(tree, sop, psi, flavour):
+def _check(tree, sop, psi, flavour, tol=TOL_DF, noise_tol=1e-11):
     flat = psi.flat()
     r = O.derivative(tree, sop, flat)
     pv = PlanView(tree, sop, flavour | TENSOR, prec=1)
     pv.run(flat)
     h00, s00 = pv.energy_parts()
-    assert abs(h00.real / s00.real - r.energy) < TOL_DF * max(1, abs(r.energy))
-    assert rel_err(rho_weighted(tree, pv.dpsi(), r.rho), rho_weighted(tree, r.dpsi, r.rho)) < TOL_DF
+    assert abs(h00.real / s00.real - r.energy) < tol * max(1, abs(r.energy))
+    assert rel_err(rho_weighted(tree, pv.dpsi(), r.rho), rho_weighted(tree, r.dpsi, r.rho)) < tol
     err, noise = deriv_errors(tree, pv.dpsi(), r.dpsi, r.rho)
-    assert err <= TOL_DF and noise <= 1e-11
+    print(f"emulated tensor-core sweep: dE {abs(h00.real / s00.real - r.energy):.2e} dpsi {err:.2e} noise {noise:.2e}")
+    assert err <= tol and noise <= noise_tol
     # the digit arithmetic ran: the same plan without the tensor bit differs at rounding level
     exact = PlanView(tree, sop, flavour, prec=1)
     exact.run(flat)
@@ -51,6 +52,16 @@ def _check(tree, sop, psi, flavour):
 def test_emulated_tensor_core_sweep_cfg0(flavour):
     tree, sop, psi = config_problem(0)
     _check(tree, sop, psi, flavour)
+
+
+@pytest.mark.parametrize("flavour", [1, 2])
+def test_emulated_tensor_core_sweep_cfg4(flavour):
+    # bonds and leaves of 32: hole products and accumulations take the
+    # digit arithmetic too (the GPU tolerance of the tensor-core plans)
+    tree, sop, psi = config_problem(4)
+    pv = PlanView(tree, sop, flavour | TENSOR, prec=1)
+    assert len(pv.tables[52]) > 0 and len(pv.tables[57]) > 0
+    _check(tree, sop, psi, flavour, tol=1e-10, noise_tol=1e-10)
 
 
 @pytest.mark.parametrize("leaves,p,b,seed", [(7, 5, 4, 2), (5, 80, 12, 3)])

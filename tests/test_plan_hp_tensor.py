@@ -1,15 +1,18 @@
-"""Planner side of the tensor-core hole products (double-float plans with
-flavour bit 0x8000), on the CPU.  In every hole-product stage the tasks with
+"""Planner side of the tensor-core hole products and accumulations
+(double-float plans with flavour bit 0x8000), on the CPU.  In every hole-product stage the tasks with
 16 <= a <= 64 and at least 128 reduction rows go into groups of up to
 min(8, 128 / a) tasks that share the operand A (same buffer, offset and
 shape); every group's work items cover its 64-row chunks exactly once, in
 ranges of the length the member tasks record (kchunk, splits); split tasks
 own disjoint workspace slots; one pre-pass image per distinct A, private
-within the stage and inside B_OZ; the other tasks keep their classic tiles."""
+within the stage and inside B_OZ; the other tasks keep their classic tiles.
+Accumulations with 16 <= d <= 64 and at least 64 rows get one item per
+128-row block (all terms in order, one unit each, items ordered by their
+units-before count) and an image slot per term."""
 import numpy as np
 import pytest
 
-from plan_emulator import ST_HP, PlanView, hp_tc_eligible
+from plan_emulator import ST_ACC, ST_HP, PlanView, acc_tc_eligible, hp_tc_eligible
 from qutree_gb300.model import balanced_tree, config_problem, coupled_oscillators
 
 TENSOR = 0x8000
@@ -108,3 +111,46 @@ def test_no_tensor_core_hole_products_outside_double_float_tensor_plans(flavour,
     tree, sop, _ = config_problem(4)
     pv = PlanView(tree, sop, flavour=flavour, prec=prec)
     assert len(pv.tables[52]) == 0 and len(pv.tables[53]) == 0
+
+
+@pytest.mark.parametrize("name", ["cfg0", "cfg4", "cfg1", "wide_leaves"])
+@pytest.mark.parametrize("plan", [1, 2])
+def test_accumulation_items(name, plan):
+    tree, sop = problem(name)
+    pv = PlanView(tree, sop, flavour=plan | TENSOR, prec=1)
+    T = pv.tables
+    acc, tiles, items, units, ranges, imgs = T[3], T[49], T[57], T[58], T[59], T[60]
+    oz_bytes = int(T[56][0])
+    n_tc = 0
+    for si, (kind, t0, nt, tile0, ntile) in enumerate(T[0]):
+        ati0, nati, atu0, natu, nunits = (int(x) for x in ranges[si])
+        if kind != ST_ACC:
+            assert nati == 0 and natu == 0
+            continue
+        eligible = {t for t in range(t0, t0 + nt)
+                    if int(acc[t][7]) >= 1 and acc_tc_eligible(int(acc[t][4]), int(acc[t][5]))}
+        its = items[ati0:ati0 + nati]
+        # items: every 128-row block of every eligible task once, units-before ascending
+        blocks = {}
+        pre = 0
+        for task, blk, before, _ in its:
+            assert int(before) == pre
+            pre += int(acc[task][7])
+            blocks.setdefault(int(task), []).append(int(blk))
+        assert pre == nunits
+        assert set(blocks) == eligible
+        for t, b in blocks.items():
+            assert sorted(b) == list(range(-(-int(acc[t][4]) // 128)))
+        # image units: every term of every eligible task once; slots disjoint in B_OZ
+        seen = sorted((int(t), int(s)) for t, s in units[atu0:atu0 + natu])
+        assert seen == sorted((t, s) for t in eligible for s in range(int(acc[t][7])))
+        spans = sorted((int(imgs[t]), int(imgs[t]) + int(acc[t][7]) * chunk_bytes(int(acc[t][5]))) for t in eligible)
+        assert all(e0 <= s1 for (_, e0), (s1, _) in zip(spans, spans[1:]))
+        assert all(0 <= s and e <= oz_bytes for s, e in spans)
+        for t in range(t0, t0 + nt):
+            assert (int(imgs[t]) >= 0) == (t in eligible)
+        # classic tiles: only the other tasks
+        assert not eligible & {int(r[0]) for r in tiles[tile0:tile0 + ntile]}
+        n_tc += len(eligible)
+    if name in ("cfg4", "cfg1"):
+        assert n_tc > 0
