@@ -47,14 +47,14 @@ struct HPTask {
 // hole products on the tensor cores (qt_umma.cu, double-float plans): groups
 // of up to eight tasks that share the operand A form one 128-row accumulator
 // tile (rows: the tasks' B columns j, columns: A's i, real and imaginary
-// parts); the reduction runs in chunks of 64 k, each chunk with its own
-// power-of-two scales.  A group's member tasks (indices into the task table)
+// parts); the reduction runs in chunks of hp_tc_kc(ap) k, each chunk with
+// its own power-of-two scales.  A group's member tasks (indices into the task table)
 // all have the same a, before and after.
-constexpr int kHpTcChunk = 64;     // k per chunk
+constexpr int kHpTcChunk = 64;     // k of the shorter chunks
 constexpr int kHpTcMembers = 8;    // tasks per group (a >= 16)
 struct HpTcGroup {
   const double2* A;
-  unsigned char* img;  // A's operand images, one per chunk (hp_tc_chunk_bytes)
+  unsigned char* img;  // A's operand images, one per chunk of hp_tc_kc(ap) k
   int before, a, after;
   int ap;              // a padded to a multiple of 8
   int n, nchunks;
@@ -64,12 +64,20 @@ struct HpTcGroup {
 inline bool hp_tc_eligible(int before, int a, int after) {
   return a >= 16 && a <= 64 && (int64_t)before * after >= 2 * kHpTcChunk;
 }
-// bytes of one chunk of A's image: 4 steps of 16 k x 7 digits x rows
-// [Ai | Ar | -Ai] (3 ap) x 16 bf16, then ap column exponents (int, 64 slots)
 #ifdef __CUDACC__
-__host__ __device__
+#define QT_HD __host__ __device__
+#else
+#define QT_HD
 #endif
-constexpr int64_t hp_tc_chunk_bytes(int ap) { return (int64_t)4 * 7 * 3 * ap * 16 * 2 + 64 * 4; }
+// reduction length of a chunk: 128 k for ap > 32, whose four level
+// accumulators keep the levels 0..2 exact up to 170 k, else 64 k (seven
+// exact levels up to 73 k)
+QT_HD constexpr int hp_tc_kc(int ap) { return ap > 32 ? 2 * kHpTcChunk : kHpTcChunk; }
+// bytes of one unit's operand image: steps of 16 k x 7 digits x rows
+// [-Wi | Wr | Wi] (3 ap) x 16 bf16, then the column exponents (int, 64 slots)
+QT_HD constexpr int64_t hp_tc_chunk_bytes(int ap, int steps) {
+  return (int64_t)steps * 7 * 3 * ap * 16 * 2 + 64 * 4;
+}
 
 // out[r, j] (+)= alpha * sum_t sum_j' H_t(j, j') X_t[r, j'] over the terms
 // [first, first+count) of the AccTerm table; H == nullptr means identity.
@@ -84,7 +92,7 @@ struct AccTask {
   int rows, d;
   int first, count;
   int add, pad;
-  void* tc_img = nullptr;  // tensor-core path: images of alpha H_t, one per term (hp_tc_chunk_bytes)
+  void* tc_img = nullptr;  // tensor-core path: images of alpha H_t, one per term (hp_tc_chunk_bytes(., 4))
 };
 // an accumulation the planner puts on the tensor cores (double-float plans)
 inline bool acc_tc_eligible(int rows, int d) { return d >= 16 && d <= 64 && rows >= 64; }

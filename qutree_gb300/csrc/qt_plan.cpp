@@ -533,12 +533,13 @@ class Builder {
         g.before = h.before;
         g.a = h.a;
         g.after = h.after;
-        g.nchunks = (int)(((int64_t)h.before * h.after + kHpTcChunk - 1) / kHpTcChunk);
+        const int ap = (h.a + 7) & ~7, kc = hp_tc_kc(ap);
+        g.nchunks = (int)(((int64_t)h.before * h.after + kc - 1) / kc);
         const int64_t gi = (int64_t)P.hp_tc_groups.size();
         auto im = img.find(key);
         if (im == img.end()) {  // this group's pre-pass writes A's images
           g.img = stage_oz_;
-          stage_oz_ += g.nchunks * hp_tc_chunk_bytes((h.a + 7) & ~7);
+          stage_oz_ += g.nchunks * hp_tc_chunk_bytes(ap, kc / 16);
           img[key] = g.img;
           for (int c = 0; c < g.nchunks; ++c) P.hp_tc_imgs.push_back(make_int2((int)gi, c));
         } else {
@@ -552,17 +553,21 @@ class Builder {
       g.member[g.n++] = (int)t;
     }
     const int64_t g1 = (int64_t)P.hp_tc_groups.size();
+    // item length in 64-k units: about two items per SM over the stage
     int64_t units = 0;
-    for (int64_t g = g0; g < g1; ++g) units += P.hp_tc_groups[g].nchunks;
-    const int cpi = (int)std::max<int64_t>(1, (units + 2 * 152 - 1) / (2 * 152));
+    for (int64_t g = g0; g < g1; ++g)
+      units += (int64_t)P.hp_tc_groups[g].nchunks * (hp_tc_kc((P.hp_tc_groups[g].a + 7) & ~7) / kHpTcChunk);
+    const int64_t target = std::max<int64_t>(1, (units + 2 * 152 - 1) / (2 * 152));
     bool split = false;
     for (int64_t g = g0; g < g1; ++g) {
       const Plan::SHpTcGroup& G = P.hp_tc_groups[g];
+      const int kc = hp_tc_kc((G.a + 7) & ~7);
+      const int cpi = (int)std::max<int64_t>(1, target / (kc / kHpTcChunk));
       const int splits = (G.nchunks + cpi - 1) / cpi;
       for (int m = 0; m < G.n; ++m) {
         Plan::SHP& h = P.hp[G.member[m]];
         h.splits = splits;
-        h.kchunk = cpi * kHpTcChunk;
+        h.kchunk = cpi * kc;
         h.ws = 0;
         if (splits > 1) {
           h.ws = ws;
@@ -589,7 +594,7 @@ class Builder {
       if (a.count < 1 || !acc_tc_eligible(a.rows, a.d)) continue;
       tc[t - t0] = 1;
       a.tc_img = stage_oz_;
-      stage_oz_ += (int64_t)a.count * hp_tc_chunk_bytes((a.d + 7) & ~7);
+      stage_oz_ += (int64_t)a.count * hp_tc_chunk_bytes((a.d + 7) & ~7, 4);
       for (int s = 0; s < a.count; ++s) P.acc_tc_imgs.push_back(make_int2((int)t, s));
       for (int64_t b = 0; b * 128 < a.rows; ++b) {
         P.acc_tc_items.push_back(make_int4((int)t, (int)b, (int)units, 0));
@@ -660,7 +665,9 @@ class Builder {
       if (m.diag || m.a_in > 64 || m.a_out > 64) continue;
       oz[t - t0] = 1;
       m.oz_h = stage_oz_;
-      stage_oz_ += mp_oz_h_bytes();
+      // double-float plans: the sum-of-products kernel's image of alpha h;
+      // complex64 plans: the split-TF32 image
+      stage_oz_ += P.hp_tensor ? hp_tc_chunk_bytes((m.a_out + 7) & ~7, 4) : mp_oz_h_bytes();
       P.mp_oz_tasks.push_back((int)t);
       const int64_t rows = (int64_t)m.before * m.after;
       for (int64_t r = 0; r * kMpOzRows * kMpOzSub < rows; ++r)

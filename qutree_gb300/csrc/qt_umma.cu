@@ -680,7 +680,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
 // where the accumulation asks for it).
 // ---------------------------------------------------------------------------
 constexpr int kTcsNStage = kDig * 3 * 64 * 32;  // W side of one 16-k step at np = 64
-enum { TCS_HP = 0, TCS_ACC = 1 };
+
+enum { TCS_HP = 0, TCS_ACC = 1, TCS_MP = 2 };
 
 struct TcsSmem {
   unsigned char a[2][kOzAStage];
@@ -698,11 +699,24 @@ struct TcsArgs {
   double2* ws;
   const AccTask* acc;        // accumulations: tasks and terms
   const AccTerm* terms;
+  const MPTask* mp;          // mode products: tasks, tiles (task, 128-row block) and the pre-pass's tasks
+  const int2* mp_tiles;
+  const int* mp_tasks;
   const int4* items;         // HP (group, range z, first chunk, end chunk); ACC (task, block, units before, 0)
   int64_t item0, n_items;
   int64_t units;             // ACC: units of all items (weighted split over the CTAs)
   int* status;
 };
+
+// item `it` of the launch (mode products: (task, 128-row block, 0, 0))
+template <int OP>
+__device__ __forceinline__ int4 tcs_fetch(const TcsArgs& g, int64_t it) {
+  if (OP == TCS_MP) {
+    const int2 t = g.mp_tiles[g.item0 + it];
+    return make_int4(t.x, t.y, 0, 0);
+  }
+  return g.items[g.item0 + it];
+}
 
 // element k of row `row` of a hole-product operand of shape (before, a, after):
 // k = b + before c, offset b + before row + before a c; walked in steps of one
@@ -724,7 +738,7 @@ struct KWalk {
 // the items whose first unit falls into the CTA's equal share of all units
 template <int OP>
 __device__ __forceinline__ void tcs_range(const TcsArgs& g, int64_t& i0, int64_t& i1) {
-  if (OP == TCS_HP) {
+  if (OP != TCS_ACC) {
     const int64_t per = g.n_items / gridDim.x, extra = g.n_items % gridDim.x;
     i0 = blockIdx.x * per + min((int64_t)blockIdx.x, extra);
     i1 = i0 + per + (blockIdx.x < extra ? 1 : 0);
@@ -746,6 +760,7 @@ __device__ __forceinline__ void tcs_range(const TcsArgs& g, int64_t& i0, int64_t
 // per item: padded columns np, real columns, units, 16-k steps per unit
 struct TcsItem {
   int np, ncols, nunits, nks;
+  int nl;  // level accumulators
 };
 template <int OP>
 __device__ __forceinline__ TcsItem tcs_item(const TcsArgs& g, int4 itm) {
@@ -755,114 +770,172 @@ __device__ __forceinline__ TcsItem tcs_item(const TcsArgs& g, int4 itm) {
     v.np = G.ap;
     v.ncols = G.a;
     v.nunits = itm.w - itm.z;
-    v.nks = kHpTcChunk / kChunkK;
-  } else {
+    v.nks = hp_tc_kc(G.ap) / kChunkK;
+    // 128-k chunks keep four accumulators (levels 0..2 exact up to 170 k)
+    v.nl = v.nks > 4 ? min(4, levels_for(G.ap)) : levels_for(G.ap);
+  } else if (OP == TCS_ACC) {
     const AccTask& T = g.acc[itm.x];
     v.np = (T.d + 7) & ~7;
     v.ncols = T.d;
     v.nunits = T.count;
     v.nks = (T.d + kChunkK - 1) / kChunkK;
+    v.nl = levels_for(v.np);
+  } else {
+    const MPTask& t = g.mp[itm.x];
+    v.np = (t.a_out + 7) & ~7;
+    v.ncols = t.a_out;
+    v.nunits = 1;
+    v.nks = (t.a_in + kChunkK - 1) / kChunkK;
+    v.nl = levels_for(v.np);
   }
   return v;
 }
+// image steps of a unit (the image's layout; the unit may use fewer)
+template <int OP>
+__device__ __forceinline__ int tcs_img_steps(int np) {
+  return OP == TCS_HP ? hp_tc_kc(np) / kChunkK : 4;
+}
 template <int OP>
 __device__ __forceinline__ const unsigned char* tcs_image(const TcsArgs& g, int4 itm, int u, int np) {
-  if (OP == TCS_HP) return g.groups[itm.x].img + (size_t)(itm.z + u) * hp_tc_chunk_bytes(np);
-  return static_cast<const unsigned char*>(g.acc[itm.x].tc_img) + (size_t)u * hp_tc_chunk_bytes(np);
+  const int64_t cb = hp_tc_chunk_bytes(np, tcs_img_steps<OP>(np));
+  if (OP == TCS_HP) return g.groups[itm.x].img + (size_t)(itm.z + u) * cb;
+  if (OP == TCS_MP) return static_cast<const unsigned char*>(g.mp[itm.x].oz_h);
+  return static_cast<const unsigned char*>(g.acc[itm.x].tc_img) + (size_t)u * cb;
 }
 
 // pre-pass: the image of W for one unit -- per 16-k step and digit a plane of
 // 3 np rows, -Wi at row n, Wr at np + n, Wi at 2 np + n (rows past the last
-// column zero) -- and the unit's row exponents F_n.  Thread (n, ks) takes
-// row n of the 16-k step ks.  HP units (group, chunk): W(i, k) = conj(A[k; i]);
-// ACC units (task, term): W(j, k) = alpha H(j, k), alpha I for identity terms.
+// column zero) -- and the unit's row exponents F_n.  Thread (n, q) takes row
+// n of the steps q, q + 4, ...  HP units (group, chunk): W(i, k) = conj(A[k; i]);
+// ACC units (task, term): W(j, k) = alpha H(j, k), alpha I for identity terms;
+// MP units (task): W(j, k) = alpha h(j, k).
 template <int OP>
 __global__ void __launch_bounds__(256) k_tcs_img(TcsArgs g, const int2* __restrict__ units, int64_t first) {
-  const int2 u = units[first + blockIdx.x];
-  const int n = threadIdx.x & 63, ks = threadIdx.x >> 6;
-  int np, ncols;
+  const int2 u = OP == TCS_MP ? make_int2(g.mp_tasks[first + blockIdx.x], 0) : units[first + blockIdx.x];
+  const int n = threadIdx.x & 63, q = threadIdx.x >> 6;
+  int np, ncols, steps;
   unsigned char* img;
-  float4 v[16];
+  // the 16 values of row n at step ks
+  auto load16 = [&](int ks, float4 (&v)[16]) {
+    if (OP == TCS_HP) {
+      const HpTcGroup& G = g.groups[u.x];
+      const int K = G.before * G.after, k0 = u.y * hp_tc_kc(G.ap) + ks * kChunkK;
+      const float4* __restrict__ A = reinterpret_cast<const float4*>(G.A);
+      KWalk w(min(k0, K), G.before);
+#pragma unroll
+      for (int kk = 0; kk < 16; ++kk) {
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n < G.a && k0 + kk < K) {
+          x = __ldg(A + w.off(n, G.before, G.a));
+          x.z = -x.z;
+          x.w = -x.w;
+        }
+        v[kk] = x;
+        w.next(G.before);
+      }
+    } else if (OP == TCS_MP) {
+      const MPTask& t = g.mp[u.x];
+      const float4 cf = DF64::coef(t.alpha);
+      const bool one = t.alpha.x == 1.0 && t.alpha.y == 0.0;
+      const float4* __restrict__ H = reinterpret_cast<const float4*>(t.h);
+#pragma unroll
+      for (int kk = 0; kk < 16; ++kk) {
+        const int k = ks * kChunkK + kk;
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n < t.a_out && k < t.a_in) {
+          x = __ldg(H + n + (int64_t)t.a_out * k);
+          if (!one) x = DF64::mul(cf, x);
+        }
+        v[kk] = x;
+      }
+    } else {
+      const AccTask& T = g.acc[u.x];
+      const AccTerm tm = g.terms[T.first + u.y];
+      const double2 alpha = T.alpha_ptr ? *T.alpha_ptr : T.alpha;
+      const float4 cf = DF64::coef(alpha);
+      const float4* __restrict__ H = reinterpret_cast<const float4*>(tm.H);
+#pragma unroll
+      for (int kk = 0; kk < 16; ++kk) {
+        const int k = ks * kChunkK + kk;
+        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (n < T.d && k < T.d) {
+          if (H) x = DF64::mul(cf, __ldg(H + n + (int64_t)T.d * k));
+          else if (n == k) x = cf;
+        }
+        v[kk] = x;
+      }
+    }
+  };
   if (OP == TCS_HP) {
-    const HpTcGroup G = g.groups[u.x];
+    const HpTcGroup& G = g.groups[u.x];
     np = G.ap;
     ncols = G.a;
-    const int K = G.before * G.after, k0 = u.y * kHpTcChunk + ks * kChunkK;
-    img = G.img + (size_t)u.y * hp_tc_chunk_bytes(np);
-    const float4* __restrict__ A = reinterpret_cast<const float4*>(G.A);
-    KWalk w(min(k0, K), G.before);
-#pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (n < ncols && k0 + kk < K) {
-        x = __ldg(A + w.off(n, G.before, G.a));
-        x.z = -x.z;
-        x.w = -x.w;
-      }
-      v[kk] = x;
-      w.next(G.before);
-    }
+    steps = hp_tc_kc(np) / kChunkK;
+    img = G.img + (size_t)u.y * hp_tc_chunk_bytes(np, steps);
+  } else if (OP == TCS_MP) {
+    const MPTask& t = g.mp[u.x];
+    np = (t.a_out + 7) & ~7;
+    ncols = t.a_out;
+    steps = 4;
+    img = static_cast<unsigned char*>(t.oz_h);
   } else {
-    const AccTask T = g.acc[u.x];
-    const AccTerm tm = g.terms[T.first + u.y];
+    const AccTask& T = g.acc[u.x];
     np = (T.d + 7) & ~7;
     ncols = T.d;
-    img = static_cast<unsigned char*>(T.tc_img) + (size_t)u.y * hp_tc_chunk_bytes(np);
-    const double2 alpha = T.alpha_ptr ? *T.alpha_ptr : T.alpha;
-    const float4 cf = DF64::coef(alpha);
-    const float4* __restrict__ H = reinterpret_cast<const float4*>(tm.H);
-#pragma unroll
-    for (int kk = 0; kk < 16; ++kk) {
-      const int k = ks * kChunkK + kk;
-      float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (n < ncols && k < ncols) {
-        if (H) x = DF64::mul(cf, __ldg(H + n + (int64_t)ncols * k));
-        else if (n == k) x = cf;
-      }
-      v[kk] = x;
-    }
+    steps = 4;
+    img = static_cast<unsigned char*>(T.tc_img) + (size_t)u.y * hp_tc_chunk_bytes(np, steps);
   }
+  (void)ncols;
   __shared__ int fx[64];
   if (threadIdx.x < 64) fx[threadIdx.x] = 1;
   __syncthreads();
   int m = 1;
+  for (int ks = q; ks < steps; ks += 4) {
+    float4 v[16];
+    load16(ks, v);
 #pragma unroll
-  for (int kk = 0; kk < 16; ++kk) m = max(m, max(fexp(v[kk].x), fexp(v[kk].z)));
+    for (int kk = 0; kk < 16; ++kk) m = max(m, max(fexp(v[kk].x), fexp(v[kk].z)));
+  }
   atomicMax(&fx[n], m);
   __syncthreads();
   if (n < np) {
     const int f = fx[n];
     const int rows = 3 * np, plane = rows * 32;
-    unsigned char* base = img + (size_t)ks * kDig * plane;
+    for (int ks = q; ks < steps; ks += 4) {
+      float4 v[16];
+      load16(ks, v);
+      unsigned char* base = img + (size_t)ks * kDig * plane;
 #pragma unroll
-    for (int c = 0; c < 2; ++c) {  // the two 8-k core rows of the step
-      uint32_t wr[kDig][4], wi[kDig][4];
+      for (int c = 0; c < 2; ++c) {  // the two 8-k core rows of the step
+        uint32_t wr[kDig][4], wi[kDig][4];
 #pragma unroll
-      for (int p = 0; p < 4; ++p) {
-        float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
-        digits_f32(v[8 * c + 2 * p].x, v[8 * c + 2 * p].y, f, d0);
-        digits_f32(v[8 * c + 2 * p + 1].x, v[8 * c + 2 * p + 1].y, f, d1);
-        digits_f32(v[8 * c + 2 * p].z, v[8 * c + 2 * p].w, f, e0);
-        digits_f32(v[8 * c + 2 * p + 1].z, v[8 * c + 2 * p + 1].w, f, e1);
+        for (int p = 0; p < 4; ++p) {
+          float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
+          digits_f32(v[8 * c + 2 * p].x, v[8 * c + 2 * p].y, f, d0);
+          digits_f32(v[8 * c + 2 * p + 1].x, v[8 * c + 2 * p + 1].y, f, d1);
+          digits_f32(v[8 * c + 2 * p].z, v[8 * c + 2 * p].w, f, e0);
+          digits_f32(v[8 * c + 2 * p + 1].z, v[8 * c + 2 * p + 1].w, f, e1);
+#pragma unroll
+          for (int d = 0; d < kDig; ++d) {
+            wr[d][p] = pack_bf16(d0[d], d1[d]);
+            wi[d][p] = pack_bf16(e0[d], e1[d]);
+          }
+        }
 #pragma unroll
         for (int d = 0; d < kDig; ++d) {
-          wr[d][p] = pack_bf16(d0[d], d1[d]);
-          wi[d][p] = pack_bf16(e0[d], e1[d]);
+          unsigned char* pl = base + (size_t)d * plane;
+          const uint4 re = make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
+          const uint4 im = make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
+          const uint4 nim =
+              make_uint4(im.x ^ 0x80008000u, im.y ^ 0x80008000u, im.z ^ 0x80008000u, im.w ^ 0x80008000u);
+          *reinterpret_cast<uint4*>(pl + core_off(n, c, rows)) = nim;
+          *reinterpret_cast<uint4*>(pl + core_off(np + n, c, rows)) = re;
+          *reinterpret_cast<uint4*>(pl + core_off(2 * np + n, c, rows)) = im;
         }
-      }
-#pragma unroll
-      for (int d = 0; d < kDig; ++d) {
-        unsigned char* pl = base + (size_t)d * plane;
-        const uint4 re = make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
-        const uint4 im = make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
-        const uint4 nim = make_uint4(im.x ^ 0x80008000u, im.y ^ 0x80008000u, im.z ^ 0x80008000u, im.w ^ 0x80008000u);
-        *reinterpret_cast<uint4*>(pl + core_off(n, c, rows)) = nim;
-        *reinterpret_cast<uint4*>(pl + core_off(np + n, c, rows)) = re;
-        *reinterpret_cast<uint4*>(pl + core_off(2 * np + n, c, rows)) = im;
       }
     }
   }
-  if (threadIdx.x < 64) reinterpret_cast<int*>(img + (size_t)4 * kDig * 3 * np * 32)[threadIdx.x] = fx[threadIdx.x];
+  if (threadIdx.x < 64) reinterpret_cast<int*>(img + (size_t)steps * kDig * 3 * np * 32)[threadIdx.x] = fx[threadIdx.x];
 }
 
 // the producers' view of row r of an item: its source of X and validity
@@ -907,13 +980,13 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
     const int r = tid & (kRows - 1), h = tid >> 7;
     uint32_t q = 0, un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it) {
-      const int4 itm = g.items[g.item0 + it];
+      const int4 itm = tcs_fetch<OP>(g, it);
       const TcsItem I = tcs_item<OP>(g, itm);
       const uint32_t nbytes = (uint32_t)(kDig * 3 * I.np * 32);
       // row r of the item
       TcsRow R;
       int before = 1, a = 1, K = 0;
-      int64_t rows = 0;
+      int64_t rows = 0;  // k stride of X (ACC: the task's rows; MP: before)
       int tfirst = 0;
       if (OP == TCS_HP) {
         const HpTcGroup& G = g.groups[itm.x];
@@ -925,7 +998,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
         R.valid = mi < G.n;
         R.src = R.valid ? reinterpret_cast<const float4*>(g.hp[G.member[mi]].B) : nullptr;
         R.rg = 0;
-      } else {
+      } else if (OP == TCS_ACC) {
         const AccTask& T = g.acc[itm.x];
         rows = T.rows;
         K = T.d;
@@ -934,12 +1007,23 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
         R.valid = R.rg < rows;
         R.src = nullptr;
         R.j = 0;
+      } else {
+        // mode product: row (b, c) of the input, its k-th element at b + before (k + a_in c)
+        const MPTask& t = g.mp[itm.x];
+        const int64_t rg = (int64_t)itm.y * kRows + r;
+        K = t.a_in;
+        rows = t.before;
+        R.valid = rg < (int64_t)t.before * t.after;
+        const int64_t b = R.valid ? rg % t.before : 0, c = R.valid ? rg / t.before : 0;
+        R.src = reinterpret_cast<const float4*>(t.in) + b + (int64_t)t.before * K * c;
+        R.rg = 0;
+        R.j = 0;
       }
       for (int u = 0; u < I.nunits; ++u, ++un) {
         const int buf = (int)(un & 1);
         const uint32_t use_par = (un >> 1) & 1;
-        const float4* X = OP == TCS_HP ? R.src : reinterpret_cast<const float4*>(g.terms[tfirst + u].X);
-        const int kbase = OP == TCS_HP ? (itm.z + u) * kHpTcChunk : 0;
+        const float4* X = OP != TCS_ACC ? R.src : reinterpret_cast<const float4*>(g.terms[tfirst + u].X) + R.rg;
+        const int kbase = OP == TCS_HP ? (itm.z + u) * I.nks * kChunkK : 0;
         // this thread's values of step ks: k = kbase + 16 ks + 8 h + i
         auto load8 = [&](float4 (&x)[8], int ks) {
           const int k0 = kbase + ks * kChunkK + h * 8;
@@ -953,7 +1037,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
           } else {
 #pragma unroll
             for (int i = 0; i < 8; ++i)
-              x[i] = (R.valid && k0 + i < K) ? __ldg(X + R.rg + rows * (k0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
+              x[i] = (R.valid && k0 + i < K) ? __ldg(X + rows * (k0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         };
         int m = 1;
@@ -1035,9 +1119,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
     if (lane == 0) {
       uint32_t q = 0, un = 0;
       for (int64_t it = my0; it < my1 && ok; ++it) {
-        const int4 itm = g.items[g.item0 + it];
+        const int4 itm = tcs_fetch<OP>(g, it);
         const TcsItem I = tcs_item<OP>(g, itm);
-        const int np = I.np, NL = levels_for(np);
+        const int np = I.np, NL = I.nl;
         const uint32_t id = idesc_m128(1, 2 * np, false);
         const uint32_t lboA = (kRows / 8) * 128, lboN = (uint32_t)(3 * np / 8) * 128;
         const uint64_t pA = kOzAPlane >> 4, pN = (uint64_t)((3 * np * 32) >> 4);
@@ -1090,9 +1174,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
     int* fxw = sm.fx[qd];
     uint32_t un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it) {
-      const int4 itm = g.items[g.item0 + it];
+      const int4 itm = tcs_fetch<OP>(g, it);
       const TcsItem I = tcs_item<OP>(g, itm);
-      const int np = I.np, NL = levels_for(np);
+      const int np = I.np, NL = I.nl;
       // output row r: element n at base[n * stride]
       float4* base = nullptr;
       int64_t stride = 1;
@@ -1105,15 +1189,23 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
           double2* dst = t.splits <= 1 ? t.S : g.ws + t.ws + (int64_t)itm.y * G.a * G.a;
           base = reinterpret_cast<float4*>(dst) + (int64_t)G.a * j;
         }
-      } else {
+      } else if (OP == TCS_ACC) {
         const AccTask& T = g.acc[itm.x];
         const int64_t rg = (int64_t)itm.y * kRows + r;
         if (rg < T.rows) base = reinterpret_cast<float4*>(T.out) + rg;
         stride = T.rows;
         add_first = T.add != 0;
+      } else {
+        const MPTask& t = g.mp[itm.x];
+        const int64_t rg = (int64_t)itm.y * kRows + r;
+        if (rg < (int64_t)t.before * t.after)
+          base = reinterpret_cast<float4*>(t.out) + rg % t.before + (int64_t)t.before * t.a_out * (rg / t.before);
+        stride = t.before;
+        add_first = t.add != 0;
       }
       for (int u = 0; u < I.nunits; ++u, ++un) {
         const int buf = (int)(un & 1);
+        const bool store = u == 0 && !add_first;
         if (!mbar_wait(&sm.bar.exready[buf], (un >> 1) & 1, kSpin) || !mbar_wait(&sm.bar.tfull, un & 1, kSpin)) {
           set_status(status, 17);
           ok = false;
@@ -1122,26 +1214,31 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
         fence_after_sync();
         const int er = (int)sm.ex[buf][r];
         mbar_arrive(&sm.bar.exfree[buf]);
-        const int* fxg =
-            reinterpret_cast<const int*>(tcs_image<OP>(g, itm, u, np) + (size_t)4 * kDig * 3 * np * 32);
+        const int* fxg = reinterpret_cast<const int*>(tcs_image<OP>(g, itm, u, np) +
+                                                      (size_t)tcs_img_steps<OP>(np) * kDig * 3 * np * 32);
         __syncwarp();
         for (int i = lane; i < 64; i += 32) fxw[i] = __ldg(fxg + i);
         __syncwarp();
-        const bool store = u == 0 && !add_first;
-        for (int n0 = 0; n0 < np; n0 += 8) {
+        for (int n0 = 0; n0 < np; n0 += 4) {
+          // the old outputs of these four columns: their loads in flight
+          // together, under the tensor-memory reads
+          float4 old[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e)
+            old[e] = (base && !store && n0 + e < I.ncols) ? base[stride * (n0 + e)] : make_float4(0.f, 0.f, 0.f, 0.f);
           __syncwarp();
-          float vre[8], vim[8], lre[8], lim[8];
-          float lv[kDig][8];
+          float vre[4], vim[4], lre[4], lim[4];
 #pragma unroll
           for (int part = 0; part < 2; ++part) {
+            float lv[kDig][4];
 #pragma unroll
             for (int L = 0; L < kDig; ++L)
-              if (L < NL) tmem_ld8(lane_addr + (uint32_t)(L * 2 * np + part * np + n0), lv[L]);
+              if (L < NL) tmem_ld4(lane_addr + (uint32_t)(L * 2 * np + part * np + n0), lv[L]);
             tmem_wait_ld();
             float* v = part ? vim : vre;
             float* l = part ? lim : lre;
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
+            for (int i = 0; i < 4; ++i) {
               v[i] = lv[0][i];
               l[i] = 0.f;
               if (NL > 1) df_add(v[i], l[i], lv[1][i], 0.f);
@@ -1155,7 +1252,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
           }
           if (!base) continue;
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
+          for (int i = 0; i < 4; ++i) {
             const int col = n0 + i;
             if (col >= I.ncols) continue;
             const int fn = fxw[col];
@@ -1167,11 +1264,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
             } else {
               v = make_float4(scale2(vre[i], sh), scale2(lre[i], sh), scale2(vim[i], sh), scale2(lim[i], sh));
             }
-            float4* o = base + stride * col;
             if (!store) {
-              const float4 p = *o;
-              df_add(v.x, v.y, p.x, p.y);
-              df_add(v.z, v.w, p.z, p.w);
+              df_add(v.x, v.y, old[i].x, old[i].y);
+              df_add(v.z, v.w, old[i].z, old[i].w);
             }
             df_norm(v.x, v.y);
             df_norm(v.z, v.w);
@@ -1179,7 +1274,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
               const float nan = __int_as_float(0x7fffffff);
               v = make_float4(nan, nan, nan, nan);
             }
-            *o = v;
+            base[stride * col] = v;
           }
         }
         fence_before_sync();
@@ -1252,6 +1347,19 @@ cudaError_t launch_hp_tc(const HPTask* tasks, const HpTcGroup* groups, const int
   return launch_tcs<TCS_HP>(g, img_units, first_unit, n_units, s);
 }
 
+cudaError_t launch_mp_tcs(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
+                          const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s) {
+  if (n_tiles <= 0) return cudaSuccess;
+  TcsArgs g{};
+  g.mp = tasks;
+  g.mp_tiles = tiles;
+  g.mp_tasks = tc_tasks;
+  g.item0 = first_tile;
+  g.n_items = n_tiles;
+  g.status = status;
+  return launch_tcs<TCS_MP>(g, nullptr, first_task, n_tasks, s);
+}
+
 cudaError_t launch_acc_tc(const AccTask* tasks, const AccTerm* terms, const int4* items, int64_t first_item,
                           int64_t n_items, int64_t units, const int2* img_units, int64_t first_unit,
                           int64_t n_units, int* status, cudaStream_t s) {
@@ -1270,10 +1378,7 @@ cudaError_t launch_acc_tc(const AccTask* tasks, const AccTerm* terms, const int4
 cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles,
                          const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s) {
   if (n_tiles <= 0) return cudaSuccess;
-  if (oz) {
-    if (n_tasks > 0) k_mp_tc_h<true><<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
-    return launch_tc<true>(tasks, tiles, first_tile, n_tiles, status, s);
-  }
+  if (oz) return launch_mp_tcs(tasks, tiles, first_tile, n_tiles, tc_tasks, first_task, n_tasks, status, s);
   if (n_tasks > 0) k_mp_tc_h<false><<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
   return launch_tc<false>(tasks, tiles, first_tile, n_tiles, status, s);
 }

@@ -495,10 +495,15 @@ def hp_tc_eligible(before, a, after):
     return 16 <= a <= 64 and before * after >= 2 * HP_CHUNK
 
 
+def hp_tc_kc(a):
+    """Reduction length of a tensor-core hole-product chunk (qt_internal.h)."""
+    return 2 * HP_CHUNK if (a + 7) // 8 * 8 > 32 else HP_CHUNK
+
+
 def oz_hole_product(A, B):
     """S(i, j) = sum_k conj(A[b, i, c]) B[b, j, c], k = b + before c, with
     the digit arithmetic of the tensor-core hole products: the reduction in
-    chunks of 64 k, every chunk with its own exponents per row of B (per j)
+    chunks of hp_tc_kc(a) k, every chunk with its own exponents per row of B (per j)
     and of A (per i); complex products as Re = Br Ar + Bi Ai and
     Im = Bi Ar - Br Ai; levels 0..2 exact, levels 3..6 in one float32 sum
     (the fewest accumulators), each chunk scaled by 2^(E_j + F_i) and the
@@ -508,9 +513,10 @@ def oz_hole_product(A, B):
     XB = np.transpose(B, (2, 0, 1)).reshape(-1, B.shape[1])
     K = XA.shape[0]
     S = np.zeros((B.shape[1], a), np.complex128)  # rows j, columns i
-    for k0 in range(0, K, HP_CHUNK):
-        Eb, br, bi = _oz_digits(XB[k0:k0 + HP_CHUNK].T)
-        Fa, ar, ai = _oz_digits(XA[k0:k0 + HP_CHUNK].T)
+    kc = hp_tc_kc(a)
+    for k0 in range(0, K, kc):
+        Eb, br, bi = _oz_digits(XB[k0:k0 + kc].T)
+        Fa, ar, ai = _oz_digits(XA[k0:k0 + kc].T)
         re = np.zeros((br.shape[1], ar.shape[1]))
         im = np.zeros_like(re)
         r3 = np.zeros_like(re)

@@ -19,9 +19,13 @@ TENSOR = 0x8000
 CHUNK = 64
 
 
-def chunk_bytes(a):
+def kc_of(a):
+    return 2 * CHUNK if (a + 7) // 8 * 8 > 32 else CHUNK  # 128 k where four level accumulators are used
+
+
+def chunk_bytes(a, steps):
     ap = (a + 7) // 8 * 8
-    return 4 * 7 * 3 * ap * 16 * 2 + 64 * 4
+    return steps * 7 * 3 * ap * 16 * 2 + 64 * 4
 
 
 def wide_leaf_problem():
@@ -63,7 +67,7 @@ def test_hole_product_groups_and_items(name, plan):
             Abuf, Aoff, bef, a, aft, n, nch, img = (int(x) for x in groups[g][:8])
             mem = [int(m) for m in groups[g][8:8 + n]]
             assert 1 <= n <= min(8, 128 // a)
-            assert nch == -(-bef * aft // CHUNK)
+            assert nch == -(-bef * aft // kc_of(a))
             for m in mem:
                 assert m in stage_tasks
                 ab, ao, _, _, _, _, tb, ta, tf = (int(x) for x in hp[m])
@@ -73,8 +77,8 @@ def test_hole_product_groups_and_items(name, plan):
             gi = sorted((int(z), int(c0), int(c1)) for gg, z, c0, c1 in its if int(gg) == g)
             splits, kchunk = int(hpx[mem[0]][0]), int(hpx[mem[0]][1])
             assert [z for z, _, _ in gi] == list(range(splits))
-            assert kchunk % CHUNK == 0
-            cpi = kchunk // CHUNK
+            assert kchunk % kc_of(a) == 0
+            cpi = kchunk // kc_of(a)
             assert [(c0, c1) for _, c0, c1 in gi] == [(z * cpi, min(nch, (z + 1) * cpi)) for z in range(splits)]
             for m in mem:
                 assert (int(hpx[m][0]), int(hpx[m][1])) == (splits, kchunk)
@@ -89,7 +93,7 @@ def test_hole_product_groups_and_items(name, plan):
         for g, cs in owners.items():
             nch, img, a = int(groups[g][6]), int(groups[g][7]), int(groups[g][3])
             assert sorted(cs) == list(range(nch))
-            spans.append((img, img + nch * chunk_bytes(a)))
+            spans.append((img, img + nch * chunk_bytes(a, kc_of(a) // 16)))
         assert len(spans) == len(img_of)
         spans.sort()
         assert all(e0 <= s1 for (_, e0), (s1, _) in zip(spans, spans[1:]))
@@ -144,7 +148,7 @@ def test_accumulation_items(name, plan):
         # image units: every term of every eligible task once; slots disjoint in B_OZ
         seen = sorted((int(t), int(s)) for t, s in units[atu0:atu0 + natu])
         assert seen == sorted((t, s) for t in eligible for s in range(int(acc[t][7])))
-        spans = sorted((int(imgs[t]), int(imgs[t]) + int(acc[t][7]) * chunk_bytes(int(acc[t][5]))) for t in eligible)
+        spans = sorted((int(imgs[t]), int(imgs[t]) + int(acc[t][7]) * chunk_bytes(int(acc[t][5]), 4)) for t in eligible)
         assert all(e0 <= s1 for (_, e0), (s1, _) in zip(spans, spans[1:]))
         assert all(0 <= s and e <= oz_bytes for s, e in spans)
         for t in range(t0, t0 + nt):
