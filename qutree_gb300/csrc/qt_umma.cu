@@ -687,9 +687,8 @@ struct TcsSmem {
   unsigned char a[2][kOzAStage];
   unsigned char n[2][kTcsNStage];
   Bars bar;
-  uint8_t ex[2][kRows];
-  uint8_t pm[2][2][kRows];
-  int fx[4][64];
+  uint8_t ex[2][kRows];  // the row exponents of the two units in flight
+  int fx[8][64];         // the unit's column exponents, one copy per epilogue warp
 };
 static_assert(sizeof(TcsSmem) <= 232448, "shared memory of the sum-of-products kernel exceeds 227 KB");
 
@@ -946,6 +945,16 @@ struct TcsRow {
   int j;              // HP: column of S_t
 };
 
+// Roles (416 threads): warps 0-3 produce X's digits, one thread per row of
+// the tile (each 16-k step in two halves of eight k; first the row's
+// exponent over the unit's k, then the digits step by step, the next half's
+// loads in flight); warp 4 allocates tensor memory and issues the MMAs from
+// one thread; warps 5-12 read the accumulators and update the outputs,
+// warp w reading lanes 32 (w % 4).. (tensor memory's lane quarter of its
+// sub-partition) for half (w - 5) / 4 of the columns.  Every wait is bounded:
+// a wait that runs out sets the status word, and the CTA drains its issued
+// MMAs, frees tensor memory and returns.
+constexpr int kTcsProducers = 128, kTcsEpilogue = 256;
 template <int OP>
 __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
   extern __shared__ __align__(128) unsigned char tcs_raw[];
@@ -957,27 +966,26 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
 
   if (tid == 0) {
     for (int s = 0; s < 2; ++s) {
-      mbar_init(&sm.bar.full[s], 256);
+      mbar_init(&sm.bar.full[s], kTcsProducers);
       mbar_init(&sm.bar.empty[s], 1);
-      mbar_init(&sm.bar.exready[s], 128);
-      mbar_init(&sm.bar.exfree[s], 128);
-      mbar_init(&sm.bar.pmax[s], 256);
+      mbar_init(&sm.bar.exready[s], kTcsProducers);
+      mbar_init(&sm.bar.exfree[s], kTcsEpilogue);
     }
     mbar_init(&sm.bar.tfull, 1);
-    mbar_init(&sm.bar.tempty, 128);
+    mbar_init(&sm.bar.tempty, kTcsEpilogue);
     mbar_init(&sm.bar.drain, 1);
     mbar_fence_init();
   }
-  if (warp == 12) tmem_alloc(&sm.bar.tmem, 512u);
+  if (warp == 4) tmem_alloc(&sm.bar.tmem, 512u);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
   const uint32_t tmem = sm.bar.tmem;
   bool ok = true;
 
-  if (warp < 8) {
-    // ---------------- producers: two per row, each 8 k of every 16-k step ----------------
-    const int r = tid & (kRows - 1), h = tid >> 7;
+  if (warp < 4) {
+    // ---------------- producers: one per row ----------------
+    const int r = tid;
     uint32_t q = 0, un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it) {
       const int4 itm = tcs_fetch<OP>(g, it);
@@ -1024,9 +1032,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
         const uint32_t use_par = (un >> 1) & 1;
         const float4* X = OP != TCS_ACC ? R.src : reinterpret_cast<const float4*>(g.terms[tfirst + u].X) + R.rg;
         const int kbase = OP == TCS_HP ? (itm.z + u) * I.nks * kChunkK : 0;
-        // this thread's values of step ks: k = kbase + 16 ks + 8 h + i
-        auto load8 = [&](float4 (&x)[8], int ks) {
-          const int k0 = kbase + ks * kChunkK + h * 8;
+        // the eight values of half hh of step ks: k = kbase + 16 ks + 8 hh + i
+        auto load8 = [&](float4 (&x)[8], int ks, int hh) {
+          const int k0 = kbase + ks * kChunkK + hh * 8;
           if (OP == TCS_HP) {
             KWalk w(min(k0, K), before);
 #pragma unroll
@@ -1040,40 +1048,28 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
               x[i] = (R.valid && k0 + i < K) ? __ldg(X + rows * (k0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         };
-        int m = 1;
+        // the row's largest exponent over the unit's k, eight loads in flight
+        int eb = 1;
         if (R.valid)
-          for (int ks = 0; ks < I.nks; ++ks) {
+          for (int h8 = 0; h8 < 2 * I.nks; ++h8) {
             float4 x[8];
-            load8(x, ks);
+            load8(x, h8 >> 1, h8 & 1);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) m = max(m, max(fexp(x[i].x), fexp(x[i].z)));
+            for (int i = 0; i < 8; ++i) eb = max(eb, max(fexp(x[i].x), fexp(x[i].z)));
           }
-        sm.pm[buf][h][r] = (uint8_t)m;
-        mbar_arrive(&sm.bar.pmax[buf]);
-        if (!mbar_wait(&sm.bar.pmax[buf], use_par, kSpin)) {
-          set_status(status, 19);
+        // the epilogue of the unit two back has read ex of this buffer
+        if (!mbar_wait(&sm.bar.exfree[buf], use_par ^ 1, kSpin)) {
+          set_status(status, 18);
           ok = false;
           break;
         }
-        const int eb = max(sm.pm[buf][0][r], sm.pm[buf][1][r]);
-        if (h == 0) {
-          if (!mbar_wait(&sm.bar.exfree[buf], use_par ^ 1, kSpin)) {
-            set_status(status, 18);
-            ok = false;
-            break;
-          }
-          sm.ex[buf][r] = (uint8_t)eb;
-          mbar_arrive(&sm.bar.exready[buf]);
-        }
+        sm.ex[buf][r] = (uint8_t)eb;
+        mbar_arrive(&sm.bar.exready[buf]);
         const unsigned char* img = tcs_image<OP>(g, itm, u, I.np);
         float4 nx[8];
-        load8(nx, 0);
+        load8(nx, 0, 0);
         for (int ks = 0; ks < I.nks; ++ks, ++q) {
           const int s = q & 1;
-          float4 x[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) x[i] = nx[i];
-          if (ks + 1 < I.nks) load8(nx, ks + 1);
           if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
             set_status(status, 11);
             ok = false;
@@ -1086,27 +1082,35 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
             bulk_g2s(sm.n[s], img + (size_t)ks * nbytes, nbytes, &sm.bar.full[s]);
           }
           unsigned char* As = sm.a[s];
-          uint32_t wr[kDig][4], wi[kDig][4];
+#pragma unroll 1
+          for (int hh = 0; hh < 2; ++hh) {
+            float4 x[8];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
-            digits_f32(x[2 * i].x, x[2 * i].y, eb, d0);
-            digits_f32(x[2 * i + 1].x, x[2 * i + 1].y, eb, d1);
-            digits_f32(x[2 * i].z, x[2 * i].w, eb, e0);
-            digits_f32(x[2 * i + 1].z, x[2 * i + 1].w, eb, e1);
+            for (int i = 0; i < 8; ++i) x[i] = nx[i];
+            const int nk = ks + hh;  // the next half: (ks, 1) or (ks + 1, 0)
+            if (nk < I.nks) load8(nx, nk, hh ^ 1);
+            uint32_t wr[kDig][4], wi[kDig][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+              float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
+              digits_f32(x[2 * i].x, x[2 * i].y, eb, d0);
+              digits_f32(x[2 * i + 1].x, x[2 * i + 1].y, eb, d1);
+              digits_f32(x[2 * i].z, x[2 * i].w, eb, e0);
+              digits_f32(x[2 * i + 1].z, x[2 * i + 1].w, eb, e1);
+#pragma unroll
+              for (int d = 0; d < kDig; ++d) {
+                wr[d][i] = pack_bf16(d0[d], d1[d]);
+                wi[d][i] = pack_bf16(e0[d], e1[d]);
+              }
+            }
+            const int off = core_off(r, hh, kRows);
 #pragma unroll
             for (int d = 0; d < kDig; ++d) {
-              wr[d][i] = pack_bf16(d0[d], d1[d]);
-              wi[d][i] = pack_bf16(e0[d], e1[d]);
+              *reinterpret_cast<uint4*>(As + (2 * d + 0) * kOzAPlane + off) =
+                  make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
+              *reinterpret_cast<uint4*>(As + (2 * d + 1) * kOzAPlane + off) =
+                  make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
             }
-          }
-          const int off = core_off(r, h, kRows);
-#pragma unroll
-          for (int d = 0; d < kDig; ++d) {
-            *reinterpret_cast<uint4*>(As + (2 * d + 0) * kOzAPlane + off) =
-                make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
-            *reinterpret_cast<uint4*>(As + (2 * d + 1) * kOzAPlane + off) =
-                make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
           }
           fence_proxy_async();
           mbar_arrive(&sm.bar.full[s]);
@@ -1114,7 +1118,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
         if (!ok) break;
       }
     }
-  } else if (warp == 12) {
+  } else if (warp == 4) {
     // ---------------- MMA issue (one thread) ----------------
     if (lane == 0) {
       uint32_t q = 0, un = 0;
@@ -1166,17 +1170,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
       commit(&sm.bar.drain);
       if (!mbar_wait(&sm.bar.drain, 0, kSpin)) set_status(status, 16);
     }
-  } else if (warp < 12) {
-    // ---------------- epilogue: warp 8 + qd reads lanes 32 qd .. ----------------
-    const int qd = warp - 8;
+  } else {
+    // ---------------- epilogue: warps 5..12, lane quarter w % 4, column half (w - 5) / 4 ----------------
+    const int qd = warp & 3, half = (warp - 5) >> 2;
     const int r = 32 * qd + lane;
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * qd) << 16);
-    int* fxw = sm.fx[qd];
+    int* fxw = sm.fx[warp - 5];
     uint32_t un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it) {
       const int4 itm = tcs_fetch<OP>(g, it);
       const TcsItem I = tcs_item<OP>(g, itm);
       const int np = I.np, NL = I.nl;
+      const int c0 = half * (np >> 1), c1 = c0 + (np >> 1);  // this warp's columns
       // output row r: element n at base[n * stride]
       float4* base = nullptr;
       int64_t stride = 1;
@@ -1219,7 +1224,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
         __syncwarp();
         for (int i = lane; i < 64; i += 32) fxw[i] = __ldg(fxg + i);
         __syncwarp();
-        for (int n0 = 0; n0 < np; n0 += 4) {
+        for (int n0 = c0; n0 < c1; n0 += 4) {
           // the old outputs of these four columns: their loads in flight
           // together, under the tensor-memory reads
           float4 old[4];
@@ -1284,7 +1289,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
   }
   fence_before_sync();
   __syncthreads();
-  if (warp == 12) {
+  if (warp == 4) {
     fence_after_sync();
     tmem_dealloc(tmem, 512u);
   }
