@@ -515,9 +515,8 @@ class Builder {
 
   // Tensor-core hole products of the stage: the qualifying tasks (tc) in
   // groups of up to 128 / a tasks sharing A, one image of A per distinct A in
-  // the stage's part of B_OZ, and work items of about equal length: ranges of
-  // cpi chunks, cpi chosen so that the stage has about two items per SM.  A
-  // task cut into several ranges gets workspace slots for its partial tiles.
+  // the stage's part of B_OZ, and one work item per chunk of the reduction.
+  // A task of several chunks gets workspace slots for its partial tiles.
   // Returns whether any task was cut.
   bool hp_tensor_items(int64_t t0, int64_t t1, const std::vector<char>& tc, int64_t& ws) {
     const int64_t g0 = (int64_t)P.hp_tc_groups.size();
@@ -553,16 +552,14 @@ class Builder {
       g.member[g.n++] = (int)t;
     }
     const int64_t g1 = (int64_t)P.hp_tc_groups.size();
-    // item length in 64-k units: about two items per SM over the stage
-    int64_t units = 0;
-    for (int64_t g = g0; g < g1; ++g)
-      units += (int64_t)P.hp_tc_groups[g].nchunks * (hp_tc_kc((P.hp_tc_groups[g].a + 7) & ~7) / kHpTcChunk);
-    const int64_t target = std::max<int64_t>(1, (units + 2 * 152 - 1) / (2 * 152));
+    // one chunk per item: every unit stores its partial tiles (an item of
+    // several chunks would add each chunk into them, whose loads of rows of
+    // S stall the epilogue longer than the partial-tile sum takes)
     bool split = false;
     for (int64_t g = g0; g < g1; ++g) {
       const Plan::SHpTcGroup& G = P.hp_tc_groups[g];
       const int kc = hp_tc_kc((G.a + 7) & ~7);
-      const int cpi = (int)std::max<int64_t>(1, target / (kc / kHpTcChunk));
+      const int cpi = 1;
       const int splits = (G.nchunks + cpi - 1) / cpi;
       for (int m = 0; m < G.n; ++m) {
         Plan::SHP& h = P.hp[G.member[m]];
