@@ -162,6 +162,13 @@ def _rho_weighted_err(tree, dpsi, ref, rho):
     return num / den
 
 
+# DRAM bytes per sweep of the sum-of-products kernels (dram__bytes_read.sum +
+# dram__bytes_write.sum over all launches of one sweep of the 64-mode
+# workload, one ncu capture; profiles/launches_sweep_64mode_compressed_df64_tc.md)
+TRAFFIC = {}
+TRAFFIC_SOURCE = "ncu capture of one sweep (profiles/launches_sweep_64mode_compressed_df64_tc.md)"
+
+
 def measured_peaks():
     """HBM GB/s and bf16 TFLOP/s (burst) measured on the GB300s, or
     the stated fallback when the file is absent."""
@@ -374,27 +381,26 @@ def run_ours(args, ws, rank, local):
             d["launches"] += 1 / reps
     fp64_peak = hrep.ctx.fp64_peak()
     df64_peak = hrep.ctx.df64_peak()
-    names = {0: "k_mp_tc + k_mp (mode products: tcgen05 digit MMAs, diagonal ones on the FP32 pipe)",
-             1: "k_hp (hole products)", 2: "k_acc (last-mode accumulate)",
+    names = {0: "k_tcs<MP> + k_mp (mode products)", 1: "k_tcs<HP> + k_hp (hole products)",
+             2: "k_tcs<ACC> + k_acc (last-mode accumulations)",
              3: "k_lin (matrix sums)", 4: "k_eig (density inverses)", 5: "k_proj (projectors)",
              6: "k_cvt (precision conversions)", 7: "k_grad (gradient preparation)",
              8: "k_mm (small matrix products)"}
+    # stage kinds whose qualifying tasks run on the tensor cores (each stage
+    # timed with its image pre-pass and, for the hole products, its partial sums)
+    TENSOR_KINDS = (0, 1, 2)
     dom = max(per_kind, key=lambda k: per_kind[k]["ms"])
     d = per_kind[dom]
-    achieved = d["flops"] / (d["ms"] * 1e-3) / 1e12
-    # the tensor-core mode products: 28 digit pairs x 4 real bf16 products per
-    # complex multiply-add, i.e. 28 bf16 flops per complex128-equivalent flop
+    c128_tflops = d["flops"] / (d["ms"] * 1e-3) / 1e12
     peaks = measured_peaks()
-    mp = per_kind.get(0)
-    tensor = None
-    if mp and mp["ms"] > 0:
-        bf16 = 28.0 * mp["flops"] / (mp["ms"] * 1e-3) / 1e12
-        tensor = {"kernel": names[0], "ms": mp["ms"], "bf16_tflops": bf16, "bf16_peak": peaks["bf16_tflops"],
-                  "frac": bf16 / peaks["bf16_tflops"], "peak_source": peaks["source"],
-                  "complex128_equivalent_tflops": mp["flops"] / (mp["ms"] * 1e-3) / 1e12}
+    # digit arithmetic: 28 digit pairs x 2 parts x 4 real products ... = 28 bf16
+    # tensor flops per complex128-equivalent flop (8 per complex multiply-add)
+    bf16_tflops = 28.0 * c128_tflops
     total_stage_ms = sum(v["ms"] for v in per_kind.values())
     kernels = {names[k]: {"ms": round(v["ms"], 3), "share": round(v["ms"] / total_stage_ms, 4),
-                          "tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4),
+                          "complex128_equivalent_tflops": round(v["flops"] / max(v["ms"], 1e-9) / 1e9, 4),
+                          **({"bf16_tensor_tflops": round(28.0 * v["flops"] / max(v["ms"], 1e-9) / 1e9, 2)}
+                             if k in TENSOR_KINDS else {}),
                           "launches_per_sweep": int(round(v["launches"]))}
                for k, v in sorted(per_kind.items())}
     hrep.close()
@@ -601,16 +607,23 @@ def run_ours(args, ws, rank, local):
                                 "dpsi_rel_rho_weighted": _rho_weighted_err(tree, head_dpsi, plain_dpsi, plain_rho)
                                 if head_dpsi is not None else None},
         "flops_per_sweep": {"reference_algorithm": stats["ref_flops"], "executed": stats["exec_flops"]},
-        "roofline": {"bound": "fp32 pipe (double-float arithmetic)", "kernel": names[dom],
-                     "achieved": achieved, "unit": "TFLOP/s (complex128-equivalent)",
-                     "peak": df64_peak, "frac": achieved / df64_peak,
-                     "peak_source": "measured in this run: the kernels' double-float complex multiply-add on "
-                                    "register accumulators (qt_probe_df64_peak); HBM and bf16 peaks of "
-                                    "MEASURED_PEAKS.json do not bound this path (DRAM < 2% busy)",
-                     "fp64_pipe_peak": fp64_peak,
-                     "speedup_over_fp64_pipe": achieved / fp64_peak,
-                     "traffic": None, "kernels": kernels,
-                     "tensor_core_mode_products": tensor},
+        "roofline": ({"bound": "tensor", "kernel": names[dom], "achieved": bf16_tflops,
+                      "peak": peaks["bf16_tflops"], "unit": "TFLOP/s (bf16 digit products on the tensor cores)",
+                      "frac": bf16_tflops / peaks["bf16_tflops"],
+                      "peak_source": peaks["source"] + ", bf16 burst",
+                      "achieved_note": "28 bf16 tensor flops per complex128-equivalent flop of the reference "
+                                       "algorithm (seven digits per operand, 28 digit pairs)",
+                      "complex128_equivalent_tflops": c128_tflops,
+                      "df64_fp32_pipe_peak_tflops": df64_peak,
+                      "speedup_over_df64_fp32_pipe_peak": c128_tflops / df64_peak,
+                      "fp64_pipe_peak_tflops": fp64_peak,
+                      "traffic": TRAFFIC.get(dom), "traffic_unit": "bytes per sweep (all launches of the kernel)",
+                      "traffic_source": TRAFFIC_SOURCE, "kernels": kernels}
+                     if dom in TENSOR_KINDS else
+                     {"bound": "fp32 pipe (double-float arithmetic)", "kernel": names[dom], "achieved": c128_tflops,
+                      "unit": "TFLOP/s (complex128-equivalent)", "peak": df64_peak, "frac": c128_tflops / df64_peak,
+                      "peak_source": "measured in this run (qt_probe_df64_peak)", "traffic": None,
+                      "kernels": kernels}),
         "clocks": clocks,
         "gpu_launches": launches,
     }

@@ -1,46 +1,22 @@
-// qt_umma.cu -- mode products of the mixed-precision plans on the
+// qt_umma.cu -- the contractions of the mixed-precision plans on the
 // fifth-generation tensor cores (tcgen05.mma, accumulators in tensor memory).
 //
-// out[b, j, c] = alpha sum_a h(j, a) in[b, a, c] is the GEMM Y = X H^T with
-// rows r = (b, c): X is R x K (K = a_in), H^T is K x N (N = a_out), K, N <= 64.
-// A CTA owns 128 consecutive rows at a time (one M = 128 accumulator tile)
-// and all N columns; the complex product is four real MMAs per operand pair,
-//   Y_re += X_re H_re^T - X_im H_im^T,   Y_im += X_re H_im^T + X_im H_re^T,
-// the minus sign by the instruction's negate-A bit.
+// Double-float plans (QT_PREC_DF64_TC): mode products, hole products and
+// last-index accumulations run on one sum-of-products kernel (k_tcs, its
+// design above it).  Every operand row is scaled by the power of two 2^-E
+// of its largest exponent and cut into seven signed digits by error-free
+// splits x_s = fl(fl(r + sigma_s) - sigma_s), sigma_s = 1.5 * 2^(16 - 7s):
+// x_s is r rounded to a multiple of 2^(-7(s+1)), r - x_s is exact, the
+// value's low word joins from s = 3.  The digit integers
+// q_s = x_s 2^(7(s+1)) have |q_s| <= 128, so q_s 2^(-7s) is exact in bf16 and
+// every digit product is exact.  Pairs with s + t <= 6 are summed in fp32
+// accumulators, one per level L = s + t, as far as tensor memory holds them
+// (the last taking the remaining levels together); the epilogue adds the
+// levels in double-float and scales by 2^(E_row + F_column).
 //
-// Two arithmetics share the kernel:
-//  * OZ (double-float plans, QT_PREC_DF64_TC): every operand row (of X, resp.
-//    of h) is scaled by the power of two 2^-E of its largest exponent and cut
-//    into seven signed digits by error-free splits
-//    x_s = fl(fl(r + sigma_s) - sigma_s), sigma_s = 1.5 * 2^(16 - 7s): x_s is
-//    r rounded to a multiple of 2^(-7(s+1)), r - x_s is exact, the value's low
-//    word joins from s = 3.  The digit integers q_s = x_s 2^(7(s+1)) have
-//    |q_s| <= 128, so q_s 2^(-7s) is exact in bf16 and every digit product is
-//    exact.  Pairs with s + t <= 6 are summed in fp32 accumulators, one per
-//    level L = s + t (sums of at most 7 * 2 * 64 * 128^2 < 2^24 units of the
-//    level: exact) as far as tensor memory holds them -- NL = min(7, 512 /
-//    (2 Np)) accumulators for Np padded output columns: all seven levels for
-//    Np <= 32, five for Np = 48, four for Np = 64 -- the last one taking the
-//    remaining levels together; its fp32 rounding is the method's error
-//    beyond the digits' truncation (2^-49 of the row scale).  The epilogue
-//    adds the levels in double-float and scales by 2^(E_row + F_j); the
-//    task's coefficient is already in the h operand.
-//  * TF (complex64 plans, QT_PREC_TF32X3): X and h (fp32) split into TF32
-//    halves hi + lo; hi*hi + hi*lo + lo*hi accumulate in one fp32 sum per
-//    output (split-TF32, 3 passes).
-//
-// Roles (416 threads): warps 0-7 produce the operand X of each 16-wide
-// k-chunk into a two-stage shared-memory ring (two threads per row, each
-// taking half of the row: first the row's exponent over all of K, then the
-// digits / TF32 halves chunk by chunk, the next chunk's loads in flight);
-// warp 12 allocates tensor memory, loads the h operand of the unit (prepared
-// once per stage by a pre-pass in the exact shared-memory image) with bulk
-// copies, and issues the MMAs from one thread; warps 8-11 read the
-// accumulators (warp 8 + q owns tensor-memory lanes 32q..32q+31, i.e. rows
-// 32q..) and write the outputs.  A CTA takes a contiguous range of 128-row
-// tiles, so consecutive tiles mostly share the task and its h.  Every wait
-// is bounded: a wait that runs out sets the status word, and the CTA drains
-// its issued MMAs, frees tensor memory and returns.
+// Complex64 plans (QT_PREC_TF32X3): the mode products as split-TF32 (k_mp_tf):
+// X and h (fp32) split into TF32 halves hi + lo; hi*hi + hi*lo + lo*hi
+// accumulate in one fp32 sum per output (3 passes).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -55,44 +31,32 @@ namespace {
 using namespace tc05;
 
 constexpr int kRows = 128;                 // rows per tile (M)
-constexpr int kDig = 7;                    // digits per value (OZ)
-constexpr int kThreadsTc = 416;            // 8 producer warps, 4 epilogue warps, 1 MMA warp
+constexpr int kDig = 7;                    // digits per value (double-float plans)
+constexpr int kThreadsTc = 416;            // thirteen warps (roles per kernel below)
 constexpr uint64_t kSpin = 2000000000ull;  // ns before a wait gives up (2 s)
 constexpr int kChunkK = 16;                // k per ring stage
 
-// OZ: a digit plane of one stage: 128 rows x 16 k bf16 (core layout [kc][g][8][8])
+// a digit plane of one 16-k step: 128 rows x 16 k bf16 (core layout [kc][g][8][8])
 constexpr int kOzAPlane = kRows * kChunkK * 2;        // 4096 bytes
-constexpr int kOzAStage = kDig * 2 * kOzAPlane;       // 57344
-constexpr int kOzBMax = 4 * kDig * 2 * 64 * 32;       // 114688: K 64, N 64
+constexpr int kOzAStage = kDig * 2 * kOzAPlane;       // 57344: seven digits, re and im
 // TF: a TF32 plane of one stage: 128 rows x 16 k fp32 (core layout [kc][g][8][4])
 constexpr int kTfAPlane = kRows * kChunkK * 4;        // 8192 bytes
 constexpr int kTfAStage = 4 * kTfAPlane;              // hi_re, hi_im, lo_re, lo_im
 constexpr int kTfBMax = 4 * 4 * 64 * 64;              // 65536: K 64, N 64
-static_assert(kOzBMax + 64 * 4 <= kMpOzImageBytes && kTfBMax <= kMpOzImageBytes, "operand image slot too small");
-
-template <bool OZ>
-struct Cfg {
-  static constexpr int AStage = OZ ? kOzAStage : kTfAStage;
-  static constexpr int BMax = OZ ? kOzBMax : kTfBMax;
-  static constexpr int BHeader = kOzBMax;  // F_j (OZ) follow the digit planes in the global image
-};
+static_assert(kTfBMax <= kMpOzImageBytes, "operand image slot too small");
 
 struct Bars {
-  uint64_t full[2], empty[2], exready[2], exfree[2], pmax[2], tfull, tempty, bfull, drain;
+  uint64_t full[2], empty[2], exready[2], exfree[2], tfull, tempty, bfull, drain;
   uint32_t tmem;
   int pad;
 };
 
-template <bool OZ>
-struct TcSmem {
-  unsigned char b[Cfg<OZ>::BMax];
-  unsigned char a[2][Cfg<OZ>::AStage];
+struct TfSmem {
+  unsigned char b[kTfBMax];
+  unsigned char a[2][kTfAStage];
   Bars bar;
-  uint8_t ex[2][kRows];     // biased row exponents (OZ) of the two units in flight
-  uint8_t pm[2][2][kRows];  // the two halves' partial row exponents
-  int fx[4][64];            // column exponents of h, one copy per epilogue warp
 };
-static_assert(sizeof(TcSmem<true>) <= 232448, "shared memory of the digit kernel exceeds 227 KB");
+static_assert(sizeof(TfSmem) <= 232448, "shared memory of the split-TF32 kernel exceeds 227 KB");
 
 __device__ __forceinline__ int fexp(float v) { return (__float_as_int(v) >> 23) & 0xff; }
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((k + 127) << 23); }
@@ -164,80 +128,45 @@ __device__ __forceinline__ void set_status(int* status, int code) {
   if (status) atomicCAS(status, 0, code);
 }
 
-// Write element (j, k) of H^T, value v, into an operand image: OZ
-// [ks][digit][re/im][core layout Np x 16 k] bf16 (row exponent fj), TF
+// Write element (j, k) of H^T, value v, into the split-TF32 operand image
 // [ks][hi_re, hi_im, lo_re, lo_im][core layout Np x 16 k] fp32.
-template <bool OZ>
-__device__ __forceinline__ void put_image(unsigned char* img, int Np, int j, int k, float4 v, int fj) {
-  const int planes = OZ ? kDig * 2 : 4;
-  const int esz = OZ ? 2 : 4;
-  const int plane_bytes = Np * kChunkK * esz;
+__device__ __forceinline__ void put_image_tf(unsigned char* img, int Np, int j, int k, float4 v) {
+  const int plane_bytes = Np * kChunkK * 4;
   const int ks = k / kChunkK, kk = k % kChunkK;
-  const int per = 16 / esz;  // elements per core row
-  const int off = core_off(j, kk / per, Np) + (kk % per) * esz;
-  unsigned char* base = img + (size_t)ks * planes * plane_bytes;
-  if (OZ) {
-    float dr[kDig], di[kDig];
-    digits_f32(v.x, v.y, fj, dr);
-    digits_f32(v.z, v.w, fj, di);
-#pragma unroll
-    for (int d = 0; d < kDig; ++d) {
-      *reinterpret_cast<uint16_t*>(base + (size_t)(2 * d + 0) * plane_bytes + off) =
-          (uint16_t)(__float_as_uint(dr[d]) >> 16);
-      *reinterpret_cast<uint16_t*>(base + (size_t)(2 * d + 1) * plane_bytes + off) =
-          (uint16_t)(__float_as_uint(di[d]) >> 16);
-    }
-  } else {
-    uint32_t hr, lr, hi_, li;
-    tf32_split(v.x, hr, lr);
-    tf32_split(v.z, hi_, li);
-    *reinterpret_cast<uint32_t*>(base + 0 * plane_bytes + off) = hr;
-    *reinterpret_cast<uint32_t*>(base + 1 * plane_bytes + off) = hi_;
-    *reinterpret_cast<uint32_t*>(base + 2 * plane_bytes + off) = lr;
-    *reinterpret_cast<uint32_t*>(base + 3 * plane_bytes + off) = li;
-  }
-}
-
-// alpha h: the operand images carry the task's coefficient, so the epilogue
-// multiplies by nothing but powers of two
-template <bool OZ>
-__device__ __forceinline__ float4 scaled_h(double2 alpha, float4 v) {
-  if (alpha.x == 1.0 && alpha.y == 0.0) return v;
-  return OZ ? DF64::mul(DF64::coef(alpha), v) : C32::mul(C32::coef(alpha), v);
+  const int off = core_off(j, kk / 4, Np) + (kk % 4) * 4;
+  unsigned char* base = img + (size_t)ks * 4 * plane_bytes;
+  uint32_t hr, lr, hi_, li;
+  tf32_split(v.x, hr, lr);
+  tf32_split(v.z, hi_, li);
+  *reinterpret_cast<uint32_t*>(base + 0 * plane_bytes + off) = hr;
+  *reinterpret_cast<uint32_t*>(base + 1 * plane_bytes + off) = hi_;
+  *reinterpret_cast<uint32_t*>(base + 2 * plane_bytes + off) = lr;
+  *reinterpret_cast<uint32_t*>(base + 3 * plane_bytes + off) = li;
 }
 
 // ---------------------------------------------------------------------------
-// pre-pass of the mode products: the operand image of alpha h for every task
-// of the stage, H^T rows j (N, padded to Np = 16 ceil(N / 16)), k < Kp
-// zero-padded, then the rows' exponents F_j (OZ)
+// pre-pass of the split-TF32 mode products: the operand image of alpha h for
+// every task of the stage, H^T rows j (N, padded to Np = 16 ceil(N / 16)),
+// k < Kp zero-padded
 // ---------------------------------------------------------------------------
-template <bool OZ>
-__global__ void __launch_bounds__(256) k_mp_tc_h(const MPTask* __restrict__ tasks, const int* __restrict__ ids,
+__global__ void __launch_bounds__(256) k_mp_tf_h(const MPTask* __restrict__ tasks, const int* __restrict__ ids,
                                                  int64_t first) {
   const MPTask t = tasks[ids[first + blockIdx.x]];
   unsigned char* img = static_cast<unsigned char*>(t.oz_h);
   const float4* __restrict__ h = reinterpret_cast<const float4*>(t.h);
   const int K = t.a_in, N = t.a_out;
   const int Np = (N + 15) & ~15, Kp = (K + 15) & ~15;
-  __shared__ int fx[64];
-  if (OZ) {
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) fx[i] = 1;
-    __syncthreads();
-    for (int e = threadIdx.x; e < N * K; e += blockDim.x) {
-      const int j = e % N, a = e / N;
-      const float4 v = scaled_h<OZ>(t.alpha, h[j + (int64_t)N * a]);
-      atomicMax(&fx[j], max(fexp(v.x), fexp(v.z)));
-    }
-    __syncthreads();
-  }
+  const bool one = t.alpha.x == 1.0 && t.alpha.y == 0.0;
+  const float4 cf = C32::coef(t.alpha);
   for (int e = threadIdx.x; e < Np * Kp; e += blockDim.x) {
     const int j = e % Np, k = e / Np;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (j < N && k < K) v = scaled_h<OZ>(t.alpha, h[j + (int64_t)N * k]);
-    put_image<OZ>(img, Np, j, k, v, OZ ? fx[j < N ? j : 0] : 0);
+    if (j < N && k < K) {
+      v = h[j + (int64_t)N * k];
+      if (!one) v = C32::mul(cf, v);
+    }
+    put_image_tf(img, Np, j, k, v);
   }
-  if (OZ)
-    for (int i = threadIdx.x; i < 64; i += blockDim.x) reinterpret_cast<int*>(img + Cfg<true>::BHeader)[i] = fx[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -267,17 +196,25 @@ __device__ __forceinline__ TcUnit make_unit(const MPTask* tasks, int task) {
 }
 
 // ---------------------------------------------------------------------------
-// the tensor-core kernel
+// Split-TF32 mode products (complex64 plans).  out[b, j, c] =
+// alpha sum_a h(j, a) in[b, a, c] is the GEMM Y = X H^T with rows r = (b, c)
+// (K = a_in, N = a_out <= 64); four real MMAs per operand pair,
+//   Y_re += X_re H_re^T - X_im H_im^T,   Y_im += X_re H_im^T + X_im H_re^T,
+// the minus sign by the instruction's negate-A bit.  Roles (416 threads):
+// warps 0-7 produce X's TF32 halves of each 16-k step into a two-stage ring
+// (two threads per row, eight k each); warp 12 allocates tensor memory, loads
+// the h image of the unit (bulk copies, once per change of task) and issues
+// the MMAs from one thread; warps 8-11 read the accumulators (warp 8 + q:
+// lanes 32q..) and write the outputs.  A CTA takes a contiguous range of
+// 128-row tiles.  Every wait is bounded: a wait that runs out sets the status
+// word, and the CTA drains its issued MMAs, frees tensor memory and returns.
 // ---------------------------------------------------------------------------
-template <bool OZ>
-__global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restrict__ tasks,
+__global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tf(const MPTask* __restrict__ tasks,
                                                           const int2* __restrict__ tiles, int64_t tile0,
                                                           int64_t n_tiles, int* status) {
-  typedef TcSmem<OZ> Sm;
   extern __shared__ __align__(128) unsigned char tc_raw[];
-  Sm& sm = *reinterpret_cast<Sm*>(tc_raw);
+  TfSmem& sm = *reinterpret_cast<TfSmem*>(tc_raw);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  // contiguous tile range of this CTA
   const int64_t per = n_tiles / gridDim.x, extra = n_tiles % gridDim.x;
   const int64_t my0 = blockIdx.x * per + min((int64_t)blockIdx.x, extra);
   const int64_t my1 = my0 + per + (blockIdx.x < extra ? 1 : 0);
@@ -286,9 +223,6 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
     for (int s = 0; s < 2; ++s) {
       mbar_init(&sm.bar.full[s], 256);
       mbar_init(&sm.bar.empty[s], 1);
-      mbar_init(&sm.bar.exready[s], 128);
-      mbar_init(&sm.bar.exfree[s], 128);
-      mbar_init(&sm.bar.pmax[s], 256);
     }
     mbar_init(&sm.bar.tfull, 1);
     mbar_init(&sm.bar.tempty, 128);
@@ -296,8 +230,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
     mbar_init(&sm.bar.drain, 1);
     mbar_fence_init();
   }
-  const uint32_t ncols = OZ ? 512u : 128u;
-  if (warp == 12) tmem_alloc(&sm.bar.tmem, ncols);
+  if (warp == 12) tmem_alloc(&sm.bar.tmem, 128u);
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
@@ -305,121 +238,58 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
   bool ok = true;
 
   if (warp < 8) {
-    // ---------------- producers: two per row, each half of every chunk ----------------
+    // ---------------- producers: two per row, eight k of every step each ----------------
     const int r = tid & (kRows - 1), h = tid >> 7;
-    uint32_t q = 0;   // chunk counter over all units
-    uint32_t un = 0;  // unit counter
-    for (int64_t it = my0; it < my1 && ok; ++it, ++un) {
+    uint32_t q = 0;
+    for (int64_t it = my0; it < my1 && ok; ++it) {
       const int2 tl = tiles[tile0 + it];
-      {
-        const TcUnit U = make_unit(tasks, tl.x);
-        const int K = U.K;
-        const int64_t rg = (int64_t)tl.y * kRows + r;
-        const bool valid = rg < U.nrows;
-        const int64_t b = valid ? rg % U.before : 0, c = valid ? rg / U.before : 0;
-        const float4* base = U.in + b + U.before * (int64_t)K * c;
-        const int buf = (int)(un & 1);
-        const uint32_t use_par = (un >> 1) & 1;  // parity of this buffer's use
-        int eb = 0;
-        if (OZ) {
-          // the row's largest exponent: each half of the row, eight loads in flight
-          const int kh = (K + 1) >> 1, a_lo = h * kh, a_hi = min(K, a_lo + kh);
-          int m = 1;
-          if (valid)
-            for (int a0 = a_lo; a0 < a_hi; a0 += 8) {
-              float4 v[8];
+      const TcUnit U = make_unit(tasks, tl.x);
+      const int K = U.K;
+      const int64_t rg = (int64_t)tl.y * kRows + r;
+      const bool valid = rg < U.nrows;
+      const int64_t b = valid ? rg % U.before : 0, c = valid ? rg / U.before : 0;
+      const float4* base = U.in + b + U.before * (int64_t)K * c;
+      const int nks = (K + kChunkK - 1) / kChunkK;
+      // this thread's eight values of step ks; the next step's loads are in
+      // flight while the current one is split
+      auto load8 = [&](float4 (&x)[8], int ks) {
 #pragma unroll
-              for (int i = 0; i < 8; ++i)
-                v[i] = a0 + i < a_hi ? __ldg(base + U.before * (a0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-              for (int i = 0; i < 8; ++i) m = max(m, max(fexp(v[i].x), fexp(v[i].z)));
-            }
-          sm.pm[buf][h][r] = (uint8_t)m;
-          mbar_arrive(&sm.bar.pmax[buf]);
-          if (!mbar_wait(&sm.bar.pmax[buf], use_par, kSpin)) {
-            set_status(status, 9);
-            ok = false;
-            break;
-          }
-          eb = max(sm.pm[buf][0][r], sm.pm[buf][1][r]);
+        for (int i = 0; i < 8; ++i) {
+          const int a = ks * kChunkK + h * 8 + i;
+          x[i] = (valid && a < K) ? __ldg(base + U.before * a) : make_float4(0.f, 0.f, 0.f, 0.f);
         }
-        if (h == 0) {
-          // the epilogue of the unit two back has read ex of this buffer
-          if (!mbar_wait(&sm.bar.exfree[buf], use_par ^ 1, kSpin)) {
-            set_status(status, 8);
-            ok = false;
-            break;
-          }
-          sm.ex[buf][r] = (uint8_t)eb;
-          mbar_arrive(&sm.bar.exready[buf]);
+      };
+      float4 nx[8];
+      load8(nx, 0);
+      for (int ks = 0; ks < nks; ++ks, ++q) {
+        const int s = q & 1;
+        float4 x[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) x[i] = nx[i];
+        if (ks + 1 < nks) load8(nx, ks + 1);
+        if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
+          set_status(status, 1);
+          ok = false;
+          break;
         }
-        const int nks = (K + kChunkK - 1) / kChunkK;
-        // this thread's eight values of chunk ks; the next chunk's loads are in
-        // flight while the current chunk is cut into digits
-        auto load8 = [&](float4 (&x)[8], int ks) {
+        unsigned char* A = sm.a[s];
+        // fp32 values (complex64 storage keeps them in the hi words)
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int a = ks * kChunkK + h * 8 + i;
-            x[i] = (valid && a < K) ? __ldg(base + U.before * a) : make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int g2 = 0; g2 < 2; ++g2) {  // two 16-byte core rows of 4 k each
+          uint32_t hr[4], hi_[4], lr[4], li[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            tf32_split(x[4 * g2 + i].x, hr[i], lr[i]);
+            tf32_split(x[4 * g2 + i].z, hi_[i], li[i]);
           }
-        };
-        float4 nx[8];
-        load8(nx, 0);
-        for (int ks = 0; ks < nks; ++ks, ++q) {
-          const int s = q & 1;
-          float4 x[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) x[i] = nx[i];
-          if (ks + 1 < nks) load8(nx, ks + 1);
-          if (!mbar_wait(&sm.bar.empty[s], ((q >> 1) & 1) ^ 1, kSpin)) {
-            set_status(status, 1);
-            ok = false;
-            break;
-          }
-          unsigned char* A = sm.a[s];
-          if (OZ) {
-            uint32_t wr[kDig][4], wi[kDig][4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              float d0[kDig], d1[kDig], e0[kDig], e1[kDig];
-              digits_f32(x[2 * i].x, x[2 * i].y, eb, d0);
-              digits_f32(x[2 * i + 1].x, x[2 * i + 1].y, eb, d1);
-              digits_f32(x[2 * i].z, x[2 * i].w, eb, e0);
-              digits_f32(x[2 * i + 1].z, x[2 * i + 1].w, eb, e1);
-#pragma unroll
-              for (int d = 0; d < kDig; ++d) {
-                wr[d][i] = pack_bf16(d0[d], d1[d]);
-                wi[d][i] = pack_bf16(e0[d], e1[d]);
-              }
-            }
-            const int off = core_off(r, h, kRows);
-#pragma unroll
-            for (int d = 0; d < kDig; ++d) {
-              *reinterpret_cast<uint4*>(A + (2 * d + 0) * kOzAPlane + off) =
-                  make_uint4(wr[d][0], wr[d][1], wr[d][2], wr[d][3]);
-              *reinterpret_cast<uint4*>(A + (2 * d + 1) * kOzAPlane + off) =
-                  make_uint4(wi[d][0], wi[d][1], wi[d][2], wi[d][3]);
-            }
-          } else {
-            // fp32 values (complex64 storage keeps them in the hi words)
-#pragma unroll
-            for (int g2 = 0; g2 < 2; ++g2) {  // two 16-byte core rows of 4 k each
-              uint32_t hr[4], hi_[4], lr[4], li[4];
-#pragma unroll
-              for (int i = 0; i < 4; ++i) {
-                tf32_split(x[4 * g2 + i].x, hr[i], lr[i]);
-                tf32_split(x[4 * g2 + i].z, hi_[i], li[i]);
-              }
-              const int off = core_off(r, 2 * h + g2, kRows);
-              *reinterpret_cast<uint4*>(A + 0 * kTfAPlane + off) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
-              *reinterpret_cast<uint4*>(A + 1 * kTfAPlane + off) = make_uint4(hi_[0], hi_[1], hi_[2], hi_[3]);
-              *reinterpret_cast<uint4*>(A + 2 * kTfAPlane + off) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
-              *reinterpret_cast<uint4*>(A + 3 * kTfAPlane + off) = make_uint4(li[0], li[1], li[2], li[3]);
-            }
-          }
-          fence_proxy_async();
-          mbar_arrive(&sm.bar.full[s]);
+          const int off = core_off(r, 2 * h + g2, kRows);
+          *reinterpret_cast<uint4*>(A + 0 * kTfAPlane + off) = make_uint4(hr[0], hr[1], hr[2], hr[3]);
+          *reinterpret_cast<uint4*>(A + 1 * kTfAPlane + off) = make_uint4(hi_[0], hi_[1], hi_[2], hi_[3]);
+          *reinterpret_cast<uint4*>(A + 2 * kTfAPlane + off) = make_uint4(lr[0], lr[1], lr[2], lr[3]);
+          *reinterpret_cast<uint4*>(A + 3 * kTfAPlane + off) = make_uint4(li[0], li[1], li[2], li[3]);
         }
+        fence_proxy_async();
+        mbar_arrive(&sm.bar.full[s]);
       }
     }
   } else if (warp == 12) {
@@ -429,114 +299,84 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
       const void* cur = nullptr;
       for (int64_t it = my0; it < my1 && ok; ++it, ++un) {
         const int2 tl = tiles[tile0 + it];
-        {
-          const TcUnit U = make_unit(tasks, tl.x);
-          const int K = U.K, Np = U.Np, nks = (K + kChunkK - 1) / kChunkK;
-          const int esz = OZ ? 2 : 4;
-          const int planes = OZ ? kDig * 2 : 4;
-          const int plane_b = Np * kChunkK * esz;  // bytes of one h plane per chunk
-          const uint32_t tpar = un & 1;
-          if (U.img != cur) {
-            // the previous unit's MMAs read the old h: wait until they completed
-            if (un > 0 && !mbar_wait(&sm.bar.tfull, tpar ^ 1, kSpin)) {
-              set_status(status, 2);
-              ok = false;
-              break;
-            }
-            const uint32_t bytes = (uint32_t)(nks * planes * plane_b);
-            mbar_arrive_expect_tx(&sm.bar.bfull, bytes);
-            for (uint32_t o = 0; o < bytes; o += 32768u) {
-              const uint32_t n = bytes - o < 32768u ? bytes - o : 32768u;
-              bulk_g2s(sm.b + o, U.img + o, n, &sm.bar.bfull);
-            }
-            if (!mbar_wait(&sm.bar.bfull, nb & 1, kSpin)) {
-              set_status(status, 3);
-              ok = false;
-              break;
-            }
-            ++nb;
-            cur = U.img;
+        const TcUnit U = make_unit(tasks, tl.x);
+        const int K = U.K, Np = U.Np, nks = (K + kChunkK - 1) / kChunkK;
+        const int plane_b = Np * kChunkK * 4;  // bytes of one h plane per step
+        const uint32_t tpar = un & 1;
+        if (U.img != cur) {
+          // the previous unit's MMAs read the old h: wait until they completed
+          if (un > 0 && !mbar_wait(&sm.bar.tfull, tpar ^ 1, kSpin)) {
+            set_status(status, 2);
+            ok = false;
+            break;
           }
-          // the epilogue released the accumulators of the previous unit
-          if (!mbar_wait(&sm.bar.tempty, tpar ^ 1, kSpin)) {
-            set_status(status, 4);
+          const uint32_t bytes = (uint32_t)(nks * 4 * plane_b);
+          mbar_arrive_expect_tx(&sm.bar.bfull, bytes);
+          for (uint32_t o = 0; o < bytes; o += 32768u) {
+            const uint32_t n = bytes - o < 32768u ? bytes - o : 32768u;
+            bulk_g2s(sm.b + o, U.img + o, n, &sm.bar.bfull);
+          }
+          if (!mbar_wait(&sm.bar.bfull, nb & 1, kSpin)) {
+            set_status(status, 3);
+            ok = false;
+            break;
+          }
+          ++nb;
+          cur = U.img;
+        }
+        // the epilogue released the accumulators of the previous unit
+        if (!mbar_wait(&sm.bar.tempty, tpar ^ 1, kSpin)) {
+          set_status(status, 4);
+          ok = false;
+          break;
+        }
+        fence_after_sync();
+        const uint32_t lboB = (uint32_t)(Np / 8) * 128;
+        const uint32_t lboA4 = (kRows / 8) * 128;  // kc stride of a 16-k fp32 plane: [kc (4)][g][8][4]
+        const uint32_t id = idesc_m128(2, Np, false), idn = idesc_m128(2, Np, true);
+        uint32_t used = 0;  // 0 until the unit's first MMAs
+        for (int ks = 0; ks < nks; ++ks, ++q) {
+          const int s = q & 1;
+          if (!mbar_wait(&sm.bar.full[s], (q >> 1) & 1, kSpin)) {
+            set_status(status, 5);
             ok = false;
             break;
           }
           fence_after_sync();
-          const uint32_t lboA = (kRows / 8) * 128, lboB = (uint32_t)(Np / 8) * 128;
-          uint32_t used = 0;  // TF: 0 until the unit's first MMAs
-          for (int ks = 0; ks < nks; ++ks, ++q) {
-            const int s = q & 1;
-            if (!mbar_wait(&sm.bar.full[s], (q >> 1) & 1, kSpin)) {
-              set_status(status, 5);
-              ok = false;
-              break;
-            }
-            fence_after_sync();
-            const uint32_t a0 = smem_u32(sm.a[s]);
-            const uint32_t b0 = smem_u32(sm.b) + (uint32_t)(ks * planes * plane_b);
-            if (OZ) {
-              // descriptors of the first planes; the others differ only in
-              // the start address field (address / 16)
-              const int NL = levels_for(Np);
-              const uint32_t id = idesc_m128(1, Np, false), idn = idesc_m128(1, Np, true);
-              const uint64_t dA = desc_kmajor(a0, lboA, 128), dB = desc_kmajor(b0, lboB, 128);
-              const uint64_t pA = kOzAPlane >> 4, pB = (uint64_t)(plane_b >> 4);
-              const uint32_t first = ks == 0 ? 1u : 0u;  // the unit's first chunk initialises the levels
-#pragma unroll
-              for (int sd = 0; sd < kDig; ++sd) {
-                const uint64_t are = dA + (uint64_t)(2 * sd) * pA, aim = are + pA;
-#pragma unroll
-                for (int td = 0; td + sd < kDig; ++td) {
-                  const int L = sd + td < NL - 1 ? sd + td : NL - 1;
-                  const uint64_t bre = dB + (uint64_t)(2 * td) * pB, bim = bre + pB;
-                  const uint32_t dre = tmem + (uint32_t)(L * 2 * Np), dim_ = dre + (uint32_t)Np;
-                  // the first write of level L in the unit: pair (0, L), or (0, NL - 1) for the last level
-                  const uint32_t acc = (first && sd == 0 && td == L) ? 0u : 1u;
-                  mma_bf16(dre, are, bre, id, acc);
-                  mma_bf16(dim_, are, bim, id, acc);
-                  mma_bf16(dre, aim, bim, idn, 1);
-                  mma_bf16(dim_, aim, bre, id, 1);
-                }
-              }
-            } else {
-              const uint32_t id = idesc_m128(2, Np, false), idn = idesc_m128(2, Np, true);
-              const uint32_t lboA4 = (kRows / 8) * 128;  // kc stride of a 16-k fp32 plane: [kc (4)][g][8][4]
+          const uint32_t a0 = smem_u32(sm.a[s]);
+          const uint32_t b0 = smem_u32(sm.b) + (uint32_t)(ks * 4 * plane_b);
 #pragma unroll 1
-              for (int h8 = 0; h8 < 2; ++h8) {  // two MMAs of k = 8 per chunk
-                const uint32_t ao = (uint32_t)(2 * h8) * lboA4, bo = (uint32_t)(2 * h8) * lboB;
-                const uint64_t ahr = desc_kmajor(a0 + 0 * kTfAPlane + ao, lboA4, 128);
-                const uint64_t ahi = desc_kmajor(a0 + 1 * kTfAPlane + ao, lboA4, 128);
-                const uint64_t alr = desc_kmajor(a0 + 2 * kTfAPlane + ao, lboA4, 128);
-                const uint64_t ali = desc_kmajor(a0 + 3 * kTfAPlane + ao, lboA4, 128);
-                const uint64_t bhr = desc_kmajor(b0 + 0 * plane_b + bo, lboB, 128);
-                const uint64_t bhi = desc_kmajor(b0 + 1 * plane_b + bo, lboB, 128);
-                const uint64_t blr = desc_kmajor(b0 + 2 * plane_b + bo, lboB, 128);
-                const uint64_t bli = desc_kmajor(b0 + 3 * plane_b + bo, lboB, 128);
-                const uint32_t dre = tmem, dim_ = tmem + (uint32_t)Np;
-                const uint32_t f = used;  // 0 only for the first MMAs of the unit
-                // lo x hi and hi x lo first, then hi x hi
-                mma_tf32(dre, alr, bhr, id, f);
-                mma_tf32(dim_, alr, bhi, id, f);
-                mma_tf32(dre, ali, bhi, idn, 1);
-                mma_tf32(dim_, ali, bhr, id, 1);
-                mma_tf32(dre, ahr, blr, id, 1);
-                mma_tf32(dim_, ahr, bli, id, 1);
-                mma_tf32(dre, ahi, bli, idn, 1);
-                mma_tf32(dim_, ahi, blr, id, 1);
-                mma_tf32(dre, ahr, bhr, id, 1);
-                mma_tf32(dim_, ahr, bhi, id, 1);
-                mma_tf32(dre, ahi, bhi, idn, 1);
-                mma_tf32(dim_, ahi, bhr, id, 1);
-                used = 1;
-              }
-            }
-            commit(&sm.bar.empty[s]);  // the stage is free once these MMAs completed
+          for (int h8 = 0; h8 < 2; ++h8) {  // two MMAs of k = 8 per step
+            const uint32_t ao = (uint32_t)(2 * h8) * lboA4, bo = (uint32_t)(2 * h8) * lboB;
+            const uint64_t ahr = desc_kmajor(a0 + 0 * kTfAPlane + ao, lboA4, 128);
+            const uint64_t ahi = desc_kmajor(a0 + 1 * kTfAPlane + ao, lboA4, 128);
+            const uint64_t alr = desc_kmajor(a0 + 2 * kTfAPlane + ao, lboA4, 128);
+            const uint64_t ali = desc_kmajor(a0 + 3 * kTfAPlane + ao, lboA4, 128);
+            const uint64_t bhr = desc_kmajor(b0 + 0 * plane_b + bo, lboB, 128);
+            const uint64_t bhi = desc_kmajor(b0 + 1 * plane_b + bo, lboB, 128);
+            const uint64_t blr = desc_kmajor(b0 + 2 * plane_b + bo, lboB, 128);
+            const uint64_t bli = desc_kmajor(b0 + 3 * plane_b + bo, lboB, 128);
+            const uint32_t dre = tmem, dim_ = tmem + (uint32_t)Np;
+            const uint32_t f = used;  // 0 only for the first MMAs of the unit
+            // lo x hi and hi x lo first, then hi x hi
+            mma_tf32(dre, alr, bhr, id, f);
+            mma_tf32(dim_, alr, bhi, id, f);
+            mma_tf32(dre, ali, bhi, idn, 1);
+            mma_tf32(dim_, ali, bhr, id, 1);
+            mma_tf32(dre, ahr, blr, id, 1);
+            mma_tf32(dim_, ahr, bli, id, 1);
+            mma_tf32(dre, ahi, bli, idn, 1);
+            mma_tf32(dim_, ahi, blr, id, 1);
+            mma_tf32(dre, ahr, bhr, id, 1);
+            mma_tf32(dim_, ahr, bhi, id, 1);
+            mma_tf32(dre, ahi, bhi, idn, 1);
+            mma_tf32(dim_, ahi, bhr, id, 1);
+            used = 1;
           }
-          if (!ok) break;
-          commit(&sm.bar.tfull);
+          commit(&sm.bar.empty[s]);  // the step is free once these MMAs completed
         }
+        if (!ok) break;
+        commit(&sm.bar.tfull);
       }
       // drain: every MMA issued by this thread completed before tensor memory is freed
       commit(&sm.bar.drain);
@@ -550,105 +390,38 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_mp_tc(const MPTask* __restric
     uint32_t un = 0;
     for (int64_t it = my0; it < my1 && ok; ++it, ++un) {
       const int2 tl = tiles[tile0 + it];
-      {
-        const TcUnit U = make_unit(tasks, tl.x);
-        const int N = U.N, Np = U.Np;
-        const int buf = (int)(un & 1);
-        const uint32_t tpar = un & 1;
-        if (!mbar_wait(&sm.bar.exready[buf], (un >> 1) & 1, kSpin) || !mbar_wait(&sm.bar.tfull, tpar, kSpin)) {
-          set_status(status, 7);
-          ok = false;
-          break;
-        }
-        fence_after_sync();
-        const int er = OZ ? (int)sm.ex[buf][r] : 0;
-        mbar_arrive(&sm.bar.exfree[buf]);
-        const int64_t rg = (int64_t)tl.y * kRows + r;
-        const bool live = rg < U.nrows;
-        const int64_t ro = live ? rg % U.before + U.before * (int64_t)N * (rg / U.before) : 0;
-        int* fxw = sm.fx[qd];
-        if (OZ) {
-          // the unit's column exponents of h into this warp's copy
-          const int* fxg = reinterpret_cast<const int*>(U.img + Cfg<true>::BHeader);
-          __syncwarp();
-          for (int j = lane; j < 64; j += 32) fxw[j] = __ldg(fxg + j);
-          __syncwarp();
-        }
-        for (int j0 = 0; j0 < Np; j0 += 8) {
-          __syncwarp();  // the tensor-memory loads below are warp-collective
-          float vre[8], vim[8], lre[8], lim[8];
-          if (OZ) {
-            // all levels of eight columns: one wait for the real parts, one for the imaginary
-            const int NL = levels_for(Np);
-            float a[kDig][8];
-#pragma unroll
-            for (int part = 0; part < 2; ++part) {
-#pragma unroll
-              for (int L = 0; L < kDig; ++L)
-                if (L < NL) tmem_ld8(lane_addr + (uint32_t)(L * 2 * Np + part * Np + j0), a[L]);
-              tmem_wait_ld();
-              float* v = part ? vim : vre;
-              float* l = part ? lim : lre;
-#pragma unroll
-              for (int i = 0; i < 8; ++i) {
-                // levels 0..2 in double-float; levels 3.. lie below 2^-21 of
-                // level 0's scale, their fp32 sum in the low word errs by
-                // less than 2^-45 of it
-                v[i] = a[0][i];
-                l[i] = 0.f;
-                if (NL > 1) df_add(v[i], l[i], a[1][i], 0.f);
-                if (NL > 2) df_add(v[i], l[i], a[2][i], 0.f);
-                float t3 = 0.f;
-#pragma unroll
-                for (int L = 3; L < kDig; ++L)
-                  if (L < NL) t3 = __fadd_rn(t3, a[L][i]);
-                l[i] = __fadd_rn(l[i], t3);
-              }
-            }
-          } else {
-            tmem_ld8(lane_addr + (uint32_t)j0, vre);
-            tmem_ld8(lane_addr + (uint32_t)(Np + j0), vim);
-            tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 8; ++i) lre[i] = lim[i] = 0.f;
-          }
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int j = j0 + i;
-            if (!live || j >= N) continue;
-            float4 v;
-            float4* o = U.out + ro + U.before * j;
-            if (OZ) {
-              const int fj = fxw[j];
-              const int sh = (er - 126) + (fj - 126);
-              if (sh >= -126 && sh <= 127) {
-                const float f = pow2f(sh);
-                v = make_float4(vre[i] * f, lre[i] * f, vim[i] * f, lim[i] * f);
-              } else {
-                v = make_float4(scale2(vre[i], sh), scale2(lre[i], sh), scale2(vim[i], sh), scale2(lim[i], sh));
-              }
-              df_norm(v.x, v.y);
-              df_norm(v.z, v.w);
-              if (er == 255 || fj == 255) {  // an Inf or NaN in the row: propagate it
-                const float nan = __int_as_float(0x7fffffff);
-                v = make_float4(nan, nan, nan, nan);
-              }
-            } else {
-              v = make_float4(vre[i], 0.f, vim[i], 0.f);
-            }
-            *o = v;
-          }
-        }
-        fence_before_sync();
-        mbar_arrive(&sm.bar.tempty);
+      const TcUnit U = make_unit(tasks, tl.x);
+      const int N = U.N, Np = U.Np;
+      if (!mbar_wait(&sm.bar.tfull, un & 1, kSpin)) {
+        set_status(status, 7);
+        ok = false;
+        break;
       }
+      fence_after_sync();
+      const int64_t rg = (int64_t)tl.y * kRows + r;
+      const bool live = rg < U.nrows;
+      const int64_t ro = live ? rg % U.before + U.before * (int64_t)N * (rg / U.before) : 0;
+      for (int j0 = 0; j0 < Np; j0 += 8) {
+        __syncwarp();  // the tensor-memory loads below are warp-collective
+        float vre[8], vim[8];
+        tmem_ld8(lane_addr + (uint32_t)j0, vre);
+        tmem_ld8(lane_addr + (uint32_t)(Np + j0), vim);
+        tmem_wait_ld();
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int j = j0 + i;
+          if (live && j < N) U.out[ro + U.before * j] = make_float4(vre[i], 0.f, vim[i], 0.f);
+        }
+      }
+      fence_before_sync();
+      mbar_arrive(&sm.bar.tempty);
     }
   }
   fence_before_sync();
   __syncthreads();
   if (warp == 12) {
     fence_after_sync();
-    tmem_dealloc(tmem, ncols);
+    tmem_dealloc(tmem, 128u);
   }
 }
 
@@ -1309,16 +1082,15 @@ cudaError_t tc_grid(int64_t n_tiles, unsigned* grid) {
   return cudaSuccess;
 }
 
-template <bool OZ>
-cudaError_t launch_tc(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles, int* status,
+cudaError_t launch_tf(const MPTask* tasks, const int2* tiles, int64_t first_tile, int64_t n_tiles, int* status,
                       cudaStream_t s) {
   unsigned grid = 0;
   cudaError_t e = tc_grid(n_tiles, &grid);
   if (e != cudaSuccess) return e;
-  const int sm = (int)sizeof(TcSmem<OZ>);
-  e = cudaFuncSetAttribute(k_mp_tc<OZ>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  const int sm = (int)sizeof(TfSmem);
+  e = cudaFuncSetAttribute(k_mp_tf, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (e != cudaSuccess) return e;
-  k_mp_tc<OZ><<<grid, kThreadsTc, sm, s>>>(tasks, tiles, first_tile, n_tiles, status);
+  k_mp_tf<<<grid, kThreadsTc, sm, s>>>(tasks, tiles, first_tile, n_tiles, status);
   return cudaGetLastError();
 }
 
@@ -1384,8 +1156,8 @@ cudaError_t launch_mp_tc(bool oz, const MPTask* tasks, const int2* tiles, int64_
                          const int* tc_tasks, int64_t first_task, int64_t n_tasks, int* status, cudaStream_t s) {
   if (n_tiles <= 0) return cudaSuccess;
   if (oz) return launch_mp_tcs(tasks, tiles, first_tile, n_tiles, tc_tasks, first_task, n_tasks, status, s);
-  if (n_tasks > 0) k_mp_tc_h<false><<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
-  return launch_tc<false>(tasks, tiles, first_tile, n_tiles, status, s);
+  if (n_tasks > 0) k_mp_tf_h<<<(unsigned)n_tasks, 256, 0, s>>>(tasks, tc_tasks, first_task);
+  return launch_tf(tasks, tiles, first_tile, n_tiles, status, s);
 }
 
 }  // namespace qt
