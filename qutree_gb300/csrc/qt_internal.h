@@ -60,10 +60,18 @@ struct HpTcGroup {
   int n, nchunks;
   int member[kHpTcMembers];
 };
-// a qualifying task: 16 <= a <= 64 and at least two chunks of reduction
+// Which contractions the planner puts on the tensor cores: shapes from 32 to
+// 64 (padded to at most 64 output columns).  Below 32 the fixed costs of a
+// tile (row exponents, the level recombination, the 128-row tile itself)
+// outweigh the products: on a forest of uneven trees with bonds 4..24 the
+// double-float sweep took 82.7 ms with every shape up to 64 on the tensor
+// cores, 57.2 ms with the threshold (as many as on the FP32 pipe alone).
+// hole product: 32 <= a <= 64 and at least two 64-k chunks of reduction
 inline bool hp_tc_eligible(int before, int a, int after) {
-  return a >= 16 && a <= 64 && (int64_t)before * after >= 2 * kHpTcChunk;
+  return a >= 32 && a <= 64 && (int64_t)before * after >= 2 * kHpTcChunk;
 }
+// mode product (not diagonal): 32 <= a_in, a_out <= 64
+inline bool mp_tc_eligible(int a_in, int a_out) { return a_in >= 32 && a_in <= 64 && a_out >= 32 && a_out <= 64; }
 #ifdef __CUDACC__
 #define QT_HD __host__ __device__
 #else
@@ -94,8 +102,9 @@ struct AccTask {
   int add, pad;
   void* tc_img = nullptr;  // tensor-core path: images of alpha H_t, one per term (hp_tc_chunk_bytes(., 4))
 };
-// an accumulation the planner puts on the tensor cores (double-float plans)
-inline bool acc_tc_eligible(int rows, int d) { return d >= 16 && d <= 64 && rows >= 64; }
+// an accumulation the planner puts on the tensor cores (double-float plans):
+// 32 <= d <= 64 and at least 64 rows
+inline bool acc_tc_eligible(int rows, int d) { return d >= 32 && d <= 64 && rows >= 64; }
 
 // out = sum_t c_t * M_t for d x d matrices (grouped mean fields).
 struct LinTerm {

@@ -659,7 +659,7 @@ class Builder {
     std::vector<char> oz(t1 - t0, 0);
     for (int64_t t = t0; t < t1; ++t) {
       auto& m = P.mp[t];
-      if (m.diag || m.a_in > 64 || m.a_out > 64) continue;
+      if (m.diag || !mp_tc_eligible(m.a_in, m.a_out)) continue;
       oz[t - t0] = 1;
       m.oz_h = stage_oz_;
       // double-float plans: the sum-of-products kernel's image of alpha h;

@@ -200,7 +200,7 @@ class PlanView:
                         y = x * h[None, :, None]
                     else:
                         h = view(hb, ho, aout * ain).reshape((aout, ain), order="F")
-                        if self.tensor and ain <= 64 and aout <= 64:
+                        if self.tensor and 32 <= ain <= 64 and 32 <= aout <= 64:
                             y = oz_mode_product(h, x)
                         else:
                             y = np.einsum("ja,bac->bjc", h, x)
@@ -487,12 +487,12 @@ HP_CHUNK = 64
 
 def acc_tc_eligible(rows, d):
     """The accumulations the planner puts on the tensor cores (qt_internal.h)."""
-    return 16 <= d <= 64 and rows >= 64
+    return 32 <= d <= 64 and rows >= 64
 
 
 def hp_tc_eligible(before, a, after):
     """The hole products the planner puts on the tensor cores (qt_internal.h)."""
-    return 16 <= a <= 64 and before * after >= 2 * HP_CHUNK
+    return 32 <= a <= 64 and before * after >= 2 * HP_CHUNK
 
 
 def hp_tc_kc(a):

@@ -42,16 +42,32 @@ def _check(tree, sop, psi, flavour, tol=TOL_DF, noise_tol=1e-11):
     err, noise = deriv_errors(tree, pv.dpsi(), r.dpsi, r.rho)
     print(f"emulated tensor-core sweep: dE {abs(h00.real / s00.real - r.energy):.2e} dpsi {err:.2e} noise {noise:.2e}")
     assert err <= tol and noise <= noise_tol
-    # the digit arithmetic ran: the same plan without the tensor bit differs at rounding level
+    # where the planner put contractions on the tensor cores (shapes 32..64)
+    # the digit arithmetic ran: the plan without the tensor bit differs at
+    # rounding level; elsewhere the two plans are the same
     exact = PlanView(tree, sop, flavour, prec=1)
     exact.run(flat)
-    assert not np.array_equal(pv.dpsi(), exact.dpsi())
+    tc = len(pv.tables[40]) + len(pv.tables[53]) + len(pv.tables[57])
+    assert np.array_equal(pv.dpsi(), exact.dpsi()) == (tc == 0)
+    return tc
 
 
 @pytest.mark.parametrize("flavour", [0, 1, 2])
 def test_emulated_tensor_core_sweep_cfg0(flavour):
+    # bonds 4, leaves 16: nothing qualifies for the tensor cores
     tree, sop, psi = config_problem(0)
-    _check(tree, sop, psi, flavour)
+    assert _check(tree, sop, psi, flavour) == 0
+
+
+@pytest.mark.parametrize("flavour", [1, 2])
+def test_emulated_tensor_core_sweep_bonds_36(flavour):
+    # leaves of 40 points, bonds 36: mode products with 40 padded columns
+    # (six level accumulators), hole products in 128-k chunks with four,
+    # accumulations over 40 padded columns
+    tree = balanced_tree(4, 40, 36)
+    sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=np.random.default_rng(6),
+                              omega=1.0)
+    assert _check(tree, sop, random_wavefunction(tree, 6), flavour, tol=1e-10, noise_tol=1e-10) > 0
 
 
 @pytest.mark.parametrize("flavour", [1, 2])
@@ -66,7 +82,8 @@ def test_emulated_tensor_core_sweep_cfg4(flavour):
 
 @pytest.mark.parametrize("leaves,p,b,seed", [(7, 5, 4, 2), (5, 80, 12, 3)])
 def test_emulated_tensor_core_sweep_random_trees(leaves, p, b, seed):
-    # p = 80: the leaf products (k = 80) stay exact, the rest use digits
+    # p = 80, bonds 12: the leaf products (k = 80) and the bonds below 32
+    # stay on the FP32 pipe
     tree = balanced_tree(leaves, p, b)
     sop = coupled_oscillators(tree, n_pairs=None, coupling=0.2, quartic=0.1, rng=np.random.default_rng(seed),
                               omega=1.0)
@@ -74,9 +91,9 @@ def test_emulated_tensor_core_sweep_random_trees(leaves, p, b, seed):
 
 
 def test_emulated_tensor_core_forest():
-    # five uneven trees in one compressed plan: small and ragged mode products
-    # (bonds 4..24, k not a multiple of 16) through the digit arithmetic;
-    # each tree's slice equals its own oracle sweep at the double-float tolerances
+    # five uneven trees in one compressed plan (bonds 4..24, leaves up to 32):
+    # only the 32-point leaf products qualify for the digit arithmetic; each
+    # tree's slice equals its own oracle sweep at the double-float tolerances
     from qutree_gb300.model import batched_problem, forest, forest_psi, forest_sop
     trees, sops, psis = batched_problem(5)
     f, node_off, mode_off = forest(trees)

@@ -1,6 +1,6 @@
 """Planner side of the tensor-core mode products (flavour bit 0x8000 with
 double-float or complex64 arithmetic), on the CPU: in every mode-product
-stage the tasks with a_in, a_out <= 64 (not diagonal) get tensor-core tiles
+stage the tasks with 32 <= a_in, a_out <= 64 (not diagonal) get tensor-core tiles
 covering their rows exactly once and a slot of their own in the stage for
 the operand image of h; every other task keeps its classic tiles, which
 cover its output slots exactly once.  Image slots are private within a
@@ -41,7 +41,7 @@ def test_tensor_core_tiles_cover_eligible_tasks(problem, plan):
             assert noz == 0 and nozt == 0
             continue
         eligible = {t for t in range(t0, t0 + nt)
-                    if not mp[t][10] and mp[t][7] <= 64 and mp[t][8] <= 64}
+                    if not mp[t][10] and 32 <= mp[t][7] <= 64 and 32 <= mp[t][8] <= 64}
         # tensor-core tiles: each eligible task's rows exactly once
         got = {}
         for task, q in oz_tiles[oz0:oz0 + noz]:
