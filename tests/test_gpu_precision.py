@@ -1,7 +1,8 @@
-"""Double-float arithmetic against complex128 on the 48..96-bond 64-mode tree
-(regularisation 1e-8): one sweep, then constant-mean-field steps of dt = 0.01
-in lockstep; the energies stay within |dE| <= 1e-8 (the headline metric's
-bar) and the projected derivatives within 1e-9 relative (rho-weighted)."""
+"""Double-float arithmetic (FP32 pipe, and with the tensor-core digit
+products) against complex128 on the 48..96-bond 64-mode tree (regularisation
+1e-8): one sweep, then constant-mean-field steps of dt = 0.01 in lockstep;
+the energies stay within |dE| <= 1e-8 (the headline metric's bar) and the
+projected derivatives within 1e-9 relative (rho-weighted)."""
 import numpy as np
 import pytest
 
@@ -12,11 +13,11 @@ from qutree_gb300.model import config_problem
 pytestmark = pytest.mark.gpu
 
 
-def test_double_float_tracks_complex128_along_cmf():
+@pytest.mark.parametrize("prec", [qtgpu.QT_PREC_DF64, qtgpu.QT_PREC_DF64_TC])
+def test_double_float_tracks_complex128_along_cmf(prec):
     tree, sop, psi = config_problem(3)
     hf = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_COMPRESSED, eps=1e-8)
-    hd = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_COMPRESSED | qtgpu.QT_PREC_DF64,
-                                         eps=1e-8)
+    hd = qtgpu.HamiltonianRepresentation(sop, tree, flavour=qtgpu.QT_PLAN_COMPRESSED | prec, eps=1e-8)
     try:
         for h in (hf, hd):
             h.upload(psi.flat())
