@@ -384,6 +384,18 @@ int qt_last_mode_product(qt_ctx* ctx, void* C, const void* A, const void* B,
 int qt_rho_inverse_noalloc(qt_ctx* ctx, void* rhoinv, const void* rho, int n_mats, int d,
                            double eps);
 
+/* qrOrthogonal (include/TreeClasses/TensorTree_Implementation.h:173-187) on
+ * the uploaded wavefunction, in place on the device: bottom-up, every
+ * non-top node tensor, as a (lastBefore x d_up) matrix, is replaced by the
+ * thin Q of its Householder QR (qr, include/Core/Matrix_Implementation.h:
+ * 795-806: reflectors mapping each column to -e^{i arg x_0} |x| e_1, as
+ * Eigen's HouseholderQR) and R = Q^H Phi is multiplied into the parent along
+ * the node's child index (matrixTensor).  Complex128 on the FP64 pipe, one
+ * block per node; the nodes of one height run together.  Uses the
+ * context's chain scratch (QT_ERR_ALLOC when a height's Q and R do not fit).
+ * QT_ERR_STATE without a prepared context and an uploaded wavefunction. */
+int qt_qr_orthogonal(qt_ctx* ctx);
+
 /* Device memory helpers for callers without their own allocator. */
 int qt_dev_alloc(qt_ctx* ctx, int64_t bytes, void** ptr);
 int qt_dev_free(qt_ctx* ctx, void* ptr);

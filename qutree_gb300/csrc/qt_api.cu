@@ -1246,6 +1246,73 @@ int qt_last_mode_product(qt_ctx* c, void* C, const void* A, const void* B, int64
   return qt_mode_product(c, C, A, B, last_before, active, active, 1, add);
 }
 
+int qt_qr_orthogonal(qt_ctx* c) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  QT_DEVICE(c);
+  if (!c->prepared) return fail(c, QT_ERR_STATE, "qt_qr_orthogonal before qt_prepare");
+  if (!c->have_psi) return fail(c, QT_ERR_STATE, "no wavefunction uploaded");
+  const qt::Plan& P = c->plan;
+  const auto& nd = P.nodes;
+  double2* psi = c->buf[qt::B_PSI64];
+  double2* scr = c->buf[qt::B_SCR];
+  const int64_t cap = c->buf_elems[qt::B_SCR];
+  int max_h = 0;
+  for (const auto& g : nd) max_h = std::max(max_h, g.height);
+  // per height: Q scratch, R, the task records and the parent's temporary copy
+  for (int h = 0; h <= max_h; ++h) {
+    std::vector<int> ids;
+    for (int a = 0; a < (int)nd.size(); ++a)
+      if (!nd[a].top() && nd[a].height == h) ids.push_back(a);
+    if (ids.empty()) continue;
+    std::vector<qt::QRTask> tasks;
+    int64_t off = 0, tmp = 0;
+    for (int a : ids) {
+      const int64_t n = nd[a].dup(), m = nd[a].N / n;
+      qt::QRTask t;
+      t.A = psi + nd[a].off;
+      t.Qs = scr + off;
+      off += m * n;
+      t.R = scr + off;
+      off += n * n;
+      t.m = (int)m;
+      t.n = (int)n;
+      tasks.push_back(t);
+      tmp = std::max(tmp, nd[nd[a].parent].N);
+    }
+    const int64_t task_elems = ((int64_t)(tasks.size() * sizeof(qt::QRTask)) + 15) / 16;
+    if (off + tmp + task_elems > cap)
+      return fail(c, QT_ERR_ALLOC, "qt_qr_orthogonal: the chain scratch is too small for one height");
+    double2* ptmp = scr + off;
+    void* dtasks = scr + off + tmp;
+    QT_CUDA(c, cudaMemcpyAsync(dtasks, tasks.data(), tasks.size() * sizeof(qt::QRTask), cudaMemcpyHostToDevice,
+                               c->stream));
+    QT_CUDA(c, qt::launch_house_qr(dtasks, (int)tasks.size(), c->stream));
+    c->launches += 1;
+    // R into the parents along the child index (siblings of one parent in turn)
+    for (size_t i = 0; i < ids.size(); ++i) {
+      const qt::NodeGeo& g = nd[ids[i]];
+      const qt::NodeGeo& pg = nd[g.parent];
+      qt::MPTask t;
+      t.in = psi + pg.off;
+      t.out = ptmp;
+      t.h = tasks[i].R;
+      t.alpha = make_double2(1.0, 0.0);
+      t.before = (int)pg.before(g.child_idx);
+      t.a_in = t.a_out = g.dup();
+      t.after = (int)pg.after(g.child_idx);
+      t.diag = 0;
+      t.add = 0;
+      QT_CUDA(c, qt::launch_single_mp(t, c->stream, nullptr));
+      QT_CUDA(c, cudaMemcpyAsync(psi + pg.off, ptmp, pg.N * 16, cudaMemcpyDeviceToDevice, c->stream));
+      c->launches += 1;
+    }
+    // the task records must outlive their copy
+    QT_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  c->swept = false;
+  return QT_OK;
+}
+
 int qt_dev_alloc(qt_ctx* c, int64_t bytes, void** p) {
   if (!c || !p || bytes <= 0) return fail(c, QT_ERR_ARG, "qt_dev_alloc: bad argument");
   QT_DEVICE(c);

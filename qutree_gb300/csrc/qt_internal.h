@@ -643,6 +643,15 @@ cudaError_t launch_stage(const Stage& st, const DevTables& t, double eps, int ma
 cudaError_t launch_set_identity(double2* m, int d, int prec, cudaStream_t s);
 // single-op launches for the primitive C ABI calls
 cudaError_t launch_single_mp(const MPTask& task, cudaStream_t s, void* scratch);
+// Householder QR of node tensors, one block per task {A, R, Qs, m, n}: A (m x n)
+// replaced by its thin Q, R (n x n) written, Qs (m x n) scratch
+struct QRTask {
+  double2* A;
+  double2* R;
+  double2* Qs;
+  int m, n;
+};
+cudaError_t launch_house_qr(const void* tasks, int n_tasks, cudaStream_t s);
 cudaError_t launch_single_hp(const HPTask& task, cudaStream_t s, void* scratch);
 // allocation-free density inverse (scratch in a static device array)
 int64_t static_eig_capacity();

@@ -1822,4 +1822,121 @@ cudaError_t launch_rho_inverse_static(const double2* rho, double2* rhoinv, int n
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// Householder QR of node tensors (qrOrthogonal, complex128 on the FP64 pipe).
+// One block per node: A (m x n, column-major: the node tensor as a
+// (lastBefore x d_up) matrix) is factored in place by n reflectors
+// H_j = I - tau_j v_j v_j^H (v_j in A[j:m, j], the diagonal of R aside);
+// then the thin Q = H_0 ... H_{n-1} [I; 0] is formed in the scratch Qs and
+// copied over A, and R (n x n, column-major, upper triangular) is written to R.
+// Reflector j maps x = A[j:m, j] to alpha e_1 with alpha = -e^{i arg x_0} |x|
+// (the LAPACK / Eigen choice).  Warps take columns (k = j + 1 + warp,
+// j + 1 + warp + 8, ...), each column's dot product a warp reduction.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double2 warp_sum2(double2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+    v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+  }
+  return v;
+}
+
+__global__ void __launch_bounds__(kThreads) k_house_qr(const QRTask* __restrict__ tasks) {
+  const QRTask t = tasks[blockIdx.x];
+  double2* __restrict__ A = t.A;
+  const int m = t.m, n = t.n, steps = min(m, n);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, nw = kThreads / 32;
+  __shared__ double s_tau[112];
+  __shared__ double2 s_alpha[112];
+  __shared__ double s_nrm[kThreads / 32];
+  for (int j = 0; j < steps; ++j) {
+    double2* x = A + (int64_t)m * j;
+    // |x|^2 over rows j..m-1
+    double q = 0.0;
+    for (int i = j + tid; i < m; i += kThreads) q += x[i].x * x[i].x + x[i].y * x[i].y;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if (lane == 0) s_nrm[warp] = q;
+    __syncthreads();
+    if (tid == 0) {
+      double nrm2 = 0.0;
+      for (int w = 0; w < nw; ++w) nrm2 += s_nrm[w];
+      const double2 x0 = x[j];
+      const double ax0 = sqrt(x0.x * x0.x + x0.y * x0.y), nrm = sqrt(nrm2);
+      const double2 ph = ax0 > 0.0 ? make_double2(x0.x / ax0, x0.y / ax0) : make_double2(1.0, 0.0);
+      const double2 alpha = make_double2(-ph.x * nrm, -ph.y * nrm);
+      const double2 v0 = make_double2(x0.x - alpha.x, x0.y - alpha.y);
+      const double vn2 = nrm2 - ax0 * ax0 + v0.x * v0.x + v0.y * v0.y;
+      s_tau[j] = vn2 > 0.0 ? 2.0 / vn2 : 0.0;
+      s_alpha[j] = nrm2 > 0.0 ? alpha : make_double2(0.0, 0.0);
+      x[j] = v0;  // v_j = x - alpha e_1 (rows j..m-1 of column j)
+    }
+    __syncthreads();
+    const double tau = s_tau[j];
+    // columns k > j: a -= tau v (v^H a)
+    for (int k = j + 1 + warp; k < n; k += nw) {
+      double2* a = A + (int64_t)m * k;
+      double2 w = make_double2(0.0, 0.0);
+      for (int i = j + lane; i < m; i += 32) {
+        const double2 vi = x[i], ai = a[i];
+        w.x += vi.x * ai.x + vi.y * ai.y;  // conj(v) a
+        w.y += vi.x * ai.y - vi.y * ai.x;
+      }
+      w = warp_sum2(w);
+      const double2 tw = make_double2(tau * w.x, tau * w.y);
+      for (int i = j + lane; i < m; i += 32) {
+        const double2 vi = x[i];
+        a[i].x -= vi.x * tw.x - vi.y * tw.y;
+        a[i].y -= vi.x * tw.y + vi.y * tw.x;
+      }
+    }
+    __syncthreads();
+  }
+  // R: the upper triangle above the diagonal is final in A, the diagonal is alpha
+  for (int e = tid; e < n * n; e += kThreads) {
+    const int i = e % n, k = e / n;
+    double2 r = make_double2(0.0, 0.0);
+    if (i < k && i < m) r = A[i + (int64_t)m * k];
+    else if (i == k && i < steps) r = s_alpha[i];
+    t.R[e] = r;
+  }
+  // thin Q = H_0 ... H_{n-1} [I; 0], accumulated backwards in Qs
+  double2* __restrict__ Q = t.Qs;
+  for (int64_t e = tid; e < (int64_t)m * n; e += kThreads) {
+    const int i = (int)(e % m), k = (int)(e / m);
+    Q[e] = make_double2(i == k ? 1.0 : 0.0, 0.0);
+  }
+  __syncthreads();
+  for (int j = steps - 1; j >= 0; --j) {
+    const double2* v = A + (int64_t)m * j;
+    const double tau = s_tau[j];
+    for (int k = j + warp; k < n; k += nw) {
+      double2* qk = Q + (int64_t)m * k;
+      double2 w = make_double2(0.0, 0.0);
+      for (int i = j + lane; i < m; i += 32) {
+        const double2 vi = v[i], ai = qk[i];
+        w.x += vi.x * ai.x + vi.y * ai.y;
+        w.y += vi.x * ai.y - vi.y * ai.x;
+      }
+      w = warp_sum2(w);
+      const double2 tw = make_double2(tau * w.x, tau * w.y);
+      for (int i = j + lane; i < m; i += 32) {
+        const double2 vi = v[i];
+        qk[i].x -= vi.x * tw.x - vi.y * tw.y;
+        qk[i].y -= vi.x * tw.y + vi.y * tw.x;
+      }
+    }
+    __syncthreads();
+  }
+  for (int64_t e = tid; e < (int64_t)m * n; e += kThreads) A[e] = Q[e];
+}
+
+cudaError_t launch_house_qr(const void* tasks, int n_tasks, cudaStream_t s) {
+  if (n_tasks <= 0) return cudaSuccess;
+  k_house_qr<<<(unsigned)n_tasks, kThreads, 0, s>>>(static_cast<const QRTask*>(tasks));
+  return cudaGetLastError();
+}
+
 }  // namespace qt

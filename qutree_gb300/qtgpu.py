@@ -105,6 +105,7 @@ def load(build_if_missing: bool = True):
         "qt_stage_launch": ([_vp, ctypes.c_int], ctypes.c_int),
         "qt_probe_fp64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_probe_df64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
+        "qt_qr_orthogonal": ([_vp], ctypes.c_int),
         "qt_rho_inverse_noalloc": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double],
                                    ctypes.c_int),
         "qt_tree_count": ([_vp], ctypes.c_int),
@@ -142,7 +143,7 @@ def exported_symbols():
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
         "qt_tree_count", "qt_energies", "qt_gradient_download", "qt_psi_save", "qt_psi_load",
         "qt_build", "qt_layer_derivatives", "qt_cmf_propagate", "qt_scf", "qt_probe_df64_peak",
-        "qt_cdvr_upload",
+        "qt_cdvr_upload", "qt_qr_orthogonal",
     ]
 
 
@@ -312,6 +313,10 @@ class HamiltonianRepresentation:
         self.ctx.check(self.ctx.L.qt_scf(self.ctx.h, n_iter, n_krylov, n_itp, beta, _ptr(out), cap,
                                          ctypes.byref(cnt)))
         return out[:cnt.value].copy()
+
+    def qr_orthogonal(self):
+        """qrOrthogonal on the uploaded wavefunction, on the device (qt_qr_orthogonal)."""
+        self.ctx.check(self.ctx.L.qt_qr_orthogonal(self.ctx.h))
 
     def psi(self) -> np.ndarray:
         out = np.zeros(self.n_psi, dtype=np.complex128)
