@@ -384,6 +384,15 @@ int qt_last_mode_product(qt_ctx* ctx, void* C, const void* A, const void* B,
 int qt_rho_inverse_noalloc(qt_ctx* ctx, void* rhoinv, const void* rho, int n_mats, int d,
                            double eps);
 
+/* Lower bounds of the shapes the next qt_prepare puts on the tensor cores
+ * (QT_PREC_DF64_TC; QT_PREC_TF32X3 uses the mode-product bound): mode
+ * products with mp_min <= a_in, a_out <= 64, hole products with
+ * hp_min <= a <= 64, accumulations with acc_min <= d <= 64; 65 keeps a kind
+ * on the FP32 pipe.  Defaults 32, 32, 32 (measured on GB300); the autotuner
+ * (qutree_gb300/autotune.py) times probe problems per size on the device
+ * and caches the bounds per device.  QT_ERR_ARG outside 1..65. */
+int qt_set_tc_thresholds(qt_ctx* ctx, int mp_min, int hp_min, int acc_min);
+
 /* qrOrthogonal (include/TreeClasses/TensorTree_Implementation.h:173-187) on
  * the uploaded wavefunction, in place on the device: bottom-up, every
  * non-top node tensor, as a (lastBefore x d_up) matrix, is replaced by the

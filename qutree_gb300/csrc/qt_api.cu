@@ -33,6 +33,7 @@ struct qt_ctx {
   qt::OpTable ops;
   qt::SopDesc sop;
   qt::CdvrDesc cdvr;  // potential of a Hamiltonian with hasV (qt_cdvr_upload)
+  qt::TcTune tune;     // tensor-core bounds for the next qt_prepare (qt_set_tc_thresholds)
   bool have_cdvr = false;
   double eps = 1e-10;
   Plan plan;
@@ -375,6 +376,16 @@ int qt_cdvr_upload(qt_ctx* c, int n_modes, const int* leaf_dim, const double* le
   return QT_OK;
 }
 
+int qt_set_tc_thresholds(qt_ctx* c, int mp_min, int hp_min, int acc_min) {
+  if (!c) return fail(c, QT_ERR_ARG, "null context");
+  for (int v : {mp_min, hp_min, acc_min})
+    if (v < 1 || v > 65) return fail(c, QT_ERR_ARG, "qt_set_tc_thresholds: bounds must lie in 1..65");
+  c->tune.mp = mp_min;
+  c->tune.hp = hp_min;
+  c->tune.acc = acc_min;
+  return QT_OK;
+}
+
 int qt_set_regularization(qt_ctx* c, double eps) {
   if (!c) return fail(c, QT_ERR_ARG, "null context");
   if (!(eps > 0) || !std::isfinite(eps)) return fail(c, QT_ERR_ARG, "eps must be positive and finite");
@@ -407,7 +418,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
   }
   std::string msg = qt::build_plan(c->plan, c->nodes, c->ops, c->sop,
                                    flavour | (scf ? 0x2000 : 0) | (tensor_mp ? 0x8000 : 0), prec, budget, grad,
-                                   cdvr ? &c->cdvr : nullptr);
+                                   cdvr ? &c->cdvr : nullptr, c->tune);
   if (!msg.empty()) return fail(c, QT_ERR_SHAPE, "qt_prepare: " + msg);
   Plan& P = c->plan;
   c->buf_elems[qt::B_PSI] = P.psi_arena;

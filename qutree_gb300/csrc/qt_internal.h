@@ -60,18 +60,26 @@ struct HpTcGroup {
   int n, nchunks;
   int member[kHpTcMembers];
 };
-// Which contractions the planner puts on the tensor cores: shapes from 32 to
-// 64 (padded to at most 64 output columns).  Below 32 the fixed costs of a
-// tile (row exponents, the level recombination, the 128-row tile itself)
-// outweigh the products: on a forest of uneven trees with bonds 4..24 the
-// double-float sweep took 82.7 ms with every shape up to 64 on the tensor
-// cores, 57.2 ms with the threshold (as many as on the FP32 pipe alone).
-// hole product: 32 <= a <= 64 and at least two 64-k chunks of reduction
-inline bool hp_tc_eligible(int before, int a, int after) {
-  return a >= 32 && a <= 64 && (int64_t)before * after >= 2 * kHpTcChunk;
+// Which contractions the planner puts on the tensor cores: shapes from a
+// lower bound per kind to 64 (padded to at most 64 output columns).  Below
+// the bound the fixed costs of a tile (row exponents, the level
+// recombination, the 128-row tile itself) outweigh the products.  The
+// default bounds, 32, were measured on a forest of uneven trees with bonds
+// 4..24: the double-float sweep took 82.7 ms with every shape up to 64 on the
+// tensor cores, 57.2 ms with the bounds (as on the FP32 pipe alone);
+// qt_set_tc_thresholds takes bounds found by the autotuner
+// (qutree_gb300/autotune.py).  65 keeps a kind off the tensor cores.
+struct TcTune {
+  int mp = 32, hp = 32, acc = 32;
+};
+// hole product: lo <= a <= 64 and at least two 64-k chunks of reduction
+inline bool hp_tc_eligible(int before, int a, int after, int lo = 32) {
+  return a >= lo && a <= 64 && (int64_t)before * after >= 2 * kHpTcChunk;
 }
-// mode product (not diagonal): 32 <= a_in, a_out <= 64
-inline bool mp_tc_eligible(int a_in, int a_out) { return a_in >= 32 && a_in <= 64 && a_out >= 32 && a_out <= 64; }
+// mode product (not diagonal): lo <= a_in, a_out <= 64
+inline bool mp_tc_eligible(int a_in, int a_out, int lo = 32) {
+  return a_in >= lo && a_in <= 64 && a_out >= lo && a_out <= 64;
+}
 #ifdef __CUDACC__
 #define QT_HD __host__ __device__
 #else
@@ -103,8 +111,8 @@ struct AccTask {
   void* tc_img = nullptr;  // tensor-core path: images of alpha H_t, one per term (hp_tc_chunk_bytes(., 4))
 };
 // an accumulation the planner puts on the tensor cores (double-float plans):
-// 32 <= d <= 64 and at least 64 rows
-inline bool acc_tc_eligible(int rows, int d) { return d >= 32 && d <= 64 && rows >= 64; }
+// lo <= d <= 64 and at least 64 rows
+inline bool acc_tc_eligible(int rows, int d, int lo = 32) { return d >= lo && d <= 64 && rows >= 64; }
 
 // out = sum_t c_t * M_t for d x d matrices (grouped mean fields).
 struct LinTerm {
@@ -537,6 +545,7 @@ struct Plan {
   int64_t oz_bytes = 0;  // B_OZ: operand images of the tensor-core tasks of one stage (reused by every stage)
   // double-float plans with tensor-core hole products (groups bound to HpTcGroup)
   bool hp_tensor = false;
+  TcTune tune;  // the tensor-core bounds the plan was built with
   struct SHpTcGroup {
     Ref A;
     int before = 0, a = 0, after = 0, n = 0, nchunks = 0;
@@ -586,9 +595,10 @@ double cdvr_plan(Plan& P, const CdvrDesc& D, int part);
 // flavour: 0 reference call sequence, 1 grouped; prec: 0 complex128, 1 double-float;
 // grad: also compute the energy gradient with respect to every node tensor
 // cdvr: the potential of a Hamiltonian with hasV (nullptr: pure SOP)
+// tune: the tensor-core bounds per kind
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
                        const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems,
-                       bool grad = false, const CdvrDesc* cdvr = nullptr);
+                       bool grad = false, const CdvrDesc* cdvr = nullptr, const TcTune& tune = TcTune());
 
 // kernel launches (qt_kernels.cu)
 struct DevTables {

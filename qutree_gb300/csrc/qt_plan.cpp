@@ -469,7 +469,8 @@ class Builder {
     // take the tensor-core path (hp_tensor_items), the others the tiles below
     std::vector<char> tc(t1 - t0, 0);
     if (P.hp_tensor)
-      for (int64_t t = t0; t < t1; ++t) tc[t - t0] = hp_tc_eligible(P.hp[t].before, P.hp[t].a, P.hp[t].after);
+      for (int64_t t = t0; t < t1; ++t)
+        tc[t - t0] = hp_tc_eligible(P.hp[t].before, P.hp[t].a, P.hp[t].after, P.tune.hp);
     double work = 0;
     for (int64_t t = t0; t < t1; ++t)
       if (!tc[t - t0]) work += (double)ntiles(P.hp[t]) * P.hp[t].before * P.hp[t].after;
@@ -588,7 +589,7 @@ class Builder {
     units = 0;
     for (int64_t t = t0; t < t1; ++t) {
       Plan::SAcc& a = P.acc[t];
-      if (a.count < 1 || !acc_tc_eligible(a.rows, a.d)) continue;
+      if (a.count < 1 || !acc_tc_eligible(a.rows, a.d, P.tune.acc)) continue;
       tc[t - t0] = 1;
       a.tc_img = stage_oz_;
       stage_oz_ += (int64_t)a.count * hp_tc_chunk_bytes((a.d + 7) & ~7, 4);
@@ -659,7 +660,7 @@ class Builder {
     std::vector<char> oz(t1 - t0, 0);
     for (int64_t t = t0; t < t1; ++t) {
       auto& m = P.mp[t];
-      if (m.diag || !mp_tc_eligible(m.a_in, m.a_out)) continue;
+      if (m.diag || !mp_tc_eligible(m.a_in, m.a_out, P.tune.mp)) continue;
       oz[t - t0] = 1;
       m.oz_h = stage_oz_;
       // double-float plans: the sum-of-products kernel's image of alpha h;
@@ -2111,9 +2112,10 @@ class Builder {
 
 std::string build_plan(Plan& plan, const std::vector<NodeGeo>& nodes, const OpTable& ops,
                        const SopDesc& sop, int flavour, int prec, int64_t scratch_budget_elems,
-                       bool grad, const CdvrDesc* cdvr) {
+                       bool grad, const CdvrDesc* cdvr, const TcTune& tune) {
   plan = Plan();
   plan.want_grad = grad;
+  plan.tune = tune;
   try {
     if (prec < 0 || prec > 2) throw std::runtime_error("unknown precision");
     const bool scf = (flavour & 0x2000) != 0;

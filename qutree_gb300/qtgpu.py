@@ -106,6 +106,7 @@ def load(build_if_missing: bool = True):
         "qt_probe_fp64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_probe_df64_peak": ([_vp, ctypes.POINTER(ctypes.c_double)], ctypes.c_int),
         "qt_qr_orthogonal": ([_vp], ctypes.c_int),
+        "qt_set_tc_thresholds": ([_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int], ctypes.c_int),
         "qt_rho_inverse_noalloc": ([_vp, _vp, _vp, ctypes.c_int, ctypes.c_int, ctypes.c_double],
                                    ctypes.c_int),
         "qt_tree_count": ([_vp], ctypes.c_int),
@@ -143,7 +144,7 @@ def exported_symbols():
         "qt_stage_info", "qt_stage_launch", "qt_probe_fp64_peak", "qt_rho_inverse_noalloc",
         "qt_tree_count", "qt_energies", "qt_gradient_download", "qt_psi_save", "qt_psi_load",
         "qt_build", "qt_layer_derivatives", "qt_cmf_propagate", "qt_scf", "qt_probe_df64_peak",
-        "qt_cdvr_upload", "qt_qr_orthogonal",
+        "qt_cdvr_upload", "qt_qr_orthogonal", "qt_set_tc_thresholds",
     ]
 
 
@@ -239,9 +240,13 @@ class HamiltonianRepresentation:
 
     def __init__(self, H: SOP, tree: Tree, flavour: int = QT_PLAN_REFERENCE, eps: float = 1e-10,
                  device: int = 0, ctx: Context | None = None, potential=None, leaf_x=None,
-                 aligned_hole_grids: bool = False):
+                 aligned_hole_grids: bool = False, tc_thresholds=None):
         """potential (a PolyPotential) with leaf_x (mode -> DVR grid points):
-        the Hamiltonian also has that potential, applied by CDVR."""
+        the Hamiltonian also has that potential, applied by CDVR.
+        tc_thresholds: (mp, hp, acc) lower bounds of the shapes put on the
+        tensor cores, or "auto" for the bounds the autotuner cached for this
+        device (qutree_gb300.autotune; the built-in bounds when none is
+        cached); None keeps the built-in bounds."""
         if potential is not None:
             flavour |= QT_PLAN_CDVR
         self.tree, self.H, self.flavour = tree, H, flavour
@@ -255,6 +260,11 @@ class HamiltonianRepresentation:
         self.ctx.check(L.qt_sop_upload(h, len(kind), kind, odim, ooff, _ptr(odata), len(H),
                                        _ptr(coeff), ptr, modes, opids))
         self.ctx.check(L.qt_set_regularization(h, eps))
+        if tc_thresholds == "auto":
+            from . import autotune
+            tc_thresholds = autotune.cached(device)
+        if tc_thresholds is not None:
+            self.ctx.check(L.qt_set_tc_thresholds(h, *(int(v) for v in tc_thresholds)))
         if potential is not None:
             f = tree.n_leaves
             ldim = np.array([len(leaf_x[m]) for m in range(f)], dtype=np.int32)
