@@ -514,6 +514,7 @@ int qt_prepare(qt_ctx* c, int flavour) {
     qt::HpTcGroup g;
     g.A = ptr_of(c, s.A);
     g.img = (unsigned char*)c->buf[qt::B_OZ] + s.img;
+    g.ex = (unsigned char*)c->buf[qt::B_OZ] + s.ex;
     g.before = s.before;
     g.a = s.a;
     g.after = s.after;
@@ -931,7 +932,7 @@ int64_t kernels_in(const qt::Plan& P, int64_t b0, int64_t b1) {
   for (int64_t i = b0; i < b1; ++i) {
     const qt::Stage& st = P.stages[i];
     if (st.kind == qt::ST_HP)
-      n += st.nseg + (st.nhti > 0 ? (st.nhtu > 0 ? 2 : 1) : 0) + (st.aux ? 1 : 0);
+      n += st.nseg + (st.nhti > 0 ? (st.nhtu > 0 ? 3 : 2) : 0) + (st.aux ? 1 : 0);
     else if (st.kind == qt::ST_MP)
       n += (st.n_tiles > 0 ? 1 : 0) + (st.noz > 0 ? (st.nozt > 0 ? 2 : 1) : 0);
     else if (st.kind == qt::ST_ACC)

@@ -55,6 +55,7 @@ constexpr int kHpTcMembers = 8;    // tasks per group (a >= 16)
 struct HpTcGroup {
   const double2* A;
   unsigned char* img;  // A's operand images, one per chunk of hp_tc_kc(ap) k
+  unsigned char* ex;   // biased row exponents of the members' B, 128 rows per chunk
   int before, a, after;
   int ap;              // a padded to a multiple of 8
   int n, nchunks;
@@ -551,6 +552,7 @@ struct Plan {
     int before = 0, a = 0, after = 0, n = 0, nchunks = 0;
     int member[kHpTcMembers] = {0, 0, 0, 0, 0, 0, 0, 0};
     int64_t img = 0;  // byte offset of the images in B_OZ
+    int64_t ex = 0;   // byte offset of the row exponents in B_OZ (128 per chunk)
   };
   std::vector<SHpTcGroup> hp_tc_groups;
   std::vector<int4> hp_tc_items;  // (group, z, first chunk, end chunk)

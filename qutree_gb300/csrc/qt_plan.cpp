@@ -545,6 +545,8 @@ class Builder {
         } else {
           g.img = im->second;
         }
+        g.ex = stage_oz_;  // the row exponents of this group's B, written by the items' pre-pass
+        stage_oz_ += (int64_t)g.nchunks * 128;
         P.hp_tc_groups.push_back(g);
         open[key] = gi;
         it = open.find(key);

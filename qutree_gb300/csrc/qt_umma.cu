@@ -710,6 +710,73 @@ __global__ void __launch_bounds__(256) k_tcs_img(TcsArgs g, const int2* __restri
   if (threadIdx.x < 64) reinterpret_cast<int*>(img + (size_t)steps * kDig * 3 * np * 32)[threadIdx.x] = fx[threadIdx.x];
 }
 
+// pre-pass of the hole products: the biased row exponents E of the M side
+// (the members' B rows j, 128 per item) over the item's chunk, into the
+// group's table, so that the producers need not read every row twice.  Block
+// (item, q) takes the rows 32 q .. 32 q + 31.  With before > 1 a row's k are
+// contiguous in memory: a warp takes four rows at once, its lanes along k;
+// with before == 1 consecutive rows are: lane l takes row 32 q + l, the
+// eight warps an eighth of the chunk each.
+__global__ void __launch_bounds__(256) k_hp_ex(TcsArgs g) {
+  const int4 itm = g.items[g.item0 + blockIdx.x];
+  const HpTcGroup& G = g.groups[itm.x];
+  const int before = G.before, a = G.a, K = before * G.after, kc = hp_tc_kc(G.ap);
+  const int k0 = itm.z * kc, k1 = min(K, k0 + kc);
+  const int rows = G.n * a, m0 = 32 * (int)blockIdx.y;
+  unsigned char* ex = G.ex + (size_t)itm.z * kRows;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (before > 1) {
+    int e[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int m = m0 + warp + 8 * r;
+      e[r] = 1;
+      if (m < rows) {
+        const int mi = m / a, j = m - mi * a;
+        const float4* __restrict__ B = reinterpret_cast<const float4*>(g.hp[G.member[mi]].B);
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {  // kc <= 128: four k per lane
+          const int k = k0 + lane + 32 * s;
+          if (k < k1) {
+            const int c = k / before, b = k - c * before;
+            const float4 x = __ldg(B + b + (int64_t)before * j + (int64_t)before * a * c);
+            e[r] = max(e[r], max(fexp(x.x), fexp(x.z)));
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      int v = e[r];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+      if (lane == 0) ex[m0 + warp + 8 * r] = (uint8_t)v;
+    }
+  } else {
+    __shared__ int part[8][32];
+    const int m = m0 + lane;
+    int e = 1;
+    if (m < rows) {
+      const int mi = m / a, j = m - mi * a;
+      const float4* __restrict__ B = reinterpret_cast<const float4*>(g.hp[G.member[mi]].B);
+      const int span = (k1 - k0 + 7) >> 3;
+      const int ka = k0 + warp * span, kb = min(k1, ka + span);
+      for (int k = ka; k < kb; ++k) {
+        const float4 x = __ldg(B + j + (int64_t)a * k);
+        e = max(e, max(fexp(x.x), fexp(x.z)));
+      }
+    }
+    part[warp][lane] = e;
+    __syncthreads();
+    if (warp == 0) {
+      int v = part[0][lane];
+#pragma unroll
+      for (int w = 1; w < 8; ++w) v = max(v, part[w][lane]);
+      ex[m] = (uint8_t)v;
+    }
+  }
+}
+
 // the producers' view of row r of an item: its source of X and validity
 struct TcsRow {
   bool valid;
@@ -821,9 +888,12 @@ __global__ void __launch_bounds__(kThreadsTc, 1) k_tcs(TcsArgs g) {
               x[i] = (R.valid && k0 + i < K) ? __ldg(X + rows * (k0 + i)) : make_float4(0.f, 0.f, 0.f, 0.f);
           }
         };
-        // the row's largest exponent over the unit's k, eight loads in flight
+        // the row's largest exponent over the unit's k (hole products: from
+        // the pre-pass), eight loads in flight
         int eb = 1;
-        if (R.valid)
+        if (OP == TCS_HP)
+          eb = g.groups[itm.x].ex[(size_t)(itm.z + u) * kRows + r];
+        else if (R.valid)
           for (int h8 = 0; h8 < 2 * I.nks; ++h8) {
             float4 x[8];
             load8(x, h8 >> 1, h8 & 1);
@@ -1097,6 +1167,7 @@ cudaError_t launch_tf(const MPTask* tasks, const int2* tiles, int64_t first_tile
 template <int OP>
 cudaError_t launch_tcs(const TcsArgs& g, const int2* img_units, int64_t first_unit, int64_t n_units, cudaStream_t s) {
   if (n_units > 0) k_tcs_img<OP><<<(unsigned)n_units, 256, 0, s>>>(g, img_units, first_unit);
+  if (OP == TCS_HP) k_hp_ex<<<dim3((unsigned)g.n_items, kRows / 32), 256, 0, s>>>(g);
   unsigned grid = 0;
   cudaError_t e = tc_grid(g.n_items, &grid);
   if (e != cudaSuccess) return e;
