@@ -22,11 +22,17 @@
 //  * the 3x3 symmetric eigenproblem of the optimiser (Matrix::rDiag, Eigen's
 //    SelfAdjointEigenSolver in the reference) is solved for what the
 //    optimiser uses of it -- the eigenvector of the largest eigenvalue as
-//    ratios v0/v2, v1/v2 and its squared first two components: the largest
-//    root of the characteristic polynomial by Newton's method from the
-//    Gershgorin bound (monotone from above), then v as the largest cross
-//    product of two rows of H - lambda (absolute accuracy like a rotation
-//    method's);
+//    ratios v0/v2, v1/v2 and its squared first two components: H is scaled
+//    by a power of two (largest |entry| in [1, 2)); the largest root of the
+//    characteristic polynomial comes from Newton's method in binary32 from
+//    the Gershgorin bound, then Newton's method in binary64, monotone from
+//    above, from that root plus 2^-17 (or from the Gershgorin bound when the
+//    signs of p, p' and p'' there do not prove it an upper bound), each
+//    step's quotient taken in binary32, until a step is below 2^-30; then v
+//    is the largest cross product of two rows of H - lambda (absolute
+//    accuracy like a rotation method's).  Binary32 values enter and leave
+//    by bit operations: truncation of the significand to 23 bits, zero
+//    below 2^-126, infinity above the binary32 range;
 //  * the two step-size searches stop after 64 rounds at the latest (the
 //    reference's own conditions end them far earlier).
 #include <cmath>
@@ -72,25 +78,111 @@ struct Mat {
 extern "C" void orc_eig3_top(const double H[9], double* u0, double* u1, double* top2);
 void eig3_top(const double H[9], double* u0, double* u1, double* top2) { orc_eig3_top(H, u0, u1, top2); }
 }  // namespace
+// binary64 -> binary32 by truncation of the significand (bit operations, the
+// same on every host and on the device); zero below 2^-126, infinity above
+static float f32_trunc(double x) {
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  const uint32_t sign = (uint32_t)(b >> 32) & 0x80000000u;
+  const int e = (int)((b >> 52) & 0x7ff) - 896;
+  uint32_t r;
+  if (e <= 0)
+    r = sign;
+  else if (e >= 255)
+    r = sign | 0x7f800000u;
+  else
+    r = sign | ((uint32_t)e << 23) | (uint32_t)((b >> 29) & 0x7fffffu);
+  float f;
+  std::memcpy(&f, &r, 4);
+  return f;
+}
+// binary32 -> binary64, exact for normal numbers; subnormals become zero
+static double f64_of(float f) {
+  uint32_t r;
+  std::memcpy(&r, &f, 4);
+  const uint64_t sign = (uint64_t)(r & 0x80000000u) << 32;
+  const uint32_t e = (r >> 23) & 0xffu;
+  uint64_t b;
+  if (e == 0)
+    b = sign;
+  else if (e == 255)
+    b = sign | 0x7ff0000000000000ull | ((uint64_t)(r & 0x7fffffu) << 29);
+  else
+    b = sign | ((uint64_t)(e + 896) << 52) | ((uint64_t)(r & 0x7fffffu) << 29);
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
+}
 extern "C" void orc_eig3_top(const double H[9], double* u0, double* u1, double* top2) {
-  const double h00 = H[0], h01 = H[3], h02 = H[6], h11 = H[4], h12 = H[7], h22 = H[8];
+  double h00 = H[0], h01 = H[3], h02 = H[6], h11 = H[4], h12 = H[7], h22 = H[8];
+  // scale by 2^(1023 - e), e the largest biased exponent: max |entry| in [1, 2)
+  {
+    const double hv[6] = {h00, h01, h02, h11, h12, h22};
+    int e = 0;
+    for (int i = 0; i < 6; ++i) {
+      uint64_t b;
+      std::memcpy(&b, &hv[i], 8);
+      const int ei = (int)((b >> 52) & 0x7ff);
+      if (ei > e) e = ei;
+    }
+    if (e >= 1 && e <= 2045) {
+      const uint64_t sb = (uint64_t)(2046 - e) << 52;
+      double sc;
+      std::memcpy(&sc, &sb, 8);
+      h00 *= sc;
+      h01 *= sc;
+      h02 *= sc;
+      h11 *= sc;
+      h12 *= sc;
+      h22 *= sc;
+    }
+  }
   const double tr = h00 + h11 + h22;
   const double m = (h00 * h11 - h01 * h01) + (h00 * h22 - h02 * h02) + (h11 * h22 - h12 * h12);
   const double det = h00 * (h11 * h22 - h12 * h12) - h01 * (h01 * h22 - h12 * h02) + h02 * (h01 * h12 - h11 * h02);
   // Gershgorin upper bound of the largest eigenvalue
-  double lam = h00 + std::fabs(h01) + std::fabs(h02);
+  double lam_g = h00 + std::fabs(h01) + std::fabs(h02);
   const double r1 = h11 + std::fabs(h01) + std::fabs(h12);
   const double r2 = h22 + std::fabs(h02) + std::fabs(h12);
-  if (r1 > lam) lam = r1;
-  if (r2 > lam) lam = r2;
-  // p(l) = -l^3 + tr l^2 - m l + det; Newton decreases l monotonically to the largest root
+  if (r1 > lam_g) lam_g = r1;
+  if (r2 > lam_g) lam_g = r2;
+  // binary32 Newton from the bound: p(l) = -l^3 + tr l^2 - m l + det
+  float fl = f32_trunc(lam_g);
+  {
+    const float f00 = f32_trunc(h00), f01 = f32_trunc(h01), f02 = f32_trunc(h02);
+    const float f11 = f32_trunc(h11), f12 = f32_trunc(h12), f22 = f32_trunc(h22);
+    const float ftr = f00 + f11 + f22;
+    const float fm = (f00 * f11 - f01 * f01) + (f00 * f22 - f02 * f02) + (f11 * f22 - f12 * f12);
+    const float fdet = f00 * (f11 * f22 - f12 * f12) - f01 * (f01 * f22 - f12 * f02) + f02 * (f01 * f12 - f11 * f02);
+    for (int it = 0; it < 40; ++it) {
+      const float p = ((-fl + ftr) * fl - fm) * fl + fdet;
+      const float dp = (-3.0f * fl + 2.0f * ftr) * fl - fm;
+      if (!(dp < 0.0f)) break;
+      const float nx = fl - p / dp;
+      if (!(nx < fl)) break;
+      fl = nx;
+    }
+  }
+  // binary64 Newton, monotone from above; p < 0, p' < 0 and p'' < 0 at the
+  // start prove it above the largest root
+  double lam = f64_of(fl) + 0x1p-17;
+  double p = ((-lam + tr) * lam - m) * lam + det;
+  double dp = (-3.0 * lam + 2.0 * tr) * lam - m;
+  if (!(p < 0.0 && dp < 0.0 && 3.0 * lam > tr)) {
+    lam = lam_g;
+    p = ((-lam + tr) * lam - m) * lam + det;
+    dp = (-3.0 * lam + 2.0 * tr) * lam - m;
+  }
   for (int it = 0; it < 100; ++it) {
-    const double p = ((-lam + tr) * lam - m) * lam + det;
-    const double dp = (-3.0 * lam + 2.0 * tr) * lam - m;
     if (!(dp < 0.0)) break;
-    const double nxt = lam - p / dp;
+    double step = f64_of(f32_trunc(p) / f32_trunc(dp));
+    if (!(std::fabs(step) <= 16.0)) step = p / dp;
+    const double nxt = lam - step;
     if (!(nxt < lam)) break;
     lam = nxt;
+    if (step <= 0x1p-30) break;
+    p = ((-lam + tr) * lam - m) * lam + det;
+    dp = (-3.0 * lam + 2.0 * tr) * lam - m;
   }
   // eigenvector: the largest cross product of two rows of H - lambda
   const double m00 = h00 - lam, m11 = h11 - lam, m22 = h22 - lam;
