@@ -82,6 +82,23 @@ def lib(fast: bool = False):
         ctypes.c_int, ctypes.c_void_p, _i32, _i32, _i32,
         ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
         ctypes.c_double, ctypes.c_int, ctypes.c_int]
+    L.orc_frozen_new.restype = ctypes.c_void_p
+    L.orc_frozen_new.argtypes = [
+        ctypes.c_int, ctypes.c_int, _i32, _i32, _i32, _i32, _i32,
+        ctypes.c_int, _i32, _i32, _i64, ctypes.c_void_p,
+        ctypes.c_int, ctypes.c_void_p, _i32, _i32, _i32, ctypes.c_double]
+    L.orc_frozen_build.restype = ctypes.c_int
+    L.orc_frozen_build.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.orc_frozen_deriv.restype = ctypes.c_int
+    L.orc_frozen_deriv.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                   ctypes.c_void_p]
+    L.orc_frozen_deriv_node.restype = ctypes.c_int
+    L.orc_frozen_deriv_node.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_double,
+                                        ctypes.c_double, ctypes.c_void_p]
+    L.orc_frozen_rho.restype = ctypes.c_int
+    L.orc_frozen_rho.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.orc_frozen_free.restype = None
+    L.orc_frozen_free.argtypes = [ctypes.c_void_p]
     _libs[fast] = L
     return L
 
@@ -241,6 +258,64 @@ def cmf(tree, sop, psi, dt, n_steps, n_sub=1, phase=1.0, eps=1e-10, backend=LOOP
     if rc != 0:
         raise RuntimeError(f"oracle cmf failed: {rc}")
     return y
+
+
+class Frozen:
+    """Frozen-matrix session: build(psi) = HamiltonianRepresentation::build,
+    deriv(psi) = LayerDerivative of every node with those matrices, rho() =
+    the build's density matrices (per node d_up x d_up, column-major, in
+    node order)."""
+
+    def __init__(self, tree, sop, eps=1e-10, phase=1.0, backend=LOOPS, fast=False):
+        self.tree, self.phase = tree, complex(phase)
+        self._desc = tree.descriptor()
+        kind, odim, ooff, odata = sop.ops.descriptor()
+        coeff, ptr, modes, opids = sop.descriptor()
+        self._keep = (kind, odim, ooff, np.ascontiguousarray(odata), np.ascontiguousarray(coeff), ptr,
+                      modes, opids)
+        k = self._keep
+        self.n = int(tree.offsets()[-1])
+        self.nrho = sum(n.d_up * n.d_up for n in tree.nodes)
+        self.L = lib(fast)
+        order, dims, parent, child_idx, leaf_mode = self._desc
+        self.h = self.L.orc_frozen_new(backend, tree.n_nodes, order, dims, parent, child_idx, leaf_mode,
+                                       len(k[0]), k[0], k[1], k[2], k[3].ctypes.data, len(sop),
+                                       k[4].ctypes.data, k[5], k[6], k[7], eps)
+
+    def build(self, psi):
+        psi = np.ascontiguousarray(psi, dtype=np.complex128)
+        self.L.orc_frozen_build(self.h, psi.ctypes.data)
+
+    def deriv(self, psi):
+        psi = np.ascontiguousarray(psi, dtype=np.complex128)
+        out = np.zeros(self.n, np.complex128)
+        self.L.orc_frozen_deriv(self.h, psi.ctypes.data, self.phase.real, self.phase.imag, out.ctypes.data)
+        return out
+
+    def deriv_node(self, n, phi):
+        """LayerDerivative of node n at node tensor phi (other nodes untouched)."""
+        phi = np.ascontiguousarray(phi, dtype=np.complex128)
+        out = np.zeros(phi.size, np.complex128)
+        if self.L.orc_frozen_deriv_node(self.h, n, phi.ctypes.data, self.phase.real, self.phase.imag,
+                                        out.ctypes.data) != 0:
+            raise ValueError("node index out of range")
+        return out
+
+    def rho(self):
+        out = np.zeros(self.nrho, np.complex128)
+        self.L.orc_frozen_rho(self.h, out.ctypes.data)
+        return out
+
+    def close(self):
+        if self.h:
+            self.L.orc_frozen_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def sparse_offsets(tree, sop):

@@ -777,4 +777,76 @@ int orc_cmf(int backend, int n_nodes, const int* order, const int* dims, const i
   return 0;
 }
 
+// Frozen-matrix session (the LayerInterface of CMFIntegrator,
+// src/Applications/CMFIntegrator.cpp:11-23, include/TreeClasses/LayerInterface.h):
+// orc_frozen_build = HamiltonianRepresentation::build at a wavefunction;
+// orc_frozen_deriv = LayerDerivative of every node at another wavefunction
+// with those matrices (node n's result depends on node n's tensor only);
+// orc_frozen_rho = the density matrices of the build.  The caller keeps the
+// operator and SOP arrays alive for the session's life.
+struct Frozen {
+  Tree t;
+  Ops ops;
+  Sop s;
+  std::vector<cd> at;
+  Sweep* sw = nullptr;
+};
+
+void* orc_frozen_new(int backend, int n_nodes, const int* order, const int* dims, const int* parent,
+                     const int* child_idx, const int* leaf_mode, int n_ops, const int* op_kind,
+                     const int* op_dim, const int64_t* op_off, const double* op_data, int n_terms,
+                     const double* coeff, const int* term_ptr, const int* term_mode, const int* term_op,
+                     double eps) {
+  (void)n_ops;
+  Frozen* f = new Frozen;
+  f->t = make_tree(n_nodes, order, dims, parent, child_idx, leaf_mode);
+  f->ops = Ops{op_kind, op_dim, op_off, (const cd*)op_data};
+  f->s = Sop{n_terms, (const cd*)coeff, term_ptr, term_mode, term_op};
+  f->at.assign(f->t.off[f->t.n], cd(0));
+  f->sw = new Sweep(f->t, f->ops, f->s, (Backend)backend, f->at.data(), eps);
+  return f;
+}
+
+int orc_frozen_build(void* h, const double* psi) {
+  Frozen* f = (Frozen*)h;
+  std::memcpy(f->at.data(), psi, sizeof(cd) * f->at.size());
+  f->sw->psi = f->at.data();
+  f->sw->density();
+  f->sw->invert();
+  f->sw->represent();
+  f->sw->meanfield();
+  return 0;
+}
+
+int orc_frozen_deriv(void* h, const double* psi, double phase_re, double phase_im, double* out) {
+  Frozen* f = (Frozen*)h;
+  std::memcpy(f->at.data(), psi, sizeof(cd) * f->at.size());
+  f->sw->psi = f->at.data();
+  const cd phase(phase_re, phase_im);
+  for (int n = 0; n < f->t.n; ++n) f->sw->layer_derivative(n, (cd*)out + f->t.off[n], phase);
+  return 0;
+}
+
+// LayerDerivative of node n alone, at node tensor phi
+int orc_frozen_deriv_node(void* h, int n, const double* phi, double phase_re, double phase_im, double* out) {
+  Frozen* f = (Frozen*)h;
+  if (n < 0 || n >= f->t.n) return 1;
+  std::memcpy(f->at.data() + f->t.off[n], phi, sizeof(cd) * f->t.size[n]);
+  f->sw->psi = f->at.data();
+  f->sw->layer_derivative(n, (cd*)out, cd(phase_re, phase_im));
+  return 0;
+}
+
+int orc_frozen_rho(void* h, double* out) {
+  Frozen* f = (Frozen*)h;
+  std::memcpy(out, f->sw->rho.data(), sizeof(cd) * f->sw->rho.size());
+  return 0;
+}
+
+void orc_frozen_free(void* h) {
+  Frozen* f = (Frozen*)h;
+  delete f->sw;
+  delete f;
+}
+
 }  // extern "C"

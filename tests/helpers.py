@@ -112,3 +112,21 @@ def node_matrices(tree, flat):
         out.append(flat[off:off + d * d].reshape((d, d), order="F"))
         off += d * d
     return out
+
+
+def tree_overlap(tree, psi_a, psi_b):
+    """<Psi_a|Psi_b> of two flat tensor trees (QuTree's dotProduct, bottom
+    up: S_node = Phi_a^H (Phi_b with the children's S applied), the top's
+    (0, 0) element); independent of the gauge of either tree."""
+    off = tree.offsets()
+    S = {}
+    for n in tree.nodes:
+        a = n.address
+        shape = list(n.shape)
+        A = psi_a[off[a]:off[a + 1]].reshape(shape, order="F")
+        Bt = psi_b[off[a]:off[a + 1]].reshape(shape, order="F")
+        for k, c in enumerate(n.children):
+            Bt = np.moveaxis(np.tensordot(S[c], Bt, axes=([1], [k])), 0, k)
+        d = shape[-1]
+        S[a] = A.reshape((-1, d), order="F").conj().T @ Bt.reshape((-1, d), order="F")
+    return S[tree.top.address][0, 0]

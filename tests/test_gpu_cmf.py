@@ -80,3 +80,31 @@ def test_cmf_conserves_energy_and_relaxes_in_imaginary_time():
         h.close()
     assert abs(e_real - e0) <= 1e-4 * abs(e0)
     assert e_imag < e0 - 0.1 * abs(e0)
+
+
+@pytest.mark.parametrize("flavour,tol", [(qtgpu.QT_PLAN_GROUPED, 1e-9),
+                                         (qtgpu.QT_PLAN_GROUPED | qtgpu.QT_PREC_DF64, 1e-8)])
+def test_adaptive_cmf_matches_the_restatement(flavour, tol):
+    # CMFIntegrator::Integrate with Bulirsch-Stoer node integrators on the
+    # device's frozen-matrix derivatives (qutree_gb300/cmf.py), against the
+    # oracle's sequential restatement (oracle/cmf_bs.py) on the oracle's
+    # derivatives: the same accept / refuse decisions, the same wavefunction
+    import cmf_bs as B
+    from helpers import tree_overlap
+    from qutree_gb300.cmf import CMFIntegrator
+    tree, sop, psi = config_problem(0)
+    flat = psi.flat()
+    want, dt_want, st = B.cmf_integrate(tree, O.Frozen(tree, sop), flat, 0.0, 2.0, 0.5, 2.0, 1e-6, 1e-7)
+    h = qtgpu.HamiltonianRepresentation(sop, tree, flavour=flavour)
+    try:
+        I = CMFIntegrator(h)
+        got, dt_got = I.integrate(flat, 0.0, 2.0, 0.5, acc_root=1e-6, acc_leaf=1e-7)
+        on_device = h.psi()
+    finally:
+        h.close()
+    assert np.array_equal(on_device, got)
+    assert I.stats["accepted"] == st["accepted"] and I.stats["refused"] == st["refused"]
+    assert rel_err(got, want) <= tol
+    ov = tree_overlap(tree, want, got) / np.sqrt(tree_overlap(tree, want, want).real *
+                                                 tree_overlap(tree, got, got).real)
+    assert abs(1 - abs(ov)) < tol
