@@ -303,7 +303,8 @@ int qt_tree_count(const qt_ctx* ctx);
  * ascending address order), for t < n_trees. Synchronises. */
 int qt_energies(qt_ctx* ctx, double* out, int n_trees);
 
-/* Matrices of the last sweep.  Sparse layout (QT_MAT_HMAT / QT_MAT_HCON):
+/* Matrices of the last sweep or qt_build (QT_ERR_STATE before either).
+ * Sparse layout (QT_MAT_HMAT / QT_MAT_HCON):
  * for each term, for each node on its leaf-to-root paths (SparseTree with
  * tail, src/TreeClasses/SparseTree.cpp:33-89) in address order, a d_up x d_up
  * matrix.  Dense layout (QT_MAT_RHO / QT_MAT_RHOINV): per node in address

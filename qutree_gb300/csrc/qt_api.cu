@@ -1138,7 +1138,8 @@ int64_t qt_matrices_size(const qt_ctx* c, int which) {
 int qt_matrices_download(qt_ctx* c, int which, double* out) {
   if (!c || !out) return fail(c, QT_ERR_ARG, "null argument");
   QT_DEVICE(c);
-  if (!c->swept) return fail(c, QT_ERR_STATE, "no sweep has run");
+  // the build graph writes every matrix set; a sweep runs it too
+  if (!c->swept && !c->built) return fail(c, QT_ERR_STATE, "no sweep or qt_build has run");
   const Plan& P = c->plan;
   if (which == QT_MAT_CDVR) {
     if (!P.cdvr) return fail(c, QT_ERR_STATE, "plan prepared without QT_PLAN_CDVR");
