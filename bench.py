@@ -593,9 +593,10 @@ def run_ours(args, ws, rank, local):
         "data": "synthetic (seeded N(0,1) node tensors, QR-orthonormalised)",
         "config": {"workload": WORKLOAD, "plan": "compressed (per node one block matrix of the terms "
                    "inside its subtree, summed mean fields per boundary restriction, represent chains "
-                   "kept in HBM for Apply), double-float arithmetic: mode products on the tcgen05 tensor "
-                   "cores as exact bf16 digit products, the other contractions on the FP32 pipe "
-                   "(complex128 in and out; density inverses complex128)",
+                   "kept in HBM for Apply), double-float arithmetic: mode products, hole products and "
+                   "last-mode accumulations of shapes 32..64 on the tcgen05 tensor cores as exact bf16 "
+                   "digit products, the rest on the FP32 pipe (complex128 in and out; density inverses "
+                   "complex128)",
                    "parallelism": f"replicas x{ws}",
                    "l2": "flushed between timed sweeps (256 MB fill, outside the events)"},
         "energy": energy,
