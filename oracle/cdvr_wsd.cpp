@@ -10,7 +10,8 @@
 // The iteration is discontinuous in its inputs (accept / reject decisions of
 // the rational-function optimiser), so this file fixes one operation order
 // and the device kernel follows it bit for bit:
-//  * a complex product is (ac - bd) + i(ad + bc), sums are left to right and
+//  * a complex product is (ac - bd) + i(ad + bc) (the Givens rotations' real
+//    c multiplies both parts alone), sums are left to right and
 //    nothing is fused (compiled with -ffp-contract=off; the device file with
 //    -fmad=false); a sum over the matrices of a problem is the pairwise tree
 //    of the values padded with zeros to a power of two (level by level,
@@ -344,12 +345,15 @@ struct Problem {
   }
 
   // givensRotation (src/Core/JacobiRotationFramework.cpp:4-30)
+  // c is real (the optimiser's c always is): c x = (c.r x.r, c.r x.i); the
+  // full complex product would differ only in the sign of a zero
+  static cd rmul(cd c, cd x) { return cd{c.r * x.r, c.r * x.i}; }
   static void givens(Mat& B, cd c, cd s, int i, int j) {
     const int d = B.d;
     std::vector<cd> c0(d), c1(d);
     for (int r = 0; r < d; ++r) {
-      c0[r] = cadd(cmul(c, B(r, i)), cmul(s, B(r, j)));
-      c1[r] = csub(cmul(c, B(r, j)), cmul(cconj(s), B(r, i)));
+      c0[r] = cadd(rmul(c, B(r, i)), cmul(s, B(r, j)));
+      c1[r] = csub(rmul(c, B(r, j)), cmul(cconj(s), B(r, i)));
     }
     for (int r = 0; r < d; ++r) {
       B(r, i) = c0[r];
@@ -360,8 +364,8 @@ struct Problem {
       c1[r] = B(j, r);
     }
     for (int r = 0; r < d; ++r) {
-      B(i, r) = cadd(cmul(c, c0[r]), cmul(cconj(s), c1[r]));
-      B(j, r) = csub(cmul(c, c1[r]), cmul(s, c0[r]));
+      B(i, r) = cadd(rmul(c, c0[r]), cmul(cconj(s), c1[r]));
+      B(j, r) = csub(rmul(c, c1[r]), cmul(s, c0[r]));
     }
   }
 
@@ -369,8 +373,8 @@ struct Problem {
   static void givens_trafo(Mat& T, cd c, cd s, int i, int j) {
     for (int r = 0; r < T.d; ++r) {
       const cd ti = T(r, i), tj = T(r, j);
-      T(r, i) = cadd(cmul(c, ti), cmul(s, tj));
-      T(r, j) = csub(cmul(c, tj), cmul(cconj(s), ti));
+      T(r, i) = cadd(rmul(c, ti), cmul(s, tj));
+      T(r, j) = csub(rmul(c, tj), cmul(cconj(s), ti));
     }
   }
 

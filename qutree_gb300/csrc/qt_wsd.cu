@@ -9,7 +9,8 @@
 // discontinuous function of the inputs; this file therefore fixes one
 // operation order, which the CPU restatement follows bit for bit:
 //  * compiled with -fmad=false: no multiply-add is fused; a complex product
-//    is (ac - bd) + i(ad + bc), sums run left to right; a sum over the
+//    is (ac - bd) + i(ad + bc) (a Givens rotation's real c multiplies both
+//    parts alone), sums run left to right; a sum over the
 //    matrices of a problem is the pairwise tree of the values padded with
 //    zeros to a power of two, and the measure adds its per-matrix traces in
 //    index order;
@@ -60,6 +61,8 @@ __device__ __forceinline__ double2 cm(double2 a, double2 b) {
 __device__ __forceinline__ double2 ca(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 cs(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cc(double2 a) { return make_double2(a.x, -a.y); }
+// product with the real c of a rotation: (c x.re, c x.im)
+__device__ __forceinline__ double2 rm(double2 c, double2 a) { return make_double2(c.x * a.x, c.x * a.y); }
 __device__ __forceinline__ double cabs_(double2 a) { return sqrt(a.x * a.x + a.y * a.y); }
 __device__ __forceinline__ double cdiv_re(double2 x, double2 w) {
   return (x.x * w.x + x.y * w.y) / (w.x * w.x + w.y * w.y);
@@ -633,12 +636,12 @@ __device__ void rotations(const Prob& P) {
         if (mi <= n) {
           double2* B = mi < n ? P.X(mi) : P.w;
           const double2 bri = B[r + (int64_t)d * i], brj = B[r + (int64_t)d * j];
-          B[r + (int64_t)d * i] = ca(cm(c, bri), cm(s, brj));
-          B[r + (int64_t)d * j] = cs(cm(c, brj), cm(cc(s), bri));
+          B[r + (int64_t)d * i] = ca(rm(c, bri), cm(s, brj));
+          B[r + (int64_t)d * j] = cs(rm(c, brj), cm(cc(s), bri));
         } else {
           const double2 ti = P.T[r + (int64_t)d * i], tj = P.T[r + (int64_t)d * j];
-          P.T[r + (int64_t)d * i] = ca(cm(c, ti), cm(s, tj));
-          P.T[r + (int64_t)d * j] = cs(cm(c, tj), cm(cc(s), ti));
+          P.T[r + (int64_t)d * i] = ca(rm(c, ti), cm(s, tj));
+          P.T[r + (int64_t)d * j] = cs(rm(c, tj), cm(cc(s), ti));
         }
       }
       bsync();
@@ -647,8 +650,8 @@ __device__ void rotations(const Prob& P) {
         const int mi = e / d, r = e % d;
         double2* B = mi < n ? P.X(mi) : P.w;
         const double2 c0 = B[i + (int64_t)d * r], c1 = B[j + (int64_t)d * r];
-        B[i + (int64_t)d * r] = ca(cm(c, c0), cm(cc(s), c1));
-        B[j + (int64_t)d * r] = cs(cm(c, c1), cm(s, c0));
+        B[i + (int64_t)d * r] = ca(rm(c, c0), cm(cc(s), c1));
+        B[j + (int64_t)d * r] = cs(rm(c, c1), cm(s, c0));
       }
       bsync();
     }
