@@ -82,6 +82,13 @@ def lib(fast: bool = False):
         ctypes.c_int, ctypes.c_void_p, _i32, _i32, _i32,
         ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
         ctypes.c_double, ctypes.c_int, ctypes.c_int]
+    L.orc_scf.restype = ctypes.c_int
+    L.orc_scf.argtypes = [
+        ctypes.c_int, ctypes.c_int, _i32, _i32, _i32, _i32, _i32,
+        ctypes.c_int, _i32, _i32, _i64, ctypes.c_void_p,
+        ctypes.c_int, ctypes.c_void_p, _i32, _i32, _i32,
+        ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+        ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(ctypes.c_int64)]
     L.orc_frozen_new.restype = ctypes.c_void_p
     L.orc_frozen_new.argtypes = [
         ctypes.c_int, ctypes.c_int, _i32, _i32, _i32, _i32, _i32,
@@ -258,6 +265,29 @@ def cmf(tree, sop, psi, dt, n_steps, n_sub=1, phase=1.0, eps=1e-10, backend=LOOP
     if rc != 0:
         raise RuntimeError(f"oracle cmf failed: {rc}")
     return y
+
+
+def scf(tree, sop, psi, n_iter=1, n_krylov=5, n_itp=0, beta=1.0, breakdown=None, backend=LOOPS,
+        fast=False):
+    """The SCF sweep in compiled code (orc_scf, the twin of oracle/scf.py):
+    returns (lowest Ritz value of every Krylov solve, final flat psi)."""
+    order, dims, parent, child_idx, leaf_mode = tree.descriptor()
+    kind, odim, ooff, odata = sop.ops.descriptor()
+    coeff, ptr, modes, opids = sop.descriptor()
+    y = np.array(psi, dtype=np.complex128, copy=True)
+    odata = np.ascontiguousarray(odata)
+    coeff = np.ascontiguousarray(coeff)
+    cap = n_iter * (2 * tree.n_nodes - 1)
+    E = np.zeros(max(cap, 1))
+    cnt = ctypes.c_int64(0)
+    rc = lib(fast).orc_scf(backend, tree.n_nodes, order, dims, parent, child_idx, leaf_mode,
+                           len(kind), kind, odim, ooff, odata.ctypes.data, len(sop),
+                           coeff.ctypes.data, ptr, modes, opids, y.ctypes.data, n_iter, n_krylov, n_itp,
+                           beta, -1.0 if breakdown is None else breakdown, E.ctypes.data, cap,
+                           ctypes.byref(cnt))
+    if rc != 0:
+        raise RuntimeError(f"oracle scf failed: {rc}")
+    return E[:cnt.value].copy(), y
 
 
 class Frozen:

@@ -23,6 +23,7 @@
 #include <complex>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <set>
 #include <vector>
@@ -847,6 +848,367 @@ void orc_frozen_free(void* h) {
   Frozen* f = (Frozen*)h;
   delete f->sw;
   delete f;
+}
+
+// ---------------------------------------------------------------------------
+// SCF / Krylov sweep (src/Applications/SCF.cpp:14-341) with the tail-free
+// HamiltonianRepresentation and its corrections
+// (src/TreeClasses/HamiltonianRepresentation.cpp:117-203), the compiled twin
+// of oracle/scf.py (same routines, same order; the products through
+// mode_product / hole_product, zgemm when a BLAS is attached).
+// ---------------------------------------------------------------------------
+struct ScfRep {
+  const Tree& t;
+  const Ops& ops;
+  const Sop& s;
+  Backend be;
+  int L;
+  std::vector<std::vector<char>> stree;        // [term][node], tail-free sparse tree
+  std::vector<std::vector<int>> nact;          // [node][term]
+  std::vector<std::vector<std::vector<cd>>> hmat, hcon;  // [term][node] d x d
+  std::vector<std::vector<cd>> hcorr, hconcorr;          // [node] d x d
+
+  ScfRep(const Tree& t_, const Ops& o_, const Sop& s_, Backend be_) : t(t_), ops(o_), s(s_), be(be_) {
+    L = s.n_terms;
+    stree.assign(L, std::vector<char>(t.n, 0));
+    for (int l = 0; l < L; ++l) {
+      // SparseTree without tail (src/TreeClasses/SparseTree.cpp:34-84)
+      std::vector<char> path(t.n, 0);
+      for (int f = s.ptr[l]; f < s.ptr[l + 1]; ++f)
+        for (int a = t.leaf_node.at(s.mode[f]); a >= 0; a = t.parent[a]) path[a] = 1;
+      std::vector<int> order;
+      for (int a = 0; a < t.n; ++a)
+        if (path[a]) order.push_back(a);
+      int m = (int)order.size() - 1;
+      while (m > 0) {
+        int k = 0;
+        for (int c : t.children[order[m]]) k += path[c];
+        if (k > 1) break;
+        --m;
+      }
+      ++m;
+      for (int q = 0; q < m; ++q) stree[l][order[q]] = 1;
+    }
+    nact.assign(t.n, std::vector<int>(L, 0));
+    for (int a = 0; a < t.n; ++a)
+      for (int l = 0; l < L; ++l) {
+        if (t.bottom(a)) {
+          int hit = 0;
+          for (int f = s.ptr[l]; f < s.ptr[l + 1]; ++f) hit |= (s.mode[f] == t.leaf_mode[a]);
+          nact[a][l] = hit;
+          continue;
+        }
+        int k = 0;
+        for (int c : t.children[a]) k += stree[l][c];
+        nact[a][l] = t.top(a) ? k : k + stree[l][a];
+      }
+    hmat.assign(L, std::vector<std::vector<cd>>(t.n));
+    hcon.assign(L, std::vector<std::vector<cd>>(t.n));
+    for (int l = 0; l < L; ++l)
+      for (int a = 0; a < t.n; ++a)
+        if (stree[l][a]) {
+          hmat[l][a].assign((size_t)t.dup(a) * t.dup(a), cd(0));
+          hcon[l][a].assign((size_t)t.dup(a) * t.dup(a), cd(0));
+        }
+    hcorr.assign(t.n, {});
+    hconcorr.assign(t.n, {});
+    for (int a = 0; a < t.n; ++a) {
+      hcorr[a].assign((size_t)t.dup(a) * t.dup(a), cd(0));
+      hconcorr[a].assign((size_t)t.dup(a) * t.dup(a), cd(0));
+    }
+  }
+
+  // C = h x_k B on node a's geometry
+  void mp(std::vector<cd>& C, const std::vector<cd>& h, const std::vector<cd>& B, int a, int k) const {
+    C.resize(B.size());
+    const int64_t d = t.shape[a][k];
+    mode_product(be, C.data(), h.data(), B.data(), t.before(a, k), d, d, t.after(a, k), true);
+  }
+  // S = contraction of A and B over every index but k
+  void hole(std::vector<cd>& S, const std::vector<cd>& A, const std::vector<cd>& B, int a, int k) const {
+    const int64_t d = t.shape[a][k];
+    S.assign((size_t)d * d, cd(0));
+    hole_product(be, S.data(), A.data(), B.data(), t.before(a, k), d, d, t.after(a, k));
+  }
+  std::vector<cd> leaf_apply(int l, const std::vector<cd>& x, int a) const {
+    std::vector<cd> buf(x), tmp(x.size());
+    apply_mlo(be, ops, s, l, t.leaf_mode[a], buf.data(), tmp.data(), t.shape[a][0], t.dup(a));
+    return buf;
+  }
+  std::vector<cd> apply_children(int l, const std::vector<cd>& x, int a, int skip) const {
+    std::vector<cd> y(x), z;
+    for (size_t k = 0; k < t.children[a].size(); ++k) {
+      const int c = t.children[a][k];
+      if ((int)k == skip || !stree[l][c]) continue;
+      mp(z, hmat[l][c], y, a, (int)k);
+      y.swap(z);
+    }
+    return y;
+  }
+  static void axpy(std::vector<cd>& y, cd a, const std::vector<cd>& x) {
+    for (size_t i = 0; i < y.size(); ++i) y[i] += a * x[i];
+  }
+
+  void build_up(const std::vector<std::vector<cd>>& psi, int a) {
+    const std::vector<cd>& phi = psi[a];
+    const int last = t.last(a);
+    for (int l = 0; l < L; ++l) {
+      if (!stree[l][a]) continue;
+      hole(hmat[l][a], phi, t.bottom(a) ? leaf_apply(l, phi, a) : apply_children(l, phi, a, -1), a, last);
+    }
+    // buildUpCorrection
+    const int d = t.dup(a);
+    std::vector<cd> corr((size_t)d * d, cd(0)), z;
+    if (!t.bottom(a)) {
+      std::vector<cd> hA(phi.size(), cd(0));
+      for (size_t k = 0; k < t.children[a].size(); ++k) {
+        mp(z, hcorr[t.children[a][k]], phi, a, (int)k);
+        axpy(hA, cd(1), z);
+      }
+      hole(corr, phi, hA, a, last);
+    }
+    if (!t.top(a)) {
+      const int p = t.parent[a];
+      for (int l = 0; l < L; ++l)
+        if (nact[p][l] == 1 && stree[l][a]) axpy(corr, s.coeff[l], hmat[l][a]);
+    }
+    hcorr[a] = corr;
+  }
+
+  void build_down(const std::vector<std::vector<cd>>& psi, int a) {
+    if (t.top(a)) return;
+    const int p = t.parent[a];
+    const std::vector<cd>& phi = psi[p];
+    const int plast = t.last(p), ci = t.child_idx[a];
+    std::vector<cd> z;
+    for (int l = 0; l < L; ++l) {
+      if (!stree[l][a]) continue;
+      std::vector<cd> x = apply_children(l, phi, p, ci);
+      if (!t.top(p) && stree[l][p]) {
+        mp(z, hcon[l][p], x, p, plast);
+        x.swap(z);
+      }
+      hole(hcon[l][a], phi, x, p, ci);
+    }
+    // buildDownCorrection(hole = a)
+    std::vector<cd> hA(phi.size(), cd(0));
+    for (int l = 0; l < L; ++l) {
+      if (nact[p][l] < 2 || stree[l][a]) continue;
+      std::vector<cd> x = apply_children(l, phi, p, ci);
+      if (!t.top(p) && stree[l][p]) {
+        mp(z, hcon[l][p], x, p, plast);
+        x.swap(z);
+      }
+      axpy(hA, s.coeff[l], x);
+    }
+    for (size_t k = 0; k < t.children[p].size(); ++k) {
+      if ((int)k == ci) continue;
+      mp(z, hcorr[t.children[p][k]], phi, p, (int)k);
+      axpy(hA, cd(1), z);
+    }
+    if (!t.top(p)) {
+      mp(z, hconcorr[p], phi, p, plast);
+      axpy(hA, cd(1), z);
+    }
+    hole(hconcorr[a], phi, hA, p, ci);
+  }
+
+  // effective Hamiltonian at node a (SCF.cpp:36-84)
+  std::vector<cd> apply(const std::vector<cd>& A, int a) const {
+    const int last = t.last(a);
+    std::vector<cd> HA(A.size(), cd(0)), z;
+    for (int l = 0; l < L; ++l) {
+      if (t.bottom(a)) {
+        if (stree[l][a]) {
+          mp(z, hcon[l][a], leaf_apply(l, A, a), a, last);
+          axpy(HA, s.coeff[l], z);
+        }
+      } else if (nact[a][l] > 1) {
+        std::vector<cd> x = apply_children(l, A, a, -1);
+        if (!t.top(a) && stree[l][a]) {
+          mp(z, hcon[l][a], x, a, last);
+          x.swap(z);
+        }
+        axpy(HA, s.coeff[l], x);
+      }
+    }
+    if (!t.bottom(a))
+      for (size_t k = 0; k < t.children[a].size(); ++k) {
+        mp(z, hcorr[t.children[a][k]], A, a, (int)k);
+        axpy(HA, cd(1), z);
+      }
+    if (!t.top(a)) {
+      mp(z, hconcorr[a], A, a, last);
+      axpy(HA, cd(1), z);
+    }
+    return HA;
+  }
+};
+
+static cd vdot(const std::vector<cd>& a, const std::vector<cd>& b) {
+  cd acc = 0;
+  for (size_t i = 0; i < a.size(); ++i) acc += std::conj(a[i]) * b[i];
+  return acc;
+}
+
+// thin Householder QR of node a's tensor with index `mode` as the column
+// index (toMatrix / qr / toTensor, include/Core/Tensor_Implementation.h:863-869)
+static std::vector<cd> qr_mode(const Tree& t, int a, const std::vector<cd>& x, int mode) {
+  const int64_t before = t.before(a, mode), C = t.shape[a][mode], after = t.after(a, mode);
+  const int64_t R = before * after;
+  std::vector<cd> M((size_t)(R * C));
+  for (int64_t aft = 0; aft < after; ++aft)
+    for (int64_t c = 0; c < C; ++c)
+      for (int64_t b = 0; b < before; ++b) M[(b + before * aft) + R * c] = x[b + before * (c + C * aft)];
+  // Householder: M = H_0 .. H_{C-1} [R; 0]
+  std::vector<std::vector<cd>> V(C);
+  std::vector<cd> tau(C, cd(0));
+  for (int64_t j = 0; j < C; ++j) {
+    double nrm2 = 0;
+    for (int64_t i = j; i < R; ++i) nrm2 += std::norm(M[i + R * j]);
+    const double nrm = std::sqrt(nrm2);
+    const cd x0 = M[j + R * j];
+    const double ax0 = std::abs(x0);
+    const cd ph = ax0 > 0 ? x0 / ax0 : cd(1);
+    const cd alpha = -ph * nrm;
+    std::vector<cd> v(R - j);
+    for (int64_t i = j; i < R; ++i) v[i - j] = M[i + R * j];
+    v[0] -= alpha;
+    double vn = 0;
+    for (auto& e : v) vn += std::norm(e);
+    if (vn > 0) {
+      tau[j] = 2.0 / vn;
+      for (int64_t k = j; k < C; ++k) {
+        cd w = 0;
+        for (int64_t i = j; i < R; ++i) w += std::conj(v[i - j]) * M[i + R * k];
+        w *= tau[j];
+        for (int64_t i = j; i < R; ++i) M[i + R * k] -= v[i - j] * w;
+      }
+    }
+    V[j] = v;
+  }
+  // Q = H_0 .. H_{C-1} [I; 0]
+  std::vector<cd> Q((size_t)(R * C), cd(0));
+  for (int64_t j = 0; j < C; ++j) Q[j + R * j] = 1.0;
+  for (int64_t j = C - 1; j >= 0; --j) {
+    if (tau[j] == cd(0)) continue;
+    for (int64_t k = 0; k < C; ++k) {
+      cd w = 0;
+      for (int64_t i = j; i < R; ++i) w += std::conj(V[j][i - j]) * Q[i + R * k];
+      w *= tau[j];
+      for (int64_t i = j; i < R; ++i) Q[i + R * k] -= V[j][i - j] * w;
+    }
+  }
+  std::vector<cd> out(x.size());
+  for (int64_t aft = 0; aft < after; ++aft)
+    for (int64_t c = 0; c < C; ++c)
+      for (int64_t b = 0; b < before; ++b) out[b + before * (c + C * aft)] = Q[(b + before * aft) + R * c];
+  return out;
+}
+
+int orc_scf(int backend, int n_nodes, const int* order, const int* dims, const int* parent,
+            const int* child_idx, const int* leaf_mode, int n_ops, const int* op_kind, const int* op_dim,
+            const int64_t* op_off, const double* op_data, int n_terms, const double* coeff,
+            const int* term_ptr, const int* term_mode, const int* term_op, double* psi_io, int n_iter,
+            int n_krylov, int n_itp, double beta, double breakdown, double* energies, int64_t cap,
+            int64_t* count) {
+  (void)n_ops;
+  Tree t = make_tree(n_nodes, order, dims, parent, child_idx, leaf_mode);
+  Ops ops{op_kind, op_dim, op_off, (const cd*)op_data};
+  Sop s{n_terms, (const cd*)coeff, term_ptr, term_mode, term_op};
+  cd* flat = (cd*)psi_io;
+  std::vector<std::vector<cd>> psi(t.n);
+  for (int a = 0; a < t.n; ++a) psi[a].assign(flat + t.off[a], flat + t.off[a] + t.size[a]);
+  ScfRep rep(t, ops, s, (Backend)backend);
+  for (int a = 0; a < t.n; ++a)
+    if (!t.top(a)) rep.build_up(psi, a);
+  // sweep order: depth first from the top, back to a node after each child
+  std::vector<int> ord;
+  std::function<void(int)> add = [&](int a) {
+    ord.push_back(a);
+    for (int c : t.children[a]) {
+      add(c);
+      ord.push_back(a);
+    }
+  };
+  add(t.n - 1);
+  auto adjacent = [&](int frm, int to) -> int {
+    if (to < 0) return t.last(frm);
+    for (size_t k = 0; k < t.children[frm].size(); ++k)
+      if (t.children[frm][k] == to) return (int)k;
+    return t.last(frm);
+  };
+  int64_t ne = 0;
+  for (int it = 0; it < n_iter; ++it) {
+    for (size_t i = 0; i < ord.size(); ++i) {
+      const int a = ord[i];
+      int size = (int)std::min<int64_t>(n_krylov, t.size[a]);
+      // solveKrylovSpace (SCF.cpp:138-195)
+      std::vector<std::vector<cd>> space;
+      std::vector<double> al, be;
+      std::vector<cd> x = psi[a];
+      {
+        const double nx = std::sqrt(vdot(x, x).real());
+        for (auto& e : x) e /= nx;
+      }
+      space.push_back(x);
+      std::vector<cd> hx = rep.apply(x, a);
+      al.push_back(vdot(x, hx).real());
+      for (size_t q = 0; q < x.size(); ++q) x[q] = hx[q] - al.back() * x[q];
+      for (int l = 1; l < size; ++l) {
+        const double nrm = std::sqrt(vdot(x, x).real());
+        if (breakdown >= 0) {
+          double sc = 0;
+          for (double v : al) sc = std::max(sc, std::fabs(v));
+          for (double v : be) sc = std::max(sc, v);
+          if (nrm <= breakdown * sc) break;
+        }
+        be.push_back(nrm);
+        for (auto& e : x) e /= nrm;
+        space.push_back(x);
+        hx = rep.apply(x, a);
+        al.push_back(vdot(x, hx).real());
+        for (size_t q = 0; q < x.size(); ++q) x[q] = hx[q] - al.back() * space[l][q] - be.back() * space[l - 1][q];
+      }
+      size = (int)al.size();
+      std::vector<cd> T((size_t)size * size, cd(0)), U((size_t)size * size);
+      std::vector<double> E(size);
+      for (int l = 0; l < size; ++l) T[l + size * l] = al[l];
+      for (int l = 0; l + 1 < size; ++l) T[(l + 1) + size * l] = T[l + size * (l + 1)] = be[l];
+      herm_eig(size, T.data(), U.data(), E.data());
+      if (energies && ne < cap) energies[ne] = E[0];
+      ++ne;
+      std::vector<cd> w(t.size[a], cd(0));
+      if (it < n_itp) {
+        // imaginaryTimePropagation: the k = 0 term enters twice (SCF.cpp:208-214)
+        for (int l = 0; l < size; ++l) {
+          cd c = U[l] * std::conj(U[0]);
+          for (int k = 0; k < size; ++k) c += U[l + size * k] * std::exp(-beta * (E[k] - E[0])) * std::conj(U[size * k]);
+          ScfRep::axpy(w, c, space[l]);
+        }
+        const double nw = std::sqrt(vdot(w, w).real());
+        for (auto& e : w) e /= nw;
+      } else {
+        for (int l = 0; l < size; ++l) ScfRep::axpy(w, U[l], space[l]);
+      }
+      const int nxt = i + 1 < ord.size() ? ord[i + 1] : -1;
+      const int out_idx = adjacent(a, nxt);
+      psi[a] = qr_mode(t, a, w, out_idx);
+      if (nxt < 0) break;
+      std::vector<cd> r, z;
+      rep.hole(r, psi[a], w, a, out_idx);
+      const int in_idx = adjacent(nxt, a);
+      rep.mp(z, r, psi[nxt], nxt, in_idx);
+      psi[nxt] = z;
+      if (!t.top(a) && t.parent[a] == nxt)
+        rep.build_up(psi, a);
+      else
+        rep.build_down(psi, nxt);
+    }
+  }
+  for (int a = 0; a < t.n; ++a) std::copy(psi[a].begin(), psi[a].end(), flat + t.off[a]);
+  if (count) *count = ne;
+  return 0;
 }
 
 }  // extern "C"

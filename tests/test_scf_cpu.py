@@ -121,3 +121,18 @@ def test_plan_scf_double_float_segments():
     pv = PlanView(tree, sop, QT_PLAN_COMPRESSED | QT_PLAN_SCF, prec=1)
     E1, _ = scf_emulated(pv, tree, psi.flat(), n_iter=1, n_krylov=6)
     assert np.abs(E0 - E1).max() <= 1e-12 * np.abs(E0).max()
+
+
+@pytest.mark.parametrize("cfg,kw", [(0, dict(n_iter=2, n_krylov=6, n_itp=1, beta=200.0)),
+                                    (0, dict(n_iter=1, n_krylov=4, breakdown=1e-12))])
+def test_compiled_scf_equals_the_numpy_restatement(cfg, kw):
+    # orc_scf (the compiled twin, used as the bench's CPU baseline) against
+    # oracle/scf.py: the same Ritz value for every Krylov solve
+    import oracle as O
+    tree, sop, psi = config_problem(cfg)
+    E0, _ = S.scf(tree, sop, psi.tensors, **kw)
+    E1, fin = O.scf(tree, sop, psi.flat(), **kw)
+    assert len(E1) == len(E0)
+    assert np.abs(E1 - E0).max() <= 1e-12 * max(1.0, np.abs(E0).max())
+    # the final state's energy equals the last Ritz value (the last solve is at the top)
+    assert abs(O.derivative(tree, sop, fin).energy - E1[-1]) <= 1e-11 * max(1.0, abs(E1[-1]))
