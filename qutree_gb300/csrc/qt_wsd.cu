@@ -185,6 +185,10 @@ __device__ __forceinline__ bool lt_pos(double x, double c) {
 __device__ __forceinline__ double half_pow2(double a) { return __longlong_as_double((long long)(bits_of(a) - (1ull << 52))); }
 __device__ __forceinline__ double twice_pow2(double a) { return __longlong_as_double((long long)(bits_of(a) + (1ull << 52))); }
 
+// p / dp as a call, so that the rare fallback of the Newton step is a branch
+// and not an always-executed division
+__device__ __noinline__ double exact_quotient(double p, double dp) { return p / dp; }
+
 // Levels of the 3x3 eigenproblem.  Slots at entry: 0 h00, 1 h01, 2 h11,
 // 3 h02, 4 h12, 5 h22 (= 0).
 constexpr int kEigLevels = 11;
@@ -301,7 +305,7 @@ __device__ void eig3_top(const uint32_t* lut, double p0, double p2, double p3, d
     if (!is_negative(dp)) break;
     double step = f64_of(f32_trunc(p) / f32_trunc(dp));
     if (!(((unsigned long long)__double_as_longlong(step) & 0x7fffffffffffffffull) <= 0x4030000000000000ull))
-      step = p / dp;  // |step| > 16 or NaN: the binary32 quotient left its range
+      step = exact_quotient(p, dp);  // |step| > 16 or NaN: the binary32 quotient left its range
     const double nxt = lam - step;
     if (!(nxt < lam)) break;
     lam = nxt;
