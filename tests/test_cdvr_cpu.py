@@ -248,3 +248,39 @@ def test_cdvr_plan_rejections():
     bad = {m: basis.x[:4] for m in range(4)}
     with pytest.raises(ValueError, match="leaf dimension"):
         PlanView(tree, sop, flavour=0, cdvr=(bad, V, False))
+
+
+def test_wsd_eigensolve_matches_a_dense_eigensolver():
+    # the optimiser's 3x3 eigenproblem (rfoBuildHessian's H: h22 = 0) as the
+    # restatement solves it -- power-of-two scaling, binary32 Newton start,
+    # binary64 Newton with binary32 step quotients -- against numpy's eigh:
+    # the top eigenvector's ratios v0/v2, v1/v2 and v0^2 + v1^2 over twelve
+    # decades of scale (top eigenvalue separated, v2 not small)
+    import ctypes
+    lib = ctypes.CDLL(C.build_wsd())
+    f = lib.orc_eig3_top
+    dp = ctypes.POINTER(ctypes.c_double)
+    f.argtypes = [ctypes.c_void_p, dp, dp, dp]
+    rng = np.random.default_rng(0)
+    worst, checked = 0.0, 0
+    for _ in range(3000):
+        sc = 10.0 ** rng.uniform(-12, 6)
+        a = 10.0 ** rng.uniform(-6, 0)
+        pre = rng.normal(size=3) * sc
+        g = rng.normal(size=2) * np.sqrt(sc)
+        H = np.zeros((3, 3))
+        H[0, 0], H[1, 1] = pre[0] * a * a, pre[2] * a * a
+        H[0, 1] = H[1, 0] = pre[1] * a * a
+        H[0, 2] = H[2, 0] = g[0] * a
+        H[1, 2] = H[2, 1] = g[1] * a
+        Hc = np.ascontiguousarray(H.T.reshape(-1))
+        u0, u1, t2 = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        f(Hc.ctypes.data, ctypes.byref(u0), ctypes.byref(u1), ctypes.byref(t2))
+        w, V = np.linalg.eigh(H)
+        v = V[:, -1]
+        if abs(v[2]) < 1e-3 * np.abs(v).max() or abs(w[-1] - w[-2]) < 1e-6 * np.abs(w).max():
+            continue
+        checked += 1
+        worst = max(worst, abs(u0.value - v[0] / v[2]) / (1 + abs(v[0] / v[2])),
+                    abs(u1.value - v[1] / v[2]) / (1 + abs(v[1] / v[2])), abs(t2.value - (v[0] ** 2 + v[1] ** 2)))
+    assert checked > 2000 and worst < 1e-11
