@@ -578,7 +578,6 @@ __device__ void angles(const Prob& P, double xo0, double xo1, double2& c_out, do
 __device__ void rotations(const Prob& P) {
   const int d = P.d, n = P.n, H = P.H, tid = threadIdx.x;
   const bool master = tid < 32;
-  const int64_t dd = (int64_t)d * d;
   for (int i = 0; i < d - 1; ++i)
     for (int j = i + 1; j < d; ++j) {
       // the (i, j) blocks of every matrix and of w; the squared current
@@ -659,7 +658,6 @@ __device__ void rotations(const Prob& P) {
       }
       bsync();
     }
-  (void)dd;
 }
 
 // measureWeightedOffDiagonality: sum_k Re tr(W (D_k - T^H X_k T)^2), the
