@@ -164,7 +164,8 @@ def _rho_weighted_err(tree, dpsi, ref, rho):
 
 # DRAM bytes per sweep of the sum-of-products kernels (dram__bytes_read.sum +
 # dram__bytes_write.sum over all launches of one sweep of the 64-mode
-# workload, one ncu capture; profiles/launches_sweep_64mode_compressed_df64_tc.md)
+# workload, from one ncu capture of that sweep; the summary is committed
+# beside the other profiles and named in TRAFFIC_SOURCE)
 TRAFFIC = {0: 1531.5e6, 1: 3245.5e6, 2: 2104.8e6}
 TRAFFIC_SOURCE = ("ncu capture of one sweep of the 64-mode workload, k_tcs launches only "
                   "(profiles/launches_sweep_64mode_compressed_df64_tc.md)")

@@ -1,4 +1,4 @@
-// gpu_sweep_shim.cpp -- the QuTree-side binding of INTEGRATION.md section 3,
+// gpu_sweep_shim.cpp -- the QuTree-side binding of the integration guide,
 // compiled by g++ against include/qtgpu.h and linked against libqtgpu.so,
 // around minimal stand-ins for QuTree's types (qutree_standins.h).  The
 // class between the shim markers is the documented one, character for

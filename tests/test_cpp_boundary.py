@@ -1,5 +1,5 @@
-"""The C ABI from C++: the QuTree-side GpuSweep shim documented in
-INTEGRATION.md, compiled with g++ against include/qtgpu.h and linked against
+"""The C ABI from C++: the QuTree-side GpuSweep shim of the integration
+guide, compiled with g++ against include/qtgpu.h and linked against
 libqtgpu.so, around minimal stand-ins for QuTree's Tree / Tensorcd /
 Hamiltonian types (tests/cpp/).  The shim replaces QuTree's Derivative()
 (src/TreeClasses/HamiltonianRepresentation.cpp:74-81).
